@@ -1,0 +1,394 @@
+"""Seeded synthetic black-oil Newton systems (input generator for benchmarks and size-independent tests).
+
+The reference produces its Jacobians with its full black-oil simulator (engine/src/simulator.cpp:2500-3033),
+which is not part of this solver. For the large configurations (60x220x85 SPE10-model-2-sized grid, the
+64-realisation 40x40x10 ensemble, the serving stream) this module builds Jacobians of the same structure
+directly, in the style of the reference's own synthetic test matrices (``testMatrix``,
+app/src/gpu_compute.cpp:720-750; ``makeBlockLaplace``, tests/run_tests.cpp:3694-3724) but with the physics
+shape of the assembled system:
+
+* cells on a Cartesian grid (natural ordering, i fastest), optional ACTNUM mask, active cells renumbered in
+  natural order; 7-point TPFA connections with harmonic-mean transmissibilities;
+* unknowns per cell (p, Sw, Sg), equations (water, oil, gas) in surface volumes, rows scaled by dt / PV as the
+  reference scales them (engine/src/simulator.cpp:3303-3310), upstream-weighted Corey mobilities with their
+  saturation derivatives, accumulation derivatives (the true-IMPES ``acc`` blocks);
+* log-normal correlated permeability (Gaussian moving-average filter per layer, as ``generateRock``,
+  engine/src/tools.cpp:195-245), optional seeded binary channels, porosity phi = 0.05 + 0.02 ln k;
+* wells with one BHP unknown each (rate-controlled producers and water injectors); the well rows are
+  eliminated exactly (S = Acc - Acw Dww^-1 Awc, engine/src/bsr.cpp:733-840), which adds the fill blocks that
+  couple all perforated cells of a well;
+* a manufactured solution x_true and b = S x_true, so every solve can be checked against a known answer.
+
+Nothing here is on the timed path: it only produces inputs.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+from scipy.ndimage import gaussian_filter1d
+
+from .bsr import BSR, NewtonSystem, ScalarCSR
+
+NB = 3
+SWC, SOR, SGC = 0.2, 0.2, 0.05
+MU = (0.5, 1.5, 0.02)          # cp: water, oil, gas
+BF = (1.0 / 1.02, 1.0 / 1.25, 1.0 / 0.006)   # inverse formation volume factors (surface / reservoir)
+RS = 0.45                      # dissolved gas-oil ratio
+COMP = (3e-6, 1.2e-5, 4e-4)    # phase compressibilities (1/psi)
+CROCK = 4e-6
+
+
+def correlated_normal(shape, corr, rng):
+    """Unit-variance Gaussian field, independent per layer, filtered in y then x (corr in cells)."""
+    nz, ny, nx = shape
+    w = rng.standard_normal(shape)
+    f = w
+    if corr[1] > 0:
+        f = gaussian_filter1d(f, sigma=0.5 * corr[1], axis=1, mode="reflect")
+    if corr[0] > 0:
+        f = gaussian_filter1d(f, sigma=0.5 * corr[0], axis=2, mode="reflect")
+    if len(corr) > 2 and corr[2] > 1:
+        f = gaussian_filter1d(f, sigma=0.5 * corr[2], axis=0, mode="reflect")
+    s = f.reshape(nz, -1).std(axis=1)
+    s[s == 0] = 1.0
+    return f / s[:, None, None]
+
+
+def channel_mask(nx, ny, nz, layers, width, rng, n_channels=None):
+    """Seeded sinuous binary channels along y, ``width`` cells wide, in the given layers."""
+    m = np.zeros((nz, ny, nx), dtype=bool)
+    jj = np.arange(ny)[:, None]
+    ii = np.arange(nx)[None, :]
+    for k in layers:
+        nc = n_channels if n_channels is not None else max(1, nx // 20)
+        for _ in range(nc):
+            x0 = rng.uniform(0, nx)
+            amp = rng.uniform(2, max(3.0, nx / 6))
+            lam = rng.uniform(ny / 3, ny)
+            ph = rng.uniform(0, 2 * math.pi)
+            xc = x0 + amp * np.sin(2 * math.pi * jj / lam + ph)
+            m[k] |= np.abs(ii - xc) < 0.5 * width
+    return m
+
+
+def _corey(sw, sg):
+    """Mobilities (per phase) and their derivatives w.r.t. (Sw, Sg)."""
+    den = 1.0 - SWC - SOR
+    se = np.clip((sw - SWC) / den, 0.0, 1.0)
+    dse = np.where((sw > SWC) & (sw < 1 - SOR), 1.0 / den, 0.0)
+    krw = 0.6 * se**2
+    dkrw = 1.2 * se * dse
+    sgn = np.clip((sg - SGC) / (1.0 - SWC - SGC), 0.0, 1.0)
+    dsgn = np.where(sg > SGC, 1.0 / (1.0 - SWC - SGC), 0.0)
+    krg = 0.8 * sgn**2
+    dkrg = 1.6 * sgn * dsgn
+    so_n = np.clip((1.0 - sw - sg - SOR) / (1.0 - SWC - SOR), 0.0, 1.0)
+    dso = np.where((so_n > 0) & (so_n < 1), -1.0 / (1.0 - SWC - SOR), 0.0)
+    kro = so_n**2
+    dkro = 2.0 * so_n * dso   # same derivative w.r.t. Sw and Sg
+    lw, lo, lg = krw / MU[0], kro / MU[1], krg / MU[2]
+    # surface-volume mobilities of the three equations: water, oil, gas (free + dissolved)
+    lam = np.stack([BF[0] * lw, BF[1] * lo, BF[2] * lg + RS * BF[1] * lo], axis=-1)
+    dlam_sw = np.stack([BF[0] * dkrw / MU[0], BF[1] * dkro / MU[1], RS * BF[1] * dkro / MU[1]], axis=-1)
+    dlam_sg = np.stack([np.zeros_like(sw), BF[1] * dkro / MU[1], BF[2] * dkrg / MU[2] + RS * BF[1] * dkro / MU[1]], axis=-1)
+    lt = lw + lo + lg
+    dlt_sw = dkrw / MU[0] + dkro / MU[1]
+    dlt_sg = dkro / MU[1] + dkrg / MU[2]
+    return lam, dlam_sw, dlam_sg, lt, dlt_sw, dlt_sg
+
+
+def make_system(nx, ny, nz, *, sigma=1.0, corr=(5, 5, 1), seed=0, dx=100.0, dy=100.0, dz=20.0, kmean=100.0,
+                actnum_fraction=0.0, channels=None, wells="corners+center", n_wells=None, dt=1.0, porosity=None,
+                with_full=False, xtrue_seed=None) -> NewtonSystem:
+    """Build one Schur-reduced black-oil Newton system.
+
+    channels: None or (first_layer, last_layer, width, multiplier) (layers zero-based inclusive).
+    wells: "corners+center" (central water injector + 4 corner producers, all layers, as tools/gen_bigcase.py:44-52),
+           "diagonal" (injector at (0,0), producer at (nx-1,ny-1), all layers), or "random" (n_wells seeded columns).
+    """
+    rng = np.random.default_rng(seed)
+    shape = (nz, ny, nx)
+    z = correlated_normal(shape, corr, rng)
+    lnk = math.log(kmean) + sigma * z
+    if channels is not None:
+        k0, k1, width, mult = channels
+        cm = channel_mask(nx, ny, nz, range(k0, min(k1, nz - 1) + 1), width, rng)
+        lnk = np.where(cm, lnk + math.log(mult), lnk)
+    k = np.exp(lnk)
+    phi = np.clip(0.05 + 0.02 * lnk if porosity is None else np.full(shape, porosity), 0.01, 0.45)
+    active = np.ones(shape, dtype=bool)
+    if actnum_fraction > 0:
+        f = correlated_normal(shape, (6, 6, 2), rng)
+        thr = np.quantile(f, actnum_fraction)
+        active = f > thr
+    ncell = nx * ny * nz
+    act_flat = active.reshape(-1)
+    idx = np.full(ncell, -1, dtype=np.int64)
+    na = int(act_flat.sum())
+    idx[act_flat] = np.arange(na)
+    kf = k.reshape(-1)[act_flat]
+    phif = phi.reshape(-1)[act_flat]
+    kk_, jj_, ii_ = np.unravel_index(np.nonzero(act_flat)[0], shape)
+    depth = (kk_ + 0.5) * dz
+
+    # ---- state: pressure and saturation fields around the wells
+    ci, cj = (nx - 1) / 2.0, (ny - 1) / 2.0
+    well_cols = []
+    if wells == "corners+center":
+        well_cols = [("INJ", int(round(ci)), int(round(cj)), "inj")] + [
+            ("P%d" % (q + 1), i, j, "prod") for q, (i, j) in enumerate([(0, 0), (nx - 1, 0), (0, ny - 1), (nx - 1, ny - 1)])]
+    elif wells == "diagonal":
+        well_cols = [("INJ", 0, 0, "inj"), ("PROD", nx - 1, ny - 1, "prod")]
+    elif wells == "random":
+        nwr = n_wells if n_wells is not None else 2
+        for q in range(nwr):
+            well_cols.append(("W%d" % q, int(rng.integers(0, nx)), int(rng.integers(0, ny)), "inj" if q % 3 == 0 else "prod"))
+    L = 0.35 * math.hypot(nx * dx, ny * dy)
+    p = 4000.0 + 0.45 * depth
+    front = np.zeros(na)
+    for (_, wi, wj, kind) in well_cols:
+        r = np.hypot((ii_ - wi) * dx, (jj_ - wj) * dy) + 0.5 * dx
+        if kind == "inj":
+            p = p + 600.0 * np.exp(-r / L)
+            front = np.maximum(front, 1.0 / (1.0 + np.exp((r - 0.5 * L) / (0.1 * L))))
+        else:
+            p = p - 400.0 * np.exp(-r / L)
+    p = p + 5.0 * rng.standard_normal(na)
+    sw = SWC + (1 - SWC - SOR) * front * (0.8 + 0.2 * rng.random(na))
+    sw = np.clip(sw + 0.02 * rng.random(na), SWC, 1 - SOR - 1e-3)
+    sg = np.where(kk_ < max(1, nz // 4), 0.1 * rng.random(na) * (1.0 - front), 0.0)
+    sg = np.clip(sg, 0.0, 1.0 - sw - SOR - 1e-3)
+    lam, dlsw, dlsg, lt, dltsw, dltsg = _corey(sw, sg)
+
+    pv = phif * dx * dy * dz / 5.615        # reservoir barrels
+    scale = dt / pv                          # row scaling dt / PV
+
+    # ---- accumulation derivatives per unit pore volume (rows: water, oil, gas; cols: p, Sw, Sg)
+    so = 1.0 - sw - sg
+    acc = np.zeros((na, 3, 3))
+    acc[:, 0, 0] = BF[0] * sw * (CROCK + COMP[0])
+    acc[:, 0, 1] = BF[0]
+    acc[:, 1, 0] = BF[1] * so * (CROCK + COMP[1])
+    acc[:, 1, 1] = -BF[1]
+    acc[:, 1, 2] = -BF[1]
+    acc[:, 2, 0] = BF[2] * sg * (CROCK + COMP[2]) + RS * BF[1] * so * (CROCK + COMP[1]) + 1e-4 * BF[1] * so
+    acc[:, 2, 1] = -RS * BF[1]
+    acc[:, 2, 2] = BF[2] - RS * BF[1]
+
+    # ---- connections (i < j in active numbering): +x, +y, +z neighbours
+    conns = []
+    for (di, dj, dk, area, dist) in ((1, 0, 0, dy * dz, dx), (0, 1, 0, dx * dz, dy), (0, 0, 1, dx * dy, dz)):
+        m = np.ones(shape, dtype=bool)
+        if di:
+            m[:, :, -1] = False
+        if dj:
+            m[:, -1, :] = False
+        if dk:
+            m[-1, :, :] = False
+        src = np.nonzero(m.reshape(-1))[0]
+        dst = src + di + dj * nx + dk * nx * ny
+        a, b_ = idx[src], idx[dst]
+        ok = (a >= 0) & (b_ >= 0)
+        a, b_ = a[ok], b_[ok]
+        kz = 0.1 if dk else 1.0
+        kh = 2.0 / (1.0 / (kz * kf[a]) + 1.0 / (kz * kf[b_]))
+        T = 0.001127 * kh * area / dist
+        conns.append((a, b_, T))
+    ca = np.concatenate([c[0] for c in conns])
+    cb = np.concatenate([c[1] for c in conns])
+    cT = np.concatenate([c[2] for c in conns])
+    dpc = p[cb] - p[ca]                                   # flow from a to b when dpc < 0
+    up = np.where(dpc < 0, ca, cb)
+    lam_u = lam[up]                                        # (nc, 3)
+    dsw_u = dlsw[up]
+    dsg_u = dlsg[up]
+    up_is_a = up == ca
+
+    # flux into a from b: F = T lam_u (p_b - p_a); residual R_a -= F, R_b += F (rows scaled by dt/PV)
+    # d R_a / d x:   p_a: +T lam, p_b: -T lam, S_u: -T dp dlam
+    # d R_b / d x:   p_a: -T lam, p_b: +T lam, S_u: +T dp dlam
+    nconn = ca.size
+    blk_aa = np.zeros((nconn, 3, 3)); blk_ab = np.zeros((nconn, 3, 3))
+    blk_ba = np.zeros((nconn, 3, 3)); blk_bb = np.zeros((nconn, 3, 3))
+    Tl = cT[:, None] * lam_u
+    blk_aa[:, :, 0] += Tl; blk_ab[:, :, 0] -= Tl
+    blk_ba[:, :, 0] -= Tl; blk_bb[:, :, 0] += Tl
+    gs = -(cT * dpc)[:, None]
+    dS = np.stack([dsw_u, dsg_u], axis=-1) * gs[:, :, None]          # (nc, 3 eq, 2 sat)
+    ua = up_is_a[:, None, None]
+    blk_aa[:, :, 1:] += np.where(ua, dS, 0.0)
+    blk_ab[:, :, 1:] += np.where(ua, 0.0, dS)
+    blk_ba[:, :, 1:] -= np.where(ua, dS, 0.0)
+    blk_bb[:, :, 1:] -= np.where(ua, 0.0, dS)
+    sa = scale[ca][:, None, None]
+    sb = scale[cb][:, None, None]
+    diag = acc.copy()
+    np.add.at(diag, ca, sa * blk_aa)
+    np.add.at(diag, cb, sb * blk_bb)
+
+    # ---- wells: one BHP unknown each; perforations in every active layer of the column
+    wrow_cells, wcw, wwc, Dw, wnames = [], [], [], [], []
+    for (name, wi, wj, kind) in well_cols:
+        cells = idx[(np.arange(nz) * ny + wj) * nx + wi]
+        cells = cells[cells >= 0]
+        if cells.size == 0:
+            continue
+        WI = 2.0 * 0.001127 * kf[cells] * dz / math.log(0.2 * dx / 0.25)
+        pw = p[cells].mean() + (300.0 if kind == "inj" else -300.0)
+        if kind == "inj":
+            # water injection with total mobility; only the water equation gets the source
+            c_cw = np.zeros((cells.size, 3))
+            c_cw[:, 0] = -scale[cells] * WI * lt[cells] * BF[0]
+            dpp = np.zeros((cells.size, 3, 3))
+            dpp[:, 0, 0] = scale[cells] * WI * lt[cells] * BF[0]
+            wc = np.zeros((cells.size, 3))
+            wc[:, 0] = -WI * lt[cells]
+            wc[:, 1] = WI * (pw - p[cells]) * dltsw[cells]
+            wc[:, 2] = WI * (pw - p[cells]) * dltsg[cells]
+            D = float(np.sum(WI * lt[cells]))
+        else:
+            c_cw = -scale[cells][:, None] * WI[:, None] * lam[cells]
+            dpp = np.zeros((cells.size, 3, 3))
+            dpp[:, :, 0] = scale[cells][:, None] * WI[:, None] * lam[cells]
+            dd = (p[cells] - pw)
+            dpp[:, :, 1] = scale[cells][:, None] * (WI * dd)[:, None] * dlsw[cells]
+            dpp[:, :, 2] = scale[cells][:, None] * (WI * dd)[:, None] * dlsg[cells]
+            wc = np.zeros((cells.size, 3))
+            wc[:, 0] = WI * lt[cells]
+            wc[:, 1] = WI * dd * dltsw[cells]
+            wc[:, 2] = WI * dd * dltsg[cells]
+            D = -float(np.sum(WI * lt[cells]))
+        np.add.at(diag, cells, dpp)
+        wrow_cells.append(cells); wcw.append(c_cw); wwc.append(wc); Dw.append(D); wnames.append(name)
+    nw = len(Dw)
+
+    # ---- assemble the cell block matrix + Schur fill, merged and sorted per row
+    rows = [np.arange(na), ca, cb]
+    cols = [np.arange(na), cb, ca]
+    vals = [diag, sa * blk_ab, sb * blk_ba]
+    for w in range(nw):
+        cells = wrow_cells[w]
+        m = cells.size
+        ri = np.repeat(cells, m)
+        cj = np.tile(cells, m)
+        fill = -(wcw[w][:, None, :, None] * wwc[w][None, :, None, :]) / Dw[w]     # (m, m, 3 eq, 3 col)
+        rows.append(ri); cols.append(cj); vals.append(fill.reshape(m * m, 3, 3))
+    R = np.concatenate(rows).astype(np.int64)
+    Cc = np.concatenate(cols).astype(np.int64)
+    V = np.concatenate(vals, axis=0)
+    key = R * na + Cc
+    order = np.argsort(key, kind="stable")
+    key_s = key[order]
+    uniq, start = np.unique(key_s, return_index=True)
+    Vs = np.add.reduceat(V[order], start, axis=0)
+    ur = (uniq // na).astype(np.int32)
+    uc = (uniq % na).astype(np.int32)
+    rowPtr = np.zeros(na + 1, dtype=np.int32)
+    np.add.at(rowPtr, ur + 1, 1)
+    rowPtr = np.cumsum(rowPtr, dtype=np.int64).astype(np.int32)
+    A = BSR(na, NB, rowPtr, uc, Vs.reshape(-1))
+
+    # ---- manufactured solution and right-hand side b = S x_true
+    rng2 = np.random.default_rng(seed + 7919 if xtrue_seed is None else xtrue_seed)
+    xt = np.empty((na, 3))
+    xt[:, 0] = 20.0 * np.sin(0.05 * ii_ + 0.07 * jj_) * np.cos(0.3 * kk_) + rng2.standard_normal(na)
+    xt[:, 1] = 0.01 * rng2.standard_normal(na)
+    xt[:, 2] = 0.005 * rng2.standard_normal(na)
+    xt = xt.reshape(-1)
+    b = bsr_matvec_host(A, xt)
+
+    full = None
+    full_b = None
+    if with_full:
+        full, full_b = _full_jacobian(A, na, nw, diag, ca, cb, sa * blk_ab, sb * blk_ba, wrow_cells, wcw, wwc, Dw, xt, rng2)
+    meta = dict(nx=nx, ny=ny, nz=nz, sigma=sigma, seed=seed, wells=wnames, dt=dt, active=na)
+    return NewtonSystem(A, b, acc=acc.reshape(-1), full=full, full_b=full_b, na=na, nv=3, nw=nw, x_true=xt, meta=meta)
+
+
+def bsr_matvec_host(A: BSR, x: np.ndarray) -> np.ndarray:
+    """Host matvec used only to manufacture right-hand sides for generated inputs."""
+    blk = A.blocks()
+    xv = x.reshape(A.n, A.nb)
+    contrib = np.einsum("kij,kj->ki", blk, xv[A.col])
+    rows = np.repeat(np.arange(A.n), np.diff(A.rowPtr))
+    y = np.zeros((A.n, A.nb))
+    np.add.at(y, rows, contrib)
+    return y.reshape(-1)
+
+
+def _full_jacobian(A, na, nw, diag, ca, cb, bab, bba, wcells, wcw, wwc, Dw, xt, rng):
+    """Scalar CSR with well rows (cells first, then one BHP row per well), values before the Schur step, and its
+    right-hand side for a manufactured (cells, BHP) solution."""
+    nc = na * 3
+    ent_r, ent_c, ent_v = [], [], []
+
+    def add_blocks(bi, bj, blocks):
+        e = np.arange(3)
+        r = (bi[:, None, None] * 3 + e[None, :, None]).repeat(3, axis=2)
+        c = (bj[:, None, None] * 3 + e[None, None, :]).repeat(3, axis=1)
+        ent_r.append(r.reshape(-1)); ent_c.append(c.reshape(-1)); ent_v.append(blocks.reshape(-1))
+
+    add_blocks(np.arange(na), np.arange(na), diag)
+    add_blocks(ca, cb, bab)
+    add_blocks(cb, ca, bba)
+    for w in range(nw):
+        cells = wcells[w]
+        for e in range(3):
+            ent_r.append(cells * 3 + e); ent_c.append(np.full(cells.size, nc + w)); ent_v.append(wcw[w][:, e])
+        for e in range(3):
+            ent_r.append(np.full(cells.size, nc + w)); ent_c.append(cells * 3 + e); ent_v.append(wwc[w][:, e])
+        ent_r.append(np.array([nc + w])); ent_c.append(np.array([nc + w])); ent_v.append(np.array([Dw[w]]))
+    R = np.concatenate(ent_r).astype(np.int64)
+    Cc = np.concatenate(ent_c).astype(np.int64)
+    V = np.concatenate(ent_v)
+    ntot = nc + nw
+    key = R * ntot + Cc
+    order = np.argsort(key, kind="stable")
+    uniq, start = np.unique(key[order], return_index=True)
+    Vs = np.add.reduceat(V[order], start)
+    ur = (uniq // ntot).astype(np.int32)
+    uc = (uniq % ntot).astype(np.int32)
+    rp = np.zeros(ntot + 1, dtype=np.int64)
+    np.add.at(rp, ur + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    J = ScalarCSR(rp, uc, Vs)
+    xfull = np.concatenate([xt, 50.0 * rng.standard_normal(nw)])
+    rows = np.repeat(np.arange(ntot), np.diff(rp))
+    bf = np.zeros(ntot)
+    np.add.at(bf, rows, Vs * xfull[uc])
+    return J, bf
+
+
+# ---------------------------------------------------------------- named workloads
+def spe10_like(day: int = 1, seed: int = 0, nx=60, ny=220, nz=85) -> NewtonSystem:
+    """60x220x85 SPE10-model-2-sized grid: sigma ln k = 2.5, channels (x100, 4 cells wide) in layers 36-85,
+    phi = 0.05 + 0.02 ln k, central injector + 4 corner producers in all layers; ``day`` sets the time step
+    (1 or 100 days: the two Jacobian dates)."""
+    return make_system(nx, ny, nz, sigma=2.5, corr=(5, 5, 1), seed=seed, dx=20.0, dy=10.0, dz=2.0,
+                       channels=(35, 84, 4, 100.0), wells="corners+center", dt=float(day))
+
+
+def ensemble(n_real: int = 64, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0, dt: float = 10.0):
+    """Realisations with their own permeability seed and a seeded inactive fraction U[0.1, 0.5]."""
+    out = []
+    for r in range(n_real):
+        frac = float(np.random.default_rng(10_000 + seed0 + r).uniform(0.1, 0.5))
+        out.append(make_system(nx, ny, nz, sigma=sigma, seed=seed0 + r, actnum_fraction=frac, wells="corners+center",
+                               dt=dt))
+    return out
+
+
+def serving_request(rng: np.random.Generator, cells_lo=1e3, cells_hi=1e6, max_cells=None) -> NewtonSystem:
+    """One serving request: log-uniform cell count, random box with nz in [1, 50], sigma ln k in [0.5, 3],
+    time step in [0.1, 30] days, 1-8 wells."""
+    hi = cells_hi if max_cells is None else min(cells_hi, max_cells)
+    ncell = int(round(math.exp(rng.uniform(math.log(cells_lo), math.log(hi)))))
+    nz = int(rng.integers(1, 51))
+    nz = max(1, min(nz, ncell))
+    area = max(1, ncell // nz)
+    asp = math.exp(rng.uniform(-1.0, 1.0))
+    nx = max(1, int(round(math.sqrt(area * asp))))
+    ny = max(1, area // nx)
+    return make_system(nx, ny, nz, sigma=float(rng.uniform(0.5, 3.0)), seed=int(rng.integers(0, 2**31 - 1)),
+                       dt=float(rng.uniform(0.1, 30.0)), wells="random", n_wells=int(rng.integers(1, 9)))
