@@ -1,0 +1,348 @@
+"""Benchmark: solves/s of the batched mixed-precision GPU solve of the 64-realisation ensemble.
+
+Workload (one step): 64 Newton systems of a 40x40x10 black-oil waterflood (sigma ln k = 1.5, seeded inactive
+fraction U[0.1, 0.5] -> 8k-14.4k active cells each, BSR 3x3), generated by ressim_gb300.synth with seeds
+0..63 (+64 * rank under torchrun: weak scaling, each GPU its own ensemble). A step is the solve path of all
+64 systems at once: BILU0 factorisation of every system (lean FP32 factors) and a batched BiCGSTAB to true
+relative residual <= 1e-6 (FP64 outer vectors / inner products / true residual, FP32 preconditioner).
+
+Reported besides ``value`` (device-resident inputs, CUDA events on the solver stream):
+* ``e2e``: the same step through the C ABI with host buffers (matrix values and right-hand sides copied in,
+  solutions copied out, every step);
+* ``fp64_plain``: the plain FP64 GPU path, the 64 systems solved one after another (one handle each);
+* ``roofline`` of the dominant kernel and ``kernels`` (per-launch device time and algorithmic bytes);
+* ``cpu_baseline``: the C restatement (oracle/) of the reference FP64 BILU0-BiCGSTAB on the host cores,
+  on a bounded sample of the same systems.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_REAL, NX, NY, NZ, SIGMA = 64, 40, 40, 10, 1.5
+TOL, MAXIT = 1e-6, 500
+WORKLOAD = "ensemble64_40x40x10_bilu0_bicgstab"
+METRIC = "solves/s & p99 latency: batched mixed-prec vs plain FP64 GPU, true rel.res <=1e-6"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ensemble(rank):
+    from ressim_gb300 import synth
+    return synth.ensemble(n_real=N_REAL, nx=NX, ny=NY, nz=NZ, sigma=SIGMA, seed0=64 * rank)
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def spmv_bytes(nnzb, n):
+    return nnzb * (9 * 8 + 4) + (n + 1) * 4 + 2 * 3 * n * 8
+
+
+def ilu_bytes(nnzb, n, sv, sx):
+    return nnzb * (9 * sv + 4) + 2 * (n + 1) * 4 + 2 * 3 * n * sx
+
+
+def cpu_baseline(systems, budget_s=20.0):
+    """Oracle (C restatement of the reference FP64 BILU0 + BiCGSTAB) on the host cores, bounded sample."""
+    from oracle import Oracle
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    t0 = time.perf_counter()
+    done = 0
+    for s in systems:
+        x, conv, its, rr, ts, tv = o.solve(s.A, s.b, prec=0, method=0, tol=TOL, maxit=MAXIT)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{done} of the {len(systems)} ensemble systems, FP64 BILU0-BiCGSTAB to 1e-6 (C restatement, OpenMP SpMV/vector ops)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    systems = ensemble(0)
+    per_step = max(1, int(os.environ.get("RSG_REF_SYSTEMS_PER_STEP", "4")))
+    from oracle import Oracle
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    times = []
+    k = 0
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for _ in range(per_step):
+            s = systems[k % len(systems)]
+            k += 1
+            o.solve(s.A, s.b, prec=0, method=0, tol=TOL, maxit=MAXIT)
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    T = sum(times)
+    v = per_step * len(times) / T
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * T / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (ressim_gb300.synth, seeded)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "systems_per_step": per_step, "solver": "BILU0-BiCGSTAB FP64 (reference CPU algorithm)"},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{per_step} ensemble systems per step (C restatement of the reference CPU path)"},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="rsg")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+    torch.cuda.set_device(local)
+    from ressim_gb300.solver import DeviceSolver
+
+    systems = ensemble(rank)
+    mats = [s.A for s in systems]
+    b_host = np.concatenate([s.b for s in systems])
+    n_rows = sum(A.n for A in mats)
+    nnzb = sum(A.nnzb for A in mats)
+    N = 3 * n_rows
+    val_bytes = nnzb * 72
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- batched mixed-precision path, device-resident inputs
+    dev = DeviceSolver(precond="bilu0", krylov="bicgstab", precision="mixed", check_every=8, use_graphs=True, device=local)
+    dev.set_batch(mats)
+    stream = torch.cuda.ExternalStream(dev.stream)
+    d_b = torch.from_numpy(b_host).to(f"cuda:{local}")
+    d_x = torch.zeros_like(d_b)
+    torch.cuda.synchronize()
+
+    def step():
+        dev.setup()
+        return dev.solve_device(d_b.data_ptr(), d_x.data_ptr(), tol=TOL, maxit=MAXIT)
+
+    for _ in range(args.warmup):
+        step()
+    l0 = dev.stats().kernel_launches
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    results = []
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            res = step()
+            ev[k][1].record(stream)
+            results.append(res)
+        barrier()
+    launches = dev.stats().kernel_launches - l0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    its, rr, tr = dev.batch_results()
+    x_dev = d_x.cpu().numpy()
+    T = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([T], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        T = float(t.item())
+    value = world * N_REAL * args.steps / T
+    ok = all(r.converged for r in results) and float(np.max(tr)) <= TOL
+
+    # ---------------- per-kernel device time (events on the solver stream) for the roofline
+    d_y = torch.empty_like(d_b)
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        dev.spmv_device(d_x.data_ptr(), d_y.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_spmv = e0.elapsed_time(e1) / reps / 1e3
+    e0.record(stream)
+    for _ in range(reps):
+        dev.precond_apply_device(d_b.data_ptr(), d_y.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_prec = e0.elapsed_time(e1) / reps / 1e3      # forward + backward sweep
+    hbm, peak_kind = peaks()
+    B_spmv = spmv_bytes(nnzb, n_rows)
+    B_ilu = ilu_bytes(nnzb, n_rows, 4, 4)
+    mean_its = float(np.mean(its))
+    share_spmv = 2 * t_spmv * mean_its
+    share_prec = 2 * t_prec * mean_its
+    kernels = {
+        "bsr3_spmv_f64": {"ms": 1e3 * t_spmv, "bytes": B_spmv, "gbs": B_spmv / t_spmv / 1e9, "per_iteration": 2},
+        "bilu0_sweeps_f32": {"ms": 1e3 * t_prec, "bytes": B_ilu, "gbs": B_ilu / t_prec / 1e9, "per_iteration": 2},
+    }
+    dom = "bilu0_sweeps_f32" if share_prec >= share_spmv else "bsr3_spmv_f64"
+    ach = kernels[dom]["gbs"]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "peak_kind": peak_kind + " burst copy", "traffic": None}
+    roofline_spmv = {"bound": "hbm", "kernel": "bsr3_spmv_f64", "achieved": kernels["bsr3_spmv_f64"]["gbs"], "peak": hbm,
+                     "unit": "GB/s", "frac": kernels["bsr3_spmv_f64"]["gbs"] / hbm}
+
+    # ---------------- e2e through the C ABI with host buffers (values + rhs in, solutions out, every step)
+    x_host = np.zeros(N)
+    from ressim_gb300 import _lib
+    import ctypes as C
+    L = _lib.load()
+    e2e_t = []
+    for k in range(args.warmup + args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        dev.set_batch(mats)
+        dev.setup()
+        itc, rrc = C.c_int(0), C.c_double(0)
+        rc = L.rsg_solve(dev.h, _lib.ptr(b_host), _lib.ptr(x_host), TOL, MAXIT, C.byref(itc), C.byref(rrc))
+        _lib.check(rc)
+        barrier()
+        if k >= args.warmup:
+            e2e_t.append(time.perf_counter() - t0)
+    Te = sum(e2e_t)
+    if dist:
+        t = torch.tensor([Te], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        Te = float(t.item())
+    e2e = {"value": world * N_REAL * len(e2e_t) / Te, "unit": "solves/s", "h2d_bytes_per_step": val_bytes + N * 8,
+           "d2h_bytes_per_step": N * 8, "p50_ms": 1e3 * statistics.median(e2e_t)}
+    dev.close()
+
+    # ---------------- plain FP64 GPU path: one system after another (one handle each)
+    plain = []
+    for A in mats:
+        d = DeviceSolver(precond="bilu0", krylov="bicgstab", precision="fp64", check_every=8, use_graphs=True, device=local)
+        d.set_matrix(A)
+        plain.append(d)
+    bs = [torch.from_numpy(s.b).to(f"cuda:{local}") for s in systems]
+    xs = [torch.zeros_like(b) for b in bs]
+    for d, b, x in zip(plain, bs, xs):
+        d.setup()
+        d.solve_device(b.data_ptr(), x.data_ptr(), tol=TOL, maxit=MAXIT)
+    torch.cuda.synchronize()
+    lat = []
+    t0 = time.perf_counter()
+    plain_ok = True
+    for d, b, x in zip(plain, bs, xs):
+        s0 = time.perf_counter()
+        d.setup()
+        r = d.solve_device(b.data_ptr(), x.data_ptr(), tol=TOL, maxit=MAXIT)
+        plain_ok &= r.converged and r.trueRelResidual <= TOL
+        lat.append(time.perf_counter() - s0)
+    torch.cuda.synchronize()
+    Tp = time.perf_counter() - t0
+    for d in plain:
+        d.close()
+    fp64_plain = {"value": len(mats) / Tp, "unit": "solves/s", "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                  "p99_ms": 1e3 * float(np.percentile(lat, 99)), "all_converged": bool(plain_ok)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(systems)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (ressim_gb300.synth: seeded black-oil Jacobians of the named shapes)",
+            "config": {"workload": WORKLOAD, "systems": N_REAL, "grid": f"{NX}x{NY}x{NZ}", "sigma_lnk": SIGMA,
+                       "active_cells": [int(min(A.n for A in mats)), int(max(A.n for A in mats))], "block_rows": n_rows,
+                       "nnzb": nnzb, "precision": "mixed (FP32 BILU0 factors/sweeps, FP64 Krylov)", "tol": TOL,
+                       "l2": f"inputs larger than L2 (matrix values {val_bytes / 1e6:.0f} MB)", "parallelism": f"replicas{world}"},
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                           "note": "batched step: all 64 systems complete together"},
+            "iterations": {"mean": mean_its, "max": int(np.max(its))}, "max_true_relres": float(np.max(tr)), "all_converged": bool(ok),
+            "fp64_plain": fp64_plain, "batched_mixed_over_plain_fp64": value / world / fp64_plain["value"],
+            "e2e": e2e, "roofline": roofline, "roofline_spmv": roofline_spmv, "kernels": kernels, "gpu_launches": int(launches),
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

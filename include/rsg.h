@@ -1,0 +1,144 @@
+/* rsg -- GB300-native (sm_103a) Newton linear solver for ResSim Studio's black-oil engine: C ABI.
+ *
+ * Plain pointers and sizes only. Every call returns RSG_OK (0) or a negative status; rsg_last_error() gives the
+ * message of the last failure on the calling thread (the convention of engine/include/ressim/capi.h:5-7:
+ * int >= 0 success, -1-style errors, thread-local error text, caller-owned buffers).
+ *
+ * Each handle owns one CUDA stream and its device memory. A handle is used by one thread at a time;
+ * different handles may be used concurrently from different threads.
+ *
+ * Data layout (identical to ressim::BSR, engine/include/ressim/bsr.h:23-37): n block rows, nb unknowns per cell
+ * (nb = 3 for the black-oil system), rowPtr[n+1] / col[nnzb] int32 with sorted columns per row and a diagonal
+ * block in every row, val[nnzb*nb*nb] float64 row-major blocks (row = equation, column = unknown); vectors of
+ * n*nb float64 interleaved per cell.
+ */
+#ifndef RSG_H
+#define RSG_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSG_OK 0
+#define RSG_EINVAL -1       /* bad argument (sizes, pattern, missing diagonal block) */
+#define RSG_ECUDA -2        /* CUDA runtime failure (message has the CUDA error) */
+#define RSG_ENOMEM -3       /* device allocation failed or the memory budget is exhausted */
+#define RSG_ESTATE -4       /* call out of order (e.g. solve before setup) */
+#define RSG_ETIMEOUT -5     /* a bounded device-side wait ran out (the kernel returned instead of hanging) */
+#define RSG_EBREAKDOWN -6   /* Krylov breakdown (rho or <r0,v> vanished) before convergence */
+#define RSG_ENOTCONV 1      /* finished without reaching the tolerance (x holds the last iterate) */
+
+/* preconditioners */
+#define RSG_PREC_BILU0 0    /* block ILU(0), natural-order exact (ressim::BILU0, engine/include/ressim/bsr.h:50-94) */
+#define RSG_PREC_CPR 1      /* two-stage CPR: AMG on the pressure system + BILU0 (ressim::BlockCPR, bsr.h:224-250) */
+#define RSG_PREC_JACOBI 2   /* block Jacobi (diagonal-block inverses) */
+/* Krylov methods */
+#define RSG_KRYLOV_BICGSTAB 0 /* ressim::bicgstab, engine/include/ressim/linsolve.h:99-100 */
+#define RSG_KRYLOV_GMRES 1    /* ressim::gmres (flexible, restarted), linsolve.h:101-102 */
+/* precision */
+#define RSG_FP64 0          /* everything in FP64 */
+#define RSG_MIXED 1         /* FP32 factors / AMG / preconditioner SpMV with FP32 accumulation; FP64 outer Krylov
+                               vectors, inner products, true residual and 3x3 diagonal-block inversions */
+
+typedef struct rsg_options {
+    int precond;            /* RSG_PREC_* */
+    int krylov;             /* RSG_KRYLOV_* */
+    int restart;            /* GMRES restart length (reference default 40; 30 for the SPE10-sized system) */
+    int precision;          /* RSG_FP64 / RSG_MIXED */
+    int gmres_fallback;     /* 1: a BiCGSTAB solve that does not converge is retried with GMRES(restart), as the
+                               engine does (engine/src/simulator.cpp:3388-3398) */
+    int check_every;        /* iterations launched between host convergence checks (0 = default 4) */
+    int use_graphs;         /* 1: capture the iteration in a CUDA graph and replay it */
+    int device;             /* CUDA device ordinal */
+    size_t mem_budget;      /* bytes this handle may hold on the device (0 = no limit) */
+} rsg_options;
+
+typedef struct rsg_stats {
+    int iterations;         /* Krylov iterations of the last solve (max over the systems of a batch) */
+    int converged;          /* 1 when every system reached the tolerance */
+    double rel_residual;    /* recursive relative residual reported by the Krylov method (max over systems) */
+    double true_rel_residual; /* ||b - A x|| / ||b|| recomputed in FP64 after the solve (max over systems), or -1 */
+    double setup_ms;        /* device time of the last rsg_setup (factorisation, AMG refresh) */
+    double solve_ms;        /* device time of the last solve */
+    int regularised_blocks; /* singular pivot blocks shifted by the factorisation (ressim::BILU0::regularisedBlocks) */
+    int amg_levels;         /* CPR: levels of the pressure AMG hierarchy */
+    size_t device_bytes;    /* device memory held by the handle */
+    long long kernel_launches; /* kernels launched by this handle since creation (graph nodes included) */
+} rsg_stats;
+
+typedef struct rsg_solver rsg_solver;
+
+void rsg_default_options(rsg_options* o);
+const char* rsg_last_error(void);
+const char* rsg_version(void);
+
+/* Create / destroy a solver handle (one CUDA stream). */
+int rsg_create(rsg_solver** h, const rsg_options* opts);
+int rsg_destroy(rsg_solver* h);
+
+/* Upload (or refresh) one system matrix from host memory. The pattern-dependent plan (level schedule,
+ * elimination lists, AMG aggregates) is rebuilt only when the pattern changes; a values-only refresh
+ * reuses it (the engine's pattern reuse, engine/src/bsr.cpp:759-769 and AMG::refresh, amg.cpp:257-271).
+ * Replaces: the BSR the engine hands to GpuBlockSolver::solve (engine/include/ressim/bsr.h:147). */
+int rsg_set_matrix(rsg_solver* h, int n, int nb, const int* rowPtr, const int* col, const double* val);
+
+/* Upload a batch of independent systems (uneven sizes) that are solved together; system s has
+ * n[s] block rows. Arrays are host pointers, one per system. */
+int rsg_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
+                  const double* const* val);
+
+/* Preconditioner set-up on the device: BILU0 factorisation (and, for CPR, the pressure matrix, the AMG
+ * hierarchy and its refresh). acc: optional accumulation blocks (n*nb*nb per system, concatenated) for
+ * true-IMPES weights, or NULL for quasi-IMPES (Jacobian diagonal block).
+ * Replaces: BILU0::factor (engine/src/bsr.cpp:347-435), BlockCPR::setup (engine/src/bsr.cpp:993-1059). */
+int rsg_setup(rsg_solver* h, const double* acc);
+
+/* Solve A x = b from x0 = 0 with host vectors (copied in and out on the handle's stream, timed inside).
+ * For a batch, b and x are the concatenation of the systems' vectors.
+ * Returns RSG_OK when converged, RSG_ENOTCONV when the iteration limit was hit, or a negative error.
+ * Replaces: GpuBlockSolver::solve (engine/include/ressim/bsr.h:147) and bicgstab / gmres with the
+ * set-up preconditioner (engine/include/ressim/linsolve.h:99-102). */
+int rsg_solve(rsg_solver* h, const double* b, double* x, double tol, int maxIt, int* iterations, double* relres);
+
+/* Same with device-resident vectors (b, x: device pointers of n*nb float64 on the handle's device). */
+int rsg_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres);
+
+/* Per-system results of the last (batched) solve: its[nsys], relres[nsys] (host arrays, may be NULL). */
+int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relres);
+
+/* y = A x with host / device vectors. Replaces BSR::spmv (engine/src/bsr.cpp:109-126). */
+int rsg_spmv(rsg_solver* h, const double* x, double* y);
+int rsg_spmv_device(rsg_solver* h, const double* d_x, double* d_y);
+
+/* z = M^-1 r with the set-up preconditioner (host vectors). Replaces Preconditioner::apply for BILU0 /
+ * BlockCPR (engine/src/bsr.cpp:437-596, 1061-1084). */
+int rsg_precond_apply(rsg_solver* h, const double* r, double* z);
+
+/* Same with device vectors (no synchronisation: ordered on the handle's stream). */
+int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z);
+
+/* Copy the BILU0 factors (FP64 path: L strictly lower, U_ii^-1 on the diagonal, U upper, in the matrix's
+ * own pattern and block order -- the storage of ressim::BILU0, engine/src/bsr.cpp:183-215). */
+int rsg_get_factors(rsg_solver* h, double* lu);
+
+/* Statistics of the last setup / solve. */
+int rsg_get_stats(rsg_solver* h, rsg_stats* st);
+
+/* Handle's CUDA stream (cudaStream_t as void*), for callers that order their own work with it. */
+void* rsg_stream(rsg_solver* h);
+
+/* Well Schur complement on the host (pattern + values), the reduction the engine performs before calling
+ * the solver: A is the scalar CSR Jacobian with na*nv cell rows followed by nw well (BHP) rows.
+ * First call with sRowPtr == NULL to get the block count in *nnzb; then with arrays of that size.
+ * Returns RSG_EINVAL when a well row has no usable BHP derivative or couples wells (the engine then keeps the
+ * full system). Replaces WellSchur::build / reduceRhs (engine/src/bsr.cpp:733-840, 973-980). */
+int rsg_wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                         const double* b, int* nnzb, int* sRowPtr, int* sCol, double* sVal, double* bc);
+/* x = [xc ; Dww^-1 (b_w - Awc xc)]. Replaces WellSchur::recover (engine/src/bsr.cpp:982-990). */
+int rsg_wellschur_recover(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                          const double* b, const double* xc, double* x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,100 @@
+"""ctypes binding of the native library ``librsg.so`` (the C ABI declared in include/rsg.h).
+
+There is no CPU fallback: if the library is missing it is built from ressim_gb300/csrc (nvcc required); if that
+fails the import error is raised to the caller.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+RSG_OK, RSG_EINVAL, RSG_ECUDA, RSG_ENOMEM, RSG_ESTATE, RSG_ETIMEOUT, RSG_EBREAKDOWN, RSG_ENOTCONV = 0, -1, -2, -3, -4, -5, -6, 1
+PREC = {"bilu0": 0, "cpr": 1, "jacobi": 2}
+KRYLOV = {"bicgstab": 0, "gmres": 1}
+PRECISION = {"fp64": 0, "mixed": 1}
+
+# every symbol include/rsg.h declares
+EXPORTS = [
+    "rsg_default_options", "rsg_last_error", "rsg_version", "rsg_create", "rsg_destroy", "rsg_set_matrix", "rsg_set_batch",
+    "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
+    "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
+]
+
+
+class Options(C.Structure):
+    _fields_ = [("precond", C.c_int), ("krylov", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
+                ("gmres_fallback", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
+                ("mem_budget", C.c_size_t)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
+                ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("regularised_blocks", C.c_int), ("amg_levels", C.c_int),
+                ("device_bytes", C.c_size_t), ("kernel_launches", C.c_longlong)]
+
+
+class RsgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"rsg error {code}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def load(build_if_missing: bool = True):
+    """Load (building if needed) ``librsg.so``."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError("librsg.so is not built (run __graft_entry__.build())")
+        _build.build()
+    L = C.CDLL(path)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.rsg_default_options.argtypes = [C.POINTER(Options)]
+    L.rsg_last_error.restype = C.c_char_p
+    L.rsg_version.restype = C.c_char_p
+    L.rsg_create.argtypes = [C.POINTER(vp), C.POINTER(Options)]
+    L.rsg_destroy.argtypes = [vp]
+    L.rsg_set_matrix.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp]
+    L.rsg_set_batch.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp]
+    L.rsg_setup.argtypes = [vp, vp]
+    L.rsg_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
+    L.rsg_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
+    L.rsg_batch_results.argtypes = [vp, vp, vp, vp]
+    L.rsg_spmv.argtypes = [vp, vp, vp]
+    L.rsg_spmv_device.argtypes = [vp, vp, vp]
+    L.rsg_precond_apply.argtypes = [vp, vp, vp]
+    L.rsg_precond_apply_device.argtypes = [vp, vp, vp]
+    L.rsg_get_factors.argtypes = [vp, vp]
+    L.rsg_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.rsg_stream.argtypes = [vp]
+    L.rsg_stream.restype = vp
+    L.rsg_wellschur_reduce.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, ip, vp, vp, vp, vp]
+    L.rsg_wellschur_recover.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+    for name in EXPORTS:
+        getattr(L, name).restype = getattr(L, name).restype if name in ("rsg_last_error", "rsg_version", "rsg_stream") else (
+            None if name == "rsg_default_options" else C.c_int)
+    _LIB = L
+    return L
+
+
+def last_error() -> str:
+    return load().rsg_last_error().decode()
+
+
+def check(code: int, allow_notconv: bool = True) -> int:
+    if code < 0 or (code > 0 and not allow_notconv):
+        raise RsgError(code, last_error())
+    return code
+
+
+def ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a is not None else None

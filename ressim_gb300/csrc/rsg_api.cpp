@@ -1,0 +1,596 @@
+// C ABI of the rsg solver: handle lifecycle, uploads with pattern reuse, device set-up, Krylov drivers.
+#include "rsg.h"
+#include "rsg_impl.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace rsg;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define RSG_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return fail(RSG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct DevMem {
+    std::vector<std::pair<void*, size_t>> blocks;
+    size_t bytes = 0, budget = 0;
+    int alloc(void** p, size_t n) {
+        if (n == 0) n = 16;
+        if (budget && bytes + n > budget) return fail(RSG_ENOMEM, "device memory budget exhausted");
+        cudaError_t e = cudaMalloc(p, n);
+        if (e != cudaSuccess) return fail(RSG_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        blocks.push_back({*p, n});
+        bytes += n;
+        return RSG_OK;
+    }
+    void release(void* p) {
+        if (!p) return;
+        for (size_t k = 0; k < blocks.size(); ++k)
+            if (blocks[k].first == p) {
+                cudaFree(p);
+                bytes -= blocks[k].second;
+                blocks.erase(blocks.begin() + long(k));
+                return;
+            }
+    }
+    void release_all() {
+        for (auto& b : blocks) cudaFree(b.first);
+        blocks.clear();
+        bytes = 0;
+    }
+};
+
+template <class T>
+int dalloc(DevMem& M, T** p, size_t count) {
+    return M.alloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+}  // namespace
+
+struct rsg_solver {
+    rsg_options opt{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevMem mem;
+    DevMem pmem;                 // pattern-plan allocations (freed on pattern change)
+    // plan
+    HostPlan plan;
+    DevPlan dp;
+    bool havePlan = false, haveMatrix = false, haveSetup = false;
+    int nsys = 0;
+    // matrix values and preconditioner storage
+    double* val = nullptr;
+    double* lu = nullptr;
+    float* luf = nullptr;
+    double* work = nullptr;
+    double* dinv = nullptr;
+    // vectors
+    BicgVecs V{};
+    double *b = nullptr, *xout = nullptr, *tmp = nullptr;
+    // sync-free state, reductions, scalars
+    SweepState S{};
+    ReduceState R{};
+    KScal* ks = nullptr;
+    int* d_active = nullptr;
+    int* d_err = nullptr;
+    int* d_nreg = nullptr;
+    double* d_trueres = nullptr;
+    int* h_pin = nullptr;        // pinned: [0] active, [1] err, [2] nreg
+    int epoch = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // graph of `check_every` iterations
+    cudaGraphExec_t gexec = nullptr;
+    int gIters = 0, gKind = -1;
+    // results
+    rsg_stats st{};
+    long long launches = 0;
+    std::vector<KScal> hks;
+    std::vector<double> htrue;
+    std::mutex mu;
+};
+
+namespace {
+
+void free_plan(rsg_solver* h) {
+    if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+    h->pmem.release_all();
+    h->dp = DevPlan{};
+    h->val = nullptr; h->lu = nullptr; h->luf = nullptr; h->work = nullptr; h->dinv = nullptr;
+    h->V = BicgVecs{};
+    h->b = h->xout = h->tmp = nullptr;
+    h->S = SweepState{};
+    h->R = ReduceState{};
+    h->ks = nullptr; h->d_trueres = nullptr;
+    h->havePlan = h->haveMatrix = h->haveSetup = false;
+}
+
+template <class T>
+int upload(DevMem& M, T** d, const std::vector<T>& v, cudaStream_t st) {
+    int rc = dalloc(M, d, v.size());
+    if (rc) return rc;
+    if (!v.empty()) RSG_CUDA(cudaMemcpyAsync(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return RSG_OK;
+}
+
+int alloc_plan(rsg_solver* h) {
+    HostPlan& P = h->plan;
+    DevMem& M = h->pmem;
+    M.budget = h->opt.mem_budget ? (h->opt.mem_budget > h->mem.bytes ? h->opt.mem_budget - h->mem.bytes : 1) : 0;
+    DevPlan& D = h->dp;
+    cudaStream_t st = h->stream;
+    D.n = P.n; D.nnzb = P.nnzb; D.nsys = P.nsys; D.ntiles = int(P.tileSys.size());
+    int rc;
+    if ((rc = upload(M, &D.rowPtr, P.rowPtr, st)) || (rc = upload(M, &D.col, P.col, st)) || (rc = upload(M, &D.diag, P.diag, st)) ||
+        (rc = upload(M, &D.ford, P.ford, st)) || (rc = upload(M, &D.bord, P.bord, st)) || (rc = upload(M, &D.elimPtr, P.elimPtr, st)) ||
+        (rc = upload(M, &D.elimT, P.elimT, st)) || (rc = upload(M, &D.elimQ, P.elimQ, st)) || (rc = upload(M, &D.rowSys, P.rowSys, st)) ||
+        (rc = upload(M, &D.tileRow0, P.tileRow0, st)) || (rc = upload(M, &D.tileSys, P.tileSys, st)) ||
+        (rc = upload(M, &D.sysTile0, P.sysTile0, st)) || (rc = upload(M, &D.sysRow0, P.sysRow0, st)))
+        return rc;
+    const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
+    if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) || (rc = dalloc(M, &h->tmp, N)))
+        return rc;
+    double** vecs[] = {&h->V.x, &h->V.r, &h->V.rh, &h->V.p, &h->V.v, &h->V.s, &h->V.t, &h->V.ph, &h->V.sh};
+    for (double** v : vecs)
+        if ((rc = dalloc(M, v, N))) return rc;
+    if ((rc = dalloc(M, &h->S.flagF, size_t(P.n))) || (rc = dalloc(M, &h->S.flagB, size_t(P.n))) ||
+        (rc = dalloc(M, &h->S.flagL, size_t(P.n))) || (rc = dalloc(M, &h->S.ctr, 4)))
+        return rc;
+    RSG_CUDA(cudaMemsetAsync(h->S.flagF, 0, sizeof(int) * size_t(P.n), st));
+    RSG_CUDA(cudaMemsetAsync(h->S.flagB, 0, sizeof(int) * size_t(P.n), st));
+    RSG_CUDA(cudaMemsetAsync(h->S.flagL, 0, sizeof(int) * size_t(P.n), st));
+    RSG_CUDA(cudaMemsetAsync(h->S.ctr, 0, sizeof(unsigned) * 4, st));
+    if ((rc = dalloc(M, &h->R.part, size_t(D.ntiles) * MAX_DOTS)) || (rc = dalloc(M, &h->R.done, 1)) ||
+        (rc = dalloc(M, &h->R.sysdot, size_t(P.nsys) * MAX_DOTS)) || (rc = dalloc(M, &h->ks, size_t(P.nsys))) ||
+        (rc = dalloc(M, &h->d_trueres, size_t(P.nsys))))
+        return rc;
+    RSG_CUDA(cudaMemsetAsync(h->R.done, 0, sizeof(unsigned), st));
+    RSG_CUDA(cudaMemsetAsync(h->ks, 0, sizeof(KScal) * size_t(P.nsys), st));
+    h->epoch = 0;
+    h->havePlan = true;
+    return RSG_OK;
+}
+
+// device-side status after a kernel sequence: timeouts become RSG_ETIMEOUT and the sweep state is reset
+int check_device_errors(rsg_solver* h) {
+    RSG_CUDA(cudaMemcpyAsync(h->h_pin + 1, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->h_pin[1] != 0) {
+        const int e = h->h_pin[1];
+        cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
+        cudaMemsetAsync(h->S.flagF, 0, sizeof(int) * size_t(h->plan.n), h->stream);
+        cudaMemsetAsync(h->S.flagB, 0, sizeof(int) * size_t(h->plan.n), h->stream);
+        cudaMemsetAsync(h->S.ctr, 0, sizeof(unsigned) * 4, h->stream);
+        cudaMemsetAsync(h->R.done, 0, sizeof(unsigned), h->stream);
+        cudaStreamSynchronize(h->stream);
+        if (e & ERR_TIMEOUT) return fail(RSG_ETIMEOUT, "a bounded device wait ran out (sweep dependency not satisfied)");
+        return fail(RSG_ECUDA, "device error flag " + std::to_string(e));
+    }
+    return RSG_OK;
+}
+
+PrecDev prec_dev(rsg_solver* h) {
+    PrecDev M;
+    if (h->opt.precond == RSG_PREC_JACOBI) { M.kind = 2; M.dinv = h->dinv; }
+    else if (h->opt.precision == RSG_MIXED) { M.kind = 1; M.luf = h->luf; }
+    else { M.kind = 0; M.lu = h->lu; }
+    M.val = h->val;
+    return M;
+}
+
+int set_values(rsg_solver* h, const std::vector<const double*>& vals, const std::vector<int>& nnzbs) {
+    size_t off = 0;
+    for (size_t s = 0; s < vals.size(); ++s) {
+        const size_t cnt = size_t(nnzbs[s]) * NB2;
+        if (cnt) RSG_CUDA(cudaMemcpyAsync(h->val + off, vals[s], cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        off += cnt;
+    }
+    h->haveMatrix = true;
+    h->haveSetup = false;
+    return RSG_OK;
+}
+
+int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
+                 const double* const* val) {
+    if (nsys < 1 || !n || !rowPtr || !col || !val) return fail(RSG_EINVAL, "set_batch: null argument or nsys < 1");
+    if (nb != NB) return fail(RSG_EINVAL, "only nb = 3 (black-oil blocks) is supported, got nb = " + std::to_string(nb));
+    std::vector<int> sysRow0(size_t(nsys) + 1, 0);
+    for (int s = 0; s < nsys; ++s) {
+        if (n[s] < 1 || !rowPtr[s] || !col[s] || !val[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " is empty");
+        sysRow0[size_t(s) + 1] = sysRow0[size_t(s)] + n[s];
+    }
+    const int ntot = sysRow0[size_t(nsys)];
+    // concatenated pattern of the block-diagonal batch
+    std::vector<int> rp(size_t(ntot) + 1, 0), ci;
+    std::vector<int> nnzbs(static_cast<size_t>(nsys));
+    size_t total = 0;
+    for (int s = 0; s < nsys; ++s) total += size_t(rowPtr[s][n[s]]);
+    ci.reserve(total);
+    for (int s = 0; s < nsys; ++s) {
+        const int r0 = sysRow0[size_t(s)];
+        if (rowPtr[s][0] != 0) return fail(RSG_EINVAL, "rowPtr[0] must be 0 (system " + std::to_string(s) + ")");
+        for (int i = 0; i < n[s]; ++i) {
+            rp[size_t(r0 + i) + 1] = rp[size_t(r0)] + rowPtr[s][i + 1];
+            for (int p = rowPtr[s][i]; p < rowPtr[s][i + 1]; ++p) {
+                const int c = col[s][p];
+                if (c < 0 || c >= n[s]) return fail(RSG_EINVAL, "column out of range in system " + std::to_string(s));
+                ci.push_back(c + r0);
+            }
+        }
+        nnzbs[size_t(s)] = rowPtr[s][n[s]];
+    }
+    const bool same = h->havePlan && h->plan.nsys == nsys && h->plan.rowPtr == rp && h->plan.col == ci && h->plan.sysRow0 == sysRow0;
+    if (!same) {
+        free_plan(h);
+        std::string err;
+        if (!build_plan(h->plan, nsys, sysRow0, rp, ci, err)) return fail(RSG_EINVAL, err);
+        int rc = alloc_plan(h);
+        if (rc) { free_plan(h); return rc; }
+        h->nsys = nsys;
+    }
+    std::vector<const double*> vals(val, val + nsys);
+    return set_values(h, vals, nnzbs);
+}
+
+int ensure_precond_storage(rsg_solver* h) {
+    const size_t E = size_t(h->plan.nnzb) * NB2;
+    int rc;
+    if (h->opt.precond == RSG_PREC_JACOBI) {
+        if (!h->dinv && (rc = dalloc(h->pmem, &h->dinv, size_t(h->plan.n) * NB2))) return rc;
+    } else if (h->opt.precision == RSG_MIXED) {
+        if (!h->luf && (rc = dalloc(h->pmem, &h->luf, E))) return rc;
+        if (!h->work && (rc = dalloc(h->pmem, &h->work, E))) return rc;
+        if (!h->V.y32 && (rc = dalloc(h->pmem, &h->V.y32, size_t(h->plan.n) * NB))) return rc;
+    } else {
+        if (!h->lu && (rc = dalloc(h->pmem, &h->lu, E))) return rc;
+    }
+    return RSG_OK;
+}
+
+int do_setup(rsg_solver* h, const double* acc) {
+    (void)acc;
+    if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
+    if (h->opt.precond == RSG_PREC_CPR) return fail(RSG_EINVAL, "CPR preconditioner is not available in this build");
+    int rc = ensure_precond_storage(h);
+    if (rc) return rc;
+    RSG_CUDA(cudaMemsetAsync(h->d_nreg, 0, sizeof(int), h->stream));
+    RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
+    h->launches += 1;
+    if (h->opt.precond == RSG_PREC_JACOBI) {
+        launch_block_jacobi_setup(h->dp, h->val, h->dinv, h->d_nreg, h->stream);
+    } else {
+        ++h->epoch;
+        if (h->opt.precision == RSG_MIXED)
+            launch_factor_lean(h->dp, h->val, h->luf, h->work, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
+        else
+            launch_factor_f64(h->dp, h->val, h->lu, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
+    }
+    RSG_CUDA(cudaGetLastError());
+    RSG_CUDA(cudaEventRecord(h->ev1, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(h->h_pin + 2, h->d_nreg, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = check_device_errors(h))) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->st.setup_ms = ms;
+    h->st.regularised_blocks = h->h_pin[2];
+    h->haveSetup = true;
+    return RSG_OK;
+}
+
+int launch_iterations(rsg_solver* h, int k) {
+    const PrecDev M = prec_dev(h);
+    h->launches += (long long)k * (M.kind == 2 ? 5 : 7);
+    if (h->opt.use_graphs) {
+        const int kind = M.kind;
+        if (!h->gexec || h->gIters != k || h->gKind != kind) {
+            if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+            cudaGraph_t g = nullptr;
+            RSG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            for (int i = 0; i < k; ++i) launch_bicg_iteration(h->dp, h->val, M, h->V, h->ks, h->R, h->S, h->d_active, h->d_err, h->stream);
+            RSG_CUDA(cudaStreamEndCapture(h->stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { h->gexec = nullptr; return fail(RSG_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)); }
+            h->gIters = k;
+            h->gKind = kind;
+        }
+        RSG_CUDA(cudaGraphLaunch(h->gexec, h->stream));
+    } else {
+        for (int i = 0; i < k; ++i) launch_bicg_iteration(h->dp, h->val, M, h->V, h->ks, h->R, h->S, h->d_active, h->d_err, h->stream);
+        RSG_CUDA(cudaGetLastError());
+    }
+    return RSG_OK;
+}
+
+int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
+    if (h->opt.krylov != RSG_KRYLOV_BICGSTAB) return fail(RSG_EINVAL, "GMRES is not available in this build");
+    if (!(tol > 0) || maxIt < 0) return fail(RSG_EINVAL, "tol must be > 0 and maxIt >= 0");
+    const size_t N = size_t(h->plan.n) * NB;
+    RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
+    launch_bicg_init(h->dp, d_b, h->V, h->ks, h->R, tol, maxIt, h->d_active, h->stream);
+    h->launches += 2;   // init + true residual
+    RSG_CUDA(cudaGetLastError());
+    const int chunk = h->opt.check_every > 0 ? h->opt.check_every : 4;
+    int launched = 0, rc;
+    for (;;) {
+        RSG_CUDA(cudaMemcpyAsync(h->h_pin, h->d_active, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        if (h->h_pin[0] <= 0 || launched >= maxIt) break;
+        if ((rc = launch_iterations(h, chunk))) return rc;
+        launched += chunk;
+    }
+    if (d_x != h->V.x) RSG_CUDA(cudaMemcpyAsync(d_x, h->V.x, N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    RSG_CUDA(cudaEventRecord(h->ev1, h->stream));
+    launch_true_residual(h->dp, h->val, d_b, h->V.x, h->tmp, h->R, h->d_trueres, h->stream);
+    RSG_CUDA(cudaGetLastError());
+    if ((rc = check_device_errors(h))) return rc;
+    h->hks.resize(size_t(h->plan.nsys));
+    h->htrue.resize(size_t(h->plan.nsys));
+    RSG_CUDA(cudaMemcpyAsync(h->hks.data(), h->ks, sizeof(KScal) * h->hks.size(), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(h->htrue.data(), h->d_trueres, sizeof(double) * h->htrue.size(), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    int maxits = 0, conv = 1, brk = 0;
+    double mrel = 0, mtrue = 0;
+    for (size_t s = 0; s < h->hks.size(); ++s) {
+        const KScal& k = h->hks[s];
+        maxits = std::max(maxits, k.its);
+        mrel = std::max(mrel, k.relres);
+        mtrue = std::max(mtrue, h->htrue[s]);
+        if (k.status != ST_CONV) conv = 0;
+        if (k.status == ST_BREAKDOWN) brk = 1;
+    }
+    h->st.iterations = maxits;
+    h->st.converged = conv;
+    h->st.rel_residual = mrel;
+    h->st.true_rel_residual = mtrue;
+    h->st.solve_ms = ms;
+    h->st.device_bytes = h->mem.bytes + h->pmem.bytes;
+    if (iterations) *iterations = maxits;
+    if (relres) *relres = mrel;
+    if (conv) return RSG_OK;
+    if (brk) return fail(RSG_EBREAKDOWN, "Krylov breakdown before convergence");
+    return RSG_ENOTCONV;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rsg_version(void) { return "rsg 0.1 (sm_103a)"; }
+const char* rsg_last_error(void) { return g_err.c_str(); }
+
+void rsg_default_options(rsg_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precond = RSG_PREC_BILU0;
+    o->krylov = RSG_KRYLOV_BICGSTAB;
+    o->restart = 40;
+    o->precision = RSG_FP64;
+    o->gmres_fallback = 0;
+    o->check_every = 4;
+    o->use_graphs = 1;
+    o->device = 0;
+    o->mem_budget = 0;
+}
+
+int rsg_create(rsg_solver** out, const rsg_options* opts) {
+    if (!out) return fail(RSG_EINVAL, "null handle pointer");
+    *out = nullptr;
+    rsg_options o;
+    rsg_default_options(&o);
+    if (opts) o = *opts;
+    if (o.precond < 0 || o.precond > 2 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 1)
+        return fail(RSG_EINVAL, "invalid options");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
+    if (o.device < 0 || o.device >= ndev) return fail(RSG_EINVAL, "device ordinal out of range");
+    RSG_CUDA(cudaSetDevice(o.device));
+    rsg_solver* h = new rsg_solver();
+    h->opt = o;
+    h->device = o.device;
+    h->mem.budget = o.mem_budget;
+    auto bail = [&](cudaError_t e, const char* what) {
+        std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+        if (h->stream) cudaStreamDestroy(h->stream);
+        delete h;
+        return fail(RSG_ECUDA, m);
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
+    if ((e = cudaMallocHost(&h->h_pin, 4 * sizeof(int))) != cudaSuccess) return bail(e, "cudaMallocHost");
+    int rc;
+    if ((rc = dalloc(h->mem, &h->d_active, 1)) || (rc = dalloc(h->mem, &h->d_err, 1)) || (rc = dalloc(h->mem, &h->d_nreg, 1))) {
+        h->mem.release_all();
+        cudaFreeHost(h->h_pin);
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return rc;
+    }
+    cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
+    cudaMemsetAsync(h->d_active, 0, sizeof(int), h->stream);
+    *out = h;
+    return RSG_OK;
+}
+
+int rsg_destroy(rsg_solver* h) {
+    if (!h) return RSG_OK;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    free_plan(h);
+    h->mem.release_all();
+    if (h->h_pin) cudaFreeHost(h->h_pin);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return RSG_OK;
+}
+
+int rsg_set_matrix(rsg_solver* h, int n, int nb, const int* rowPtr, const int* col, const double* val) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_set_batch(h, 1, nb, &n, &rowPtr, &col, &val);
+}
+
+int rsg_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
+                  const double* const* val) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_set_batch(h, nsys, nb, n, rowPtr, col, val);
+}
+
+int rsg_setup(rsg_solver* h, const double* acc) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_setup(h, acc);
+}
+
+int rsg_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h || !d_b || !d_x) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_solve_device(h, d_b, d_x, tol, maxIt, iterations, relres);
+}
+
+int rsg_solve(rsg_solver* h, const double* b, double* x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h || !b || !x) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->havePlan) return fail(RSG_ESTATE, "solve before set_matrix");
+    const size_t N = size_t(h->plan.n) * NB;
+    RSG_CUDA(cudaMemcpyAsync(h->b, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const int rc = do_solve_device(h, h->b, h->xout, tol, maxIt, iterations, relres);
+    if (rc < 0) return rc;
+    RSG_CUDA(cudaMemcpyAsync(x, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    return rc;
+}
+
+int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relres) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    for (size_t s = 0; s < h->hks.size(); ++s) {
+        if (its) its[s] = h->hks[s].its;
+        if (relres) relres[s] = h->hks[s].relres;
+        if (true_relres) true_relres[s] = h->htrue[s];
+    }
+    return RSG_OK;
+}
+
+int rsg_spmv_device(rsg_solver* h, const double* d_x, double* d_y) {
+    if (!h || !d_x || !d_y) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
+    launch_spmv_f64(h->dp, h->val, d_x, d_y, h->stream);
+    h->launches += 1;
+    RSG_CUDA(cudaGetLastError());
+    return RSG_OK;
+}
+
+int rsg_spmv(rsg_solver* h, const double* x, double* y) {
+    if (!h || !x || !y) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
+    const size_t N = size_t(h->plan.n) * NB;
+    RSG_CUDA(cudaMemcpyAsync(h->b, x, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_spmv_f64(h->dp, h->val, h->b, h->xout, h->stream);
+    RSG_CUDA(cudaGetLastError());
+    RSG_CUDA(cudaMemcpyAsync(y, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    return RSG_OK;
+}
+
+static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
+    const PrecDev M = prec_dev(h);
+    if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
+    else if (M.kind == 1) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.y32, h->S, h->d_err, h->stream); h->launches += 2; }
+    else { launch_block_jacobi_apply(h->dp, h->dinv, d_r, d_z, h->stream); h->launches += 1; }
+    RSG_CUDA(cudaGetLastError());
+    return RSG_OK;
+}
+
+int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z) {
+    if (!h || !d_r || !d_z) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
+    return precond_apply_dev(h, d_r, d_z);
+}
+
+int rsg_precond_apply(rsg_solver* h, const double* r, double* z) {
+    if (!h || !r || !z) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
+    const size_t N = size_t(h->plan.n) * NB;
+    RSG_CUDA(cudaMemcpyAsync(h->b, r, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    int rc = precond_apply_dev(h, h->b, h->xout);
+    if (rc) return rc;
+    rc = check_device_errors(h);
+    if (rc) return rc;
+    RSG_CUDA(cudaMemcpyAsync(z, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    return RSG_OK;
+}
+
+int rsg_get_factors(rsg_solver* h, double* lu) {
+    if (!h || !lu) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->haveSetup || !h->lu) return fail(RSG_ESTATE, "no FP64 BILU0 factors (setup not run, or not the FP64 BILU0 path)");
+    RSG_CUDA(cudaMemcpyAsync(lu, h->lu, size_t(h->plan.nnzb) * NB2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    return RSG_OK;
+}
+
+int rsg_get_stats(rsg_solver* h, rsg_stats* st) {
+    if (!h || !st) return fail(RSG_EINVAL, "null argument");
+    *st = h->st;
+    st->device_bytes = h->mem.bytes + h->pmem.bytes;
+    st->kernel_launches = h->launches;
+    return RSG_OK;
+}
+
+void* rsg_stream(rsg_solver* h) { return h ? (void*)h->stream : nullptr; }
+
+int rsg_wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                         const double* b, int* nnzb, int* sRowPtr, int* sCol, double* sVal, double* bc) {
+    if (!rowPtr || !col || !val || !nnzb) return fail(RSG_EINVAL, "null argument");
+    std::string err;
+    if (wellschur_reduce(nrows, rowPtr, col, val, na, nv, nw, b, nnzb, sRowPtr, sCol, sVal, bc, err)) return fail(RSG_EINVAL, err);
+    return RSG_OK;
+}
+
+int rsg_wellschur_recover(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                          const double* b, const double* xc, double* x) {
+    if (!rowPtr || !col || !val || !b || !xc || !x) return fail(RSG_EINVAL, "null argument");
+    std::string err;
+    if (wellschur_recover(nrows, rowPtr, col, val, na, nv, nw, b, xc, x, err)) return fail(RSG_EINVAL, err);
+    return RSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// Internal declarations of the rsg library (host plan structures, device buffers, kernel launchers).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace rsg {
+
+constexpr int NB = 3;                 // block size of the black-oil system (p, Sw, x_g)
+constexpr int NB2 = NB * NB;
+constexpr int TILE_ROWS = 256;        // block rows per tile of the tile kernels (64-row steps, 3 threads per block row)
+constexpr int TILE_THREADS = TILE_ROWS * NB;
+constexpr int MAX_DOTS = 4;           // partial sums per tile in the fused reductions
+
+// Krylov status per system (device int)
+enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3 };
+
+// Error bits written by kernels (device int, OR-ed)
+enum : int { ERR_TIMEOUT = 1, ERR_NONFINITE = 2 };
+
+// Per-system Krylov scalars, resident on the device (no host round trip per inner product).
+struct KScal {
+    double rho, alpha, omega, beta;   // BiCGSTAB recurrences (engine/src/linsolve.cpp:166-211)
+    double bn;                        // ||b||
+    double relres;                    // recursive relative residual of the last completed iteration
+    double sn;                        // ||s|| of the current iteration
+    int status, its, maxit, pad;
+    double tol;
+};
+
+// Host-built, pattern-only plan of the sync-free triangular sweeps and the factorisation.
+struct HostPlan {
+    int n = 0, nnzb = 0, nsys = 1;
+    std::vector<int> rowPtr, col, diag;
+    std::vector<int> ford, bord;      // claim orders: forward (by L level) and backward (by U level)
+    int nlevF = 0, nlevB = 0;
+    std::vector<int> elimPtr;         // per block entry p (lower entries only non-empty): range in elimT/elimQ
+    std::vector<int> elimT, elimQ;    // target block t in row i, U block q in row k: A_it -= L_ik U_kq
+    std::vector<int> rowSys;          // system of every block row
+    std::vector<int> sysRow0;         // first block row of every system (nsys + 1)
+    std::vector<int> tileRow0;        // first row of every tile (ntiles + 1); tiles never cross systems
+    std::vector<int> tileSys;         // system of every tile
+    std::vector<int> sysTile0;        // first tile of every system (nsys + 1)
+    bool symmetric = true;
+};
+
+// Builds the plan of a (block-diagonal batch of) BSR pattern(s). Returns false with a message on bad input.
+bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
+                const std::vector<int>& col, std::string& err);
+
+// ---- AMG hierarchy (host set-up of the aggregation; engine/src/amg.cpp:137-252)
+struct HostCsr {
+    int n = 0, m = 0;                 // rows, columns
+    std::vector<int> rp, ci;
+    std::vector<double> v;
+};
+struct HostAmgLevel {
+    HostCsr A;                        // level operator (square), diagonal present in every row
+    std::vector<int> diag;
+    std::vector<int> agg;             // coarse index of every row (empty on the coarsest level)
+    int nc = 0;
+};
+struct HostAmg {
+    std::vector<HostAmgLevel> lv;
+};
+// Aggregation set-up of a pressure matrix (pattern + values); the Galerkin values of coarser levels are
+// produced on the device afterwards (rsg_amg_refresh on device) -- the host computes them too for the plan.
+void amg_setup_host(HostAmg& H, const HostCsr& A0);
+
+// ---- well Schur complement (engine/src/bsr.cpp:733-840, 973-990)
+int wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                     const double* b, int* nnzb, int* sRowPtr, int* sCol, double* sVal, double* bc, std::string& err);
+int wellschur_recover(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                      const double* b, const double* xc, double* x, std::string& err);
+
+// ---- device plan (mirrors HostPlan) and buffers
+struct DevPlan {
+    int n = 0, nnzb = 0, nsys = 0, ntiles = 0;
+    int *rowPtr = nullptr, *col = nullptr, *diag = nullptr;
+    int *ford = nullptr, *bord = nullptr;
+    int *elimPtr = nullptr, *elimT = nullptr, *elimQ = nullptr;
+    int *rowSys = nullptr, *tileRow0 = nullptr, *tileSys = nullptr, *sysTile0 = nullptr, *sysRow0 = nullptr;
+};
+
+struct SweepState {                   // sync-free sweep flags and claim counters
+    int *flagF = nullptr, *flagB = nullptr, *flagL = nullptr;
+    unsigned *ctr = nullptr;          // [0] forward, [1] backward, [2] factorisation, [3] spare
+};
+
+struct ReduceState {                  // fused tile reductions
+    double* part = nullptr;           // ntiles * MAX_DOTS
+    unsigned* done = nullptr;         // arrival counter of the last-block pattern
+    double* sysdot = nullptr;         // nsys * MAX_DOTS (results of the last reduction)
+};
+
+// ---- kernel launchers (rsg_kernels.cu)
+int device_sm_count();
+void launch_factor_f64(const DevPlan& P, const double* val, double* lu, SweepState& S, int epoch, int* nreg, int* err,
+                       cudaStream_t st);
+void launch_factor_lean(const DevPlan& P, const double* val, float* luf, double* work, SweepState& S, int epoch, int* nreg,
+                        int* err, cudaStream_t st);
+// z = U^-1 L^-1 r (FP64 factors, FP64 vectors) or with FP32 factors / FP32 vectors and accumulation.
+void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, double* z, SweepState& S, int* err,
+                          cudaStream_t st);
+void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S,
+                          int* err, cudaStream_t st);
+void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st);
+// block-Jacobi: dinv = inverse diagonal blocks (FP64), z = dinv r
+void launch_block_jacobi_setup(const DevPlan& P, const double* val, double* dinv, int* nreg, cudaStream_t st);
+void launch_block_jacobi_apply(const DevPlan& P, const double* dinv, const double* r, double* z, cudaStream_t st);
+
+// BiCGSTAB building blocks (per-system scalars on the device).
+struct BicgVecs {
+    double *x, *r, *rh, *p, *v, *s, *t, *ph, *sh;
+    float* y32;                       // FP32 sweep intermediate (mixed precision)
+};
+void launch_bicg_init(const DevPlan& P, const double* b, BicgVecs& V, KScal* ks, ReduceState& R, double tol, int maxit,
+                      int* active, cudaStream_t st);
+// one BiCGSTAB iteration (engine/src/linsolve.cpp:166-214) with the preconditioner given by prec:
+// 0 = BILU0 FP64, 1 = BILU0 FP32 (mixed), 2 = block Jacobi
+struct PrecDev {
+    int kind = 0;
+    const double* lu = nullptr;
+    const float* luf = nullptr;
+    const double* dinv = nullptr;
+    const double* val = nullptr;
+};
+void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M, BicgVecs& V, KScal* ks, ReduceState& R,
+                           SweepState& S, int* active, int* err, cudaStream_t st);
+// true residual ||b - A x|| / ||b|| per system (FP64)
+void launch_true_residual(const DevPlan& P, const double* val, const double* b, const double* x, double* tmp, ReduceState& R,
+                          double* out, cudaStream_t st);
+
+}  // namespace rsg

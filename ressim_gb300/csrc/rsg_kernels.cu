@@ -1,0 +1,909 @@
+// Device kernels of the rsg solver (sm_103a).
+//
+// * BILU0 factorisation and the forward / backward sweeps are exact natural-order ILU(0): rows are processed in
+//   a level order (a topological order of the L, resp. U, dependencies) by a persistent grid whose warps claim
+//   32 rows at a time from an atomic counter; a row waits for the rows it depends on through per-row flags
+//   (release / acquire at GPU scope). Claiming in order guarantees that every awaited row belongs to a warp that
+//   is already running, so the waits always end; each wait is additionally bounded and reports RSG_ETIMEOUT.
+// * FP64 block arithmetic uses explicitly rounded multiplies and adds in the reference's loop order
+//   (engine/src/bsr.cpp:13-64), so factors, sweeps and SpMV are bitwise those of the reference's serial code.
+// * Tile kernels (SpMV, vector updates) cover TILE_ROWS block rows of one system with 3 threads per block row;
+//   inner products are reduced per tile and then, in the last tile to finish, per system in a fixed order
+//   (deterministic), and the BiCGSTAB scalar recurrences are evaluated on the device.
+#include "rsg_impl.h"
+
+#include <cuda_runtime.h>
+#include <cstdio>
+
+namespace rsg {
+
+namespace {
+
+constexpr unsigned kSpinLimit = 1u << 22;   // x up to 256 ns back-off: about one second per wait
+constexpr int kSweepThreads = 128;
+constexpr int kTileThreads = 192;           // 64 block rows x 3 per step
+
+// ------------------------------------------------------------------ memory-order helpers
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// bounded wait for *f == want; on time-out sets ERR_TIMEOUT and returns false (the caller then proceeds)
+__device__ __noinline__ bool wait_flag(const int* f, int want, int* err) {
+    if (ld_acquire(f) == want) return true;
+    unsigned ns = 32;
+    for (unsigned it = 0; it < kSpinLimit; ++it) {
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+        if (ld_acquire(f) == want) return true;
+        if ((it & 255u) == 255u && *(volatile int*)err != 0) return false;   // another wait already gave up
+    }
+    atomicOr(err, ERR_TIMEOUT);
+    return false;
+}
+__device__ __forceinline__ int warp_claim(unsigned* ctr) {
+    unsigned base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(ctr, 32u);
+    return int(__shfl_sync(0xffffffffu, base, 0));
+}
+
+// ------------------------------------------------------------------ FP64 block arithmetic, reference order, unfused
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+
+// c = a b   (engine/src/bsr.cpp:26-32: row accumulator, k outer, j inner)
+__device__ __forceinline__ void gemm3(const double* a, const double* b, double* c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double r0 = 0, r1 = 0, r2 = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double f = a[i * 3 + k];
+            r0 = da(r0, dm(f, b[k * 3 + 0]));
+            r1 = da(r1, dm(f, b[k * 3 + 1]));
+            r2 = da(r2, dm(f, b[k * 3 + 2]));
+        }
+        c[i * 3 + 0] = r0; c[i * 3 + 1] = r1; c[i * 3 + 2] = r2;
+    }
+}
+// c -= a b  (engine/src/bsr.cpp:33-39)
+__device__ __forceinline__ void gemm3_sub(const double* a, const double* b, double* c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double r0 = 0, r1 = 0, r2 = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double f = a[i * 3 + k];
+            r0 = da(r0, dm(f, b[k * 3 + 0]));
+            r1 = da(r1, dm(f, b[k * 3 + 1]));
+            r2 = da(r2, dm(f, b[k * 3 + 2]));
+        }
+        c[i * 3 + 0] = ds(c[i * 3 + 0], r0); c[i * 3 + 1] = ds(c[i * 3 + 1], r1); c[i * 3 + 2] = ds(c[i * 3 + 2], r2);
+    }
+}
+// one row of a 3x3 block times a 3-vector, accumulated from zero left to right
+__device__ __forceinline__ double dot3(const double* a, const double* x) {
+    return da(da(dm(a[0], x[0]), dm(a[1], x[1])), dm(a[2], x[2]));
+}
+
+// engine/src/bsr.cpp:67-87 for nb = 3: Gauss-Jordan on [A | I], partial pivoting, singular below 1e-14 max|a|
+__device__ bool invert3(double* a) {
+    double m[3][6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) { m[i][j] = a[i * 3 + j]; m[i][3 + j] = (i == j) ? 1.0 : 0.0; }
+    double scale = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) scale = fmax(scale, fabs(a[i]));
+    if (!(scale > 0) || !isfinite(scale)) return false;
+    for (int k = 0; k < 3; ++k) {
+        int pr = k;
+        for (int i = k + 1; i < 3; ++i)
+            if (fabs(m[i][k]) > fabs(m[pr][k])) pr = i;
+        if (fabs(m[pr][k]) <= dm(1e-14, scale)) return false;
+        if (pr != k)
+            for (int j = 0; j < 6; ++j) { const double t = m[k][j]; m[k][j] = m[pr][j]; m[pr][j] = t; }
+        const double inv = __ddiv_rn(1.0, m[k][k]);
+        for (int j = 0; j < 6; ++j) m[k][j] = dm(m[k][j], inv);
+        for (int i = 0; i < 3; ++i) {
+            if (i == k || m[i][k] == 0.0) continue;
+            const double f = m[i][k];
+            for (int j = 0; j < 6; ++j) m[i][j] = ds(m[i][j], dm(f, m[k][j]));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) a[i * 3 + j] = m[i][3 + j];
+    return true;
+}
+// pivot inversion with the reference's regularisation of singular blocks (engine/src/bsr.cpp:204-212);
+// returns 1 when the block had to be regularised
+__device__ int invert_pivot3(double* d) {
+    double tmp[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) tmp[e] = d[e];
+    if (invert3(d)) return 0;
+    double sc = 0;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) sc = fmax(sc, fabs(tmp[e]));
+    if (!(sc > 0) || !isfinite(sc)) sc = 1.0;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) d[e] = tmp[e];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const double de = d[e * 4];
+        d[e * 4] = da(de, da(dm(de >= 0 ? 1e-8 : -1e-8, sc), de == 0 ? dm(sc, 1e-8) : 0.0));
+    }
+    if (!invert3(d)) {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) d[e] = 0;
+        const double inv = __ddiv_rn(1.0, sc);
+        d[0] = inv; d[4] = inv; d[8] = inv;
+    }
+    return 1;
+}
+
+__device__ __forceinline__ void load9(const double* p, double* a) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) a[e] = p[e];
+}
+__device__ __forceinline__ void store9(double* p, const double* a) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) p[e] = a[e];
+}
+__device__ __forceinline__ void load9_ro(const double* p, double* a) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) a[e] = __ldg(p + e);
+}
+
+// ------------------------------------------------------------------ BILU0 factorisation (sync-free, level order)
+// engine/src/bsr.cpp:183-215 row by row; rows of a system claimed in forward level order.
+__global__ void __launch_bounds__(kSweepThreads) k_factor_f64(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                             const int* __restrict__ diag, const int* __restrict__ ford,
+                                                             const int* __restrict__ elimPtr, const int* __restrict__ elimT,
+                                                             const int* __restrict__ elimQ, double* lu, int* flagL, int epoch,
+                                                             unsigned* ctr, int* nreg, int* err) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr);
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int i = __ldg(ford + idx);
+            const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+            for (int p = r0; p < d; ++p) {
+                const int k = __ldg(col + p);
+                wait_flag(flagL + k, epoch, err);
+                double a[9], u[9], L[9];
+                load9(lu + size_t(p) * 9, a);
+                load9(lu + size_t(__ldg(diag + k)) * 9, u);
+                gemm3(a, u, L);                                   // L_ik = A_ik U_kk^-1
+                store9(lu + size_t(p) * 9, L);
+                for (int e = __ldg(elimPtr + p); e < __ldg(elimPtr + p + 1); ++e) {
+                    const int t = __ldg(elimT + e), q = __ldg(elimQ + e);
+                    double U[9], Cb[9];
+                    load9(lu + size_t(q) * 9, U);
+                    load9(lu + size_t(t) * 9, Cb);
+                    gemm3_sub(L, U, Cb);                          // A_ij -= L_ik U_kj
+                    store9(lu + size_t(t) * 9, Cb);
+                }
+            }
+            double D[9];
+            load9(lu + size_t(d) * 9, D);
+            if (invert_pivot3(D)) atomicAdd(nreg, 1);
+            store9(lu + size_t(d) * 9, D);
+            __threadfence();
+            st_release(flagL + i, epoch);
+        }
+    }
+}
+
+// C45 lean factorisation (engine/src/bsr.cpp:219-263): the row is eliminated in double (work) against the float
+// factors of earlier rows, the pivot inverted in double, and the row stored rounded to float.
+__global__ void __launch_bounds__(kSweepThreads) k_factor_lean(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                              const int* __restrict__ diag, const int* __restrict__ ford,
+                                                              const int* __restrict__ elimPtr, const int* __restrict__ elimT,
+                                                              const int* __restrict__ elimQ, const double* __restrict__ val,
+                                                              float* F, double* work, int* flagL, int epoch, unsigned* ctr,
+                                                              int* nreg, int* err) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr);
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int i = __ldg(ford + idx);
+            const int r0 = __ldg(rowPtr + i), r1 = __ldg(rowPtr + i + 1), d = __ldg(diag + i);
+            for (int p = r0; p < r1; ++p)
+                for (int e = 0; e < 9; ++e) work[size_t(p) * 9 + e] = double(float(__ldg(val + size_t(p) * 9 + e)));
+            for (int p = r0; p < d; ++p) {
+                const int k = __ldg(col + p);
+                wait_flag(flagL + k, epoch, err);
+                double a[9], u[9], L[9];
+                load9(work + size_t(p) * 9, a);
+                const float* fk = F + size_t(__ldg(diag + k)) * 9;
+                for (int e = 0; e < 9; ++e) u[e] = double(fk[e]);
+                gemm3(a, u, L);
+                store9(work + size_t(p) * 9, L);
+                for (int e = __ldg(elimPtr + p); e < __ldg(elimPtr + p + 1); ++e) {
+                    const int t = __ldg(elimT + e), q = __ldg(elimQ + e);
+                    double U[9], Cb[9];
+                    const float* fq = F + size_t(q) * 9;
+                    for (int j = 0; j < 9; ++j) U[j] = double(fq[j]);
+                    load9(work + size_t(t) * 9, Cb);
+                    gemm3_sub(L, U, Cb);
+                    store9(work + size_t(t) * 9, Cb);
+                }
+            }
+            double D[9];
+            load9(work + size_t(d) * 9, D);
+            if (invert_pivot3(D)) atomicAdd(nreg, 1);
+            store9(work + size_t(d) * 9, D);
+            for (int p = r0; p < r1; ++p)
+                for (int e = 0; e < 9; ++e) F[size_t(p) * 9 + e] = float(work[size_t(p) * 9 + e]);
+            __threadfence();
+            st_release(flagL + i, epoch);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ sweeps
+// Input modes of the forward sweep (fusions of the BiCGSTAB vector updates, engine/src/linsolve.cpp:172-186):
+enum { IN_PLAIN = 0, IN_PUPDATE = 1, IN_SUPDATE = 2 };
+
+__device__ __forceinline__ bool sys_running(const KScal* ks, const int* rowSys, int i) {
+    return ks == nullptr || ks[__ldg(rowSys + i)].status == ST_RUNNING;
+}
+
+// y_i = in_i - sum_{k<i} L_ik y_k   (engine/src/bsr.cpp:568-575)
+// IN_PUPDATE: in = p = r + beta (p - omega v) (p stored); IN_SUPDATE: in = s = r - alpha v (s stored in pv)
+template <int MODE>
+__global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                          const int* __restrict__ diag, const int* __restrict__ ford,
+                                                          const double* __restrict__ lu, const double* r, double* pv,
+                                                          const double* v, double* y, const int* __restrict__ rowSys,
+                                                          const KScal* ks, int* flagF, int* flagB, unsigned* ctr, int* err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1] = 0u;   // backward claim counter for the next sweep
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr);
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int i = __ldg(ford + idx);
+            const bool run = sys_running(ks, rowSys, i);
+            double yi[3];
+            if (MODE == IN_PUPDATE) {
+                const KScal& K = ks[__ldg(rowSys + i)];
+                const double beta = K.beta, omega = K.omega;
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const size_t q = size_t(i) * 3 + e;
+                    double pe = pv[q];
+                    if (run) { pe = da(r[q], dm(beta, ds(pe, dm(omega, v[q])))); pv[q] = pe; }
+                    yi[e] = pe;
+                }
+            } else if (MODE == IN_SUPDATE) {
+                const KScal& K = ks[__ldg(rowSys + i)];
+                const double alpha = K.alpha;
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const size_t q = size_t(i) * 3 + e;
+                    const double se = ds(r[q], dm(alpha, v[q]));
+                    if (run) pv[q] = se;
+                    yi[e] = se;
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 3; ++e) yi[e] = r[size_t(i) * 3 + e];
+            }
+            if (run) {
+                const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+                for (int p = r0; p < d; ++p) {
+                    const int k = __ldg(col + p);
+                    wait_flag(flagF + k, 1, err);
+                    double a[9], yk[3];
+                    load9_ro(lu + size_t(p) * 9, a);
+                    yk[0] = y[size_t(k) * 3 + 0]; yk[1] = y[size_t(k) * 3 + 1]; yk[2] = y[size_t(k) * 3 + 2];
+                    yi[0] = ds(yi[0], dot3(a, yk));
+                    yi[1] = ds(yi[1], dot3(a + 3, yk));
+                    yi[2] = ds(yi[2], dot3(a + 6, yk));
+                }
+            }
+            y[size_t(i) * 3 + 0] = yi[0]; y[size_t(i) * 3 + 1] = yi[1]; y[size_t(i) * 3 + 2] = yi[2];
+            flagB[i] = 0;
+            __threadfence();
+            st_release(flagF + i, 1);
+        }
+    }
+}
+
+// z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j), in place   (engine/src/bsr.cpp:577-587)
+__global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                          const int* __restrict__ diag, const int* __restrict__ bord,
+                                                          const double* __restrict__ lu, double* y, const int* __restrict__ rowSys,
+                                                          const KScal* ks, int* flagF, int* flagB, unsigned* ctr, int* err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[0] = 0u;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr + 1);
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int i = __ldg(bord + idx);
+            if (sys_running(ks, rowSys, i)) {
+                double yi[3] = {y[size_t(i) * 3 + 0], y[size_t(i) * 3 + 1], y[size_t(i) * 3 + 2]};
+                const int d = __ldg(diag + i), r1 = __ldg(rowPtr + i + 1);
+                for (int p = d + 1; p < r1; ++p) {
+                    const int j = __ldg(col + p);
+                    wait_flag(flagB + j, 1, err);
+                    double a[9], zj[3];
+                    load9_ro(lu + size_t(p) * 9, a);
+                    zj[0] = y[size_t(j) * 3 + 0]; zj[1] = y[size_t(j) * 3 + 1]; zj[2] = y[size_t(j) * 3 + 2];
+                    yi[0] = ds(yi[0], dot3(a, zj));
+                    yi[1] = ds(yi[1], dot3(a + 3, zj));
+                    yi[2] = ds(yi[2], dot3(a + 6, zj));
+                }
+                double D[9];
+                load9_ro(lu + size_t(d) * 9, D);
+                y[size_t(i) * 3 + 0] = dot3(D, yi);
+                y[size_t(i) * 3 + 1] = dot3(D + 3, yi);
+                y[size_t(i) * 3 + 2] = dot3(D + 6, yi);
+            }
+            flagF[i] = 0;
+            __threadfence();
+            st_release(flagB + i, 1);
+        }
+    }
+}
+
+// FP32 factors, FP32 vectors and accumulation (BILU0f, engine/src/bsr.cpp:1100-1121); y32 holds the float
+// intermediate, the result is written to z in double.
+template <int MODE>
+__global__ void __launch_bounds__(kSweepThreads) k_fwd_f32(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                          const int* __restrict__ diag, const int* __restrict__ ford,
+                                                          const float* __restrict__ lu, const double* r, double* pv,
+                                                          const double* v, float* y, const int* __restrict__ rowSys,
+                                                          const KScal* ks, int* flagF, int* flagB, unsigned* ctr, int* err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1] = 0u;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr);
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int i = __ldg(ford + idx);
+            const bool run = sys_running(ks, rowSys, i);
+            float yi[3];
+            if (MODE == IN_PUPDATE) {
+                const KScal& K = ks[__ldg(rowSys + i)];
+                const double beta = K.beta, omega = K.omega;
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const size_t q = size_t(i) * 3 + e;
+                    double pe = pv[q];
+                    if (run) { pe = da(r[q], dm(beta, ds(pe, dm(omega, v[q])))); pv[q] = pe; }
+                    yi[e] = float(pe);
+                }
+            } else if (MODE == IN_SUPDATE) {
+                const KScal& K = ks[__ldg(rowSys + i)];
+                const double alpha = K.alpha;
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const size_t q = size_t(i) * 3 + e;
+                    const double se = ds(r[q], dm(alpha, v[q]));
+                    if (run) pv[q] = se;
+                    yi[e] = float(se);
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 3; ++e) yi[e] = float(r[size_t(i) * 3 + e]);
+            }
+            if (run) {
+                const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+                for (int p = r0; p < d; ++p) {
+                    const int k = __ldg(col + p);
+                    wait_flag(flagF + k, 1, err);
+                    const float* a = lu + size_t(p) * 9;
+                    const float y0 = y[size_t(k) * 3 + 0], y1 = y[size_t(k) * 3 + 1], y2 = y[size_t(k) * 3 + 2];
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) {
+                        float s = 0.f;
+                        s += __ldg(a + e * 3 + 0) * y0;
+                        s += __ldg(a + e * 3 + 1) * y1;
+                        s += __ldg(a + e * 3 + 2) * y2;
+                        yi[e] -= s;
+                    }
+                }
+            }
+            y[size_t(i) * 3 + 0] = yi[0]; y[size_t(i) * 3 + 1] = yi[1]; y[size_t(i) * 3 + 2] = yi[2];
+            flagB[i] = 0;
+            __threadfence();
+            st_release(flagF + i, 1);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                          const int* __restrict__ diag, const int* __restrict__ bord,
+                                                          const float* __restrict__ lu, float* y, double* z,
+                                                          const int* __restrict__ rowSys, const KScal* ks, int* flagF, int* flagB,
+                                                          unsigned* ctr, int* err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[0] = 0u;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr + 1);
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int i = __ldg(bord + idx);
+            if (sys_running(ks, rowSys, i)) {
+                float yi[3] = {y[size_t(i) * 3 + 0], y[size_t(i) * 3 + 1], y[size_t(i) * 3 + 2]};
+                const int d = __ldg(diag + i), r1 = __ldg(rowPtr + i + 1);
+                for (int p = d + 1; p < r1; ++p) {
+                    const int j = __ldg(col + p);
+                    wait_flag(flagB + j, 1, err);
+                    const float* a = lu + size_t(p) * 9;
+                    const float z0 = y[size_t(j) * 3 + 0], z1 = y[size_t(j) * 3 + 1], z2 = y[size_t(j) * 3 + 2];
+#pragma unroll
+                    for (int e = 0; e < 3; ++e) {
+                        float s = 0.f;
+                        s += __ldg(a + e * 3 + 0) * z0;
+                        s += __ldg(a + e * 3 + 1) * z1;
+                        s += __ldg(a + e * 3 + 2) * z2;
+                        yi[e] -= s;
+                    }
+                }
+                const float* D = lu + size_t(d) * 9;
+                float t[3];
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    float s = 0.f;
+                    s += __ldg(D + e * 3 + 0) * yi[0];
+                    s += __ldg(D + e * 3 + 1) * yi[1];
+                    s += __ldg(D + e * 3 + 2) * yi[2];
+                    t[e] = s;
+                }
+                y[size_t(i) * 3 + 0] = t[0]; y[size_t(i) * 3 + 1] = t[1]; y[size_t(i) * 3 + 2] = t[2];
+                z[size_t(i) * 3 + 0] = double(t[0]); z[size_t(i) * 3 + 1] = double(t[1]); z[size_t(i) * 3 + 2] = double(t[2]);
+            }
+            flagF[i] = 0;
+            __threadfence();
+            st_release(flagB + i, 1);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ tile kernels with fused reductions
+// Block reduction of up to MAX_DOTS values; result valid in thread 0.
+template <int ND>
+__device__ __forceinline__ void block_reduce(double (&v)[MAX_DOTS], double* sh /* [ND][kTileThreads/32] */) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+        double x = v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[j * 32 + w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int j = 0; j < ND; ++j) {
+            double s = 0;
+            for (int q = 0; q < nw; ++q) s += sh[j * 32 + q];
+            v[j] = s;
+        }
+    }
+}
+
+// Last-tile-done: the block that completes the last tile reduces the per-tile partials of every system in a fixed
+// order into sysdot[s*MAX_DOTS + j] and returns true (in every thread of that block).
+template <int ND>
+__device__ bool last_tile_reduce(int ntiles, int nsys, const int* __restrict__ sysTile0, const double* part, unsigned* done,
+                                 double* sysdot, double* sh) {
+    __shared__ int amLast;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned ticket = atomicAdd(done, 1u);
+        amLast = (ticket == unsigned(ntiles) - 1u);
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (nsys <= 4) {
+        for (int s = 0; s < nsys; ++s) {
+            double v[MAX_DOTS] = {0, 0, 0, 0};
+            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
+            for (int t = t0 + int(threadIdx.x); t < t1; t += blockDim.x)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
+            block_reduce<ND>(v, sh);
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) sysdot[size_t(s) * MAX_DOTS + j] = v[j];
+            __syncthreads();
+        }
+    } else {
+        for (int s = w; s < nsys; s += nw) {
+            double v[MAX_DOTS] = {0, 0, 0, 0};
+            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
+            for (int t = t0 + lane; t < t1; t += 32)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+                double x = v[j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                if (lane == 0) sysdot[size_t(s) * MAX_DOTS + j] = x;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *done = 0u;
+    __threadfence();
+    return true;
+}
+
+// SpMV epilogues / fused dot products
+enum { SP_PLAIN = 0, SP_RV = 1, SP_OMEGA = 2, SP_TRUERES = 3 };
+
+// y = A x on one tile (3 threads per block row), reference order per block (engine/src/bsr.cpp:109-117).
+// SP_RV: partial <rh, y>; then alpha = rho / <rh, v>. SP_OMEGA: partials <t,t>, <t,s>, <s,s>; then omega or the
+// early exit on ||s||. SP_TRUERES: y = b - A x, partials <y,y>, <b,b>, result sqrt ratio into out[s].
+template <int MODE>
+__global__ void __launch_bounds__(kTileThreads) k_spmv_tile(int ntiles, int nsys, const int* __restrict__ tileRow0,
+                                                           const int* __restrict__ tileSys, const int* __restrict__ sysTile0,
+                                                           const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                           const double* __restrict__ val, const double* __restrict__ x, double* y,
+                                                           const double* __restrict__ a1, const double* __restrict__ a2, KScal* ks,
+                                                           double* part, unsigned* done, double* sysdot, int* active, double* out) {
+    __shared__ double sh[MAX_DOTS * 32];
+    const int tile = blockIdx.x;
+    const int s = __ldg(tileSys + tile);
+    const bool run = (MODE == SP_PLAIN || MODE == SP_TRUERES) || ks[s].status == ST_RUNNING;
+    double acc[MAX_DOTS] = {0, 0, 0, 0};
+    if (run) {
+        const int r0 = __ldg(tileRow0 + tile), r1 = __ldg(tileRow0 + tile + 1);
+        const int e = threadIdx.x % 3;
+        for (int row = r0 + int(threadIdx.x) / 3; row < r1; row += kTileThreads / 3) {
+            double yv = 0;
+            const int p1 = __ldg(rowPtr + row + 1);
+            for (int p = __ldg(rowPtr + row); p < p1; ++p) {
+                const double* a = val + size_t(p) * 9 + e * 3;
+                const double* xc = x + size_t(__ldg(col + p)) * 3;
+                const double sblk = da(da(dm(__ldg(a), __ldg(xc)), dm(__ldg(a + 1), __ldg(xc + 1))), dm(__ldg(a + 2), __ldg(xc + 2)));
+                yv = da(yv, sblk);
+            }
+            const size_t q = size_t(row) * 3 + e;
+            if (MODE == SP_TRUERES) {
+                const double bq = __ldg(a1 + q);
+                const double rq = ds(bq, yv);
+                if (y) y[q] = rq;
+                acc[0] += rq * rq;
+                acc[1] += bq * bq;
+            } else {
+                y[q] = yv;
+                if (MODE == SP_RV) acc[0] += __ldg(a1 + q) * yv;
+                if (MODE == SP_OMEGA) {
+                    const double sq = __ldg(a1 + q);
+                    acc[0] += yv * yv;
+                    acc[1] += yv * sq;
+                    acc[2] += sq * sq;
+                }
+            }
+        }
+    }
+    if (MODE == SP_PLAIN) return;
+    constexpr int ND = MODE == SP_RV ? 1 : (MODE == SP_OMEGA ? 3 : 2);
+    block_reduce<ND>(acc, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) part[size_t(tile) * MAX_DOTS + j] = acc[j];
+    if (!last_tile_reduce<ND>(ntiles, nsys, sysTile0, part, done, sysdot, sh)) return;
+    for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
+        const double* dd = sysdot + size_t(q) * MAX_DOTS;
+        if (MODE == SP_TRUERES) {
+            out[q] = dd[1] > 0 ? sqrt(dd[0]) / sqrt(dd[1]) : 0.0;
+            continue;
+        }
+        KScal& K = ks[q];
+        if (K.status != ST_RUNNING) continue;
+        if (MODE == SP_RV) {
+            const double rv = dd[0];
+            if (fabs(rv) < 1e-300 || !isfinite(rv)) {   // engine/src/linsolve.cpp:179
+                K.status = ST_BREAKDOWN;
+                atomicSub(active, 1);
+            } else {
+                K.alpha = K.rho / rv;
+            }
+        } else if (MODE == SP_OMEGA) {
+            const double tt = dd[0], ts = dd[1], ss = dd[2];
+            K.sn = sqrt(ss);
+            K.omega = tt > 0 ? ts / tt : 0.0;             // engine/src/linsolve.cpp:196
+        }
+    }
+}
+
+// BiCGSTAB initial state: x = 0, r = rh = b, p = v = 0; rho = <b,b>, alpha = omega = 1 (engine/src/linsolve.cpp:162-168)
+__global__ void __launch_bounds__(kTileThreads) k_bicg_init(int ntiles, int nsys, const int* __restrict__ tileRow0,
+                                                           const int* __restrict__ tileSys, const int* __restrict__ sysTile0,
+                                                           const double* __restrict__ b, double* x, double* r, double* rh, double* p,
+                                                           double* v, KScal* ks, double tol, int maxit, double* part,
+                                                           unsigned* done, double* sysdot, int* active) {
+    __shared__ double sh[MAX_DOTS * 32];
+    const int tile = blockIdx.x;
+    const size_t q0 = size_t(__ldg(tileRow0 + tile)) * 3, q1 = size_t(__ldg(tileRow0 + tile + 1)) * 3;
+    double acc[MAX_DOTS] = {0, 0, 0, 0};
+    for (size_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+        const double bq = __ldg(b + q);
+        x[q] = 0; r[q] = bq; rh[q] = bq; p[q] = 0; v[q] = 0;
+        acc[0] += bq * bq;
+    }
+    block_reduce<1>(acc, sh);
+    if (threadIdx.x == 0) part[size_t(tile) * MAX_DOTS] = acc[0];
+    if (!last_tile_reduce<1>(ntiles, nsys, sysTile0, part, done, sysdot, sh)) return;
+    if (threadIdx.x == 0) *active = 0;
+    __syncthreads();
+    int nact = 0;
+    for (int s = threadIdx.x; s < nsys; s += blockDim.x) {
+        KScal& K = ks[s];
+        const double bb = sysdot[size_t(s) * MAX_DOTS];
+        K.bn = sqrt(bb);
+        K.tol = tol; K.maxit = maxit; K.its = 0; K.relres = 0; K.sn = 0;
+        K.alpha = 1; K.omega = 1; K.rho = bb; K.beta = bb;   // rhoN of iteration 1 = <rh, r> = <b, b>
+        if (K.bn == 0) { K.status = ST_CONV; }                // engine/src/linsolve.cpp:165
+        else if (fabs(bb) < 1e-300 || !isfinite(bb)) { K.status = ST_BREAKDOWN; }
+        else if (maxit < 1) { K.status = ST_MAXIT; }
+        else { K.status = ST_RUNNING; ++nact; }
+    }
+    if (nact) atomicAdd(active, nact);
+}
+
+// End of a BiCGSTAB iteration (engine/src/linsolve.cpp:183-213):
+//   ||s|| small: x += alpha ph and stop; else x += alpha ph + omega sh, r = s - omega t, then ||r||, <rh, r>.
+__global__ void __launch_bounds__(kTileThreads) k_bicg_update(int ntiles, int nsys, const int* __restrict__ tileRow0,
+                                                             const int* __restrict__ tileSys, const int* __restrict__ sysTile0,
+                                                             double* x, double* r, const double* __restrict__ rh,
+                                                             const double* __restrict__ s, const double* __restrict__ t,
+                                                             const double* __restrict__ ph, const double* __restrict__ sh_,
+                                                             KScal* ks, double* part, unsigned* done, double* sysdot, int* active) {
+    __shared__ double sh[MAX_DOTS * 32];
+    const int tile = blockIdx.x;
+    const int sy = __ldg(tileSys + tile);
+    KScal K = ks[sy];
+    double acc[MAX_DOTS] = {0, 0, 0, 0};
+    if (K.status == ST_RUNNING) {
+        const size_t q0 = size_t(__ldg(tileRow0 + tile)) * 3, q1 = size_t(__ldg(tileRow0 + tile + 1)) * 3;
+        const bool sconv = K.sn / K.bn < K.tol;
+        for (size_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+            if (sconv) {
+                x[q] = da(x[q], dm(K.alpha, __ldg(ph + q)));
+            } else {
+                x[q] = da(x[q], da(dm(K.alpha, __ldg(ph + q)), dm(K.omega, __ldg(sh_ + q))));
+                const double rq = ds(__ldg(s + q), dm(K.omega, __ldg(t + q)));
+                r[q] = rq;
+                acc[0] += rq * rq;
+                acc[1] += __ldg(rh + q) * rq;
+            }
+        }
+    }
+    block_reduce<2>(acc, sh);
+    if (threadIdx.x == 0) { part[size_t(tile) * MAX_DOTS] = acc[0]; part[size_t(tile) * MAX_DOTS + 1] = acc[1]; }
+    if (!last_tile_reduce<2>(ntiles, nsys, sysTile0, part, done, sysdot, sh)) return;
+    for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
+        KScal& k = ks[q];
+        if (k.status != ST_RUNNING) continue;
+        const int it = k.its + 1;
+        k.its = it;
+        if (k.sn / k.bn < k.tol) {                              // engine/src/linsolve.cpp:187-191
+            k.relres = k.sn / k.bn;
+            k.status = ST_CONV;
+            atomicSub(active, 1);
+            continue;
+        }
+        const double rn = sqrt(sysdot[size_t(q) * MAX_DOTS]);
+        const double rhoN = sysdot[size_t(q) * MAX_DOTS + 1];
+        k.relres = rn / k.bn;
+        if (rn / k.bn < k.tol) { k.status = ST_CONV; atomicSub(active, 1); continue; }
+        if (k.omega == 0 || !isfinite(rn)) { k.status = ST_BREAKDOWN; atomicSub(active, 1); continue; }
+        if (fabs(rhoN) < 1e-300) { k.status = ST_BREAKDOWN; atomicSub(active, 1); continue; }   // next iteration's test
+        if (it >= k.maxit) { k.status = ST_MAXIT; atomicSub(active, 1); continue; }
+        k.beta = (rhoN / k.rho) * (k.alpha / k.omega);
+        k.rho = rhoN;
+    }
+}
+
+// ------------------------------------------------------------------ block Jacobi
+__global__ void k_bj_setup(int n, const int* __restrict__ diag, const double* __restrict__ val, double* dinv, int* nreg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double D[9];
+    load9_ro(val + size_t(__ldg(diag + i)) * 9, D);
+    double B[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) B[e] = D[e];
+    if (!invert3(B)) {   // DeviceCprAmg fallback: 1 / max(1e-30, |D_ee|) (engine/src/bsr.cpp:1305)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) B[e] = 0;
+        for (int e = 0; e < 3; ++e) B[e * 4] = 1.0 / fmax(1e-30, fabs(D[e * 4]));
+        atomicAdd(nreg, 1);
+    }
+    store9(dinv + size_t(i) * 9, B);
+}
+
+template <int MODE>
+__global__ void k_bj_apply(int n, const double* __restrict__ dinv, const double* r, double* pv, const double* v, double* z,
+                           const int* __restrict__ rowSys, const KScal* ks) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool run = sys_running(ks, rowSys, i);
+    if (!run) return;
+    double yi[3];
+    if (MODE == IN_PUPDATE) {
+        const KScal& K = ks[__ldg(rowSys + i)];
+        for (int e = 0; e < 3; ++e) {
+            const size_t q = size_t(i) * 3 + e;
+            const double pe = da(r[q], dm(K.beta, ds(pv[q], dm(K.omega, v[q]))));
+            pv[q] = pe; yi[e] = pe;
+        }
+    } else if (MODE == IN_SUPDATE) {
+        const KScal& K = ks[__ldg(rowSys + i)];
+        for (int e = 0; e < 3; ++e) {
+            const size_t q = size_t(i) * 3 + e;
+            const double se = ds(r[q], dm(K.alpha, v[q]));
+            pv[q] = se; yi[e] = se;
+        }
+    } else {
+        for (int e = 0; e < 3; ++e) yi[e] = r[size_t(i) * 3 + e];
+    }
+    double D[9];
+    load9_ro(dinv + size_t(i) * 9, D);
+    z[size_t(i) * 3 + 0] = dot3(D, yi);
+    z[size_t(i) * 3 + 1] = dot3(D + 3, yi);
+    z[size_t(i) * 3 + 2] = dot3(D + 6, yi);
+}
+
+int g_sm_count = 0;
+int sweep_grid(int n) {
+    const int sms = device_sm_count();
+    // enough warps for several levels in flight, at most 8 blocks of 4 warps per SM
+    const int warps = (n + 31) / 32;
+    int blocks = (warps + 3) / 4;
+    const int maxb = sms * 8;
+    if (blocks > maxb) blocks = maxb;
+    if (blocks < 1) blocks = 1;
+    return blocks;
+}
+
+}  // namespace
+
+int device_sm_count() {
+    if (g_sm_count == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sm_count <= 0) g_sm_count = 1;
+    }
+    return g_sm_count;
+}
+
+void launch_factor_f64(const DevPlan& P, const double* val, double* lu, SweepState& S, int epoch, int* nreg, int* err,
+                       cudaStream_t st) {
+    cudaMemcpyAsync(lu, val, size_t(P.nnzb) * 9 * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(S.ctr + 2, 0, sizeof(unsigned), st);
+    k_factor_f64<<<sweep_grid(P.n), kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, P.elimPtr, P.elimT, P.elimQ, lu,
+                                                           S.flagL, epoch, S.ctr + 2, nreg, err);
+}
+
+void launch_factor_lean(const DevPlan& P, const double* val, float* luf, double* work, SweepState& S, int epoch, int* nreg,
+                        int* err, cudaStream_t st) {
+    cudaMemsetAsync(S.ctr + 2, 0, sizeof(unsigned), st);
+    k_factor_lean<<<sweep_grid(P.n), kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, P.elimPtr, P.elimT, P.elimQ,
+                                                            val, luf, work, S.flagL, epoch, S.ctr + 2, nreg, err);
+}
+
+void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, double* z, SweepState& S, int* err,
+                          cudaStream_t st) {
+    const int g = sweep_grid(P.n);
+    k_fwd_f64<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, lu, r, nullptr, nullptr, z, P.rowSys,
+                                                     nullptr, S.flagF, S.flagB, S.ctr, err);
+    k_bwd_f64<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, lu, z, P.rowSys, nullptr, S.flagF, S.flagB, S.ctr,
+                                          err);
+}
+
+void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S, int* err,
+                          cudaStream_t st) {
+    const int g = sweep_grid(P.n);
+    k_fwd_f32<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, luf, r, nullptr, nullptr, y32, P.rowSys,
+                                                     nullptr, S.flagF, S.flagB, S.ctr, err);
+    k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, luf, y32, z, P.rowSys, nullptr, S.flagF, S.flagB,
+                                          S.ctr, err);
+}
+
+void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st) {
+    k_spmv_tile<SP_PLAIN><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col,
+                                                             val, x, y, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                             nullptr, nullptr);
+}
+
+void launch_block_jacobi_setup(const DevPlan& P, const double* val, double* dinv, int* nreg, cudaStream_t st) {
+    k_bj_setup<<<(P.n + 127) / 128, 128, 0, st>>>(P.n, P.diag, val, dinv, nreg);
+}
+void launch_block_jacobi_apply(const DevPlan& P, const double* dinv, const double* r, double* z, cudaStream_t st) {
+    k_bj_apply<IN_PLAIN><<<(P.n + 127) / 128, 128, 0, st>>>(P.n, dinv, r, nullptr, nullptr, z, P.rowSys, nullptr);
+}
+
+void launch_bicg_init(const DevPlan& P, const double* b, BicgVecs& V, KScal* ks, ReduceState& R, double tol, int maxit,
+                      int* active, cudaStream_t st) {
+    k_bicg_init<<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, b, V.x, V.r, V.rh, V.p, V.v,
+                                                   ks, tol, maxit, R.part, R.done, R.sysdot, active);
+}
+
+// one iteration: (a) p-update fused into M p, (c) v = A ph + <rh,v>, (d) s-update fused into M s,
+// (f) t = A sh + <t,t>, <t,s>, <s,s>, (g) x / r update + ||r||, <rh,r>
+void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M, BicgVecs& V, KScal* ks, ReduceState& R,
+                           SweepState& S, int* active, int* err, cudaStream_t st) {
+    const int g = sweep_grid(P.n);
+    auto prec = [&](bool pupd, double* out) {
+        if (M.kind == 0) {
+            if (pupd)
+                k_fwd_f64<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.p, V.v, out,
+                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            else
+                k_fwd_f64<IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.s, V.v, out,
+                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            k_bwd_f64<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.lu, out, P.rowSys, ks, S.flagF, S.flagB,
+                                                  S.ctr, err);
+        } else if (M.kind == 1) {
+            if (pupd)
+                k_fwd_f32<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.p, V.v, V.y32,
+                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            else
+                k_fwd_f32<IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.s, V.v, V.y32,
+                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, V.y32, out, P.rowSys, ks, S.flagF,
+                                                  S.flagB, S.ctr, err);
+        } else {
+            const int gb = (P.n + 127) / 128;
+            if (pupd)
+                k_bj_apply<IN_PUPDATE><<<gb, 128, 0, st>>>(P.n, M.dinv, V.r, V.p, V.v, out, P.rowSys, ks);
+            else
+                k_bj_apply<IN_SUPDATE><<<gb, 128, 0, st>>>(P.n, M.dinv, V.r, V.s, V.v, out, P.rowSys, ks);
+        }
+    };
+    prec(true, V.ph);
+    k_spmv_tile<SP_RV><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col, val,
+                                                          V.ph, V.v, V.rh, nullptr, ks, R.part, R.done, R.sysdot, active, nullptr);
+    prec(false, V.sh);
+    k_spmv_tile<SP_OMEGA><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col,
+                                                             val, V.sh, V.t, V.s, nullptr, ks, R.part, R.done, R.sysdot, active,
+                                                             nullptr);
+    k_bicg_update<<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, V.x, V.r, V.rh, V.s, V.t,
+                                                     V.ph, V.sh, ks, R.part, R.done, R.sysdot, active);
+}
+
+void launch_true_residual(const DevPlan& P, const double* val, const double* b, const double* x, double* tmp, ReduceState& R,
+                          double* out, cudaStream_t st) {
+    k_spmv_tile<SP_TRUERES><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col,
+                                                               val, x, tmp, b, nullptr, nullptr, R.part, R.done, R.sysdot, nullptr,
+                                                               out);
+}
+
+}  // namespace rsg

@@ -1,0 +1,251 @@
+// Host-side, pattern-only planning of the device solve: level schedules (claim orders of the sync-free sweeps),
+// BILU0 elimination lists, tiles of the tile kernels, and the well Schur complement.
+#include "rsg_impl.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace rsg {
+
+namespace {
+// counting sort of rows by level, ascending row index inside a level (engine/src/bsr.cpp:286-292)
+void order_by_level(const std::vector<int>& lev, int nl, std::vector<int>& ord) {
+    const int n = int(lev.size());
+    std::vector<int> start(size_t(nl) + 1, 0);
+    for (int i = 0; i < n; ++i) start[size_t(lev[size_t(i)]) + 1]++;
+    for (int l = 0; l < nl; ++l) start[size_t(l) + 1] += start[size_t(l)];
+    ord.assign(size_t(n), 0);
+    for (int i = 0; i < n; ++i) ord[size_t(start[size_t(lev[size_t(i)])]++)] = i;
+}
+}  // namespace
+
+bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
+                const std::vector<int>& col, std::string& err) {
+    const int n = int(rowPtr.size()) - 1;
+    if (n < 1) { err = "empty matrix (n < 1)"; return false; }
+    if (rowPtr[0] != 0) { err = "rowPtr[0] must be 0"; return false; }
+    for (int i = 0; i < n; ++i)
+        if (rowPtr[size_t(i) + 1] < rowPtr[size_t(i)]) { err = "rowPtr is not monotone"; return false; }
+    const int nnzb = rowPtr[size_t(n)];
+    if (int(col.size()) < nnzb) { err = "col shorter than rowPtr[n]"; return false; }
+    P = HostPlan{};
+    P.n = n; P.nnzb = nnzb; P.nsys = nsys;
+    P.rowPtr = rowPtr;
+    P.col.assign(col.begin(), col.begin() + nnzb);
+    P.sysRow0 = sysRow0;
+    P.rowSys.assign(size_t(n), 0);
+    for (int s = 0; s < nsys; ++s)
+        for (int i = sysRow0[size_t(s)]; i < sysRow0[size_t(s) + 1]; ++i) P.rowSys[size_t(i)] = s;
+    // validation: sorted columns, in range, inside the row's own system, diagonal present
+    P.diag.assign(size_t(n), -1);
+    for (int i = 0; i < n; ++i) {
+        const int s = P.rowSys[size_t(i)];
+        const int lo = sysRow0[size_t(s)], hi = sysRow0[size_t(s) + 1];
+        for (int p = rowPtr[size_t(i)]; p < rowPtr[size_t(i) + 1]; ++p) {
+            const int c = P.col[size_t(p)];
+            if (c < lo || c >= hi) { err = "column index out of range in block row " + std::to_string(i - lo); return false; }
+            if (p > rowPtr[size_t(i)] && c <= P.col[size_t(p) - 1]) {
+                err = "columns not strictly increasing in block row " + std::to_string(i - lo);
+                return false;
+            }
+            if (c == i) P.diag[size_t(i)] = p;
+        }
+        if (P.diag[size_t(i)] < 0) { err = "missing diagonal block in block row " + std::to_string(i - lo); return false; }
+    }
+    // forward levels (L dependencies) -> claim order
+    std::vector<int> lev(size_t(n), 0);
+    int nl = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int p = rowPtr[size_t(i)]; p < P.diag[size_t(i)]; ++p) l = std::max(l, lev[size_t(P.col[size_t(p)])] + 1);
+        lev[size_t(i)] = l;
+        nl = std::max(nl, l + 1);
+    }
+    P.nlevF = nl;
+    order_by_level(lev, nl, P.ford);
+    // structural symmetry: then the reversed forward order is a topological order of the U dependencies
+    P.symmetric = true;
+    for (int i = 0; i < n && P.symmetric; ++i)
+        for (int p = rowPtr[size_t(i)]; p < rowPtr[size_t(i) + 1]; ++p) {
+            const int j = P.col[size_t(p)];
+            const int* c0 = P.col.data() + rowPtr[size_t(j)];
+            const int* c1 = P.col.data() + rowPtr[size_t(j) + 1];
+            if (!std::binary_search(c0, c1, i)) { P.symmetric = false; break; }
+        }
+    if (P.symmetric) {
+        P.bord.assign(P.ford.rbegin(), P.ford.rend());
+        P.nlevB = nl;
+    } else {
+        std::vector<int> blev(size_t(n), 0);
+        int nb = 0;
+        for (int i = n - 1; i >= 0; --i) {
+            int l = 0;
+            for (int p = P.diag[size_t(i)] + 1; p < rowPtr[size_t(i) + 1]; ++p) l = std::max(l, blev[size_t(P.col[size_t(p)])] + 1);
+            blev[size_t(i)] = l;
+            nb = std::max(nb, l + 1);
+        }
+        P.nlevB = nb;
+        order_by_level(blev, nb, P.bord);
+    }
+    // BILU0 elimination lists in the reference's order: lower entries p ascending, U entries q of row k ascending,
+    // target = the block of row i in the same column (engine/src/bsr.cpp:193-201)
+    P.elimPtr.assign(size_t(nnzb) + 1, 0);
+    P.elimT.clear(); P.elimQ.clear();
+    std::vector<int> pos(size_t(n), -1);
+    for (int i = 0; i < n; ++i) {
+        const int r0 = rowPtr[size_t(i)], r1 = rowPtr[size_t(i) + 1];
+        for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = p;
+        for (int p = r0; p < r1; ++p) {
+            const int k = P.col[size_t(p)];
+            if (k < i)
+                for (int q = P.diag[size_t(k)] + 1; q < rowPtr[size_t(k) + 1]; ++q) {
+                    const int t = pos[size_t(P.col[size_t(q)])];
+                    if (t >= 0) { P.elimT.push_back(t); P.elimQ.push_back(q); }
+                }
+            P.elimPtr[size_t(p) + 1] = int(P.elimT.size());
+        }
+        for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = -1;
+    }
+    // tiles of TILE_ROWS block rows, never crossing a system boundary
+    P.tileRow0.clear(); P.tileSys.clear(); P.sysTile0.assign(size_t(nsys) + 1, 0);
+    for (int s = 0; s < nsys; ++s) {
+        P.sysTile0[size_t(s)] = int(P.tileSys.size());
+        for (int r = sysRow0[size_t(s)]; r < sysRow0[size_t(s) + 1]; r += TILE_ROWS) {
+            P.tileRow0.push_back(r);
+            P.tileSys.push_back(s);
+        }
+    }
+    P.sysTile0[size_t(nsys)] = int(P.tileSys.size());
+    P.tileRow0.push_back(n);
+    return true;
+}
+
+// ====================================================================== well Schur complement
+namespace {
+struct WellParts {
+    std::vector<double> dInv;
+    std::vector<int> wcPtr, wcCol;
+    std::vector<double> wcVal;
+    std::vector<int> cwPtr, cwWell;
+    std::vector<double> cwVal;
+};
+// well rows (diagonal + cell couplings) and the well columns of the cell rows (engine/src/bsr.cpp:737-757)
+bool well_parts(WellParts& W, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw, std::string& err) {
+    const int nc = na * nv;
+    W.dInv.assign(size_t(nw), 0.0);
+    W.wcPtr.assign(size_t(nw) + 1, 0);
+    for (int w = 0; w < nw; ++w) {
+        const int r = nc + w;
+        double d = 0, rowMax = 0;
+        for (int p = rowPtr[r]; p < rowPtr[r + 1]; ++p) {
+            const int c = col[p];
+            if (c == r) d = val[p];
+            else if (c < nc) { W.wcCol.push_back(c); W.wcVal.push_back(val[p]); rowMax = std::max(rowMax, std::fabs(val[p])); }
+            else if (val[p] != 0.0) { err = "well-well coupling in well row " + std::to_string(w) + " (not supported)"; return false; }
+        }
+        if (!(std::fabs(d) > 1e-12 * std::max(rowMax, 1e-300)) || !std::isfinite(d)) {
+            err = "well row " + std::to_string(w) + " has no usable BHP derivative";
+            return false;
+        }
+        W.dInv[size_t(w)] = 1.0 / d;
+        W.wcPtr[size_t(w) + 1] = int(W.wcCol.size());
+    }
+    W.cwPtr.assign(size_t(nc) + 1, 0);
+    for (int r = 0; r < nc; ++r) {
+        for (int p = rowPtr[r]; p < rowPtr[r + 1]; ++p)
+            if (col[p] >= nc && val[p] != 0.0) { W.cwWell.push_back(col[p] - nc); W.cwVal.push_back(val[p]); }
+        W.cwPtr[size_t(r) + 1] = int(W.cwWell.size());
+    }
+    return true;
+}
+}  // namespace
+
+int wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                     const double* b, int* nnzb, int* sRowPtr, int* sCol, double* sVal, double* bc, std::string& err) {
+    if (na < 1 || nv < 1 || nw < 0 || nrows != na * nv + nw) { err = "wellschur: nrows must equal na*nv + nw"; return -1; }
+    WellParts W;
+    if (!well_parts(W, rowPtr, col, val, na, nv, nw, err)) return -1;
+    const int nc = na * nv, b2 = nv * nv;
+    std::vector<std::vector<int>> wellCells(static_cast<size_t>(nw));
+    for (int w = 0; w < nw; ++w) {
+        auto& v = wellCells[size_t(w)];
+        for (int p = W.wcPtr[size_t(w)]; p < W.wcPtr[size_t(w) + 1]; ++p) v.push_back(W.wcCol[size_t(p)] / nv);
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    // block pattern: cell pattern + couplings through shared wells (engine/src/bsr.cpp:785-807)
+    std::vector<int> rp(size_t(na) + 1, 0), cols_all, mark(size_t(na), -1), cols, wl;
+    for (int i = 0; i < na; ++i) {
+        cols.clear(); wl.clear();
+        for (int e = 0; e < nv; ++e) {
+            const int r = i * nv + e;
+            for (int p = rowPtr[r]; p < rowPtr[r + 1]; ++p) {
+                const int c = col[p];
+                if (c < nc) { const int j = c / nv; if (mark[size_t(j)] != i) { mark[size_t(j)] = i; cols.push_back(j); } }
+            }
+            for (int p = W.cwPtr[size_t(r)]; p < W.cwPtr[size_t(r) + 1]; ++p) wl.push_back(W.cwWell[size_t(p)]);
+        }
+        if (mark[size_t(i)] != i) { mark[size_t(i)] = i; cols.push_back(i); }
+        std::sort(wl.begin(), wl.end());
+        wl.erase(std::unique(wl.begin(), wl.end()), wl.end());
+        for (int w : wl)
+            for (int j : wellCells[size_t(w)])
+                if (mark[size_t(j)] != i) { mark[size_t(j)] = i; cols.push_back(j); }
+        std::sort(cols.begin(), cols.end());
+        cols_all.insert(cols_all.end(), cols.begin(), cols.end());
+        rp[size_t(i) + 1] = int(cols_all.size());
+    }
+    *nnzb = int(cols_all.size());
+    if (!sRowPtr) return 0;
+    std::memcpy(sRowPtr, rp.data(), sizeof(int) * rp.size());
+    std::memcpy(sCol, cols_all.data(), sizeof(int) * cols_all.size());
+    std::memset(sVal, 0, sizeof(double) * cols_all.size() * size_t(b2));
+    // values S = Acc - Acw Dww^-1 Awc, in the reference's order of operations (engine/src/bsr.cpp:813-830)
+    std::vector<int> pos(size_t(na), -1);
+    for (int i = 0; i < na; ++i) {
+        for (int p = rp[size_t(i)]; p < rp[size_t(i) + 1]; ++p) pos[size_t(cols_all[size_t(p)])] = p;
+        for (int e = 0; e < nv; ++e) {
+            const int r = i * nv + e;
+            for (int p = rowPtr[r]; p < rowPtr[r + 1]; ++p) {
+                const int c = col[p];
+                if (c < nc) sVal[size_t(pos[size_t(c / nv)]) * b2 + size_t(e * nv + c % nv)] += val[p];
+            }
+            for (int p = W.cwPtr[size_t(r)]; p < W.cwPtr[size_t(r) + 1]; ++p) {
+                const int w = W.cwWell[size_t(p)];
+                const double f = W.cwVal[size_t(p)] * W.dInv[size_t(w)];
+                for (int q = W.wcPtr[size_t(w)]; q < W.wcPtr[size_t(w) + 1]; ++q) {
+                    const int c = W.wcCol[size_t(q)];
+                    sVal[size_t(pos[size_t(c / nv)]) * b2 + size_t(e * nv + c % nv)] -= f * W.wcVal[size_t(q)];
+                }
+            }
+        }
+    }
+    // bc = b_c - Acw Dww^-1 b_w (engine/src/bsr.cpp:973-980)
+    if (b && bc)
+        for (int r = 0; r < nc; ++r) {
+            double s = b[r];
+            for (int p = W.cwPtr[size_t(r)]; p < W.cwPtr[size_t(r) + 1]; ++p)
+                s -= W.cwVal[size_t(p)] * W.dInv[size_t(W.cwWell[size_t(p)])] * b[nc + W.cwWell[size_t(p)]];
+            bc[r] = s;
+        }
+    return 0;
+}
+
+int wellschur_recover(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
+                      const double* b, const double* xc, double* x, std::string& err) {
+    if (na < 1 || nv < 1 || nw < 0 || nrows != na * nv + nw) { err = "wellschur: nrows must equal na*nv + nw"; return -1; }
+    WellParts W;
+    if (!well_parts(W, rowPtr, col, val, na, nv, nw, err)) return -1;
+    const int nc = na * nv;
+    if (x != xc) std::memcpy(x, xc, sizeof(double) * size_t(nc));
+    for (int w = 0; w < nw; ++w) {
+        double s = b[nc + w];
+        for (int p = W.wcPtr[size_t(w)]; p < W.wcPtr[size_t(w) + 1]; ++p) s -= W.wcVal[size_t(p)] * xc[W.wcCol[size_t(p)]];
+        x[nc + w] = s * W.dInv[size_t(w)];
+    }
+    return 0;
+}
+
+}  // namespace rsg
