@@ -51,6 +51,8 @@ typedef struct rsg_options {
     int use_graphs;         /* 1: capture the iteration in a CUDA graph and replay it */
     int device;             /* CUDA device ordinal */
     size_t mem_budget;      /* bytes this handle may hold on the device (0 = no limit) */
+    int sweep;              /* BILU0 sweep scheduling: 0 auto, 1 one thread block per system (level barriers,
+                               shared-memory vector), 2 grid-wide sync-free (per-row flags) */
 } rsg_options;
 
 typedef struct rsg_stats {

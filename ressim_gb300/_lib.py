@@ -16,6 +16,7 @@ RSG_OK, RSG_EINVAL, RSG_ECUDA, RSG_ENOMEM, RSG_ESTATE, RSG_ETIMEOUT, RSG_EBREAKD
 PREC = {"bilu0": 0, "cpr": 1, "jacobi": 2}
 KRYLOV = {"bicgstab": 0, "gmres": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
+SWEEP = {"auto": 0, "cta": 1, "grid": 2}
 
 # every symbol include/rsg.h declares
 EXPORTS = [
@@ -28,7 +29,7 @@ EXPORTS = [
 class Options(C.Structure):
     _fields_ = [("precond", C.c_int), ("krylov", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("gmres_fallback", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
-                ("mem_budget", C.c_size_t)]
+                ("mem_budget", C.c_size_t), ("sweep", C.c_int)]
 
 
 class Stats(C.Structure):

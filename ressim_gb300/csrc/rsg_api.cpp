@@ -80,6 +80,9 @@ struct rsg_solver {
     float* luf = nullptr;
     double* work = nullptr;
     double* dinv = nullptr;
+    SplitFactors<double> s64;
+    SplitFactors<float> s32;
+    bool cta = false;
     // vectors
     BicgVecs V{};
     double *b = nullptr, *xout = nullptr, *tmp = nullptr;
@@ -112,6 +115,7 @@ void free_plan(rsg_solver* h) {
     h->pmem.release_all();
     h->dp = DevPlan{};
     h->val = nullptr; h->lu = nullptr; h->luf = nullptr; h->work = nullptr; h->dinv = nullptr;
+    h->s64 = SplitFactors<double>{}; h->s32 = SplitFactors<float>{}; h->cta = false;
     h->V = BicgVecs{};
     h->b = h->xout = h->tmp = nullptr;
     h->S = SweepState{};
@@ -140,8 +144,17 @@ int alloc_plan(rsg_solver* h) {
         (rc = upload(M, &D.ford, P.ford, st)) || (rc = upload(M, &D.bord, P.bord, st)) || (rc = upload(M, &D.elimPtr, P.elimPtr, st)) ||
         (rc = upload(M, &D.elimT, P.elimT, st)) || (rc = upload(M, &D.elimQ, P.elimQ, st)) || (rc = upload(M, &D.rowSys, P.rowSys, st)) ||
         (rc = upload(M, &D.tileRow0, P.tileRow0, st)) || (rc = upload(M, &D.tileSys, P.tileSys, st)) ||
-        (rc = upload(M, &D.sysTile0, P.sysTile0, st)) || (rc = upload(M, &D.sysRow0, P.sysRow0, st)))
+        (rc = upload(M, &D.sysTile0, P.sysTile0, st)) || (rc = upload(M, &D.sysRow0, P.sysRow0, st)) ||
+        (rc = upload(M, &D.lrow, P.lrow, st)) || (rc = upload(M, &D.lvlStart, P.lvlStart, st)) || (rc = upload(M, &D.sysLvl0, P.sysLvl0, st)) ||
+        (rc = upload(M, &D.Lptr, P.Lptr, st)) || (rc = upload(M, &D.Lcol, P.Lcol, st)) || (rc = upload(M, &D.Lsrc, P.Lsrc, st)) ||
+        (rc = upload(M, &D.Uptr, P.Uptr, st)) || (rc = upload(M, &D.Ucol, P.Ucol, st)) || (rc = upload(M, &D.Usrc, P.Usrc, st)) ||
+        (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
         return rc;
+    D.nL = int(P.Lcol.size());
+    D.nU = int(P.Ucol.size());
+    D.maxSysRows = P.maxSysRows;
+    h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
+    if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
     if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) || (rc = dalloc(M, &h->tmp, N)))
         return rc;
@@ -190,6 +203,13 @@ PrecDev prec_dev(rsg_solver* h) {
     else if (h->opt.precision == RSG_MIXED) { M.kind = 1; M.luf = h->luf; }
     else { M.kind = 0; M.lu = h->lu; }
     M.val = h->val;
+    if (M.kind != 2 && h->cta) {
+        M.smem = cta_sweep_smem(h->dp, M.kind == 1);
+        // FP32 sweeps need their vector in shared memory; FP64 may keep it in global memory
+        M.cta = M.kind == 0 || M.smem > 0;
+        M.s64 = h->s64;
+        M.s32 = h->s32;
+    }
     return M;
 }
 
@@ -256,8 +276,18 @@ int ensure_precond_storage(rsg_solver* h) {
         if (!h->luf && (rc = dalloc(h->pmem, &h->luf, E))) return rc;
         if (!h->work && (rc = dalloc(h->pmem, &h->work, E))) return rc;
         if (!h->V.y32 && (rc = dalloc(h->pmem, &h->V.y32, size_t(h->plan.n) * NB))) return rc;
+        if (h->cta && !h->s32.L) {
+            if ((rc = dalloc(h->pmem, &h->s32.L, size_t(h->dp.nL) * NB2)) || (rc = dalloc(h->pmem, &h->s32.U, size_t(h->dp.nU) * NB2)) ||
+                (rc = dalloc(h->pmem, &h->s32.D, size_t(h->dp.n) * NB2)))
+                return rc;
+        }
     } else {
         if (!h->lu && (rc = dalloc(h->pmem, &h->lu, E))) return rc;
+        if (h->cta && !h->s64.L) {
+            if ((rc = dalloc(h->pmem, &h->s64.L, size_t(h->dp.nL) * NB2)) || (rc = dalloc(h->pmem, &h->s64.U, size_t(h->dp.nU) * NB2)) ||
+                (rc = dalloc(h->pmem, &h->s64.D, size_t(h->dp.n) * NB2)))
+                return rc;
+        }
     }
     return RSG_OK;
 }
@@ -275,10 +305,13 @@ int do_setup(rsg_solver* h, const double* acc) {
         launch_block_jacobi_setup(h->dp, h->val, h->dinv, h->d_nreg, h->stream);
     } else {
         ++h->epoch;
-        if (h->opt.precision == RSG_MIXED)
+        if (h->opt.precision == RSG_MIXED) {
             launch_factor_lean(h->dp, h->val, h->luf, h->work, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
-        else
+            if (h->cta) { launch_pack_f32(h->dp, h->luf, h->s32, h->stream); h->launches += 1; }
+        } else {
             launch_factor_f64(h->dp, h->val, h->lu, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
+            if (h->cta) { launch_pack_f64(h->dp, h->lu, h->s64, h->stream); h->launches += 1; }
+        }
     }
     RSG_CUDA(cudaGetLastError());
     RSG_CUDA(cudaEventRecord(h->ev1, h->stream));
@@ -294,7 +327,7 @@ int do_setup(rsg_solver* h, const double* acc) {
 
 int launch_iterations(rsg_solver* h, int k) {
     const PrecDev M = prec_dev(h);
-    h->launches += (long long)k * (M.kind == 2 ? 5 : 7);
+    h->launches += (long long)k * (M.kind == 2 ? 5 : (M.cta ? 5 : 7));
     if (h->opt.use_graphs) {
         const int kind = M.kind;
         if (!h->gexec || h->gIters != k || h->gKind != kind) {
@@ -389,6 +422,7 @@ void rsg_default_options(rsg_options* o) {
     o->use_graphs = 1;
     o->device = 0;
     o->mem_budget = 0;
+    o->sweep = 0;
 }
 
 int rsg_create(rsg_solver** out, const rsg_options* opts) {
@@ -397,7 +431,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     rsg_options o;
     rsg_default_options(&o);
     if (opts) o = *opts;
-    if (o.precond < 0 || o.precond > 2 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 1)
+    if (o.precond < 0 || o.precond > 2 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 1 || o.sweep < 0 || o.sweep > 2)
         return fail(RSG_EINVAL, "invalid options");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
@@ -526,7 +560,8 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
 
 static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     const PrecDev M = prec_dev(h);
-    if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
+    if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
+    else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
     else if (M.kind == 1) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.y32, h->S, h->d_err, h->stream); h->launches += 2; }
     else { launch_block_jacobi_apply(h->dp, h->dinv, d_r, d_z, h->stream); h->launches += 1; }
     RSG_CUDA(cudaGetLastError());

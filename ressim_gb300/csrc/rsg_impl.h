@@ -44,6 +44,14 @@ struct HostPlan {
     std::vector<int> tileSys;         // system of every tile
     std::vector<int> sysTile0;        // first tile of every system (nsys + 1)
     bool symmetric = true;
+    // Per-system level-ordered split storage of the factors (CTA-per-system sweeps): position k in
+    // [sysRow0[s], sysRow0[s+1]) holds row lrow[k] of system s, rows sorted by (forward level, row);
+    // lvlStart[sysLvl0[s] + l] is the first position of level l (nl_s + 1 entries per system).
+    std::vector<int> lrow, lvlStart, sysLvl0;
+    std::vector<int> Lptr, Lcol, Lsrc;   // strict-lower blocks of position k: [Lptr[k], Lptr[k+1]), local column, source block
+    std::vector<int> Uptr, Ucol, Usrc;   // strict-upper blocks
+    std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of position k
+    int maxSysRows = 0;
 };
 
 // Builds the plan of a (block-diagonal batch of) BSR pattern(s). Returns false with a message on bad input.
@@ -82,6 +90,15 @@ struct DevPlan {
     int *ford = nullptr, *bord = nullptr;
     int *elimPtr = nullptr, *elimT = nullptr, *elimQ = nullptr;
     int *rowSys = nullptr, *tileRow0 = nullptr, *tileSys = nullptr, *sysTile0 = nullptr, *sysRow0 = nullptr;
+    int *lrow = nullptr, *lvlStart = nullptr, *sysLvl0 = nullptr;
+    int *Lptr = nullptr, *Lcol = nullptr, *Lsrc = nullptr, *Uptr = nullptr, *Ucol = nullptr, *Usrc = nullptr, *Dsrc = nullptr;
+    int nL = 0, nU = 0, maxSysRows = 0;
+};
+
+// Level-ordered split factors for the CTA-per-system sweeps (FP64 or FP32 storage).
+template <class T>
+struct SplitFactors {
+    T *L = nullptr, *U = nullptr, *D = nullptr;
 };
 
 struct SweepState {                   // sync-free sweep flags and claim counters
@@ -126,7 +143,22 @@ struct PrecDev {
     const float* luf = nullptr;
     const double* dinv = nullptr;
     const double* val = nullptr;
+    bool cta = false;                 // CTA-per-system level-synchronous sweeps on the split factors
+    SplitFactors<double> s64;
+    SplitFactors<float> s32;
+    size_t smem = 0;                  // dynamic shared memory of the CTA sweep (0: sweep vector in global memory)
 };
+// gather the factors (original block layout) into the level-ordered split layout
+void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st);
+void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F, cudaStream_t st);
+// z = M^-1 r with the CTA sweeps (plain input mode)
+void launch_ilu_cta_apply(const DevPlan& P, const PrecDev& M, const double* r, double* z, cudaStream_t st);
+// BiCGSTAB-fused CTA sweeps: input p = r + beta (p - omega v) (pupdate) or s = r - alpha v, stored to pv
+void launch_ilu_cta_fused(const DevPlan& P, const PrecDev& M, bool pupdate, const double* r, double* pv, const double* v, double* z,
+                          const KScal* ks, cudaStream_t st);
+// bytes of dynamic shared memory the CTA sweep needs for its vector (0 when it must stay in global memory)
+size_t cta_sweep_smem(const DevPlan& P, bool fp32);
+bool cta_sweep_supported(const DevPlan& P, const HostPlan& H);
 void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M, BicgVecs& V, KScal* ks, ReduceState& R,
                            SweepState& S, int* active, int* err, cudaStream_t st);
 // true residual ||b - A x|| / ||b|| per system (FP64)

@@ -862,7 +862,9 @@ void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M
                            SweepState& S, int* active, int* err, cudaStream_t st) {
     const int g = sweep_grid(P.n);
     auto prec = [&](bool pupd, double* out) {
-        if (M.kind == 0) {
+        if (M.cta && M.kind != 2) {
+            launch_ilu_cta_fused(P, M, pupd, V.r, pupd ? V.p : V.s, V.v, out, ks, st);
+        } else if (M.kind == 0) {
             if (pupd)
                 k_fwd_f64<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.p, V.v, out,
                                                                    P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);

@@ -119,6 +119,38 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     }
     P.sysTile0[size_t(nsys)] = int(P.tileSys.size());
     P.tileRow0.push_back(n);
+    // per-system level order (rows sorted by (forward level, row) inside each system) and the split L / U / D
+    // index arrays of the CTA-per-system sweeps; columns are local to the system
+    P.lrow.assign(size_t(n), 0);
+    P.lvlStart.clear();
+    P.sysLvl0.assign(size_t(nsys) + 1, 0);
+    P.maxSysRows = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const int r0 = sysRow0[size_t(s)], r1 = sysRow0[size_t(s) + 1];
+        P.maxSysRows = std::max(P.maxSysRows, r1 - r0);
+        int nls = 0;
+        for (int i = r0; i < r1; ++i) nls = std::max(nls, lev[size_t(i)] + 1);
+        std::vector<int> cnt(size_t(nls) + 1, 0);
+        for (int i = r0; i < r1; ++i) cnt[size_t(lev[size_t(i)]) + 1]++;
+        for (int l = 0; l < nls; ++l) cnt[size_t(l) + 1] += cnt[size_t(l)];
+        P.sysLvl0[size_t(s)] = int(P.lvlStart.size());
+        for (int l = 0; l <= nls; ++l) P.lvlStart.push_back(r0 + cnt[size_t(l)]);
+        for (int i = r0; i < r1; ++i) P.lrow[size_t(r0 + cnt[size_t(lev[size_t(i)])]++)] = i;
+    }
+    P.sysLvl0[size_t(nsys)] = int(P.lvlStart.size());
+    P.Lptr.assign(size_t(n) + 1, 0);
+    P.Uptr.assign(size_t(n) + 1, 0);
+    P.Dsrc.assign(size_t(n), 0);
+    P.Lcol.clear(); P.Lsrc.clear(); P.Ucol.clear(); P.Usrc.clear();
+    for (int k = 0; k < n; ++k) {
+        const int i = P.lrow[size_t(k)];
+        const int base = sysRow0[size_t(P.rowSys[size_t(i)])];
+        for (int p = rowPtr[size_t(i)]; p < P.diag[size_t(i)]; ++p) { P.Lcol.push_back(P.col[size_t(p)] - base); P.Lsrc.push_back(p); }
+        for (int p = P.diag[size_t(i)] + 1; p < rowPtr[size_t(i) + 1]; ++p) { P.Ucol.push_back(P.col[size_t(p)] - base); P.Usrc.push_back(p); }
+        P.Dsrc[size_t(k)] = P.diag[size_t(i)];
+        P.Lptr[size_t(k) + 1] = int(P.Lcol.size());
+        P.Uptr[size_t(k) + 1] = int(P.Ucol.size());
+    }
     return true;
 }
 

