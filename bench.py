@@ -97,6 +97,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def _lib_check(rc):
+    from ressim_gb300 import _lib
+    return _lib.check(rc)
+
+
 def spmv_bytes(nnzb, n):
     return nnzb * (9 * 8 + 4) + (n + 1) * 4 + 2 * 3 * n * 8
 
@@ -218,7 +223,8 @@ def main():
             ev[k][1].record(stream)
             results.append(res)
         barrier()
-    launches = dev.stats().kernel_launches - l0
+    st_last = dev.stats()
+    launches = st_last.kernel_launches - l0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     its, rr, tr = dev.batch_results()
     x_dev = d_x.cpu().numpy()
@@ -231,19 +237,16 @@ def main():
     ok = all(r.converged for r in results) and float(np.max(tr)) <= TOL
 
     # ---------------- per-kernel device time (events on the solver stream) for the roofline
-    d_y = torch.empty_like(d_b)
     reps = 20
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)
-    for _ in range(reps):
-        dev.spmv_device(d_x.data_ptr(), d_y.data_ptr())
+    _lib_check(dev.L.rsg_spmv_level_probe(dev.h, reps))
     e1.record(stream)
     torch.cuda.synchronize()
     t_spmv = e0.elapsed_time(e1) / reps / 1e3
     e0.record(stream)
-    for _ in range(reps):
-        dev.precond_apply_device(d_b.data_ptr(), d_y.data_ptr())
+    _lib_check(dev.L.rsg_precond_level_probe(dev.h, reps))
     e1.record(stream)
     torch.cuda.synchronize()
     t_prec = e0.elapsed_time(e1) / reps / 1e3      # forward + backward sweep
@@ -334,6 +337,7 @@ def main():
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                            "note": "batched step: all 64 systems complete together"},
             "iterations": {"mean": mean_its, "max": int(np.max(its))}, "max_true_relres": float(np.max(tr)), "all_converged": bool(ok),
+            "last_step_device_ms": {"setup": st_last.setup_ms, "solve": st_last.solve_ms},
             "fp64_plain": fp64_plain, "batched_mixed_over_plain_fp64": value / world / fp64_plain["value"],
             "e2e": e2e, "roofline": roofline, "roofline_spmv": roofline_spmv, "kernels": kernels, "gpu_launches": int(launches),
             "cpu_baseline": cpu, "clocks": clk.summary(),

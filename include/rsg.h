@@ -37,8 +37,12 @@ extern "C" {
 #define RSG_KRYLOV_GMRES 1    /* ressim::gmres (flexible, restarted), linsolve.h:101-102 */
 /* precision */
 #define RSG_FP64 0          /* everything in FP64 */
-#define RSG_MIXED 1         /* FP32 factors / AMG / preconditioner SpMV with FP32 accumulation; FP64 outer Krylov
-                               vectors, inner products, true residual and 3x3 diagonal-block inversions */
+#define RSG_MIXED 1         /* FP32 factor storage (elimination and 3x3 pivot inversions in FP64, as the reference's
+                               lean BILU0, engine/src/bsr.cpp:219-263), FP64 sweep vector and accumulation (the
+                               reference's float-factor sweeps, engine/src/bsr.cpp:500-522); FP64 outer Krylov
+                               vectors, inner products and true residual */
+#define RSG_MIXED_F32 2     /* as RSG_MIXED but the sweeps also run in FP32 (vector and accumulation, BILU0f,
+                               engine/src/bsr.cpp:1100-1121): less robust on ill-conditioned systems */
 
 typedef struct rsg_options {
     int precond;            /* RSG_PREC_* */
@@ -122,6 +126,11 @@ int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z);
 /* Copy the BILU0 factors (FP64 path: L strictly lower, U_ii^-1 on the diagonal, U upper, in the matrix's
  * own pattern and block order -- the storage of ressim::BILU0, engine/src/bsr.cpp:183-215). */
 int rsg_get_factors(rsg_solver* h, double* lu);
+
+/* Timing probes for benchmarks (no counterpart in the reference): launch the internal SpMV / the preconditioner
+ * `reps` times on the handle's own device vectors, asynchronously on its stream, without any copy around them. */
+int rsg_spmv_level_probe(rsg_solver* h, int reps);
+int rsg_precond_level_probe(rsg_solver* h, int reps);
 
 /* Statistics of the last setup / solve. */
 int rsg_get_stats(rsg_solver* h, rsg_stats* st);

@@ -15,7 +15,7 @@ from . import _build
 RSG_OK, RSG_EINVAL, RSG_ECUDA, RSG_ENOMEM, RSG_ESTATE, RSG_ETIMEOUT, RSG_EBREAKDOWN, RSG_ENOTCONV = 0, -1, -2, -3, -4, -5, -6, 1
 PREC = {"bilu0": 0, "cpr": 1, "jacobi": 2}
 KRYLOV = {"bicgstab": 0, "gmres": 1}
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed_f32": 2}
 SWEEP = {"auto": 0, "cta": 1, "grid": 2}
 
 # every symbol include/rsg.h declares
@@ -23,6 +23,7 @@ EXPORTS = [
     "rsg_default_options", "rsg_last_error", "rsg_version", "rsg_create", "rsg_destroy", "rsg_set_matrix", "rsg_set_batch",
     "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
+    "rsg_spmv_level_probe", "rsg_precond_level_probe",
 ]
 
 
@@ -74,6 +75,8 @@ def load(build_if_missing: bool = True):
     L.rsg_spmv_device.argtypes = [vp, vp, vp]
     L.rsg_precond_apply.argtypes = [vp, vp, vp]
     L.rsg_precond_apply_device.argtypes = [vp, vp, vp]
+    L.rsg_spmv_level_probe.argtypes = [vp, C.c_int]
+    L.rsg_precond_level_probe.argtypes = [vp, C.c_int]
     L.rsg_get_factors.argtypes = [vp, vp]
     L.rsg_get_stats.argtypes = [vp, C.POINTER(Stats)]
     L.rsg_stream.argtypes = [vp]

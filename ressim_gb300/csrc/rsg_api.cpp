@@ -85,7 +85,8 @@ struct rsg_solver {
     bool cta = false;
     // vectors
     BicgVecs V{};
-    double *b = nullptr, *xout = nullptr, *tmp = nullptr;
+    double *b = nullptr, *xout = nullptr, *tmp = nullptr;   // level-space b / x, original-order staging
+    double* val0 = nullptr;      // matrix values as uploaded (original block order), gathered into val
     // sync-free state, reductions, scalars
     SweepState S{};
     ReduceState R{};
@@ -145,7 +146,8 @@ int alloc_plan(rsg_solver* h) {
         (rc = upload(M, &D.elimT, P.elimT, st)) || (rc = upload(M, &D.elimQ, P.elimQ, st)) || (rc = upload(M, &D.rowSys, P.rowSys, st)) ||
         (rc = upload(M, &D.tileRow0, P.tileRow0, st)) || (rc = upload(M, &D.tileSys, P.tileSys, st)) ||
         (rc = upload(M, &D.sysTile0, P.sysTile0, st)) || (rc = upload(M, &D.sysRow0, P.sysRow0, st)) ||
-        (rc = upload(M, &D.lrow, P.lrow, st)) || (rc = upload(M, &D.lvlStart, P.lvlStart, st)) || (rc = upload(M, &D.sysLvl0, P.sysLvl0, st)) ||
+        (rc = upload(M, &D.perm, P.perm, st)) || (rc = upload(M, &D.valSrc, P.valSrc, st)) ||
+        (rc = upload(M, &D.lvlStart, P.lvlStart, st)) || (rc = upload(M, &D.sysLvl0, P.sysLvl0, st)) ||
         (rc = upload(M, &D.Lptr, P.Lptr, st)) || (rc = upload(M, &D.Lcol, P.Lcol, st)) || (rc = upload(M, &D.Lsrc, P.Lsrc, st)) ||
         (rc = upload(M, &D.Uptr, P.Uptr, st)) || (rc = upload(M, &D.Ucol, P.Ucol, st)) || (rc = upload(M, &D.Usrc, P.Usrc, st)) ||
         (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
@@ -156,7 +158,8 @@ int alloc_plan(rsg_solver* h) {
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
     if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
-    if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) || (rc = dalloc(M, &h->tmp, N)))
+    if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
+        (rc = dalloc(M, &h->tmp, N)))
         return rc;
     double** vecs[] = {&h->V.x, &h->V.r, &h->V.rh, &h->V.p, &h->V.v, &h->V.s, &h->V.t, &h->V.ph, &h->V.sh};
     for (double** v : vecs)
@@ -201,12 +204,13 @@ PrecDev prec_dev(rsg_solver* h) {
     PrecDev M;
     if (h->opt.precond == RSG_PREC_JACOBI) { M.kind = 2; M.dinv = h->dinv; }
     else if (h->opt.precision == RSG_MIXED) { M.kind = 1; M.luf = h->luf; }
+    else if (h->opt.precision == RSG_MIXED_F32) { M.kind = 3; M.luf = h->luf; }
     else { M.kind = 0; M.lu = h->lu; }
     M.val = h->val;
+    M.y32 = h->V.y32;
     if (M.kind != 2 && h->cta) {
-        M.smem = cta_sweep_smem(h->dp, M.kind == 1);
-        // FP32 sweeps need their vector in shared memory; FP64 may keep it in global memory
-        M.cta = M.kind == 0 || M.smem > 0;
+        M.smem = cta_sweep_smem(h->dp, M.kind == 3);
+        M.cta = true;
         M.s64 = h->s64;
         M.s32 = h->s32;
     }
@@ -217,9 +221,12 @@ int set_values(rsg_solver* h, const std::vector<const double*>& vals, const std:
     size_t off = 0;
     for (size_t s = 0; s < vals.size(); ++s) {
         const size_t cnt = size_t(nnzbs[s]) * NB2;
-        if (cnt) RSG_CUDA(cudaMemcpyAsync(h->val + off, vals[s], cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        if (cnt) RSG_CUDA(cudaMemcpyAsync(h->val0 + off, vals[s], cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         off += cnt;
     }
+    launch_gather_blocks(h->dp, h->val0, h->val, h->stream);   // into level space
+    h->launches += 1;
+    RSG_CUDA(cudaGetLastError());
     h->haveMatrix = true;
     h->haveSetup = false;
     return RSG_OK;
@@ -254,7 +261,7 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
         }
         nnzbs[size_t(s)] = rowPtr[s][n[s]];
     }
-    const bool same = h->havePlan && h->plan.nsys == nsys && h->plan.rowPtr == rp && h->plan.col == ci && h->plan.sysRow0 == sysRow0;
+    const bool same = h->havePlan && h->plan.nsys == nsys && h->plan.rowPtr0 == rp && h->plan.col0 == ci && h->plan.sysRow0 == sysRow0;
     if (!same) {
         free_plan(h);
         std::string err;
@@ -272,10 +279,10 @@ int ensure_precond_storage(rsg_solver* h) {
     int rc;
     if (h->opt.precond == RSG_PREC_JACOBI) {
         if (!h->dinv && (rc = dalloc(h->pmem, &h->dinv, size_t(h->plan.n) * NB2))) return rc;
-    } else if (h->opt.precision == RSG_MIXED) {
+    } else if (h->opt.precision == RSG_MIXED || h->opt.precision == RSG_MIXED_F32) {
         if (!h->luf && (rc = dalloc(h->pmem, &h->luf, E))) return rc;
         if (!h->work && (rc = dalloc(h->pmem, &h->work, E))) return rc;
-        if (!h->V.y32 && (rc = dalloc(h->pmem, &h->V.y32, size_t(h->plan.n) * NB))) return rc;
+        if (h->opt.precision == RSG_MIXED_F32 && !h->V.y32 && (rc = dalloc(h->pmem, &h->V.y32, size_t(h->plan.n) * NB))) return rc;
         if (h->cta && !h->s32.L) {
             if ((rc = dalloc(h->pmem, &h->s32.L, size_t(h->dp.nL) * NB2)) || (rc = dalloc(h->pmem, &h->s32.U, size_t(h->dp.nU) * NB2)) ||
                 (rc = dalloc(h->pmem, &h->s32.D, size_t(h->dp.n) * NB2)))
@@ -305,7 +312,7 @@ int do_setup(rsg_solver* h, const double* acc) {
         launch_block_jacobi_setup(h->dp, h->val, h->dinv, h->d_nreg, h->stream);
     } else {
         ++h->epoch;
-        if (h->opt.precision == RSG_MIXED) {
+        if (h->opt.precision == RSG_MIXED || h->opt.precision == RSG_MIXED_F32) {
             launch_factor_lean(h->dp, h->val, h->luf, h->work, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
             if (h->cta) { launch_pack_f32(h->dp, h->luf, h->s32, h->stream); h->launches += 1; }
         } else {
@@ -350,14 +357,15 @@ int launch_iterations(rsg_solver* h, int k) {
     return RSG_OK;
 }
 
+// d_b, d_x: caller's vectors in the original row order; the solve runs in level space (h->b, h->V.x)
 int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
     if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
     if (h->opt.krylov != RSG_KRYLOV_BICGSTAB) return fail(RSG_EINVAL, "GMRES is not available in this build");
     if (!(tol > 0) || maxIt < 0) return fail(RSG_EINVAL, "tol must be > 0 and maxIt >= 0");
-    const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
-    launch_bicg_init(h->dp, d_b, h->V, h->ks, h->R, tol, maxIt, h->d_active, h->stream);
-    h->launches += 2;   // init + true residual
+    launch_gather_vec(h->dp, d_b, h->b, h->stream);
+    launch_bicg_init(h->dp, h->b, h->V, h->ks, h->R, tol, maxIt, h->d_active, h->stream);
+    h->launches += 4;   // gather, init, scatter, true residual
     RSG_CUDA(cudaGetLastError());
     const int chunk = h->opt.check_every > 0 ? h->opt.check_every : 4;
     int launched = 0, rc;
@@ -368,9 +376,9 @@ int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, i
         if ((rc = launch_iterations(h, chunk))) return rc;
         launched += chunk;
     }
-    if (d_x != h->V.x) RSG_CUDA(cudaMemcpyAsync(d_x, h->V.x, N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    launch_scatter_vec(h->dp, h->V.x, d_x, h->stream);
     RSG_CUDA(cudaEventRecord(h->ev1, h->stream));
-    launch_true_residual(h->dp, h->val, d_b, h->V.x, h->tmp, h->R, h->d_trueres, h->stream);
+    launch_true_residual(h->dp, h->val, h->b, h->V.x, nullptr, h->R, h->d_trueres, h->stream);
     RSG_CUDA(cudaGetLastError());
     if ((rc = check_device_errors(h))) return rc;
     h->hks.resize(size_t(h->plan.nsys));
@@ -431,7 +439,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     rsg_options o;
     rsg_default_options(&o);
     if (opts) o = *opts;
-    if (o.precond < 0 || o.precond > 2 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 1 || o.sweep < 0 || o.sweep > 2)
+    if (o.precond < 0 || o.precond > 2 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 2)
         return fail(RSG_EINVAL, "invalid options");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
@@ -515,8 +523,8 @@ int rsg_solve(rsg_solver* h, const double* b, double* x, double tol, int maxIt, 
     cudaSetDevice(h->device);
     if (!h->havePlan) return fail(RSG_ESTATE, "solve before set_matrix");
     const size_t N = size_t(h->plan.n) * NB;
-    RSG_CUDA(cudaMemcpyAsync(h->b, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    const int rc = do_solve_device(h, h->b, h->xout, tol, maxIt, iterations, relres);
+    RSG_CUDA(cudaMemcpyAsync(h->tmp, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const int rc = do_solve_device(h, h->tmp, h->xout, tol, maxIt, iterations, relres);
     if (rc < 0) return rc;
     RSG_CUDA(cudaMemcpyAsync(x, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     RSG_CUDA(cudaStreamSynchronize(h->stream));
@@ -538,8 +546,19 @@ int rsg_spmv_device(rsg_solver* h, const double* d_x, double* d_y) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
-    launch_spmv_f64(h->dp, h->val, d_x, d_y, h->stream);
-    h->launches += 1;
+    launch_gather_vec(h->dp, d_x, h->b, h->stream);
+    launch_spmv_f64(h->dp, h->val, h->b, h->xout, h->stream);
+    launch_scatter_vec(h->dp, h->xout, d_y, h->stream);
+    h->launches += 3;
+    RSG_CUDA(cudaGetLastError());
+    return RSG_OK;
+}
+
+// level-space SpMV on the handle's own vectors (per-kernel timing)
+int rsg_spmv_level_probe(rsg_solver* h, int reps) {
+    if (!h || !h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
+    for (int r = 0; r < reps; ++r) launch_spmv_f64(h->dp, h->val, h->V.x, h->xout, h->stream);
+    h->launches += reps;
     RSG_CUDA(cudaGetLastError());
     return RSG_OK;
 }
@@ -550,19 +569,24 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
     cudaSetDevice(h->device);
     if (!h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
     const size_t N = size_t(h->plan.n) * NB;
-    RSG_CUDA(cudaMemcpyAsync(h->b, x, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(h->tmp, x, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_gather_vec(h->dp, h->tmp, h->b, h->stream);
     launch_spmv_f64(h->dp, h->val, h->b, h->xout, h->stream);
+    launch_scatter_vec(h->dp, h->xout, h->tmp, h->stream);
+    h->launches += 3;
     RSG_CUDA(cudaGetLastError());
-    RSG_CUDA(cudaMemcpyAsync(y, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(y, h->tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     RSG_CUDA(cudaStreamSynchronize(h->stream));
     return RSG_OK;
 }
 
+// level-space r -> level-space z
 static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     const PrecDev M = prec_dev(h);
     if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
     else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
-    else if (M.kind == 1) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.y32, h->S, h->d_err, h->stream); h->launches += 2; }
+    else if (M.kind == 1) { launch_ilu_apply_mixed(h->dp, h->luf, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
+    else if (M.kind == 3) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.y32, h->S, h->d_err, h->stream); h->launches += 2; }
     else { launch_block_jacobi_apply(h->dp, h->dinv, d_r, d_z, h->stream); h->launches += 1; }
     RSG_CUDA(cudaGetLastError());
     return RSG_OK;
@@ -573,7 +597,23 @@ int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
-    return precond_apply_dev(h, d_r, d_z);
+    launch_gather_vec(h->dp, d_r, h->b, h->stream);
+    int rc = precond_apply_dev(h, h->b, h->xout);
+    if (rc) return rc;
+    launch_scatter_vec(h->dp, h->xout, d_z, h->stream);
+    h->launches += 2;
+    RSG_CUDA(cudaGetLastError());
+    return RSG_OK;
+}
+
+// level-space preconditioner application on the handle's own vectors (per-kernel timing)
+int rsg_precond_level_probe(rsg_solver* h, int reps) {
+    if (!h || !h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
+    for (int r = 0; r < reps; ++r) {
+        int rc = precond_apply_dev(h, h->b, h->xout);
+        if (rc) return rc;
+    }
+    return RSG_OK;
 }
 
 int rsg_precond_apply(rsg_solver* h, const double* r, double* z) {
@@ -582,12 +622,15 @@ int rsg_precond_apply(rsg_solver* h, const double* r, double* z) {
     cudaSetDevice(h->device);
     if (!h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
     const size_t N = size_t(h->plan.n) * NB;
-    RSG_CUDA(cudaMemcpyAsync(h->b, r, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(h->tmp, r, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_gather_vec(h->dp, h->tmp, h->b, h->stream);
     int rc = precond_apply_dev(h, h->b, h->xout);
     if (rc) return rc;
+    launch_scatter_vec(h->dp, h->xout, h->tmp, h->stream);
+    h->launches += 2;
     rc = check_device_errors(h);
     if (rc) return rc;
-    RSG_CUDA(cudaMemcpyAsync(z, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(z, h->tmp, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     RSG_CUDA(cudaStreamSynchronize(h->stream));
     return RSG_OK;
 }
@@ -597,8 +640,11 @@ int rsg_get_factors(rsg_solver* h, double* lu) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveSetup || !h->lu) return fail(RSG_ESTATE, "no FP64 BILU0 factors (setup not run, or not the FP64 BILU0 path)");
-    RSG_CUDA(cudaMemcpyAsync(lu, h->lu, size_t(h->plan.nnzb) * NB2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double> lev(size_t(h->plan.nnzb) * NB2);
+    RSG_CUDA(cudaMemcpyAsync(lev.data(), h->lu, lev.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     RSG_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t p = 0; p < size_t(h->plan.nnzb); ++p)   // back to the caller's block order
+        std::memcpy(lu + size_t(h->plan.valSrc[p]) * NB2, lev.data() + p * NB2, sizeof(double) * NB2);
     return RSG_OK;
 }
 

@@ -30,10 +30,16 @@ struct KScal {
     double tol;
 };
 
-// Host-built, pattern-only plan of the sync-free triangular sweeps and the factorisation.
+// Host-built, pattern-only plan of the device solve. Everything on the device runs in "level space": inside
+// every system the block rows are renumbered by (forward level, row) -- perm[k] = original row of level-space
+// row k -- and the entries of a row keep their original order, so rows of a level are contiguous while every
+// row is still eliminated and swept in the reference's arithmetic order.
 struct HostPlan {
     int n = 0, nnzb = 0, nsys = 1;
-    std::vector<int> rowPtr, col, diag;
+    std::vector<int> rowPtr0, col0;   // original pattern (pattern-reuse test)
+    std::vector<int> perm, iperm;     // level-space row -> original row, and back
+    std::vector<int> valSrc;          // level-space block -> original block
+    std::vector<int> rowPtr, col, diag;   // level-space pattern
     std::vector<int> ford, bord;      // claim orders: forward (by L level) and backward (by U level)
     int nlevF = 0, nlevB = 0;
     std::vector<int> elimPtr;         // per block entry p (lower entries only non-empty): range in elimT/elimQ
@@ -44,10 +50,9 @@ struct HostPlan {
     std::vector<int> tileSys;         // system of every tile
     std::vector<int> sysTile0;        // first tile of every system (nsys + 1)
     bool symmetric = true;
-    // Per-system level-ordered split storage of the factors (CTA-per-system sweeps): position k in
-    // [sysRow0[s], sysRow0[s+1]) holds row lrow[k] of system s, rows sorted by (forward level, row);
-    // lvlStart[sysLvl0[s] + l] is the first position of level l (nl_s + 1 entries per system).
-    std::vector<int> lrow, lvlStart, sysLvl0;
+    // lvlStart[sysLvl0[s] + l] is the first level-space row of level l of system s (nl_s + 1 entries per system)
+    std::vector<int> lvlStart, sysLvl0;
+    // split storage of the factors for the thread-block sweeps (level-space row order)
     std::vector<int> Lptr, Lcol, Lsrc;   // strict-lower blocks of position k: [Lptr[k], Lptr[k+1]), local column, source block
     std::vector<int> Uptr, Ucol, Usrc;   // strict-upper blocks
     std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of position k
@@ -90,7 +95,8 @@ struct DevPlan {
     int *ford = nullptr, *bord = nullptr;
     int *elimPtr = nullptr, *elimT = nullptr, *elimQ = nullptr;
     int *rowSys = nullptr, *tileRow0 = nullptr, *tileSys = nullptr, *sysTile0 = nullptr, *sysRow0 = nullptr;
-    int *lrow = nullptr, *lvlStart = nullptr, *sysLvl0 = nullptr;
+    int *perm = nullptr, *valSrc = nullptr;
+    int *lvlStart = nullptr, *sysLvl0 = nullptr;
     int *Lptr = nullptr, *Lcol = nullptr, *Lsrc = nullptr, *Uptr = nullptr, *Ucol = nullptr, *Usrc = nullptr, *Dsrc = nullptr;
     int nL = 0, nU = 0, maxSysRows = 0;
 };
@@ -114,6 +120,10 @@ struct ReduceState {                  // fused tile reductions
 
 // ---- kernel launchers (rsg_kernels.cu)
 int device_sm_count();
+// level-space gathers / scatters: blocks (9 doubles) by valSrc, vectors (3 doubles per row) by perm
+void launch_gather_blocks(const DevPlan& P, const double* src, double* dst, cudaStream_t st);
+void launch_gather_vec(const DevPlan& P, const double* orig, double* lev, cudaStream_t st);
+void launch_scatter_vec(const DevPlan& P, const double* lev, double* orig, cudaStream_t st);
 void launch_factor_f64(const DevPlan& P, const double* val, double* lu, SweepState& S, int epoch, int* nreg, int* err,
                        cudaStream_t st);
 void launch_factor_lean(const DevPlan& P, const double* val, float* luf, double* work, SweepState& S, int epoch, int* nreg,
@@ -123,6 +133,9 @@ void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, d
                           cudaStream_t st);
 void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S,
                           int* err, cudaStream_t st);
+// FP32 factors, FP64 vector and accumulation (the reference's float-factor sweeps)
+void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r, double* z, SweepState& S, int* err,
+                            cudaStream_t st);
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st);
 // block-Jacobi: dinv = inverse diagonal blocks (FP64), z = dinv r
 void launch_block_jacobi_setup(const DevPlan& P, const double* val, double* dinv, int* nreg, cudaStream_t st);
@@ -146,7 +159,8 @@ struct PrecDev {
     bool cta = false;                 // CTA-per-system level-synchronous sweeps on the split factors
     SplitFactors<double> s64;
     SplitFactors<float> s32;
-    size_t smem = 0;                  // dynamic shared memory of the CTA sweep (0: sweep vector in global memory)
+    size_t smem = 0;                  // dynamic shared memory of the CTA sweep (systems whose vector fits keep it there)
+    float* y32 = nullptr;             // all-FP32 sweep vector in global memory (systems that do not fit on chip)
 };
 // gather the factors (original block layout) into the level-ordered split layout
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st);

@@ -266,10 +266,17 @@ __device__ __forceinline__ bool sys_running(const KScal* ks, const int* rowSys, 
 
 // y_i = in_i - sum_{k<i} L_ik y_k   (engine/src/bsr.cpp:568-575)
 // IN_PUPDATE: in = p = r + beta (p - omega v) (p stored); IN_SUPDATE: in = s = r - alpha v (s stored in pv)
-template <int MODE>
+// factor blocks in FP64 or FP32 storage, read as double (the float-factor sweeps, engine/src/bsr.cpp:500-522)
+__device__ __forceinline__ void ldf9(const double* p, double* a) { load9_ro(p, a); }
+__device__ __forceinline__ void ldf9(const float* p, double* a) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) a[e] = double(__ldg(p + e));
+}
+
+template <class TF, int MODE>
 __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                           const int* __restrict__ diag, const int* __restrict__ ford,
-                                                          const double* __restrict__ lu, const double* r, double* pv,
+                                                          const TF* __restrict__ lu, const double* r, double* pv,
                                                           const double* v, double* y, const int* __restrict__ rowSys,
                                                           const KScal* ks, int* flagF, int* flagB, unsigned* ctr, int* err) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1] = 0u;   // backward claim counter for the next sweep
@@ -313,7 +320,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __r
                     const int k = __ldg(col + p);
                     wait_flag(flagF + k, 1, err);
                     double a[9], yk[3];
-                    load9_ro(lu + size_t(p) * 9, a);
+                    ldf9(lu + size_t(p) * 9, a);
                     yk[0] = y[size_t(k) * 3 + 0]; yk[1] = y[size_t(k) * 3 + 1]; yk[2] = y[size_t(k) * 3 + 2];
                     yi[0] = ds(yi[0], dot3(a, yk));
                     yi[1] = ds(yi[1], dot3(a + 3, yk));
@@ -329,9 +336,10 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __r
 }
 
 // z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j), in place   (engine/src/bsr.cpp:577-587)
+template <class TF>
 __global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                           const int* __restrict__ diag, const int* __restrict__ bord,
-                                                          const double* __restrict__ lu, double* y, const int* __restrict__ rowSys,
+                                                          const TF* __restrict__ lu, double* y, const int* __restrict__ rowSys,
                                                           const KScal* ks, int* flagF, int* flagB, unsigned* ctr, int* err) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr[0] = 0u;
     const int lane = threadIdx.x & 31;
@@ -349,14 +357,14 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __r
                     const int j = __ldg(col + p);
                     wait_flag(flagB + j, 1, err);
                     double a[9], zj[3];
-                    load9_ro(lu + size_t(p) * 9, a);
+                    ldf9(lu + size_t(p) * 9, a);
                     zj[0] = y[size_t(j) * 3 + 0]; zj[1] = y[size_t(j) * 3 + 1]; zj[2] = y[size_t(j) * 3 + 2];
                     yi[0] = ds(yi[0], dot3(a, zj));
                     yi[1] = ds(yi[1], dot3(a + 3, zj));
                     yi[2] = ds(yi[2], dot3(a + 6, zj));
                 }
                 double D[9];
-                load9_ro(lu + size_t(d) * 9, D);
+                ldf9(lu + size_t(d) * 9, D);
                 y[size_t(i) * 3 + 0] = dot3(D, yi);
                 y[size_t(i) * 3 + 1] = dot3(D + 3, yi);
                 y[size_t(i) * 3 + 2] = dot3(D + 6, yi);
@@ -780,7 +788,27 @@ __global__ void k_bj_apply(int n, const double* __restrict__ dinv, const double*
     z[size_t(i) * 3 + 2] = dot3(D + 6, yi);
 }
 
+__global__ void k_gather_blocks(int nnzb, const int* __restrict__ src, const double* __restrict__ a, double* b) {
+    const size_t total = size_t(nnzb) * 9;
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < total; q += size_t(gridDim.x) * blockDim.x)
+        b[q] = __ldg(a + size_t(__ldg(src + q / 9)) * 9 + q % 9);
+}
+__global__ void k_gather_vec(int n, const int* __restrict__ perm, const double* __restrict__ orig, double* lev) {
+    const size_t total = size_t(n) * 3;
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < total; q += size_t(gridDim.x) * blockDim.x)
+        lev[q] = __ldg(orig + size_t(__ldg(perm + q / 3)) * 3 + q % 3);
+}
+__global__ void k_scatter_vec(int n, const int* __restrict__ perm, const double* __restrict__ lev, double* orig) {
+    const size_t total = size_t(n) * 3;
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < total; q += size_t(gridDim.x) * blockDim.x)
+        orig[size_t(__ldg(perm + q / 3)) * 3 + q % 3] = __ldg(lev + q);
+}
+
 int g_sm_count = 0;
+int stream_grid(size_t total) {
+    const size_t g = (total + 255) / 256, cap = size_t(device_sm_count()) * 16;
+    return int(g < cap ? (g > 0 ? g : 1) : cap);
+}
 int sweep_grid(int n) {
     const int sms = device_sm_count();
     // enough warps for several levels in flight, at most 8 blocks of 4 warps per SM
@@ -804,6 +832,16 @@ int device_sm_count() {
     return g_sm_count;
 }
 
+void launch_gather_blocks(const DevPlan& P, const double* src, double* dst, cudaStream_t st) {
+    k_gather_blocks<<<stream_grid(size_t(P.nnzb) * 9), 256, 0, st>>>(P.nnzb, P.valSrc, src, dst);
+}
+void launch_gather_vec(const DevPlan& P, const double* orig, double* lev, cudaStream_t st) {
+    k_gather_vec<<<stream_grid(size_t(P.n) * 3), 256, 0, st>>>(P.n, P.perm, orig, lev);
+}
+void launch_scatter_vec(const DevPlan& P, const double* lev, double* orig, cudaStream_t st) {
+    k_scatter_vec<<<stream_grid(size_t(P.n) * 3), 256, 0, st>>>(P.n, P.perm, lev, orig);
+}
+
 void launch_factor_f64(const DevPlan& P, const double* val, double* lu, SweepState& S, int epoch, int* nreg, int* err,
                        cudaStream_t st) {
     cudaMemcpyAsync(lu, val, size_t(P.nnzb) * 9 * sizeof(double), cudaMemcpyDeviceToDevice, st);
@@ -822,10 +860,19 @@ void launch_factor_lean(const DevPlan& P, const double* val, float* luf, double*
 void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, double* z, SweepState& S, int* err,
                           cudaStream_t st) {
     const int g = sweep_grid(P.n);
-    k_fwd_f64<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, lu, r, nullptr, nullptr, z, P.rowSys,
+    k_fwd_f64<double, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, lu, r, nullptr, nullptr, z, P.rowSys,
                                                      nullptr, S.flagF, S.flagB, S.ctr, err);
-    k_bwd_f64<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, lu, z, P.rowSys, nullptr, S.flagF, S.flagB, S.ctr,
+    k_bwd_f64<double><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, lu, z, P.rowSys, nullptr, S.flagF, S.flagB, S.ctr,
                                           err);
+}
+
+void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r, double* z, SweepState& S, int* err,
+                            cudaStream_t st) {
+    const int g = sweep_grid(P.n);
+    k_fwd_f64<float, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, luf, r, nullptr, nullptr, z, P.rowSys,
+                                                           nullptr, S.flagF, S.flagB, S.ctr, err);
+    k_bwd_f64<float><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, luf, z, P.rowSys, nullptr, S.flagF, S.flagB, S.ctr,
+                                                 err);
 }
 
 void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S, int* err,
@@ -866,14 +913,23 @@ void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M
             launch_ilu_cta_fused(P, M, pupd, V.r, pupd ? V.p : V.s, V.v, out, ks, st);
         } else if (M.kind == 0) {
             if (pupd)
-                k_fwd_f64<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.p, V.v, out,
-                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+                k_fwd_f64<double, IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.p, V.v, out,
+                                                                           P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
             else
-                k_fwd_f64<IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.s, V.v, out,
-                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
-            k_bwd_f64<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.lu, out, P.rowSys, ks, S.flagF, S.flagB,
-                                                  S.ctr, err);
-        } else if (M.kind == 1) {
+                k_fwd_f64<double, IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, V.r, V.s, V.v, out,
+                                                                           P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            k_bwd_f64<double><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.lu, out, P.rowSys, ks, S.flagF,
+                                                          S.flagB, S.ctr, err);
+        } else if (M.kind == 1) {      // FP32 factors, FP64 sweep vector
+            if (pupd)
+                k_fwd_f64<float, IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.p, V.v, out,
+                                                                          P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            else
+                k_fwd_f64<float, IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.s, V.v, out,
+                                                                          P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+            k_bwd_f64<float><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, out, P.rowSys, ks, S.flagF,
+                                                         S.flagB, S.ctr, err);
+        } else if (M.kind == 3) {      // all-FP32 sweep
             if (pupd)
                 k_fwd_f32<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.p, V.v, V.y32,
                                                                    P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);

@@ -21,89 +21,133 @@ void order_by_level(const std::vector<int>& lev, int nl, std::vector<int>& ord) 
 }
 }  // namespace
 
-bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
-                const std::vector<int>& col, std::string& err) {
-    const int n = int(rowPtr.size()) - 1;
+bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr0,
+                const std::vector<int>& col0, std::string& err) {
+    const int n = int(rowPtr0.size()) - 1;
     if (n < 1) { err = "empty matrix (n < 1)"; return false; }
-    if (rowPtr[0] != 0) { err = "rowPtr[0] must be 0"; return false; }
+    if (rowPtr0[0] != 0) { err = "rowPtr[0] must be 0"; return false; }
     for (int i = 0; i < n; ++i)
-        if (rowPtr[size_t(i) + 1] < rowPtr[size_t(i)]) { err = "rowPtr is not monotone"; return false; }
-    const int nnzb = rowPtr[size_t(n)];
-    if (int(col.size()) < nnzb) { err = "col shorter than rowPtr[n]"; return false; }
+        if (rowPtr0[size_t(i) + 1] < rowPtr0[size_t(i)]) { err = "rowPtr is not monotone"; return false; }
+    const int nnzb = rowPtr0[size_t(n)];
+    if (int(col0.size()) < nnzb) { err = "col shorter than rowPtr[n]"; return false; }
     P = HostPlan{};
     P.n = n; P.nnzb = nnzb; P.nsys = nsys;
-    P.rowPtr = rowPtr;
-    P.col.assign(col.begin(), col.begin() + nnzb);
+    P.rowPtr0 = rowPtr0;
+    P.col0.assign(col0.begin(), col0.begin() + nnzb);
     P.sysRow0 = sysRow0;
     P.rowSys.assign(size_t(n), 0);
     for (int s = 0; s < nsys; ++s)
         for (int i = sysRow0[size_t(s)]; i < sysRow0[size_t(s) + 1]; ++i) P.rowSys[size_t(i)] = s;
-    // validation: sorted columns, in range, inside the row's own system, diagonal present
-    P.diag.assign(size_t(n), -1);
+    // validation of the original pattern: sorted columns, in range, inside the row's own system, diagonal present
+    std::vector<int> diag0(size_t(n), -1);
     for (int i = 0; i < n; ++i) {
         const int s = P.rowSys[size_t(i)];
         const int lo = sysRow0[size_t(s)], hi = sysRow0[size_t(s) + 1];
-        for (int p = rowPtr[size_t(i)]; p < rowPtr[size_t(i) + 1]; ++p) {
-            const int c = P.col[size_t(p)];
+        for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p) {
+            const int c = P.col0[size_t(p)];
             if (c < lo || c >= hi) { err = "column index out of range in block row " + std::to_string(i - lo); return false; }
-            if (p > rowPtr[size_t(i)] && c <= P.col[size_t(p) - 1]) {
+            if (p > rowPtr0[size_t(i)] && c <= P.col0[size_t(p) - 1]) {
                 err = "columns not strictly increasing in block row " + std::to_string(i - lo);
                 return false;
             }
-            if (c == i) P.diag[size_t(i)] = p;
+            if (c == i) diag0[size_t(i)] = p;
         }
-        if (P.diag[size_t(i)] < 0) { err = "missing diagonal block in block row " + std::to_string(i - lo); return false; }
+        if (diag0[size_t(i)] < 0) { err = "missing diagonal block in block row " + std::to_string(i - lo); return false; }
     }
-    // forward levels (L dependencies) -> claim order
+    // forward levels of the L dependencies (engine/src/bsr.cpp:270-293)
     std::vector<int> lev(size_t(n), 0);
-    int nl = 0;
     for (int i = 0; i < n; ++i) {
         int l = 0;
-        for (int p = rowPtr[size_t(i)]; p < P.diag[size_t(i)]; ++p) l = std::max(l, lev[size_t(P.col[size_t(p)])] + 1);
+        for (int p = rowPtr0[size_t(i)]; p < diag0[size_t(i)]; ++p) l = std::max(l, lev[size_t(P.col0[size_t(p)])] + 1);
         lev[size_t(i)] = l;
-        nl = std::max(nl, l + 1);
     }
-    P.nlevF = nl;
-    order_by_level(lev, nl, P.ford);
-    // structural symmetry: then the reversed forward order is a topological order of the U dependencies
+    // level space: inside every system, rows renumbered by (forward level, row); a topological order of L, so
+    // ILU(0) is unchanged (the reference's level-ordered contiguous storage, engine/src/bsr.cpp:315-345). The
+    // entries of a row keep their original order, so every row is eliminated / swept in the reference's order.
+    P.perm.assign(size_t(n), 0);
+    P.iperm.assign(size_t(n), 0);
+    P.lvlStart.clear();
+    P.sysLvl0.assign(size_t(nsys) + 1, 0);
+    P.maxSysRows = 0;
+    std::vector<int> levNew(size_t(n), 0);
+    for (int s = 0; s < nsys; ++s) {
+        const int r0 = sysRow0[size_t(s)], r1 = sysRow0[size_t(s) + 1];
+        P.maxSysRows = std::max(P.maxSysRows, r1 - r0);
+        int nls = 0;
+        for (int i = r0; i < r1; ++i) nls = std::max(nls, lev[size_t(i)] + 1);
+        std::vector<int> cnt(size_t(nls) + 1, 0);
+        for (int i = r0; i < r1; ++i) cnt[size_t(lev[size_t(i)]) + 1]++;
+        for (int l = 0; l < nls; ++l) cnt[size_t(l) + 1] += cnt[size_t(l)];
+        P.sysLvl0[size_t(s)] = int(P.lvlStart.size());
+        for (int l = 0; l <= nls; ++l) P.lvlStart.push_back(r0 + cnt[size_t(l)]);
+        for (int i = r0; i < r1; ++i) {
+            const int k = r0 + cnt[size_t(lev[size_t(i)])]++;
+            P.perm[size_t(k)] = i;
+            P.iperm[size_t(i)] = k;
+            levNew[size_t(k)] = lev[size_t(i)];
+        }
+        P.nlevF = std::max(P.nlevF, nls);
+    }
+    P.sysLvl0[size_t(nsys)] = int(P.lvlStart.size());
+    // permuted pattern (entry order inside a row preserved) and the block source map of the value gather
+    P.rowPtr.assign(size_t(n) + 1, 0);
+    P.col.resize(size_t(nnzb));
+    P.valSrc.resize(size_t(nnzb));
+    P.diag.assign(size_t(n), -1);
+    for (int k = 0; k < n; ++k) {
+        const int i = P.perm[size_t(k)];
+        int q = P.rowPtr[size_t(k)];
+        for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p, ++q) {
+            P.col[size_t(q)] = P.iperm[size_t(P.col0[size_t(p)])];
+            P.valSrc[size_t(q)] = p;
+            if (p == diag0[size_t(i)]) P.diag[size_t(k)] = q;
+        }
+        P.rowPtr[size_t(k) + 1] = q;
+    }
+    // structural symmetry (then the reversed forward levels are a topological order of the U dependencies)
     P.symmetric = true;
     for (int i = 0; i < n && P.symmetric; ++i)
-        for (int p = rowPtr[size_t(i)]; p < rowPtr[size_t(i) + 1]; ++p) {
-            const int j = P.col[size_t(p)];
-            const int* c0 = P.col.data() + rowPtr[size_t(j)];
-            const int* c1 = P.col.data() + rowPtr[size_t(j) + 1];
+        for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p) {
+            const int j = P.col0[size_t(p)];
+            const int* c0 = P.col0.data() + rowPtr0[size_t(j)];
+            const int* c1 = P.col0.data() + rowPtr0[size_t(j) + 1];
             if (!std::binary_search(c0, c1, i)) { P.symmetric = false; break; }
         }
+    // claim orders of the grid-wide sync-free kernels: all systems' rows by forward level
+    order_by_level(levNew, P.nlevF, P.ford);
     if (P.symmetric) {
         P.bord.assign(P.ford.rbegin(), P.ford.rend());
-        P.nlevB = nl;
+        P.nlevB = P.nlevF;
     } else {
         std::vector<int> blev(size_t(n), 0);
         int nb = 0;
-        for (int i = n - 1; i >= 0; --i) {
+        for (int i = n - 1; i >= 0; --i) {                 // original order: U entries point to larger rows
             int l = 0;
-            for (int p = P.diag[size_t(i)] + 1; p < rowPtr[size_t(i) + 1]; ++p) l = std::max(l, blev[size_t(P.col[size_t(p)])] + 1);
+            for (int p = diag0[size_t(i)] + 1; p < rowPtr0[size_t(i) + 1]; ++p) l = std::max(l, blev[size_t(P.col0[size_t(p)])] + 1);
             blev[size_t(i)] = l;
             nb = std::max(nb, l + 1);
         }
+        std::vector<int> blevNew(size_t(n), 0);
+        for (int k = 0; k < n; ++k) blevNew[size_t(k)] = blev[size_t(P.perm[size_t(k)])];
         P.nlevB = nb;
-        order_by_level(blev, nb, P.bord);
+        order_by_level(blevNew, nb, P.bord);
     }
-    // BILU0 elimination lists in the reference's order: lower entries p ascending, U entries q of row k ascending,
-    // target = the block of row i in the same column (engine/src/bsr.cpp:193-201)
+    // BILU0 elimination lists (engine/src/bsr.cpp:193-201): lower entries in row order, the U entries of the
+    // eliminating row in row order, target = the block of row i in the same column
     P.elimPtr.assign(size_t(nnzb) + 1, 0);
     P.elimT.clear(); P.elimQ.clear();
     std::vector<int> pos(size_t(n), -1);
     for (int i = 0; i < n; ++i) {
-        const int r0 = rowPtr[size_t(i)], r1 = rowPtr[size_t(i) + 1];
+        const int r0 = P.rowPtr[size_t(i)], r1 = P.rowPtr[size_t(i) + 1];
         for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = p;
         for (int p = r0; p < r1; ++p) {
-            const int k = P.col[size_t(p)];
-            if (k < i)
-                for (int q = P.diag[size_t(k)] + 1; q < rowPtr[size_t(k) + 1]; ++q) {
+            if (p < P.diag[size_t(i)]) {
+                const int k = P.col[size_t(p)];
+                for (int q = P.diag[size_t(k)] + 1; q < P.rowPtr[size_t(k) + 1]; ++q) {
                     const int t = pos[size_t(P.col[size_t(q)])];
                     if (t >= 0) { P.elimT.push_back(t); P.elimQ.push_back(q); }
                 }
+            }
             P.elimPtr[size_t(p) + 1] = int(P.elimT.size());
         }
         for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = -1;
@@ -119,35 +163,16 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     }
     P.sysTile0[size_t(nsys)] = int(P.tileSys.size());
     P.tileRow0.push_back(n);
-    // per-system level order (rows sorted by (forward level, row) inside each system) and the split L / U / D
-    // index arrays of the CTA-per-system sweeps; columns are local to the system
-    P.lrow.assign(size_t(n), 0);
-    P.lvlStart.clear();
-    P.sysLvl0.assign(size_t(nsys) + 1, 0);
-    P.maxSysRows = 0;
-    for (int s = 0; s < nsys; ++s) {
-        const int r0 = sysRow0[size_t(s)], r1 = sysRow0[size_t(s) + 1];
-        P.maxSysRows = std::max(P.maxSysRows, r1 - r0);
-        int nls = 0;
-        for (int i = r0; i < r1; ++i) nls = std::max(nls, lev[size_t(i)] + 1);
-        std::vector<int> cnt(size_t(nls) + 1, 0);
-        for (int i = r0; i < r1; ++i) cnt[size_t(lev[size_t(i)]) + 1]++;
-        for (int l = 0; l < nls; ++l) cnt[size_t(l) + 1] += cnt[size_t(l)];
-        P.sysLvl0[size_t(s)] = int(P.lvlStart.size());
-        for (int l = 0; l <= nls; ++l) P.lvlStart.push_back(r0 + cnt[size_t(l)]);
-        for (int i = r0; i < r1; ++i) P.lrow[size_t(r0 + cnt[size_t(lev[size_t(i)])]++)] = i;
-    }
-    P.sysLvl0[size_t(nsys)] = int(P.lvlStart.size());
+    // split L / U / D storage of the thread-block sweeps (rows of a level contiguous; columns local to the system)
     P.Lptr.assign(size_t(n) + 1, 0);
     P.Uptr.assign(size_t(n) + 1, 0);
     P.Dsrc.assign(size_t(n), 0);
     P.Lcol.clear(); P.Lsrc.clear(); P.Ucol.clear(); P.Usrc.clear();
     for (int k = 0; k < n; ++k) {
-        const int i = P.lrow[size_t(k)];
-        const int base = sysRow0[size_t(P.rowSys[size_t(i)])];
-        for (int p = rowPtr[size_t(i)]; p < P.diag[size_t(i)]; ++p) { P.Lcol.push_back(P.col[size_t(p)] - base); P.Lsrc.push_back(p); }
-        for (int p = P.diag[size_t(i)] + 1; p < rowPtr[size_t(i) + 1]; ++p) { P.Ucol.push_back(P.col[size_t(p)] - base); P.Usrc.push_back(p); }
-        P.Dsrc[size_t(k)] = P.diag[size_t(i)];
+        const int base = sysRow0[size_t(P.rowSys[size_t(k)])];
+        for (int p = P.rowPtr[size_t(k)]; p < P.diag[size_t(k)]; ++p) { P.Lcol.push_back(P.col[size_t(p)] - base); P.Lsrc.push_back(p); }
+        for (int p = P.diag[size_t(k)] + 1; p < P.rowPtr[size_t(k) + 1]; ++p) { P.Ucol.push_back(P.col[size_t(p)] - base); P.Usrc.push_back(p); }
+        P.Dsrc[size_t(k)] = P.diag[size_t(k)];
         P.Lptr[size_t(k) + 1] = int(P.Lcol.size());
         P.Uptr[size_t(k) + 1] = int(P.Ucol.size());
     }

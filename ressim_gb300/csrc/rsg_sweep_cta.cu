@@ -1,15 +1,19 @@
-// CTA-per-system BILU0 application: exact natural-order ILU(0) sweeps for systems that fit one SM.
+// Thread-block-per-system BILU0 application: exact natural-order ILU(0) sweeps for systems that fit one SM.
 //
 // One thread block owns one system of the (block-diagonal) batch and walks its forward levels with a block
 // barrier between levels, then the same levels in reverse for the backward sweep (valid for the structurally
-// symmetric patterns of reservoir Jacobians; the plan falls back to the grid-wide sync-free sweeps otherwise).
-// The sweep vector stays in shared memory between the two sweeps (FP32: up to ~19k block rows per system),
-// so every dependency read is a shared-memory read and the two sweeps are one kernel. Factors are read from
-// the level-ordered split storage (strict lower / strict upper / diagonal inverses, rows of a level contiguous).
+// symmetric patterns of reservoir Jacobians; otherwise the plan uses the grid-wide sync-free sweeps). Rows are
+// in level space, so a level is a contiguous range of rows, of input vector entries and of split factor blocks.
 //
-// FP64 arithmetic follows the reference loop order with unfused multiply / add (engine/src/bsr.cpp:565-587),
-// so the FP64 result is bitwise that of the reference's serial sweeps. FP32 follows BILU0f
-// (engine/src/bsr.cpp:1100-1121): float factors, float vector, float accumulation.
+// * The sweep vector y stays on chip between the two sweeps when it fits the block's shared memory (chosen per
+//   system at run time), else it lives in the output vector itself (L1 / L2).
+// * Each thread prefetches, one row ahead, the next row's input entries, row pointers, column indices and up to
+//   kPre factor blocks into registers: the global-memory latency of a level overlaps the previous level's work
+//   and barrier, and only the dependency reads of y stay on the critical path.
+// * TF = factor storage type, TV = sweep vector type. FP64 (double, double) and mixed (float factors, double
+//   vector: the reference's float-factor sweeps, engine/src/bsr.cpp:500-522) use unfused multiply / add in the
+//   reference loop order, so their results are bitwise those of the reference's serial sweeps on the same
+//   factors. (float, float) is the all-FP32 BILU0f sweep (engine/src/bsr.cpp:1100-1121).
 #include "rsg_impl.h"
 
 #include <cuda_runtime.h>
@@ -19,113 +23,198 @@ namespace rsg {
 namespace {
 
 constexpr int kCtaThreads = 256;
+constexpr int kPre = 3;                    // factor blocks per row prefetched into registers (7-point: all of L or U)
 
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 
-template <class T>
-struct Ar;
-template <>
-struct Ar<double> {
-    static __device__ __forceinline__ double dot3(const double* a, const double* x) {
-        return da(da(dm(__ldg(a), x[0]), dm(__ldg(a + 1), x[1])), dm(__ldg(a + 2), x[2]));
-    }
-    static __device__ __forceinline__ double sub(double a, double b) { return ds(a, b); }
-};
-template <>
-struct Ar<float> {
-    static __device__ __forceinline__ float dot3(const float* a, const float* x) {
-        float s = 0.f;
-        s += __ldg(a) * x[0];
-        s += __ldg(a + 1) * x[1];
-        s += __ldg(a + 2) * x[2];
-        return s;
-    }
-    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
-};
+// one row of a 3x3 block (factor type TF) times a 3-vector of type TV, accumulated from zero left to right
+__device__ __forceinline__ double rdot(const double* a, const double* x) { return da(da(dm(a[0], x[0]), dm(a[1], x[1])), dm(a[2], x[2])); }
+__device__ __forceinline__ double rdot(const float* a, const double* x) {
+    return da(da(dm(double(a[0]), x[0]), dm(double(a[1]), x[1])), dm(double(a[2]), x[2]));
+}
+__device__ __forceinline__ float rdot(const float* a, const float* x) {
+    float s = 0.f;
+    s += a[0] * x[0];
+    s += a[1] * x[1];
+    s += a[2] * x[2];
+    return s;
+}
+__device__ __forceinline__ double vsub(double a, double b) { return ds(a, b); }
+__device__ __forceinline__ float vsub(float a, float b) { return a - b; }
 
 enum { IN_PLAIN = 0, IN_PUPDATE = 1, IN_SUPDATE = 2 };
 
-// YSM: sweep vector in shared memory; otherwise (FP64 only) it lives in z itself.
-template <class T, int MODE, bool YSM>
+// registers holding one row's prefetched data
+template <class TF, int MODE>
+struct RowPre {
+    int k = -1, p0 = 0, p1 = 0;
+    int c[kPre];
+    TF a[kPre][9];
+    double in[MODE == IN_PUPDATE ? 9 : (MODE == IN_SUPDATE ? 6 : 3)];
+};
+template <class TF>
+struct RowPreB {
+    int k = -1, p0 = 0, p1 = 0;
+    int c[kPre];
+    TF a[kPre][9];
+    TF d[9];
+};
+
+template <class TF, int MODE>
+__device__ __forceinline__ void prefetch_fwd(RowPre<TF, MODE>& R, int k, const int* __restrict__ Lptr, const int* __restrict__ Lcol,
+                                             const TF* __restrict__ Lv, const double* r, const double* pv, const double* v) {
+    R.k = k;
+    if (k < 0) return;
+    R.p0 = __ldg(Lptr + k);
+    R.p1 = __ldg(Lptr + k + 1);
+#pragma unroll
+    for (int j = 0; j < kPre; ++j)
+        if (R.p0 + j < R.p1) {
+            R.c[j] = __ldg(Lcol + R.p0 + j);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) R.a[j][e] = __ldg(Lv + size_t(R.p0 + j) * 9 + e);
+        }
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const size_t q = size_t(k) * 3 + e;
+        R.in[e] = r[q];
+        if (MODE == IN_PUPDATE) { R.in[3 + e] = pv[q]; R.in[6 + e] = v[q]; }
+        if (MODE == IN_SUPDATE) R.in[3 + e] = v[q];
+    }
+}
+
+template <class TF>
+__device__ __forceinline__ void prefetch_bwd(RowPreB<TF>& R, int k, const int* __restrict__ Uptr, const int* __restrict__ Ucol,
+                                             const TF* __restrict__ Uv, const TF* __restrict__ Dv) {
+    R.k = k;
+    if (k < 0) return;
+    R.p0 = __ldg(Uptr + k);
+    R.p1 = __ldg(Uptr + k + 1);
+#pragma unroll
+    for (int j = 0; j < kPre; ++j)
+        if (R.p0 + j < R.p1) {
+            R.c[j] = __ldg(Ucol + R.p0 + j);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) R.a[j][e] = __ldg(Uv + size_t(R.p0 + j) * 9 + e);
+        }
+#pragma unroll
+    for (int e = 0; e < 9; ++e) R.d[e] = __ldg(Dv + size_t(k) * 9 + e);
+}
+
+template <class TF, class TV>
+__device__ __forceinline__ void sub_block(TV (&yi)[3], const TF* a, const TV* y, int c) {
+    const TV yc[3] = {y[c * 3 + 0], y[c * 3 + 1], y[c * 3 + 2]};
+    yi[0] = vsub(yi[0], rdot(a, yc));
+    yi[1] = vsub(yi[1], rdot(a + 3, yc));
+    yi[2] = vsub(yi[2], rdot(a + 6, yc));
+}
+
+// the thread's next row after row k of level L (the next one of the same level, else its first of level L+1)
+__device__ __forceinline__ int next_row(int k, int k1, int L, int nl, int l0, const int* __restrict__ lvlStart, int forward) {
+    if (k + int(blockDim.x) < k1) return k + int(blockDim.x);
+    const int Ln = forward ? L + 1 : L - 1;
+    if (Ln < 0 || Ln >= nl) return -1;
+    const int a = __ldg(lvlStart + l0 + Ln) + int(threadIdx.x);
+    return a < __ldg(lvlStart + l0 + Ln + 1) ? a : -1;
+}
+
+template <class TF, class TV, int MODE>
 __global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
-                                                        const int* __restrict__ lvlStart, const int* __restrict__ lrow,
-                                                        const int* __restrict__ Lptr, const int* __restrict__ Lcol,
-                                                        const T* __restrict__ Lv, const int* __restrict__ Uptr,
-                                                        const int* __restrict__ Ucol, const T* __restrict__ Uv,
-                                                        const T* __restrict__ Dv, const double* r, double* pv, const double* v,
-                                                        double* z, const KScal* ks) {
+                                                        const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
+                                                        const int* __restrict__ Lcol, const TF* __restrict__ Lv,
+                                                        const int* __restrict__ Uptr, const int* __restrict__ Ucol,
+                                                        const TF* __restrict__ Uv, const TF* __restrict__ Dv, const double* r, double* pv,
+                                                        const double* v, double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int s = blockIdx.x;
-    const int row0 = __ldg(sysRow0 + s);
+    const int row0 = __ldg(sysRow0 + s), ns = __ldg(sysRow0 + s + 1) - row0;
     double beta = 0, omega = 0, alpha = 0;
     if (ks) {
         const KScal& K = ks[s];
         if (K.status != ST_RUNNING) return;                // whole block: uniform
         beta = K.beta; omega = K.omega; alpha = K.alpha;
     }
-    T* y = YSM ? reinterpret_cast<T*>(smraw) : reinterpret_cast<T*>(z + size_t(row0) * 3);
+    // sweep vector: on chip when it fits, else global (yglob: z itself for TV = double)
+    const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
+    TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
     const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
-    // forward: y_i = in_i - sum_{k<i} L_ik y_k, level by level
+    const int tid = int(threadIdx.x);
+
+    // ---- forward: y_i = in_i - sum_{k<i} L_ik y_k (engine/src/bsr.cpp:568-575), level by level
+    RowPre<TF, MODE> cur, nxt;
+    {
+        const int a = nl > 0 ? __ldg(lvlStart + l0) + tid : -1;
+        prefetch_fwd(cur, (nl > 0 && a < __ldg(lvlStart + l0 + 1)) ? a : -1, Lptr, Lcol, Lv, r, pv, v);
+    }
     for (int L = 0; L < nl; ++L) {
-        const int k0 = __ldg(lvlStart + l0 + L), k1 = __ldg(lvlStart + l0 + L + 1);
-        for (int k = k0 + int(threadIdx.x); k < k1; k += blockDim.x) {
-            const int i = __ldg(lrow + k);
-            const int li = i - row0;
-            T yi[3];
+        const int k1 = __ldg(lvlStart + l0 + L + 1);
+        for (int k = __ldg(lvlStart + l0 + L) + tid; k < k1; k += blockDim.x) {
+            if (cur.k != k) prefetch_fwd(cur, k, Lptr, Lcol, Lv, r, pv, v);
+            prefetch_fwd(nxt, next_row(k, k1, L, nl, l0, lvlStart, 1), Lptr, Lcol, Lv, r, pv, v);
+            TV yi[3];
 #pragma unroll
             for (int e = 0; e < 3; ++e) {
-                const size_t q = size_t(i) * 3 + e;
+                const size_t q = size_t(k) * 3 + e;
                 if (MODE == IN_PUPDATE) {
-                    const double pe = da(r[q], dm(beta, ds(pv[q], dm(omega, v[q]))));   // engine/src/linsolve.cpp:173
+                    const double pe = da(cur.in[e], dm(beta, ds(cur.in[3 + e], dm(omega, cur.in[6 + e]))));   // linsolve.cpp:173
                     pv[q] = pe;
-                    yi[e] = T(pe);
+                    yi[e] = TV(pe);
                 } else if (MODE == IN_SUPDATE) {
-                    const double se = ds(r[q], dm(alpha, v[q]));                         // engine/src/linsolve.cpp:183
+                    const double se = ds(cur.in[e], dm(alpha, cur.in[3 + e]));                               // linsolve.cpp:183
                     pv[q] = se;
-                    yi[e] = T(se);
+                    yi[e] = TV(se);
                 } else {
-                    yi[e] = T(r[q]);
+                    yi[e] = TV(cur.in[e]);
                 }
             }
-            const int p1 = __ldg(Lptr + k + 1);
-            for (int p = __ldg(Lptr + k); p < p1; ++p) {
-                const int c = __ldg(Lcol + p);
-                const T yc[3] = {y[c * 3 + 0], y[c * 3 + 1], y[c * 3 + 2]};
-                const T* a = Lv + size_t(p) * 9;
-                yi[0] = Ar<T>::sub(yi[0], Ar<T>::dot3(a, yc));
-                yi[1] = Ar<T>::sub(yi[1], Ar<T>::dot3(a + 3, yc));
-                yi[2] = Ar<T>::sub(yi[2], Ar<T>::dot3(a + 6, yc));
+#pragma unroll
+            for (int j = 0; j < kPre; ++j)
+                if (cur.p0 + j < cur.p1) sub_block(yi, cur.a[j], y, cur.c[j]);
+            for (int p = cur.p0 + kPre; p < cur.p1; ++p) {     // long rows (well fill): the rest on demand
+                TF a[9];
+#pragma unroll
+                for (int e = 0; e < 9; ++e) a[e] = __ldg(Lv + size_t(p) * 9 + e);
+                sub_block(yi, a, y, __ldg(Lcol + p));
             }
+            const int li = k - row0;
             y[li * 3 + 0] = yi[0]; y[li * 3 + 1] = yi[1]; y[li * 3 + 2] = yi[2];
+            cur = nxt;
         }
         __syncthreads();
     }
-    // backward: z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j), levels in reverse
+
+    // ---- backward: z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j) (engine/src/bsr.cpp:577-587), levels in reverse
+    RowPreB<TF> bc, bn;
+    {
+        const int a = nl > 0 ? __ldg(lvlStart + l0 + nl - 1) + tid : -1;
+        prefetch_bwd(bc, (nl > 0 && a < __ldg(lvlStart + l0 + nl)) ? a : -1, Uptr, Ucol, Uv, Dv);
+    }
     for (int L = nl - 1; L >= 0; --L) {
-        const int k0 = __ldg(lvlStart + l0 + L), k1 = __ldg(lvlStart + l0 + L + 1);
-        for (int k = k0 + int(threadIdx.x); k < k1; k += blockDim.x) {
-            const int i = __ldg(lrow + k);
-            const int li = i - row0;
-            T yi[3] = {y[li * 3 + 0], y[li * 3 + 1], y[li * 3 + 2]};
-            const int p1 = __ldg(Uptr + k + 1);
-            for (int p = __ldg(Uptr + k); p < p1; ++p) {
-                const int c = __ldg(Ucol + p);
-                const T yc[3] = {y[c * 3 + 0], y[c * 3 + 1], y[c * 3 + 2]};
-                const T* a = Uv + size_t(p) * 9;
-                yi[0] = Ar<T>::sub(yi[0], Ar<T>::dot3(a, yc));
-                yi[1] = Ar<T>::sub(yi[1], Ar<T>::dot3(a + 3, yc));
-                yi[2] = Ar<T>::sub(yi[2], Ar<T>::dot3(a + 6, yc));
+        const int k1 = __ldg(lvlStart + l0 + L + 1);
+        for (int k = __ldg(lvlStart + l0 + L) + tid; k < k1; k += blockDim.x) {
+            if (bc.k != k) prefetch_bwd(bc, k, Uptr, Ucol, Uv, Dv);
+            prefetch_bwd(bn, next_row(k, k1, L, nl, l0, lvlStart, 0), Uptr, Ucol, Uv, Dv);
+            const int li = k - row0;
+            TV yi[3] = {y[li * 3 + 0], y[li * 3 + 1], y[li * 3 + 2]};
+#pragma unroll
+            for (int j = 0; j < kPre; ++j)
+                if (bc.p0 + j < bc.p1) sub_block(yi, bc.a[j], y, bc.c[j]);
+            for (int p = bc.p0 + kPre; p < bc.p1; ++p) {
+                TF a[9];
+#pragma unroll
+                for (int e = 0; e < 9; ++e) a[e] = __ldg(Uv + size_t(p) * 9 + e);
+                sub_block(yi, a, y, __ldg(Ucol + p));
             }
-            const T* d = Dv + size_t(k) * 9;
-            const T t0 = Ar<T>::dot3(d, yi), t1 = Ar<T>::dot3(d + 3, yi), t2 = Ar<T>::dot3(d + 6, yi);
+            const TV t0 = rdot(bc.d, yi), t1 = rdot(bc.d + 3, yi), t2 = rdot(bc.d + 6, yi);
             y[li * 3 + 0] = t0; y[li * 3 + 1] = t1; y[li * 3 + 2] = t2;
-            if (YSM) {
-                z[size_t(i) * 3 + 0] = double(t0);
-                z[size_t(i) * 3 + 1] = double(t1);
-                z[size_t(i) * 3 + 2] = double(t2);
+            if (onchip || sizeof(TV) != sizeof(double)) {
+                z[size_t(k) * 3 + 0] = double(t0);
+                z[size_t(k) * 3 + 1] = double(t1);
+                z[size_t(k) * 3 + 2] = double(t2);
             }
+            bc = bn;
         }
         __syncthreads();
     }
@@ -143,18 +232,6 @@ __global__ void k_pack(int n, int nL, int nU, const int* __restrict__ Lsrc, cons
     }
 }
 
-template <class T, int MODE, bool YSM>
-void launch_cta(const DevPlan& P, const SplitFactors<T>& F, size_t smem, const double* r, double* pv, const double* v, double* z,
-                const KScal* ks, cudaStream_t st) {
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_ilu_cta<T, MODE, YSM>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        configured = smem;
-    }
-    k_ilu_cta<T, MODE, YSM><<<P.nsys, kCtaThreads, smem, st>>>(P.sysRow0, P.sysLvl0, P.lvlStart, P.lrow, P.Lptr, P.Lcol, F.L, P.Uptr,
-                                                               P.Ucol, F.U, F.D, r, pv, v, z, ks);
-}
-
 int max_smem_optin() {
     static int v = 0;
     if (!v) {
@@ -166,16 +243,38 @@ int max_smem_optin() {
     return v;
 }
 
+template <class TF, class TV, int MODE>
+void launch_cta(const DevPlan& P, const TF* L, const TF* U, const TF* D, size_t smem, const double* r, double* pv, const double* v,
+                double* z, TV* yglob, const KScal* ks, cudaStream_t st) {
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaFuncSetAttribute(k_ilu_cta<TF, TV, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        configured = smem;
+    }
+    k_ilu_cta<TF, TV, MODE><<<P.nsys, kCtaThreads, smem, st>>>(P.sysRow0, P.sysLvl0, P.lvlStart, P.Lptr, P.Lcol, L, P.Uptr, P.Ucol, U, D,
+                                                               r, pv, v, z, yglob, smem, ks);
+}
+
+template <int MODE>
+void dispatch(const DevPlan& P, const PrecDev& M, const double* r, double* pv, const double* v, double* z, const KScal* ks,
+              cudaStream_t st) {
+    if (M.kind == 0) launch_cta<double, double, MODE>(P, M.s64.L, M.s64.U, M.s64.D, M.smem, r, pv, v, z, z, ks, st);
+    else if (M.kind == 1) launch_cta<float, double, MODE>(P, M.s32.L, M.s32.U, M.s32.D, M.smem, r, pv, v, z, z, ks, st);
+    else launch_cta<float, float, MODE>(P, M.s32.L, M.s32.U, M.s32.D, M.smem, r, pv, v, z, M.y32, ks, st);
+}
+
 }  // namespace
 
-size_t cta_sweep_smem(const DevPlan& P, bool fp32) {
-    const size_t need = size_t(P.maxSysRows) * 3 * (fp32 ? sizeof(float) : sizeof(double));
-    return need <= size_t(max_smem_optin()) ? need : 0;
+size_t cta_sweep_smem(const DevPlan& P, bool vec32) {
+    // the largest system's vector if it fits, else all the opt-in shared memory (systems that fit use it)
+    const size_t need = size_t(P.maxSysRows) * 3 * (vec32 ? sizeof(float) : sizeof(double));
+    const size_t cap = size_t(max_smem_optin());
+    return need <= cap ? need : cap;
 }
 
 bool cta_sweep_supported(const DevPlan& P, const HostPlan& H) {
     // structurally symmetric (reversed forward levels are backward levels) and small enough for one SM
-    return H.symmetric && P.maxSysRows > 0 && P.maxSysRows <= 32768;
+    return H.symmetric && P.maxSysRows > 0 && P.maxSysRows <= 65536;
 }
 
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st) {
@@ -189,25 +288,14 @@ void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F,
     k_pack<float><<<grid, 256, 0, st>>>(P.n, P.nL, P.nU, P.Lsrc, P.Usrc, P.Dsrc, luf, F.L, F.U, F.D);
 }
 
-// z = M^-1 r (plain input) -- the fused BiCGSTAB variants are launched by launch_ilu_cta_fused
 void launch_ilu_cta_apply(const DevPlan& P, const PrecDev& M, const double* r, double* z, cudaStream_t st) {
-    if (M.kind == 1) launch_cta<float, IN_PLAIN, true>(P, M.s32, M.smem, r, nullptr, nullptr, z, nullptr, st);
-    else if (M.smem) launch_cta<double, IN_PLAIN, true>(P, M.s64, M.smem, r, nullptr, nullptr, z, nullptr, st);
-    else launch_cta<double, IN_PLAIN, false>(P, M.s64, 0, r, nullptr, nullptr, z, nullptr, st);
+    dispatch<IN_PLAIN>(P, M, r, nullptr, nullptr, z, nullptr, st);
 }
 
 void launch_ilu_cta_fused(const DevPlan& P, const PrecDev& M, bool pupdate, const double* r, double* pv, const double* v, double* z,
                           const KScal* ks, cudaStream_t st) {
-    if (M.kind == 1) {
-        if (pupdate) launch_cta<float, IN_PUPDATE, true>(P, M.s32, M.smem, r, pv, v, z, ks, st);
-        else launch_cta<float, IN_SUPDATE, true>(P, M.s32, M.smem, r, pv, v, z, ks, st);
-    } else if (M.smem) {
-        if (pupdate) launch_cta<double, IN_PUPDATE, true>(P, M.s64, M.smem, r, pv, v, z, ks, st);
-        else launch_cta<double, IN_SUPDATE, true>(P, M.s64, M.smem, r, pv, v, z, ks, st);
-    } else {
-        if (pupdate) launch_cta<double, IN_PUPDATE, false>(P, M.s64, 0, r, pv, v, z, ks, st);
-        else launch_cta<double, IN_SUPDATE, false>(P, M.s64, 0, r, pv, v, z, ks, st);
-    }
+    if (pupdate) dispatch<IN_PUPDATE>(P, M, r, pv, v, z, ks, st);
+    else dispatch<IN_SUPDATE>(P, M, r, pv, v, z, ks, st);
 }
 
 }  // namespace rsg
