@@ -86,3 +86,20 @@ def test_synth_manufactured_rhs():
     S, bc = WellSchur(s.full, s.na, s.nv, s.nw).reduce(s.full_b)
     assert np.array_equal(S.rowPtr, s.A.rowPtr) and np.array_equal(S.col, s.A.col)
     assert np.allclose(S.val, s.A.val, rtol=1e-12, atol=1e-12 * np.abs(s.A.val).max())
+
+
+def test_reference_tools_compile_against_the_adapters():
+    """The reference's own tools/lsbench.cpp compiles with the supplied ressim/blocksolve.h, and the GpuBlockSolver
+    adapter compiles against the engine's own headers (only where the reference tree exists)."""
+    import shutil
+    import subprocess
+    ref = os.environ.get("RESSIM_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "engine", "include")) or not shutil.which("g++"):
+        pytest.skip("reference tree not present on this host")
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ref, "engine", "include")]
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", *inc, os.path.join(ref, "tools", "lsbench.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", *inc, "-x", "c++", os.path.join(ROOT, "include", "rsg_ressim_adapter.hpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
