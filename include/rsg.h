@@ -132,6 +132,20 @@ int rsg_get_factors(rsg_solver* h, double* lu);
 int rsg_spmv_level_probe(rsg_solver* h, int reps);
 int rsg_precond_level_probe(rsg_solver* h, int reps);
 
+/* Allocation-free fused block SpMV and inner product: d_y = A d_x and *d_dot = <d_w, d_y>, nb = 3, all pointers
+ * device pointers owned by the caller, launched asynchronously on `stream` (a cudaStream_t; NULL = legacy default).
+ * No counterpart in the reference: it exists for callers that cannot allocate device memory during a solve --
+ * hosts that hand the whole device memory to their own allocator up front (a simulator or ensemble driver that
+ * reserves its HBM budget at start-up) or that must not let a library call cudaMalloc, which may synchronise the
+ * device and stall their other streams. Its scratch (per-tile partial sums and an arrival counter) is a fixed
+ * 129 KiB array in the library's device memory, present on every device that loads the library; hence the limit of
+ * n <= 4,194,304 block rows (larger n returns RSG_EINVAL). The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress): make that first call before any stream capture. All calls share the array; the
+ * call clears its counter first, but calls that overlap on the GPU race: order them on one stream. It calls no
+ * cudaMalloc / cudaFree or other allocating routine. */
+int rsg_spmv_dot_noalloc(int n, int nb, const int* d_rowPtr, const int* d_col, const double* d_val, const double* d_x,
+                         double* d_y, const double* d_w, double* d_dot, void* stream);
+
 /* Statistics of the last setup / solve. */
 int rsg_get_stats(rsg_solver* h, rsg_stats* st);
 

@@ -23,7 +23,7 @@ EXPORTS = [
     "rsg_default_options", "rsg_last_error", "rsg_version", "rsg_create", "rsg_destroy", "rsg_set_matrix", "rsg_set_batch",
     "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
-    "rsg_spmv_level_probe", "rsg_precond_level_probe",
+    "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc",
 ]
 
 
@@ -75,6 +75,7 @@ def load(build_if_missing: bool = True):
     L.rsg_spmv_device.argtypes = [vp, vp, vp]
     L.rsg_precond_apply.argtypes = [vp, vp, vp]
     L.rsg_precond_apply_device.argtypes = [vp, vp, vp]
+    L.rsg_spmv_dot_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     L.rsg_spmv_level_probe.argtypes = [vp, C.c_int]
     L.rsg_precond_level_probe.argtypes = [vp, C.c_int]
     L.rsg_get_factors.argtypes = [vp, vp]

@@ -22,6 +22,15 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
+}  // namespace
+
+namespace rsg {
+// error text for entry points outside this file (thread-local, read by rsg_last_error)
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace rsg
+
+namespace {
+
 #define RSG_CUDA(call)                                                                                  \
     do {                                                                                                \
         cudaError_t e_ = (call);                                                                        \
