@@ -1,0 +1,341 @@
+// Host planning of the CPR pressure AMG (engine/src/amg.cpp:137-295): aggregation in the reference's natural
+// numbering, then every level mapped to its own "level space" for the device (rows renumbered by forward
+// Gauss-Seidel level, entries of a row in their natural order), together with the gather lists that let the
+// device recompute the Galerkin operators in the reference's summation order (AMG::refresh, amg.cpp:257-271).
+#include "rsg_impl.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace rsg {
+
+namespace {
+
+struct Csr {
+    int n = 0;
+    std::vector<int> rp, ci;
+    std::vector<double> v;
+};
+
+std::vector<int> diag_of(const Csr& A) {
+    std::vector<int> d(size_t(A.n), -1);
+    for (int i = 0; i < A.n; ++i)
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p)
+            if (A.ci[size_t(p)] == i) { d[size_t(i)] = p; break; }
+    return d;
+}
+
+// reference aggregation of one level (engine/src/amg.cpp:150-201); returns the number of aggregates
+int aggregate(const Csr& A, const std::vector<int>& dg, std::vector<int>& agg) {
+    const int n = A.n;
+    const double kTheta = 0.08, kRowTheta = 0.25;
+    std::vector<int> sp(size_t(n) + 1, 0), sc;
+    sc.reserve(A.ci.size());
+    for (int i = 0; i < n; ++i) {
+        double rowMax = 0;
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p)
+            if (A.ci[size_t(p)] != i) rowMax = std::max(rowMax, std::fabs(A.v[size_t(p)]));
+        const double di = A.v[size_t(dg[size_t(i)])];
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) {
+            const int j = A.ci[size_t(p)];
+            if (j == i) continue;
+            const double dj = A.v[size_t(dg[size_t(j)])];
+            if (std::fabs(A.v[size_t(p)]) >= kTheta * std::sqrt(std::fabs(di * dj)) || std::fabs(A.v[size_t(p)]) >= kRowTheta * rowMax)
+                sc.push_back(j);
+        }
+        sp[size_t(i) + 1] = int(sc.size());
+    }
+    agg.assign(size_t(n), -1);
+    int na = 0;
+    for (int i = 0; i < n; ++i) {                       // pass 1: roots with free strong neighbourhoods
+        if (agg[size_t(i)] >= 0) continue;
+        bool fr = true;
+        for (int p = sp[size_t(i)]; p < sp[size_t(i) + 1]; ++p)
+            if (agg[size_t(sc[size_t(p)])] >= 0) { fr = false; break; }
+        if (!fr || sp[size_t(i)] == sp[size_t(i) + 1]) continue;
+        agg[size_t(i)] = na;
+        for (int p = sp[size_t(i)]; p < sp[size_t(i) + 1]; ++p) agg[size_t(sc[size_t(p)])] = na;
+        ++na;
+    }
+    const std::vector<int> agg1 = agg;
+    for (int i = 0; i < n; ++i) {                       // pass 2: join the most strongly coupled pass-1 aggregate
+        if (agg[size_t(i)] >= 0) continue;
+        double best = 0;
+        int ba = -1;
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) {
+            const int j = A.ci[size_t(p)];
+            if (j != i && agg1[size_t(j)] >= 0 && std::fabs(A.v[size_t(p)]) > best) { best = std::fabs(A.v[size_t(p)]); ba = agg1[size_t(j)]; }
+        }
+        if (ba >= 0 && sp[size_t(i)] != sp[size_t(i) + 1]) agg[size_t(i)] = ba;
+    }
+    for (int i = 0; i < n; ++i) {                       // pass 3: leftovers start new aggregates
+        if (agg[size_t(i)] >= 0) continue;
+        agg[size_t(i)] = na;
+        for (int p = sp[size_t(i)]; p < sp[size_t(i) + 1]; ++p)
+            if (agg[size_t(sc[size_t(p)])] < 0) agg[size_t(sc[size_t(p)])] = na;
+        ++na;
+    }
+    return na;
+}
+
+// Galerkin A_c = P^T A P for an aggregation P, in the reference's order (engine/src/amg.cpp:37-70): AP(i, J) sums
+// row i's entries of aggregate column J in row order; A_c(I, J) sums AP(i, J) over the members i of I in ascending
+// order. Also returns the two gather lists (positions in A for AP, AP entries for A_c).
+struct Galerkin {
+    Csr AP, Ac;
+    std::vector<int> apPtr, apSrc;   // AP entry -> A positions
+    std::vector<int> acPtr, acSrc;   // A_c entry -> AP entries
+};
+void galerkin(const Csr& A, const std::vector<int>& agg, int na, Galerkin& G) {
+    const int n = A.n;
+    Csr& AP = G.AP;
+    AP.n = n;
+    AP.rp.assign(size_t(n) + 1, 0);
+    AP.ci.clear(); AP.v.clear();
+    G.apPtr.assign(1, 0); G.apSrc.clear();
+    std::vector<int> mark(size_t(na), -1);
+    std::vector<std::vector<int>> lists;
+    for (int i = 0; i < n; ++i) {
+        std::vector<std::pair<int, int>> cols;   // (J, slot in first-appearance order)
+        lists.clear();
+        std::vector<double> vals;
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) {
+            const int J = agg[size_t(A.ci[size_t(p)])];
+            if (mark[size_t(J)] < 0) { mark[size_t(J)] = int(cols.size()); cols.push_back({J, int(cols.size())}); lists.push_back({}); vals.push_back(A.v[size_t(p)]); }
+            else vals[size_t(mark[size_t(J)])] += A.v[size_t(p)];
+            lists[size_t(mark[size_t(J)])].push_back(p);
+        }
+        for (auto& c : cols) mark[size_t(c.first)] = -1;
+        std::sort(cols.begin(), cols.end());
+        for (auto& c : cols) {
+            AP.ci.push_back(c.first);
+            AP.v.push_back(vals[size_t(c.second)]);
+            for (int p : lists[size_t(c.second)]) G.apSrc.push_back(p);
+            G.apPtr.push_back(int(G.apSrc.size()));
+        }
+        AP.rp[size_t(i) + 1] = int(AP.ci.size());
+    }
+    // members of every aggregate in ascending row order (the rows of R = P^T)
+    std::vector<int> mPtr(size_t(na) + 1, 0), mem(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) mPtr[size_t(agg[size_t(i)]) + 1]++;
+    for (int I = 0; I < na; ++I) mPtr[size_t(I) + 1] += mPtr[size_t(I)];
+    {
+        std::vector<int> fill(mPtr.begin(), mPtr.end() - 1);
+        for (int i = 0; i < n; ++i) mem[size_t(fill[size_t(agg[size_t(i)])]++)] = i;
+    }
+    Csr& Ac = G.Ac;
+    Ac.n = na;
+    Ac.rp.assign(size_t(na) + 1, 0);
+    Ac.ci.clear(); Ac.v.clear();
+    G.acPtr.assign(1, 0); G.acSrc.clear();
+    for (int I = 0; I < na; ++I) {
+        std::vector<std::pair<int, int>> cols;
+        lists.clear();
+        std::vector<double> vals;
+        for (int q = mPtr[size_t(I)]; q < mPtr[size_t(I) + 1]; ++q) {
+            const int i = mem[size_t(q)];
+            for (int e = AP.rp[size_t(i)]; e < AP.rp[size_t(i) + 1]; ++e) {
+                const int J = AP.ci[size_t(e)];
+                if (mark[size_t(J)] < 0) { mark[size_t(J)] = int(cols.size()); cols.push_back({J, int(cols.size())}); lists.push_back({}); vals.push_back(AP.v[size_t(e)]); }
+                else vals[size_t(mark[size_t(J)])] += AP.v[size_t(e)];
+                lists[size_t(mark[size_t(J)])].push_back(e);
+            }
+        }
+        for (auto& c : cols) mark[size_t(c.first)] = -1;
+        std::sort(cols.begin(), cols.end());
+        bool haveDiag = false;
+        for (auto& c : cols) {
+            if (!haveDiag && c.first > I) {                  // inserted zero diagonal (engine/src/amg.cpp:83-91)
+                Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(int(G.acSrc.size())); haveDiag = true;
+            }
+            if (c.first == I) haveDiag = true;
+            Ac.ci.push_back(c.first);
+            Ac.v.push_back(vals[size_t(c.second)]);
+            for (int e : lists[size_t(c.second)]) G.acSrc.push_back(e);
+            G.acPtr.push_back(int(G.acSrc.size()));
+        }
+        if (!haveDiag) { Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(int(G.acSrc.size())); }
+        Ac.rp[size_t(I) + 1] = int(Ac.ci.size());
+    }
+}
+
+void fix_diag(Csr& A, const std::vector<int>& dg) {
+    for (int i = 0; i < A.n; ++i)
+        if (std::fabs(A.v[size_t(dg[size_t(i)])]) < 1e-300) A.v[size_t(dg[size_t(i)])] = 1.0;
+}
+
+// forward Gauss-Seidel levels of a natural-order CSR and the level-space renumbering of its rows
+void gs_levels(const Csr& A, const std::vector<int>& dg, std::vector<int>& perm, std::vector<int>& iperm, std::vector<int>& lvlStart) {
+    const int n = A.n;
+    std::vector<int> lev(size_t(n), 0);
+    int nl = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int p = A.rp[size_t(i)]; p < dg[size_t(i)]; ++p) l = std::max(l, lev[size_t(A.ci[size_t(p)])] + 1);
+        lev[size_t(i)] = l;
+        nl = std::max(nl, l + 1);
+    }
+    std::vector<int> cnt(size_t(nl) + 1, 0);
+    for (int i = 0; i < n; ++i) cnt[size_t(lev[size_t(i)]) + 1]++;
+    for (int l = 0; l < nl; ++l) cnt[size_t(l) + 1] += cnt[size_t(l)];
+    lvlStart = cnt;
+    perm.assign(size_t(n), 0);
+    iperm.assign(size_t(n), 0);
+    for (int i = 0; i < n; ++i) {
+        const int k = cnt[size_t(lev[size_t(i)])]++;
+        perm[size_t(k)] = i;
+        iperm[size_t(i)] = k;
+    }
+}
+
+}  // namespace
+
+// Builds the hierarchy of one system. ap0: values of the fine pressure matrix in the system's LEVEL-SPACE block
+// order (positions [bp0, bp1) of the block pattern); the level-space pattern and its original numbering come from
+// the solver plan. Levels l >= 1 are expressed in their own level space.
+bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, SysAmg& out, std::string& err) {
+    const int r0 = P.sysRow0[size_t(s)], r1 = P.sysRow0[size_t(s) + 1], n0 = r1 - r0;
+    const int b0 = P.rowPtr[size_t(r0)];
+    // natural-order fine matrix (original numbering of this system)
+    Csr A;
+    A.n = n0;
+    A.rp.assign(size_t(n0) + 1, 0);
+    std::vector<int> natPos;                     // natural position -> level-space position (relative to b0)
+    for (int io = 0; io < n0; ++io) {
+        const int k = P.iperm[size_t(r0 + io)];
+        for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p) {
+            A.ci.push_back(P.perm[size_t(P.col[size_t(p)])] - r0);
+            A.v.push_back(ap0[size_t(p - b0)]);
+            natPos.push_back(p - b0);
+        }
+        A.rp[size_t(io) + 1] = int(A.ci.size());
+    }
+    std::vector<int> dg = diag_of(A);
+    for (int i = 0; i < n0; ++i)
+        if (dg[size_t(i)] < 0) { err = "pressure matrix without a diagonal entry"; return false; }
+    fix_diag(A, dg);
+    out = SysAmg{};
+    // level 0 lives in the solver's level space (its GS levels are the BILU0 forward levels)
+    {
+        AmgLevel L0;
+        L0.n = n0;
+        L0.rp.assign(size_t(n0) + 1, 0);
+        for (int k = r0; k < r1; ++k) {
+            for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p) L0.ci.push_back(P.col[size_t(p)] - r0);
+            L0.rp[size_t(k - r0) + 1] = int(L0.ci.size());
+            L0.diag.push_back(P.diag[size_t(k)] - b0);
+        }
+        for (int q = P.sysLvl0[size_t(s)]; q < P.sysLvl0[size_t(s) + 1]; ++q) L0.lvlStart.push_back(P.lvlStart[size_t(q)] - r0);
+        L0.perm.resize(size_t(n0));
+        L0.iperm.resize(size_t(n0));
+        for (int k = 0; k < n0; ++k) { L0.perm[size_t(k)] = P.perm[size_t(r0 + k)] - r0; L0.iperm[size_t(L0.perm[size_t(k)])] = k; }
+        L0.val.assign(ap0.begin(), ap0.end());
+        for (int k = 0; k < n0; ++k)                                     // tiny diagonals -> 1 (engine/src/amg.cpp:145)
+            if (std::fabs(L0.val[size_t(L0.diag[size_t(k)])]) < 1e-300) L0.val[size_t(L0.diag[size_t(k)])] = 1.0;
+        out.lv.push_back(std::move(L0));
+    }
+    std::vector<int> natToLev0 = natPos;        // natural position -> level-space position of the current level
+    Csr cur = A;
+    std::vector<int> curDiag = dg;
+    while (true) {
+        if (cur.n <= 400 || int(out.lv.size()) >= 14) break;          // engine/src/amg.cpp:153
+        std::vector<int> agg;
+        const int na = aggregate(cur, curDiag, agg);
+        if (na >= int(0.85 * cur.n) || na < 1) break;                   // coarsening stalled
+        Galerkin G;
+        galerkin(cur, agg, na, G);
+        std::vector<int> cd = diag_of(G.Ac);
+        fix_diag(G.Ac, cd);
+        AmgLevel& F = out.lv.back();                                    // finer level (level space)
+        AmgLevel C;
+        C.n = na;
+        gs_levels(G.Ac, cd, C.perm, C.iperm, C.lvlStart);
+        // coarse level-space CSR (entries in natural order), values, diagonal positions
+        std::vector<int> cNat2Lev(G.Ac.ci.size());
+        C.rp.assign(size_t(na) + 1, 0);
+        for (int k = 0; k < na; ++k) {
+            const int I = C.perm[size_t(k)];
+            for (int p = G.Ac.rp[size_t(I)]; p < G.Ac.rp[size_t(I) + 1]; ++p) {
+                cNat2Lev[size_t(p)] = int(C.ci.size());
+                if (p == cd[size_t(I)]) C.diag.push_back(int(C.ci.size()));
+                C.ci.push_back(C.iperm[size_t(G.Ac.ci[size_t(p)])]);
+                C.val.push_back(G.Ac.v[size_t(p)]);
+            }
+            C.rp[size_t(k) + 1] = int(C.ci.size());
+        }
+        // transfer: fine level-space row -> coarse level-space row; members of each coarse row in ascending
+        // natural fine order (restriction order)
+        F.agg.assign(size_t(cur.n), 0);
+        for (int kf = 0; kf < cur.n; ++kf) F.agg[size_t(kf)] = C.iperm[size_t(agg[size_t(F.perm[size_t(kf)])])];
+        C.memPtr.assign(size_t(na) + 1, 0);
+        for (int i = 0; i < cur.n; ++i) C.memPtr[size_t(C.iperm[size_t(agg[size_t(i)])]) + 1]++;
+        for (int k = 0; k < na; ++k) C.memPtr[size_t(k) + 1] += C.memPtr[size_t(k)];
+        C.mem.assign(size_t(cur.n), 0);
+        {
+            std::vector<int> fill(C.memPtr.begin(), C.memPtr.end() - 1);
+            for (int i = 0; i < cur.n; ++i) C.mem[size_t(fill[size_t(C.iperm[size_t(agg[size_t(i)])])]++)] = F.iperm[size_t(i)];
+        }
+        // Galerkin gathers in level-space positions: AP entries (natural) <- finer level-space positions;
+        // coarse level-space entries <- AP entries
+        C.apPtr = G.apPtr;
+        C.apSrc.resize(G.apSrc.size());
+        for (size_t q = 0; q < G.apSrc.size(); ++q) C.apSrc[q] = natToLev0[size_t(G.apSrc[q])];
+        C.acPtr.assign(G.Ac.ci.size() + 1, 0);
+        C.acSrc.clear();
+        {
+            std::vector<int> order(G.Ac.ci.size());
+            for (size_t p = 0; p < order.size(); ++p) order[size_t(cNat2Lev[p])] = int(p);
+            for (size_t e = 0; e < order.size(); ++e) {
+                const int p = order[e];
+                for (int q = G.acPtr[size_t(p)]; q < G.acPtr[size_t(p) + 1]; ++q) C.acSrc.push_back(G.acSrc[size_t(q)]);
+                C.acPtr[e + 1] = int(C.acSrc.size());
+            }
+        }
+        natToLev0 = cNat2Lev;
+        cur = G.Ac;
+        curDiag = cd;
+        out.lv.push_back(std::move(C));
+    }
+    out.coarseDense = cur.n <= 800;
+    return true;
+}
+
+}  // namespace rsg
+
+namespace rsg {
+void set_last_error(const std::string& msg);
+}
+
+// Diagnostics: the AMG hierarchy the plan builds for a single BSR system and pressure-matrix values (original block
+// order), reported in each level's natural numbering. Level l: rows[l], nnz[l]; if l == which: its CSR (rp, ci, v)
+// and, for which == 0 and a coarser level present, the aggregate of every fine row.
+extern "C" int rsg_debug_amg_plan(int n, const int* rowPtr, const int* col, const double* ap, int which, int* levels, int* rows,
+                                  int* nnz, int maxLevels, int* rp, int* ci, double* v, int* agg) {
+    using namespace rsg;
+    std::vector<int> rp0(rowPtr, rowPtr + n + 1), ci0(col, col + rowPtr[n]), s0 = {0, n};
+    HostPlan P;
+    std::string err;
+    if (!build_plan(P, 1, s0, rp0, ci0, err)) { set_last_error(err); return -1; }
+    std::vector<double> ap0(size_t(P.nnzb));
+    for (int p = 0; p < P.nnzb; ++p) ap0[size_t(p)] = ap[P.valSrc[size_t(p)]];
+    SysAmg H;
+    if (!amg_plan_system(P, 0, ap0, H, err)) { set_last_error(err); return -1; }
+    *levels = int(H.lv.size());
+    for (int l = 0; l < int(H.lv.size()) && l < maxLevels; ++l) { rows[l] = H.lv[size_t(l)].n; nnz[l] = int(H.lv[size_t(l)].ci.size()); }
+    if (which >= 0 && which < int(H.lv.size())) {
+        const AmgLevel& L = H.lv[size_t(which)];
+        int c = 0;
+        rp[0] = 0;
+        for (int I = 0; I < L.n; ++I) {
+            const int k = L.iperm[size_t(I)];
+            for (int p = L.rp[size_t(k)]; p < L.rp[size_t(k) + 1]; ++p, ++c) { ci[c] = L.perm[size_t(L.ci[size_t(p)])]; v[c] = L.val[size_t(p)]; }
+            rp[I + 1] = c;
+        }
+        if (agg && which + 1 < int(H.lv.size())) {
+            const AmgLevel& C = H.lv[size_t(which) + 1];
+            for (int i = 0; i < L.n; ++i) agg[i] = C.perm[size_t(L.agg[size_t(L.iperm[size_t(i)])])];
+        }
+    }
+    return 0;
+}

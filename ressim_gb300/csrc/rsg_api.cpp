@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -92,6 +93,11 @@ struct rsg_solver {
     SplitFactors<double> s64;
     SplitFactors<float> s32;
     bool cta = false;
+    // CPR: device AMG of the batch (allocated in pmem; built at the first CPR set-up of a pattern)
+    DevAmg amg;
+    bool haveAmg = false;
+    int amgLevels = 0;
+    int* d_nfb = nullptr;
     // vectors
     BicgVecs V{};
     double *b = nullptr, *xout = nullptr, *tmp = nullptr;   // level-space b / x, original-order staging
@@ -126,6 +132,7 @@ void free_plan(rsg_solver* h) {
     h->dp = DevPlan{};
     h->val = nullptr; h->lu = nullptr; h->luf = nullptr; h->work = nullptr; h->dinv = nullptr;
     h->s64 = SplitFactors<double>{}; h->s32 = SplitFactors<float>{}; h->cta = false;
+    h->amg = DevAmg{}; h->haveAmg = false; h->amgLevels = 0; h->d_nfb = nullptr;
     h->V = BicgVecs{};
     h->b = h->xout = h->tmp = nullptr;
     h->S = SweepState{};
@@ -217,6 +224,7 @@ PrecDev prec_dev(rsg_solver* h) {
     else { M.kind = 0; M.lu = h->lu; }
     M.val = h->val;
     M.y32 = h->V.y32;
+    if (h->opt.precond == RSG_PREC_CPR && h->haveAmg) { M.cpr = true; M.amg = &h->amg; }
     if (M.kind != 2 && h->cta) {
         M.smem = cta_sweep_smem(h->dp, M.kind == 3);
         M.cta = true;
@@ -308,14 +316,176 @@ int ensure_precond_storage(rsg_solver* h) {
     return RSG_OK;
 }
 
+// Device layout of the batch's AMG hierarchies (level-major concatenation, see DevAmg) and its upload.
+int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
+    DevAmg& G = h->amg;
+    DevMem& M = h->pmem;
+    const int nsys = int(H.size());
+    int maxL = 0;
+    for (const auto& s : H) maxL = std::max(maxL, int(s.lv.size()));
+    G.nsys = nsys;
+    G.maxL = maxL;
+    std::vector<AmgSysLv> lv(size_t(nsys) * maxL);
+    int rows = 0, rps = 0, ents = 0, lvls = 0, mems = 0, aps = 0, lus = 0, lurows = 0;
+    G.levelEntBeg.assign(size_t(maxL) + 1, 0);
+    G.levelApBeg.assign(size_t(maxL) + 1, 0);
+    G.levelRowBeg.assign(size_t(maxL) + 1, 0);
+    std::vector<int> apOff(size_t(nsys) * maxL, 0);
+    for (int l = 0; l < maxL; ++l) {
+        G.levelEntBeg[size_t(l)] = ents;
+        G.levelApBeg[size_t(l)] = aps;
+        G.levelRowBeg[size_t(l)] = rows;
+        for (int s = 0; s < nsys; ++s) {
+            if (l >= int(H[size_t(s)].lv.size())) continue;
+            const AmgLevel& A = H[size_t(s)].lv[size_t(l)];
+            AmgSysLv& d = lv[size_t(s) * maxL + l];
+            d.n = A.n;
+            d.nnz = int(A.ci.size());
+            d.nl = int(A.lvlStart.size()) - 1;
+            d.rowOff = rows; d.rpOff = rps; d.entOff = ents; d.lvlOff = lvls; d.memOff = mems;
+            apOff[size_t(s) * maxL + l] = aps;
+            if (l == 0 && ents != h->plan.rowPtr[size_t(h->plan.sysRow0[size_t(s)])])
+                return fail(RSG_EINVAL, "internal: AMG level 0 does not match the block pattern");
+            rows += A.n; rps += A.n + 1; ents += d.nnz; lvls += d.nl + 1; mems += int(A.mem.size());
+            aps += l > 0 ? int(A.apPtr.size()) - 1 : 0;
+            if (l + 1 == int(H[size_t(s)].lv.size())) {
+                d.coarse = 1;
+                d.dense = H[size_t(s)].coarseDense ? 1 : 0;
+                if (d.dense) { d.luOff = lus; d.luRowOff = lurows; lus += A.n * A.n; lurows += A.n; }
+            }
+        }
+    }
+    G.levelEntBeg[size_t(maxL)] = ents;
+    G.levelApBeg[size_t(maxL)] = aps;
+    G.levelRowBeg[size_t(maxL)] = rows;
+    G.totRows = rows; G.totEnt = ents; G.nAP = aps; G.totLu = lus; G.totLuRows = lurows;
+    std::vector<int> rp(static_cast<size_t>(rps)), ci(static_cast<size_t>(ents)), dg(static_cast<size_t>(rows)),
+        lvl(static_cast<size_t>(lvls)), agg(static_cast<size_t>(rows), 0), memPtr(static_cast<size_t>(rps), 0),
+        mem(static_cast<size_t>(mems)), dgG(static_cast<size_t>(rows)), luPerm(static_cast<size_t>(std::max(lurows, 1)), 0);
+    std::vector<int> apPtr(size_t(aps) + 1, 0), apSrc, acPtr(size_t(ents) + 1, 0), acSrc;
+    for (int l = 0; l < maxL; ++l)
+        for (int s = 0; s < nsys; ++s) {
+            if (l >= int(H[size_t(s)].lv.size())) continue;
+            const AmgLevel& A = H[size_t(s)].lv[size_t(l)];
+            const AmgSysLv& d = lv[size_t(s) * maxL + l];
+            std::copy(A.rp.begin(), A.rp.end(), rp.begin() + d.rpOff);
+            std::copy(A.ci.begin(), A.ci.end(), ci.begin() + d.entOff);
+            std::copy(A.diag.begin(), A.diag.end(), dg.begin() + d.rowOff);
+            std::copy(A.lvlStart.begin(), A.lvlStart.end(), lvl.begin() + d.lvlOff);
+            for (int k = 0; k < A.n; ++k) dgG[size_t(d.rowOff + k)] = d.entOff + A.diag[size_t(k)];
+            if (!A.agg.empty()) std::copy(A.agg.begin(), A.agg.end(), agg.begin() + d.rowOff);
+            if (l > 0) {
+                const AmgSysLv& f = lv[size_t(s) * maxL + l - 1];
+                std::copy(A.memPtr.begin(), A.memPtr.end(), memPtr.begin() + d.rpOff);
+                std::copy(A.mem.begin(), A.mem.end(), mem.begin() + d.memOff);
+                const int a0 = apOff[size_t(s) * maxL + l];
+                for (size_t e = 0; e + 1 < A.apPtr.size(); ++e) {
+                    for (int q = A.apPtr[e]; q < A.apPtr[e + 1]; ++q) apSrc.push_back(f.entOff + A.apSrc[size_t(q)]);
+                    apPtr[size_t(a0) + e + 1] = int(apSrc.size());
+                }
+                for (int e = 0; e < d.nnz; ++e) {
+                    for (int q = A.acPtr[size_t(e)]; q < A.acPtr[size_t(e) + 1]; ++q) acSrc.push_back(a0 + A.acSrc[size_t(q)]);
+                    acPtr[size_t(d.entOff + e) + 1] = int(acSrc.size());
+                }
+            } else {
+                for (int e = 0; e < d.nnz; ++e) acPtr[size_t(d.entOff + e) + 1] = int(acSrc.size());
+            }
+            if (d.coarse && d.dense) std::copy(A.perm.begin(), A.perm.end(), luPerm.begin() + d.luRowOff);
+        }
+    // pointer arrays are prefix sums over the level-major order: fill gaps (levels absent for some systems)
+    for (size_t e = 1; e < apPtr.size(); ++e) apPtr[e] = std::max(apPtr[e], apPtr[e - 1]);
+    for (size_t e = 1; e < acPtr.size(); ++e) acPtr[e] = std::max(acPtr[e], acPtr[e - 1]);
+    if (apSrc.empty()) apSrc.push_back(0);
+    if (acSrc.empty()) acSrc.push_back(0);
+    int rc;
+    cudaStream_t st = h->stream;
+    if ((rc = dalloc(M, &G.lv, lv.size())) || (rc = upload(M, &G.rp, rp, st)) || (rc = upload(M, &G.ci, ci, st)) ||
+        (rc = upload(M, &G.diag, dg, st)) || (rc = upload(M, &G.lvl, lvl, st)) || (rc = upload(M, &G.agg, agg, st)) ||
+        (rc = upload(M, &G.memPtr, memPtr, st)) || (rc = upload(M, &G.mem, mem, st)) || (rc = upload(M, &G.apPtr, apPtr, st)) ||
+        (rc = upload(M, &G.apSrc, apSrc, st)) || (rc = upload(M, &G.acPtr, acPtr, st)) || (rc = upload(M, &G.acSrc, acSrc, st)) ||
+        (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)))
+        return rc;
+    RSG_CUDA(cudaMemcpyAsync(G.lv, lv.data(), lv.size() * sizeof(AmgSysLv), cudaMemcpyHostToDevice, st));
+    if ((rc = dalloc(M, &G.val, size_t(ents))) || (rc = dalloc(M, &G.valf, size_t(ents))) || (rc = dalloc(M, &G.apVal, size_t(std::max(aps, 1)))) ||
+        (rc = dalloc(M, &G.lu, size_t(std::max(lus, 1)))) || (rc = dalloc(M, &G.luf, size_t(std::max(lus, 1)))) ||
+        (rc = dalloc(M, &G.piv, size_t(std::max(lurows, 1)))) || (rc = dalloc(M, &G.x, size_t(rows))) || (rc = dalloc(M, &G.b, size_t(rows))) ||
+        (rc = dalloc(M, &G.r, size_t(rows))) || (rc = dalloc(M, &G.xf, size_t(rows))) || (rc = dalloc(M, &G.bf, size_t(rows))) ||
+        (rc = dalloc(M, &G.rf, size_t(rows))))
+        return rc;
+    h->amgLevels = maxL;
+    return RSG_OK;
+}
+
+// CPR set-up (BlockCPR::setup, engine/src/bsr.cpp:993-1059): weights, pressure matrix, hierarchy (host aggregation
+// at the first set-up of a pattern, device Galerkin refresh afterwards), coarsest dense LU
+int setup_cpr(rsg_solver* h, const double* acc) {
+    const HostPlan& P = h->plan;
+    const DevPlan& D = h->dp;
+    cudaStream_t st = h->stream;
+    int rc;
+    DevAmg& G = h->amg;
+    if (!G.w) {
+        if ((rc = dalloc(h->pmem, &G.w, size_t(P.n) * 3)) || (rc = dalloc(h->pmem, &G.T, size_t(P.n) * 3)) ||
+            (rc = dalloc(h->pmem, &G.acc, size_t(P.n) * 9)) || (rc = dalloc(h->pmem, &h->d_nfb, 1)))
+            return rc;
+    }
+    const double* accLev = nullptr;
+    if (acc) {   // caller's blocks in the original row order, staged through val0 (free after the value gather)
+        RSG_CUDA(cudaMemcpyAsync(h->val0, acc, size_t(P.n) * 9 * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_gather_acc(D, h->val0, G.acc, st);
+        accLev = G.acc;
+        h->launches += 1;
+    }
+    RSG_CUDA(cudaMemsetAsync(h->d_nfb, 0, sizeof(int), st));
+    launch_cpr_weights(D, h->val, accLev, G.w, h->d_nfb, st);
+    h->launches += 1;
+    if (!h->haveAmg) {
+        // first set-up of this pattern: the pressure matrix goes to the host for the aggregation
+        double* ap = nullptr;
+        if ((rc = dalloc(h->mem, &ap, size_t(P.nnzb)))) return rc;
+        launch_cpr_pressure(D, h->val, G.w, ap, st);
+        std::vector<double> hap(size_t(P.nnzb));
+        cudaError_t e = cudaMemcpyAsync(hap.data(), ap, hap.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        h->mem.release(ap);
+        if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("pressure matrix copy: ") + cudaGetErrorString(e));
+        std::vector<SysAmg> H(size_t(P.nsys));
+        std::vector<std::string> errs(size_t(P.nsys));
+        std::vector<char> ok(size_t(P.nsys), 1);
+        const int nth = std::max(1, std::min(P.nsys, int(std::thread::hardware_concurrency())));
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nth; ++t)
+            pool.emplace_back([&, t] {
+                for (int s = t; s < P.nsys; s += nth) {
+                    const int b0 = P.rowPtr[size_t(P.sysRow0[size_t(s)])], b1 = P.rowPtr[size_t(P.sysRow0[size_t(s) + 1])];
+                    std::vector<double> ap0(hap.begin() + b0, hap.begin() + b1);
+                    ok[size_t(s)] = amg_plan_system(P, s, ap0, H[size_t(s)], errs[size_t(s)]) ? 1 : 0;
+                }
+            });
+        for (auto& th : pool) th.join();
+        for (int s = 0; s < P.nsys; ++s)
+            if (!ok[size_t(s)]) return fail(RSG_EINVAL, "AMG set-up of system " + std::to_string(s) + ": " + errs[size_t(s)]);
+        if ((rc = build_dev_amg(h, H))) return rc;
+        h->haveAmg = true;
+    }
+    launch_cpr_pressure(D, h->val, G.w, G.val, st);          // level 0 of every system = the block pattern
+    launch_amg_refresh(G, st);
+    launch_amg_coarse_lu(G, h->opt.precision != RSG_FP64, st);
+    if (h->opt.precision != RSG_FP64) launch_amg_round(G, st);
+    h->launches += 3 + 3 * std::max(0, G.maxL - 1) + (h->opt.precision != RSG_FP64 ? 2 : 0);
+    RSG_CUDA(cudaGetLastError());
+    return RSG_OK;
+}
+
 int do_setup(rsg_solver* h, const double* acc) {
-    (void)acc;
     if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
-    if (h->opt.precond == RSG_PREC_CPR) return fail(RSG_EINVAL, "CPR preconditioner is not available in this build");
+    if (h->opt.precond == RSG_PREC_CPR && !h->cta)
+        return fail(RSG_EINVAL, "the CPR preconditioner needs structurally symmetric systems of <= 65536 block rows each");
     int rc = ensure_precond_storage(h);
     if (rc) return rc;
     RSG_CUDA(cudaMemsetAsync(h->d_nreg, 0, sizeof(int), h->stream));
     RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
+    if (h->opt.precond == RSG_PREC_CPR && (rc = setup_cpr(h, acc))) return rc;
     h->launches += 1;
     if (h->opt.precond == RSG_PREC_JACOBI) {
         launch_block_jacobi_setup(h->dp, h->val, h->dinv, h->d_nreg, h->stream);
@@ -337,6 +507,7 @@ int do_setup(rsg_solver* h, const double* acc) {
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->st.setup_ms = ms;
     h->st.regularised_blocks = h->h_pin[2];
+    h->st.amg_levels = h->opt.precond == RSG_PREC_CPR ? h->amgLevels : 0;
     h->haveSetup = true;
     return RSG_OK;
 }
@@ -592,7 +763,8 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
 // level-space r -> level-space z
 static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     const PrecDev M = prec_dev(h);
-    if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
+    if (M.cpr) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
+    else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
     else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
     else if (M.kind == 1) { launch_ilu_apply_mixed(h->dp, h->luf, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
     else if (M.kind == 3) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.y32, h->S, h->d_err, h->stream); h->launches += 2; }

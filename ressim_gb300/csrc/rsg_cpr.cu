@@ -1,0 +1,206 @@
+// CPR set-up on the device (BlockCPR::setup, engine/src/bsr.cpp:993-1059; AMG::refresh / factorCoarsest,
+// engine/src/amg.cpp:257-295): decoupling weights, pressure matrix, Galerkin values of the coarse levels in the
+// reference's summation order, and the dense LU of the coarsest level. All FP64 arithmetic explicitly rounded.
+#include "rsg_impl.h"
+#include "rsg_block3.cuh"
+
+#include <cuda_runtime.h>
+
+namespace rsg {
+
+namespace {
+
+int grid_for(size_t work) {
+    const size_t g = (work + 255) / 256, cap = size_t(device_sm_count()) * 16;
+    return int(g < cap ? (g > 0 ? g : 1) : cap);
+}
+
+__global__ void k_gather_acc(int n, const int* __restrict__ perm, const double* __restrict__ acc, double* out) {
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < size_t(n) * 9; q += size_t(gridDim.x) * blockDim.x)
+        out[q] = __ldg(acc + size_t(__ldg(perm + q / 9)) * 9 + q % 9);
+}
+
+// w_i = first row of D^-1, D = accumulation block when its 1-norm condition estimate is <= 1e10 (true IMPES),
+// else the Jacobian diagonal block (quasi IMPES); fallbacks as engine/src/bsr.cpp:1000-1040
+__global__ void k_cpr_weights(int n, const int* __restrict__ diag, const double* __restrict__ val, const double* __restrict__ acc,
+                              double* w, int* nfallback) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double D[9];
+    load9_ro(val + size_t(__ldg(diag + k)) * 9, D);
+    bool inverted = false;
+    if (acc) {
+        double B[9], inv[9];
+        load9_ro(acc + size_t(k) * 9, B);
+        for (int e = 0; e < 9; ++e) inv[e] = B[e];
+        if (invert3(inv)) {
+            double n1 = 0, ni = 0;
+            for (int j = 0; j < 3; ++j) {
+                double c = 0, d = 0;
+                for (int r = 0; r < 3; ++r) { c = da(c, fabs(B[r * 3 + j])); d = da(d, fabs(inv[r * 3 + j])); }
+                n1 = fmax(n1, c);
+                ni = fmax(ni, d);
+            }
+            if (dm(n1, ni) <= 1e10) { for (int e = 0; e < 9; ++e) D[e] = inv[e]; inverted = true; }
+            else atomicAdd(nfallback, 1);
+        } else {
+            atomicAdd(nfallback, 1);
+        }
+    }
+    double wk[3];
+    if (inverted || invert3(D)) {
+        wk[0] = D[0]; wk[1] = D[1]; wk[2] = D[2];
+    } else {
+        double s = 0;
+        const double* A = val + size_t(__ldg(diag + k)) * 9;
+        for (int e = 0; e < 3; ++e) s = da(s, __ldg(A + e * 3));
+        for (int e = 0; e < 3; ++e) wk[e] = fabs(s) > 1e-300 ? __ddiv_rn(1.0, s) : 1.0;
+    }
+    double wm = 0;
+    for (int e = 0; e < 3; ++e) wm = fmax(wm, fabs(wk[e]));
+    if (!(wm > 0) || !isfinite(wm)) wk[0] = wk[1] = wk[2] = 1.0;
+    w[size_t(k) * 3 + 0] = wk[0]; w[size_t(k) * 3 + 1] = wk[1]; w[size_t(k) * 3 + 2] = wk[2];
+}
+
+// Ap_ij = sum_e w_ie S_ij[e][0] on S's block pattern (engine/src/bsr.cpp:1044-1053), tiny diagonals -> 1
+__global__ void k_cpr_pressure(int n, const int* __restrict__ rowPtr, const int* __restrict__ diag, const double* __restrict__ val,
+                               const double* __restrict__ w, double* ap) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double w0 = w[size_t(k) * 3], w1 = w[size_t(k) * 3 + 1], w2 = w[size_t(k) * 3 + 2];
+    for (int p = __ldg(rowPtr + k); p < __ldg(rowPtr + k + 1); ++p) {
+        const double* a = val + size_t(p) * 9;
+        ap[p] = da(da(dm(w0, __ldg(a)), dm(w1, __ldg(a + 3))), dm(w2, __ldg(a + 6)));
+    }
+    const int d = __ldg(diag + k);
+    if (fabs(ap[d]) < 1e-300) ap[d] = 1.0;
+}
+
+// Galerkin refresh of one level: AP entries, then the level's entries, in the reference's order (first term
+// assigned, the others added)
+__global__ void k_gather_sum(int beg, int end, const int* __restrict__ ptr, const int* __restrict__ src, const double* __restrict__ in,
+                             double* out) {
+    for (int e = beg + int(blockIdx.x * blockDim.x + threadIdx.x); e < end; e += int(gridDim.x * blockDim.x)) {
+        const int q0 = __ldg(ptr + e), q1 = __ldg(ptr + e + 1);
+        double s = 0;
+        if (q0 < q1) {
+            s = in[__ldg(src + q0)];
+            for (int q = q0 + 1; q < q1; ++q) s = da(s, in[__ldg(src + q)]);
+        }
+        out[e] = s;
+    }
+}
+__global__ void k_diag_fix(int beg, int end, const int* __restrict__ diagGlob, double* val) {
+    for (int i = beg + int(blockIdx.x * blockDim.x + threadIdx.x); i < end; i += int(gridDim.x * blockDim.x)) {
+        const int d = __ldg(diagGlob + i);
+        if (fabs(val[d]) < 1e-300) val[d] = 1.0;
+    }
+}
+
+// dense LU with partial pivoting of every system's coarsest level in its natural numbering
+// (engine/src/amg.cpp:273-295); one thread block per system
+__global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                   const int* __restrict__ ci, const double* __restrict__ val,
+                                                   const int* __restrict__ luPerm, double* luAll, int* pivAll) {
+    const int s = blockIdx.x;
+    AmgSysLv L;
+    bool found = false;
+    for (int l = 0; l < maxL; ++l) {
+        const AmgSysLv c = lv[s * maxL + l];
+        if (c.n > 0 && c.coarse) { L = c; found = true; break; }
+    }
+    if (!found || !L.dense) return;
+    const int m = L.n;
+    double* lu = luAll + L.luOff;
+    int* piv = pivAll + L.luRowOff;
+    const int* nat = luPerm + L.luRowOff;
+    for (size_t q = threadIdx.x; q < size_t(m) * m; q += blockDim.x) lu[q] = 0.0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const int I = __ldg(nat + k);
+        for (int p = __ldg(rp + L.rpOff + k); p < __ldg(rp + L.rpOff + k + 1); ++p)
+            lu[size_t(I) * m + __ldg(nat + __ldg(ci + L.entOff + p))] = val[L.entOff + p];
+    }
+    __syncthreads();
+    __shared__ double smax[256];
+    __shared__ int sidx[256];
+    for (int k = 0; k < m; ++k) {
+        // pivot: first row with the largest |a_ik|, i >= k
+        double best = -1.0;
+        int bi = m;
+        for (int i = k + int(threadIdx.x); i < m; i += blockDim.x) {
+            const double a = fabs(lu[size_t(i) * m + k]);
+            if (a > best || (a == best && i < bi)) { best = a; bi = i; }
+        }
+        smax[threadIdx.x] = best;
+        sidx[threadIdx.x] = bi;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (int(threadIdx.x) < o) {
+                const double b2 = smax[threadIdx.x + o];
+                const int i2 = sidx[threadIdx.x + o];
+                if (b2 > smax[threadIdx.x] || (b2 == smax[threadIdx.x] && i2 < sidx[threadIdx.x])) { smax[threadIdx.x] = b2; sidx[threadIdx.x] = i2; }
+            }
+            __syncthreads();
+        }
+        // reference: pr starts at k and moves only on a strictly larger value -> first maximum
+        const int pr = (smax[0] > fabs(lu[size_t(k) * m + k])) ? sidx[0] : k;
+        __syncthreads();
+        if (threadIdx.x == 0) piv[k] = pr;
+        if (pr != k)
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                const double t = lu[size_t(k) * m + j];
+                lu[size_t(k) * m + j] = lu[size_t(pr) * m + j];
+                lu[size_t(pr) * m + j] = t;
+            }
+        __syncthreads();
+        if (threadIdx.x == 0 && fabs(lu[size_t(k) * m + k]) < 1e-300) lu[size_t(k) * m + k] = 1e-300;
+        __syncthreads();
+        const double dk = lu[size_t(k) * m + k];
+        for (int i = k + 1 + int(threadIdx.x); i < m; i += blockDim.x) lu[size_t(i) * m + k] = __ddiv_rn(lu[size_t(i) * m + k], dk);
+        __syncthreads();
+        const int w = m - k - 1;
+        for (size_t q = threadIdx.x; q < size_t(w) * w; q += blockDim.x) {
+            const int i = k + 1 + int(q / w), j = k + 1 + int(q % w);
+            const double f = lu[size_t(i) * m + k];
+            if (f != 0) lu[size_t(i) * m + j] = ds(lu[size_t(i) * m + j], dm(f, lu[size_t(k) * m + j]));
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_round(size_t n, const double* __restrict__ a, float* b) {
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += size_t(gridDim.x) * blockDim.x) b[q] = float(a[q]);
+}
+
+}  // namespace
+
+void launch_gather_acc(const DevPlan& P, const double* accOrig, double* accLev, cudaStream_t st) {
+    k_gather_acc<<<grid_for(size_t(P.n) * 9), 256, 0, st>>>(P.n, P.perm, accOrig, accLev);
+}
+void launch_cpr_weights(const DevPlan& P, const double* val, const double* accLev, double* w, int* nfallback, cudaStream_t st) {
+    k_cpr_weights<<<(P.n + 127) / 128, 128, 0, st>>>(P.n, P.diag, val, accLev, w, nfallback);
+}
+void launch_cpr_pressure(const DevPlan& P, const double* val, const double* w, double* ap, cudaStream_t st) {
+    k_cpr_pressure<<<(P.n + 127) / 128, 128, 0, st>>>(P.n, P.rowPtr, P.diag, val, w, ap);
+}
+void launch_amg_refresh(const DevAmg& G, cudaStream_t st) {
+    for (int l = 1; l < G.maxL; ++l) {
+        const int a0 = G.levelApBeg[size_t(l)], a1 = G.levelApBeg[size_t(l) + 1];
+        const int e0 = G.levelEntBeg[size_t(l)], e1 = G.levelEntBeg[size_t(l) + 1];
+        const int r0 = G.levelRowBeg[size_t(l)], r1 = G.levelRowBeg[size_t(l) + 1];
+        if (e1 <= e0) continue;
+        if (a1 > a0) k_gather_sum<<<grid_for(size_t(a1 - a0)), 256, 0, st>>>(a0, a1, G.apPtr, G.apSrc, G.val, G.apVal);
+        k_gather_sum<<<grid_for(size_t(e1 - e0)), 256, 0, st>>>(e0, e1, G.acPtr, G.acSrc, G.apVal, G.val);
+        k_diag_fix<<<grid_for(size_t(r1 - r0)), 256, 0, st>>>(r0, r1, G.diagGlob, G.val);
+    }
+}
+void launch_amg_coarse_lu(const DevAmg& G, bool fp32copy, cudaStream_t st) {
+    if (G.totLu > 0) k_coarse_lu<<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv);
+    if (fp32copy && G.totLu > 0) k_round<<<grid_for(size_t(G.totLu)), 256, 0, st>>>(size_t(G.totLu), G.lu, G.luf);
+}
+void launch_amg_round(const DevAmg& G, cudaStream_t st) {
+    k_round<<<grid_for(size_t(G.totEnt)), 256, 0, st>>>(size_t(G.totEnt), G.val, G.valf);
+}
+
+}  // namespace rsg

@@ -59,28 +59,76 @@ struct HostPlan {
     int maxSysRows = 0;
 };
 
+struct PrecDev;
+struct DevPlan;
 // Builds the plan of a (block-diagonal batch of) BSR pattern(s). Returns false with a message on bad input.
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
                 const std::vector<int>& col, std::string& err);
 
-// ---- AMG hierarchy (host set-up of the aggregation; engine/src/amg.cpp:137-252)
-struct HostCsr {
-    int n = 0, m = 0;                 // rows, columns
-    std::vector<int> rp, ci;
-    std::vector<double> v;
+// ---- CPR pressure AMG of one system (host plan; engine/src/amg.cpp:137-295). Every level is kept in its own level
+// space: rows renumbered by forward Gauss-Seidel level, entries of a row in their natural order.
+struct AmgLevel {
+    int n = 0;
+    std::vector<int> rp, ci, diag;     // level-space CSR and diagonal positions
+    std::vector<int> lvlStart;         // forward GS levels (level-space row ranges)
+    std::vector<int> perm, iperm;      // level space <-> natural numbering of the level
+    std::vector<double> val;           // values at plan time (the device recomputes them on every set-up)
+    std::vector<int> agg;              // all but the coarsest: level-space row -> coarse level-space row
+    std::vector<int> memPtr, mem;      // l >= 1: finer level-space members of each row, in restriction order
+    std::vector<int> apPtr, apSrc;     // l >= 1: AP entries <- finer-level positions (Galerkin, first product)
+    std::vector<int> acPtr, acSrc;     // l >= 1: this level's entries <- AP entries (Galerkin, second product)
 };
-struct HostAmgLevel {
-    HostCsr A;                        // level operator (square), diagonal present in every row
-    std::vector<int> diag;
-    std::vector<int> agg;             // coarse index of every row (empty on the coarsest level)
-    int nc = 0;
+struct SysAmg {
+    std::vector<AmgLevel> lv;
+    bool coarseDense = true;           // coarsest level <= 800 rows: dense solve (else 20 symmetric GS sweeps)
 };
-struct HostAmg {
-    std::vector<HostAmgLevel> lv;
+bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, SysAmg& out, std::string& err);
+
+// Device AMG of a batch: all arrays concatenated level-major (every system's level 0, then every system's level 1,
+// ...); indices inside a (system, level) are local. AmgSysLv[s * maxL + l] describes level l of system s.
+struct AmgSysLv {
+    int n = 0, nnz = 0, nl = 0;        // rows, entries, forward GS levels (n = 0: level absent)
+    int rowOff = 0;                    // rows: x, b, r, diag, agg, diagGlob
+    int rpOff = 0;                     // (n + 1) row pointers in rp, (n + 1) member pointers in memPtr
+    int entOff = 0;                    // entries: ci, val
+    int lvlOff = 0;                    // (nl + 1) GS level boundaries in lvl
+    int memOff = 0;                    // fine members of the rows (coarse levels) in mem
+    int coarse = 0;                    // 1 on the system's coarsest level
+    int dense = 0;                     // coarsest level solved by dense LU (else 20 symmetric GS sweeps)
+    int luOff = 0, luRowOff = 0;       // coarsest: dense LU (m*m) and pivots / natural order (m)
 };
-// Aggregation set-up of a pressure matrix (pattern + values); the Galerkin values of coarser levels are
-// produced on the device afterwards (rsg_amg_refresh on device) -- the host computes them too for the plan.
-void amg_setup_host(HostAmg& H, const HostCsr& A0);
+struct DevAmg {
+    int nsys = 0, maxL = 0;
+    int totRows = 0, totEnt = 0, totLu = 0, totLuRows = 0, nAP = 0;
+    std::vector<int> levelEntBeg, levelApBeg, levelRowBeg;   // host: per level l, [beg[l], beg[l+1]) ranges
+    AmgSysLv* lv = nullptr;
+    int *rp = nullptr, *ci = nullptr, *diag = nullptr, *lvl = nullptr;   // rp: (n+1) per (s,l) at rowOff + l
+    int *agg = nullptr, *memPtr = nullptr, *mem = nullptr;               // memPtr: (n+1) per coarse (s,l) at rowOff + l
+    int *apPtr = nullptr, *apSrc = nullptr, *acPtr = nullptr, *acSrc = nullptr;   // global indices
+    int *diagGlob = nullptr;           // global diagonal entry of every row (diagonal fix after the refresh)
+    int *luPerm = nullptr, *piv = nullptr;   // coarsest: level space -> natural, LU pivots
+    double* val = nullptr;             // entries of every level (level 0 = pressure matrix)
+    float* valf = nullptr;             // FP32 copy (mixed V-cycle)
+    double* apVal = nullptr;           // AP intermediate of the refresh
+    double* lu = nullptr;              // coarsest dense LU (FP64)
+    float* luf = nullptr;              // FP32 copy
+    double *x = nullptr, *b = nullptr, *r = nullptr;   // V-cycle vectors (every level)
+    float *xf = nullptr, *bf = nullptr, *rf = nullptr;
+    double* w = nullptr;               // CPR weights, level-space block rows of S (n * 3)
+    double* T = nullptr;               // second-stage input t = r - S[:,p] xp (n * 3)
+    double* acc = nullptr;             // accumulation blocks gathered into level space (n * 9), optional
+};
+// CPR set-up kernels (rsg_cpr.cu)
+void launch_cpr_weights(const DevPlan& P, const double* val, const double* accLev, double* w, int* nfallback, cudaStream_t st);
+void launch_cpr_pressure(const DevPlan& P, const double* val, const double* w, double* ap, cudaStream_t st);
+void launch_gather_acc(const DevPlan& P, const double* accOrig, double* accLev, cudaStream_t st);
+void launch_amg_refresh(const DevAmg& G, cudaStream_t st);           // Galerkin values of levels >= 1, diagonal fix
+void launch_amg_coarse_lu(const DevAmg& G, bool fp32copy, cudaStream_t st);
+void launch_amg_round(const DevAmg& G, cudaStream_t st);             // valf = float(val), luf = float(lu)
+// one CPR application per system (thread block per system), fused with the BiCGSTAB input update:
+// mode 0 plain (r -> z), 1 p-update, 2 s-update (as the BILU0 sweeps)
+void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, bool amgFp32, const double* r, double* pv,
+                    const double* v, double* z, const KScal* ks, cudaStream_t st);
 
 // ---- well Schur complement (engine/src/bsr.cpp:733-840, 973-990)
 int wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
@@ -161,6 +209,8 @@ struct PrecDev {
     SplitFactors<float> s32;
     size_t smem = 0;                  // dynamic shared memory of the CTA sweep (systems whose vector fits keep it there)
     float* y32 = nullptr;             // all-FP32 sweep vector in global memory (systems that do not fit on chip)
+    bool cpr = false;                 // CPR two-stage preconditioner (AMG on the pressure system + BILU0)
+    const DevAmg* amg = nullptr;
 };
 // gather the factors (original block layout) into the level-ordered split layout
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st);

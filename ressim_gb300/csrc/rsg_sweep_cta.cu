@@ -17,6 +17,7 @@
 #include "rsg_impl.h"
 
 #include <cuda_runtime.h>
+#include <type_traits>
 
 namespace rsg {
 
@@ -120,28 +121,13 @@ __device__ __forceinline__ int next_row(int k, int k1, int L, int nl, int l0, co
     return a < __ldg(lvlStart + l0 + Ln + 1) ? a : -1;
 }
 
+// Both sweeps of one system by the calling thread block (y: the sweep vector of this system, on chip or in z).
 template <class TF, class TV, int MODE>
-__global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
-                                                        const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
-                                                        const int* __restrict__ Lcol, const TF* __restrict__ Lv,
-                                                        const int* __restrict__ Uptr, const int* __restrict__ Ucol,
-                                                        const TF* __restrict__ Uv, const TF* __restrict__ Dv, const double* r, double* pv,
-                                                        const double* v, double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    const int s = blockIdx.x;
-    const int row0 = __ldg(sysRow0 + s), ns = __ldg(sysRow0 + s + 1) - row0;
-    double beta = 0, omega = 0, alpha = 0;
-    if (ks) {
-        const KScal& K = ks[s];
-        if (K.status != ST_RUNNING) return;                // whole block: uniform
-        beta = K.beta; omega = K.omega; alpha = K.alpha;
-    }
-    // sweep vector: on chip when it fits, else global (yglob: z itself for TV = double)
-    const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
-    TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
-    const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
+__device__ void ilu_body(int row0, int l0, int nl, const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
+                         const int* __restrict__ Lcol, const TF* __restrict__ Lv, const int* __restrict__ Uptr,
+                         const int* __restrict__ Ucol, const TF* __restrict__ Uv, const TF* __restrict__ Dv, const double* r, double* pv,
+                         const double* v, double* z, TV* y, bool writeZ, double beta, double omega, double alpha) {
     const int tid = int(threadIdx.x);
-
     // ---- forward: y_i = in_i - sum_{k<i} L_ik y_k (engine/src/bsr.cpp:568-575), level by level
     RowPre<TF, MODE> cur, nxt;
     {
@@ -184,7 +170,6 @@ __global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__
         }
         __syncthreads();
     }
-
     // ---- backward: z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j) (engine/src/bsr.cpp:577-587), levels in reverse
     RowPreB<TF> bc, bn;
     {
@@ -209,7 +194,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__
             }
             const TV t0 = rdot(bc.d, yi), t1 = rdot(bc.d + 3, yi), t2 = rdot(bc.d + 6, yi);
             y[li * 3 + 0] = t0; y[li * 3 + 1] = t1; y[li * 3 + 2] = t2;
-            if (onchip || sizeof(TV) != sizeof(double)) {
+            if (writeZ) {
                 z[size_t(k) * 3 + 0] = double(t0);
                 z[size_t(k) * 3 + 1] = double(t1);
                 z[size_t(k) * 3 + 2] = double(t2);
@@ -219,6 +204,233 @@ __global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__
         __syncthreads();
     }
 }
+
+template <class TF, class TV, int MODE>
+__global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
+                                                        const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
+                                                        const int* __restrict__ Lcol, const TF* __restrict__ Lv,
+                                                        const int* __restrict__ Uptr, const int* __restrict__ Ucol,
+                                                        const TF* __restrict__ Uv, const TF* __restrict__ Dv, const double* r, double* pv,
+                                                        const double* v, double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int s = blockIdx.x;
+    const int row0 = __ldg(sysRow0 + s), ns = __ldg(sysRow0 + s + 1) - row0;
+    double beta = 0, omega = 0, alpha = 0;
+    if (ks) {
+        const KScal& K = ks[s];
+        if (K.status != ST_RUNNING) return;                // whole block: uniform
+        beta = K.beta; omega = K.omega; alpha = K.alpha;
+    }
+    // sweep vector: on chip when it fits, else global (yglob: z itself for TV = double)
+    const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
+    TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
+    const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
+    ilu_body<TF, TV, MODE>(row0, l0, nl, lvlStart, Lptr, Lcol, Lv, Uptr, Ucol, Uv, Dv, r, pv, v, z, y,
+                           onchip || sizeof(TV) != sizeof(double), beta, omega, alpha);
+}
+
+// ------------------------------------------------------------------ CPR (BlockCPR::apply, engine/src/bsr.cpp:1061-1084)
+struct AmgArgs {
+    const AmgSysLv* lv;
+    int maxL;
+    const int *rp, *ci, *diag, *lvl, *agg, *memPtr, *mem, *luPerm, *piv;
+};
+
+// V-cycle arithmetic type: FP64 explicitly rounded (bitwise the reference) or FP32
+__device__ __forceinline__ double amul(double a, double b) { return dm(a, b); }
+__device__ __forceinline__ double aadd(double a, double b) { return da(a, b); }
+__device__ __forceinline__ double asub(double a, double b) { return ds(a, b); }
+__device__ __forceinline__ double adiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float amul(float a, float b) { return a * b; }
+__device__ __forceinline__ float aadd(float a, float b) { return a + b; }
+__device__ __forceinline__ float asub(float a, float b) { return a - b; }
+__device__ __forceinline__ float adiv(float a, float b) { return a / b; }
+
+// Gauss-Seidel sweep of one level (engine/src/amg.cpp:98-113) over its GS levels: forward from x = 0 (only the
+// lower entries contribute, bitwise the full sum), or forward / backward from the current x (full rows: entries of
+// later rows still hold the old x). Rows of one GS level are independent.
+template <class TA>
+__device__ void gs_sweep(const AmgSysLv& A, const AmgArgs& G, const TA* __restrict__ val, TA* x, const TA* b, bool forward, bool fromZero) {
+    const int* rp = G.rp + A.rpOff;
+    const int* ci = G.ci + A.entOff;
+    const int* dg = G.diag + A.rowOff;
+    const int* lv = G.lvl + A.lvlOff;
+    const TA* v = val + A.entOff;
+    for (int g = 0; g < A.nl; ++g) {
+        const int L = forward ? g : A.nl - 1 - g;
+        const int k1 = __ldg(lv + L + 1);
+        for (int k = __ldg(lv + L) + int(threadIdx.x); k < k1; k += blockDim.x) {
+            const int d = __ldg(dg + k);
+            const int pe = fromZero ? d : __ldg(rp + k + 1);
+            TA s = b[k];
+            for (int p = __ldg(rp + k); p < pe; ++p)
+                if (p != d) s = asub(s, amul(v[p], x[__ldg(ci + p)]));
+            x[k] = adiv(s, v[d]);
+        }
+        __syncthreads();
+    }
+}
+
+// coarsest level: x = LU^-1 b with the dense LU of the natural numbering (engine/src/amg.cpp:306-312), one warp;
+// work = the level's residual vector, used in natural order
+template <class TA>
+__device__ void coarse_solve(const AmgSysLv& A, const AmgArgs& G, const TA* __restrict__ luAll, TA* x, const TA* b, TA* work) {
+    const int m = A.n;
+    const TA* lu = luAll + A.luOff;
+    const int* nat = G.luPerm + A.luRowOff;
+    const int* piv = G.piv + A.luRowOff;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int k = lane; k < m; k += 32) work[__ldg(nat + k)] = b[k];
+        __syncwarp();
+        if (lane == 0)
+            for (int k = 0; k < m; ++k) {
+                const int pk = __ldg(piv + k);
+                if (pk != k) { const TA t = work[k]; work[k] = work[pk]; work[pk] = t; }
+            }
+        __syncwarp();
+        for (int j = 0; j < m; ++j) {                    // unit lower: every row gets its terms in ascending j
+            const TA xj = work[j];
+            for (int i = j + 1 + lane; i < m; i += 32) work[i] = asub(work[i], amul(lu[size_t(i) * m + j], xj));
+            __syncwarp();
+        }
+        for (int j = m - 1; j >= 0; --j) {               // upper
+            if (lane == 0) work[j] = adiv(work[j], lu[size_t(j) * m + j]);
+            __syncwarp();
+            const TA xj = work[j];
+            for (int i = lane; i < j; i += 32) work[i] = asub(work[i], amul(lu[size_t(i) * m + j], xj));
+            __syncwarp();
+        }
+        for (int k = lane; k < m; k += 32) x[k] = work[__ldg(nat + k)];
+    }
+    __syncthreads();
+}
+
+// AMG::cycle (engine/src/amg.cpp:303-329) for system s, level 0 rhs in b + lv[0].rowOff
+template <class TA>
+__device__ void vcycle(int s, const AmgArgs& G, const TA* __restrict__ val, const TA* __restrict__ lu, TA* x, TA* b, TA* r) {
+    int nlev = 0;
+    while (nlev < G.maxL && G.lv[s * G.maxL + nlev].n > 0) ++nlev;
+    int l = 0;
+    for (; l < nlev; ++l) {
+        const AmgSysLv A = G.lv[s * G.maxL + l];
+        TA* xl = x + A.rowOff;
+        TA* bl = b + A.rowOff;
+        TA* rl = r + A.rowOff;
+        if (A.coarse) {
+            if (A.dense) {
+                coarse_solve(A, G, lu, xl, bl, rl);
+            } else {                                      // 20 symmetric GS sweeps from x = 0 (amg.cpp:313-315)
+                for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = TA(0);
+                __syncthreads();
+                for (int it = 0; it < 20; ++it) {
+                    gs_sweep(A, G, val, xl, bl, true, false);
+                    gs_sweep(A, G, val, xl, bl, false, false);
+                }
+            }
+            break;
+        }
+        gs_sweep(A, G, val, xl, bl, true, true);
+        // residual r = b - A x (amg.cpp:321-322)
+        {
+            const int* rp = G.rp + A.rpOff;
+            const int* ci = G.ci + A.entOff;
+            const TA* v = val + A.entOff;
+            for (int k = threadIdx.x; k < A.n; k += blockDim.x) {
+                TA t = TA(0);
+                for (int p = __ldg(rp + k); p < __ldg(rp + k + 1); ++p) t = aadd(t, amul(v[p], xl[__ldg(ci + p)]));
+                rl[k] = asub(bl[k], t);
+            }
+        }
+        __syncthreads();
+        // restriction b_{l+1} = R r: members in ascending natural order (amg.cpp:324)
+        {
+            const AmgSysLv C = G.lv[s * G.maxL + l + 1];
+            const int* mp = G.memPtr + C.rpOff;
+            const int* mem = G.mem + C.memOff;
+            TA* bc = b + C.rowOff;
+            for (int I = threadIdx.x; I < C.n; I += blockDim.x) {
+                TA t = TA(0);
+                for (int q = __ldg(mp + I); q < __ldg(mp + I + 1); ++q) t = aadd(t, rl[__ldg(mem + q)]);
+                bc[I] = t;
+            }
+        }
+        __syncthreads();
+    }
+    for (l = l - 1; l >= 0; --l) {                          // prolongation and post-smoothing (amg.cpp:326-327)
+        const AmgSysLv A = G.lv[s * G.maxL + l];
+        const AmgSysLv C = G.lv[s * G.maxL + l + 1];
+        TA* xl = x + A.rowOff;
+        const TA* xc = x + C.rowOff;
+        const int* agg = G.agg + A.rowOff;
+        for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = aadd(xl[k], xc[__ldg(agg + k)]);
+        __syncthreads();
+        gs_sweep(A, G, val, xl, b + A.rowOff, false, false);
+    }
+}
+
+template <class TF, class TV, class TA, int MODE>
+__global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
+                                                        const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
+                                                        const int* __restrict__ Lcol, const TF* __restrict__ Lv,
+                                                        const int* __restrict__ Uptr, const int* __restrict__ Ucol,
+                                                        const TF* __restrict__ Uv, const TF* __restrict__ Dv,
+                                                        const int* __restrict__ rowPtr, const int* __restrict__ col,
+                                                        const double* __restrict__ val, const double* __restrict__ w, double* T,
+                                                        AmgArgs G, const TA* __restrict__ aval, const TA* __restrict__ alu, TA* ax, TA* ab,
+                                                        TA* ar, const double* r, double* pv, const double* v, double* z, TV* yglob,
+                                                        size_t smemBytes, const KScal* ks) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int s = blockIdx.x;
+    const int row0 = __ldg(sysRow0 + s), ns = __ldg(sysRow0 + s + 1) - row0;
+    double beta = 0, omega = 0, alpha = 0;
+    if (ks) {
+        const KScal& K = ks[s];
+        if (K.status != ST_RUNNING) return;
+        beta = K.beta; omega = K.omega; alpha = K.alpha;
+    }
+    const AmgSysLv A0 = G.lv[s * G.maxL];
+    TA* b0 = ab + A0.rowOff;
+    const TA* xp = ax + A0.rowOff;
+    // input (fused Krylov update) and pressure restriction rp = w . r (bsr.cpp:1064-1067)
+    for (int k = row0 + int(threadIdx.x); k < row0 + ns; k += blockDim.x) {
+        double in[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const size_t q = size_t(k) * 3 + e;
+            if (MODE == IN_PUPDATE) { in[e] = da(r[q], dm(beta, ds(pv[q], dm(omega, v[q])))); pv[q] = in[e]; }
+            else if (MODE == IN_SUPDATE) { in[e] = ds(r[q], dm(alpha, v[q])); pv[q] = in[e]; }
+            else in[e] = r[q];
+            T[q] = in[e];
+        }
+        const double* wk = w + size_t(k) * 3;
+        b0[k - row0] = TA(da(da(dm(wk[0], in[0]), dm(wk[1], in[1])), dm(wk[2], in[2])));
+    }
+    __syncthreads();
+    vcycle<TA>(s, G, aval, alu, ax, ab, ar);
+    // second stage on t = r - S[:,p] xp (pressure column only, bsr.cpp:1071-1081)
+    for (int k = row0 + int(threadIdx.x); k < row0 + ns; k += blockDim.x) {
+        double acc[3] = {T[size_t(k) * 3], T[size_t(k) * 3 + 1], T[size_t(k) * 3 + 2]};
+        for (int p = __ldg(rowPtr + k); p < __ldg(rowPtr + k + 1); ++p) {
+            const double xk = double(xp[__ldg(col + p) - row0]);
+            const double* B = val + size_t(p) * 9;
+            acc[0] = ds(acc[0], dm(__ldg(B), xk));
+            acc[1] = ds(acc[1], dm(__ldg(B + 3), xk));
+            acc[2] = ds(acc[2], dm(__ldg(B + 6), xk));
+        }
+        T[size_t(k) * 3] = acc[0]; T[size_t(k) * 3 + 1] = acc[1]; T[size_t(k) * 3 + 2] = acc[2];
+    }
+    __syncthreads();
+    const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
+    TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
+    const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
+    ilu_body<TF, TV, IN_PLAIN>(row0, l0, nl, lvlStart, Lptr, Lcol, Lv, Uptr, Ucol, Uv, Dv, T, nullptr, nullptr, z, y,
+                               onchip || sizeof(TV) != sizeof(double), 0, 0, 0);
+    // z_p += xp (bsr.cpp:1083)
+    for (int k = row0 + int(threadIdx.x); k < row0 + ns; k += blockDim.x) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xp[k - row0]));
+}
+
+
 
 template <class T>
 __global__ void k_pack(int n, int nL, int nU, const int* __restrict__ Lsrc, const int* __restrict__ Usrc, const int* __restrict__ Dsrc,
@@ -296,6 +508,48 @@ void launch_ilu_cta_fused(const DevPlan& P, const PrecDev& M, bool pupdate, cons
                           const KScal* ks, cudaStream_t st) {
     if (pupdate) dispatch<IN_PUPDATE>(P, M, r, pv, v, z, ks, st);
     else dispatch<IN_SUPDATE>(P, M, r, pv, v, z, ks, st);
+}
+
+}  // namespace rsg
+
+namespace rsg {
+namespace {
+template <class TF, class TV, class TA, int MODE>
+void launch_cpr_t(const DevPlan& P, const double* Sval, const TF* Lf, const TF* Uf, const TF* Df, size_t smem, const DevAmg& G, const TA* aval, const TA* alu,
+                  TA* ax, TA* ab, TA* ar, const double* r, double* pv, const double* v, double* z, TV* yglob, const KScal* ks,
+                  cudaStream_t st) {
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaFuncSetAttribute(k_cpr_cta<TF, TV, TA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        configured = smem;
+    }
+    AmgArgs A{G.lv, G.maxL, G.rp, G.ci, G.diag, G.lvl, G.agg, G.memPtr, G.mem, G.luPerm, G.piv};
+    k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, kCtaThreads, smem, st>>>(P.sysRow0, P.sysLvl0, P.lvlStart, P.Lptr, P.Lcol, Lf, P.Uptr, P.Ucol, Uf,
+                                                                  Df, P.rowPtr, P.col, Sval, G.w, G.T, A, aval, alu, ax, ab, ar, r,
+                                                                  pv, v, z, yglob, smem, ks);
+}
+}  // namespace
+
+void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, bool amgFp32, const double* r, double* pv,
+                    const double* v, double* z, const KScal* ks, cudaStream_t st) {
+    (void)amgFp32;
+    const double* S = M.val;
+    auto go = [&](auto tag_mode) {
+        constexpr int MODE = decltype(tag_mode)::value;
+        if (M.kind == 0)
+            launch_cpr_t<double, double, double, MODE>(P, S, M.s64.L, M.s64.U, M.s64.D, M.smem, G, G.val, G.lu, G.x, G.b, G.r, r, pv, v, z, z,
+                                                      ks, st);
+        else if (M.kind == 1)
+            launch_cpr_t<float, double, float, MODE>(P, S, M.s32.L, M.s32.U, M.s32.D, M.smem, G, G.valf, G.luf, G.xf, G.bf, G.rf, r, pv, v, z,
+                                                    z, ks, st);
+        else
+            launch_cpr_t<float, float, float, MODE>(P, S, M.s32.L, M.s32.U, M.s32.D, M.smem, G, G.valf, G.luf, G.xf, G.bf, G.rf, r, pv, v, z,
+                                                   M.y32, ks, st);
+    };
+    (void)S;
+    if (mode == IN_PUPDATE) go(std::integral_constant<int, IN_PUPDATE>());
+    else if (mode == IN_SUPDATE) go(std::integral_constant<int, IN_SUPDATE>());
+    else go(std::integral_constant<int, IN_PLAIN>());
 }
 
 }  // namespace rsg
