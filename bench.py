@@ -34,7 +34,9 @@ sys.path.insert(0, ROOT)
 
 N_REAL, NX, NY, NZ, SIGMA = 64, 40, 40, 10, 1.5
 TOL, MAXIT = 1e-6, 500
-WORKLOAD = "ensemble64_40x40x10_bilu0_bicgstab"
+WORKLOAD = "ensemble64_40x40x10_cpr_bicgstab"
+BATCH_PREC = dict(precond="cpr", precision="mixed_f32")     # batched mixed-precision form
+PLAIN_PREC = dict(precond="cpr", precision="fp64")          # plain FP64 GPU path
 METRIC = "solves/s & p99 latency: batched mixed-prec vs plain FP64 GPU, true rel.res <=1e-6"
 
 
@@ -199,7 +201,7 @@ def main():
         torch.cuda.synchronize()
 
     # ---------------- batched mixed-precision path, device-resident inputs
-    dev = DeviceSolver(precond="bilu0", krylov="bicgstab", precision="mixed", check_every=8, use_graphs=True, device=local)
+    dev = DeviceSolver(krylov="bicgstab", check_every=4, use_graphs=True, device=local, **BATCH_PREC)
     dev.set_batch(mats)
     stream = torch.cuda.ExternalStream(dev.stream)
     d_b = torch.from_numpy(b_host).to(f"cuda:{local}")
@@ -252,15 +254,15 @@ def main():
     t_prec = e0.elapsed_time(e1) / reps / 1e3      # forward + backward sweep
     hbm, peak_kind = peaks()
     B_spmv = spmv_bytes(nnzb, n_rows)
-    B_ilu = ilu_bytes(nnzb, n_rows, 4, 4)
+    B_ilu = ilu_bytes(nnzb, n_rows, 4, 4)   # lower bound of the CPR application: its BILU0 stage
     mean_its = float(np.mean(its))
     share_spmv = 2 * t_spmv * mean_its
     share_prec = 2 * t_prec * mean_its
     kernels = {
         "bsr3_spmv_f64": {"ms": 1e3 * t_spmv, "bytes": B_spmv, "gbs": B_spmv / t_spmv / 1e9, "per_iteration": 2},
-        "bilu0_sweeps_f32": {"ms": 1e3 * t_prec, "bytes": B_ilu, "gbs": B_ilu / t_prec / 1e9, "per_iteration": 2},
+        "cpr_apply_f32": {"ms": 1e3 * t_prec, "bytes": B_ilu, "gbs": B_ilu / t_prec / 1e9, "per_iteration": 2},
     }
-    dom = "bilu0_sweeps_f32" if share_prec >= share_spmv else "bsr3_spmv_f64"
+    dom = "cpr_apply_f32" if share_prec >= share_spmv else "bsr3_spmv_f64"
     ach = kernels[dom]["gbs"]
     roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                 "peak_kind": peak_kind + " burst copy", "traffic": None}
@@ -296,7 +298,7 @@ def main():
     # ---------------- plain FP64 GPU path: one system after another (one handle each)
     plain = []
     for A in mats:
-        d = DeviceSolver(precond="bilu0", krylov="bicgstab", precision="fp64", check_every=8, use_graphs=True, device=local)
+        d = DeviceSolver(krylov="bicgstab", check_every=4, use_graphs=True, device=local, **PLAIN_PREC)
         d.set_matrix(A)
         plain.append(d)
     bs = [torch.from_numpy(s.b).to(f"cuda:{local}") for s in systems]
@@ -332,7 +334,9 @@ def main():
             "data": "synthetic (ressim_gb300.synth: seeded black-oil Jacobians of the named shapes)",
             "config": {"workload": WORKLOAD, "systems": N_REAL, "grid": f"{NX}x{NY}x{NZ}", "sigma_lnk": SIGMA,
                        "active_cells": [int(min(A.n for A in mats)), int(max(A.n for A in mats))], "block_rows": n_rows,
-                       "nnzb": nnzb, "precision": "mixed (FP32 BILU0 factors/sweeps, FP64 Krylov)", "tol": TOL,
+                       "nnzb": nnzb, "preconditioner": "CPR: aggregation AMG V-cycle (Gauss-Seidel) on the pressure system + BILU0",
+                       "precision": "mixed: FP32 BILU0 factors/sweeps and AMG, FP64 Krylov vectors, dots, true residual; plain path FP64",
+                       "tol": TOL,
                        "l2": f"inputs larger than L2 (matrix values {val_bytes / 1e6:.0f} MB)", "parallelism": f"replicas{world}"},
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                            "note": "batched step: all 64 systems complete together"},
