@@ -247,7 +247,7 @@ def test_cpr_refresh_equals_fresh_setup():
     assert rel(z1, z2) < 1e-12
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
 def test_cpr_batched_ensemble(precision):
     from ressim_gb300 import synth
     systems = synth.ensemble(n_real=6, nx=24, ny=24, nz=6, sigma=1.5)
