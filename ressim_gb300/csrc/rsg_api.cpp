@@ -164,12 +164,13 @@ int alloc_plan(rsg_solver* h) {
         (rc = upload(M, &D.sysTile0, P.sysTile0, st)) || (rc = upload(M, &D.sysRow0, P.sysRow0, st)) ||
         (rc = upload(M, &D.perm, P.perm, st)) || (rc = upload(M, &D.valSrc, P.valSrc, st)) ||
         (rc = upload(M, &D.lvlStart, P.lvlStart, st)) || (rc = upload(M, &D.sysLvl0, P.sysLvl0, st)) ||
-        (rc = upload(M, &D.Lptr, P.Lptr, st)) || (rc = upload(M, &D.Lcol, P.Lcol, st)) || (rc = upload(M, &D.Lsrc, P.Lsrc, st)) ||
-        (rc = upload(M, &D.Uptr, P.Uptr, st)) || (rc = upload(M, &D.Ucol, P.Ucol, st)) || (rc = upload(M, &D.Usrc, P.Usrc, st)) ||
-        (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
+        (rc = upload(M, reinterpret_cast<int**>(&D.Lslot), P.Lslot, st)) || (rc = upload(M, &D.LslotSrc, P.LslotSrc, st)) ||
+        (rc = upload(M, &D.LovCol, P.LovCol, st)) || (rc = upload(M, &D.LovSrc, P.LovSrc, st)) ||
+        (rc = upload(M, reinterpret_cast<int**>(&D.Uslot), P.Uslot, st)) || (rc = upload(M, &D.UslotSrc, P.UslotSrc, st)) ||
+        (rc = upload(M, &D.UovCol, P.UovCol, st)) || (rc = upload(M, &D.UovSrc, P.UovSrc, st)) || (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
         return rc;
-    D.nL = int(P.Lcol.size());
-    D.nU = int(P.Ucol.size());
+    D.nLov = int(P.LovCol.size());
+    D.nUov = int(P.UovCol.size());
     D.maxSysRows = P.maxSysRows;
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
     if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
@@ -291,6 +292,15 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
     return set_values(h, vals, nnzbs);
 }
 
+template <class T>
+int alloc_split(rsg_solver* h, SplitFactors<T>& F) {
+    int rc;
+    if ((rc = dalloc(h->pmem, &F.L, size_t(h->dp.n) * LREC)) || (rc = dalloc(h->pmem, &F.UD, size_t(h->dp.n) * UREC)) ||
+        (rc = dalloc(h->pmem, &F.Lov, size_t(h->dp.nLov) * NB2)) || (rc = dalloc(h->pmem, &F.Uov, size_t(h->dp.nUov) * NB2)))
+        return rc;
+    return RSG_OK;
+}
+
 int ensure_precond_storage(rsg_solver* h) {
     const size_t E = size_t(h->plan.nnzb) * NB2;
     int rc;
@@ -300,18 +310,10 @@ int ensure_precond_storage(rsg_solver* h) {
         if (!h->luf && (rc = dalloc(h->pmem, &h->luf, E))) return rc;
         if (!h->work && (rc = dalloc(h->pmem, &h->work, E))) return rc;
         if (h->opt.precision == RSG_MIXED_F32 && !h->V.y32 && (rc = dalloc(h->pmem, &h->V.y32, size_t(h->plan.n) * NB))) return rc;
-        if (h->cta && !h->s32.L) {
-            if ((rc = dalloc(h->pmem, &h->s32.L, size_t(h->dp.nL) * NB2)) || (rc = dalloc(h->pmem, &h->s32.U, size_t(h->dp.nU) * NB2)) ||
-                (rc = dalloc(h->pmem, &h->s32.D, size_t(h->dp.n) * NB2)))
-                return rc;
-        }
+        if (h->cta && !h->s32.L && (rc = alloc_split(h, h->s32))) return rc;
     } else {
         if (!h->lu && (rc = dalloc(h->pmem, &h->lu, E))) return rc;
-        if (h->cta && !h->s64.L) {
-            if ((rc = dalloc(h->pmem, &h->s64.L, size_t(h->dp.nL) * NB2)) || (rc = dalloc(h->pmem, &h->s64.U, size_t(h->dp.nU) * NB2)) ||
-                (rc = dalloc(h->pmem, &h->s64.D, size_t(h->dp.n) * NB2)))
-                return rc;
-        }
+        if (h->cta && !h->s64.L && (rc = alloc_split(h, h->s64))) return rc;
     }
     return RSG_OK;
 }
@@ -326,7 +328,8 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
     G.nsys = nsys;
     G.maxL = maxL;
     std::vector<AmgSysLv> lv(size_t(nsys) * maxL);
-    int rows = 0, rps = 0, ents = 0, lvls = 0, mems = 0, aps = 0, lus = 0, lurows = 0;
+    int rows = 0, rps = 0, ents = 0, lvls = 0, mems = 0, aps = 0, lus = 0, lurows = 0, slots = 0;
+    std::vector<int> sysRows(size_t(nsys), 0);
     G.levelEntBeg.assign(size_t(maxL) + 1, 0);
     G.levelApBeg.assign(size_t(maxL) + 1, 0);
     G.levelRowBeg.assign(size_t(maxL) + 1, 0);
@@ -343,6 +346,11 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             d.nnz = int(A.ci.size());
             d.nl = int(A.lvlStart.size()) - 1;
             d.rowOff = rows; d.rpOff = rps; d.entOff = ents; d.lvlOff = lvls; d.memOff = mems;
+            d.W = l == 0 ? AMG_W0 : AMG_W1;
+            d.slotOff = slots;
+            d.locOff = sysRows[size_t(s)];
+            slots += A.n * d.W;
+            sysRows[size_t(s)] += A.n;
             apOff[size_t(s) * maxL + l] = aps;
             if (l == 0 && ents != h->plan.rowPtr[size_t(h->plan.sysRow0[size_t(s)])])
                 return fail(RSG_EINVAL, "internal: AMG level 0 does not match the block pattern");
@@ -359,6 +367,32 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
     G.levelApBeg[size_t(maxL)] = aps;
     G.levelRowBeg[size_t(maxL)] = rows;
     G.totRows = rows; G.totEnt = ents; G.nAP = aps; G.totLu = lus; G.totLuRows = lurows;
+    G.totSlots = slots;
+    G.maxSysAmgRows = 0;
+    for (int r : sysRows) G.maxSysAmgRows = std::max(G.maxSysAmgRows, r);
+    // V-cycle row slots: first W off-diagonal entries of every row in row order, the rest from the CSR
+    std::vector<int> slotSrc(size_t(std::max(slots, 1)), -1), slotCol(size_t(std::max(slots, 1)), -1), meta(size_t(rows) * 4, -1);
+    for (int l = 0; l < maxL; ++l)
+        for (int s = 0; s < nsys; ++s) {
+            if (l >= int(H[size_t(s)].lv.size())) continue;
+            const AmgLevel& A = H[size_t(s)].lv[size_t(l)];
+            const AmgSysLv& d = lv[size_t(s) * maxL + l];
+            for (int k = 0; k < A.n; ++k) {
+                const int p0 = A.rp[size_t(k)], p1 = A.rp[size_t(k) + 1], pd = A.diag[size_t(k)];
+                int* m = &meta[size_t(d.rowOff + k) * 4];
+                m[0] = pd - p0;
+                m[1] = p1 - p0 - 1;
+                m[2] = -1;
+                m[3] = pd;
+                for (int p = p0, j = 0; p < p1 && j < d.W; ++p) {
+                    if (p == pd) continue;
+                    slotSrc[size_t(d.slotOff) + size_t(k) * d.W + size_t(j)] = d.entOff + p;
+                    slotCol[size_t(d.slotOff) + size_t(k) * d.W + size_t(j)] = A.ci[size_t(p)];
+                    if (j == d.W - 1) m[2] = p + 1;   // the row continues here (diagonal and / or further entries)
+                    ++j;
+                }
+            }
+        }
     std::vector<int> rp(static_cast<size_t>(rps)), ci(static_cast<size_t>(ents)), dg(static_cast<size_t>(rows)),
         lvl(static_cast<size_t>(lvls)), agg(static_cast<size_t>(rows), 0), memPtr(static_cast<size_t>(rps), 0),
         mem(static_cast<size_t>(mems)), dgG(static_cast<size_t>(rows)), luPerm(static_cast<size_t>(std::max(lurows, 1)), 0);
@@ -403,8 +437,19 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = upload(M, &G.diag, dg, st)) || (rc = upload(M, &G.lvl, lvl, st)) || (rc = upload(M, &G.agg, agg, st)) ||
         (rc = upload(M, &G.memPtr, memPtr, st)) || (rc = upload(M, &G.mem, mem, st)) || (rc = upload(M, &G.apPtr, apPtr, st)) ||
         (rc = upload(M, &G.apSrc, apSrc, st)) || (rc = upload(M, &G.acPtr, acPtr, st)) || (rc = upload(M, &G.acSrc, acSrc, st)) ||
-        (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)))
+        (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)) ||
+        (rc = upload(M, &G.slotSrc, slotSrc, st)) || (rc = upload(M, &G.slotCol, slotCol, st)) ||
+        (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)))
         return rc;
+    {
+        const size_t S = size_t(std::max(slots, 1)), R = size_t(std::max(rows, 1)), n = size_t(h->plan.n);
+        const size_t nLo = size_t(h->dp.nLov) * 3, nUo = size_t(h->dp.nUov) * 3;
+        if ((rc = dalloc(M, &G.slotVal, S)) || (rc = dalloc(M, &G.slotValf, S)) || (rc = dalloc(M, &G.diagVal, R)) ||
+            (rc = dalloc(M, &G.diagValf, R)) || (rc = dalloc(M, &G.cin, size_t(std::max(lurows, 1)))) ||
+            (rc = dalloc(M, &G.sp, n * SPREC)) || (rc = dalloc(M, &G.spf, n * SPREC)) || (rc = dalloc(M, &G.spLov, nLo)) ||
+            (rc = dalloc(M, &G.spLovf, nLo)) || (rc = dalloc(M, &G.spUov, nUo)) || (rc = dalloc(M, &G.spUovf, nUo)))
+            return rc;
+    }
     RSG_CUDA(cudaMemcpyAsync(G.lv, lv.data(), lv.size() * sizeof(AmgSysLv), cudaMemcpyHostToDevice, st));
     if ((rc = dalloc(M, &G.val, size_t(ents))) || (rc = dalloc(M, &G.valf, size_t(ents))) || (rc = dalloc(M, &G.apVal, size_t(std::max(aps, 1)))) ||
         (rc = dalloc(M, &G.lu, size_t(std::max(lus, 1)))) || (rc = dalloc(M, &G.luf, size_t(std::max(lus, 1)))) ||
@@ -472,7 +517,9 @@ int setup_cpr(rsg_solver* h, const double* acc) {
     launch_amg_refresh(G, st);
     launch_amg_coarse_lu(G, h->opt.precision != RSG_FP64, st);
     if (h->opt.precision != RSG_FP64) launch_amg_round(G, st);
-    h->launches += 3 + 3 * std::max(0, G.maxL - 1) + (h->opt.precision != RSG_FP64 ? 2 : 0);
+    launch_amg_slots(G, h->opt.precision != RSG_FP64, st);
+    launch_cpr_sp(D, h->val, G, h->opt.precision != RSG_FP64, st);
+    h->launches += 5 + 3 * std::max(0, G.maxL - 1) + (h->opt.precision != RSG_FP64 ? 2 : 0);
     RSG_CUDA(cudaGetLastError());
     return RSG_OK;
 }

@@ -101,7 +101,7 @@ __global__ void k_diag_fix(int beg, int end, const int* __restrict__ diagGlob, d
 // (engine/src/amg.cpp:273-295); one thread block per system
 __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
                                                    const int* __restrict__ ci, const double* __restrict__ val,
-                                                   const int* __restrict__ luPerm, double* luAll, int* pivAll) {
+                                                   const int* __restrict__ luPerm, double* luAll, int* pivAll, int* cinAll) {
     const int s = blockIdx.x;
     AmgSysLv L;
     bool found = false;
@@ -167,6 +167,76 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
         }
         __syncthreads();
     }
+    // gather order of the solve: the level-space row whose value lands at position i once the natural-order
+    // vector has gone through the row interchanges piv[0], piv[1], ... (engine/src/amg.cpp:306-308)
+    int* cin = cinAll + L.luRowOff;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) cin[__ldg(nat + k)] = k;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < m; ++k) {
+            const int pk = piv[k];
+            if (pk != k) { const int t = cin[k]; cin[k] = cin[pk]; cin[pk] = t; }
+        }
+}
+
+// V-cycle row slots from the level values (zero padding), FP32 copies for the FP32 V-cycle
+__global__ void k_amg_slots(int totSlots, int totRows, const int* __restrict__ slotSrc, const int* __restrict__ diagGlob,
+                            const double* __restrict__ val, double* slotVal, float* slotValf, double* diagVal, float* diagValf) {
+    const int total = totSlots + totRows;
+    for (int q = int(blockIdx.x * blockDim.x + threadIdx.x); q < total; q += int(gridDim.x * blockDim.x)) {
+        if (q < totSlots) {
+            const int src = __ldg(slotSrc + q);
+            const double v = src >= 0 ? val[src] : 0.0;
+            slotVal[q] = v;
+            if (slotValf) slotValf[q] = float(v);
+        } else {
+            const int g = q - totSlots;
+            const double v = val[__ldg(diagGlob + g)];
+            diagVal[g] = v;
+            if (diagValf) diagValf[g] = float(v);
+        }
+    }
+}
+
+// pressure columns S_ij[e][0] of the second stage in the factors' slot order: per row SPREC values (L slots,
+// diagonal, U slots, padding), overflow blocks 3 values each
+template <class T>
+__device__ __forceinline__ void put_sp(const double* __restrict__ val, int src, T* out) {
+    for (int e = 0; e < 3; ++e) out[e] = src >= 0 ? T(val[size_t(src) * 9 + size_t(e) * 3]) : T(0);
+}
+__global__ void k_cpr_sp(int n, int nLov, int nUov, const int* __restrict__ LslotSrc, const int* __restrict__ UslotSrc,
+                         const int* __restrict__ Dsrc, const int* __restrict__ LovSrc, const int* __restrict__ UovSrc,
+                         const double* __restrict__ val, double* sp, float* spf, double* spLov, float* spLovf, double* spUov,
+                         float* spUovf) {
+    const int total = n + nLov + nUov;
+    for (int q = int(blockIdx.x * blockDim.x + threadIdx.x); q < total; q += int(gridDim.x * blockDim.x)) {
+        if (q < n) {
+            const int k = q;
+            int src[2 * SLOTS + 1];
+            for (int j = 0; j < SLOTS; ++j) {
+                src[j] = __ldg(LslotSrc + size_t(k) * SLOTS + j);
+                src[SLOTS + 1 + j] = __ldg(UslotSrc + size_t(k) * SLOTS + j);
+            }
+            src[SLOTS] = __ldg(Dsrc + k);
+            if (spf) {
+                float* o = spf + size_t(k) * SPREC;
+                for (int j = 0; j < 2 * SLOTS + 1; ++j) put_sp(val, src[j], o + 3 * j);
+                for (int e = 3 * (2 * SLOTS + 1); e < SPREC; ++e) o[e] = 0.f;
+            } else {
+                double* o = sp + size_t(k) * SPREC;
+                for (int j = 0; j < 2 * SLOTS + 1; ++j) put_sp(val, src[j], o + 3 * j);
+                for (int e = 3 * (2 * SLOTS + 1); e < SPREC; ++e) o[e] = 0.0;
+            }
+        } else if (q < n + nLov) {
+            const int i = q - n, src = __ldg(LovSrc + i);
+            if (spLovf) put_sp(val, src, spLovf + size_t(i) * 3);
+            else put_sp(val, src, spLov + size_t(i) * 3);
+        } else {
+            const int i = q - n - nLov, src = __ldg(UovSrc + i);
+            if (spUovf) put_sp(val, src, spUovf + size_t(i) * 3);
+            else put_sp(val, src, spUov + size_t(i) * 3);
+        }
+    }
 }
 
 __global__ void k_round(size_t n, const double* __restrict__ a, float* b) {
@@ -196,11 +266,21 @@ void launch_amg_refresh(const DevAmg& G, cudaStream_t st) {
     }
 }
 void launch_amg_coarse_lu(const DevAmg& G, bool fp32copy, cudaStream_t st) {
-    if (G.totLu > 0) k_coarse_lu<<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv);
+    if (G.totLu > 0) k_coarse_lu<<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin);
     if (fp32copy && G.totLu > 0) k_round<<<grid_for(size_t(G.totLu)), 256, 0, st>>>(size_t(G.totLu), G.lu, G.luf);
 }
 void launch_amg_round(const DevAmg& G, cudaStream_t st) {
     k_round<<<grid_for(size_t(G.totEnt)), 256, 0, st>>>(size_t(G.totEnt), G.val, G.valf);
+}
+void launch_amg_slots(const DevAmg& G, bool fp32, cudaStream_t st) {
+    k_amg_slots<<<grid_for(size_t(G.totSlots) + size_t(G.totRows)), 256, 0, st>>>(G.totSlots, G.totRows, G.slotSrc, G.diagGlob, G.val,
+                                                                                   G.slotVal, fp32 ? G.slotValf : nullptr, G.diagVal,
+                                                                                   fp32 ? G.diagValf : nullptr);
+}
+void launch_cpr_sp(const DevPlan& P, const double* val, const DevAmg& G, bool fp32, cudaStream_t st) {
+    k_cpr_sp<<<grid_for(size_t(P.n) + size_t(P.nLov) + size_t(P.nUov)), 256, 0, st>>>(
+        P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, val, G.sp, fp32 ? G.spf : nullptr, G.spLov,
+        fp32 ? G.spLovf : nullptr, G.spUov, fp32 ? G.spUovf : nullptr);
 }
 
 }  // namespace rsg

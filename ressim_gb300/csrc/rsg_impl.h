@@ -13,6 +13,10 @@ constexpr int NB2 = NB * NB;
 constexpr int TILE_ROWS = 256;        // block rows per tile of the tile kernels (64-row steps, 3 threads per block row)
 constexpr int TILE_THREADS = TILE_ROWS * NB;
 constexpr int MAX_DOTS = 4;           // partial sums per tile in the fused reductions
+constexpr int SLOTS = 3;              // factor block slots per row and triangle (7-point stencil: 3 lower, 3 upper)
+constexpr int LREC = 28;              // factor values per row record of L: SLOTS blocks + 1 pad (16-byte multiple)
+constexpr int UREC = 36;              // per row record of U and D: SLOTS blocks + the inverted diagonal block
+constexpr int SPREC = 24;             // CPR pressure columns of S per row: (SLOTS + 1 + SLOTS) blocks x 3 + 3 pad
 
 // Krylov status per system (device int)
 enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3 };
@@ -52,10 +56,15 @@ struct HostPlan {
     bool symmetric = true;
     // lvlStart[sysLvl0[s] + l] is the first level-space row of level l of system s (nl_s + 1 entries per system)
     std::vector<int> lvlStart, sysLvl0;
-    // split storage of the factors for the thread-block sweeps (level-space row order)
-    std::vector<int> Lptr, Lcol, Lsrc;   // strict-lower blocks of position k: [Lptr[k], Lptr[k+1]), local column, source block
-    std::vector<int> Uptr, Ucol, Usrc;   // strict-upper blocks
-    std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of position k
+    // Slot storage of the factors for the thread-block sweeps (level-space row order). Every row k has SLOTS
+    // strict-lower and SLOTS strict-upper block slots holding its first blocks of that part in row order; a row's
+    // further blocks continue in an overflow list, terminated by a column of -1.
+    //   Lslot[4k + j], j < SLOTS: local column of slot j (-1 empty); Lslot[4k + 3]: overflow start (-1 none)
+    //   LslotSrc[SLOTS k + j]: source block position of slot j (-1 empty)
+    //   LovCol / LovSrc: overflow entries (local column, source block; -1 / -1 ends a row's list)
+    std::vector<int> Lslot, LslotSrc, LovCol, LovSrc;
+    std::vector<int> Uslot, UslotSrc, UovCol, UovSrc;
+    std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of row k
     int maxSysRows = 0;
 };
 
@@ -96,7 +105,11 @@ struct AmgSysLv {
     int coarse = 0;                    // 1 on the system's coarsest level
     int dense = 0;                     // coarsest level solved by dense LU (else 20 symmetric GS sweeps)
     int luOff = 0, luRowOff = 0;       // coarsest: dense LU (m*m) and pivots / natural order (m)
+    int slotOff = 0, W = 0;            // row slots of the V-cycle (W off-diagonal entries per row at slotOff + W k)
+    int locOff = 0;                    // offset of the level's rows inside the system's V-cycle vectors
 };
+constexpr int AMG_W0 = 8;              // V-cycle row slots on the finest level (7-point pressure matrix)
+constexpr int AMG_W1 = 16;             // on the Galerkin levels
 struct DevAmg {
     int nsys = 0, maxL = 0;
     int totRows = 0, totEnt = 0, totLu = 0, totLuRows = 0, nAP = 0;
@@ -117,6 +130,21 @@ struct DevAmg {
     double* w = nullptr;               // CPR weights, level-space block rows of S (n * 3)
     double* T = nullptr;               // second-stage input t = r - S[:,p] xp (n * 3)
     double* acc = nullptr;             // accumulation blocks gathered into level space (n * 9), optional
+    // V-cycle row slots (refreshed from val at every set-up): the first W off-diagonal entries of every row in
+    // row order (value, local column; 0 / -1 padding), the diagonal value, and per row {number of entries before
+    // the diagonal, off-diagonal entries, entry position where the entries beyond the slots continue, diagonal
+    // position} (positions local to the level's entries)
+    int totSlots = 0, maxSysAmgRows = 0;
+    int* slotSrc = nullptr;            // global entry of every slot (-1 padding)
+    int* slotCol = nullptr;
+    int4* rowMeta = nullptr;
+    double *slotVal = nullptr, *diagVal = nullptr;
+    float *slotValf = nullptr, *diagValf = nullptr;
+    int* cin = nullptr;                // coarsest dense level: level-space row feeding position i of the pivoted natural order
+    // pressure columns of S per level-space block row in slot order (L slots, diagonal, U slots; SPREC values) and
+    // of the overflow blocks (3 values each)
+    double *sp = nullptr, *spLov = nullptr, *spUov = nullptr;
+    float *spf = nullptr, *spLovf = nullptr, *spUovf = nullptr;
 };
 // CPR set-up kernels (rsg_cpr.cu)
 void launch_cpr_weights(const DevPlan& P, const double* val, const double* accLev, double* w, int* nfallback, cudaStream_t st);
@@ -125,6 +153,9 @@ void launch_gather_acc(const DevPlan& P, const double* accOrig, double* accLev, 
 void launch_amg_refresh(const DevAmg& G, cudaStream_t st);           // Galerkin values of levels >= 1, diagonal fix
 void launch_amg_coarse_lu(const DevAmg& G, bool fp32copy, cudaStream_t st);
 void launch_amg_round(const DevAmg& G, cudaStream_t st);             // valf = float(val), luf = float(lu)
+void launch_amg_slots(const DevAmg& G, bool fp32, cudaStream_t st);  // V-cycle row slots from val
+// pressure columns of S in the slot order of the factors (second stage of the CPR application)
+void launch_cpr_sp(const DevPlan& P, const double* val, const DevAmg& G, bool fp32, cudaStream_t st);
 // one CPR application per system (thread block per system), fused with the BiCGSTAB input update:
 // mode 0 plain (r -> z), 1 p-update, 2 s-update (as the BILU0 sweeps)
 void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, bool amgFp32, const double* r, double* pv,
@@ -145,14 +176,17 @@ struct DevPlan {
     int *rowSys = nullptr, *tileRow0 = nullptr, *tileSys = nullptr, *sysTile0 = nullptr, *sysRow0 = nullptr;
     int *perm = nullptr, *valSrc = nullptr;
     int *lvlStart = nullptr, *sysLvl0 = nullptr;
-    int *Lptr = nullptr, *Lcol = nullptr, *Lsrc = nullptr, *Uptr = nullptr, *Ucol = nullptr, *Usrc = nullptr, *Dsrc = nullptr;
-    int nL = 0, nU = 0, maxSysRows = 0;
+    int4 *Lslot = nullptr, *Uslot = nullptr;
+    int *LslotSrc = nullptr, *UslotSrc = nullptr, *LovCol = nullptr, *LovSrc = nullptr, *UovCol = nullptr, *UovSrc = nullptr;
+    int* Dsrc = nullptr;
+    int nLov = 0, nUov = 0, maxSysRows = 0;
 };
 
-// Level-ordered split factors for the CTA-per-system sweeps (FP64 or FP32 storage).
+// Slot-layout factors for the CTA-per-system sweeps (FP64 or FP32 storage): L = n x LREC, UD = n x UREC,
+// Lov / Uov = overflow blocks (9 values each).
 template <class T>
 struct SplitFactors {
-    T *L = nullptr, *U = nullptr, *D = nullptr;
+    T *L = nullptr, *UD = nullptr, *Lov = nullptr, *Uov = nullptr;
 };
 
 struct SweepState {                   // sync-free sweep flags and claim counters

@@ -163,18 +163,32 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     }
     P.sysTile0[size_t(nsys)] = int(P.tileSys.size());
     P.tileRow0.push_back(n);
-    // split L / U / D storage of the thread-block sweeps (rows of a level contiguous; columns local to the system)
-    P.Lptr.assign(size_t(n) + 1, 0);
-    P.Uptr.assign(size_t(n) + 1, 0);
+    // slot storage of the thread-block sweeps (rows of a level contiguous; columns local to the system)
+    P.Lslot.assign(size_t(n) * 4, -1);
+    P.Uslot.assign(size_t(n) * 4, -1);
+    P.LslotSrc.assign(size_t(n) * SLOTS, -1);
+    P.UslotSrc.assign(size_t(n) * SLOTS, -1);
     P.Dsrc.assign(size_t(n), 0);
-    P.Lcol.clear(); P.Lsrc.clear(); P.Ucol.clear(); P.Usrc.clear();
+    P.LovCol.clear(); P.LovSrc.clear(); P.UovCol.clear(); P.UovSrc.clear();
+    auto fill = [&](int k, int p0, int p1, int base, std::vector<int>& slot, std::vector<int>& slotSrc, std::vector<int>& ovCol,
+                    std::vector<int>& ovSrc) {
+        for (int p = p0, j = 0; p < p1; ++p, ++j) {
+            if (j < SLOTS) {
+                slot[size_t(k) * 4 + size_t(j)] = P.col[size_t(p)] - base;
+                slotSrc[size_t(k) * SLOTS + size_t(j)] = p;
+            } else {
+                if (j == SLOTS) slot[size_t(k) * 4 + 3] = int(ovCol.size());
+                ovCol.push_back(P.col[size_t(p)] - base);
+                ovSrc.push_back(p);
+                if (p + 1 == p1) { ovCol.push_back(-1); ovSrc.push_back(-1); }
+            }
+        }
+    };
     for (int k = 0; k < n; ++k) {
         const int base = sysRow0[size_t(P.rowSys[size_t(k)])];
-        for (int p = P.rowPtr[size_t(k)]; p < P.diag[size_t(k)]; ++p) { P.Lcol.push_back(P.col[size_t(p)] - base); P.Lsrc.push_back(p); }
-        for (int p = P.diag[size_t(k)] + 1; p < P.rowPtr[size_t(k) + 1]; ++p) { P.Ucol.push_back(P.col[size_t(p)] - base); P.Usrc.push_back(p); }
+        fill(k, P.rowPtr[size_t(k)], P.diag[size_t(k)], base, P.Lslot, P.LslotSrc, P.LovCol, P.LovSrc);
+        fill(k, P.diag[size_t(k)] + 1, P.rowPtr[size_t(k) + 1], base, P.Uslot, P.UslotSrc, P.UovCol, P.UovSrc);
         P.Dsrc[size_t(k)] = P.diag[size_t(k)];
-        P.Lptr[size_t(k) + 1] = int(P.Lcol.size());
-        P.Uptr[size_t(k) + 1] = int(P.Ucol.size());
     }
     return true;
 }

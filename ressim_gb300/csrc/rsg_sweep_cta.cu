@@ -1,19 +1,24 @@
-// Thread-block-per-system BILU0 application: exact natural-order ILU(0) sweeps for systems that fit one SM.
+// Thread-block-per-system BILU0 and CPR application: exact natural-order ILU(0) sweeps and the CPR V-cycle for
+// systems that fit one SM.
 //
 // One thread block owns one system of the (block-diagonal) batch and walks its forward levels with a block
 // barrier between levels, then the same levels in reverse for the backward sweep (valid for the structurally
 // symmetric patterns of reservoir Jacobians; otherwise the plan uses the grid-wide sync-free sweeps). Rows are
-// in level space, so a level is a contiguous range of rows, of input vector entries and of split factor blocks.
+// in level space, so a level is a contiguous range of rows, of input vector entries and of factor records.
 //
-// * The sweep vector y stays on chip between the two sweeps when it fits the block's shared memory (chosen per
-//   system at run time), else it lives in the output vector itself (L1 / L2).
-// * Each thread prefetches, one row ahead, the next row's input entries, row pointers, column indices and up to
-//   kPre factor blocks into registers: the global-memory latency of a level overlaps the previous level's work
-//   and barrier, and only the dependency reads of y stay on the critical path.
-// * TF = factor storage type, TV = sweep vector type. FP64 (double, double) and mixed (float factors, double
-//   vector: the reference's float-factor sweeps, engine/src/bsr.cpp:500-522) use unfused multiply / add in the
-//   reference loop order, so their results are bitwise those of the reference's serial sweeps on the same
-//   factors. (float, float) is the all-FP32 BILU0f sweep (engine/src/bsr.cpp:1100-1121).
+// Latency is the whole game in these sweeps (one level = one barrier and one dependent step), so:
+// * factors are stored in slot records: per row a fixed 16-byte-multiple record of its first SLOTS blocks of L
+//   (resp. U and the inverted diagonal) and a vector of their columns. A row's data sits at an address computed
+//   from its index -- no pointer chasing -- and comes in as a few 16-byte loads;
+// * every thread holds two register buffers and loads its next row into one while it works on the other, so a
+//   row's loads are issued a whole level (work + barrier) before they are used;
+// * thread 0 asks the bulk-copy unit to prefetch the records of the level kAhead levels ahead into L2
+//   (cp.async.bulk.prefetch.L2), so the register loads above hit L2, not HBM;
+// * the sweep vector y and the V-cycle vectors stay in shared memory when they fit (chosen per system).
+// TF = factor storage type, TV = sweep vector type. FP64 (double, double) and mixed (float factors, double
+// vector: the reference's float-factor sweeps, engine/src/bsr.cpp:500-522) use unfused multiply / add in the
+// reference loop order, so their results are bitwise those of the reference's serial sweeps on the same
+// factors. (float, float) is the all-FP32 BILU0f sweep (engine/src/bsr.cpp:1100-1121).
 #include "rsg_impl.h"
 
 #include <cuda_runtime.h>
@@ -24,7 +29,7 @@ namespace rsg {
 namespace {
 
 constexpr int kCtaThreads = 256;
-constexpr int kPre = 3;                    // factor blocks per row prefetched into registers (7-point: all of L or U)
+constexpr int kAhead = 4;                  // levels prefetched into L2 ahead of the sweep front
 
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
@@ -47,36 +52,80 @@ __device__ __forceinline__ float vsub(float a, float b) { return a - b; }
 
 enum { IN_PLAIN = 0, IN_PUPDATE = 1, IN_SUPDATE = 2 };
 
-// registers holding one row's prefetched data
-template <class TF, int MODE>
-struct RowPre {
-    int k = -1, p0 = 0, p1 = 0;
-    int c[kPre];
-    TF a[kPre][9];
-    double in[MODE == IN_PUPDATE ? 9 : (MODE == IN_SUPDATE ? 6 : 3)];
-};
+// L2 prefetch of bytes [b, e) of base by the bulk-copy unit. The bulk unit wants a 16-byte aligned address and
+// a 16-byte multiple size: the range is rounded inward on the absolute addresses, so it never leaves [b, e)
+// whatever the alignment of base. A hint: nothing waits for it.
+__device__ __forceinline__ void l2_prefetch(const void* base, size_t b, size_t e) {
+    const unsigned long long a = reinterpret_cast<unsigned long long>(base);
+    const unsigned long long a0 = (a + b + 15) & ~15ull, a1 = (a + e) & ~15ull;
+    if (a1 > a0) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a0), "r"(unsigned(a1 - a0)) : "memory");
+}
+
+// N values from a 16-byte aligned record (read-only data)
+template <int N>
+__device__ __forceinline__ void ldrec(float (&a)[N], const float* p) {
+    static_assert(N % 4 == 0, "record of whole float4s");
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+        const float4 t = __ldg(q + i);
+        a[4 * i] = t.x; a[4 * i + 1] = t.y; a[4 * i + 2] = t.z; a[4 * i + 3] = t.w;
+    }
+}
+template <int N>
+__device__ __forceinline__ void ldrec(double (&a)[N], const double* p) {
+    static_assert(N % 2 == 0, "record of whole double2s");
+    const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+        const double2 t = __ldg(q + i);
+        a[2 * i] = t.x; a[2 * i + 1] = t.y;
+    }
+}
+template <int N>
+__device__ __forceinline__ void ldrec(int (&a)[N], const int* p) {
+    static_assert(N % 4 == 0, "record of whole int4s");
+    const int4* q = reinterpret_cast<const int4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 4; ++i) {
+        const int4 t = __ldg(q + i);
+        a[4 * i] = t.x; a[4 * i + 1] = t.y; a[4 * i + 2] = t.z; a[4 * i + 3] = t.w;
+    }
+}
+__device__ __forceinline__ int slot_col(const int4& c, int j) { return j == 0 ? c.x : (j == 1 ? c.y : c.z); }
+
+// ------------------------------------------------------------------ BILU0 sweeps on slot records
 template <class TF>
-struct RowPreB {
-    int k = -1, p0 = 0, p1 = 0;
-    int c[kPre];
-    TF a[kPre][9];
-    TF d[9];
+struct IluArgs {
+    const int *sysRow0, *sysLvl0, *lvlStart;
+    const int4 *Lslot, *Uslot;
+    const int *LovCol, *UovCol;
+    const TF *L, *UD, *Lov, *Uov;
 };
 
-template <class TF, int MODE>
-__device__ __forceinline__ void prefetch_fwd(RowPre<TF, MODE>& R, int k, const int* __restrict__ Lptr, const int* __restrict__ Lcol,
-                                             const TF* __restrict__ Lv, const double* r, const double* pv, const double* v) {
+// Registers of one row: slot columns, factor record, input (TI: the sweep input's storage type)
+template <class TF, class TI, int MODE>
+struct FwdRow {
+    int k;
+    int4 c;
+    TF a[LREC];
+    TI in[MODE == IN_PUPDATE ? 9 : (MODE == IN_SUPDATE ? 6 : 3)];
+};
+template <class TF>
+struct BwdRow {
+    int k;
+    int4 c;
+    TF a[UREC];
+    double xp;
+};
+
+template <class TF, class TI, int MODE>
+__device__ __forceinline__ void load_fwd(FwdRow<TF, TI, MODE>& R, int k, const IluArgs<TF>& F, const TI* r, const double* pv,
+                                         const double* v) {
     R.k = k;
     if (k < 0) return;
-    R.p0 = __ldg(Lptr + k);
-    R.p1 = __ldg(Lptr + k + 1);
-#pragma unroll
-    for (int j = 0; j < kPre; ++j)
-        if (R.p0 + j < R.p1) {
-            R.c[j] = __ldg(Lcol + R.p0 + j);
-#pragma unroll
-            for (int e = 0; e < 9; ++e) R.a[j][e] = __ldg(Lv + size_t(R.p0 + j) * 9 + e);
-        }
+    R.c = __ldg(F.Lslot + k);
+    ldrec(R.a, F.L + size_t(k) * LREC);
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
         const size_t q = size_t(k) * 3 + e;
@@ -85,23 +134,13 @@ __device__ __forceinline__ void prefetch_fwd(RowPre<TF, MODE>& R, int k, const i
         if (MODE == IN_SUPDATE) R.in[3 + e] = v[q];
     }
 }
-
-template <class TF>
-__device__ __forceinline__ void prefetch_bwd(RowPreB<TF>& R, int k, const int* __restrict__ Uptr, const int* __restrict__ Ucol,
-                                             const TF* __restrict__ Uv, const TF* __restrict__ Dv) {
+template <class TF, class TX>
+__device__ __forceinline__ void load_bwd(BwdRow<TF>& R, int k, const IluArgs<TF>& F, const TX* xp, int row0) {
     R.k = k;
     if (k < 0) return;
-    R.p0 = __ldg(Uptr + k);
-    R.p1 = __ldg(Uptr + k + 1);
-#pragma unroll
-    for (int j = 0; j < kPre; ++j)
-        if (R.p0 + j < R.p1) {
-            R.c[j] = __ldg(Ucol + R.p0 + j);
-#pragma unroll
-            for (int e = 0; e < 9; ++e) R.a[j][e] = __ldg(Uv + size_t(R.p0 + j) * 9 + e);
-        }
-#pragma unroll
-    for (int e = 0; e < 9; ++e) R.d[e] = __ldg(Dv + size_t(k) * 9 + e);
+    R.c = __ldg(F.Uslot + k);
+    ldrec(R.a, F.UD + size_t(k) * UREC);
+    if (xp) R.xp = double(xp[k - row0]);
 }
 
 template <class TF, class TV>
@@ -112,109 +151,197 @@ __device__ __forceinline__ void sub_block(TV (&yi)[3], const TF* a, const TV* y,
     yi[2] = vsub(yi[2], rdot(a + 6, yc));
 }
 
-// the thread's next row after row k of level L (the next one of the same level, else its first of level L+1)
-__device__ __forceinline__ int next_row(int k, int k1, int L, int nl, int l0, const int* __restrict__ lvlStart, int forward) {
-    if (k + int(blockDim.x) < k1) return k + int(blockDim.x);
-    const int Ln = forward ? L + 1 : L - 1;
-    if (Ln < 0 || Ln >= nl) return -1;
-    const int a = __ldg(lvlStart + l0 + Ln) + int(threadIdx.x);
-    return a < __ldg(lvlStart + l0 + Ln + 1) ? a : -1;
+// y_i = in_i - sum_{k<i} L_ik y_k (engine/src/bsr.cpp:568-575): slots, then the overflow list, in row order
+template <class TF, class TV, class TI, int MODE>
+__device__ __forceinline__ void fwd_step(const FwdRow<TF, TI, MODE>& R, const IluArgs<TF>& F, int row0, TV* y, double* pv, double beta,
+                                         double omega, double alpha) {
+    const int k = R.k;
+    TV yi[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const size_t q = size_t(k) * 3 + e;
+        if (MODE == IN_PUPDATE) {
+            const double pe = da(R.in[e], dm(beta, ds(R.in[3 + e], dm(omega, R.in[6 + e]))));   // linsolve.cpp:173
+            pv[q] = pe;
+            yi[e] = TV(pe);
+        } else if (MODE == IN_SUPDATE) {
+            const double se = ds(R.in[e], dm(alpha, R.in[3 + e]));                              // linsolve.cpp:183
+            pv[q] = se;
+            yi[e] = TV(se);
+        } else {
+            yi[e] = TV(R.in[e]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j) {
+        const int c = slot_col(R.c, j);
+        if (c >= 0) sub_block(yi, R.a + 9 * j, y, c);
+    }
+    if (R.c.w >= 0)
+        for (int q = R.c.w;; ++q) {
+            const int c = __ldg(F.LovCol + q);
+            if (c < 0) break;
+            TF a[9];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[e] = __ldg(F.Lov + size_t(q) * 9 + e);
+            sub_block(yi, a, y, c);
+        }
+    const int li = k - row0;
+    y[li * 3 + 0] = yi[0]; y[li * 3 + 1] = yi[1]; y[li * 3 + 2] = yi[2];
 }
 
-// Both sweeps of one system by the calling thread block (y: the sweep vector of this system, on chip or in z).
-template <class TF, class TV, int MODE>
-__device__ void ilu_body(int row0, int l0, int nl, const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
-                         const int* __restrict__ Lcol, const TF* __restrict__ Lv, const int* __restrict__ Uptr,
-                         const int* __restrict__ Ucol, const TF* __restrict__ Uv, const TF* __restrict__ Dv, const double* r, double* pv,
-                         const double* v, double* z, TV* y, bool writeZ, double beta, double omega, double alpha) {
-    const int tid = int(threadIdx.x);
-    // ---- forward: y_i = in_i - sum_{k<i} L_ik y_k (engine/src/bsr.cpp:568-575), level by level
-    RowPre<TF, MODE> cur, nxt;
-    {
-        const int a = nl > 0 ? __ldg(lvlStart + l0) + tid : -1;
-        prefetch_fwd(cur, (nl > 0 && a < __ldg(lvlStart + l0 + 1)) ? a : -1, Lptr, Lcol, Lv, r, pv, v);
+// z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j) (engine/src/bsr.cpp:577-587); with XP the CPR correction z_p += xp
+// (bsr.cpp:1083) is applied to the stored z
+template <class TF, class TV, bool XP>
+__device__ __forceinline__ void bwd_step(const BwdRow<TF>& R, const IluArgs<TF>& F, int row0, TV* y, double* z, bool writeZ) {
+    const int k = R.k, li = k - row0;
+    TV yi[3] = {y[li * 3 + 0], y[li * 3 + 1], y[li * 3 + 2]};
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j) {
+        const int c = slot_col(R.c, j);
+        if (c >= 0) sub_block(yi, R.a + 9 * j, y, c);
     }
-    for (int L = 0; L < nl; ++L) {
-        const int k1 = __ldg(lvlStart + l0 + L + 1);
-        for (int k = __ldg(lvlStart + l0 + L) + tid; k < k1; k += blockDim.x) {
-            if (cur.k != k) prefetch_fwd(cur, k, Lptr, Lcol, Lv, r, pv, v);
-            prefetch_fwd(nxt, next_row(k, k1, L, nl, l0, lvlStart, 1), Lptr, Lcol, Lv, r, pv, v);
-            TV yi[3];
+    if (R.c.w >= 0)
+        for (int q = R.c.w;; ++q) {
+            const int c = __ldg(F.UovCol + q);
+            if (c < 0) break;
+            TF a[9];
 #pragma unroll
-            for (int e = 0; e < 3; ++e) {
-                const size_t q = size_t(k) * 3 + e;
-                if (MODE == IN_PUPDATE) {
-                    const double pe = da(cur.in[e], dm(beta, ds(cur.in[3 + e], dm(omega, cur.in[6 + e]))));   // linsolve.cpp:173
-                    pv[q] = pe;
-                    yi[e] = TV(pe);
-                } else if (MODE == IN_SUPDATE) {
-                    const double se = ds(cur.in[e], dm(alpha, cur.in[3 + e]));                               // linsolve.cpp:183
-                    pv[q] = se;
-                    yi[e] = TV(se);
-                } else {
-                    yi[e] = TV(cur.in[e]);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < kPre; ++j)
-                if (cur.p0 + j < cur.p1) sub_block(yi, cur.a[j], y, cur.c[j]);
-            for (int p = cur.p0 + kPre; p < cur.p1; ++p) {     // long rows (well fill): the rest on demand
-                TF a[9];
-#pragma unroll
-                for (int e = 0; e < 9; ++e) a[e] = __ldg(Lv + size_t(p) * 9 + e);
-                sub_block(yi, a, y, __ldg(Lcol + p));
-            }
-            const int li = k - row0;
-            y[li * 3 + 0] = yi[0]; y[li * 3 + 1] = yi[1]; y[li * 3 + 2] = yi[2];
-            cur = nxt;
+            for (int e = 0; e < 9; ++e) a[e] = __ldg(F.Uov + size_t(q) * 9 + e);
+            sub_block(yi, a, y, c);
         }
-        __syncthreads();
-    }
-    // ---- backward: z_i = U_ii^-1 (y_i - sum_{j>i} U_ij z_j) (engine/src/bsr.cpp:577-587), levels in reverse
-    RowPreB<TF> bc, bn;
-    {
-        const int a = nl > 0 ? __ldg(lvlStart + l0 + nl - 1) + tid : -1;
-        prefetch_bwd(bc, (nl > 0 && a < __ldg(lvlStart + l0 + nl)) ? a : -1, Uptr, Ucol, Uv, Dv);
-    }
-    for (int L = nl - 1; L >= 0; --L) {
-        const int k1 = __ldg(lvlStart + l0 + L + 1);
-        for (int k = __ldg(lvlStart + l0 + L) + tid; k < k1; k += blockDim.x) {
-            if (bc.k != k) prefetch_bwd(bc, k, Uptr, Ucol, Uv, Dv);
-            prefetch_bwd(bn, next_row(k, k1, L, nl, l0, lvlStart, 0), Uptr, Ucol, Uv, Dv);
-            const int li = k - row0;
-            TV yi[3] = {y[li * 3 + 0], y[li * 3 + 1], y[li * 3 + 2]};
-#pragma unroll
-            for (int j = 0; j < kPre; ++j)
-                if (bc.p0 + j < bc.p1) sub_block(yi, bc.a[j], y, bc.c[j]);
-            for (int p = bc.p0 + kPre; p < bc.p1; ++p) {
-                TF a[9];
-#pragma unroll
-                for (int e = 0; e < 9; ++e) a[e] = __ldg(Uv + size_t(p) * 9 + e);
-                sub_block(yi, a, y, __ldg(Ucol + p));
-            }
-            const TV t0 = rdot(bc.d, yi), t1 = rdot(bc.d + 3, yi), t2 = rdot(bc.d + 6, yi);
-            y[li * 3 + 0] = t0; y[li * 3 + 1] = t1; y[li * 3 + 2] = t2;
-            if (writeZ) {
-                z[size_t(k) * 3 + 0] = double(t0);
-                z[size_t(k) * 3 + 1] = double(t1);
-                z[size_t(k) * 3 + 2] = double(t2);
-            }
-            bc = bn;
-        }
-        __syncthreads();
+    const TF* d = R.a + 9 * SLOTS;
+    const TV t0 = rdot(d, yi), t1 = rdot(d + 3, yi), t2 = rdot(d + 6, yi);
+    y[li * 3 + 0] = t0; y[li * 3 + 1] = t1; y[li * 3 + 2] = t2;
+    if (writeZ) {
+        z[size_t(k) * 3 + 0] = XP ? da(double(t0), R.xp) : double(t0);
+        z[size_t(k) * 3 + 1] = double(t1);
+        z[size_t(k) * 3 + 2] = double(t2);
     }
 }
 
+template <class TF, class TI, int MODE>
+__device__ __forceinline__ void prefetch_fwd_level(const IluArgs<TF>& F, const int* lv, int L, const TI* r, const double* pv,
+                                                   const double* v) {
+    const size_t s = size_t(__ldg(lv + L)), e = size_t(__ldg(lv + L + 1));
+    l2_prefetch(F.L, s * LREC * sizeof(TF), e * LREC * sizeof(TF));
+    l2_prefetch(F.Lslot, s * sizeof(int4), e * sizeof(int4));
+    l2_prefetch(r, s * 3 * sizeof(TI), e * 3 * sizeof(TI));
+    if (MODE == IN_PUPDATE) l2_prefetch(pv, s * 24, e * 24);
+    if (MODE != IN_PLAIN) l2_prefetch(v, s * 24, e * 24);
+}
+template <class TF>
+__device__ __forceinline__ void prefetch_bwd_level(const IluArgs<TF>& F, const int* lv, int L) {
+    const size_t s = size_t(__ldg(lv + L)), e = size_t(__ldg(lv + L + 1));
+    l2_prefetch(F.UD, s * UREC * sizeof(TF), e * UREC * sizeof(TF));
+    l2_prefetch(F.Uslot, s * sizeof(int4), e * sizeof(int4));
+}
+
+// The level loops below run levels in pairs with fixed register roles (cur, nxt) = (A, B) then (B, A): a level
+// works on the rows in cur while the same threads' rows of the next level load into nxt, so every row's loads
+// are in flight for a whole level. NSET row sets cover levels of up to NSET x blockDim rows this way; further
+// rows of a level load when they are reached.
+template <int NSET>
+__device__ __forceinline__ int row_of(int s, int e, int j) {
+    const int k = s + int(threadIdx.x) + j * int(blockDim.x);
+    return k < e ? k : -1;
+}
+
+template <class TF, class TV, class TI, int MODE, int NSET>
+__device__ __forceinline__ void fwd_level(const IluArgs<TF>& F, const int* lv, int L, int nl, FwdRow<TF, TI, MODE>* cur,
+                                          FwdRow<TF, TI, MODE>* nxt, int row0, const TI* r, double* pv, const double* v, TV* y,
+                                          double beta, double omega, double alpha) {
+    const int s = __ldg(lv + L), e = __ldg(lv + L + 1);
+    if (threadIdx.x == 0 && L + kAhead < nl) prefetch_fwd_level<TF, TI, MODE>(F, lv, L + kAhead, r, pv, v);
+    if (L + 1 < nl) {
+        const int e1 = __ldg(lv + L + 2);
+#pragma unroll
+        for (int j = 0; j < NSET; ++j) load_fwd(nxt[j], row_of<NSET>(e, e1, j), F, r, pv, v);
+    }
+#pragma unroll
+    for (int j = 0; j < NSET; ++j) {
+        const int k = row_of<NSET>(s, e, j);
+        if (k >= 0) {
+            if (cur[j].k != k) load_fwd(cur[j], k, F, r, pv, v);
+            fwd_step<TF, TV, TI, MODE>(cur[j], F, row0, y, pv, beta, omega, alpha);
+        }
+    }
+    for (int k = s + int(threadIdx.x) + NSET * int(blockDim.x); k < e; k += blockDim.x) {
+        load_fwd(cur[0], k, F, r, pv, v);
+        fwd_step<TF, TV, TI, MODE>(cur[0], F, row0, y, pv, beta, omega, alpha);
+    }
+    __syncthreads();
+}
+
+template <class TF, class TV, bool XP, int NSET, class TX>
+__device__ __forceinline__ void bwd_level(const IluArgs<TF>& F, const int* lv, int L, BwdRow<TF>* cur, BwdRow<TF>* nxt, int row0,
+                                          const TX* xp, TV* y, double* z, bool writeZ) {
+    const int s = __ldg(lv + L), e = __ldg(lv + L + 1);
+    if (threadIdx.x == 0 && L - kAhead >= 0) prefetch_bwd_level(F, lv, L - kAhead);
+    if (L > 0) {
+        const int s1 = __ldg(lv + L - 1);
+#pragma unroll
+        for (int j = 0; j < NSET; ++j) load_bwd(nxt[j], row_of<NSET>(s1, s, j), F, xp, row0);
+    }
+#pragma unroll
+    for (int j = 0; j < NSET; ++j) {
+        const int k = row_of<NSET>(s, e, j);
+        if (k >= 0) {
+            if (cur[j].k != k) load_bwd(cur[j], k, F, xp, row0);
+            bwd_step<TF, TV, XP>(cur[j], F, row0, y, z, writeZ);
+        }
+    }
+    for (int k = s + int(threadIdx.x) + NSET * int(blockDim.x); k < e; k += blockDim.x) {
+        load_bwd(cur[0], k, F, xp, row0);
+        bwd_step<TF, TV, XP>(cur[0], F, row0, y, z, writeZ);
+    }
+    __syncthreads();
+}
+
+// Both sweeps of one system by the calling thread block (y: the sweep vector of this system, on chip or in z;
+// xp: with XP, the CPR pressure correction added to z_p as z is written)
+template <class TF, class TV, class TI, int MODE, bool XP, class TX>
+__device__ void ilu_body(const IluArgs<TF>& F, int row0, int l0, int nl, const TI* r, double* pv, const double* v, double* z, TV* y,
+                         bool writeZ, double beta, double omega, double alpha, const TX* xp) {
+    constexpr int NSET = (sizeof(TF) == 4 && MODE == IN_PLAIN) ? 2 : 1;
+    const int* lv = F.lvlStart + l0;
+    if (threadIdx.x == 0)
+        for (int L = 0; L < kAhead && L < nl; ++L) prefetch_fwd_level<TF, TI, MODE>(F, lv, L, r, pv, v);
+    {
+        FwdRow<TF, TI, MODE> A[NSET], B[NSET];
+        if (nl > 0) {
+            const int s = __ldg(lv), e = __ldg(lv + 1);
+#pragma unroll
+            for (int j = 0; j < NSET; ++j) load_fwd(A[j], row_of<NSET>(s, e, j), F, r, pv, v);
+        }
+        for (int L = 0; L < nl; L += 2) {
+            fwd_level<TF, TV, TI, MODE, NSET>(F, lv, L, nl, A, B, row0, r, pv, v, y, beta, omega, alpha);
+            if (L + 1 < nl) fwd_level<TF, TV, TI, MODE, NSET>(F, lv, L + 1, nl, B, A, row0, r, pv, v, y, beta, omega, alpha);
+        }
+    }
+    if (threadIdx.x == 0)
+        for (int L = nl - 1; L >= 0 && L >= nl - kAhead; --L) prefetch_bwd_level(F, lv, L);
+    {
+        const TX* xq = XP ? xp : nullptr;
+        BwdRow<TF> A[NSET], B[NSET];
+        if (nl > 0) {
+            const int s = __ldg(lv + nl - 1), e = __ldg(lv + nl);
+#pragma unroll
+            for (int j = 0; j < NSET; ++j) load_bwd(A[j], row_of<NSET>(s, e, j), F, xq, row0);
+        }
+        for (int L = nl - 1; L >= 0; L -= 2) {
+            bwd_level<TF, TV, XP, NSET>(F, lv, L, A, B, row0, xq, y, z, writeZ);
+            if (L - 1 >= 0) bwd_level<TF, TV, XP, NSET>(F, lv, L - 1, B, A, row0, xq, y, z, writeZ);
+        }
+    }
+}
+
 template <class TF, class TV, int MODE>
-__global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
-                                                        const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
-                                                        const int* __restrict__ Lcol, const TF* __restrict__ Lv,
-                                                        const int* __restrict__ Uptr, const int* __restrict__ Ucol,
-                                                        const TF* __restrict__ Uv, const TF* __restrict__ Dv, const double* r, double* pv,
-                                                        const double* v, double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
+__global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(IluArgs<TF> F, const double* r, double* pv, const double* v, double* z,
+                                                        TV* yglob, size_t smemBytes, const KScal* ks) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int s = blockIdx.x;
-    const int row0 = __ldg(sysRow0 + s), ns = __ldg(sysRow0 + s + 1) - row0;
+    const int row0 = __ldg(F.sysRow0 + s), ns = __ldg(F.sysRow0 + s + 1) - row0;
     double beta = 0, omega = 0, alpha = 0;
     if (ks) {
         const KScal& K = ks[s];
@@ -224,16 +351,30 @@ __global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(const int* __restrict__
     // sweep vector: on chip when it fits, else global (yglob: z itself for TV = double)
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
     TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
-    const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
-    ilu_body<TF, TV, MODE>(row0, l0, nl, lvlStart, Lptr, Lcol, Lv, Uptr, Ucol, Uv, Dv, r, pv, v, z, y,
-                           onchip || sizeof(TV) != sizeof(double), beta, omega, alpha);
+    const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
+    ilu_body<TF, TV, double, MODE, false, double>(F, row0, l0, nl, r, pv, v, z, y, onchip || sizeof(TV) != sizeof(double), beta, omega,
+                                                  alpha, nullptr);
 }
 
 // ------------------------------------------------------------------ CPR (BlockCPR::apply, engine/src/bsr.cpp:1061-1084)
-struct AmgArgs {
+template <class TA>
+struct CprArgs {
     const AmgSysLv* lv;
     int maxL;
-    const int *rp, *ci, *diag, *lvl, *agg, *memPtr, *mem, *luPerm, *piv;
+    const int* lvl;                   // GS levels of every (system, level)
+    const int* ci;                    // level CSR columns / values (entries beyond the row slots)
+    const TA* val;
+    const int* slotCol;
+    const TA* slotVal;
+    const TA* diagVal;
+    const int4* rowMeta;
+    const int *agg, *memPtr, *mem;
+    const TA* lu;                     // coarsest dense LU
+    const int *luPerm, *cin;
+    TA *x, *b, *r;                    // V-cycle vectors in global memory (levels that do not fit on chip)
+    const double* w;
+    double* T;
+    const TA *sp, *spLov, *spUov;     // pressure columns of S in slot order
 };
 
 // V-cycle arithmetic type: FP64 explicitly rounded (bitwise the reference) or FP32
@@ -246,154 +387,316 @@ __device__ __forceinline__ float aadd(float a, float b) { return a + b; }
 __device__ __forceinline__ float asub(float a, float b) { return a - b; }
 __device__ __forceinline__ float adiv(float a, float b) { return a / b; }
 
-// Gauss-Seidel sweep of one level (engine/src/amg.cpp:98-113) over its GS levels: forward from x = 0 (only the
-// lower entries contribute, bitwise the full sum), or forward / backward from the current x (full rows: entries of
-// later rows still hold the old x). Rows of one GS level are independent.
-template <class TA>
-__device__ void gs_sweep(const AmgSysLv& A, const AmgArgs& G, const TA* __restrict__ val, TA* x, const TA* b, bool forward, bool fromZero) {
-    const int* rp = G.rp + A.rpOff;
-    const int* ci = G.ci + A.entOff;
-    const int* dg = G.diag + A.rowOff;
-    const int* lv = G.lvl + A.lvlOff;
-    const TA* v = val + A.entOff;
-    for (int g = 0; g < A.nl; ++g) {
-        const int L = forward ? g : A.nl - 1 - g;
-        const int k1 = __ldg(lv + L + 1);
-        for (int k = __ldg(lv + L) + int(threadIdx.x); k < k1; k += blockDim.x) {
-            const int d = __ldg(dg + k);
-            const int pe = fromZero ? d : __ldg(rp + k + 1);
-            TA s = b[k];
-            for (int p = __ldg(rp + k); p < pe; ++p)
-                if (p != d) s = asub(s, amul(v[p], x[__ldg(ci + p)]));
-            x[k] = adiv(s, v[d]);
+// one row of an AMG level in registers: W slot values / columns, diagonal, {entries before the diagonal,
+// off-diagonal entries, continuation position, diagonal position}
+template <class TA, int W>
+struct GsRow {
+    int k;
+    int4 m;
+    TA v[W];
+    int c[W];
+    TA d;
+};
+template <class TA, int W>
+__device__ __forceinline__ void load_gs(GsRow<TA, W>& R, int k, const AmgSysLv& A, const CprArgs<TA>& C) {
+    R.k = k;
+    if (k < 0) return;
+    R.m = __ldg(C.rowMeta + A.rowOff + k);
+    ldrec(R.v, C.slotVal + size_t(A.slotOff) + size_t(k) * W);
+    ldrec(R.c, C.slotCol + size_t(A.slotOff) + size_t(k) * W);
+    R.d = __ldg(C.diagVal + A.rowOff + k);
+}
+// Gauss-Seidel update of row k (engine/src/amg.cpp:98-113): s = b_k - sum_{p != diag} a_p x_col(p), in row order;
+// from x = 0 only the entries before the diagonal (the others multiply zeros)
+template <class TA, int W>
+__device__ __forceinline__ void gs_step(const GsRow<TA, W>& R, const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, bool fromZero) {
+    TA s = b[R.k];
+    const int lim = fromZero ? R.m.x : R.m.y;
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+        if (j < lim) s = asub(s, amul(R.v[j], x[R.c[j]]));
+    if (lim > W) {
+        const int* ci = C.ci + A.entOff;
+        const TA* val = C.val + A.entOff;
+        for (int p = R.m.z, jo = W; jo < lim; ++p) {
+            if (p == R.m.w) continue;
+            s = asub(s, amul(val[p], x[__ldg(ci + p)]));
+            ++jo;
         }
-        __syncthreads();
     }
+    x[R.k] = adiv(s, R.d);
 }
 
-// coarsest level: x = LU^-1 b with the dense LU of the natural numbering (engine/src/amg.cpp:306-312), one warp;
-// work = the level's residual vector, used in natural order
-template <class TA>
-__device__ void coarse_solve(const AmgSysLv& A, const AmgArgs& G, const TA* __restrict__ luAll, TA* x, const TA* b, TA* work) {
-    const int m = A.n;
-    const TA* lu = luAll + A.luOff;
-    const int* nat = G.luPerm + A.luRowOff;
-    const int* piv = G.piv + A.luRowOff;
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        for (int k = lane; k < m; k += 32) work[__ldg(nat + k)] = b[k];
-        __syncwarp();
-        if (lane == 0)
-            for (int k = 0; k < m; ++k) {
-                const int pk = __ldg(piv + k);
-                if (pk != k) { const TA t = work[k]; work[k] = work[pk]; work[pk] = t; }
-            }
-        __syncwarp();
-        for (int j = 0; j < m; ++j) {                    // unit lower: every row gets its terms in ascending j
-            const TA xj = work[j];
-            for (int i = j + 1 + lane; i < m; i += 32) work[i] = asub(work[i], amul(lu[size_t(i) * m + j], xj));
-            __syncwarp();
+template <class TA, int W>
+__device__ __forceinline__ void prefetch_gs_level(const AmgSysLv& A, const CprArgs<TA>& C, const int* lv, int L, const TA* bg) {
+    const size_t s = size_t(__ldg(lv + L)), e = size_t(__ldg(lv + L + 1));
+    l2_prefetch(C.slotVal + A.slotOff, s * W * sizeof(TA), e * W * sizeof(TA));
+    l2_prefetch(C.slotCol + A.slotOff, s * W * sizeof(int), e * W * sizeof(int));
+    l2_prefetch(C.rowMeta + A.rowOff, s * sizeof(int4), e * sizeof(int4));
+    if (bg) l2_prefetch(bg, s * sizeof(TA), e * sizeof(TA));
+}
+
+template <class TA, int W, int NSET>
+__device__ __forceinline__ void gs_level(const AmgSysLv& A, const CprArgs<TA>& C, const int* lv, int L, int Lnext, int g, int dir,
+                                         GsRow<TA, W>* cur, GsRow<TA, W>* nxt, TA* x, const TA* b, const TA* bg, bool fromZero) {
+    const int s = __ldg(lv + L), e = __ldg(lv + L + 1);
+    if (threadIdx.x == 0 && g + kAhead < A.nl) prefetch_gs_level<TA, W>(A, C, lv, L + dir * kAhead, bg);
+    if (Lnext >= 0 && Lnext < A.nl) {
+        const int s1 = __ldg(lv + Lnext), e1 = __ldg(lv + Lnext + 1);
+#pragma unroll
+        for (int j = 0; j < NSET; ++j) load_gs(nxt[j], row_of<NSET>(s1, e1, j), A, C);
+    }
+#pragma unroll
+    for (int j = 0; j < NSET; ++j) {
+        const int k = row_of<NSET>(s, e, j);
+        if (k >= 0) {
+            if (cur[j].k != k) load_gs(cur[j], k, A, C);
+            gs_step(cur[j], A, C, x, b, fromZero);
         }
-        for (int j = m - 1; j >= 0; --j) {               // upper
-            if (lane == 0) work[j] = adiv(work[j], lu[size_t(j) * m + j]);
-            __syncwarp();
-            const TA xj = work[j];
-            for (int i = lane; i < j; i += 32) work[i] = asub(work[i], amul(lu[size_t(i) * m + j], xj));
-            __syncwarp();
-        }
-        for (int k = lane; k < m; k += 32) x[k] = work[__ldg(nat + k)];
+    }
+    for (int k = s + int(threadIdx.x) + NSET * int(blockDim.x); k < e; k += blockDim.x) {
+        load_gs(cur[0], k, A, C);
+        gs_step(cur[0], A, C, x, b, fromZero);
     }
     __syncthreads();
 }
 
-// AMG::cycle (engine/src/amg.cpp:303-329) for system s, level 0 rhs in b + lv[0].rowOff
+// one Gauss-Seidel sweep of a level over its GS levels (forward, or backward for the post-smoothing: valid on the
+// structurally symmetric levels), rows of one GS level in parallel; levels in pairs as the BILU0 sweeps
+template <class TA, int W>
+__device__ __noinline__ void gs_sweep(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, bool bGlobal, bool forward, bool fromZero) {
+    constexpr int NSET = (sizeof(TA) == 4 || W == AMG_W0) ? 2 : 1;
+    const int* lv = C.lvl + A.lvlOff;
+    const int nl = A.nl, dir = forward ? 1 : -1;
+    const TA* bg = bGlobal ? b : nullptr;
+    const int Lfirst = forward ? 0 : nl - 1;
+    if (threadIdx.x == 0)
+        for (int g = 0; g < kAhead && g < nl; ++g) prefetch_gs_level<TA, W>(A, C, lv, Lfirst + dir * g, bg);
+    GsRow<TA, W> P[NSET], Q[NSET];
+    if (nl > 0) {
+        const int s = __ldg(lv + Lfirst), e = __ldg(lv + Lfirst + 1);
+#pragma unroll
+        for (int j = 0; j < NSET; ++j) load_gs(P[j], row_of<NSET>(s, e, j), A, C);
+    }
+    for (int g = 0; g < nl; g += 2) {
+        const int L = Lfirst + dir * g;
+        gs_level<TA, W, NSET>(A, C, lv, L, L + dir, g, dir, P, Q, x, b, bg, fromZero);
+        if (g + 1 < nl) gs_level<TA, W, NSET>(A, C, lv, L + dir, L + 2 * dir, g + 1, dir, Q, P, x, b, bg, fromZero);
+    }
+}
+
+// r = b - A x (engine/src/amg.cpp:321-322: the row sum from zero in entry order, diagonal at its place)
+template <class TA, int W>
+__device__ __noinline__ void residual(const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b, TA* r) {
+    for (int k = threadIdx.x; k < A.n; k += blockDim.x) {
+        GsRow<TA, W> R;
+        load_gs(R, k, A, C);
+        const int nlow = R.m.x, noff = R.m.y;
+        TA t = TA(0);
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            if (j == nlow) t = aadd(t, amul(R.d, x[k]));
+            if (j < noff) t = aadd(t, amul(R.v[j], x[R.c[j]]));
+        }
+        // entries after the slots (the diagonal among them when it comes after W off-diagonal entries)
+        int rem = noff + 1 - (noff < W ? noff : W) - (nlow < W ? 1 : 0);
+        if (rem > 0) {
+            const int* ci = C.ci + A.entOff;
+            const TA* val = C.val + A.entOff;
+            for (int p = R.m.z; rem > 0; ++p, --rem) t = aadd(t, amul(val[p], x[__ldg(ci + p)]));
+        }
+        r[k] = asub(b[k], t);
+    }
+}
+
+// coarsest level: x = LU^-1 b with the dense LU of the natural numbering (engine/src/amg.cpp:306-312). 32-column
+// panels: warp 0 solves the panel's triangle with shuffles, then every thread updates its rows below (forward)
+// or above (backward) with the panel. The forward substitution subtracts every row's terms in ascending column
+// order, as the reference; the backward one takes the panels last to first (rounding-level differences).
 template <class TA>
-__device__ void vcycle(int s, const AmgArgs& G, const TA* __restrict__ val, const TA* __restrict__ lu, TA* x, TA* b, TA* r) {
+__device__ __noinline__ void coarse_dense(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, TA* work) {
+    const int m = A.n, tid = int(threadIdx.x), nt = int(blockDim.x), lane = tid & 31;
+    const TA* lu = C.lu + A.luOff;
+    const int* nat = C.luPerm + A.luRowOff;
+    const int* cin = C.cin + A.luRowOff;
+    for (int i = tid; i < m; i += nt) work[i] = b[__ldg(cin + i)];
+    __syncthreads();
+    for (int j0 = 0; j0 < m; j0 += 32) {
+        const int jb = min(32, m - j0);
+        if (tid < 32) {
+            const int i = j0 + lane;
+            TA a[32];
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) a[jj] = (lane < jb && jj < lane) ? __ldg(lu + size_t(i) * m + j0 + jj) : TA(0);
+            TA s = lane < jb ? work[i] : TA(0);
+#pragma unroll
+            for (int jj = 0; jj < 31; ++jj) {
+                const TA xj = __shfl_sync(0xffffffffu, s, jj);
+                if (jj < lane && lane < jb) s = asub(s, amul(a[jj], xj));
+            }
+            if (lane < jb) work[i] = s;
+        }
+        __syncthreads();
+        for (int i = j0 + jb + tid; i < m; i += nt) {
+            const TA* row = lu + size_t(i) * m + j0;
+            TA s = work[i];
+#pragma unroll 8
+            for (int jj = 0; jj < jb; ++jj) s = asub(s, amul(__ldg(row + jj), work[j0 + jj]));
+            work[i] = s;
+        }
+        __syncthreads();
+    }
+    for (int j0 = ((m - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
+        const int jb = min(32, m - j0);
+        if (tid < 32) {
+            const int i = j0 + lane;
+            TA a[32];
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) a[jj] = (lane < jb && jj > lane && jj < jb) ? __ldg(lu + size_t(i) * m + j0 + jj) : TA(0);
+            const TA dg = lane < jb ? __ldg(lu + size_t(i) * m + i) : TA(1);
+            TA s = lane < jb ? work[i] : TA(0);
+#pragma unroll
+            for (int jj = 31; jj >= 0; --jj) {
+                if (jj < jb) {
+                    if (lane == jj) s = adiv(s, dg);
+                    const TA xj = __shfl_sync(0xffffffffu, s, jj);
+                    if (lane < jj) s = asub(s, amul(a[jj], xj));
+                }
+            }
+            if (lane < jb) work[i] = s;
+        }
+        __syncthreads();
+        for (int i = tid; i < j0; i += nt) {
+            const TA* row = lu + size_t(i) * m + j0;
+            TA s = work[i];
+#pragma unroll 8
+            for (int jj = 0; jj < jb; ++jj) s = asub(s, amul(__ldg(row + jj), work[j0 + jj]));
+            work[i] = s;
+        }
+        __syncthreads();
+    }
+    for (int k = tid; k < m; k += nt) x[k] = work[__ldg(nat + k)];
+    __syncthreads();
+}
+
+// where the V-cycle vectors of system s live: shared memory (x, then b, then r, as far as they fit) or global
+template <class TA>
+struct VVecs {
+    TA *xs, *bs, *rs;                 // on-chip bases (null when global)
+    bool bGlobal;
+    __device__ TA* x(const AmgSysLv& A, const CprArgs<TA>& C) const { return xs ? xs + A.locOff : C.x + A.rowOff; }
+    __device__ TA* b(const AmgSysLv& A, const CprArgs<TA>& C) const { return bs ? bs + A.locOff : C.b + A.rowOff; }
+    __device__ TA* r(const AmgSysLv& A, const CprArgs<TA>& C) const { return rs ? rs + A.locOff : C.r + A.rowOff; }
+};
+
+template <class TA, int W>
+__device__ void gs_sweep_w(const AmgSysLv& A, const CprArgs<TA>& C, const VVecs<TA>& V, bool forward, bool fromZero) {
+    gs_sweep<TA, W>(A, C, V.x(A, C), V.b(A, C), V.bGlobal, forward, fromZero);
+}
+template <class TA>
+__device__ void gs_any(const AmgSysLv& A, const CprArgs<TA>& C, const VVecs<TA>& V, bool forward, bool fromZero) {
+    if (A.W == AMG_W0) gs_sweep_w<TA, AMG_W0>(A, C, V, forward, fromZero);
+    else gs_sweep_w<TA, AMG_W1>(A, C, V, forward, fromZero);
+}
+
+// AMG::cycle (engine/src/amg.cpp:303-329) for system s, level-0 right-hand side already in place
+template <class TA>
+__device__ __noinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
     int nlev = 0;
-    while (nlev < G.maxL && G.lv[s * G.maxL + nlev].n > 0) ++nlev;
+    while (nlev < C.maxL && C.lv[s * C.maxL + nlev].n > 0) ++nlev;
     int l = 0;
     for (; l < nlev; ++l) {
-        const AmgSysLv A = G.lv[s * G.maxL + l];
-        TA* xl = x + A.rowOff;
-        TA* bl = b + A.rowOff;
-        TA* rl = r + A.rowOff;
+        const AmgSysLv A = C.lv[s * C.maxL + l];
         if (A.coarse) {
             if (A.dense) {
-                coarse_solve(A, G, lu, xl, bl, rl);
+                coarse_dense(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
             } else {                                      // 20 symmetric GS sweeps from x = 0 (amg.cpp:313-315)
+                TA* xl = V.x(A, C);
                 for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = TA(0);
                 __syncthreads();
                 for (int it = 0; it < 20; ++it) {
-                    gs_sweep(A, G, val, xl, bl, true, false);
-                    gs_sweep(A, G, val, xl, bl, false, false);
+                    gs_any(A, C, V, true, false);
+                    gs_any(A, C, V, false, false);
                 }
             }
             break;
         }
-        gs_sweep(A, G, val, xl, bl, true, true);
-        // residual r = b - A x (amg.cpp:321-322)
-        {
-            const int* rp = G.rp + A.rpOff;
-            const int* ci = G.ci + A.entOff;
-            const TA* v = val + A.entOff;
-            for (int k = threadIdx.x; k < A.n; k += blockDim.x) {
-                TA t = TA(0);
-                for (int p = __ldg(rp + k); p < __ldg(rp + k + 1); ++p) t = aadd(t, amul(v[p], xl[__ldg(ci + p)]));
-                rl[k] = asub(bl[k], t);
-            }
-        }
+        gs_any(A, C, V, true, true);
+        if (A.W == AMG_W0) residual<TA, AMG_W0>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
+        else residual<TA, AMG_W1>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
         __syncthreads();
         // restriction b_{l+1} = R r: members in ascending natural order (amg.cpp:324)
         {
-            const AmgSysLv C = G.lv[s * G.maxL + l + 1];
-            const int* mp = G.memPtr + C.rpOff;
-            const int* mem = G.mem + C.memOff;
-            TA* bc = b + C.rowOff;
-            for (int I = threadIdx.x; I < C.n; I += blockDim.x) {
+            const AmgSysLv Cl = C.lv[s * C.maxL + l + 1];
+            const int* mp = C.memPtr + Cl.rpOff;
+            const int* mem = C.mem + Cl.memOff;
+            const TA* rl = V.r(A, C);
+            TA* bc = V.b(Cl, C);
+            for (int I = threadIdx.x; I < Cl.n; I += blockDim.x) {
+                const int q0 = __ldg(mp + I), q1 = __ldg(mp + I + 1);
                 TA t = TA(0);
-                for (int q = __ldg(mp + I); q < __ldg(mp + I + 1); ++q) t = aadd(t, rl[__ldg(mem + q)]);
+                for (int q = q0; q < q1; ++q) t = aadd(t, rl[__ldg(mem + q)]);
                 bc[I] = t;
             }
         }
         __syncthreads();
     }
     for (l = l - 1; l >= 0; --l) {                          // prolongation and post-smoothing (amg.cpp:326-327)
-        const AmgSysLv A = G.lv[s * G.maxL + l];
-        const AmgSysLv C = G.lv[s * G.maxL + l + 1];
-        TA* xl = x + A.rowOff;
-        const TA* xc = x + C.rowOff;
-        const int* agg = G.agg + A.rowOff;
+        const AmgSysLv A = C.lv[s * C.maxL + l];
+        const AmgSysLv Cl = C.lv[s * C.maxL + l + 1];
+        TA* xl = V.x(A, C);
+        const TA* xc = V.x(Cl, C);
+        const int* agg = C.agg + A.rowOff;
         for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = aadd(xl[k], xc[__ldg(agg + k)]);
         __syncthreads();
-        gs_sweep(A, G, val, xl, b + A.rowOff, false, false);
+        gs_any(A, C, V, false, false);
     }
 }
 
+// t -= S_kj[:,p] xp_j for the pressure column of one block (TT: the arithmetic of the second-stage input)
+__device__ __forceinline__ void sub_p(double (&acc)[3], const double* s3, double xk) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) acc[e] = ds(acc[e], dm(s3[e], xk));
+}
+__device__ __forceinline__ void sub_p(double (&acc)[3], const float* s3, double xk) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) acc[e] = ds(acc[e], dm(double(s3[e]), xk));
+}
+__device__ __forceinline__ void sub_p(float (&acc)[3], const float* s3, float xk) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) acc[e] = acc[e] - s3[e] * xk;
+}
+
+// One CPR application per system. The second-stage input t lives in C.T with the sweep vector's type TV: FP64
+// for the FP64 and mixed forms, FP32 for the all-FP32 preconditioner, whose restriction w . r, t = r - S[:,p] xp
+// and sweeps then run in FP32 arithmetic (the FP64 unit is a small fraction of the FP32 rate on this part).
 template <class TF, class TV, class TA, int MODE>
-__global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
-                                                        const int* __restrict__ lvlStart, const int* __restrict__ Lptr,
-                                                        const int* __restrict__ Lcol, const TF* __restrict__ Lv,
-                                                        const int* __restrict__ Uptr, const int* __restrict__ Ucol,
-                                                        const TF* __restrict__ Uv, const TF* __restrict__ Dv,
-                                                        const int* __restrict__ rowPtr, const int* __restrict__ col,
-                                                        const double* __restrict__ val, const double* __restrict__ w, double* T,
-                                                        AmgArgs G, const TA* __restrict__ aval, const TA* __restrict__ alu, TA* ax, TA* ab,
-                                                        TA* ar, const double* r, double* pv, const double* v, double* z, TV* yglob,
-                                                        size_t smemBytes, const KScal* ks) {
+__global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(IluArgs<TF> F, CprArgs<TA> C, const double* r, double* pv, const double* v,
+                                                        double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int s = blockIdx.x;
-    const int row0 = __ldg(sysRow0 + s), ns = __ldg(sysRow0 + s + 1) - row0;
+    const int s = blockIdx.x, tid = int(threadIdx.x), nt = int(blockDim.x);
+    const int row0 = __ldg(F.sysRow0 + s), ns = __ldg(F.sysRow0 + s + 1) - row0;
     double beta = 0, omega = 0, alpha = 0;
     if (ks) {
         const KScal& K = ks[s];
         if (K.status != ST_RUNNING) return;
         beta = K.beta; omega = K.omega; alpha = K.alpha;
     }
-    const AmgSysLv A0 = G.lv[s * G.maxL];
-    TA* b0 = ab + A0.rowOff;
-    const TA* xp = ax + A0.rowOff;
+    TV* T = reinterpret_cast<TV*>(C.T);
+    // V-cycle vectors of this system: as many of x, b, r on chip as fit
+    int R = 0;
+    for (int l = 0; l < C.maxL; ++l) R += C.lv[s * C.maxL + l].n;
+    const size_t vb = size_t(R) * sizeof(TA);
+    VVecs<TA> V;
+    TA* sm = reinterpret_cast<TA*>(smraw);
+    V.xs = vb <= smemBytes ? sm : nullptr;
+    V.bs = 2 * vb <= smemBytes ? sm + R : nullptr;
+    V.rs = 3 * vb <= smemBytes ? sm + 2 * R : nullptr;
+    V.bGlobal = V.bs == nullptr;
+    const AmgSysLv A0 = C.lv[s * C.maxL];
+    TA* b0 = V.b(A0, C);
     // input (fused Krylov update) and pressure restriction rp = w . r (bsr.cpp:1064-1067)
-    for (int k = row0 + int(threadIdx.x); k < row0 + ns; k += blockDim.x) {
+    for (int k = row0 + tid; k < row0 + ns; k += nt) {
         double in[3];
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
@@ -401,46 +704,90 @@ __global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(const int* __restrict__
             if (MODE == IN_PUPDATE) { in[e] = da(r[q], dm(beta, ds(pv[q], dm(omega, v[q])))); pv[q] = in[e]; }
             else if (MODE == IN_SUPDATE) { in[e] = ds(r[q], dm(alpha, v[q])); pv[q] = in[e]; }
             else in[e] = r[q];
-            T[q] = in[e];
+            T[q] = TV(in[e]);
         }
-        const double* wk = w + size_t(k) * 3;
-        b0[k - row0] = TA(da(da(dm(wk[0], in[0]), dm(wk[1], in[1])), dm(wk[2], in[2])));
+        const double* wk = C.w + size_t(k) * 3;
+        if (sizeof(TV) == 4) {
+            const float i0 = float(in[0]), i1 = float(in[1]), i2 = float(in[2]);
+            b0[k - row0] = TA(float(__ldg(wk)) * i0 + float(__ldg(wk + 1)) * i1 + float(__ldg(wk + 2)) * i2);
+        } else {
+            b0[k - row0] = TA(da(da(dm(__ldg(wk), in[0]), dm(__ldg(wk + 1), in[1])), dm(__ldg(wk + 2), in[2])));
+        }
     }
     __syncthreads();
-    vcycle<TA>(s, G, aval, alu, ax, ab, ar);
-    // second stage on t = r - S[:,p] xp (pressure column only, bsr.cpp:1071-1081)
-    for (int k = row0 + int(threadIdx.x); k < row0 + ns; k += blockDim.x) {
-        double acc[3] = {T[size_t(k) * 3], T[size_t(k) * 3 + 1], T[size_t(k) * 3 + 2]};
-        for (int p = __ldg(rowPtr + k); p < __ldg(rowPtr + k + 1); ++p) {
-            const double xk = double(xp[__ldg(col + p) - row0]);
-            const double* B = val + size_t(p) * 9;
-            acc[0] = ds(acc[0], dm(__ldg(B), xk));
-            acc[1] = ds(acc[1], dm(__ldg(B + 3), xk));
-            acc[2] = ds(acc[2], dm(__ldg(B + 6), xk));
-        }
+    vcycle<TA>(s, C, V);
+    // second stage on t = r - S[:,p] xp (pressure columns in S's row order, bsr.cpp:1071-1081); xp to global
+    // memory for the final correction when it lived on chip
+    const TA* xp = V.x(A0, C);
+    TA* xpg = C.x + A0.rowOff;
+    for (int k = row0 + tid; k < row0 + ns; k += nt) {
+        const int4 lc = __ldg(F.Lslot + k), uc = __ldg(F.Uslot + k);
+        TA sp[SPREC];
+        ldrec(sp, C.sp + size_t(k) * SPREC);
+        TV acc[3] = {T[size_t(k) * 3], T[size_t(k) * 3 + 1], T[size_t(k) * 3 + 2]};
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (slot_col(lc, j) >= 0) sub_p(acc, sp + 3 * j, TV(xp[slot_col(lc, j)]));
+        if (lc.w >= 0)
+            for (int q = lc.w;; ++q) {
+                const int c = __ldg(F.LovCol + q);
+                if (c < 0) break;
+                const TA s3[3] = {__ldg(C.spLov + size_t(q) * 3), __ldg(C.spLov + size_t(q) * 3 + 1), __ldg(C.spLov + size_t(q) * 3 + 2)};
+                sub_p(acc, s3, TV(xp[c]));
+            }
+        sub_p(acc, sp + 3 * SLOTS, TV(xp[k - row0]));
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (slot_col(uc, j) >= 0) sub_p(acc, sp + 3 * (SLOTS + 1 + j), TV(xp[slot_col(uc, j)]));
+        if (uc.w >= 0)
+            for (int q = uc.w;; ++q) {
+                const int c = __ldg(F.UovCol + q);
+                if (c < 0) break;
+                const TA s3[3] = {__ldg(C.spUov + size_t(q) * 3), __ldg(C.spUov + size_t(q) * 3 + 1), __ldg(C.spUov + size_t(q) * 3 + 2)};
+                sub_p(acc, s3, TV(xp[c]));
+            }
         T[size_t(k) * 3] = acc[0]; T[size_t(k) * 3 + 1] = acc[1]; T[size_t(k) * 3 + 2] = acc[2];
+        if (V.xs) xpg[k - row0] = xp[k - row0];
     }
     __syncthreads();
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
     TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
-    const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
-    ilu_body<TF, TV, IN_PLAIN>(row0, l0, nl, lvlStart, Lptr, Lcol, Lv, Uptr, Ucol, Uv, Dv, T, nullptr, nullptr, z, y,
-                               onchip || sizeof(TV) != sizeof(double), 0, 0, 0);
-    // z_p += xp (bsr.cpp:1083)
-    for (int k = row0 + int(threadIdx.x); k < row0 + ns; k += blockDim.x) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xp[k - row0]));
+    const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
+    const bool writeZ = onchip || sizeof(TV) != sizeof(double);
+    if (writeZ) {   // y is not z: z_p += xp (bsr.cpp:1083) as z is written
+        ilu_body<TF, TV, TV, IN_PLAIN, true, TA>(F, row0, l0, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
+    } else {        // y is z itself: the correction after the sweeps
+        ilu_body<TF, TV, TV, IN_PLAIN, false, TA>(F, row0, l0, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
+        for (int k = row0 + tid; k < row0 + ns; k += nt) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xpg[k - row0]));
+    }
 }
 
-
-
+// factors (level-space CSR block order) -> slot records; overflow blocks
 template <class T>
-__global__ void k_pack(int n, int nL, int nU, const int* __restrict__ Lsrc, const int* __restrict__ Usrc, const int* __restrict__ Dsrc,
-                       const T* __restrict__ lu, T* L, T* U, T* D) {
-    const size_t total = (size_t(nL) + size_t(nU) + size_t(n)) * 9;
+__global__ void k_pack(int n, int nLov, int nUov, const int* __restrict__ LslotSrc, const int* __restrict__ UslotSrc,
+                       const int* __restrict__ Dsrc, const int* __restrict__ LovSrc, const int* __restrict__ UovSrc,
+                       const T* __restrict__ lu, T* L, T* UD, T* Lov, T* Uov) {
+    const size_t nL = size_t(n) * LREC, nUD = size_t(n) * UREC, nO = (size_t(nLov) + size_t(nUov)) * 9;
+    const size_t total = nL + nUD + nO;
     for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < total; q += size_t(gridDim.x) * blockDim.x) {
-        const size_t b = q / 9, e = q % 9;
-        if (b < size_t(nL)) L[q] = lu[size_t(__ldg(Lsrc + b)) * 9 + e];
-        else if (b < size_t(nL) + size_t(nU)) { const size_t bb = b - nL; U[bb * 9 + e] = lu[size_t(__ldg(Usrc + bb)) * 9 + e]; }
-        else { const size_t bb = b - nL - nU; D[bb * 9 + e] = lu[size_t(__ldg(Dsrc + bb)) * 9 + e]; }
+        if (q < nL) {
+            const size_t k = q / LREC, e = q % LREC, j = e / 9;
+            const int src = j < size_t(SLOTS) ? __ldg(LslotSrc + k * SLOTS + j) : -1;
+            L[q] = src >= 0 ? lu[size_t(src) * 9 + e % 9] : T(0);
+        } else if (q < nL + nUD) {
+            const size_t q2 = q - nL, k = q2 / UREC, e = q2 % UREC, j = e / 9;
+            const int src = j < size_t(SLOTS) ? __ldg(UslotSrc + k * SLOTS + j) : __ldg(Dsrc + k);
+            UD[q2] = src >= 0 ? lu[size_t(src) * 9 + e % 9] : T(0);
+        } else {
+            const size_t q3 = q - nL - nUD, b = q3 / 9, e = q3 % 9;
+            if (b < size_t(nLov)) {
+                const int src = __ldg(LovSrc + b);
+                Lov[q3] = src >= 0 ? lu[size_t(src) * 9 + e] : T(0);
+            } else {
+                const int src = __ldg(UovSrc + (b - nLov));
+                Uov[q3 - size_t(nLov) * 9] = src >= 0 ? lu[size_t(src) * 9 + e] : T(0);
+            }
+        }
     }
 }
 
@@ -455,24 +802,28 @@ int max_smem_optin() {
     return v;
 }
 
+template <class TF>
+IluArgs<TF> ilu_args(const DevPlan& P, const SplitFactors<TF>& S) {
+    return IluArgs<TF>{P.sysRow0, P.sysLvl0, P.lvlStart, P.Lslot, P.Uslot, P.LovCol, P.UovCol, S.L, S.UD, S.Lov, S.Uov};
+}
+
 template <class TF, class TV, int MODE>
-void launch_cta(const DevPlan& P, const TF* L, const TF* U, const TF* D, size_t smem, const double* r, double* pv, const double* v,
-                double* z, TV* yglob, const KScal* ks, cudaStream_t st) {
+void launch_cta(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, const double* r, double* pv, const double* v, double* z,
+                TV* yglob, const KScal* ks, cudaStream_t st) {
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaFuncSetAttribute(k_ilu_cta<TF, TV, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
-    k_ilu_cta<TF, TV, MODE><<<P.nsys, kCtaThreads, smem, st>>>(P.sysRow0, P.sysLvl0, P.lvlStart, P.Lptr, P.Lcol, L, P.Uptr, P.Ucol, U, D,
-                                                               r, pv, v, z, yglob, smem, ks);
+    k_ilu_cta<TF, TV, MODE><<<P.nsys, kCtaThreads, smem, st>>>(ilu_args(P, S), r, pv, v, z, yglob, smem, ks);
 }
 
 template <int MODE>
 void dispatch(const DevPlan& P, const PrecDev& M, const double* r, double* pv, const double* v, double* z, const KScal* ks,
               cudaStream_t st) {
-    if (M.kind == 0) launch_cta<double, double, MODE>(P, M.s64.L, M.s64.U, M.s64.D, M.smem, r, pv, v, z, z, ks, st);
-    else if (M.kind == 1) launch_cta<float, double, MODE>(P, M.s32.L, M.s32.U, M.s32.D, M.smem, r, pv, v, z, z, ks, st);
-    else launch_cta<float, float, MODE>(P, M.s32.L, M.s32.U, M.s32.D, M.smem, r, pv, v, z, M.y32, ks, st);
+    if (M.kind == 0) launch_cta<double, double, MODE>(P, M.s64, M.smem, r, pv, v, z, z, ks, st);
+    else if (M.kind == 1) launch_cta<float, double, MODE>(P, M.s32, M.smem, r, pv, v, z, z, ks, st);
+    else launch_cta<float, float, MODE>(P, M.s32, M.smem, r, pv, v, z, M.y32, ks, st);
 }
 
 }  // namespace
@@ -490,14 +841,16 @@ bool cta_sweep_supported(const DevPlan& P, const HostPlan& H) {
 }
 
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st) {
-    const size_t total = (size_t(P.nL) + size_t(P.nU) + size_t(P.n)) * 9;
+    const size_t total = size_t(P.n) * (LREC + UREC) + (size_t(P.nLov) + size_t(P.nUov)) * 9;
     const int grid = int(std::min<size_t>((total + 255) / 256, size_t(device_sm_count()) * 16));
-    k_pack<double><<<grid, 256, 0, st>>>(P.n, P.nL, P.nU, P.Lsrc, P.Usrc, P.Dsrc, lu, F.L, F.U, F.D);
+    k_pack<double><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, lu, F.L, F.UD, F.Lov,
+                                         F.Uov);
 }
 void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F, cudaStream_t st) {
-    const size_t total = (size_t(P.nL) + size_t(P.nU) + size_t(P.n)) * 9;
+    const size_t total = size_t(P.n) * (LREC + UREC) + (size_t(P.nLov) + size_t(P.nUov)) * 9;
     const int grid = int(std::min<size_t>((total + 255) / 256, size_t(device_sm_count()) * 16));
-    k_pack<float><<<grid, 256, 0, st>>>(P.n, P.nL, P.nU, P.Lsrc, P.Usrc, P.Dsrc, luf, F.L, F.U, F.D);
+    k_pack<float><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, luf, F.L, F.UD, F.Lov,
+                                        F.Uov);
 }
 
 void launch_ilu_cta_apply(const DevPlan& P, const PrecDev& M, const double* r, double* z, cudaStream_t st) {
@@ -510,43 +863,43 @@ void launch_ilu_cta_fused(const DevPlan& P, const PrecDev& M, bool pupdate, cons
     else dispatch<IN_SUPDATE>(P, M, r, pv, v, z, ks, st);
 }
 
-}  // namespace rsg
-
-namespace rsg {
 namespace {
+template <class TA>
+CprArgs<TA> cpr_args(const DevAmg& G, const TA* val, const TA* slotVal, const TA* diagVal, const TA* lu, TA* x, TA* b, TA* r, const TA* sp,
+                     const TA* spLov, const TA* spUov) {
+    return CprArgs<TA>{G.lv, G.maxL, G.lvl, G.ci, val, G.slotCol, slotVal, diagVal, G.rowMeta, G.agg, G.memPtr, G.mem, lu, G.luPerm,
+                       G.cin, x, b, r, G.w, G.T, sp, spLov, spUov};
+}
+
 template <class TF, class TV, class TA, int MODE>
-void launch_cpr_t(const DevPlan& P, const double* Sval, const TF* Lf, const TF* Uf, const TF* Df, size_t smem, const DevAmg& G, const TA* aval, const TA* alu,
-                  TA* ax, TA* ab, TA* ar, const double* r, double* pv, const double* v, double* z, TV* yglob, const KScal* ks,
-                  cudaStream_t st) {
+void launch_cpr_t(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, const CprArgs<TA>& C, const DevAmg& G, const double* r,
+                  double* pv, const double* v, double* z, TV* yglob, const KScal* ks, cudaStream_t st) {
+    // shared memory: the larger of the sweep vector and the V-cycle vectors of the largest system, within the cap
+    const size_t cap = size_t(max_smem_optin());
+    smem = std::max(smem, std::min(cap, size_t(G.maxSysAmgRows) * 3 * sizeof(TA)));
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaFuncSetAttribute(k_cpr_cta<TF, TV, TA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
-    AmgArgs A{G.lv, G.maxL, G.rp, G.ci, G.diag, G.lvl, G.agg, G.memPtr, G.mem, G.luPerm, G.piv};
-    k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, kCtaThreads, smem, st>>>(P.sysRow0, P.sysLvl0, P.lvlStart, P.Lptr, P.Lcol, Lf, P.Uptr, P.Ucol, Uf,
-                                                                  Df, P.rowPtr, P.col, Sval, G.w, G.T, A, aval, alu, ax, ab, ar, r,
-                                                                  pv, v, z, yglob, smem, ks);
+    k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, kCtaThreads, smem, st>>>(ilu_args(P, S), C, r, pv, v, z, yglob, smem, ks);
 }
 }  // namespace
 
 void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, bool amgFp32, const double* r, double* pv,
                     const double* v, double* z, const KScal* ks, cudaStream_t st) {
     (void)amgFp32;
-    const double* S = M.val;
     auto go = [&](auto tag_mode) {
         constexpr int MODE = decltype(tag_mode)::value;
-        if (M.kind == 0)
-            launch_cpr_t<double, double, double, MODE>(P, S, M.s64.L, M.s64.U, M.s64.D, M.smem, G, G.val, G.lu, G.x, G.b, G.r, r, pv, v, z, z,
-                                                      ks, st);
-        else if (M.kind == 1)
-            launch_cpr_t<float, double, float, MODE>(P, S, M.s32.L, M.s32.U, M.s32.D, M.smem, G, G.valf, G.luf, G.xf, G.bf, G.rf, r, pv, v, z,
-                                                    z, ks, st);
-        else
-            launch_cpr_t<float, float, float, MODE>(P, S, M.s32.L, M.s32.U, M.s32.D, M.smem, G, G.valf, G.luf, G.xf, G.bf, G.rf, r, pv, v, z,
-                                                   M.y32, ks, st);
+        if (M.kind == 0) {
+            const CprArgs<double> C = cpr_args<double>(G, G.val, G.slotVal, G.diagVal, G.lu, G.x, G.b, G.r, G.sp, G.spLov, G.spUov);
+            launch_cpr_t<double, double, double, MODE>(P, M.s64, M.smem, C, G, r, pv, v, z, z, ks, st);
+        } else {
+            const CprArgs<float> C = cpr_args<float>(G, G.valf, G.slotValf, G.diagValf, G.luf, G.xf, G.bf, G.rf, G.spf, G.spLovf, G.spUovf);
+            if (M.kind == 1) launch_cpr_t<float, double, float, MODE>(P, M.s32, M.smem, C, G, r, pv, v, z, z, ks, st);
+            else launch_cpr_t<float, float, float, MODE>(P, M.s32, M.smem, C, G, r, pv, v, z, M.y32, ks, st);
+        }
     };
-    (void)S;
     if (mode == IN_PUPDATE) go(std::integral_constant<int, IN_PUPDATE>());
     else if (mode == IN_SUPDATE) go(std::integral_constant<int, IN_SUPDATE>());
     else go(std::integral_constant<int, IN_PLAIN>());

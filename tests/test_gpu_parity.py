@@ -263,3 +263,33 @@ def test_cpr_batched_ensemble(precision):
         N = s.A.n * 3
         assert true_res(s.A, x[off:off + N], s.b) <= 1e-5
         off += N
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
+def test_cpr_large_systems(precision, oracle):
+    """Systems too large to keep every V-cycle / sweep vector on chip (b and r of the V-cycle and the FP64 sweep
+    vector in global memory): the CPR application against the oracle, and batched solves to the true residual."""
+    from ressim_gb300 import synth
+    systems = synth.ensemble(n_real=3, nx=60, ny=60, nz=8, sigma=1.5)
+    assert max(s.A.n for s in systems) > 16000
+    A0 = systems[0].A
+    r = np.random.default_rng(5).standard_normal(A0.n * 3)
+    with dev(precond="cpr", precision=precision) as d:
+        d.set_matrix(A0)
+        d.setup()
+        z = d.precond_apply(r)
+    zo = oracle.prec_apply(A0, r, prec=1)
+    # FP64: the reference arithmetic up to the coarsest back substitution's order; FP32 V-cycle / sweeps: float
+    assert rel(z, zo) < (1e-10 if precision == "fp64" else 1e-3)
+    with dev(precond="cpr", precision=precision, check_every=4) as d:
+        d.set_batch([s.A for s in systems])
+        d.setup()
+        x, res = d.solve(np.concatenate([s.b for s in systems]), tol=1e-6, maxit=300)
+        its, rr, tr = d.batch_results()
+    assert res.converged
+    assert np.all(tr <= 1e-5)
+    off = 0
+    for s in systems:
+        N = s.A.n * 3
+        assert true_res(s.A, x[off:off + N], s.b) <= 1e-5
+        off += N
