@@ -116,6 +116,13 @@ struct rsg_solver {
     // graph of `check_every` iterations
     cudaGraphExec_t gexec = nullptr;
     int gIters = 0, gKind = -1;
+    // GMRES (allocated at the first GMRES solve of a plan): state, graphs of its phases
+    // ([0] cycle start, [1 + j] inner step j, [m + 1] cycle end), BiCGSTAB result kept for the fallback
+    GmState gm{};
+    std::vector<cudaGraphExec_t> gmExec;
+    int gmKind = -1;
+    double* xPrev = nullptr;
+    KScal* ksPrev = nullptr;
     // results
     rsg_stats st{};
     long long launches = 0;
@@ -126,8 +133,13 @@ struct rsg_solver {
 
 namespace {
 
+void drop_gm_graphs(rsg_solver* h);
+
 void free_plan(rsg_solver* h) {
     if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+    drop_gm_graphs(h);
+    h->gmExec.clear();
+    h->gm = GmState{}; h->gmKind = -1; h->xPrev = nullptr; h->ksPrev = nullptr;
     h->pmem.release_all();
     h->dp = DevPlan{};
     h->val = nullptr; h->lu = nullptr; h->luf = nullptr; h->work = nullptr; h->dinv = nullptr;
@@ -584,15 +596,12 @@ int launch_iterations(rsg_solver* h, int k) {
     return RSG_OK;
 }
 
-// d_b, d_x: caller's vectors in the original row order; the solve runs in level space (h->b, h->V.x)
-int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
-    if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
-    if (h->opt.krylov != RSG_KRYLOV_BICGSTAB) return fail(RSG_EINVAL, "GMRES is not available in this build");
-    if (!(tol > 0) || maxIt < 0) return fail(RSG_EINVAL, "tol must be > 0 and maxIt >= 0");
-    RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
-    launch_gather_vec(h->dp, d_b, h->b, h->stream);
+int precond_launches(const PrecDev& M) { return M.cpr || M.cta || M.kind == 2 ? 1 : 2; }
+
+// BiCGSTAB of every system from the gathered right-hand side h->b into h->V.x
+int run_bicgstab(rsg_solver* h, double tol, int maxIt) {
     launch_bicg_init(h->dp, h->b, h->V, h->ks, h->R, tol, maxIt, h->d_active, h->stream);
-    h->launches += 4;   // gather, init, scatter, true residual
+    h->launches += 1;
     RSG_CUDA(cudaGetLastError());
     const int chunk = h->opt.check_every > 0 ? h->opt.check_every : 4;
     int launched = 0, rc;
@@ -602,6 +611,125 @@ int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, i
         if (h->h_pin[0] <= 0 || launched >= maxIt) break;
         if ((rc = launch_iterations(h, chunk))) return rc;
         launched += chunk;
+    }
+    return RSG_OK;
+}
+
+int ensure_gmres(rsg_solver* h) {
+    if (h->gm.V) return RSG_OK;
+    const int m = h->opt.restart > 0 ? h->opt.restart : 40;
+    const size_t N = size_t(h->plan.n) * NB;
+    GmState& G = h->gm;
+    int rc;
+    if ((rc = dalloc(h->pmem, &G.V, N * size_t(m + 1))) || (rc = dalloc(h->pmem, &G.Z, N * size_t(m))) || (rc = dalloc(h->pmem, &G.w, N)) ||
+        (rc = dalloc(h->pmem, &G.H, gm_stride(m) * size_t(h->plan.nsys))) || (rc = dalloc(h->pmem, &G.inner, 2)))
+        return rc;
+    G.m = m;
+    h->gmExec.assign(size_t(m) + 2, nullptr);
+    return RSG_OK;
+}
+
+void drop_gm_graphs(rsg_solver* h) {
+    for (auto& g : h->gmExec)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+// the launches of one GMRES phase: replayed from a cached graph (captured at first use) or issued directly
+template <class F>
+int gm_phase(rsg_solver* h, size_t idx, F&& launches) {
+    if (!h->opt.use_graphs) {
+        launches();
+        RSG_CUDA(cudaGetLastError());
+        return RSG_OK;
+    }
+    cudaGraphExec_t& ex = h->gmExec[idx];
+    if (!ex) {
+        cudaGraph_t g = nullptr;
+        RSG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        launches();
+        RSG_CUDA(cudaStreamEndCapture(h->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { ex = nullptr; return fail(RSG_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)); }
+    }
+    RSG_CUDA(cudaGraphLaunch(ex, h->stream));
+    return RSG_OK;
+}
+
+// Restarted flexible GMRES(m) of the batch (engine/src/linsolve.cpp:218-273) from h->b into h->V.x. onlyFailed:
+// systems whose status is ST_CONV keep their solution and are not restarted (the BiCGSTAB fallback).
+int run_gmres(rsg_solver* h, double tol, int maxIt, bool onlyFailed) {
+    int rc = ensure_gmres(h);
+    if (rc) return rc;
+    const PrecDev M = prec_dev(h);
+    const int kind = M.kind * 4 + (M.cpr ? 2 : 0) + (M.cta ? 1 : 0);
+    if (kind != h->gmKind) { drop_gm_graphs(h); h->gmKind = kind; }
+    GmState& G = h->gm;
+    const int m = G.m;
+    const size_t N = size_t(h->plan.n) * NB;
+    launch_gm_init(h->dp, h->b, h->V.x, h->ks, h->R, tol, maxIt, onlyFailed, h->d_active, h->stream);
+    h->launches += 1;
+    RSG_CUDA(cudaGetLastError());
+    const int check = h->opt.check_every > 0 ? h->opt.check_every : 4;
+    for (int cycle = 0; cycle <= maxIt + 1; ++cycle) {   // every cycle adds an iteration to each system it keeps running
+        RSG_CUDA(cudaMemcpyAsync(h->h_pin, h->d_active, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        if (h->h_pin[0] <= 0) break;
+        if ((rc = gm_phase(h, 0, [&] { launch_gm_cycle_start(h->dp, h->val, h->b, h->V.x, G, h->ks, h->R, h->d_active, h->stream); })))
+            return rc;
+        h->launches += 2;
+        for (int j = 0; j < m; ++j) {
+            rc = gm_phase(h, size_t(1 + j), [&] {
+                launch_precond_gm(h->dp, M, G.V + size_t(j) * N, G.Z + size_t(j) * N, h->ks, h->S, h->d_err, h->stream);
+                launch_gm_step(h->dp, h->val, j, G, h->ks, h->R, h->d_active, h->stream);
+            });
+            if (rc) return rc;
+            h->launches += precond_launches(M) + 3 + j;
+            if ((j + 1) % check == 0 || j + 1 == m) {
+                RSG_CUDA(cudaMemcpyAsync(h->h_pin + 3, G.inner, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+                RSG_CUDA(cudaStreamSynchronize(h->stream));
+                if (h->h_pin[3] <= 0) break;
+            }
+        }
+        if ((rc = gm_phase(h, size_t(m) + 1, [&] { launch_gm_cycle_end(h->dp, h->V.x, G, h->ks, h->d_active, h->stream); }))) return rc;
+        h->launches += 3;
+    }
+    return RSG_OK;
+}
+
+// d_b, d_x: caller's vectors in the original row order; the solve runs in level space (h->b, h->V.x)
+int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
+    if (!(tol > 0) || maxIt < 0) return fail(RSG_EINVAL, "tol must be > 0 and maxIt >= 0");
+    RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
+    launch_gather_vec(h->dp, d_b, h->b, h->stream);
+    h->launches += 3;   // gather, scatter, true residual
+    RSG_CUDA(cudaGetLastError());
+    int rc;
+    if (h->opt.krylov == RSG_KRYLOV_GMRES) {
+        if ((rc = run_gmres(h, tol, maxIt, false))) return rc;
+    } else {
+        if ((rc = run_bicgstab(h, tol, maxIt))) return rc;
+        if (h->opt.gmres_fallback) {
+            // systems that did not converge are solved again with GMRES from x = 0; per system the result with the
+            // smaller recursive residual is kept (engine/src/simulator.cpp:3388-3398)
+            std::vector<KScal> k0(size_t(h->plan.nsys));
+            RSG_CUDA(cudaMemcpyAsync(k0.data(), h->ks, sizeof(KScal) * k0.size(), cudaMemcpyDeviceToHost, h->stream));
+            RSG_CUDA(cudaStreamSynchronize(h->stream));
+            bool failed = false;
+            for (const KScal& k : k0) failed |= k.status != ST_CONV;
+            if (failed) {
+                const size_t N = size_t(h->plan.n) * NB;
+                if (!h->xPrev && ((rc = dalloc(h->pmem, &h->xPrev, N)) || (rc = dalloc(h->pmem, &h->ksPrev, size_t(h->plan.nsys)))))
+                    return rc;
+                RSG_CUDA(cudaMemcpyAsync(h->xPrev, h->V.x, N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+                RSG_CUDA(cudaMemcpyAsync(h->ksPrev, h->ks, sizeof(KScal) * size_t(h->plan.nsys), cudaMemcpyDeviceToDevice, h->stream));
+                if ((rc = run_gmres(h, tol, maxIt, true))) return rc;
+                launch_gm_pick(h->dp, h->V.x, h->xPrev, h->ksPrev, h->ks, h->stream);
+                h->launches += 2;
+                RSG_CUDA(cudaGetLastError());
+            }
+        }
     }
     launch_scatter_vec(h->dp, h->V.x, d_x, h->stream);
     RSG_CUDA(cudaEventRecord(h->ev1, h->stream));

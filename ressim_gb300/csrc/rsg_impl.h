@@ -19,7 +19,7 @@ constexpr int UREC = 36;              // per row record of U and D: SLOTS blocks
 constexpr int SPREC = 24;             // CPR pressure columns of S per row: (SLOTS + 1 + SLOTS) blocks x 3 + 3 pad
 
 // Krylov status per system (device int)
-enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3 };
+enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3, ST_CYCLE = 4 /* GMRES: restart cycle ended */ };
 
 // Error bits written by kernels (device int, OR-ed)
 enum : int { ERR_TIMEOUT = 1, ERR_NONFINITE = 2 };
@@ -32,6 +32,8 @@ struct KScal {
     double sn;                        // ||s|| of the current iteration
     int status, its, maxit, pad;
     double tol;
+    double hn;                        // GMRES: norm of the last orthogonalised vector
+    int gj, gend;                     // GMRES: inner steps of the current cycle; cycle ended by convergence
 };
 
 // Host-built, pattern-only plan of the device solve. Everything on the device runs in "level space": inside
@@ -249,8 +251,9 @@ struct PrecDev {
 // gather the factors (original block layout) into the level-ordered split layout
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st);
 void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F, cudaStream_t st);
-// z = M^-1 r with the CTA sweeps (plain input mode)
+// z = M^-1 r with the CTA sweeps (plain input mode); the _ks form skips systems whose status is not running
 void launch_ilu_cta_apply(const DevPlan& P, const PrecDev& M, const double* r, double* z, cudaStream_t st);
+void launch_ilu_cta_apply_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, cudaStream_t st);
 // BiCGSTAB-fused CTA sweeps: input p = r + beta (p - omega v) (pupdate) or s = r - alpha v, stored to pv
 void launch_ilu_cta_fused(const DevPlan& P, const PrecDev& M, bool pupdate, const double* r, double* pv, const double* v, double* z,
                           const KScal* ks, cudaStream_t st);
@@ -259,6 +262,36 @@ size_t cta_sweep_smem(const DevPlan& P, bool fp32);
 bool cta_sweep_supported(const DevPlan& P, const HostPlan& H);
 void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M, BicgVecs& V, KScal* ks, ReduceState& R,
                            SweepState& S, int* active, int* err, cudaStream_t st);
+// ---- restarted flexible GMRES(m) of the batch (engine/src/linsolve.cpp:218-273), all systems in lockstep; per-system
+// Hessenberg / Givens / y state on the device (GmState). Vectors: V (m+1 basis vectors), Z (m preconditioned), w.
+struct GmState {
+    int m = 0;
+    double *V = nullptr, *Z = nullptr, *w = nullptr;
+    double* H = nullptr;              // nsys x gm_stride(m): H (m+1) x m, cs m, sn m, g m+1, y m
+    int* inner = nullptr;             // systems still in the inner loop of the current cycle
+};
+#ifdef __CUDACC__
+#define RSG_HD __host__ __device__
+#else
+#define RSG_HD
+#endif
+inline RSG_HD size_t gm_stride(int m) { return size_t(m + 1) * m + 3 * size_t(m) + size_t(m + 1); }
+// x = 0 for the systems (re)started (all, or only those whose status is not ST_CONV when onlyFailed), ||b||
+void launch_gm_init(const DevPlan& P, const double* b, double* x, KScal* ks, ReduceState& R, double tol, int maxit, bool onlyFailed,
+                    int* active, cudaStream_t st);
+// cycle start: r = b - A x into V_0, beta, convergence / iteration-limit tests, V_0 = r / beta, g = beta e_1
+void launch_gm_cycle_start(const DevPlan& P, const double* val, const double* b, const double* x, GmState& G, KScal* ks, ReduceState& R,
+                           int* active, cudaStream_t st);
+// inner step j after the preconditioner wrote Z_j: w = A Z_j, MGS against V_0..V_j, Givens, V_{j+1} = w / h
+void launch_gm_step(const DevPlan& P, const double* val, int j, GmState& G, KScal* ks, ReduceState& R, int* active, cudaStream_t st);
+// cycle end: y = H^-1 g, x += Z y; converged / iteration limit / restart
+void launch_gm_cycle_end(const DevPlan& P, double* x, GmState& G, KScal* ks, int* active, cudaStream_t st);
+// fallback bookkeeping: keep, per retried system, the solution with the smaller recursive residual
+void launch_gm_pick(const DevPlan& P, double* x, const double* xPrev, const KScal* ksPrev, KScal* ks, cudaStream_t st);
+// preconditioner input / output copy of the systems still in the inner loop (plain input mode, status-gated)
+void launch_precond_gm(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
+                       cudaStream_t st);
+
 // true residual ||b - A x|| / ||b|| per system (FP64)
 void launch_true_residual(const DevPlan& P, const double* val, const double* b, const double* x, double* tmp, ReduceState& R,
                           double* out, cudaStream_t st);

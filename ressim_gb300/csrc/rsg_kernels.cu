@@ -12,6 +12,7 @@
 //   (deterministic), and the BiCGSTAB scalar recurrences are evaluated on the device.
 #include "rsg_impl.h"
 #include "rsg_block3.cuh"
+#include "rsg_reduce.cuh"
 
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -22,7 +23,6 @@ namespace {
 
 constexpr unsigned kSpinLimit = 1u << 22;   // x up to 256 ns back-off: about one second per wait
 constexpr int kSweepThreads = 128;
-constexpr int kTileThreads = 192;           // 64 block rows x 3 per step
 
 // ------------------------------------------------------------------ memory-order helpers
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -384,80 +384,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __r
     }
 }
 
-// ------------------------------------------------------------------ tile kernels with fused reductions
-// Block reduction of up to MAX_DOTS values; result valid in thread 0.
-template <int ND>
-__device__ __forceinline__ void block_reduce(double (&v)[MAX_DOTS], double* sh /* [ND][kTileThreads/32] */) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int j = 0; j < ND; ++j) {
-        double x = v[j];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[j * 32 + w] = x;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int j = 0; j < ND; ++j) {
-            double s = 0;
-            for (int q = 0; q < nw; ++q) s += sh[j * 32 + q];
-            v[j] = s;
-        }
-    }
-}
-
-// Last-tile-done: the block that completes the last tile reduces the per-tile partials of every system in a fixed
-// order into sysdot[s*MAX_DOTS + j] and returns true (in every thread of that block).
-template <int ND>
-__device__ bool last_tile_reduce(int ntiles, int nsys, const int* __restrict__ sysTile0, const double* part, unsigned* done,
-                                 double* sysdot, double* sh) {
-    __shared__ int amLast;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned ticket = atomicAdd(done, 1u);
-        amLast = (ticket == unsigned(ntiles) - 1u);
-    }
-    __syncthreads();
-    if (!amLast) return false;
-    __threadfence();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (nsys <= 4) {
-        for (int s = 0; s < nsys; ++s) {
-            double v[MAX_DOTS] = {0, 0, 0, 0};
-            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
-            for (int t = t0 + int(threadIdx.x); t < t1; t += blockDim.x)
-#pragma unroll
-                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
-            block_reduce<ND>(v, sh);
-            if (threadIdx.x == 0)
-#pragma unroll
-                for (int j = 0; j < ND; ++j) sysdot[size_t(s) * MAX_DOTS + j] = v[j];
-            __syncthreads();
-        }
-    } else {
-        for (int s = w; s < nsys; s += nw) {
-            double v[MAX_DOTS] = {0, 0, 0, 0};
-            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
-            for (int t = t0 + lane; t < t1; t += 32)
-#pragma unroll
-                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
-#pragma unroll
-            for (int j = 0; j < ND; ++j) {
-                double x = v[j];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                if (lane == 0) sysdot[size_t(s) * MAX_DOTS + j] = x;
-            }
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *done = 0u;
-    __threadfence();
-    return true;
-}
-
+// ------------------------------------------------------------------ tile kernels with fused reductions (rsg_reduce.cuh)
 // SpMV epilogues / fused dot products
 enum { SP_PLAIN = 0, SP_RV = 1, SP_OMEGA = 2, SP_TRUERES = 3 };
 

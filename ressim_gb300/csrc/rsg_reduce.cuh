@@ -1,0 +1,88 @@
+// Deterministic tile reductions shared by the device translation units (internal linkage in each): a tile of
+// TILE_ROWS block rows of one system writes its partial sums, and the block that completes the last tile reduces
+// every system's partials in a fixed order.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rsg_impl.h"
+
+namespace rsg {
+namespace {
+
+constexpr int kTileThreads = 192;           // 64 block rows x 3 per step
+
+// Block reduction of up to MAX_DOTS values; result valid in thread 0.
+template <int ND>
+__device__ __forceinline__ void block_reduce(double (&v)[MAX_DOTS], double* sh /* [ND][kTileThreads/32] */) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+        double x = v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[j * 32 + w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int j = 0; j < ND; ++j) {
+            double s = 0;
+            for (int q = 0; q < nw; ++q) s += sh[j * 32 + q];
+            v[j] = s;
+        }
+    }
+}
+
+// Last-tile-done: the block that completes the last tile reduces the per-tile partials of every system in a fixed
+// order into sysdot[s*MAX_DOTS + j] and returns true (in every thread of that block).
+template <int ND>
+__device__ bool last_tile_reduce(int ntiles, int nsys, const int* __restrict__ sysTile0, const double* part, unsigned* done,
+                                 double* sysdot, double* sh) {
+    __shared__ int amLast;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned ticket = atomicAdd(done, 1u);
+        amLast = (ticket == unsigned(ntiles) - 1u);
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (nsys <= 4) {
+        for (int s = 0; s < nsys; ++s) {
+            double v[MAX_DOTS] = {0, 0, 0, 0};
+            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
+            for (int t = t0 + int(threadIdx.x); t < t1; t += blockDim.x)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
+            block_reduce<ND>(v, sh);
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) sysdot[size_t(s) * MAX_DOTS + j] = v[j];
+            __syncthreads();
+        }
+    } else {
+        for (int s = w; s < nsys; s += nw) {
+            double v[MAX_DOTS] = {0, 0, 0, 0};
+            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
+            for (int t = t0 + lane; t < t1; t += 32)
+#pragma unroll
+                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+                double x = v[j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                if (lane == 0) sysdot[size_t(s) * MAX_DOTS + j] = x;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *done = 0u;
+    __threadfence();
+    return true;
+}
+
+}  // namespace
+}  // namespace rsg

@@ -856,6 +856,9 @@ void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F,
 void launch_ilu_cta_apply(const DevPlan& P, const PrecDev& M, const double* r, double* z, cudaStream_t st) {
     dispatch<IN_PLAIN>(P, M, r, nullptr, nullptr, z, nullptr, st);
 }
+void launch_ilu_cta_apply_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, cudaStream_t st) {
+    dispatch<IN_PLAIN>(P, M, r, nullptr, nullptr, z, ks, st);
+}
 
 void launch_ilu_cta_fused(const DevPlan& P, const PrecDev& M, bool pupdate, const double* r, double* pv, const double* v, double* z,
                           const KScal* ks, cudaStream_t st) {

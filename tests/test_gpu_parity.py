@@ -293,3 +293,105 @@ def test_cpr_large_systems(precision, oracle):
         N = s.A.n * 3
         assert true_res(s.A, x[off:off + N], s.b) <= 1e-5
         off += N
+
+
+# ---------------------------------------------------------------- GMRES (flexible, restarted; linsolve.cpp:218-273)
+@pytest.mark.parametrize("name", GOLDEN_SYSTEMS + ["singular_pivots.npz"])
+def test_gmres_bilu0_matches_reference(name):
+    A, z = load_golden(name)
+    if not bool(z["conv_gmres_bilu0"]):
+        pytest.skip("the reference does not converge on this case")
+    with dev(krylov="gmres", restart=30, check_every=5) as d:
+        d.set_matrix(A)
+        d.setup()
+        x, res = d.solve(z["b"], tol=1e-6, maxit=300)
+    assert res.converged
+    assert abs(res.iterations - int(z["its_gmres_bilu0"])) <= 1
+    assert rel(x, z["x_gmres_bilu0"]) < 1e-6
+    assert true_res(A, x, z["b"]) <= 1e-5
+
+
+@pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
+def test_gmres_cpr_matches_reference(name):
+    A, z = load_golden(name)
+    with dev(krylov="gmres", precond="cpr", restart=30) as d:
+        d.set_matrix(A)
+        d.setup()
+        x, res = d.solve(z["b"], tol=1e-6, maxit=300)
+    assert res.converged
+    assert abs(res.iterations - int(z["its_gmres_cpr"])) <= 1
+    assert rel(x, z["x_gmres_cpr"]) < 1e-6
+    assert true_res(A, x, z["b"]) <= 1e-5
+
+
+def test_gmres_restarts_and_batch(oracle):
+    """Short restart cycles (several restarts) on a batch: every system equals its own solve and the oracle's."""
+    mats, bs = [], []
+    for name in ["waterflood_sys0.npz", "synth_small.npz", "waterflood_sys2.npz"]:
+        A, z = load_golden(name)
+        mats.append(A)
+        bs.append(z["b"])
+    singles = []
+    for A, b in zip(mats, bs):
+        with dev(krylov="gmres", restart=10, check_every=2) as d:
+            d.set_matrix(A)
+            d.setup()
+            x, res = d.solve(b, tol=1e-8, maxit=400)
+            singles.append((x, res.iterations))
+        xo, conv, its, rr, _, _ = oracle.solve(A, b, prec=0, method=1, restart=10, tol=1e-8, maxit=400)
+        assert res.converged and conv                     # 91 / 265 / 264 iterations, 9 to 27 restarts
+        assert abs(res.iterations - its) <= max(2, its // 30)
+        assert rel(x, xo) < 1e-5
+        assert true_res(A, x, b) <= 1e-7
+    with dev(krylov="gmres", restart=10, check_every=2) as d:
+        d.set_batch(mats)
+        d.setup()
+        xb, res = d.solve(np.concatenate(bs), tol=1e-8, maxit=400)
+        its, rr, tr = d.batch_results()
+    off = 0
+    for k, A in enumerate(mats):
+        N = A.n * A.nb
+        assert its[k] == singles[k][1]
+        assert rel(xb[off:off + N], singles[k][0]) < 1e-12
+        off += N
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_f32"])
+def test_gmres_mixed_and_graphs(precision):
+    A, z = load_golden("waterflood_sys1.npz")
+    out = []
+    for graphs in (True, False):
+        with dev(krylov="gmres", precision=precision, use_graphs=graphs) as d:
+            d.set_matrix(A)
+            d.setup()
+            x, res = d.solve(z["b"], tol=1e-8, maxit=300)
+        assert res.converged and true_res(A, x, z["b"]) <= 1e-7
+        out.append((x, res.iterations))
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
+def test_gmres_fallback_keeps_the_better_result():
+    """BiCGSTAB capped below convergence, GMRES retried on the failed systems: per system the result with the
+    smaller recursive residual is kept and both solves' iterations count (engine/src/simulator.cpp:3388-3398)."""
+    from ressim_gb300 import _lib
+    A, z = load_golden("waterflood_sys0.npz")
+    b = z["b"]
+    maxit = 8
+
+    def run(**kw):
+        with dev(check_every=1, **kw) as d:
+            d.set_matrix(A)
+            d.setup()
+            x, res = d.solve(b, tol=1e-10, maxit=maxit)      # not converged: the iterate comes back (RSG_ENOTCONV)
+            assert res.status == _lib.RSG_ENOTCONV
+            its, rr, tr = d.batch_results()
+        return x, int(its[0]), float(rr[0])
+
+    x1, i1, r1 = run()
+    x2, i2, r2 = run(krylov="gmres", restart=30)
+    x3, i3, r3 = run(gmres_fallback=True, restart=30)
+    assert i3 == i1 + i2
+    if r2 < r1:
+        assert r3 == r2 and np.array_equal(x3, x2)
+    else:
+        assert r3 == r1 and np.array_equal(x3, x1)
