@@ -82,6 +82,10 @@ const char* rsg_version(void);
 int rsg_create(rsg_solver** h, const rsg_options* opts);
 int rsg_destroy(rsg_solver* h);
 
+/* Free the handle's pattern-dependent device state (plan, factors, hierarchy, Krylov vectors); the handle stays
+ * usable and the next rsg_set_matrix plans again. No reference counterpart (device memory management). */
+int rsg_release(rsg_solver* h);
+
 /* Upload (or refresh) one system matrix from host memory. The pattern-dependent plan (level schedule,
  * elimination lists, AMG aggregates) is rebuilt only when the pattern changes; a values-only refresh
  * reuses it (the engine's pattern reuse, engine/src/bsr.cpp:759-769 and AMG::refresh, amg.cpp:257-271).
@@ -162,6 +166,45 @@ int rsg_wellschur_reduce(int nrows, const int* rowPtr, const int* col, const dou
 /* x = [xc ; Dww^-1 (b_w - Awc xc)]. Replaces WellSchur::recover (engine/src/bsr.cpp:982-990). */
 int rsg_wellschur_recover(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
                           const double* b, const double* xc, double* x);
+
+/* ---- Serving form: continuous batching of independent Newton systems (the "batched/serving variants
+ * rsg_submit / rsg_poll" of the reference's block-solver boundary; no reference implementation exists).
+ * A server runs `slots` workers, each with its own solver handle and CUDA stream. Requests are admitted in
+ * arrival order as soon as a slot is free and their estimated device bytes fit the memory budget, so work that
+ * arrives while others are on the GPU overlaps with them on the device. Matrices, factors and Krylov state stay
+ * resident in HBM for the life of a request and are freed when it completes. Every request is solved exactly as
+ * it would be alone (its own plan, deterministic kernels): the result does not depend on the mix. */
+typedef struct rsg_server rsg_server;
+
+typedef struct rsg_result {
+    int status;               /* RSG_OK, RSG_ENOTCONV or a negative error of the request */
+    int iterations;
+    double rel_residual;      /* recursive (Krylov) relative residual */
+    double true_rel_residual; /* ||b - A x|| / ||b|| in FP64 */
+    double queue_ms;          /* submit -> admitted */
+    double run_ms;            /* admitted -> done (upload, set-up, solve, download) */
+    double total_ms;          /* submit -> done */
+    size_t device_bytes;      /* device memory the request held */
+    int slot;                 /* worker that ran it */
+    int precond;              /* preconditioner used (RSG_PREC_*; CPR requests too large for one SM run BILU0) */
+} rsg_result;
+
+/* opts: solver options of every slot (device, precision, preconditioner, Krylov method); slots >= 1;
+ * mem_budget: bytes of device memory the admitted requests may hold together (0 = no limit). */
+int rsg_server_create(rsg_server** s, const rsg_options* opts, int slots, size_t mem_budget);
+/* Waits for the requests in flight, drops the queued ones, frees everything. */
+int rsg_server_destroy(rsg_server* s);
+/* Copies one system (n block rows, BSR with nb x nb blocks) and its right-hand side into the queue and returns
+ * the request id (>= 0), or RSG_ENOMEM when its estimated footprint exceeds the whole budget. */
+long long rsg_submit(rsg_server* s, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b,
+                     double tol, int maxIt);
+/* 1: request finished (x: n*nb doubles, res filled; the request is retired), 0: still queued or running (wait = 0),
+ * negative: unknown id. wait != 0 blocks until the request finishes. */
+int rsg_poll(rsg_server* s, long long id, int wait, double* x, rsg_result* res);
+/* The admission figure: estimated device bytes of one request of n block rows and nnzb blocks under opts. */
+size_t rsg_request_bytes(const rsg_options* opts, int n, long long nnzb);
+/* Requests queued / running and device bytes admitted right now. */
+int rsg_server_load(rsg_server* s, int* queued, int* running, size_t* bytes_in_use);
 
 #ifdef __cplusplus
 }

@@ -23,7 +23,8 @@ EXPORTS = [
     "rsg_default_options", "rsg_last_error", "rsg_version", "rsg_create", "rsg_destroy", "rsg_set_matrix", "rsg_set_batch",
     "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
-    "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc",
+    "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
+    "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes",
 ]
 
 
@@ -31,6 +32,12 @@ class Options(C.Structure):
     _fields_ = [("precond", C.c_int), ("krylov", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("gmres_fallback", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
                 ("mem_budget", C.c_size_t), ("sweep", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double), ("device_bytes", C.c_size_t),
+                ("slot", C.c_int), ("precond", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -84,9 +91,17 @@ def load(build_if_missing: bool = True):
     L.rsg_stream.restype = vp
     L.rsg_wellschur_reduce.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, ip, vp, vp, vp, vp]
     L.rsg_wellschur_recover.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+    L.rsg_release.argtypes = [vp]
+    L.rsg_server_create.argtypes = [C.POINTER(vp), C.POINTER(Options), C.c_int, C.c_size_t]
+    L.rsg_server_destroy.argtypes = [vp]
+    L.rsg_submit.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_double, C.c_int]
+    L.rsg_poll.argtypes = [vp, C.c_longlong, C.c_int, vp, C.POINTER(Result)]
+    L.rsg_server_load.argtypes = [vp, ip, ip, C.POINTER(C.c_size_t)]
+    L.rsg_request_bytes.argtypes = [C.POINTER(Options), C.c_int, C.c_longlong]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype if name in ("rsg_last_error", "rsg_version", "rsg_stream") else (
-            None if name == "rsg_default_options" else C.c_int)
+            None if name == "rsg_default_options" else (C.c_longlong if name == "rsg_submit" else
+                                                         (C.c_size_t if name == "rsg_request_bytes" else C.c_int)))
     _LIB = L
     return L
 

@@ -38,14 +38,17 @@ namespace {
         if (e_ != cudaSuccess) return fail(RSG_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// Device allocations of a handle, stream-ordered on the handle's stream (cudaMallocAsync / cudaFreeAsync): a
+// handle that frees its plan does not synchronise the device under the other handles' work (serving slots).
 struct DevMem {
     std::vector<std::pair<void*, size_t>> blocks;
     size_t bytes = 0, budget = 0;
+    cudaStream_t st = nullptr;
     int alloc(void** p, size_t n) {
         if (n == 0) n = 16;
         if (budget && bytes + n > budget) return fail(RSG_ENOMEM, "device memory budget exhausted");
-        cudaError_t e = cudaMalloc(p, n);
-        if (e != cudaSuccess) return fail(RSG_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        cudaError_t e = cudaMallocAsync(p, n, st);
+        if (e != cudaSuccess) return fail(RSG_ENOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
         blocks.push_back({*p, n});
         bytes += n;
         return RSG_OK;
@@ -54,14 +57,14 @@ struct DevMem {
         if (!p) return;
         for (size_t k = 0; k < blocks.size(); ++k)
             if (blocks[k].first == p) {
-                cudaFree(p);
+                cudaFreeAsync(p, st);
                 bytes -= blocks[k].second;
                 blocks.erase(blocks.begin() + long(k));
                 return;
             }
     }
     void release_all() {
-        for (auto& b : blocks) cudaFree(b.first);
+        for (auto& b : blocks) cudaFreeAsync(b.first, st);
         blocks.clear();
         bytes = 0;
     }
@@ -812,6 +815,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    h->mem.st = h->pmem.st = h->stream;
     if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaMallocHost(&h->h_pin, 4 * sizeof(int))) != cudaSuccess) return bail(e, "cudaMallocHost");
@@ -840,6 +844,14 @@ int rsg_destroy(rsg_solver* h) {
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+    return RSG_OK;
+}
+
+int rsg_release(rsg_solver* h) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    free_plan(h);
     return RSG_OK;
 }
 

@@ -1,0 +1,264 @@
+// Serving form of the solver: continuous batching of independent Newton systems over worker slots.
+//
+// Each slot is a host thread with its own solver handle (own CUDA stream, own device memory). Requests wait in
+// arrival order; the head of the queue is admitted as soon as a slot is free and its estimated device footprint
+// fits in what the admitted requests leave of the budget. Admitted requests run concurrently on their slots'
+// streams, so a request that arrives while others are on the GPU overlaps with them on the device; its matrix,
+// factors, hierarchy and Krylov state stay resident until it completes and are then freed (stream-ordered, no
+// device-wide synchronisation). A request is solved exactly as it would be alone: its own plan, deterministic
+// kernels, nothing shared with the other slots but the device.
+#include "rsg.h"
+#include "rsg_impl.h"
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace rsg {
+void set_last_error(const std::string& msg);
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    long long id = 0;
+    int n = 0, nb = 0;
+    std::vector<int> rp, ci;
+    std::vector<double> val, b, x;
+    double tol = 1e-6;
+    int maxit = 100;
+    size_t est = 0;
+    bool done = false;
+    rsg_result res{};
+    Clock::time_point tSubmit, tStart, tEnd;
+};
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+// Device bytes a request will hold (an upper estimate of what its handle allocates: values twice, factors and
+// their slot copy, plan arrays, Krylov vectors, CPR hierarchy and second-stage arrays, GMRES basis).
+size_t footprint(int n, long long nnzb, const rsg_options& o) {
+    const double N = double(n), E = double(nnzb);
+    double bytes = E * (2 * 72.0 + 100.0) + N * 700.0;           // values + staging, plan arrays, level / slot plan
+    bytes += o.precision == RSG_FP64 ? E * 72.0 + N * 512.0 : E * 108.0 + N * 256.0;   // factors (+ lean work)
+    bytes += N * 3 * 8 * 14;                                      // Krylov and staging vectors
+    if (o.precond == RSG_PREC_CPR) bytes += E * 40.0 + N * 600.0;
+    if (o.krylov == RSG_KRYLOV_GMRES || o.gmres_fallback) bytes += N * 3 * 8 * (2.0 * (o.restart > 0 ? o.restart : 40) + 3);
+    return size_t(bytes) + (size_t(16) << 20);
+}
+
+}  // namespace
+
+struct rsg_server {
+    rsg_options opt{};
+    int slots = 1;
+    size_t budget = 0;
+    std::mutex mu;
+    std::condition_variable cvWork, cvDone;
+    std::deque<std::shared_ptr<Request>> queue;
+    std::unordered_map<long long, std::shared_ptr<Request>> live;
+    size_t inUse = 0;
+    int running = 0;
+    long long nextId = 0;
+    bool stop = false;
+    std::vector<std::thread> workers;
+    std::vector<rsg_solver*> handles, bilu;   // per slot: the configured handle, a BILU0 handle for large CPR requests
+};
+
+namespace {
+
+void run_request(rsg_server* S, int slot, Request& R) {
+    rsg_solver* h = S->handles[size_t(slot)];
+    int prec = S->opt.precond;
+    if (prec == RSG_PREC_CPR && R.n > 65536) {                    // CPR runs one system per SM: larger ones take BILU0
+        if (!S->bilu[size_t(slot)]) {
+            rsg_options o = S->opt;
+            o.precond = RSG_PREC_BILU0;
+            rsg_create(&S->bilu[size_t(slot)], &o);
+        }
+        if (S->bilu[size_t(slot)]) { h = S->bilu[size_t(slot)]; prec = RSG_PREC_BILU0; }
+    }
+    R.res.precond = prec;
+    R.res.slot = slot;
+    int rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
+    if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
+    int its = 0;
+    double rr = 0;
+    if (rc == RSG_OK) {
+        R.x.assign(R.b.size(), 0.0);
+        rc = rsg_solve(h, R.b.data(), R.x.data(), R.tol, R.maxit, &its, &rr);
+    }
+    rsg_stats st{};
+    rsg_get_stats(h, &st);
+    R.res.status = rc;
+    R.res.iterations = its;
+    R.res.rel_residual = rr;
+    R.res.true_rel_residual = rc >= 0 ? st.true_rel_residual : -1.0;
+    R.res.device_bytes = st.device_bytes;
+    rsg_release(h);                                               // the request's state leaves the device
+}
+
+void worker(rsg_server* S, int slot) {
+    for (;;) {
+        std::shared_ptr<Request> R;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cvWork.wait(lk, [&] {
+                if (S->stop) return true;
+                if (S->queue.empty()) return false;
+                const size_t e = S->queue.front()->est;
+                return S->budget == 0 || S->inUse + e <= S->budget || S->running == 0;
+            });
+            if (S->stop) return;
+            R = S->queue.front();
+            S->queue.pop_front();
+            S->inUse += R->est;
+            ++S->running;
+        }
+        S->cvWork.notify_all();                                   // the next head may fit as well
+        R->tStart = Clock::now();
+        run_request(S, slot, *R);
+        R->tEnd = Clock::now();
+        R->res.queue_ms = ms_between(R->tSubmit, R->tStart);
+        R->res.run_ms = ms_between(R->tStart, R->tEnd);
+        R->res.total_ms = ms_between(R->tSubmit, R->tEnd);
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->inUse -= R->est;
+            --S->running;
+            R->done = true;
+        }
+        S->cvDone.notify_all();
+        S->cvWork.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsg_server_create(rsg_server** out, const rsg_options* opts, int slots, size_t mem_budget) {
+    using rsg::set_last_error;
+    if (!out) { set_last_error("null server pointer"); return RSG_EINVAL; }
+    *out = nullptr;
+    if (slots < 1 || slots > 256) { set_last_error("slots must be in [1, 256]"); return RSG_EINVAL; }
+    rsg_server* S = new rsg_server();
+    rsg_default_options(&S->opt);
+    if (opts) S->opt = *opts;
+    S->opt.mem_budget = 0;                                        // the server accounts for the budget
+    S->slots = slots;
+    S->budget = mem_budget;
+    S->handles.assign(size_t(slots), nullptr);
+    S->bilu.assign(size_t(slots), nullptr);
+    for (int i = 0; i < slots; ++i) {
+        const int rc = rsg_create(&S->handles[size_t(i)], &S->opt);
+        if (rc != RSG_OK) {
+            for (rsg_solver* h : S->handles) rsg_destroy(h);
+            delete S;
+            return rc;                                            // the handle's message stays in rsg_last_error
+        }
+    }
+    for (int i = 0; i < slots; ++i) S->workers.emplace_back(worker, S, i);
+    *out = S;
+    return RSG_OK;
+}
+
+int rsg_server_destroy(rsg_server* S) {
+    if (!S) return RSG_OK;
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        for (auto& R : S->queue) {                                // dropped: a waiting poll returns RSG_ESTATE
+            R->done = true;
+            R->res.status = RSG_ESTATE;
+        }
+        S->queue.clear();
+        S->cvDone.notify_all();
+        S->cvDone.wait(lk, [&] { return S->running == 0; });
+        S->stop = true;
+    }
+    S->cvWork.notify_all();
+    for (auto& t : S->workers) t.join();
+    for (rsg_solver* h : S->handles) rsg_destroy(h);
+    for (rsg_solver* h : S->bilu) rsg_destroy(h);
+    delete S;
+    return RSG_OK;
+}
+
+long long rsg_submit(rsg_server* S, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b, double tol,
+                     int maxIt) {
+    using rsg::set_last_error;
+    if (!S || !rowPtr || !col || !val || !b) { set_last_error("null argument"); return RSG_EINVAL; }
+    if (n <= 0 || nb != rsg::NB) { set_last_error("n must be > 0 and nb = 3"); return RSG_EINVAL; }
+    const long long nnzb = rowPtr[n];
+    if (nnzb <= 0) { set_last_error("empty matrix"); return RSG_EINVAL; }
+    auto R = std::make_shared<Request>();
+    R->n = n;
+    R->nb = nb;
+    R->rp.assign(rowPtr, rowPtr + n + 1);
+    R->ci.assign(col, col + nnzb);
+    R->val.assign(val, val + nnzb * nb * nb);
+    R->b.assign(b, b + size_t(n) * size_t(nb));
+    R->tol = tol;
+    R->maxit = maxIt;
+    R->est = footprint(n, nnzb, S->opt);
+    if (S->budget && R->est > S->budget) {
+        set_last_error("request needs about " + std::to_string(R->est >> 20) + " MiB, more than the whole budget");
+        return RSG_ENOMEM;
+    }
+    R->tSubmit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        R->id = S->nextId++;
+        S->live[R->id] = R;
+        S->queue.push_back(R);
+    }
+    S->cvWork.notify_all();
+    return R->id;
+}
+
+int rsg_poll(rsg_server* S, long long id, int wait, double* x, rsg_result* res) {
+    using rsg::set_last_error;
+    if (!S) { set_last_error("null server"); return RSG_EINVAL; }
+    std::shared_ptr<Request> R;
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        auto it = S->live.find(id);
+        if (it == S->live.end()) { set_last_error("unknown request id"); return RSG_EINVAL; }
+        R = it->second;
+        if (!R->done) {
+            if (!wait) return 0;
+            S->cvDone.wait(lk, [&] { return R->done; });
+        }
+        S->live.erase(id);
+    }
+    if (x && !R->x.empty()) std::copy(R->x.begin(), R->x.end(), x);
+    if (res) *res = R->res;
+    return 1;
+}
+
+size_t rsg_request_bytes(const rsg_options* opts, int n, long long nnzb) {
+    rsg_options o;
+    rsg_default_options(&o);
+    if (opts) o = *opts;
+    return footprint(n, nnzb, o);
+}
+
+int rsg_server_load(rsg_server* S, int* queued, int* running, size_t* bytes) {
+    if (!S) return RSG_EINVAL;
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (queued) *queued = int(S->queue.size());
+    if (running) *running = S->running;
+    if (bytes) *bytes = S->inUse;
+    return RSG_OK;
+}
+
+}  // extern "C"

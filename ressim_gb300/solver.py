@@ -156,6 +156,76 @@ class DeviceSolver:
         return int(self.L.rsg_stream(self.h) or 0)
 
 
+class Server:
+    """Serving form (``rsg_server_*``): continuous batching of independent systems over ``slots`` workers under a
+    device-memory budget. ``submit`` copies a system and returns its id; ``poll`` returns ``None`` while it is
+    queued or running, else ``(x, result)`` with the per-request latency split (queue / run / total ms)."""
+
+    def __init__(self, slots: int = 4, mem_budget: int = 0, precond: str = "cpr", krylov: str = "bicgstab",
+                 precision: str = "mixed_f32", restart: int = 40, check_every: int = 4, use_graphs: bool = True, device: int = 0,
+                 gmres_fallback: bool = False):
+        self.L = _lib.load()
+        o = _lib.Options()
+        self.L.rsg_default_options(C.byref(o))
+        o.precond = _lib.PREC[precond]
+        o.krylov = _lib.KRYLOV[krylov]
+        o.precision = _lib.PRECISION[precision]
+        o.restart = restart
+        o.check_every = check_every
+        o.use_graphs = 1 if use_graphs else 0
+        o.device = device
+        o.gmres_fallback = 1 if gmres_fallback else 0
+        self.opts = o
+        self.s = C.c_void_p()
+        _lib.check(self.L.rsg_server_create(C.byref(self.s), C.byref(o), slots, mem_budget))
+        self.sizes = {}
+
+    def request_bytes(self, A: BSR) -> int:
+        """The admission figure of a system under this server's options."""
+        return int(self.L.rsg_request_bytes(C.byref(self.opts), A.n, A.nnzb))
+
+    def submit(self, A: BSR, b, tol: float = 1e-6, maxit: int = 200) -> int:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        rid = int(self.L.rsg_submit(self.s, A.n, A.nb, _lib.ptr(A.rowPtr), _lib.ptr(A.col), _lib.ptr(A.val), _lib.ptr(b), tol, maxit))
+        if rid < 0:
+            raise _lib.RsgError(rid, _lib.last_error())
+        self.sizes[rid] = A.n * A.nb
+        return rid
+
+    def poll(self, rid: int, wait: bool = True):
+        x = np.zeros(self.sizes[rid])
+        r = _lib.Result()
+        rc = self.L.rsg_poll(self.s, rid, 1 if wait else 0, _lib.ptr(x), C.byref(r))
+        if rc < 0:
+            raise _lib.RsgError(rc, _lib.last_error())
+        if rc == 0:
+            return None
+        del self.sizes[rid]
+        return x, {k: getattr(r, k) for k, _ in _lib.Result._fields_}
+
+    def load(self):
+        q, rn, by = C.c_int(0), C.c_int(0), C.c_size_t(0)
+        _lib.check(self.L.rsg_server_load(self.s, C.byref(q), C.byref(rn), C.byref(by)))
+        return q.value, rn.value, by.value
+
+    def close(self):
+        if getattr(self, "s", None):
+            self.L.rsg_server_destroy(self.s)
+            self.s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class GpuBlockSolver:
     """``ressim::GpuBlockSolver`` over the device solver: every call uploads A (pattern reuse keeps the plan),
     factors and solves; ``False`` on any device failure or non-finite output (the engine then falls back)."""

@@ -44,6 +44,24 @@ def test_create_without_gpu_fails_cleanly():
     assert "CUDA" in _lib.last_error() or "device" in _lib.last_error()
 
 
+def test_server_without_gpu_fails_cleanly_and_footprint_is_monotone():
+    from conftest import gpu_available
+    from ressim_gb300 import _lib
+    L = _lib.load()
+    o = _lib.Options()
+    L.rsg_default_options(C.byref(o))
+    small, big = L.rsg_request_bytes(C.byref(o), 1000, 7000), L.rsg_request_bytes(C.byref(o), 100000, 700000)
+    assert 0 < small < big
+    o.krylov = _lib.KRYLOV["gmres"]
+    assert L.rsg_request_bytes(C.byref(o), 100000, 700000) > big          # the GMRES basis is counted
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    s = C.c_void_p()
+    assert L.rsg_server_create(C.byref(s), None, 2, 0) == _lib.RSG_ECUDA
+    assert L.rsg_server_create(C.byref(s), None, 0, 0) == _lib.RSG_EINVAL
+    assert not s.value
+
+
 @pytest.mark.parametrize("name", ["waterflood_dump.npz", "synth_small.npz"])
 def test_wellschur_host_matches_reference(name):
     from ressim_gb300.bsr import ScalarCSR
