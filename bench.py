@@ -33,9 +33,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_REAL, NX, NY, NZ, SIGMA = 64, 40, 40, 10, 1.5
+N_REAL, NX, NY, NZ, SIGMA = 64, 40, 40, 10, 1.5      # N_REAL: --systems (64 = the headline workload)
 TOL, MAXIT = 1e-6, 500
-WORKLOAD = "ensemble64_40x40x10_cpr_bicgstab"
+def workload():
+    return f"ensemble{N_REAL}_40x40x10_cpr_bicgstab"
 BATCH_PREC = dict(precond="cpr", precision="mixed_f32")     # batched mixed-precision form
 PLAIN_PREC = dict(precond="cpr", precision="fp64")          # plain FP64 GPU path
 # the reference CPU solver's preconditioner for these systems: BlockCPR (auto mode picks CPR for >= 500 cells,
@@ -51,6 +52,15 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def traffic_of(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summary of this workload (profiles/traffic.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)[kernel]["traffic_bytes_per_launch"]
+    except Exception:
+        return None
 
 
 def ensemble(rank):
@@ -158,7 +168,7 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * T / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (ressim_gb300.synth, seeded)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "systems_per_step": per_step, "solver": "CPR-BiCGSTAB FP64 (reference CPU algorithm)"},
+            "config": {"workload": workload(), "systems_per_step": per_step, "solver": "CPR-BiCGSTAB FP64 (reference CPU algorithm)"},
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"{per_step} ensemble systems per step (C restatement of the reference CPU path)"},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -173,7 +183,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="rsg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--systems", type=int, default=64, help="ensemble size (64: the headline workload; smaller: profiling)")
     args = ap.parse_args()
+    global N_REAL
+    N_REAL = args.systems
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -269,7 +282,7 @@ def main():
     dom = "cpr_apply_f32" if share_prec >= share_spmv else "bsr3_spmv_f64"
     ach = kernels[dom]["gbs"]
     roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "peak_kind": peak_kind + " burst copy", "traffic": None}
+                "peak_kind": peak_kind + " burst copy", "traffic": traffic_of(dom) if N_REAL == 64 else None}
     roofline_spmv = {"bound": "hbm", "kernel": "bsr3_spmv_f64", "achieved": kernels["bsr3_spmv_f64"]["gbs"], "peak": hbm,
                      "unit": "GB/s", "frac": kernels["bsr3_spmv_f64"]["gbs"] / hbm}
 
@@ -336,7 +349,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (ressim_gb300.synth: seeded black-oil Jacobians of the named shapes)",
-            "config": {"workload": WORKLOAD, "systems": N_REAL, "grid": f"{NX}x{NY}x{NZ}", "sigma_lnk": SIGMA,
+            "config": {"workload": workload(), "systems": N_REAL, "grid": f"{NX}x{NY}x{NZ}", "sigma_lnk": SIGMA,
                        "active_cells": [int(min(A.n for A in mats)), int(max(A.n for A in mats))], "block_rows": n_rows,
                        "nnzb": nnzb, "preconditioner": "CPR: aggregation AMG V-cycle (Gauss-Seidel) on the pressure system + BILU0",
                        "precision": "mixed: FP32 BILU0 factors/sweeps and AMG, FP64 Krylov vectors, dots, true residual; plain path FP64",
