@@ -41,8 +41,11 @@ extern "C" {
                                lean BILU0, engine/src/bsr.cpp:219-263), FP64 sweep vector and accumulation (the
                                reference's float-factor sweeps, engine/src/bsr.cpp:500-522); FP64 outer Krylov
                                vectors, inner products and true residual */
-#define RSG_MIXED_F32 2     /* as RSG_MIXED but the sweeps also run in FP32 (vector and accumulation, BILU0f,
-                               engine/src/bsr.cpp:1100-1121): less robust on ill-conditioned systems */
+#define RSG_MIXED_F32 2     /* the all-FP32 preconditioner of the precision form: BILU0 factors eliminated and stored in
+                               FP32 with the 3x3 pivot blocks inverted in FP64 (thread-block path; the grid path keeps
+                               the lean factors), FP32 sweeps (BILU0f, engine/src/bsr.cpp:1100-1121), FP32 AMG
+                               hierarchy, V-cycle, coarsest LU and second-stage input; FP64 outer Krylov vectors,
+                               inner products and true residual */
 
 typedef struct rsg_options {
     int precond;            /* RSG_PREC_* */
@@ -127,8 +130,9 @@ int rsg_precond_apply(rsg_solver* h, const double* r, double* z);
 /* Same with device vectors (no synchronisation: ordered on the handle's stream). */
 int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z);
 
-/* Copy the BILU0 factors (FP64 path: L strictly lower, U_ii^-1 on the diagonal, U upper, in the matrix's
- * own pattern and block order -- the storage of ressim::BILU0, engine/src/bsr.cpp:183-215). */
+/* Copy the BILU0 factors (L strictly lower, U_ii^-1 on the diagonal, U upper, in the matrix's own pattern and
+ * block order -- the storage of ressim::BILU0, engine/src/bsr.cpp:183-215); FP32 factors of the mixed forms are
+ * widened exactly. */
 int rsg_get_factors(rsg_solver* h, double* lu);
 
 /* Timing probes for benchmarks (no counterpart in the reference): launch the internal SpMV / the preconditioner

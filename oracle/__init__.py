@@ -60,6 +60,8 @@ class Oracle:
         L.orc_bilu0_factor.restype = C.c_int
         L.orc_bilu0_factor_lean.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f32p]
         L.orc_bilu0_factor_lean.restype = C.c_int
+        L.orc_bilu0_factor_f32.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f32p]
+        L.orc_bilu0_factor_f32.restype = C.c_int
         L.orc_bilu0_apply.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
         L.orc_bilu0_apply_fd.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f64p, _f64p]
         L.orc_bilu0_apply_ff.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f64p, _f64p]
@@ -113,6 +115,11 @@ class Oracle:
     def bilu0_factor_lean(self, A):
         luf = np.zeros(A.val.size, dtype=np.float32)
         nreg = self.L.orc_bilu0_factor_lean(A.n, A.nb, A.rowPtr, A.col, A.val, luf)
+        return luf, nreg
+
+    def bilu0_factor_f32(self, A):
+        luf = np.zeros(A.val.size, dtype=np.float32)
+        nreg = self.L.orc_bilu0_factor_f32(A.n, A.nb, A.rowPtr, A.col, A.val, luf)
         return luf, nreg
 
     def bilu0_apply(self, A, lu, r):

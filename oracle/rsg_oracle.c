@@ -68,6 +68,29 @@ static void gemmSub(const double* a, const double* b, double* c, int nb) {
         for (int j = 0; j < nb; ++j) c[i * nb + j] -= r[j];
     }
 }
+/* float versions of gemm / gemmSub (same loop order, every operation rounded to float) */
+static void gemmf(const float* a, const float* b, float* c, int nb) {
+    for (int i = 0; i < nb; ++i) {
+        float r[KMAXB];
+        for (int j = 0; j < nb; ++j) r[j] = 0;
+        for (int k = 0; k < nb; ++k) {
+            const float f = a[i * nb + k];
+            for (int j = 0; j < nb; ++j) r[j] += f * b[k * nb + j];
+        }
+        for (int j = 0; j < nb; ++j) c[i * nb + j] = r[j];
+    }
+}
+static void gemmSubf(const float* a, const float* b, float* c, int nb) {
+    for (int i = 0; i < nb; ++i) {
+        float r[KMAXB];
+        for (int j = 0; j < nb; ++j) r[j] = 0;
+        for (int k = 0; k < nb; ++k) {
+            const float f = a[i * nb + k];
+            for (int j = 0; j < nb; ++j) r[j] += f * b[k * nb + j];
+        }
+        for (int j = 0; j < nb; ++j) c[i * nb + j] -= r[j];
+    }
+}
 /* y += a x / y -= a x, row sums accumulated from zero first */
 static void gemvAdd(const double* a, const double* x, double* y, int nb) {
     for (int i = 0; i < nb; ++i) {
@@ -250,6 +273,43 @@ int orc_bilu0_factor_lean(int n, int nb, const int* rowPtr, const int* col, cons
             for (int e = 0; e < b2; ++e) F[(size_t)p * b2 + e] = (float)buf[(size_t)(p - r0) * b2 + e];
     }
     free(buf);
+    free(pos);
+    free(diag);
+    return nReg;
+}
+
+/* All-FP32 factorisation of the precision form (FP32 elimination and storage, FP64 3x3 pivot inversion rounded to
+ * float). No reference counterpart: it is the row algorithm of engine/src/bsr.cpp:183-215 with float arithmetic
+ * (the reference's BILU0f factors in FP64, bsr.cpp:1087-1096). */
+int orc_bilu0_factor_f32(int n, int nb, const int* rowPtr, const int* col, const double* val, float* F) {
+    const int b2 = nb * nb;
+    const size_t nnzb = (size_t)rowPtr[n];
+    for (size_t e = 0; e < nnzb * b2; ++e) F[e] = (float)val[e];
+    int* diag = diag_positions(n, rowPtr, col);
+    int* pos = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) pos[i] = -1;
+    float tmp[KMAXB * KMAXB];
+    double D[KMAXB * KMAXB];
+    int nReg = 0;
+    for (int i = 0; i < n; ++i) {
+        const int r0 = rowPtr[i], r1 = rowPtr[i + 1];
+        for (int p = r0; p < r1; ++p) pos[col[p]] = p;
+        for (int p = r0; p < r1; ++p) {
+            const int k = col[p];
+            if (k >= i) break;
+            gemmf(F + (size_t)p * b2, F + (size_t)diag[k] * b2, tmp, nb);
+            memcpy(F + (size_t)p * b2, tmp, sizeof(float) * b2);
+            for (int q = diag[k] + 1; q < rowPtr[k + 1]; ++q) {
+                const int j = col[q];
+                if (pos[j] >= r0 && pos[j] < r1 && col[pos[j]] == j) gemmSubf(tmp, F + (size_t)q * b2, F + (size_t)pos[j] * b2, nb);
+            }
+        }
+        for (int p = r0; p < r1; ++p) pos[col[p]] = -1;
+        float* fd = F + (size_t)diag[i] * b2;
+        for (int e = 0; e < b2; ++e) D[e] = (double)fd[e];
+        nReg += invert_pivot(D, nb);
+        for (int e = 0; e < b2; ++e) fd[e] = (float)D[e];
+    }
     free(pos);
     free(diag);
     return nReg;

@@ -34,6 +34,8 @@ void orc_bsr_spmv_f(int n, int nb, const int* rowPtr, const int* col, const floa
 int orc_bilu0_factor(int n, int nb, const int* rowPtr, const int* col, const double* val, double* lu);
 /* C45 lean factorisation: double scratch row, float storage (engine/src/bsr.cpp:219-263) */
 int orc_bilu0_factor_lean(int n, int nb, const int* rowPtr, const int* col, const double* val, float* luf);
+/* all-FP32 elimination, FP64 pivot inversion (the device's precision form; returns the regularised block count) */
+int orc_bilu0_factor_f32(int n, int nb, const int* rowPtr, const int* col, const double* val, float* luf);
 /* z = U^-1 L^-1 r, serial sweeps (engine/src/bsr.cpp:565-596) */
 void orc_bilu0_apply(int n, int nb, const int* rowPtr, const int* col, const double* lu, const double* r, double* z);
 /* float factors, double vectors and accumulation (C38/C45, engine/src/bsr.cpp:500-522) */

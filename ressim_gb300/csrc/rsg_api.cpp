@@ -554,7 +554,8 @@ int do_setup(rsg_solver* h, const double* acc) {
     } else {
         ++h->epoch;
         if (h->opt.precision == RSG_MIXED || h->opt.precision == RSG_MIXED_F32) {
-            launch_factor_lean(h->dp, h->val, h->luf, h->work, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
+            if (h->cta && h->opt.precision == RSG_MIXED_F32) launch_factor_cta_f32(h->dp, h->val, h->luf, h->d_nreg, h->stream);
+            else launch_factor_lean(h->dp, h->val, h->luf, h->work, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
             if (h->cta) { launch_pack_f32(h->dp, h->luf, h->s32, h->stream); h->launches += 1; }
         } else {
             launch_factor_f64(h->dp, h->val, h->lu, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
@@ -1007,10 +1008,17 @@ int rsg_get_factors(rsg_solver* h, double* lu) {
     if (!h || !lu) return fail(RSG_EINVAL, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
-    if (!h->haveSetup || !h->lu) return fail(RSG_ESTATE, "no FP64 BILU0 factors (setup not run, or not the FP64 BILU0 path)");
+    if (!h->haveSetup || (!h->lu && !h->luf)) return fail(RSG_ESTATE, "no BILU0 factors (setup not run, or not a BILU0 / CPR path)");
     std::vector<double> lev(size_t(h->plan.nnzb) * NB2);
-    RSG_CUDA(cudaMemcpyAsync(lev.data(), h->lu, lev.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->lu) {
+        RSG_CUDA(cudaMemcpyAsync(lev.data(), h->lu, lev.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+    } else {                                     // FP32 factors of the mixed forms, exactly widened
+        std::vector<float> f(lev.size());
+        RSG_CUDA(cudaMemcpyAsync(f.data(), h->luf, f.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        for (size_t e = 0; e < f.size(); ++e) lev[e] = double(f[e]);
+    }
     for (size_t p = 0; p < size_t(h->plan.nnzb); ++p)   // back to the caller's block order
         std::memcpy(lu + size_t(h->plan.valSrc[p]) * NB2, lev.data() + p * NB2, sizeof(double) * NB2);
     return RSG_OK;

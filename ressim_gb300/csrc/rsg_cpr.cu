@@ -98,10 +98,22 @@ __global__ void k_diag_fix(int beg, int end, const int* __restrict__ diagGlob, d
 }
 
 // dense LU with partial pivoting of every system's coarsest level in its natural numbering
-// (engine/src/amg.cpp:273-295); one thread block per system
+// (engine/src/amg.cpp:273-295); one thread block per system. T = double (reference arithmetic) or float (the FP32
+// hierarchy of the precision forms: same algorithm, float operations).
+__device__ __forceinline__ double cmul(double a, double b) { return dm(a, b); }
+__device__ __forceinline__ double csub(double a, double b) { return ds(a, b); }
+__device__ __forceinline__ double cdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float cmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float csub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float cdiv(float a, float b) { return __fdiv_rn(a, b); }
+template <class T> __device__ __forceinline__ T tiny_pivot();
+template <> __device__ __forceinline__ double tiny_pivot<double>() { return 1e-300; }
+template <> __device__ __forceinline__ float tiny_pivot<float>() { return 1.17549435e-38f; }   // smallest normal float
+
+template <class T>
 __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
                                                    const int* __restrict__ ci, const double* __restrict__ val,
-                                                   const int* __restrict__ luPerm, double* luAll, int* pivAll, int* cinAll) {
+                                                   const int* __restrict__ luPerm, T* luAll, int* pivAll, int* cinAll) {
     const int s = blockIdx.x;
     AmgSysLv L;
     bool found = false;
@@ -111,25 +123,25 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
     }
     if (!found || !L.dense) return;
     const int m = L.n;
-    double* lu = luAll + L.luOff;
+    T* lu = luAll + L.luOff;
     int* piv = pivAll + L.luRowOff;
     const int* nat = luPerm + L.luRowOff;
-    for (size_t q = threadIdx.x; q < size_t(m) * m; q += blockDim.x) lu[q] = 0.0;
+    for (size_t q = threadIdx.x; q < size_t(m) * m; q += blockDim.x) lu[q] = T(0);
     __syncthreads();
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
         const int I = __ldg(nat + k);
         for (int p = __ldg(rp + L.rpOff + k); p < __ldg(rp + L.rpOff + k + 1); ++p)
-            lu[size_t(I) * m + __ldg(nat + __ldg(ci + L.entOff + p))] = val[L.entOff + p];
+            lu[size_t(I) * m + __ldg(nat + __ldg(ci + L.entOff + p))] = T(val[L.entOff + p]);
     }
     __syncthreads();
-    __shared__ double smax[256];
+    __shared__ T smax[256];
     __shared__ int sidx[256];
     for (int k = 0; k < m; ++k) {
         // pivot: first row with the largest |a_ik|, i >= k
-        double best = -1.0;
+        T best = T(-1);
         int bi = m;
         for (int i = k + int(threadIdx.x); i < m; i += blockDim.x) {
-            const double a = fabs(lu[size_t(i) * m + k]);
+            const T a = fabs(lu[size_t(i) * m + k]);
             if (a > best || (a == best && i < bi)) { best = a; bi = i; }
         }
         smax[threadIdx.x] = best;
@@ -137,7 +149,7 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
         __syncthreads();
         for (int o = blockDim.x / 2; o > 0; o >>= 1) {
             if (int(threadIdx.x) < o) {
-                const double b2 = smax[threadIdx.x + o];
+                const T b2 = smax[threadIdx.x + o];
                 const int i2 = sidx[threadIdx.x + o];
                 if (b2 > smax[threadIdx.x] || (b2 == smax[threadIdx.x] && i2 < sidx[threadIdx.x])) { smax[threadIdx.x] = b2; sidx[threadIdx.x] = i2; }
             }
@@ -149,21 +161,21 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
         if (threadIdx.x == 0) piv[k] = pr;
         if (pr != k)
             for (int j = threadIdx.x; j < m; j += blockDim.x) {
-                const double t = lu[size_t(k) * m + j];
+                const T t = lu[size_t(k) * m + j];
                 lu[size_t(k) * m + j] = lu[size_t(pr) * m + j];
                 lu[size_t(pr) * m + j] = t;
             }
         __syncthreads();
-        if (threadIdx.x == 0 && fabs(lu[size_t(k) * m + k]) < 1e-300) lu[size_t(k) * m + k] = 1e-300;
+        if (threadIdx.x == 0 && fabs(lu[size_t(k) * m + k]) < tiny_pivot<T>()) lu[size_t(k) * m + k] = tiny_pivot<T>();
         __syncthreads();
-        const double dk = lu[size_t(k) * m + k];
-        for (int i = k + 1 + int(threadIdx.x); i < m; i += blockDim.x) lu[size_t(i) * m + k] = __ddiv_rn(lu[size_t(i) * m + k], dk);
+        const T dk = lu[size_t(k) * m + k];
+        for (int i = k + 1 + int(threadIdx.x); i < m; i += blockDim.x) lu[size_t(i) * m + k] = cdiv(lu[size_t(i) * m + k], dk);
         __syncthreads();
         const int w = m - k - 1;
         for (size_t q = threadIdx.x; q < size_t(w) * w; q += blockDim.x) {
             const int i = k + 1 + int(q / w), j = k + 1 + int(q % w);
-            const double f = lu[size_t(i) * m + k];
-            if (f != 0) lu[size_t(i) * m + j] = ds(lu[size_t(i) * m + j], dm(f, lu[size_t(k) * m + j]));
+            const T f = lu[size_t(i) * m + k];
+            if (f != T(0)) lu[size_t(i) * m + j] = csub(lu[size_t(i) * m + j], cmul(f, lu[size_t(k) * m + j]));
         }
         __syncthreads();
     }
@@ -265,9 +277,10 @@ void launch_amg_refresh(const DevAmg& G, cudaStream_t st) {
         k_diag_fix<<<grid_for(size_t(r1 - r0)), 256, 0, st>>>(r0, r1, G.diagGlob, G.val);
     }
 }
-void launch_amg_coarse_lu(const DevAmg& G, bool fp32copy, cudaStream_t st) {
-    if (G.totLu > 0) k_coarse_lu<<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin);
-    if (fp32copy && G.totLu > 0) k_round<<<grid_for(size_t(G.totLu)), 256, 0, st>>>(size_t(G.totLu), G.lu, G.luf);
+void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st) {
+    if (G.totLu <= 0) return;
+    if (fp32) k_coarse_lu<float><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.luf, G.piv, G.cin);
+    else k_coarse_lu<double><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin);
 }
 void launch_amg_round(const DevAmg& G, cudaStream_t st) {
     k_round<<<grid_for(size_t(G.totEnt)), 256, 0, st>>>(size_t(G.totEnt), G.val, G.valf);

@@ -153,7 +153,7 @@ void launch_cpr_weights(const DevPlan& P, const double* val, const double* accLe
 void launch_cpr_pressure(const DevPlan& P, const double* val, const double* w, double* ap, cudaStream_t st);
 void launch_gather_acc(const DevPlan& P, const double* accOrig, double* accLev, cudaStream_t st);
 void launch_amg_refresh(const DevAmg& G, cudaStream_t st);           // Galerkin values of levels >= 1, diagonal fix
-void launch_amg_coarse_lu(const DevAmg& G, bool fp32copy, cudaStream_t st);
+void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st);     // fp32: the LU in FP32 (luf), else FP64 (lu)
 void launch_amg_round(const DevAmg& G, cudaStream_t st);             // valf = float(val), luf = float(lu)
 void launch_amg_slots(const DevAmg& G, bool fp32, cudaStream_t st);  // V-cycle row slots from val
 // pressure columns of S in the slot order of the factors (second stage of the CPR application)
@@ -248,6 +248,8 @@ struct PrecDev {
     bool cpr = false;                 // CPR two-stage preconditioner (AMG on the pressure system + BILU0)
     const DevAmg* amg = nullptr;
 };
+// all-FP32 factorisation (FP32 elimination, FP64 pivot inversion), one thread block per system
+void launch_factor_cta_f32(const DevPlan& P, const double* val, float* luf, int* nreg, cudaStream_t st);
 // gather the factors (original block layout) into the level-ordered split layout
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st);
 void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F, cudaStream_t st);

@@ -20,6 +20,7 @@
 // reference loop order, so their results are bitwise those of the reference's serial sweeps on the same
 // factors. (float, float) is the all-FP32 BILU0f sweep (engine/src/bsr.cpp:1100-1121).
 #include "rsg_impl.h"
+#include "rsg_block3.cuh"
 
 #include <cuda_runtime.h>
 #include <type_traits>
@@ -30,10 +31,6 @@ namespace {
 
 constexpr int kCtaThreads = 256;
 constexpr int kAhead = 4;                  // levels prefetched into L2 ahead of the sweep front
-
-__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 
 // one row of a 3x3 block (factor type TF) times a 3-vector of type TV, accumulated from zero left to right
 __device__ __forceinline__ double rdot(const double* a, const double* x) { return da(da(dm(a[0], x[0]), dm(a[1], x[1])), dm(a[2], x[2])); }
@@ -762,6 +759,82 @@ __global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(IluArgs<TF> F, CprArgs<
     }
 }
 
+// ------------------------------------------------------------------ all-FP32 BILU0 factorisation
+// The precision form's factorisation: FP32 elimination and storage, the pivot block inverted in FP64
+// (invert_pivot3: the reference's pivoting and singular-block shift, engine/src/bsr.cpp:67-87, 204-212) and rounded.
+// One thread block per system walks the forward levels; a thread eliminates whole rows (row algorithm of
+// engine/src/bsr.cpp:183-215 with the plan's elimination lists, every float operation rounded on its own).
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ void gemm3f(const float* a, const float* b, float* c) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float f = a[i * 3 + k];
+            r0 = fa(r0, fm(f, b[k * 3 + 0]));
+            r1 = fa(r1, fm(f, b[k * 3 + 1]));
+            r2 = fa(r2, fm(f, b[k * 3 + 2]));
+        }
+        c[i * 3 + 0] = r0; c[i * 3 + 1] = r1; c[i * 3 + 2] = r2;
+    }
+}
+__device__ __forceinline__ void gemm3f_sub(const float* a, const float* b, float* c) {
+    float t[9];
+    gemm3f(a, b, t);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) c[e] = fs(c[e], t[e]);
+}
+
+__global__ void __launch_bounds__(kCtaThreads) k_factor_cta_f32(const int* __restrict__ sysRow0, const int* __restrict__ sysLvl0,
+                                                               const int* __restrict__ lvlStart, const int* __restrict__ rowPtr,
+                                                               const int* __restrict__ col, const int* __restrict__ diag,
+                                                               const int* __restrict__ elimPtr, const int* __restrict__ elimT,
+                                                               const int* __restrict__ elimQ, const double* __restrict__ val, float* F,
+                                                               int* nreg) {
+    const int s = blockIdx.x, tid = int(threadIdx.x), nt = int(blockDim.x);
+    const int r0 = __ldg(sysRow0 + s), r1 = __ldg(sysRow0 + s + 1);
+    const size_t e0 = size_t(__ldg(rowPtr + r0)) * 9, e1 = size_t(__ldg(rowPtr + r1)) * 9;
+    for (size_t e = e0 + size_t(tid); e < e1; e += size_t(nt)) F[e] = float(__ldg(val + e));
+    __syncthreads();
+    const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
+    int reg = 0;
+    for (int L = 0; L < nl; ++L) {
+        const int k1 = __ldg(lvlStart + l0 + L + 1);
+        for (int i = __ldg(lvlStart + l0 + L) + tid; i < k1; i += nt) {
+            const int p0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+            for (int p = p0; p < d; ++p) {
+                const int k = __ldg(col + p);
+                float a[9], u[9], Lb[9];
+#pragma unroll
+                for (int e = 0; e < 9; ++e) { a[e] = F[size_t(p) * 9 + e]; u[e] = F[size_t(__ldg(diag + k)) * 9 + e]; }
+                gemm3f(a, u, Lb);                                     // L_ik = A_ik U_kk^-1
+#pragma unroll
+                for (int e = 0; e < 9; ++e) F[size_t(p) * 9 + e] = Lb[e];
+                for (int q = __ldg(elimPtr + p); q < __ldg(elimPtr + p + 1); ++q) {
+                    const int t = __ldg(elimT + q), uq = __ldg(elimQ + q);
+                    float U[9], Cb[9];
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) { U[e] = F[size_t(uq) * 9 + e]; Cb[e] = F[size_t(t) * 9 + e]; }
+                    gemm3f_sub(Lb, U, Cb);                            // A_it -= L_ik U_kq
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) F[size_t(t) * 9 + e] = Cb[e];
+                }
+            }
+            double D[9];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) D[e] = double(F[size_t(d) * 9 + e]);
+            reg += invert_pivot3(D);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) F[size_t(d) * 9 + e] = float(D[e]);
+        }
+        __syncthreads();
+    }
+    if (reg) atomicAdd(nreg, reg);
+}
+
 // factors (level-space CSR block order) -> slot records; overflow blocks
 template <class T>
 __global__ void k_pack(int n, int nLov, int nUov, const int* __restrict__ LslotSrc, const int* __restrict__ UslotSrc,
@@ -851,6 +924,11 @@ void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F,
     const int grid = int(std::min<size_t>((total + 255) / 256, size_t(device_sm_count()) * 16));
     k_pack<float><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, luf, F.L, F.UD, F.Lov,
                                         F.Uov);
+}
+
+void launch_factor_cta_f32(const DevPlan& P, const double* val, float* luf, int* nreg, cudaStream_t st) {
+    k_factor_cta_f32<<<P.nsys, kCtaThreads, 0, st>>>(P.sysRow0, P.sysLvl0, P.lvlStart, P.rowPtr, P.col, P.diag, P.elimPtr, P.elimT,
+                                                     P.elimQ, val, luf, nreg);
 }
 
 void launch_ilu_cta_apply(const DevPlan& P, const PrecDev& M, const double* r, double* z, cudaStream_t st) {

@@ -88,10 +88,16 @@ def test_graph_and_eager_identical(graphs):
 def test_mixed_precision(name, oracle, sweep):
     A, z = load_golden(name)
     luf, _ = oracle.bilu0_factor_lean(A)
-    with dev(precision="mixed_f32", sweep=sweep) as d:     # all-FP32 sweep: float rounding of the oracle's BILU0f
+    with dev(precision="mixed_f32", sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
-        assert rel(d.precond_apply(z["b"]), oracle.bilu0_apply_ff(A, luf, z["b"])) < 1e-5
+        # thread-block path: FP32 elimination with FP64 pivot inversions, bit for bit the oracle's restatement;
+        # grid path: the lean factors. Sweeps in FP32: float rounding of the oracle's all-float sweep.
+        f32, nreg = oracle.bilu0_factor_f32(A) if sweep == "cta" else (luf, 0)
+        if sweep == "cta":
+            assert np.array_equal(d.factors(A.nnzb), f32.astype(np.float64))
+            assert d.stats().regularised_blocks == nreg
+        assert rel(d.precond_apply(z["b"]), oracle.bilu0_apply_ff(A, f32, z["b"])) < 1e-5
     with dev(precision="mixed", sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()

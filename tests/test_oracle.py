@@ -125,3 +125,17 @@ def test_reference_shim_agrees_on_fresh_inputs(oracle):
         x1, c1, i1, r1, _, _ = oracle.solve(s.A, s.b, prec=prec, method=0, tol=1e-8, maxit=300)
         x2, c2, i2, r2 = R.solve(s.A, s.b, prec=prec, method=0, tol=1e-8, maxit=300)
         assert i1 == i2 and np.array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("name", ["waterflood_sys0.npz", "singular_pivots.npz", "synth_small.npz"])
+def test_fp32_factorisation_restatement(name, oracle):
+    """All-FP32 elimination with FP64 pivot inversions: within float rounding of the reference's FP64 factors,
+    with the same regularised pivot blocks."""
+    A, z = load_golden(name)
+    f32, nreg = oracle.bilu0_factor_f32(A)
+    assert nreg == int(z["nreg"])
+    if nreg:
+        return          # a shifted singular pivot block (1e-8 relative) amplifies float rounding by its condition number
+    lu = z["lu"]
+    scale = np.abs(lu).reshape(-1, 9).max(axis=1).repeat(9)
+    assert np.max(np.abs(f32.astype(np.float64) - lu) / np.maximum(scale, 1e-300)) < 1e-4
