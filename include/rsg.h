@@ -60,6 +60,9 @@ typedef struct rsg_options {
     size_t mem_budget;      /* bytes this handle may hold on the device (0 = no limit) */
     int sweep;              /* BILU0 sweep scheduling: 0 auto, 1 one thread block per system (level barriers,
                                shared-memory vector), 2 grid-wide sync-free (per-row flags) */
+    int fma;                /* 1 (default): the SpMV accumulates with fused multiply-adds (half the FP64
+                               instructions; results within rounding of the reference); 0: the reference's separately
+                               rounded products and sums, bit for bit (engine/src/bsr.cpp:109-117) */
 } rsg_options;
 
 typedef struct rsg_stats {

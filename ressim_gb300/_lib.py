@@ -31,7 +31,7 @@ EXPORTS = [
 class Options(C.Structure):
     _fields_ = [("precond", C.c_int), ("krylov", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("gmres_fallback", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
-                ("mem_budget", C.c_size_t), ("sweep", C.c_int)]
+                ("mem_budget", C.c_size_t), ("sweep", C.c_int), ("fma", C.c_int)]
 
 
 class Result(C.Structure):

@@ -157,8 +157,8 @@ void free_plan(rsg_solver* h) {
 }
 
 template <class T>
-int upload(DevMem& M, T** d, const std::vector<T>& v, cudaStream_t st) {
-    int rc = dalloc(M, d, v.size());
+int upload(DevMem& M, T** d, const std::vector<T>& v, cudaStream_t st, size_t pad = 0) {
+    int rc = dalloc(M, d, v.size() + pad);
     if (rc) return rc;
     if (!v.empty()) RSG_CUDA(cudaMemcpyAsync(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return RSG_OK;
@@ -172,7 +172,8 @@ int alloc_plan(rsg_solver* h) {
     cudaStream_t st = h->stream;
     D.n = P.n; D.nnzb = P.nnzb; D.nsys = P.nsys; D.ntiles = int(P.tileSys.size());
     int rc;
-    if ((rc = upload(M, &D.rowPtr, P.rowPtr, st)) || (rc = upload(M, &D.col, P.col, st)) || (rc = upload(M, &D.diag, P.diag, st)) ||
+    // col and the values carry 64 bytes of padding: the staged SpMV copies whole 16-byte granules
+    if ((rc = upload(M, &D.rowPtr, P.rowPtr, st)) || (rc = upload(M, &D.col, P.col, st, 16)) || (rc = upload(M, &D.diag, P.diag, st)) ||
         (rc = upload(M, &D.ford, P.ford, st)) || (rc = upload(M, &D.bord, P.bord, st)) || (rc = upload(M, &D.elimPtr, P.elimPtr, st)) ||
         (rc = upload(M, &D.elimT, P.elimT, st)) || (rc = upload(M, &D.elimQ, P.elimQ, st)) || (rc = upload(M, &D.rowSys, P.rowSys, st)) ||
         (rc = upload(M, &D.tileRow0, P.tileRow0, st)) || (rc = upload(M, &D.tileSys, P.tileSys, st)) ||
@@ -184,13 +185,18 @@ int alloc_plan(rsg_solver* h) {
         (rc = upload(M, reinterpret_cast<int**>(&D.Uslot), P.Uslot, st)) || (rc = upload(M, &D.UslotSrc, P.UslotSrc, st)) ||
         (rc = upload(M, &D.UovCol, P.UovCol, st)) || (rc = upload(M, &D.UovSrc, P.UovSrc, st)) || (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
         return rc;
+    D.spmvStage = P.spmvStage;
+    D.spmvCol = P.spmvCol;
+    D.spmvFma = h->opt.fma != 0;
+    D.spmvErr = h->d_err;
+    prepare_spmv(D);
     D.nLov = int(P.LovCol.size());
     D.nUov = int(P.UovCol.size());
     D.maxSysRows = P.maxSysRows;
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
     if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
-    if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
+    if ((rc = dalloc(M, &h->val, E + 8)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
         (rc = dalloc(M, &h->tmp, N)))
         return rc;
     double** vecs[] = {&h->V.x, &h->V.r, &h->V.rh, &h->V.p, &h->V.v, &h->V.s, &h->V.t, &h->V.ph, &h->V.sh};
@@ -785,6 +791,7 @@ void rsg_default_options(rsg_options* o) {
     o->restart = 40;
     o->precision = RSG_FP64;
     o->gmres_fallback = 0;
+    o->fma = 1;
     o->check_every = 4;
     o->use_graphs = 1;
     o->device = 0;

@@ -16,6 +16,8 @@
 
 #include <cuda_runtime.h>
 #include <cstdio>
+#include <map>
+#include <mutex>
 
 namespace rsg {
 
@@ -388,22 +390,75 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __r
 // SpMV epilogues / fused dot products
 enum { SP_PLAIN = 0, SP_RV = 1, SP_OMEGA = 2, SP_TRUERES = 3 };
 
-// y = A x on one tile (3 threads per block row), reference order per block (engine/src/bsr.cpp:109-117).
-// SP_RV: partial <rh, y>; then alpha = rho / <rh, v>. SP_OMEGA: partials <t,t>, <t,s>, <s,s>; then omega or the
-// early exit on ||s||. SP_TRUERES: y = b - A x, partials <y,y>, <b,b>, result sqrt ratio into out[s].
+// y = A x on one tile (3 threads per block row). SP_RV: partial <rh, y>; then alpha = rho / <rh, v>. SP_OMEGA:
+// partials <t,t>, <t,s>, <s,s>; then omega or the early exit on ||s||. SP_TRUERES: y = b - A x, partials <y,y>,
+// <b,b>, result sqrt ratio into out[s].
+//
+// Arithmetic (FMA): false = the reference's order and rounding per block (engine/src/bsr.cpp:109-117: row sum of
+// the block from zero, then added; bitwise the reference), true = one fused multiply-add per term (half the FP64
+// instructions; the FP64 unit, not HBM, bounds the unfused form on this part).
+// Staging (BULK): the tile is walked in chunks of 64 block rows; the chunk's value blocks and column indices are
+// contiguous and arrive in shared memory by bulk copies (cp.async.bulk, completion on an mbarrier), two chunks in
+// flight, so HBM streams at full line utilisation while the previous chunk is computed.
+struct SpmvCfg {
+    int stageBytes = 0, colBytes = 0;   // per stage: value / column bytes (16-byte multiples; 0 = no staging)
+    int* err = nullptr;
+};
+
+template <bool FMA>
+__device__ __forceinline__ double block_row_term(double yv, const double* a, const double* xc) {
+    if (FMA) return fma(a[2], __ldg(xc + 2), fma(a[1], __ldg(xc + 1), fma(a[0], __ldg(xc), yv)));
+    return da(yv, da(da(dm(a[0], __ldg(xc)), dm(a[1], __ldg(xc + 1))), dm(a[2], __ldg(xc + 2))));
+}
+
 template <int MODE>
+__device__ __forceinline__ void spmv_out(size_t q, double yv, double* y, const double* __restrict__ a1, double (&acc)[MAX_DOTS]) {
+    if (MODE == SP_TRUERES) {
+        const double bq = __ldg(a1 + q);
+        const double rq = ds(bq, yv);
+        if (y) y[q] = rq;
+        acc[0] += rq * rq;
+        acc[1] += bq * bq;
+    } else {
+        y[q] = yv;
+        if (MODE == SP_RV) acc[0] += __ldg(a1 + q) * yv;
+        if (MODE == SP_OMEGA) {
+            const double sq = __ldg(a1 + q);
+            acc[0] += yv * yv;
+            acc[1] += yv * sq;
+            acc[2] += sq * sq;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+// bounded wait for a phase of an mbarrier (each try_wait suspends for a while; about a second in all)
+__device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (unsigned it = 0; it < (1u << 20); ++it)
+        if (mbar_try(bar, parity)) return true;
+    return false;
+}
+
+template <int MODE, bool BULK, bool FMA>
 __global__ void __launch_bounds__(kTileThreads) k_spmv_tile(int ntiles, int nsys, const int* __restrict__ tileRow0,
                                                            const int* __restrict__ tileSys, const int* __restrict__ sysTile0,
                                                            const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                            const double* __restrict__ val, const double* __restrict__ x, double* y,
                                                            const double* __restrict__ a1, const double* __restrict__ a2, KScal* ks,
-                                                           double* part, unsigned* done, double* sysdot, int* active, double* out) {
+                                                           double* part, unsigned* done, double* sysdot, int* active, double* out,
+                                                           SpmvCfg cfg) {
     __shared__ double sh[MAX_DOTS * 32];
     const int tile = blockIdx.x;
     const int s = __ldg(tileSys + tile);
     const bool run = (MODE == SP_PLAIN || MODE == SP_TRUERES) || ks[s].status == ST_RUNNING;
     double acc[MAX_DOTS] = {0, 0, 0, 0};
-    if (run) {
+    if (run && !BULK) {
         const int r0 = __ldg(tileRow0 + tile), r1 = __ldg(tileRow0 + tile + 1);
         const int e = threadIdx.x % 3;
         for (int row = r0 + int(threadIdx.x) / 3; row < r1; row += kTileThreads / 3) {
@@ -411,27 +466,79 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_tile(int ntiles, int nsys
             const int p1 = __ldg(rowPtr + row + 1);
             for (int p = __ldg(rowPtr + row); p < p1; ++p) {
                 const double* a = val + size_t(p) * 9 + e * 3;
-                const double* xc = x + size_t(__ldg(col + p)) * 3;
-                const double sblk = da(da(dm(__ldg(a), __ldg(xc)), dm(__ldg(a + 1), __ldg(xc + 1))), dm(__ldg(a + 2), __ldg(xc + 2)));
-                yv = da(yv, sblk);
+                const double av[3] = {__ldg(a), __ldg(a + 1), __ldg(a + 2)};
+                yv = block_row_term<FMA>(yv, av, x + size_t(__ldg(col + p)) * 3);
             }
-            const size_t q = size_t(row) * 3 + e;
-            if (MODE == SP_TRUERES) {
-                const double bq = __ldg(a1 + q);
-                const double rq = ds(bq, yv);
-                if (y) y[q] = rq;
-                acc[0] += rq * rq;
-                acc[1] += bq * bq;
-            } else {
-                y[q] = yv;
-                if (MODE == SP_RV) acc[0] += __ldg(a1 + q) * yv;
-                if (MODE == SP_OMEGA) {
-                    const double sq = __ldg(a1 + q);
-                    acc[0] += yv * yv;
-                    acc[1] += yv * sq;
-                    acc[2] += sq * sq;
+            spmv_out<MODE>(size_t(row) * 3 + e, yv, y, a1, acc);
+        }
+    }
+    if (run && BULK) {
+        extern __shared__ __align__(128) unsigned char stg[];
+        __shared__ __align__(8) unsigned long long bar[2];
+        __shared__ int timedOut;
+        __shared__ int nIss[2], nDone[2];                          // uses issued / waited per stage (thread 0)
+        constexpr int CH = kTileThreads / 3;                      // block rows per chunk: one per thread triple
+        const int r0 = __ldg(tileRow0 + tile), r1 = __ldg(tileRow0 + tile + 1);
+        const int nch = (r1 - r0 + CH - 1) / CH;
+        const int sb = cfg.stageBytes + cfg.colBytes;
+        const unsigned long long vbase = reinterpret_cast<unsigned long long>(val), cbase = reinterpret_cast<unsigned long long>(col);
+        auto issue = [&](int c) {                                  // thread 0: chunk c into stage c & 1
+            const int rs = r0 + c * CH, re = min(r1, rs + CH);
+            const unsigned long long b0 = unsigned(__ldg(rowPtr + rs)), b1 = unsigned(__ldg(rowPtr + re));
+            const unsigned long long v0 = (vbase + b0 * 72) & ~15ull, v1 = (vbase + b1 * 72 + 15) & ~15ull;
+            const unsigned long long c0 = (cbase + b0 * 4) & ~15ull, c1 = (cbase + b1 * 4 + 15) & ~15ull;
+            const unsigned b = smem_addr(&bar[c & 1]);
+            unsigned char* dst = stg + size_t(c & 1) * sb;
+            ++nIss[c & 1];
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(unsigned((v1 - v0) + (c1 - c0))) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(smem_addr(dst)), "l"(v0), "r"(unsigned(v1 - v0)), "r"(b) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(smem_addr(dst + cfg.stageBytes)), "l"(c0), "r"(unsigned(c1 - c0)), "r"(b) : "memory");
+        };
+        if (threadIdx.x == 0) {
+            timedOut = 0;
+            nIss[0] = nIss[1] = nDone[0] = nDone[1] = 0;
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[0])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[1])) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            issue(0);
+            if (nch > 1) issue(1);
+        }
+        __syncthreads();
+        const int e = threadIdx.x % 3;
+        for (int c = 0; c < nch; ++c) {
+            const bool ok = mbar_wait(smem_addr(&bar[c & 1]), unsigned((c >> 1) & 1));
+            if (!ok) timedOut = 1;
+            if (ok && threadIdx.x == 0) ++nDone[c & 1];
+            __syncthreads();
+            if (!timedOut) {
+                const int rs = r0 + c * CH, re = min(r1, rs + CH);
+                const int b0 = __ldg(rowPtr + rs);
+                const unsigned char* st = stg + size_t(c & 1) * sb;
+                const double* vs = reinterpret_cast<const double*>(st + ((vbase + unsigned(b0) * 72ull) & 15ull));
+                const int* cs = reinterpret_cast<const int*>(st + cfg.stageBytes + ((cbase + unsigned(b0) * 4ull) & 15ull));
+                const int row = rs + int(threadIdx.x) / 3;
+                if (row < re) {
+                    double yv = 0;
+                    const int p1 = __ldg(rowPtr + row + 1);
+                    for (int p = __ldg(rowPtr + row); p < p1; ++p) {
+                        const int j = p - b0;
+                        yv = block_row_term<FMA>(yv, vs + size_t(j) * 9 + e * 3, x + size_t(cs[j]) * 3);
+                    }
+                    spmv_out<MODE>(size_t(row) * 3 + e, yv, y, a1, acc);
                 }
             }
+            __syncthreads();                                      // stage c & 1 free
+            if (threadIdx.x == 0 && c + 2 < nch && !timedOut) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(c + 2);
+            }
+        }
+        if (timedOut && threadIdx.x == 0) {                       // let the copies in flight land before the block ends
+            for (int st = 0; st < 2; ++st)
+                while (nDone[st] < nIss[st] && mbar_wait(smem_addr(&bar[st]), unsigned(nDone[st] & 1))) ++nDone[st];
+            atomicOr(cfg.err, ERR_TIMEOUT);
         }
     }
     if (MODE == SP_PLAIN) return;
@@ -700,10 +807,59 @@ void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, d
                                           S.ctr, err);
 }
 
+// SpMV tile kernel with the handle's arithmetic (P.spmvFma) and, when the plan sized the stages, bulk staging
+template <int MODE, bool BULK, bool FMA>
+void spmv_go(const DevPlan& P, const double* val, const double* x, double* y, const double* a1, KScal* ks, ReduceState* R, int* active,
+             double* out, cudaStream_t st) {
+    const SpmvCfg cfg{BULK ? P.spmvStage : 0, BULK ? P.spmvCol : 0, P.spmvErr};
+    const size_t smem = BULK ? 2 * size_t(P.spmvStage + P.spmvCol) : 0;   // opt-in set by prepare_spmv
+    k_spmv_tile<MODE, BULK, FMA><<<P.ntiles, kTileThreads, smem, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr,
+                                                                      P.col, val, x, y, a1, nullptr, ks, R ? R->part : nullptr,
+                                                                      R ? R->done : nullptr, R ? R->sysdot : nullptr, active, out, cfg);
+}
+template <int MODE>
+void spmv(const DevPlan& P, const double* val, const double* x, double* y, const double* a1, KScal* ks, ReduceState* R, int* active,
+          double* out, cudaStream_t st) {
+    const bool bulk = P.spmvStage > 0;
+    if (bulk && P.spmvFma) spmv_go<MODE, true, true>(P, val, x, y, a1, ks, R, active, out, st);
+    else if (bulk) spmv_go<MODE, true, false>(P, val, x, y, a1, ks, R, active, out, st);
+    else if (P.spmvFma) spmv_go<MODE, false, true>(P, val, x, y, a1, ks, R, active, out, st);
+    else spmv_go<MODE, false, false>(P, val, x, y, a1, ks, R, active, out, st);
+}
+
+template <int MODE>
+void allow_smem(int bytes) {
+    raise_smem_limit(reinterpret_cast<const void*>(k_spmv_tile<MODE, true, true>), bytes);
+    raise_smem_limit(reinterpret_cast<const void*>(k_spmv_tile<MODE, true, false>), bytes);
+}
+
+// The dynamic shared-memory opt-in of a kernel is one process-wide value per device: handles on several threads
+// (serving slots) with plans of different sizes only ever raise it, under one lock.
+void raise_smem_limit(const void* fn, int bytes) {
+    if (bytes <= 48 * 1024) return;
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, int> lim;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    int& cur = lim[{dev, fn}];
+    if (bytes > cur) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cur = bytes;
+    }
+}
+
+void prepare_spmv(const DevPlan& P) {
+    const int smem = 2 * (P.spmvStage + P.spmvCol);
+    if (smem <= 48 * 1024) return;
+    allow_smem<SP_PLAIN>(smem);
+    allow_smem<SP_RV>(smem);
+    allow_smem<SP_OMEGA>(smem);
+    allow_smem<SP_TRUERES>(smem);
+}
+
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st) {
-    k_spmv_tile<SP_PLAIN><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col,
-                                                             val, x, y, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                                                             nullptr, nullptr);
+    spmv<SP_PLAIN>(P, val, x, y, nullptr, nullptr, nullptr, nullptr, nullptr, st);
 }
 
 void launch_block_jacobi_setup(const DevPlan& P, const double* val, double* dinv, int* nreg, cudaStream_t st) {
@@ -765,21 +921,16 @@ void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M
         }
     };
     prec(true, V.ph);
-    k_spmv_tile<SP_RV><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col, val,
-                                                          V.ph, V.v, V.rh, nullptr, ks, R.part, R.done, R.sysdot, active, nullptr);
+    spmv<SP_RV>(P, val, V.ph, V.v, V.rh, ks, &R, active, nullptr, st);
     prec(false, V.sh);
-    k_spmv_tile<SP_OMEGA><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col,
-                                                             val, V.sh, V.t, V.s, nullptr, ks, R.part, R.done, R.sysdot, active,
-                                                             nullptr);
+    spmv<SP_OMEGA>(P, val, V.sh, V.t, V.s, ks, &R, active, nullptr, st);
     k_bicg_update<<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, V.x, V.r, V.rh, V.s, V.t,
                                                      V.ph, V.sh, ks, R.part, R.done, R.sysdot, active);
 }
 
 void launch_true_residual(const DevPlan& P, const double* val, const double* b, const double* x, double* tmp, ReduceState& R,
                           double* out, cudaStream_t st) {
-    k_spmv_tile<SP_TRUERES><<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col,
-                                                               val, x, tmp, b, nullptr, nullptr, R.part, R.done, R.sysdot, nullptr,
-                                                               out);
+    spmv<SP_TRUERES>(P, val, x, tmp, b, nullptr, &R, nullptr, out, st);
 }
 
 }  // namespace rsg

@@ -883,11 +883,7 @@ IluArgs<TF> ilu_args(const DevPlan& P, const SplitFactors<TF>& S) {
 template <class TF, class TV, int MODE>
 void launch_cta(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, const double* r, double* pv, const double* v, double* z,
                 TV* yglob, const KScal* ks, cudaStream_t st) {
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_ilu_cta<TF, TV, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        configured = smem;
-    }
+    raise_smem_limit(reinterpret_cast<const void*>(k_ilu_cta<TF, TV, MODE>), int(smem));
     k_ilu_cta<TF, TV, MODE><<<P.nsys, kCtaThreads, smem, st>>>(ilu_args(P, S), r, pv, v, z, yglob, smem, ks);
 }
 
@@ -958,11 +954,7 @@ void launch_cpr_t(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, cons
     // shared memory: the larger of the sweep vector and the V-cycle vectors of the largest system, within the cap
     const size_t cap = size_t(max_smem_optin());
     smem = std::max(smem, std::min(cap, size_t(G.maxSysAmgRows) * 3 * sizeof(TA)));
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_cpr_cta<TF, TV, TA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        configured = smem;
-    }
+    raise_smem_limit(reinterpret_cast<const void*>(k_cpr_cta<TF, TV, TA, MODE>), int(smem));
     k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, kCtaThreads, smem, st>>>(ilu_args(P, S), C, r, pv, v, z, yglob, smem, ks);
 }
 }  // namespace

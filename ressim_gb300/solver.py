@@ -36,7 +36,7 @@ class DeviceSolver:
 
     def __init__(self, precond: str = "bilu0", krylov: str = "bicgstab", precision: str = "fp64", restart: int = 40,
                  check_every: int = 4, use_graphs: bool = True, device: int = 0, mem_budget: int = 0,
-                 gmres_fallback: bool = False, sweep: str = "auto"):
+                 gmres_fallback: bool = False, sweep: str = "auto", fma: bool = True):
         self.L = _lib.load()
         o = _lib.Options()
         self.L.rsg_default_options(C.byref(o))
@@ -49,6 +49,7 @@ class DeviceSolver:
         o.device = device
         o.mem_budget = mem_budget
         o.gmres_fallback = 1 if gmres_fallback else 0
+        o.fma = 1 if fma else 0
         o.sweep = _lib.SWEEP[sweep]
         self.opts = o
         h = C.c_void_p()

@@ -19,7 +19,7 @@ def test_spmv_dot_noalloc_matches_existing_entry_point():
     L = _lib.load()
     A, z = load_golden("waterflood_sys1.npz")
     x, w = z["x_seed"], z["b"]
-    with DeviceSolver() as d:                 # the existing entry point (allocates its own device memory)
+    with DeviceSolver(fma=False) as d:        # the existing entry point with the same (reference) rounding
         d.set_matrix(A)
         y_ref = d.spmv(x)
     dot_ref = float(np.dot(w, y_ref))
