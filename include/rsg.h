@@ -192,6 +192,7 @@ typedef struct rsg_result {
     double run_ms;            /* admitted -> done (upload, set-up, solve, download) */
     double total_ms;          /* submit -> done */
     size_t device_bytes;      /* device memory the request held */
+    double start_ms, end_ms;  /* admitted / done, ms since the server was created (one clock for all requests) */
     int slot;                 /* worker that ran it */
     int precond;              /* preconditioner used (RSG_PREC_*; CPR requests too large for one SM run BILU0) */
 } rsg_result;

@@ -62,6 +62,8 @@ class Oracle:
         L.orc_bilu0_factor_lean.restype = C.c_int
         L.orc_bilu0_factor_f32.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f32p]
         L.orc_bilu0_factor_f32.restype = C.c_int
+        L.orc_set_mc_smoother.argtypes = [C.c_int]
+        L.orc_set_mc_smoother.restype = None
         L.orc_bilu0_apply.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
         L.orc_bilu0_apply_fd.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f64p, _f64p]
         L.orc_bilu0_apply_ff.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f32p, _f64p, _f64p]
@@ -116,6 +118,10 @@ class Oracle:
         luf = np.zeros(A.val.size, dtype=np.float32)
         nreg = self.L.orc_bilu0_factor_lean(A.n, A.nb, A.rowPtr, A.col, A.val, luf)
         return luf, nreg
+
+    def set_mc_smoother(self, on: bool):
+        """AMG smoother: multicolour Gauss-Seidel (the device's FP32 precision forms) or the reference's (default)."""
+        self.L.orc_set_mc_smoother(1 if on else 0)
 
     def bilu0_factor_f32(self, A):
         luf = np.zeros(A.val.size, dtype=np.float32)

@@ -820,9 +820,49 @@ int orc_amg_refresh(orc_amg* h, int n, const int* rowPtr, const int* col, const 
     return 1;
 }
 
+/* Multicolour smoother of the device's FP32 precision forms (no reference counterpart): greedy colours assigned
+ * in the level's natural order, the sweep colour by colour (backward: colours in reverse); rows of a colour are
+ * independent, so the order inside a colour does not matter. Off by default (the reference's smoother). */
+static int g_mc_smoother = 0;
+void orc_set_mc_smoother(int on) { g_mc_smoother = on; }
+
+static void gauss_seidel_mc(const sp_t* A, const int* dg, const double* b, double* x, int forward) {
+    const int n = A->nr;
+    int* colr = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    char* used = (char*)xcalloc((size_t)n + 2, 1);
+    int nc = 0;
+    for (int i = 0; i < n; ++i) colr[i] = -1;
+    for (int i = 0; i < n; ++i) {
+        for (int p = A->rp[i]; p < A->rp[i + 1]; ++p)
+            if (A->ci[p] != i && colr[A->ci[p]] >= 0) used[colr[A->ci[p]]] = 1;
+        int c = 0;
+        while (used[c]) ++c;
+        colr[i] = c;
+        if (c + 1 > nc) nc = c + 1;
+        for (int p = A->rp[i]; p < A->rp[i + 1]; ++p)
+            if (A->ci[p] != i && colr[A->ci[p]] >= 0) used[colr[A->ci[p]]] = 0;
+    }
+    for (int cc = 0; cc < nc; ++cc) {
+        const int c = forward ? cc : nc - 1 - cc;
+        for (int i = 0; i < n; ++i) {
+            if (colr[i] != c) continue;
+            double s = b[i];
+            for (int p = A->rp[i]; p < A->rp[i + 1]; ++p)
+                if (A->ci[p] != i) s -= A->v[p] * x[A->ci[p]];
+            x[i] = s / A->v[dg[i]];
+        }
+    }
+    free(used);
+    free(colr);
+}
+
 /* engine/src/amg.cpp:98-113 */
 static void gauss_seidel(const sp_t* A, const int* dg, const double* b, double* x, int forward) {
     const int n = A->nr;
+    if (g_mc_smoother) {
+        gauss_seidel_mc(A, dg, b, x, forward);
+        return;
+    }
     if (forward) {
         for (int i = 0; i < n; ++i) {
             double s = b[i];

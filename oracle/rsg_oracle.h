@@ -35,6 +35,9 @@ int orc_bilu0_factor(int n, int nb, const int* rowPtr, const int* col, const dou
 /* C45 lean factorisation: double scratch row, float storage (engine/src/bsr.cpp:219-263) */
 int orc_bilu0_factor_lean(int n, int nb, const int* rowPtr, const int* col, const double* val, float* luf);
 /* all-FP32 elimination, FP64 pivot inversion (the device's precision form; returns the regularised block count) */
+/* 1: the AMG smoother is the multicolour Gauss-Seidel of the device's FP32 precision forms (test switch; 0 = the
+ * reference's natural-order smoother) */
+void orc_set_mc_smoother(int on);
 int orc_bilu0_factor_f32(int n, int nb, const int* rowPtr, const int* col, const double* val, float* luf);
 /* z = U^-1 L^-1 r, serial sweeps (engine/src/bsr.cpp:565-596) */
 void orc_bilu0_apply(int n, int nb, const int* rowPtr, const int* col, const double* lu, const double* r, double* z);

@@ -37,7 +37,7 @@ class Options(C.Structure):
 class Result(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
                 ("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double), ("device_bytes", C.c_size_t),
-                ("slot", C.c_int), ("precond", C.c_int)]
+                ("start_ms", C.c_double), ("end_ms", C.c_double), ("slot", C.c_int), ("precond", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <numeric>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -339,6 +340,42 @@ int ensure_precond_storage(rsg_solver* h) {
     return RSG_OK;
 }
 
+// Gauss-Seidel schedule of one AMG level: the reference's natural-order sweep as forward levels of its lower
+// dependencies (identity row list, engine/src/amg.cpp:98-113), or, for the FP32 precision forms, a multicolour sweep:
+// greedy colours assigned in the level's natural order, rows ordered by (colour, natural index); rows of one
+// colour are independent, so a sweep is one step per colour.
+void gs_schedule(const AmgLevel& A, bool mc, std::vector<int>& rows, std::vector<int>& start) {
+    rows.resize(size_t(A.n));
+    if (!mc) {
+        std::iota(rows.begin(), rows.end(), 0);
+        start = A.lvlStart;
+        return;
+    }
+    std::vector<int> colr(size_t(A.n), -1);
+    std::vector<char> used;
+    int nc = 0;
+    for (int I = 0; I < A.n; ++I) {
+        const int k = A.iperm[size_t(I)];
+        used.assign(size_t(nc) + 1, 0);
+        for (int p = A.rp[size_t(k)]; p < A.rp[size_t(k) + 1]; ++p) {
+            const int j = A.ci[size_t(p)];
+            if (j != k && colr[size_t(j)] >= 0) used[size_t(colr[size_t(j)])] = 1;
+        }
+        int c = 0;
+        while (used[size_t(c)]) ++c;
+        colr[size_t(k)] = c;
+        nc = std::max(nc, c + 1);
+    }
+    start.assign(size_t(nc) + 1, 0);
+    for (int k = 0; k < A.n; ++k) start[size_t(colr[size_t(k)]) + 1]++;
+    for (int c = 0; c < nc; ++c) start[size_t(c) + 1] += start[size_t(c)];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int I = 0; I < A.n; ++I) {
+        const int k = A.iperm[size_t(I)];
+        rows[size_t(fill[size_t(colr[size_t(k)])]++)] = k;
+    }
+}
+
 // Device layout of the batch's AMG hierarchies (level-major concatenation, see DevAmg) and its upload.
 int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
     DevAmg& G = h->amg;
@@ -349,6 +386,11 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
     G.nsys = nsys;
     G.maxL = maxL;
     std::vector<AmgSysLv> lv(size_t(nsys) * maxL);
+    const bool mc = h->opt.precision != RSG_FP64;
+    std::vector<std::vector<int>> schRows(size_t(nsys) * maxL), schStart(size_t(nsys) * maxL);
+    for (int s = 0; s < nsys; ++s)
+        for (int l = 0; l < int(H[size_t(s)].lv.size()); ++l)
+            gs_schedule(H[size_t(s)].lv[size_t(l)], mc, schRows[size_t(s) * maxL + l], schStart[size_t(s) * maxL + l]);
     int rows = 0, rps = 0, ents = 0, lvls = 0, mems = 0, aps = 0, lus = 0, lurows = 0, slots = 0;
     std::vector<int> sysRows(size_t(nsys), 0);
     G.levelEntBeg.assign(size_t(maxL) + 1, 0);
@@ -365,7 +407,8 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             AmgSysLv& d = lv[size_t(s) * maxL + l];
             d.n = A.n;
             d.nnz = int(A.ci.size());
-            d.nl = int(A.lvlStart.size()) - 1;
+            d.nl = int(schStart[size_t(s) * maxL + l].size()) - 1;
+            d.mc = mc ? 1 : 0;
             d.rowOff = rows; d.rpOff = rps; d.entOff = ents; d.lvlOff = lvls; d.memOff = mems;
             d.W = l == 0 ? AMG_W0 : AMG_W1;
             d.slotOff = slots;
@@ -380,7 +423,7 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             if (l + 1 == int(H[size_t(s)].lv.size())) {
                 d.coarse = 1;
                 d.dense = H[size_t(s)].coarseDense ? 1 : 0;
-                if (d.dense) { d.luOff = lus; d.luRowOff = lurows; lus += A.n * A.n; lurows += A.n; }
+                if (d.dense) { d.luOff = lus; d.luRowOff = lurows; lus += A.n * A.n; lurows += A.n; G.maxCoarse = std::max(G.maxCoarse, A.n); }
             }
         }
     }
@@ -416,7 +459,8 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         }
     std::vector<int> rp(static_cast<size_t>(rps)), ci(static_cast<size_t>(ents)), dg(static_cast<size_t>(rows)),
         lvl(static_cast<size_t>(lvls)), agg(static_cast<size_t>(rows), 0), memPtr(static_cast<size_t>(rps), 0),
-        mem(static_cast<size_t>(mems)), dgG(static_cast<size_t>(rows)), luPerm(static_cast<size_t>(std::max(lurows, 1)), 0);
+        mem(static_cast<size_t>(mems)), dgG(static_cast<size_t>(rows)), luPerm(static_cast<size_t>(std::max(lurows, 1)), 0),
+        gsRows(static_cast<size_t>(std::max(rows, 1)), 0);
     std::vector<int> apPtr(size_t(aps) + 1, 0), apSrc, acPtr(size_t(ents) + 1, 0), acSrc;
     for (int l = 0; l < maxL; ++l)
         for (int s = 0; s < nsys; ++s) {
@@ -426,7 +470,8 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             std::copy(A.rp.begin(), A.rp.end(), rp.begin() + d.rpOff);
             std::copy(A.ci.begin(), A.ci.end(), ci.begin() + d.entOff);
             std::copy(A.diag.begin(), A.diag.end(), dg.begin() + d.rowOff);
-            std::copy(A.lvlStart.begin(), A.lvlStart.end(), lvl.begin() + d.lvlOff);
+            std::copy(schStart[size_t(s) * maxL + l].begin(), schStart[size_t(s) * maxL + l].end(), lvl.begin() + d.lvlOff);
+            std::copy(schRows[size_t(s) * maxL + l].begin(), schRows[size_t(s) * maxL + l].end(), gsRows.begin() + d.rowOff);
             for (int k = 0; k < A.n; ++k) dgG[size_t(d.rowOff + k)] = d.entOff + A.diag[size_t(k)];
             if (!A.agg.empty()) std::copy(A.agg.begin(), A.agg.end(), agg.begin() + d.rowOff);
             if (l > 0) {
@@ -459,7 +504,7 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = upload(M, &G.memPtr, memPtr, st)) || (rc = upload(M, &G.mem, mem, st)) || (rc = upload(M, &G.apPtr, apPtr, st)) ||
         (rc = upload(M, &G.apSrc, apSrc, st)) || (rc = upload(M, &G.acPtr, acPtr, st)) || (rc = upload(M, &G.acSrc, acSrc, st)) ||
         (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)) ||
-        (rc = upload(M, &G.slotSrc, slotSrc, st)) || (rc = upload(M, &G.slotCol, slotCol, st)) ||
+        (rc = upload(M, &G.slotSrc, slotSrc, st)) || (rc = upload(M, &G.slotCol, slotCol, st)) || (rc = upload(M, &G.gsRows, gsRows, st)) ||
         (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)))
         return rc;
     {
@@ -474,6 +519,7 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
     RSG_CUDA(cudaMemcpyAsync(G.lv, lv.data(), lv.size() * sizeof(AmgSysLv), cudaMemcpyHostToDevice, st));
     if ((rc = dalloc(M, &G.val, size_t(ents))) || (rc = dalloc(M, &G.valf, size_t(ents))) || (rc = dalloc(M, &G.apVal, size_t(std::max(aps, 1)))) ||
         (rc = dalloc(M, &G.lu, size_t(std::max(lus, 1)))) || (rc = dalloc(M, &G.luf, size_t(std::max(lus, 1)))) ||
+        (rc = dalloc(M, &G.invf, size_t(std::max(lus, 1)))) ||
         (rc = dalloc(M, &G.piv, size_t(std::max(lurows, 1)))) || (rc = dalloc(M, &G.x, size_t(rows))) || (rc = dalloc(M, &G.b, size_t(rows))) ||
         (rc = dalloc(M, &G.r, size_t(rows))) || (rc = dalloc(M, &G.xf, size_t(rows))) || (rc = dalloc(M, &G.bf, size_t(rows))) ||
         (rc = dalloc(M, &G.rf, size_t(rows))))

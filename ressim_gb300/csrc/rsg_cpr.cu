@@ -113,7 +113,8 @@ template <> __device__ __forceinline__ float tiny_pivot<float>() { return 1.1754
 template <class T>
 __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
                                                    const int* __restrict__ ci, const double* __restrict__ val,
-                                                   const int* __restrict__ luPerm, T* luAll, int* pivAll, int* cinAll) {
+                                                   const int* __restrict__ luPerm, T* luAll, int* pivAll, int* cinAll,
+                                                   int skipUpTo) {
     const int s = blockIdx.x;
     AmgSysLv L;
     bool found = false;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
         const AmgSysLv c = lv[s * maxL + l];
         if (c.n > 0 && c.coarse) { L = c; found = true; break; }
     }
-    if (!found || !L.dense) return;
+    if (!found || !L.dense || L.n <= skipUpTo) return;        // skipUpTo: levels inverted in shared memory
     const int m = L.n;
     T* lu = luAll + L.luOff;
     int* piv = pivAll + L.luRowOff;
@@ -189,6 +190,159 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
             const int pk = piv[k];
             if (pk != k) { const int t = cin[k]; cin[k] = cin[pk]; cin[pk] = t; }
         }
+}
+
+// Explicit inverse of every coarsest level for the FP32 precision forms (the reference's device-shaped CPR keeps an
+// explicit coarse inverse, engine/src/bsr.cpp:1235-1317): column j = LU^-1 e_j of the level-space unit vector,
+// stored in natural row order: inv[j * m + nat(k)] = (A^-1)_{k j}. All m columns are eliminated together by the
+// block, column-oriented, in an m x m shared-memory work matrix (m <= kInvSmemRows), else one column per thread in
+// global memory.
+constexpr int kInvSmemRows = 224;
+__global__ void __launch_bounds__(256) k_coarse_inv(int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ cinAll,
+                                                    const float* __restrict__ luAll, float* invAll, int skipUpTo) {
+    extern __shared__ float W[];
+    const int s = blockIdx.x;
+    AmgSysLv L;
+    bool found = false;
+    for (int l = 0; l < maxL; ++l) {
+        const AmgSysLv c = lv[s * maxL + l];
+        if (c.n > 0 && c.coarse) { L = c; found = true; break; }
+    }
+    if (!found || !L.dense || L.n <= skipUpTo) return;
+    const int m = L.n;
+    const float* lu = luAll + L.luOff;
+    const int* cin = cinAll + L.luRowOff;
+    float* inv = invAll + L.luOff;
+    if (m <= kInvSmemRows && m <= int(blockDim.x)) {
+        // thread j owns column j of the work matrix W[i * m + j] (consecutive threads, consecutive banks); column k
+        // of the factors is staged in shared memory for each elimination step and read by all threads
+        float* lc = W + m * m;
+        const int j = threadIdx.x;
+        if (j < m)
+            for (int i = 0; i < m; ++i) W[i * m + j] = __ldg(cin + i) == j ? 1.f : 0.f;   // pivoted e_j
+        for (int k = 0; k + 1 < m; ++k) {                                         // unit lower
+            __syncthreads();
+            for (int i = threadIdx.x; i < m; i += blockDim.x) lc[i] = __ldg(lu + size_t(i) * m + k);
+            __syncthreads();
+            if (j < m) {
+                const float wk = W[k * m + j];
+                if (wk != 0.f)
+                    for (int i = k + 1; i < m; ++i) W[i * m + j] = __fsub_rn(W[i * m + j], __fmul_rn(lc[i], wk));
+            }
+        }
+        for (int k = m - 1; k >= 0; --k) {                                        // upper
+            __syncthreads();
+            for (int i = threadIdx.x; i < m; i += blockDim.x) lc[i] = __ldg(lu + size_t(i) * m + k);
+            __syncthreads();
+            if (j < m) {
+                const float wk = __fdiv_rn(W[k * m + j], lc[k]);
+                W[k * m + j] = wk;
+                if (wk != 0.f)
+                    for (int i = 0; i < k; ++i) W[i * m + j] = __fsub_rn(W[i * m + j], __fmul_rn(lc[i], wk));
+            }
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+            const int jj = q / m, i = q - jj * m;
+            inv[q] = W[i * m + jj];
+        }
+        return;
+    }
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        float* w = inv + size_t(j) * m;
+        for (int i = 0; i < m; ++i) w[i] = __ldg(cin + i) == j ? 1.f : 0.f;
+        for (int i = 1; i < m; ++i) {
+            float t = w[i];
+            for (int k = 0; k < i; ++k) t = __fsub_rn(t, __fmul_rn(__ldg(lu + size_t(i) * m + k), w[k]));
+            w[i] = t;
+        }
+        for (int i = m - 1; i >= 0; --i) {
+            float t = w[i];
+            for (int k = i + 1; k < m; ++k) t = __fsub_rn(t, __fmul_rn(__ldg(lu + size_t(i) * m + k), w[k]));
+            w[i] = __fdiv_rn(t, __ldg(lu + size_t(i) * m + i));
+        }
+    }
+}
+
+// FP32 forms: the coarsest inverse directly, by Gauss-Jordan elimination with partial pivoting on the dense matrix
+// in its natural numbering, in shared memory (m <= kInvSmemRows): thread j owns column j, column k of every step is
+// staged for all threads; the inverse is written as the V-cycle reads it, inv[j * m + I] = (A^-1)[I][nat(j)].
+// Larger levels take the LU (k_coarse_lu<float>) and k_coarse_inv instead.
+__global__ void __launch_bounds__(256) k_coarse_gj(int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                   const int* __restrict__ ci, const double* __restrict__ val,
+                                                   const int* __restrict__ luPerm, float* invAll) {
+    extern __shared__ float W[];
+    const int s = blockIdx.x;
+    AmgSysLv L;
+    bool found = false;
+    for (int l = 0; l < maxL; ++l) {
+        const AmgSysLv c = lv[s * maxL + l];
+        if (c.n > 0 && c.coarse) { L = c; found = true; break; }
+    }
+    if (!found || !L.dense) return;
+    const int m = L.n;
+    if (m > kInvSmemRows || m > int(blockDim.x)) return;         // left to the LU path
+    float* col = W + m * m;                                      // column k of the current step
+    __shared__ float pv[256];
+    __shared__ int pi[256];
+    __shared__ int perm[kInvSmemRows];
+    const int* nat = luPerm + L.luRowOff;
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) W[q] = 0.f;
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const int I = __ldg(nat + k);
+        for (int p = __ldg(rp + L.rpOff + k); p < __ldg(rp + L.rpOff + k + 1); ++p)
+            W[I * m + __ldg(nat + __ldg(ci + L.entOff + p))] = float(val[L.entOff + p]);
+    }
+    const int j = threadIdx.x;
+    for (int k = 0; k < m; ++k) {
+        __syncthreads();
+        // pivot: largest |a_ik|, i >= k (first on ties)
+        float best = -1.f;
+        int bi = m;
+        for (int i = k + int(threadIdx.x); i < m; i += blockDim.x) {
+            const float a = fabsf(W[i * m + k]);
+            if (a > best) { best = a; bi = i; }
+        }
+        pv[threadIdx.x] = best;
+        pi[threadIdx.x] = bi;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (int(threadIdx.x) < o) {
+                const float b2 = pv[threadIdx.x + o];
+                const int i2 = pi[threadIdx.x + o];
+                if (b2 > pv[threadIdx.x] || (b2 == pv[threadIdx.x] && i2 < pi[threadIdx.x])) { pv[threadIdx.x] = b2; pi[threadIdx.x] = i2; }
+            }
+            __syncthreads();
+        }
+        const int p = pi[0];
+        if (j < m && p != k) { const float t = W[k * m + j]; W[k * m + j] = W[p * m + j]; W[p * m + j] = t; }
+        if (threadIdx.x == 0) perm[k] = p;
+        __syncthreads();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) col[i] = W[i * m + k];
+        __syncthreads();
+        if (j < m) {
+            float d = col[k];
+            if (fabsf(d) < 1.17549435e-38f) d = 1.17549435e-38f;                 // singular: smallest normal pivot
+            const float akj = j == k ? __fdiv_rn(1.f, d) : __fdiv_rn(W[k * m + j], d);
+            W[k * m + j] = akj;
+            for (int i = 0; i < m; ++i)
+                if (i != k) W[i * m + j] = __fsub_rn(j == k ? 0.f : W[i * m + j], __fmul_rn(col[i], akj));
+        }
+    }
+    __syncthreads();
+    // the row interchanges of the elimination become column interchanges of the inverse, in reverse order
+    if (j < m)
+        for (int k = m - 1; k >= 0; --k) {
+            const int p = perm[k];
+            if (p != k) { const float t = W[j * m + k]; W[j * m + k] = W[j * m + p]; W[j * m + p] = t; }
+        }
+    __syncthreads();
+    float* inv = invAll + L.luOff;
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+        const int jj = q / m, I = q - jj * m;
+        inv[q] = W[I * m + __ldg(nat + jj)];
+    }
 }
 
 // V-cycle row slots from the level values (zero padding), FP32 copies for the FP32 V-cycle
@@ -279,8 +433,19 @@ void launch_amg_refresh(const DevAmg& G, cudaStream_t st) {
 }
 void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st) {
     if (G.totLu <= 0) return;
-    if (fp32) k_coarse_lu<float><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.luf, G.piv, G.cin);
-    else k_coarse_lu<double><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin);
+    if (fp32) {
+        const int smem = int(sizeof(float)) * (kInvSmemRows * kInvSmemRows + kInvSmemRows);
+        raise_smem_limit(reinterpret_cast<const void*>(k_coarse_gj), smem);
+        k_coarse_gj<<<G.nsys, 256, smem, st>>>(G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.invf);
+        if (G.maxCoarse > kInvSmemRows) {                        // levels too large for shared memory: LU, then columns
+            raise_smem_limit(reinterpret_cast<const void*>(k_coarse_inv), smem);
+            k_coarse_lu<float><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.luf, G.piv, G.cin,
+                                                       kInvSmemRows);
+            k_coarse_inv<<<G.nsys, 256, smem, st>>>(G.maxL, G.lv, G.cin, G.luf, G.invf, kInvSmemRows);
+        }
+    } else {
+        k_coarse_lu<double><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin, 0);
+    }
 }
 void launch_amg_round(const DevAmg& G, cudaStream_t st) {
     k_round<<<grid_for(size_t(G.totEnt)), 256, 0, st>>>(size_t(G.totEnt), G.val, G.valf);

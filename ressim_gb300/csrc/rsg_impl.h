@@ -111,6 +111,7 @@ struct AmgSysLv {
     int luOff = 0, luRowOff = 0;       // coarsest: dense LU (m*m) and pivots / natural order (m)
     int slotOff = 0, W = 0;            // row slots of the V-cycle (W off-diagonal entries per row at slotOff + W k)
     int locOff = 0;                    // offset of the level's rows inside the system's V-cycle vectors
+    int mc = 0;                        // Gauss-Seidel schedule: 0 forward levels (reference order), 1 colours
 };
 constexpr int AMG_W0 = 8;              // V-cycle row slots on the finest level (7-point pressure matrix)
 constexpr int AMG_W1 = 16;             // on the Galerkin levels
@@ -128,7 +129,9 @@ struct DevAmg {
     float* valf = nullptr;             // FP32 copy (mixed V-cycle)
     double* apVal = nullptr;           // AP intermediate of the refresh
     double* lu = nullptr;              // coarsest dense LU (FP64)
-    float* luf = nullptr;              // FP32 copy
+    float* luf = nullptr;              // FP32 LU (FP32 precision forms)
+    float* invf = nullptr;             // FP32 forms: explicit inverse, column j at luOff + j m in natural row order
+    int maxCoarse = 0;                 // largest dense coarsest level (rows)
     double *x = nullptr, *b = nullptr, *r = nullptr;   // V-cycle vectors (every level)
     float *xf = nullptr, *bf = nullptr, *rf = nullptr;
     double* w = nullptr;               // CPR weights, level-space block rows of S (n * 3)
@@ -139,6 +142,9 @@ struct DevAmg {
     // the diagonal, off-diagonal entries, entry position where the entries beyond the slots continue, diagonal
     // position} (positions local to the level's entries)
     int totSlots = 0, maxSysAmgRows = 0;
+    // Gauss-Seidel schedule per (system, level): rows in processing order (level space; identity for the forward
+    // levels of the reference order, colour by colour for the multicolour smoother), boundaries in lvl
+    int* gsRows = nullptr;
     int* slotSrc = nullptr;            // global entry of every slot (-1 padding)
     int* slotCol = nullptr;
     int4* rowMeta = nullptr;

@@ -72,6 +72,7 @@ struct rsg_server {
     bool stop = false;
     std::vector<std::thread> workers;
     std::vector<rsg_solver*> handles, bilu;   // per slot: the configured handle, a BILU0 handle for large CPR requests
+    Clock::time_point t0 = Clock::now();      // the server's clock origin (start_ms / end_ms of the results)
 };
 
 namespace {
@@ -131,6 +132,8 @@ void worker(rsg_server* S, int slot) {
         R->res.queue_ms = ms_between(R->tSubmit, R->tStart);
         R->res.run_ms = ms_between(R->tStart, R->tEnd);
         R->res.total_ms = ms_between(R->tSubmit, R->tEnd);
+        R->res.start_ms = ms_between(S->t0, R->tStart);
+        R->res.end_ms = ms_between(S->t0, R->tEnd);
         {
             std::lock_guard<std::mutex> lk(S->mu);
             S->inUse -= R->est;

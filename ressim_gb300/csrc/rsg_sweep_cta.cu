@@ -30,6 +30,10 @@ namespace rsg {
 namespace {
 
 constexpr int kCtaThreads = 256;
+// threads per block of a sweep / CPR kernel (a template parameter of the kernels). 512 threads for the all-FP32
+// forms measured slower on the 64-system ensemble (the V-cycle phases spill at 128 registers), so all forms use 256.
+template <class TF, class TV>
+__host__ __device__ constexpr int cta_threads() { return 256; }
 constexpr int kAhead = 4;                  // levels prefetched into L2 ahead of the sweep front
 
 // one row of a 3x3 block (factor type TF) times a 3-vector of type TV, accumulated from zero left to right
@@ -297,10 +301,10 @@ __device__ __forceinline__ void bwd_level(const IluArgs<TF>& F, const int* lv, i
 
 // Both sweeps of one system by the calling thread block (y: the sweep vector of this system, on chip or in z;
 // xp: with XP, the CPR pressure correction added to z_p as z is written)
-template <class TF, class TV, class TI, int MODE, bool XP, class TX>
+template <class TF, class TV, class TI, int MODE, bool XP, class TX, int NT>
 __device__ void ilu_body(const IluArgs<TF>& F, int row0, int l0, int nl, const TI* r, double* pv, const double* v, double* z, TV* y,
                          bool writeZ, double beta, double omega, double alpha, const TX* xp) {
-    constexpr int NSET = (sizeof(TF) == 4 && MODE == IN_PLAIN) ? 2 : 1;
+    constexpr int NSET = (NT < 512 && sizeof(TF) == 4 && MODE == IN_PLAIN) ? 2 : 1;
     const int* lv = F.lvlStart + l0;
     if (threadIdx.x == 0)
         for (int L = 0; L < kAhead && L < nl; ++L) prefetch_fwd_level<TF, TI, MODE>(F, lv, L, r, pv, v);
@@ -333,8 +337,8 @@ __device__ void ilu_body(const IluArgs<TF>& F, int row0, int l0, int nl, const T
     }
 }
 
-template <class TF, class TV, int MODE>
-__global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(IluArgs<TF> F, const double* r, double* pv, const double* v, double* z,
+template <class TF, class TV, int MODE, int NT = cta_threads<TF, TV>()>
+__global__ void __launch_bounds__(NT) k_ilu_cta(IluArgs<TF> F, const double* r, double* pv, const double* v, double* z,
                                                         TV* yglob, size_t smemBytes, const KScal* ks) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int s = blockIdx.x;
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_ilu_cta(IluArgs<TF> F, const do
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
     TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
     const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
-    ilu_body<TF, TV, double, MODE, false, double>(F, row0, l0, nl, r, pv, v, z, y, onchip || sizeof(TV) != sizeof(double), beta, omega,
+    ilu_body<TF, TV, double, MODE, false, double, NT>(F, row0, l0, nl, r, pv, v, z, y, onchip || sizeof(TV) != sizeof(double), beta, omega,
                                                   alpha, nullptr);
 }
 
@@ -358,7 +362,8 @@ template <class TA>
 struct CprArgs {
     const AmgSysLv* lv;
     int maxL;
-    const int* lvl;                   // GS levels of every (system, level)
+    const int* lvl;                   // GS schedule boundaries of every (system, level): forward levels or colours
+    const int* gsRows;                // rows in schedule order
     const int* ci;                    // level CSR columns / values (entries beyond the row slots)
     const TA* val;
     const int* slotCol;
@@ -367,6 +372,7 @@ struct CprArgs {
     const int4* rowMeta;
     const int *agg, *memPtr, *mem;
     const TA* lu;                     // coarsest dense LU
+    const float* inv;                 // FP32 forms: coarsest explicit inverse (columns, natural row order)
     const int *luPerm, *cin;
     TA *x, *b, *r;                    // V-cycle vectors in global memory (levels that do not fit on chip)
     const double* w;
@@ -433,61 +439,114 @@ __device__ __forceinline__ void prefetch_gs_level(const AmgSysLv& A, const CprAr
     if (bg) l2_prefetch(bg, s * sizeof(TA), e * sizeof(TA));
 }
 
+// row of schedule position pos (-1 stays -1): the colour order for colours; forward levels are the identity (no
+// lookup: it would add a dependent load to every level step)
+__device__ __forceinline__ int sched_row(const int* __restrict__ rw, int pos, bool mc) { return pos >= 0 && mc ? __ldg(rw + pos) : pos; }
+
 template <class TA, int W, int NSET>
-__device__ __forceinline__ void gs_level(const AmgSysLv& A, const CprArgs<TA>& C, const int* lv, int L, int Lnext, int g, int dir,
-                                         GsRow<TA, W>* cur, GsRow<TA, W>* nxt, TA* x, const TA* b, const TA* bg, bool fromZero) {
+__device__ __forceinline__ void gs_level(const AmgSysLv& A, const CprArgs<TA>& C, const int* lv, const int* rw, int L, int Lnext, int g,
+                                         int dir, GsRow<TA, W>* cur, GsRow<TA, W>* nxt, TA* x, const TA* b, const TA* bg, bool fromZero) {
     const int s = __ldg(lv + L), e = __ldg(lv + L + 1);
-    if (threadIdx.x == 0 && g + kAhead < A.nl) prefetch_gs_level<TA, W>(A, C, lv, L + dir * kAhead, bg);
+    if (threadIdx.x == 0 && !A.mc && g + kAhead < A.nl) prefetch_gs_level<TA, W>(A, C, lv, L + dir * kAhead, bg);
     if (Lnext >= 0 && Lnext < A.nl) {
         const int s1 = __ldg(lv + Lnext), e1 = __ldg(lv + Lnext + 1);
 #pragma unroll
-        for (int j = 0; j < NSET; ++j) load_gs(nxt[j], row_of<NSET>(s1, e1, j), A, C);
+        for (int j = 0; j < NSET; ++j) load_gs(nxt[j], sched_row(rw, row_of<NSET>(s1, e1, j), A.mc), A, C);
     }
 #pragma unroll
     for (int j = 0; j < NSET; ++j) {
-        const int k = row_of<NSET>(s, e, j);
+        const int k = sched_row(rw, row_of<NSET>(s, e, j), A.mc);
         if (k >= 0) {
             if (cur[j].k != k) load_gs(cur[j], k, A, C);
             gs_step(cur[j], A, C, x, b, fromZero);
         }
     }
-    for (int k = s + int(threadIdx.x) + NSET * int(blockDim.x); k < e; k += blockDim.x) {
-        load_gs(cur[0], k, A, C);
+    for (int pos = s + int(threadIdx.x) + NSET * int(blockDim.x); pos < e; pos += blockDim.x) {
+        load_gs(cur[0], sched_row(rw, pos, A.mc), A, C);
         gs_step(cur[0], A, C, x, b, fromZero);
+    }
+    __syncthreads();
+}
+
+// Rows a thread takes at once in the parallel passes: their loads are all issued before any is used, so a batch
+// costs about one memory latency (about a microsecond under this load) instead of one per row.
+template <class TA, int W>
+__host__ __device__ constexpr int row_batch() { return sizeof(TA) == 8 ? 1 : (W <= 8 ? 4 : 2); }   // FP64: registers
+
+// One colour of the multicolour sweep: a colour's rows are independent; every thread takes its rows in batches.
+template <class TA, int W>
+__device__ __forceinline__ void gs_colour(const AmgSysLv& A, const CprArgs<TA>& C, const int* __restrict__ rw, int s, int e, TA* x,
+                                          const TA* b) {
+    constexpr int RB = row_batch<TA, W>();
+    const int nt = int(blockDim.x);
+    for (int base = s + int(threadIdx.x); base < e; base += RB * nt) {
+        // named row buffers (an array of row structs would live in local memory)
+        const int k0 = __ldg(rw + base), k1 = RB > 1 && base + nt < e ? __ldg(rw + base + nt) : -1;
+        int k2 = -1, k3 = -1;
+        if (RB > 2) {
+            k2 = base + 2 * nt < e ? __ldg(rw + base + 2 * nt) : -1;
+            k3 = base + 3 * nt < e ? __ldg(rw + base + 3 * nt) : -1;
+        }
+        GsRow<TA, W> R0, R1, R2, R3;
+        load_gs(R0, k0, A, C);
+        if (RB > 1) load_gs(R1, k1, A, C);
+        if (RB > 2) { load_gs(R2, k2, A, C); load_gs(R3, k3, A, C); }
+        gs_step(R0, A, C, x, b, false);
+        if (RB > 1 && k1 >= 0) gs_step(R1, A, C, x, b, false);
+        if (RB > 2) {
+            if (k2 >= 0) gs_step(R2, A, C, x, b, false);
+            if (k3 >= 0) gs_step(R3, A, C, x, b, false);
+        }
     }
     __syncthreads();
 }
 
 // one Gauss-Seidel sweep of a level over its GS levels (forward, or backward for the post-smoothing: valid on the
 // structurally symmetric levels), rows of one GS level in parallel; levels in pairs as the BILU0 sweeps
-template <class TA, int W>
-__device__ __noinline__ void gs_sweep(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, bool bGlobal, bool forward, bool fromZero) {
-    constexpr int NSET = (sizeof(TA) == 4 || W == AMG_W0) ? 2 : 1;
+template <class TA, int W, int NT>
+__device__ __forceinline__ void gs_sweep_body(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, bool bGlobal, bool forward,
+                                              bool fromZero) {
+    constexpr int NSET = NT >= 512 ? 1 : ((sizeof(TA) == 4 || W == AMG_W0) ? 2 : 1);
     const int* lv = C.lvl + A.lvlOff;
+    const int* rw = C.gsRows + A.rowOff;
     const int nl = A.nl, dir = forward ? 1 : -1;
     const TA* bg = bGlobal ? b : nullptr;
     const int Lfirst = forward ? 0 : nl - 1;
+    if constexpr (sizeof(TA) == 4) {                  // the multicolour schedule exists only in the FP32 forms
+        if (A.mc) {                                   // colours: each a batched pass over independent rows
+            if (threadIdx.x == 0) {                   // a colour gathers rows from the whole level: prefetch it once
+                l2_prefetch(C.slotVal + A.slotOff, 0, size_t(A.n) * W * sizeof(TA));
+                l2_prefetch(C.slotCol + A.slotOff, 0, size_t(A.n) * W * sizeof(int));
+                l2_prefetch(C.rowMeta + A.rowOff, 0, size_t(A.n) * sizeof(int4));
+            }
+            for (int g = 0; g < nl; ++g) {
+                const int L = Lfirst + dir * g;
+                gs_colour<TA, W>(A, C, rw, __ldg(lv + L), __ldg(lv + L + 1), x, b);
+            }
+            return;
+        }
+    }
     if (threadIdx.x == 0)
         for (int g = 0; g < kAhead && g < nl; ++g) prefetch_gs_level<TA, W>(A, C, lv, Lfirst + dir * g, bg);
     GsRow<TA, W> P[NSET], Q[NSET];
     if (nl > 0) {
         const int s = __ldg(lv + Lfirst), e = __ldg(lv + Lfirst + 1);
 #pragma unroll
-        for (int j = 0; j < NSET; ++j) load_gs(P[j], row_of<NSET>(s, e, j), A, C);
+        for (int j = 0; j < NSET; ++j) load_gs(P[j], sched_row(rw, row_of<NSET>(s, e, j), A.mc), A, C);
     }
     for (int g = 0; g < nl; g += 2) {
         const int L = Lfirst + dir * g;
-        gs_level<TA, W, NSET>(A, C, lv, L, L + dir, g, dir, P, Q, x, b, bg, fromZero);
-        if (g + 1 < nl) gs_level<TA, W, NSET>(A, C, lv, L + dir, L + 2 * dir, g + 1, dir, Q, P, x, b, bg, fromZero);
+        gs_level<TA, W, NSET>(A, C, lv, rw, L, L + dir, g, dir, P, Q, x, b, bg, fromZero);
+        if (g + 1 < nl) gs_level<TA, W, NSET>(A, C, lv, rw, L + dir, L + 2 * dir, g + 1, dir, Q, P, x, b, bg, fromZero);
     }
 }
 
 // r = b - A x (engine/src/amg.cpp:321-322: the row sum from zero in entry order, diagonal at its place)
 template <class TA, int W>
-__device__ __noinline__ void residual(const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b, TA* r) {
-    for (int k = threadIdx.x; k < A.n; k += blockDim.x) {
-        GsRow<TA, W> R;
-        load_gs(R, k, A, C);
+__device__ __forceinline__ void residual_row(const GsRow<TA, W>& R, const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b,
+                                             TA* r) {
+    {
+        const int k = R.k;
         const int nlow = R.m.x, noff = R.m.y;
         TA t = TA(0);
 #pragma unroll
@@ -505,13 +564,33 @@ __device__ __noinline__ void residual(const AmgSysLv& A, const CprArgs<TA>& C, c
         r[k] = asub(b[k], t);
     }
 }
+template <class TA, int W>
+__device__ __forceinline__ void residual_body(const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b, TA* r) {
+    constexpr int RB = row_batch<TA, W>();
+    const int nt = int(blockDim.x);
+    for (int base = threadIdx.x; base < A.n; base += RB * nt) {
+        GsRow<TA, W> R0, R1, R2, R3;                           // named row buffers (see gs_colour)
+        load_gs(R0, base, A, C);
+        if (RB > 1) load_gs(R1, base + nt < A.n ? base + nt : -1, A, C);
+        if (RB > 2) {
+            load_gs(R2, base + 2 * nt < A.n ? base + 2 * nt : -1, A, C);
+            load_gs(R3, base + 3 * nt < A.n ? base + 3 * nt : -1, A, C);
+        }
+        residual_row(R0, A, C, x, b, r);
+        if (RB > 1 && R1.k >= 0) residual_row(R1, A, C, x, b, r);
+        if (RB > 2) {
+            if (R2.k >= 0) residual_row(R2, A, C, x, b, r);
+            if (R3.k >= 0) residual_row(R3, A, C, x, b, r);
+        }
+    }
+}
 
 // coarsest level: x = LU^-1 b with the dense LU of the natural numbering (engine/src/amg.cpp:306-312). 32-column
 // panels: warp 0 solves the panel's triangle with shuffles, then every thread updates its rows below (forward)
 // or above (backward) with the panel. The forward substitution subtracts every row's terms in ascending column
 // order, as the reference; the backward one takes the panels last to first (rounding-level differences).
 template <class TA>
-__device__ __noinline__ void coarse_dense(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, TA* work) {
+__device__ __forceinline__ void coarse_dense_body(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, TA* work) {
     const int m = A.n, tid = int(threadIdx.x), nt = int(blockDim.x), lane = tid & 31;
     const TA* lu = C.lu + A.luOff;
     const int* nat = C.luPerm + A.luRowOff;
@@ -576,6 +655,51 @@ __device__ __noinline__ void coarse_dense(const AmgSysLv& A, const CprArgs<TA>& 
     __syncthreads();
 }
 
+// The phases above run out of line: inlined into one kernel they would share its register budget (255 at 256
+// threads, 128 at 512) and spill heavily.
+template <class TA, int W, int NT>
+__device__ __noinline__ void gs_sweep_call(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, bool bGlobal, bool forward,
+                                           bool fromZero) {
+    gs_sweep_body<TA, W, NT>(A, C, x, b, bGlobal, forward, fromZero);
+}
+template <class TA, int W, int NT>
+__device__ __forceinline__ void gs_sweep(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, bool bGlobal, bool forward,
+                                         bool fromZero) {
+    gs_sweep_call<TA, W, NT>(A, C, x, b, bGlobal, forward, fromZero);
+}
+template <class TA, int W>
+__device__ __noinline__ void residual_call(const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b, TA* r) {
+    residual_body<TA, W>(A, C, x, b, r);
+}
+template <class TA, int W, int NT>
+__device__ __forceinline__ void residual(const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b, TA* r) {
+    residual_call<TA, W>(A, C, x, b, r);
+}
+// FP32 forms: x = A^-1 b with the explicit inverse; thread k accumulates row k (natural index nat(k)) over the
+// columns, whose entries for consecutive k sit close together
+__device__ __noinline__ void coarse_inverse(const AmgSysLv& A, const CprArgs<float>& C, float* x, const float* b) {
+    const int m = A.n;
+    const float* inv = C.inv + A.luOff;
+    const int* nat = C.luPerm + A.luRowOff;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const float* col = inv + __ldg(nat + k);
+        float acc = 0.f;
+#pragma unroll 8
+        for (int j = 0; j < m; ++j) acc = fmaf(__ldg(col + size_t(j) * m), b[j], acc);
+        x[k] = acc;
+    }
+    __syncthreads();
+}
+
+template <class TA>
+__device__ __noinline__ void coarse_dense_call(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, TA* work) {
+    coarse_dense_body<TA>(A, C, x, b, work);
+}
+template <class TA, int NT>
+__device__ __forceinline__ void coarse_dense(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, TA* work) {
+    coarse_dense_call<TA>(A, C, x, b, work);
+}
+
 // where the V-cycle vectors of system s live: shared memory (x, then b, then r, as far as they fit) or global
 template <class TA>
 struct VVecs {
@@ -586,19 +710,19 @@ struct VVecs {
     __device__ TA* r(const AmgSysLv& A, const CprArgs<TA>& C) const { return rs ? rs + A.locOff : C.r + A.rowOff; }
 };
 
-template <class TA, int W>
+template <class TA, int W, int NT>
 __device__ void gs_sweep_w(const AmgSysLv& A, const CprArgs<TA>& C, const VVecs<TA>& V, bool forward, bool fromZero) {
-    gs_sweep<TA, W>(A, C, V.x(A, C), V.b(A, C), V.bGlobal, forward, fromZero);
+    gs_sweep<TA, W, NT>(A, C, V.x(A, C), V.b(A, C), V.bGlobal, forward, fromZero);
 }
-template <class TA>
+template <class TA, int NT>
 __device__ void gs_any(const AmgSysLv& A, const CprArgs<TA>& C, const VVecs<TA>& V, bool forward, bool fromZero) {
-    if (A.W == AMG_W0) gs_sweep_w<TA, AMG_W0>(A, C, V, forward, fromZero);
-    else gs_sweep_w<TA, AMG_W1>(A, C, V, forward, fromZero);
+    if (A.W == AMG_W0) gs_sweep_w<TA, AMG_W0, NT>(A, C, V, forward, fromZero);
+    else gs_sweep_w<TA, AMG_W1, NT>(A, C, V, forward, fromZero);
 }
 
 // AMG::cycle (engine/src/amg.cpp:303-329) for system s, level-0 right-hand side already in place
-template <class TA>
-__device__ __noinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
+template <class TA, int NT>
+__device__ __forceinline__ void vcycle_body(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
     int nlev = 0;
     while (nlev < C.maxL && C.lv[s * C.maxL + nlev].n > 0) ++nlev;
     int l = 0;
@@ -606,21 +730,27 @@ __device__ __noinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>
         const AmgSysLv A = C.lv[s * C.maxL + l];
         if (A.coarse) {
             if (A.dense) {
-                coarse_dense(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
+                if constexpr (sizeof(TA) == 4) coarse_inverse(A, C, V.x(A, C), V.b(A, C));
+                else coarse_dense<TA, NT>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
             } else {                                      // 20 symmetric GS sweeps from x = 0 (amg.cpp:313-315)
                 TA* xl = V.x(A, C);
                 for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = TA(0);
                 __syncthreads();
                 for (int it = 0; it < 20; ++it) {
-                    gs_any(A, C, V, true, false);
-                    gs_any(A, C, V, false, false);
+                    gs_any<TA, NT>(A, C, V, true, false);
+                    gs_any<TA, NT>(A, C, V, false, false);
                 }
             }
             break;
         }
-        gs_any(A, C, V, true, true);
-        if (A.W == AMG_W0) residual<TA, AMG_W0>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
-        else residual<TA, AMG_W1>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
+        if (A.mc) {                                     // colours: from x = 0 with full rows (x of later colours is 0)
+            TA* xl = V.x(A, C);
+            for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = TA(0);
+            __syncthreads();
+        }
+        gs_any<TA, NT>(A, C, V, true, !A.mc);
+        if (A.W == AMG_W0) residual<TA, AMG_W0, NT>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
+        else residual<TA, AMG_W1, NT>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
         __syncthreads();
         // restriction b_{l+1} = R r: members in ascending natural order (amg.cpp:324)
         {
@@ -646,8 +776,17 @@ __device__ __noinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>
         const int* agg = C.agg + A.rowOff;
         for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = aadd(xl[k], xc[__ldg(agg + k)]);
         __syncthreads();
-        gs_any(A, C, V, false, false);
+        gs_any<TA, NT>(A, C, V, false, false);
     }
+}
+
+template <class TA, int NT>
+__device__ __noinline__ void vcycle_call(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
+    vcycle_body<TA, NT>(s, C, V);
+}
+template <class TA, int NT>
+__device__ __forceinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
+    vcycle_call<TA, NT>(s, C, V);
 }
 
 // t -= S_kj[:,p] xp_j for the pressure column of one block (TT: the arithmetic of the second-stage input)
@@ -667,8 +806,8 @@ __device__ __forceinline__ void sub_p(float (&acc)[3], const float* s3, float xk
 // One CPR application per system. The second-stage input t lives in C.T with the sweep vector's type TV: FP64
 // for the FP64 and mixed forms, FP32 for the all-FP32 preconditioner, whose restriction w . r, t = r - S[:,p] xp
 // and sweeps then run in FP32 arithmetic (the FP64 unit is a small fraction of the FP32 rate on this part).
-template <class TF, class TV, class TA, int MODE>
-__global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(IluArgs<TF> F, CprArgs<TA> C, const double* r, double* pv, const double* v,
+template <class TF, class TV, class TA, int MODE, int NT = cta_threads<TF, TV>()>
+__global__ void __launch_bounds__(NT) k_cpr_cta(IluArgs<TF> F, CprArgs<TA> C, const double* r, double* pv, const double* v,
                                                         double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int s = blockIdx.x, tid = int(threadIdx.x), nt = int(blockDim.x);
@@ -692,27 +831,46 @@ __global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(IluArgs<TF> F, CprArgs<
     V.bGlobal = V.bs == nullptr;
     const AmgSysLv A0 = C.lv[s * C.maxL];
     TA* b0 = V.b(A0, C);
-    // input (fused Krylov update) and pressure restriction rp = w . r (bsr.cpp:1064-1067)
-    for (int k = row0 + tid; k < row0 + ns; k += nt) {
-        double in[3];
+    // input (fused Krylov update) and pressure restriction rp = w . r (bsr.cpp:1064-1067), rows in batches of 4
+    // (all loads of a batch issued before any use)
+    constexpr int IB = sizeof(TV) == 4 ? 4 : 1;                   // FP64 forms: registers
+    for (int base = row0 + tid; base < row0 + ns; base += IB * nt) {
+        double ri[IB][3], pi[IB][3], vi[IB][3], wi[IB][3];
 #pragma unroll
-        for (int e = 0; e < 3; ++e) {
-            const size_t q = size_t(k) * 3 + e;
-            if (MODE == IN_PUPDATE) { in[e] = da(r[q], dm(beta, ds(pv[q], dm(omega, v[q])))); pv[q] = in[e]; }
-            else if (MODE == IN_SUPDATE) { in[e] = ds(r[q], dm(alpha, v[q])); pv[q] = in[e]; }
-            else in[e] = r[q];
-            T[q] = TV(in[e]);
+        for (int u = 0; u < IB; ++u) {
+            const int k = min(base + u * nt, row0 + ns - 1);    // past the end: re-read the last row, not stored
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const size_t q = size_t(k) * 3 + e;
+                ri[u][e] = r[q];
+                pi[u][e] = MODE == IN_PUPDATE ? pv[q] : 0.0;
+                vi[u][e] = MODE != IN_PLAIN ? v[q] : 0.0;
+                wi[u][e] = __ldg(C.w + q);
+            }
         }
-        const double* wk = C.w + size_t(k) * 3;
-        if (sizeof(TV) == 4) {
-            const float i0 = float(in[0]), i1 = float(in[1]), i2 = float(in[2]);
-            b0[k - row0] = TA(float(__ldg(wk)) * i0 + float(__ldg(wk + 1)) * i1 + float(__ldg(wk + 2)) * i2);
-        } else {
-            b0[k - row0] = TA(da(da(dm(__ldg(wk), in[0]), dm(__ldg(wk + 1), in[1])), dm(__ldg(wk + 2), in[2])));
+#pragma unroll
+        for (int u = 0; u < IB; ++u) {
+            const int k = base + u * nt;
+            if (k >= row0 + ns) break;
+            double in[3];
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const size_t q = size_t(k) * 3 + e;
+                if (MODE == IN_PUPDATE) { in[e] = da(ri[u][e], dm(beta, ds(pi[u][e], dm(omega, vi[u][e])))); pv[q] = in[e]; }
+                else if (MODE == IN_SUPDATE) { in[e] = ds(ri[u][e], dm(alpha, vi[u][e])); pv[q] = in[e]; }
+                else in[e] = ri[u][e];
+                T[q] = TV(in[e]);
+            }
+            if (sizeof(TV) == 4) {
+                const float i0 = float(in[0]), i1 = float(in[1]), i2 = float(in[2]);
+                b0[k - row0] = TA(float(wi[u][0]) * i0 + float(wi[u][1]) * i1 + float(wi[u][2]) * i2);
+            } else {
+                b0[k - row0] = TA(da(da(dm(wi[u][0], in[0]), dm(wi[u][1], in[1])), dm(wi[u][2], in[2])));
+            }
         }
     }
     __syncthreads();
-    vcycle<TA>(s, C, V);
+    vcycle<TA, NT>(s, C, V);
     // second stage on t = r - S[:,p] xp (pressure columns in S's row order, bsr.cpp:1071-1081); xp to global
     // memory for the final correction when it lived on chip
     const TA* xp = V.x(A0, C);
@@ -752,9 +910,9 @@ __global__ void __launch_bounds__(kCtaThreads) k_cpr_cta(IluArgs<TF> F, CprArgs<
     const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
     const bool writeZ = onchip || sizeof(TV) != sizeof(double);
     if (writeZ) {   // y is not z: z_p += xp (bsr.cpp:1083) as z is written
-        ilu_body<TF, TV, TV, IN_PLAIN, true, TA>(F, row0, l0, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
+        ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
     } else {        // y is z itself: the correction after the sweeps
-        ilu_body<TF, TV, TV, IN_PLAIN, false, TA>(F, row0, l0, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
+        ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
         for (int k = row0 + tid; k < row0 + ns; k += nt) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xpg[k - row0]));
     }
 }
@@ -884,7 +1042,7 @@ template <class TF, class TV, int MODE>
 void launch_cta(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, const double* r, double* pv, const double* v, double* z,
                 TV* yglob, const KScal* ks, cudaStream_t st) {
     raise_smem_limit(reinterpret_cast<const void*>(k_ilu_cta<TF, TV, MODE>), int(smem));
-    k_ilu_cta<TF, TV, MODE><<<P.nsys, kCtaThreads, smem, st>>>(ilu_args(P, S), r, pv, v, z, yglob, smem, ks);
+    k_ilu_cta<TF, TV, MODE><<<P.nsys, cta_threads<TF, TV>(), smem, st>>>(ilu_args(P, S), r, pv, v, z, yglob, smem, ks);
 }
 
 template <int MODE>
@@ -944,8 +1102,8 @@ namespace {
 template <class TA>
 CprArgs<TA> cpr_args(const DevAmg& G, const TA* val, const TA* slotVal, const TA* diagVal, const TA* lu, TA* x, TA* b, TA* r, const TA* sp,
                      const TA* spLov, const TA* spUov) {
-    return CprArgs<TA>{G.lv, G.maxL, G.lvl, G.ci, val, G.slotCol, slotVal, diagVal, G.rowMeta, G.agg, G.memPtr, G.mem, lu, G.luPerm,
-                       G.cin, x, b, r, G.w, G.T, sp, spLov, spUov};
+    return CprArgs<TA>{G.lv, G.maxL, G.lvl, G.gsRows, G.ci, val, G.slotCol, slotVal, diagVal, G.rowMeta, G.agg, G.memPtr, G.mem, lu, G.invf,
+                       G.luPerm, G.cin, x, b, r, G.w, G.T, sp, spLov, spUov};
 }
 
 template <class TF, class TV, class TA, int MODE>
@@ -955,7 +1113,7 @@ void launch_cpr_t(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, cons
     const size_t cap = size_t(max_smem_optin());
     smem = std::max(smem, std::min(cap, size_t(G.maxSysAmgRows) * 3 * sizeof(TA)));
     raise_smem_limit(reinterpret_cast<const void*>(k_cpr_cta<TF, TV, TA, MODE>), int(smem));
-    k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, kCtaThreads, smem, st>>>(ilu_args(P, S), C, r, pv, v, z, yglob, smem, ks);
+    k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, cta_threads<TF, TV>(), smem, st>>>(ilu_args(P, S), C, r, pv, v, z, yglob, smem, ks);
 }
 }  // namespace
 

@@ -160,11 +160,12 @@ class DeviceSolver:
 class Server:
     """Serving form (``rsg_server_*``): continuous batching of independent systems over ``slots`` workers under a
     device-memory budget. ``submit`` copies a system and returns its id; ``poll`` returns ``None`` while it is
-    queued or running, else ``(x, result)`` with the per-request latency split (queue / run / total ms)."""
+    queued or running, else ``(x, result)`` with the per-request latency split (queue / run / total ms). As the
+    engine does, a BiCGSTAB solve that does not converge is retried with GMRES (``gmres_fallback``, on by default)."""
 
     def __init__(self, slots: int = 4, mem_budget: int = 0, precond: str = "cpr", krylov: str = "bicgstab",
                  precision: str = "mixed_f32", restart: int = 40, check_every: int = 4, use_graphs: bool = True, device: int = 0,
-                 gmres_fallback: bool = False):
+                 gmres_fallback: bool = True):
         self.L = _lib.load()
         o = _lib.Options()
         self.L.rsg_default_options(C.byref(o))
