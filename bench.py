@@ -63,9 +63,24 @@ def traffic_of(kernel):
         return None
 
 
+def rank_seed0(rank):
+    """Weak scaling: every rank solves its own ensemble (seeds 64 r .. 64 r + 63)."""
+    return 64 * rank
+
+
 def ensemble(rank):
     from ressim_gb300 import synth
-    return synth.ensemble(n_real=N_REAL, nx=NX, ny=NY, nz=NZ, sigma=SIGMA, seed0=64 * rank)
+    return synth.ensemble(n_real=N_REAL, nx=NX, ny=NY, nz=NZ, sigma=SIGMA, seed0=rank_seed0(rank))
+
+
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The slowest rank's time (the job's time): all-reduce MAX over the process group, or the value itself."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 class Clocks:
@@ -249,9 +264,7 @@ def main():
     x_dev = d_x.cpu().numpy()
     T = sum(step_ms) / 1e3
     if dist:
-        t = torch.tensor([T], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        T = float(t.item())
+        T = max_over_ranks(T, dist, f"cuda:{local}")
     value = world * N_REAL * args.steps / T
     ok = all(r.converged for r in results) and float(np.max(tr)) <= TOL
 
@@ -305,9 +318,7 @@ def main():
             e2e_t.append(time.perf_counter() - t0)
     Te = sum(e2e_t)
     if dist:
-        t = torch.tensor([Te], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        Te = float(t.item())
+        Te = max_over_ranks(Te, dist, f"cuda:{local}")
     e2e = {"value": world * N_REAL * len(e2e_t) / Te, "unit": "solves/s", "h2d_bytes_per_step": val_bytes + N * 8,
            "d2h_bytes_per_step": N * 8, "p50_ms": 1e3 * statistics.median(e2e_t)}
     dev.close()
