@@ -186,11 +186,7 @@ int alloc_plan(rsg_solver* h) {
         (rc = upload(M, reinterpret_cast<int**>(&D.Uslot), P.Uslot, st)) || (rc = upload(M, &D.UslotSrc, P.UslotSrc, st)) ||
         (rc = upload(M, &D.UovCol, P.UovCol, st)) || (rc = upload(M, &D.UovSrc, P.UovSrc, st)) || (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
         return rc;
-    D.spmvStage = P.spmvStage;
-    D.spmvCol = P.spmvCol;
     D.spmvFma = h->opt.fma != 0;
-    D.spmvErr = h->d_err;
-    prepare_spmv(D);
     D.nLov = int(P.LovCol.size());
     D.nUov = int(P.UovCol.size());
     D.maxSysRows = P.maxSysRows;

@@ -40,7 +40,7 @@ __device__ __forceinline__ double* gm_H(double* H, int s, int m) { return H + si
 // x = 0 and ||b|| for the (re)started systems; their scalars reset
 __global__ void __launch_bounds__(kTileThreads) k_gm_init(Tiles T, const double* __restrict__ b, double* x, KScal* ks, double tol, int maxit,
                                                          int onlyFailed, double* part, unsigned* done, double* sysdot, int* active) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x, s = __ldg(T.tileSys + tile);
     const bool restart = !onlyFailed || ks[s].status != ST_CONV;
     double acc[MAX_DOTS] = {0, 0, 0, 0};
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kTileThreads) k_gm_resid(Tiles T, const int* _
                                                           const double* __restrict__ val, const double* __restrict__ b, const double* x,
                                                           double* V0, KScal* ks, double* H, int m, double* part, unsigned* done,
                                                           double* sysdot, int* active, int* inner) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x, s = __ldg(T.tileSys + tile);
     double acc[MAX_DOTS] = {0, 0, 0, 0};
     if (ks[s].status == ST_RUNNING) {
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kTileThreads) k_gm_av(Tiles T, const int* __re
                                                        const double* __restrict__ val, const double* z, const double* v0, double* w,
                                                        const KScal* ks, double* H, int m, int j, double* part, unsigned* done,
                                                        double* sysdot) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x, s = __ldg(T.tileSys + tile);
     double acc[MAX_DOTS] = {0, 0, 0, 0};
     if (ks[s].status == ST_RUNNING) {
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kTileThreads) k_gm_av(Tiles T, const int* __re
 // MGS step i of column j: w -= h_{i-1,j} V_{i-1}, then <w, V_i> -> h_ij (linsolve.cpp:241-245)
 __global__ void __launch_bounds__(kTileThreads) k_gm_mgs(Tiles T, const double* vprev, const double* vi, double* w, const KScal* ks,
                                                         double* H, int m, int i, int j, double* part, unsigned* done, double* sysdot) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x, s = __ldg(T.tileSys + tile);
     double acc[MAX_DOTS] = {0, 0, 0, 0};
     if (ks[s].status == ST_RUNNING) {
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kTileThreads) k_gm_mgs(Tiles T, const double* 
 // (linsolve.cpp:246-264)
 __global__ void __launch_bounds__(kTileThreads) k_gm_norm(Tiles T, const double* vj, double* w, KScal* ks, double* H, int m, int j,
                                                          double* part, unsigned* done, double* sysdot, int* active, int* inner) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x, s = __ldg(T.tileSys + tile);
     double acc[MAX_DOTS] = {0, 0, 0, 0};
     if (ks[s].status == ST_RUNNING) {

@@ -69,7 +69,6 @@ struct HostPlan {
     std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of row k
     int maxSysRows = 0;
     // bulk-staged SpMV: bytes of one stage (values, columns) covering the largest 64-row chunk of any tile
-    int spmvStage = 0, spmvCol = 0;
 };
 
 struct PrecDev;
@@ -190,9 +189,7 @@ struct DevPlan {
     int *LslotSrc = nullptr, *UslotSrc = nullptr, *LovCol = nullptr, *LovSrc = nullptr, *UovCol = nullptr, *UovSrc = nullptr;
     int* Dsrc = nullptr;
     int nLov = 0, nUov = 0, maxSysRows = 0;
-    int spmvStage = 0, spmvCol = 0;   // bulk-staged SpMV stage sizes (0: direct loads)
     bool spmvFma = true;              // SpMV with fused multiply-adds (else the reference's rounding, bitwise)
-    int* spmvErr = nullptr;           // error bits of the staged SpMV (bounded waits)
 };
 
 // Slot-layout factors for the CTA-per-system sweeps (FP64 or FP32 storage): L = n x LREC, UD = n x UREC,
@@ -233,7 +230,6 @@ void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r,
                             cudaStream_t st);
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st);
 // shared-memory opt-in of the bulk-staged SpMV for this plan's stage sizes (before any graph capture)
-void prepare_spmv(const DevPlan& P);
 // raise (never lower) a kernel's dynamic shared-memory opt-in on the current device; thread-safe
 void raise_smem_limit(const void* fn, int bytes);
 // block-Jacobi: dinv = inverse diagonal blocks (FP64), z = dinv r

@@ -395,15 +395,13 @@ enum { SP_PLAIN = 0, SP_RV = 1, SP_OMEGA = 2, SP_TRUERES = 3 };
 // <b,b>, result sqrt ratio into out[s].
 //
 // Arithmetic (FMA): false = the reference's order and rounding per block (engine/src/bsr.cpp:109-117: row sum of
-// the block from zero, then added; bitwise the reference), true = one fused multiply-add per term (half the FP64
-// instructions; the FP64 unit, not HBM, bounds the unfused form on this part).
-// Staging (BULK): the tile is walked in chunks of 64 block rows; the chunk's value blocks and column indices are
-// contiguous and arrive in shared memory by bulk copies (cp.async.bulk, completion on an mbarrier), two chunks in
-// flight, so HBM streams at full line utilisation while the previous chunk is computed.
-struct SpmvCfg {
-    int stageBytes = 0, colBytes = 0;   // per stage: value / column bytes (16-byte multiples; 0 = no staging)
-    int* err = nullptr;
-};
+// the block from zero, then added; bitwise the reference), true = one fused multiply-add per term.
+// On GB300 the FP64 unit runs at 1/64 of the FP32 rate, and the 9 multiply-adds of a block bound this kernel
+// rather than HBM: the FMA form keeps the FP64 pipe about 90 % busy at 70 % of the HBM copy rate, the unfused
+// form needs twice the FP64 instructions. Hence direct read-only loads (the values stream once, the x gather
+// hits L2), 128 block rows per pass so the SM holds enough loads in flight, and a reduction that spends as few
+// FP64 adds as possible (rsg_reduce.cuh).
+constexpr int kSpmvThreads = 384;
 
 template <bool FMA>
 __device__ __forceinline__ double block_row_term(double yv, const double* a, const double* xc) {
@@ -431,37 +429,22 @@ __device__ __forceinline__ void spmv_out(size_t q, double yv, double* y, const d
     }
 }
 
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
-__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
-    unsigned ok;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-    return ok != 0;
-}
-// bounded wait for a phase of an mbarrier (each try_wait suspends for a while; about a second in all)
-__device__ __noinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    for (unsigned it = 0; it < (1u << 20); ++it)
-        if (mbar_try(bar, parity)) return true;
-    return false;
-}
-
-template <int MODE, bool BULK, bool FMA>
-__global__ void __launch_bounds__(kTileThreads) k_spmv_tile(int ntiles, int nsys, const int* __restrict__ tileRow0,
+template <int MODE, bool FMA>
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv_tile(int ntiles, int nsys, const int* __restrict__ tileRow0,
                                                            const int* __restrict__ tileSys, const int* __restrict__ sysTile0,
                                                            const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                            const double* __restrict__ val, const double* __restrict__ x, double* y,
-                                                           const double* __restrict__ a1, const double* __restrict__ a2, KScal* ks,
-                                                           double* part, unsigned* done, double* sysdot, int* active, double* out,
-                                                           SpmvCfg cfg) {
-    __shared__ double sh[MAX_DOTS * 32];
+                                                           const double* __restrict__ a1, KScal* ks, double* part, unsigned* done,
+                                                           double* sysdot, int* active, double* out) {
+    __shared__ double sh[MAX_DOTS * kSpmvThreads];
     const int tile = blockIdx.x;
     const int s = __ldg(tileSys + tile);
     const bool run = (MODE == SP_PLAIN || MODE == SP_TRUERES) || ks[s].status == ST_RUNNING;
     double acc[MAX_DOTS] = {0, 0, 0, 0};
-    if (run && !BULK) {
+    if (run) {
         const int r0 = __ldg(tileRow0 + tile), r1 = __ldg(tileRow0 + tile + 1);
         const int e = threadIdx.x % 3;
-        for (int row = r0 + int(threadIdx.x) / 3; row < r1; row += kTileThreads / 3) {
+        for (int row = r0 + int(threadIdx.x) / 3; row < r1; row += kSpmvThreads / 3) {
             double yv = 0;
             const int p1 = __ldg(rowPtr + row + 1);
             for (int p = __ldg(rowPtr + row); p < p1; ++p) {
@@ -470,75 +453,6 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv_tile(int ntiles, int nsys
                 yv = block_row_term<FMA>(yv, av, x + size_t(__ldg(col + p)) * 3);
             }
             spmv_out<MODE>(size_t(row) * 3 + e, yv, y, a1, acc);
-        }
-    }
-    if (run && BULK) {
-        extern __shared__ __align__(128) unsigned char stg[];
-        __shared__ __align__(8) unsigned long long bar[2];
-        __shared__ int timedOut;
-        __shared__ int nIss[2], nDone[2];                          // uses issued / waited per stage (thread 0)
-        constexpr int CH = kTileThreads / 3;                      // block rows per chunk: one per thread triple
-        const int r0 = __ldg(tileRow0 + tile), r1 = __ldg(tileRow0 + tile + 1);
-        const int nch = (r1 - r0 + CH - 1) / CH;
-        const int sb = cfg.stageBytes + cfg.colBytes;
-        const unsigned long long vbase = reinterpret_cast<unsigned long long>(val), cbase = reinterpret_cast<unsigned long long>(col);
-        auto issue = [&](int c) {                                  // thread 0: chunk c into stage c & 1
-            const int rs = r0 + c * CH, re = min(r1, rs + CH);
-            const unsigned long long b0 = unsigned(__ldg(rowPtr + rs)), b1 = unsigned(__ldg(rowPtr + re));
-            const unsigned long long v0 = (vbase + b0 * 72) & ~15ull, v1 = (vbase + b1 * 72 + 15) & ~15ull;
-            const unsigned long long c0 = (cbase + b0 * 4) & ~15ull, c1 = (cbase + b1 * 4 + 15) & ~15ull;
-            const unsigned b = smem_addr(&bar[c & 1]);
-            unsigned char* dst = stg + size_t(c & 1) * sb;
-            ++nIss[c & 1];
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(unsigned((v1 - v0) + (c1 - c0))) : "memory");
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         ::"r"(smem_addr(dst)), "l"(v0), "r"(unsigned(v1 - v0)), "r"(b) : "memory");
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         ::"r"(smem_addr(dst + cfg.stageBytes)), "l"(c0), "r"(unsigned(c1 - c0)), "r"(b) : "memory");
-        };
-        if (threadIdx.x == 0) {
-            timedOut = 0;
-            nIss[0] = nIss[1] = nDone[0] = nDone[1] = 0;
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[0])) : "memory");
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[1])) : "memory");
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            issue(0);
-            if (nch > 1) issue(1);
-        }
-        __syncthreads();
-        const int e = threadIdx.x % 3;
-        for (int c = 0; c < nch; ++c) {
-            const bool ok = mbar_wait(smem_addr(&bar[c & 1]), unsigned((c >> 1) & 1));
-            if (!ok) timedOut = 1;
-            if (ok && threadIdx.x == 0) ++nDone[c & 1];
-            __syncthreads();
-            if (!timedOut) {
-                const int rs = r0 + c * CH, re = min(r1, rs + CH);
-                const int b0 = __ldg(rowPtr + rs);
-                const unsigned char* st = stg + size_t(c & 1) * sb;
-                const double* vs = reinterpret_cast<const double*>(st + ((vbase + unsigned(b0) * 72ull) & 15ull));
-                const int* cs = reinterpret_cast<const int*>(st + cfg.stageBytes + ((cbase + unsigned(b0) * 4ull) & 15ull));
-                const int row = rs + int(threadIdx.x) / 3;
-                if (row < re) {
-                    double yv = 0;
-                    const int p1 = __ldg(rowPtr + row + 1);
-                    for (int p = __ldg(rowPtr + row); p < p1; ++p) {
-                        const int j = p - b0;
-                        yv = block_row_term<FMA>(yv, vs + size_t(j) * 9 + e * 3, x + size_t(cs[j]) * 3);
-                    }
-                    spmv_out<MODE>(size_t(row) * 3 + e, yv, y, a1, acc);
-                }
-            }
-            __syncthreads();                                      // stage c & 1 free
-            if (threadIdx.x == 0 && c + 2 < nch && !timedOut) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(c + 2);
-            }
-        }
-        if (timedOut && threadIdx.x == 0) {                       // let the copies in flight land before the block ends
-            for (int st = 0; st < 2; ++st)
-                while (nDone[st] < nIss[st] && mbar_wait(smem_addr(&bar[st]), unsigned(nDone[st] & 1))) ++nDone[st];
-            atomicOr(cfg.err, ERR_TIMEOUT);
         }
     }
     if (MODE == SP_PLAIN) return;
@@ -578,7 +492,7 @@ __global__ void __launch_bounds__(kTileThreads) k_bicg_init(int ntiles, int nsys
                                                            const double* __restrict__ b, double* x, double* r, double* rh, double* p,
                                                            double* v, KScal* ks, double tol, int maxit, double* part,
                                                            unsigned* done, double* sysdot, int* active) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x;
     const size_t q0 = size_t(__ldg(tileRow0 + tile)) * 3, q1 = size_t(__ldg(tileRow0 + tile + 1)) * 3;
     double acc[MAX_DOTS] = {0, 0, 0, 0};
@@ -615,7 +529,7 @@ __global__ void __launch_bounds__(kTileThreads) k_bicg_update(int ntiles, int ns
                                                              const double* __restrict__ s, const double* __restrict__ t,
                                                              const double* __restrict__ ph, const double* __restrict__ sh_,
                                                              KScal* ks, double* part, unsigned* done, double* sysdot, int* active) {
-    __shared__ double sh[MAX_DOTS * 32];
+    __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x;
     const int sy = __ldg(tileSys + tile);
     KScal K = ks[sy];
@@ -807,30 +721,19 @@ void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, d
                                           S.ctr, err);
 }
 
-// SpMV tile kernel with the handle's arithmetic (P.spmvFma) and, when the plan sized the stages, bulk staging
-template <int MODE, bool BULK, bool FMA>
+template <int MODE, bool FMA>
 void spmv_go(const DevPlan& P, const double* val, const double* x, double* y, const double* a1, KScal* ks, ReduceState* R, int* active,
              double* out, cudaStream_t st) {
-    const SpmvCfg cfg{BULK ? P.spmvStage : 0, BULK ? P.spmvCol : 0, P.spmvErr};
-    const size_t smem = BULK ? 2 * size_t(P.spmvStage + P.spmvCol) : 0;   // opt-in set by prepare_spmv
-    k_spmv_tile<MODE, BULK, FMA><<<P.ntiles, kTileThreads, smem, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr,
-                                                                      P.col, val, x, y, a1, nullptr, ks, R ? R->part : nullptr,
-                                                                      R ? R->done : nullptr, R ? R->sysdot : nullptr, active, out, cfg);
+    k_spmv_tile<MODE, FMA><<<P.ntiles, kSpmvThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, P.rowPtr, P.col, val,
+                                                               x, y, a1, ks, R ? R->part : nullptr, R ? R->done : nullptr,
+                                                               R ? R->sysdot : nullptr, active, out);
 }
+// SpMV tile kernel with the handle's arithmetic (P.spmvFma)
 template <int MODE>
 void spmv(const DevPlan& P, const double* val, const double* x, double* y, const double* a1, KScal* ks, ReduceState* R, int* active,
           double* out, cudaStream_t st) {
-    const bool bulk = P.spmvStage > 0;
-    if (bulk && P.spmvFma) spmv_go<MODE, true, true>(P, val, x, y, a1, ks, R, active, out, st);
-    else if (bulk) spmv_go<MODE, true, false>(P, val, x, y, a1, ks, R, active, out, st);
-    else if (P.spmvFma) spmv_go<MODE, false, true>(P, val, x, y, a1, ks, R, active, out, st);
-    else spmv_go<MODE, false, false>(P, val, x, y, a1, ks, R, active, out, st);
-}
-
-template <int MODE>
-void allow_smem(int bytes) {
-    raise_smem_limit(reinterpret_cast<const void*>(k_spmv_tile<MODE, true, true>), bytes);
-    raise_smem_limit(reinterpret_cast<const void*>(k_spmv_tile<MODE, true, false>), bytes);
+    if (P.spmvFma) spmv_go<MODE, true>(P, val, x, y, a1, ks, R, active, out, st);
+    else spmv_go<MODE, false>(P, val, x, y, a1, ks, R, active, out, st);
 }
 
 // The dynamic shared-memory opt-in of a kernel is one process-wide value per device: handles on several threads
@@ -847,15 +750,6 @@ void raise_smem_limit(const void* fn, int bytes) {
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         cur = bytes;
     }
-}
-
-void prepare_spmv(const DevPlan& P) {
-    const int smem = 2 * (P.spmvStage + P.spmvCol);
-    if (smem <= 48 * 1024) return;
-    allow_smem<SP_PLAIN>(smem);
-    allow_smem<SP_RV>(smem);
-    allow_smem<SP_OMEGA>(smem);
-    allow_smem<SP_TRUERES>(smem);
 }
 
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st) {

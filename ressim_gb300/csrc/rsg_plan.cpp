@@ -163,22 +163,6 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     }
     P.sysTile0[size_t(nsys)] = int(P.tileSys.size());
     P.tileRow0.push_back(n);
-    // stage sizes of the bulk-staged SpMV: every 64-row chunk of a tile, with 16-byte rounding on both ends
-    {
-        long long vmax = 0, cmax = 0;
-        for (size_t t = 0; t + 1 < P.tileRow0.size(); ++t)
-            for (int rs = P.tileRow0[t]; rs < P.tileRow0[t + 1]; rs += 64) {
-                const int re = std::min(P.tileRow0[t + 1], rs + 64);
-                const long long b = P.rowPtr[size_t(re)] - P.rowPtr[size_t(rs)];
-                vmax = std::max(vmax, b * 72 + 32);
-                cmax = std::max(cmax, b * 4 + 32);
-            }
-        vmax = (vmax + 127) / 128 * 128;
-        cmax = (cmax + 127) / 128 * 128;
-        const bool fits = 2 * (vmax + cmax) <= 160 * 1024;          // two stages, two blocks per SM
-        P.spmvStage = fits ? int(vmax) : 0;
-        P.spmvCol = fits ? int(cmax) : 0;
-    }
     // slot storage of the thread-block sweeps (rows of a level contiguous; columns local to the system)
     P.Lslot.assign(size_t(n) * 4, -1);
     P.Uslot.assign(size_t(n) * 4, -1);

@@ -11,25 +11,28 @@ namespace {
 
 constexpr int kTileThreads = 192;           // 64 block rows x 3 per step
 
-// Block reduction of up to MAX_DOTS values; result valid in thread 0.
+// Block reduction of ND <= MAX_DOTS values; result valid in thread 0. Every thread leaves its values in shared
+// memory and warp j sums value j (a strided pass, then a shuffle tree), in a fixed order. FP64 runs at 1/64 of
+// the FP32 rate on GB300: a shuffle tree in every warp would spend five FP64 adds per thread and value, this
+// spends about one per 32 threads. Needs blockDim.x >= 32 * ND.
 template <int ND>
-__device__ __forceinline__ void block_reduce(double (&v)[MAX_DOTS], double* sh /* [ND][kTileThreads/32] */) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+__device__ __forceinline__ void block_reduce(double (&v)[MAX_DOTS], double* sh /* [ND][blockDim.x] */) {
+    const int nt = blockDim.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int j = 0; j < ND; ++j) {
-        double x = v[j];
+    for (int j = 0; j < ND; ++j) sh[j * nt + threadIdx.x] = v[j];
+    __syncthreads();
+    if (w < ND) {
+        const double* q = sh + w * nt;
+        double x = 0;
+        for (int i = lane; i < nt; i += 32) x += q[i];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[j * 32 + w] = x;
+        if (lane == 0) sh[w * nt] = x;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int j = 0; j < ND; ++j) {
-            double s = 0;
-            for (int q = 0; q < nw; ++q) s += sh[j * 32 + q];
-            v[j] = s;
-        }
+        for (int j = 0; j < ND; ++j) v[j] = sh[j * nt];
     }
 }
 

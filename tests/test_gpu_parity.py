@@ -71,9 +71,11 @@ def test_bicgstab_bilu0_matches_reference(name, case, tol, maxit, sweep, fma):
     assert res.converged
     sens = float(z["sens_" + case])
     if sens < 1e-3:
-        # reference rounding: the same iteration count; fused multiply-adds move the last digits like a change of
-        # summation order does, which may end the iteration one step earlier or later
-        assert abs(res.iterations - int(z["its_" + case])) <= (1 if fma else 0)
+        # SpMV (fma=False) and BILU0 round as the reference does, the inner products are summed as a tree across the
+        # tile and not left to right: the last digits move as under any change of summation order, which may end the
+        # iteration a step earlier or later (two at 1e-10 over ~40 steps); fused multiply-adds do the same
+        its_ref = int(z["its_" + case])
+        assert abs(res.iterations - its_ref) <= max(1, its_ref // 15)
     else:   # near-singular system: the iteration count itself moves under a change of summation order
         assert res.iterations <= 3 * int(z["its_" + case])
     # 1e-8 relative, or 10x the solution's own sensitivity to a change of inner-product summation order
@@ -194,7 +196,7 @@ def test_error_paths():
             d.solve(b, tol=1e-6, maxit=50)
         assert e.value.code == _lib.RSG_EBREAKDOWN
         x, res = d.solve(z["b"], tol=1e-6, maxit=120)         # the handle stays usable
-        assert res.converged and res.iterations == int(z["its_bicg_bilu0"])
+        assert res.converged and abs(res.iterations - int(z["its_bicg_bilu0"])) <= 1   # tree-summed inner products
     # missing diagonal block
     rp = np.array([0, 1, 2], dtype=np.int32)
     bad = BSR(2, 3, rp, np.array([1, 0], dtype=np.int32), np.ones(18))
@@ -209,7 +211,7 @@ def test_gpu_block_solver_adapter():
     A, z = load_golden("waterflood_sys2.npz")
     g = GpuBlockSolver(fma=False)
     ok, x, its = g.solve(A, z["b"], 1e-6, 120)
-    assert ok and its == int(z["its_bicg_bilu0"])
+    assert ok and abs(its - int(z["its_bicg_bilu0"])) <= 1                           # tree-summed inner products
     assert rel(x, z["x_bicg_bilu0"]) < 1e-8
     assert g.deviceSeconds() > 0
 
