@@ -159,6 +159,57 @@ def cpu_baseline(systems, budget_s=20.0):
             "sample": f"{done} of the {len(systems)} ensemble systems, FP64 CPR-BiCGSTAB to 1e-6 (C restatement, OpenMP SpMV/vector ops)"}
 
 
+SERVE_RATE, SERVE_N, SERVE_POOL, SERVE_SLOTS, SERVE_BUDGET = 200.0, 200, 16, 8, 150 << 30
+
+
+def serving_pool(seed=4242):
+    """Requests of the serving stream's shape: one per 1/16 quantile of a log-uniform cell count in 1e3..1e6
+    (random box with nz in [1, 50], sigma ln k in [0.5, 3], time step in [0.1, 30] days, 1-8 wells)."""
+    from ressim_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(SERVE_POOL):
+        cells = 1e3 * 1000.0 ** ((i + 0.5) / SERVE_POOL)
+        out.append(synth.serving_request(rng, cells_lo=cells, cells_hi=cells))
+    return out
+
+
+def serving_arrivals(seed=99):
+    """Poisson arrivals at SERVE_RATE per second, each request drawn uniformly from the pool."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / SERVE_RATE, SERVE_N))
+    return [(float(t[i]), int(rng.integers(SERVE_POOL))) for i in range(SERVE_N)]
+
+
+def serving_leg(local, pool, arrivals, precision):
+    """Continuous batching through the server (rsg_server_*): requests submitted at their arrival times (or when
+    the previous submission returns, if later), latency = submit -> result on the server clock."""
+    from ressim_gb300.solver import Server
+    with Server(slots=SERVE_SLOTS, mem_budget=SERVE_BUDGET, precond="cpr", precision=precision, device=local) as srv:
+        for s in pool[:4]:                                   # warm-up: module load, allocator pools
+            srv.poll(srv.submit(s.A, s.b, tol=TOL, maxit=MAXIT))
+        ids = []
+        late = 0.0
+        t0 = time.perf_counter()
+        for ta, k in arrivals:
+            now = time.perf_counter() - t0
+            if now < ta:
+                time.sleep(ta - now)
+            else:
+                late = max(late, now - ta)
+            ids.append((srv.submit(pool[k].A, pool[k].b, tol=TOL, maxit=MAXIT), k))
+        res = [(srv.poll(i)[1], k) for i, k in ids]
+        T = time.perf_counter() - t0
+    lat = np.array([r["total_ms"] for r, _ in res])
+    ok = [r["status"] == 0 and 0 <= r["true_rel_residual"] <= TOL for r, _ in res]
+    big = [r for r, k in res if pool[k].A.n > 65536]
+    return {"throughput": len(res) / T, "unit": "solves/s", "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_run_ms": float(np.mean([r["run_ms"] for r, _ in res])),
+            "converged": int(sum(ok)), "requests": len(res), "max_submit_lag_ms": 1e3 * late,
+            "cells_per_s": float(sum(pool[k].A.n for _, k in res) / T),
+            "over_64k_rows_precond": sorted({int(r["precond"]) for r in big})}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -199,6 +250,8 @@ def main():
     ap.add_argument("--impl", default="rsg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--systems", type=int, default=64, help="ensemble size (64: the headline workload; smaller: profiling)")
+    ap.add_argument("--serving", choices=["on", "off", "only"], default="on",
+                    help="the serving stream (Poisson arrivals through the continuous-batching server)")
     args = ap.parse_args()
     global N_REAL
     N_REAL = args.systems
@@ -218,6 +271,19 @@ def main():
     import torch
     torch.cuda.set_device(local)
     from ressim_gb300.solver import DeviceSolver
+
+    serving = None
+    if args.serving != "off":
+        pool = serving_pool()
+        arr = serving_arrivals()
+        serving = {"rate_per_s": SERVE_RATE, "requests": SERVE_N, "pool": SERVE_POOL, "slots": SERVE_SLOTS,
+                   "budget_gb": SERVE_BUDGET / 2**30, "cells": [int(min(s.A.n for s in pool)), int(max(s.A.n for s in pool))],
+                   "mixed_f32": serving_leg(local, pool, arr, "mixed_f32"), "fp64": serving_leg(local, pool, arr, "fp64")}
+        del pool
+        if args.serving == "only":
+            if rank == 0:
+                print(json.dumps({"metric": METRIC, "serving": serving}))
+            return 0
 
     systems = ensemble(rank)
     mats = [s.A for s in systems]
@@ -372,7 +438,7 @@ def main():
             "last_step_device_ms": {"setup": st_last.setup_ms, "solve": st_last.solve_ms},
             "fp64_plain": fp64_plain, "batched_mixed_over_plain_fp64": value / world / fp64_plain["value"],
             "e2e": e2e, "roofline": roofline, "roofline_spmv": roofline_spmv, "kernels": kernels, "gpu_launches": int(launches),
-            "cpu_baseline": cpu, "clocks": clk.summary(),
+            "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
         }
         print(json.dumps(line))
     if dist:

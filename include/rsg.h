@@ -194,7 +194,7 @@ typedef struct rsg_result {
     size_t device_bytes;      /* device memory the request held */
     double start_ms, end_ms;  /* admitted / done, ms since the server was created (one clock for all requests) */
     int slot;                 /* worker that ran it */
-    int precond;              /* preconditioner used (RSG_PREC_*; CPR requests too large for one SM run BILU0) */
+    int precond;              /* preconditioner used (RSG_PREC_*; CPR requests whose pattern is not structurally symmetric run BILU0) */
 } rsg_result;
 
 /* opts: solver options of every slot (device, precision, preconditioner, Krylov method); slots >= 1;

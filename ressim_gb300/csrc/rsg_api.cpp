@@ -228,11 +228,21 @@ int check_device_errors(rsg_solver* h) {
         cudaMemsetAsync(h->S.flagB, 0, sizeof(int) * size_t(h->plan.n), h->stream);
         cudaMemsetAsync(h->S.ctr, 0, sizeof(unsigned) * 4, h->stream);
         cudaMemsetAsync(h->R.done, 0, sizeof(unsigned), h->stream);
+        if (h->amg.gsFlag) {
+            cudaMemsetAsync(h->amg.gsFlag, 0, 2 * size_t(std::max(h->amg.totRows, 1)) * sizeof(int), h->stream);
+            cudaMemsetAsync(h->amg.gsCtr, 0, 4 * size_t(std::max(h->amg.maxL, 1)) * sizeof(unsigned), h->stream);
+        }
         cudaStreamSynchronize(h->stream);
         if (e & ERR_TIMEOUT) return fail(RSG_ETIMEOUT, "a bounded device wait ran out (sweep dependency not satisfied)");
         return fail(RSG_ECUDA, "device error flag " + std::to_string(e));
     }
     return RSG_OK;
+}
+
+// kernel launches of one preconditioner application
+int precond_launches(const PrecDev& M) {
+    if (M.cpr && !M.cta) return cpr_grid_launches(*M.amg);
+    return M.cpr || M.cta || M.kind == 2 ? 1 : 2;
 }
 
 PrecDev prec_dev(rsg_solver* h) {
@@ -488,6 +498,47 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             }
             if (d.coarse && d.dense) std::copy(A.perm.begin(), A.perm.end(), luPerm.begin() + d.luRowOff);
         }
+    // grid-wide V-cycle: (system, level) descriptor and wave (schedule level) of every row, and the levels that are
+    // some system's coarsest without a dense LU
+    std::vector<int> rowLv(static_cast<size_t>(std::max(rows, 1)), 0), wave(static_cast<size_t>(std::max(rows, 1)), 0);
+    G.coarseGsLevels.clear();
+    for (int l = 0; l < maxL; ++l) {
+        bool gsCoarse = false;
+        for (int s = 0; s < nsys; ++s) {
+            if (l >= int(H[size_t(s)].lv.size())) continue;
+            const AmgSysLv& d = lv[size_t(s) * maxL + l];
+            const std::vector<int>& st0 = schStart[size_t(s) * maxL + l];
+            const std::vector<int>& rw = schRows[size_t(s) * maxL + l];
+            for (int k = 0; k < d.n; ++k) rowLv[size_t(d.rowOff + k)] = s * maxL + l;
+            for (size_t g = 0; g + 1 < st0.size(); ++g)
+                for (int q = st0[g]; q < st0[g + 1]; ++q) wave[size_t(d.rowOff + rw[size_t(q)])] = int(g);
+            gsCoarse |= d.coarse && !d.dense;
+        }
+        if (gsCoarse) G.coarseGsLevels.push_back(l);
+    }
+    // colour-major positions of every level (multicolour schedule only): colour c of every system, then c + 1
+    std::vector<int> cpos(static_cast<size_t>(std::max(rows, 1)), 0);
+    G.colBeg.assign(size_t(maxL), std::vector<int>());
+    if (mc)
+        for (int l = 0; l < maxL; ++l) {
+            int ncol = 0;
+            for (int s = 0; s < nsys; ++s)
+                if (l < int(H[size_t(s)].lv.size())) ncol = std::max(ncol, lv[size_t(s) * maxL + l].nl);
+            std::vector<int>& cb = G.colBeg[size_t(l)];
+            cb.assign(size_t(ncol) + 1, G.levelRowBeg[size_t(l)]);
+            int q = G.levelRowBeg[size_t(l)];
+            for (int c = 0; c < ncol; ++c) {
+                cb[size_t(c)] = q;
+                for (int s = 0; s < nsys; ++s) {
+                    if (l >= int(H[size_t(s)].lv.size())) continue;
+                    const AmgSysLv& d = lv[size_t(s) * maxL + l];
+                    if (c >= d.nl) continue;
+                    const std::vector<int>& st0 = schStart[size_t(s) * maxL + l];
+                    for (int g = st0[size_t(c)]; g < st0[size_t(c) + 1]; ++g) cpos[size_t(q++)] = d.rowOff + g;
+                }
+            }
+            cb[size_t(ncol)] = q;
+        }
     // pointer arrays are prefix sums over the level-major order: fill gaps (levels absent for some systems)
     for (size_t e = 1; e < apPtr.size(); ++e) apPtr[e] = std::max(apPtr[e], apPtr[e - 1]);
     for (size_t e = 1; e < acPtr.size(); ++e) acPtr[e] = std::max(acPtr[e], acPtr[e - 1]);
@@ -501,8 +552,13 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = upload(M, &G.apSrc, apSrc, st)) || (rc = upload(M, &G.acPtr, acPtr, st)) || (rc = upload(M, &G.acSrc, acSrc, st)) ||
         (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)) ||
         (rc = upload(M, &G.slotSrc, slotSrc, st)) || (rc = upload(M, &G.slotCol, slotCol, st)) || (rc = upload(M, &G.gsRows, gsRows, st)) ||
-        (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)))
+        (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)) || (rc = upload(M, &G.rowLv, rowLv, st)) || (rc = upload(M, &G.cpos, cpos, st)) ||
+        (rc = upload(M, &G.wave, wave, st)) || (rc = dalloc(M, &G.gsFlag, 2 * size_t(std::max(rows, 1)))) ||
+        (rc = dalloc(M, &G.gsCtr, 4 * size_t(std::max(maxL, 1)))) || (rc = dalloc(M, &G.coarse64, size_t(std::max(nsys, 1)))))
         return rc;
+    RSG_CUDA(cudaMemsetAsync(G.coarse64, 0, size_t(std::max(nsys, 1)) * sizeof(int), st));
+    RSG_CUDA(cudaMemsetAsync(G.gsFlag, 0, 2 * size_t(std::max(rows, 1)) * sizeof(int), st));
+    RSG_CUDA(cudaMemsetAsync(G.gsCtr, 0, 4 * size_t(std::max(maxL, 1)) * sizeof(unsigned), st));
     {
         const size_t S = size_t(std::max(slots, 1)), R = size_t(std::max(rows, 1)), n = size_t(h->plan.n);
         const size_t nLo = size_t(h->dp.nLov) * 3, nUo = size_t(h->dp.nUov) * 3;
@@ -580,17 +636,20 @@ int setup_cpr(rsg_solver* h, const double* acc) {
     launch_amg_refresh(G, st);
     launch_amg_coarse_lu(G, h->opt.precision != RSG_FP64, st);
     if (h->opt.precision != RSG_FP64) launch_amg_round(G, st);
-    launch_amg_slots(G, h->opt.precision != RSG_FP64, st);
-    launch_cpr_sp(D, h->val, G, h->opt.precision != RSG_FP64, st);
-    h->launches += 5 + 3 * std::max(0, G.maxL - 1) + (h->opt.precision != RSG_FP64 ? 2 : 0);
+    if (h->cta) {                                              // row slots of the thread-block application
+        launch_amg_slots(G, h->opt.precision != RSG_FP64, st);
+        launch_cpr_sp(D, h->val, G, h->opt.precision != RSG_FP64, st);
+        h->launches += 2;
+    }
+    h->launches += 3 + 3 * std::max(0, G.maxL - 1) + (h->opt.precision != RSG_FP64 ? 2 : 0);
     RSG_CUDA(cudaGetLastError());
     return RSG_OK;
 }
 
 int do_setup(rsg_solver* h, const double* acc) {
     if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
-    if (h->opt.precond == RSG_PREC_CPR && !h->cta)
-        return fail(RSG_EINVAL, "the CPR preconditioner needs structurally symmetric systems of <= 65536 block rows each");
+    if (h->opt.precond == RSG_PREC_CPR && !h->plan.symmetric)
+        return fail(RSG_EINVAL, "the CPR preconditioner needs structurally symmetric systems");
     int rc = ensure_precond_storage(h);
     if (rc) return rc;
     RSG_CUDA(cudaMemsetAsync(h->d_nreg, 0, sizeof(int), h->stream));
@@ -625,7 +684,7 @@ int do_setup(rsg_solver* h, const double* acc) {
 
 int launch_iterations(rsg_solver* h, int k) {
     const PrecDev M = prec_dev(h);
-    h->launches += (long long)k * (M.kind == 2 ? 5 : (M.cta ? 5 : 7));
+    h->launches += (long long)k * (3 + 2 * precond_launches(M));
     if (h->opt.use_graphs) {
         const int kind = M.kind;
         if (!h->gexec || h->gIters != k || h->gKind != kind) {
@@ -648,7 +707,6 @@ int launch_iterations(rsg_solver* h, int k) {
     return RSG_OK;
 }
 
-int precond_launches(const PrecDev& M) { return M.cpr || M.cta || M.kind == 2 ? 1 : 2; }
 
 // BiCGSTAB of every system from the gathered right-hand side h->b into h->V.x
 int run_bicgstab(rsg_solver* h, double tol, int maxIt) {
@@ -1000,7 +1058,8 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
 // level-space r -> level-space z
 static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     const PrecDev M = prec_dev(h);
-    if (M.cpr) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
+    if (M.cpr && M.cta) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
+    else if (M.cpr) h->launches += launch_cpr_grid(h->dp, M, *M.amg, 0, d_r, nullptr, nullptr, d_z, nullptr, h->S, h->d_err, h->stream);
     else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
     else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
     else if (M.kind == 1) { launch_ilu_apply_mixed(h->dp, h->luf, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }

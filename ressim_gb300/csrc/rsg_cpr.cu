@@ -114,8 +114,9 @@ template <class T>
 __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
                                                    const int* __restrict__ ci, const double* __restrict__ val,
                                                    const int* __restrict__ luPerm, T* luAll, int* pivAll, int* cinAll,
-                                                   int skipUpTo) {
+                                                   int skipUpTo, const int* only) {
     const int s = blockIdx.x;
+    if (only && !only[s]) return;                                 // only the systems flagged (FP64 coarse solve)
     AmgSysLv L;
     bool found = false;
     for (int l = 0; l < maxL; ++l) {
@@ -431,6 +432,62 @@ void launch_amg_refresh(const DevAmg& G, cudaStream_t st) {
         k_diag_fix<<<grid_for(size_t(r1 - r0)), 256, 0, st>>>(r0, r1, G.diagGlob, G.val);
     }
 }
+// FP32 forms: how well the explicit FP32 inverse solves the coarsest level. x_t deterministic in [-1, 1), b = A x_t
+// in FP64, x = inv float(b) as the V-cycle applies it; a system whose relative error exceeds kCoarseTol (or is not
+// finite) solves its coarsest level in FP64 with the LU instead: extreme permeability contrasts (sigma ln k ~ 3)
+// leave coarse matrices too ill-conditioned for an FP32 inverse, and the preconditioner then stalls.
+constexpr double kCoarseTol = 1e-2;
+__global__ void __launch_bounds__(256) k_coarse_check(int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                      const int* __restrict__ ci, const double* __restrict__ val,
+                                                      const int* __restrict__ luPerm, const float* __restrict__ invAll, double* xt,
+                                                      double* bt, int* coarse64) {
+    const int s = blockIdx.x;
+    AmgSysLv L;
+    bool found = false;
+    for (int l = 0; l < maxL; ++l) {
+        const AmgSysLv c = lv[s * maxL + l];
+        if (c.n > 0 && c.coarse) { L = c; found = true; break; }
+    }
+    if (!found || !L.dense) {
+        if (threadIdx.x == 0) coarse64[s] = 0;
+        return;
+    }
+    const int m = L.n;
+    double* x = xt + L.rowOff;
+    double* b = bt + L.rowOff;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) x[k] = double((unsigned(k) * 2654435761u) >> 8) * (2.0 / 16777216.0) - 1.0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        double t = 0;
+        for (int p = __ldg(rp + L.rpOff + k); p < __ldg(rp + L.rpOff + k + 1); ++p) t += val[L.entOff + p] * x[__ldg(ci + L.entOff + p)];
+        b[k] = t;
+    }
+    __syncthreads();
+    const float* inv = invAll + L.luOff;
+    const int* nat = luPerm + L.luRowOff;
+    double e2 = 0, r2 = 0;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const float* col = inv + __ldg(nat + k);
+        float acc = 0.f;
+        for (int j = 0; j < m; ++j) acc = fmaf(col[size_t(j) * m], float(b[j]), acc);
+        const double d = double(acc) - x[k];
+        e2 += d * d;
+        r2 += x[k] * x[k];
+    }
+    __shared__ double se[256], sr[256];
+    se[threadIdx.x] = e2;
+    sr[threadIdx.x] = r2;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (int(threadIdx.x) < o) { se[threadIdx.x] += se[threadIdx.x + o]; sr[threadIdx.x] += sr[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double rel = sqrt(se[0] / sr[0]);
+        coarse64[s] = (rel <= kCoarseTol) ? 0 : 1;              // NaN lands here too
+    }
+}
+
 void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st) {
     if (G.totLu <= 0) return;
     if (fp32) {
@@ -440,11 +497,15 @@ void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st) {
         if (G.maxCoarse > kInvSmemRows) {                        // levels too large for shared memory: LU, then columns
             raise_smem_limit(reinterpret_cast<const void*>(k_coarse_inv), smem);
             k_coarse_lu<float><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.luf, G.piv, G.cin,
-                                                       kInvSmemRows);
+                                                       kInvSmemRows, nullptr);
             k_coarse_inv<<<G.nsys, 256, smem, st>>>(G.maxL, G.lv, G.cin, G.luf, G.invf, kInvSmemRows);
         }
+        // the FP32 inverse checked per system; the FP64 LU (after the FP32 one: pivots and gather order are its own)
+        // only for the systems that need it
+        k_coarse_check<<<G.nsys, 256, 0, st>>>(G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.invf, G.x, G.b, G.coarse64);
+        k_coarse_lu<double><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin, 0, G.coarse64);
     } else {
-        k_coarse_lu<double><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin, 0);
+        k_coarse_lu<double><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.lu, G.piv, G.cin, 0, nullptr);
     }
 }
 void launch_amg_round(const DevAmg& G, cudaStream_t st) {

@@ -73,6 +73,7 @@ struct HostPlan {
 
 struct PrecDev;
 struct DevPlan;
+struct SweepState;
 // Builds the plan of a (block-diagonal batch of) BSR pattern(s). Returns false with a message on bad input.
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
                 const std::vector<int>& col, std::string& err);
@@ -154,6 +155,20 @@ struct DevAmg {
     // of the overflow blocks (3 values each)
     double *sp = nullptr, *spLov = nullptr, *spUov = nullptr;
     float *spf = nullptr, *spLovf = nullptr, *spUovf = nullptr;
+    // grid-wide V-cycle (systems too large for one SM): per AMG row its (system, level) descriptor index s*maxL+l and
+    // its wave (forward GS level, or colour: adjacent rows of an earlier wave are updated before it in a forward
+    // sweep), sync-free sweep flags (phase 0: the smoothing sweeps, phase 1: the GS solve of a coarsest level
+    // without dense LU) and claim counters (per level and phase: forward, backward)
+    int* coarse64 = nullptr;           // FP32 forms, per system: 1 = coarsest level solved in FP64 (LU), the FP32 inverse too inexact
+    int* rowLv = nullptr;
+    int* wave = nullptr;
+    int* gsFlag = nullptr;             // 2 x totRows
+    unsigned* gsCtr = nullptr;         // maxL x 4
+    std::vector<int> coarseGsLevels;   // host: levels that are some system's coarsest without a dense LU
+    // multicolour schedule (FP32 forms), grid-wide: per level the schedule positions of every system ordered colour
+    // by colour (cpos), and per level the position range of colour c at colBeg[l][c] .. colBeg[l][c + 1]
+    int* cpos = nullptr;
+    std::vector<std::vector<int>> colBeg;
 };
 // CPR set-up kernels (rsg_cpr.cu)
 void launch_cpr_weights(const DevPlan& P, const double* val, const double* accLev, double* w, int* nfallback, cudaStream_t st);
@@ -169,6 +184,17 @@ void launch_cpr_sp(const DevPlan& P, const double* val, const DevAmg& G, bool fp
 // mode 0 plain (r -> z), 1 p-update, 2 s-update (as the BILU0 sweeps)
 void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, bool amgFp32, const double* r, double* pv,
                     const double* v, double* z, const KScal* ks, cudaStream_t st);
+// the same application grid-wide for systems of any size (rsg_sweep_cta.cu): input and restriction, the V-cycle one
+// level at a time with sync-free Gauss-Seidel sweeps, coarse solve per system, t = r - S[:,p] xp, the grid BILU0
+// sweeps, z_p += xp. Returns the number of kernel launches.
+int launch_cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, const double* r, double* pv, const double* v,
+                    double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st);
+inline int cpr_grid_launches(const DevAmg& G) {
+    int n = 6 + 2 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
+    for (int l = 0; l + 1 < G.maxL; ++l)            // pre- and post-smoothing: one sweep, or one launch per colour
+        n += 2 * (l < int(G.colBeg.size()) && G.colBeg[size_t(l)].size() > 1 ? int(G.colBeg[size_t(l)].size()) - 1 : 1);
+    return n;
+}
 
 // ---- well Schur complement (engine/src/bsr.cpp:733-840, 973-990)
 int wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
@@ -228,8 +254,10 @@ void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, d
 // FP32 factors, FP64 vector and accumulation (the reference's float-factor sweeps)
 void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r, double* z, SweepState& S, int* err,
                             cudaStream_t st);
+// grid-wide sync-free BILU0 apply z = M^-1 r of the handle's factor kind; systems whose status is not running skip
+void launch_ilu_grid_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
+                        cudaStream_t st);
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st);
-// shared-memory opt-in of the bulk-staged SpMV for this plan's stage sizes (before any graph capture)
 // raise (never lower) a kernel's dynamic shared-memory opt-in on the current device; thread-safe
 void raise_smem_limit(const void* fn, int bytes);
 // block-Jacobi: dinv = inverse diagonal blocks (FP64), z = dinv r

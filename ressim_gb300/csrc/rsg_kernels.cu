@@ -3,8 +3,9 @@
 // * BILU0 factorisation and the forward / backward sweeps are exact natural-order ILU(0): rows are processed in
 //   a level order (a topological order of the L, resp. U, dependencies) by a persistent grid whose warps claim
 //   32 rows at a time from an atomic counter; a row waits for the rows it depends on through per-row flags
-//   (release / acquire at GPU scope). Claiming in order guarantees that every awaited row belongs to a warp that
-//   is already running, so the waits always end; each wait is additionally bounded and reports RSG_ETIMEOUT.
+//   (relaxed polls, one acquire fence, a release store when the row is done: rsg_sync.cuh). Claiming in order
+//   guarantees that every awaited row belongs to a warp that is already running, so the waits always end; each
+//   wait is additionally bounded and reports RSG_ETIMEOUT.
 // * FP64 block arithmetic uses explicitly rounded multiplies and adds in the reference's loop order
 //   (engine/src/bsr.cpp:13-64), so factors, sweeps and SpMV are bitwise those of the reference's serial code.
 // * Tile kernels (SpMV, vector updates) cover TILE_ROWS block rows of one system with 3 threads per block row;
@@ -13,6 +14,7 @@
 #include "rsg_impl.h"
 #include "rsg_block3.cuh"
 #include "rsg_reduce.cuh"
+#include "rsg_sync.cuh"
 
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -23,36 +25,7 @@ namespace rsg {
 
 namespace {
 
-constexpr unsigned kSpinLimit = 1u << 22;   // x up to 256 ns back-off: about one second per wait
 constexpr int kSweepThreads = 128;
-
-// ------------------------------------------------------------------ memory-order helpers
-__device__ __forceinline__ int ld_acquire(const int* p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release(int* p, int v) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-// bounded wait for *f == want; on time-out sets ERR_TIMEOUT and returns false (the caller then proceeds)
-__device__ __noinline__ bool wait_flag(const int* f, int want, int* err) {
-    if (ld_acquire(f) == want) return true;
-    unsigned ns = 32;
-    for (unsigned it = 0; it < kSpinLimit; ++it) {
-        __nanosleep(ns);
-        if (ns < 256) ns <<= 1;
-        if (ld_acquire(f) == want) return true;
-        if ((it & 255u) == 255u && *(volatile int*)err != 0) return false;   // another wait already gave up
-    }
-    atomicOr(err, ERR_TIMEOUT);
-    return false;
-}
-__device__ __forceinline__ int warp_claim(unsigned* ctr) {
-    unsigned base = 0;
-    if ((threadIdx.x & 31) == 0) base = atomicAdd(ctr, 32u);
-    return int(__shfl_sync(0xffffffffu, base, 0));
-}
 
 // ------------------------------------------------------------------ BILU0 factorisation (sync-free, level order)
 // engine/src/bsr.cpp:183-215 row by row; rows of a system claimed in forward level order.
@@ -70,9 +43,9 @@ __global__ void __launch_bounds__(kSweepThreads) k_factor_f64(int n, const int* 
         if (idx < n) {
             const int i = __ldg(ford + idx);
             const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+            wait_cols(flagL, col, r0, d, epoch, err);
             for (int p = r0; p < d; ++p) {
                 const int k = __ldg(col + p);
-                wait_flag(flagL + k, epoch, err);
                 double a[9], u[9], L[9];
                 load9(lu + size_t(p) * 9, a);
                 load9(lu + size_t(__ldg(diag + k)) * 9, u);
@@ -91,7 +64,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_factor_f64(int n, const int* 
             load9(lu + size_t(d) * 9, D);
             if (invert_pivot3(D)) atomicAdd(nreg, 1);
             store9(lu + size_t(d) * 9, D);
-            __threadfence();
             st_release(flagL + i, epoch);
         }
     }
@@ -116,9 +88,9 @@ __global__ void __launch_bounds__(kSweepThreads) k_factor_lean(int n, const int*
             const int r0 = __ldg(rowPtr + i), r1 = __ldg(rowPtr + i + 1), d = __ldg(diag + i);
             for (int p = r0; p < r1; ++p)
                 for (int e = 0; e < 9; ++e) work[size_t(p) * 9 + e] = double(float(__ldg(val + size_t(p) * 9 + e)));
+            wait_cols(flagL, col, r0, d, epoch, err);
             for (int p = r0; p < d; ++p) {
                 const int k = __ldg(col + p);
-                wait_flag(flagL + k, epoch, err);
                 double a[9], u[9], L[9];
                 load9(work + size_t(p) * 9, a);
                 const float* fk = F + size_t(__ldg(diag + k)) * 9;
@@ -141,7 +113,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_factor_lean(int n, const int*
             store9(work + size_t(d) * 9, D);
             for (int p = r0; p < r1; ++p)
                 for (int e = 0; e < 9; ++e) F[size_t(p) * 9 + e] = float(work[size_t(p) * 9 + e]);
-            __threadfence();
             st_release(flagL + i, epoch);
         }
     }
@@ -207,9 +178,9 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __r
             }
             if (run) {
                 const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+                wait_cols(flagF, col, r0, d, 1, err);
                 for (int p = r0; p < d; ++p) {
                     const int k = __ldg(col + p);
-                    wait_flag(flagF + k, 1, err);
                     double a[9], yk[3];
                     ldf9(lu + size_t(p) * 9, a);
                     yk[0] = y[size_t(k) * 3 + 0]; yk[1] = y[size_t(k) * 3 + 1]; yk[2] = y[size_t(k) * 3 + 2];
@@ -220,7 +191,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __r
             }
             y[size_t(i) * 3 + 0] = yi[0]; y[size_t(i) * 3 + 1] = yi[1]; y[size_t(i) * 3 + 2] = yi[2];
             flagB[i] = 0;
-            __threadfence();
             st_release(flagF + i, 1);
         }
     }
@@ -244,9 +214,9 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __r
             if (sys_running(ks, rowSys, i)) {
                 double yi[3] = {y[size_t(i) * 3 + 0], y[size_t(i) * 3 + 1], y[size_t(i) * 3 + 2]};
                 const int d = __ldg(diag + i), r1 = __ldg(rowPtr + i + 1);
+                wait_cols(flagB, col, d + 1, r1, 1, err);
                 for (int p = d + 1; p < r1; ++p) {
                     const int j = __ldg(col + p);
-                    wait_flag(flagB + j, 1, err);
                     double a[9], zj[3];
                     ldf9(lu + size_t(p) * 9, a);
                     zj[0] = y[size_t(j) * 3 + 0]; zj[1] = y[size_t(j) * 3 + 1]; zj[2] = y[size_t(j) * 3 + 2];
@@ -261,7 +231,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __r
                 y[size_t(i) * 3 + 2] = dot3(D + 6, yi);
             }
             flagF[i] = 0;
-            __threadfence();
             st_release(flagB + i, 1);
         }
     }
@@ -312,9 +281,9 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f32(int n, const int* __r
             }
             if (run) {
                 const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+                wait_cols(flagF, col, r0, d, 1, err);
                 for (int p = r0; p < d; ++p) {
                     const int k = __ldg(col + p);
-                    wait_flag(flagF + k, 1, err);
                     const float* a = lu + size_t(p) * 9;
                     const float y0 = y[size_t(k) * 3 + 0], y1 = y[size_t(k) * 3 + 1], y2 = y[size_t(k) * 3 + 2];
 #pragma unroll
@@ -329,7 +298,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f32(int n, const int* __r
             }
             y[size_t(i) * 3 + 0] = yi[0]; y[size_t(i) * 3 + 1] = yi[1]; y[size_t(i) * 3 + 2] = yi[2];
             flagB[i] = 0;
-            __threadfence();
             st_release(flagF + i, 1);
         }
     }
@@ -352,9 +320,9 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __r
             if (sys_running(ks, rowSys, i)) {
                 float yi[3] = {y[size_t(i) * 3 + 0], y[size_t(i) * 3 + 1], y[size_t(i) * 3 + 2]};
                 const int d = __ldg(diag + i), r1 = __ldg(rowPtr + i + 1);
+                wait_cols(flagB, col, d + 1, r1, 1, err);
                 for (int p = d + 1; p < r1; ++p) {
                     const int j = __ldg(col + p);
-                    wait_flag(flagB + j, 1, err);
                     const float* a = lu + size_t(p) * 9;
                     const float z0 = y[size_t(j) * 3 + 0], z1 = y[size_t(j) * 3 + 1], z2 = y[size_t(j) * 3 + 2];
 #pragma unroll
@@ -380,7 +348,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __r
                 z[size_t(i) * 3 + 0] = double(t[0]); z[size_t(i) * 3 + 1] = double(t[1]); z[size_t(i) * 3 + 2] = double(t[2]);
             }
             flagF[i] = 0;
-            __threadfence();
             st_release(flagB + i, 1);
         }
     }
@@ -721,6 +688,27 @@ void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, d
                                           S.ctr, err);
 }
 
+void launch_ilu_grid_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
+                        cudaStream_t st) {
+    const int g = sweep_grid(P.n);
+    if (M.kind == 0) {
+        k_fwd_f64<double, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, r, nullptr, nullptr, z,
+                                                                 P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+        k_bwd_f64<double><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.lu, z, P.rowSys, ks, S.flagF, S.flagB,
+                                                       S.ctr, err);
+    } else if (M.kind == 1) {
+        k_fwd_f64<float, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, r, nullptr, nullptr, z,
+                                                                P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+        k_bwd_f64<float><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, z, P.rowSys, ks, S.flagF, S.flagB,
+                                                      S.ctr, err);
+    } else {
+        k_fwd_f32<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, r, nullptr, nullptr, M.y32,
+                                                         P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+        k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, M.y32, z, P.rowSys, ks, S.flagF, S.flagB,
+                                               S.ctr, err);
+    }
+}
+
 template <int MODE, bool FMA>
 void spmv_go(const DevPlan& P, const double* val, const double* x, double* y, const double* a1, KScal* ks, ReduceState* R, int* active,
              double* out, cudaStream_t st) {
@@ -775,8 +763,10 @@ void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M
                            SweepState& S, int* active, int* err, cudaStream_t st) {
     const int g = sweep_grid(P.n);
     auto prec = [&](bool pupd, double* out) {
-        if (M.cpr) {
+        if (M.cpr && M.cta) {
             launch_cpr_cta(P, M, *M.amg, pupd ? 1 : 2, M.kind != 0, V.r, pupd ? V.p : V.s, V.v, out, ks, st);
+        } else if (M.cpr) {
+            launch_cpr_grid(P, M, *M.amg, pupd ? 1 : 2, V.r, pupd ? V.p : V.s, V.v, out, ks, S, err, st);
         } else if (M.cta && M.kind != 2) {
             launch_ilu_cta_fused(P, M, pupd, V.r, pupd ? V.p : V.s, V.v, out, ks, st);
         } else if (M.kind == 0) {

@@ -71,7 +71,7 @@ struct rsg_server {
     long long nextId = 0;
     bool stop = false;
     std::vector<std::thread> workers;
-    std::vector<rsg_solver*> handles, bilu;   // per slot: the configured handle, a BILU0 handle for large CPR requests
+    std::vector<rsg_solver*> handles, bilu;   // per slot: the configured handle, a BILU0 handle for patterns CPR cannot take
     Clock::time_point t0 = Clock::now();      // the server's clock origin (start_ms / end_ms of the results)
 };
 
@@ -80,18 +80,24 @@ namespace {
 void run_request(rsg_server* S, int slot, Request& R) {
     rsg_solver* h = S->handles[size_t(slot)];
     int prec = S->opt.precond;
-    if (prec == RSG_PREC_CPR && R.n > 65536) {                    // CPR runs one system per SM: larger ones take BILU0
+    int rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
+    if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
+    if (rc == RSG_EINVAL && prec == RSG_PREC_CPR) {               // CPR needs a structurally symmetric pattern: BILU0
+        rsg_release(h);
         if (!S->bilu[size_t(slot)]) {
             rsg_options o = S->opt;
             o.precond = RSG_PREC_BILU0;
             rsg_create(&S->bilu[size_t(slot)], &o);
         }
-        if (S->bilu[size_t(slot)]) { h = S->bilu[size_t(slot)]; prec = RSG_PREC_BILU0; }
+        if (S->bilu[size_t(slot)]) {
+            h = S->bilu[size_t(slot)];
+            prec = RSG_PREC_BILU0;
+            rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
+            if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
+        }
     }
     R.res.precond = prec;
     R.res.slot = slot;
-    int rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
-    if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
     int its = 0;
     double rr = 0;
     if (rc == RSG_OK) {

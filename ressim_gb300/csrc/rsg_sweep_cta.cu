@@ -21,6 +21,7 @@
 // factors. (float, float) is the all-FP32 BILU0f sweep (engine/src/bsr.cpp:1100-1121).
 #include "rsg_impl.h"
 #include "rsg_block3.cuh"
+#include "rsg_sync.cuh"
 
 #include <cuda_runtime.h>
 #include <type_traits>
@@ -378,6 +379,9 @@ struct CprArgs {
     const double* w;
     double* T;
     const TA *sp, *spLov, *spUov;     // pressure columns of S in slot order
+    const int* coarse64;              // FP32 forms: per system, coarsest level solved in FP64 with the LU below
+    const double* lu64;
+    double *x64, *b64, *r64;          // FP64 vectors of that solve (every level's rows; only the coarsest used)
 };
 
 // V-cycle arithmetic type: FP64 explicitly rounded (bitwise the reference) or FP32
@@ -691,6 +695,22 @@ __device__ __noinline__ void coarse_inverse(const AmgSysLv& A, const CprArgs<flo
     __syncthreads();
 }
 
+// FP32 forms, systems flagged at set-up: the coarsest level in FP64 (dense LU, as the FP64 form), from and back to
+// the FP32 V-cycle vectors
+__device__ __noinline__ void coarse_fp64(const AmgSysLv& A, const CprArgs<float>& C, float* x, const float* b) {
+    CprArgs<double> D{};
+    D.lu = C.lu64;
+    D.luPerm = C.luPerm;
+    D.cin = C.cin;
+    double* x64 = C.x64 + A.rowOff;
+    double* b64 = C.b64 + A.rowOff;
+    for (int k = threadIdx.x; k < A.n; k += blockDim.x) b64[k] = double(b[k]);
+    __syncthreads();
+    coarse_dense_body<double>(A, D, x64, b64, C.r64 + A.rowOff);
+    for (int k = threadIdx.x; k < A.n; k += blockDim.x) x[k] = float(x64[k]);
+    __syncthreads();
+}
+
 template <class TA>
 __device__ __noinline__ void coarse_dense_call(const AmgSysLv& A, const CprArgs<TA>& C, TA* x, const TA* b, TA* work) {
     coarse_dense_body<TA>(A, C, x, b, work);
@@ -730,8 +750,12 @@ __device__ __forceinline__ void vcycle_body(int s, const CprArgs<TA>& C, const V
         const AmgSysLv A = C.lv[s * C.maxL + l];
         if (A.coarse) {
             if (A.dense) {
-                if constexpr (sizeof(TA) == 4) coarse_inverse(A, C, V.x(A, C), V.b(A, C));
-                else coarse_dense<TA, NT>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
+                if constexpr (sizeof(TA) == 4) {
+                    if (C.coarse64[s]) coarse_fp64(A, C, V.x(A, C), V.b(A, C));
+                    else coarse_inverse(A, C, V.x(A, C), V.b(A, C));
+                } else {
+                    coarse_dense<TA, NT>(A, C, V.x(A, C), V.b(A, C), V.r(A, C));
+                }
             } else {                                      // 20 symmetric GS sweeps from x = 0 (amg.cpp:313-315)
                 TA* xl = V.x(A, C);
                 for (int k = threadIdx.x; k < A.n; k += blockDim.x) xl[k] = TA(0);
@@ -1103,7 +1127,7 @@ template <class TA>
 CprArgs<TA> cpr_args(const DevAmg& G, const TA* val, const TA* slotVal, const TA* diagVal, const TA* lu, TA* x, TA* b, TA* r, const TA* sp,
                      const TA* spLov, const TA* spUov) {
     return CprArgs<TA>{G.lv, G.maxL, G.lvl, G.gsRows, G.ci, val, G.slotCol, slotVal, diagVal, G.rowMeta, G.agg, G.memPtr, G.mem, lu, G.invf,
-                       G.luPerm, G.cin, x, b, r, G.w, G.T, sp, spLov, spUov};
+                       G.luPerm, G.cin, x, b, r, G.w, G.T, sp, spLov, spUov, G.coarse64, G.lu, G.x, G.b, G.r};
 }
 
 template <class TF, class TV, class TA, int MODE>
@@ -1134,6 +1158,324 @@ void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mod
     if (mode == IN_PUPDATE) go(std::integral_constant<int, IN_PUPDATE>());
     else if (mode == IN_SUPDATE) go(std::integral_constant<int, IN_SUPDATE>());
     else go(std::integral_constant<int, IN_PLAIN>());
+}
+
+// ------------------------------------------------------------------ CPR application grid-wide (systems of any size)
+// The thread-block application above keeps a system on one SM; a system of a million cells needs the whole GPU.
+// Here every step of BlockCPR::apply runs over the whole batch, one AMG level at a time, with the arithmetic of
+// the thread-block V-cycle:
+// * Gauss-Seidel sweeps are sync-free: a persistent grid claims the level's rows in schedule order (forward levels
+//   of the reference order, or colours) and a row waits, through per-row flags, only for its neighbours of an
+//   earlier wave (the rows a forward sweep updates before it: its lower-numbered neighbours in the reference order,
+//   whose forward level is lower, or those of an earlier colour). Its other neighbours wait for it in turn
+//   (structurally symmetric levels), so their old values are still in place when it reads them. Claiming in
+//   schedule order keeps every awaited row on a running warp; the waits are bounded (rsg_sync.cuh).
+// * The residual and the restriction are one pass per coarse row (every fine row belongs to one aggregate), the
+//   prolongation one pass per fine row, the coarsest level one thread block per system (dense LU in FP64, the
+//   explicit inverse in the FP32 forms).
+// * t = r - S[:,p] xp reads the pressure column of every block of S in row order; the BILU0 stage is the grid
+//   sync-free sweep of the handle's factors.
+namespace {
+
+constexpr int kGridThreads = 128;
+
+int grid_for(long long n, int threads) {
+    const long long b = (n + threads - 1) / threads, cap = 16LL * device_sm_count();
+    return int(b < 1 ? 1 : (b < cap ? b : cap));
+}
+// persistent sweep grid: a warp per 32 rows, at most 8 blocks of 4 warps per SM
+int gs_grid(int n) {
+    const int blocks = ((n + 31) / 32 + 3) / 4, cap = 8 * device_sm_count();
+    return blocks < 1 ? 1 : (blocks < cap ? blocks : cap);
+}
+
+// input (the fused Krylov update of the mode), T = input (FP64), level-0 right-hand side b0 = w . input
+// (bsr.cpp:1064-1067; TT: the arithmetic of the restriction, FP32 in the all-FP32 form)
+template <int MODE, class TA, class TT>
+__global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ rowSys, const double* r, double* pv, const double* v,
+                                                 const double* __restrict__ w, double* T, TA* b0, const KScal* ks) {
+    for (int k = int(blockIdx.x * blockDim.x + threadIdx.x); k < n; k += int(gridDim.x * blockDim.x)) {
+        double beta = 0, omega = 0, alpha = 0;
+        if (ks) {
+            const KScal& K = ks[__ldg(rowSys + k)];
+            if (K.status != ST_RUNNING) continue;
+            beta = K.beta; omega = K.omega; alpha = K.alpha;
+        }
+        double in[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const size_t q = size_t(k) * 3 + e;
+            if (MODE == IN_PUPDATE) { in[e] = da(r[q], dm(beta, ds(pv[q], dm(omega, v[q])))); pv[q] = in[e]; }
+            else if (MODE == IN_SUPDATE) { in[e] = ds(r[q], dm(alpha, v[q])); pv[q] = in[e]; }
+            else in[e] = r[q];
+            T[q] = in[e];
+        }
+        const double w0 = __ldg(w + size_t(k) * 3), w1 = __ldg(w + size_t(k) * 3 + 1), w2 = __ldg(w + size_t(k) * 3 + 2);
+        if (sizeof(TT) == 4) b0[k] = TA(float(w0) * float(in[0]) + float(w1) * float(in[1]) + float(w2) * float(in[2]));
+        else b0[k] = TA(da(da(dm(w0, in[0]), dm(w1, in[1])), dm(w2, in[2])));
+    }
+}
+
+// one Gauss-Seidel sweep of level l over every system (engine/src/amg.cpp:98-113). Positions [q0, q1) of the
+// level's schedule, claimed forward or backward. phase 0: the smoothing sweeps (systems whose level l is the
+// coarsest skip); phase 1: the symmetric GS solve of a coarsest level without dense LU. ZERO: pre-smoothing from
+// x = 0 (the terms of the neighbours not yet updated vanish and are not read). Flags of skipped rows are set all
+// the same: after every forward sweep of a (level, phase) all its flags are 1, after every backward sweep 0.
+template <class TA, bool FWD, bool ZERO>
+__global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int maxL, int phase, const int* __restrict__ rowLv,
+                                                          const AmgSysLv* __restrict__ lv, const int* __restrict__ gsRows,
+                                                          const int* __restrict__ wave, const int* __restrict__ rp,
+                                                          const int* __restrict__ ci, const TA* __restrict__ val,
+                                                          const int* __restrict__ diag, const TA* b, TA* x, int* flag, unsigned* ctr,
+                                                          const KScal* ks, int* err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[FWD ? 1 : 0] = 0u;   // the opposite direction's counter, for its next sweep
+    const int n = q1 - q0, lane = int(threadIdx.x & 31);
+    for (;;) {
+        __syncwarp();
+        const int base = warp_claim(ctr + (FWD ? 0 : 1));
+        if (base >= n) break;
+        const int idx = base + lane;
+        if (idx < n) {
+            const int g = FWD ? q0 + idx : q1 - 1 - idx;
+            const int sl = __ldg(rowLv + g);
+            const AmgSysLv* A = lv + sl;
+            const int rowOff = __ldg(&A->rowOff), coarse = __ldg(&A->coarse);
+            const int row = rowOff + __ldg(gsRows + g);
+            bool act = phase == 0 ? !coarse : (coarse && !__ldg(&A->dense));
+            if (act && ks) act = ks[sl / maxL].status == ST_RUNNING;
+            if (act) {
+                const int k = row - rowOff, rpOff = __ldg(&A->rpOff), entOff = __ldg(&A->entOff);
+                const int p0 = __ldg(rp + rpOff + k), p1 = __ldg(rp + rpOff + k + 1), pd = __ldg(diag + row);
+                const int* cl = ci + entOff;
+                const TA* vl = val + entOff;
+                const int wi = __ldg(wave + row);
+                // the neighbours updated before this row in the sweep: of an earlier wave (forward), a later one (backward)
+                auto dep = [&](int p) {
+                    if (p == pd) return false;
+                    const int w = __ldg(wave + rowOff + __ldg(cl + p));
+                    return FWD ? w < wi : w > wi;
+                };
+                wait_deps(flag, p0, p1, FWD ? 1 : 0, err, [&](int p) { return rowOff + __ldg(cl + p); }, dep);
+                TA s = b[row];
+                for (int p = p0; p < p1; ++p) {
+                    if (p == pd) continue;
+                    const int j = rowOff + __ldg(cl + p);
+                    if (FWD && ZERO && __ldg(wave + j) > wi) continue;   // x_j is still zero: the term vanishes
+                    s = asub(s, amul(__ldg(vl + p), x[j]));
+                }
+                x[row] = adiv(s, __ldg(vl + pd));
+            }
+            st_release(flag + row, FWD ? 1 : 0);
+        }
+    }
+}
+
+// one colour of a multicolour Gauss-Seidel sweep of level l over every system (FP32 forms): the positions
+// cpos[i0, i1) hold the colour's rows, which are independent, so this is a plain parallel pass. ZERO: pre-smoothing
+// from x = 0 (the terms of later colours vanish and are not read).
+template <class TA, bool ZERO>
+__global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, const int* __restrict__ cpos, const int* __restrict__ rowLv,
+                                                   const AmgSysLv* __restrict__ lv, const int* __restrict__ gsRows,
+                                                   const int* __restrict__ wave, const int* __restrict__ rp, const int* __restrict__ ci,
+                                                   const TA* __restrict__ val, const int* __restrict__ diag, const TA* b, TA* x,
+                                                   const KScal* ks) {
+    for (int i = i0 + int(blockIdx.x * blockDim.x + threadIdx.x); i < i1; i += int(gridDim.x * blockDim.x)) {
+        const int g = __ldg(cpos + i);
+        const int sl = __ldg(rowLv + g);
+        const AmgSysLv* A = lv + sl;
+        if (__ldg(&A->coarse) || (ks && ks[sl / maxL].status != ST_RUNNING)) continue;
+        const int rowOff = __ldg(&A->rowOff), k = __ldg(gsRows + g), row = rowOff + k;
+        const int rpOff = __ldg(&A->rpOff), entOff = __ldg(&A->entOff);
+        const int p0 = __ldg(rp + rpOff + k), p1 = __ldg(rp + rpOff + k + 1), pd = __ldg(diag + row);
+        const int* cl = ci + entOff;
+        const TA* vl = val + entOff;
+        const int wi = ZERO ? __ldg(wave + row) : 0;
+        TA s = b[row];
+        for (int p = p0; p < p1; ++p) {
+            if (p == pd) continue;
+            const int j = rowOff + __ldg(cl + p);
+            if (ZERO && __ldg(wave + j) > wi) continue;
+            s = asub(s, amul(__ldg(vl + p), x[j]));
+        }
+        x[row] = adiv(s, __ldg(vl + pd));
+    }
+}
+
+// b_{l+1} = R (b_l - A_l x_l) for the coarse rows [c0, c1) of level l + 1: the residual of each member from zero in
+// entry order, the members in restriction order (engine/src/amg.cpp:321-324)
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_restrict(int c0, int c1, int maxL, const int* __restrict__ rowLv,
+                                                       const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                       const int* __restrict__ ci, const TA* __restrict__ val,
+                                                       const int* __restrict__ memPtr, const int* __restrict__ mem, TA* b, const TA* x,
+                                                       const KScal* ks) {
+    for (int c = c0 + int(blockIdx.x * blockDim.x + threadIdx.x); c < c1; c += int(gridDim.x * blockDim.x)) {
+        const int sl = __ldg(rowLv + c);
+        if (ks && ks[sl / maxL].status != ST_RUNNING) continue;
+        const AmgSysLv* Cl = lv + sl;
+        const AmgSysLv* F = lv + sl - 1;
+        const int I = c - __ldg(&Cl->rowOff);
+        const int* mp = memPtr + __ldg(&Cl->rpOff);
+        const int* mm = mem + __ldg(&Cl->memOff);
+        const int fOff = __ldg(&F->rowOff);
+        const int* frp = rp + __ldg(&F->rpOff);
+        const int* fci = ci + __ldg(&F->entOff);
+        const TA* fv = val + __ldg(&F->entOff);
+        TA t = TA(0);
+        for (int q = __ldg(mp + I); q < __ldg(mp + I + 1); ++q) {
+            const int m = __ldg(mm + q);
+            TA acc = TA(0);
+            for (int p = __ldg(frp + m); p < __ldg(frp + m + 1); ++p) acc = aadd(acc, amul(__ldg(fv + p), x[fOff + __ldg(fci + p)]));
+            t = aadd(t, asub(b[fOff + m], acc));
+        }
+        b[c] = t;
+    }
+}
+
+// x_l += P x_{l+1} (injection of the aggregate's value, engine/src/amg.cpp:326) on the rows [q0, q1) of level l
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_prolong(int q0, int q1, int maxL, const int* __restrict__ rowLv,
+                                                      const AmgSysLv* __restrict__ lv, const int* __restrict__ agg, TA* x,
+                                                      const KScal* ks) {
+    for (int g = q0 + int(blockIdx.x * blockDim.x + threadIdx.x); g < q1; g += int(gridDim.x * blockDim.x)) {
+        const int sl = __ldg(rowLv + g);
+        if (__ldg(&lv[sl].coarse) || (ks && ks[sl / maxL].status != ST_RUNNING)) continue;
+        x[g] = aadd(x[g], x[__ldg(&lv[sl + 1].rowOff) + __ldg(agg + g)]);
+    }
+}
+
+// coarsest level of every system: dense LU (FP64) or explicit inverse (FP32 forms); without a dense LU, x = 0
+// before the symmetric GS sweeps of phase 1
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_coarse(CprArgs<TA> C, const KScal* ks) {
+    const int s = blockIdx.x;
+    if (ks && ks[s].status != ST_RUNNING) return;
+    int nlev = 0;
+    while (nlev < C.maxL && C.lv[s * C.maxL + nlev].n > 0) ++nlev;
+    if (nlev == 0) return;
+    const AmgSysLv A = C.lv[s * C.maxL + nlev - 1];
+    TA* x = C.x + A.rowOff;
+    if (A.dense) {
+        if constexpr (sizeof(TA) == 4) {
+            if (C.coarse64[s]) coarse_fp64(A, C, x, C.b + A.rowOff);
+            else coarse_inverse(A, C, x, C.b + A.rowOff);
+        } else {
+            coarse_dense<TA, 256>(A, C, x, C.b + A.rowOff, C.r + A.rowOff);
+        }
+    } else {
+        for (int k = threadIdx.x; k < A.n; k += blockDim.x) x[k] = TA(0);
+    }
+}
+
+// t = input - S[:,p] xp (pressure column of every block in row order, bsr.cpp:1071-1081), in place in T
+template <class TA, class TT>
+__global__ void __launch_bounds__(256) k_gcpr_t(int n, const int* __restrict__ rowSys, const int* __restrict__ rowPtr,
+                                                const int* __restrict__ col, const double* __restrict__ val, const TA* xp, double* T,
+                                                const KScal* ks) {
+    for (int k = int(blockIdx.x * blockDim.x + threadIdx.x); k < n; k += int(gridDim.x * blockDim.x)) {
+        if (ks && ks[__ldg(rowSys + k)].status != ST_RUNNING) continue;
+        TT acc[3] = {TT(T[size_t(k) * 3]), TT(T[size_t(k) * 3 + 1]), TT(T[size_t(k) * 3 + 2])};
+        for (int p = __ldg(rowPtr + k); p < __ldg(rowPtr + k + 1); ++p) {
+            const double* B = val + size_t(p) * 9;
+            const TT xk = TT(xp[__ldg(col + p)]);
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                if constexpr (sizeof(TT) == 8) acc[e] = ds(acc[e], dm(__ldg(B + 3 * e), xk));
+                else acc[e] = acc[e] - float(__ldg(B + 3 * e)) * xk;
+            }
+        }
+        T[size_t(k) * 3] = double(acc[0]); T[size_t(k) * 3 + 1] = double(acc[1]); T[size_t(k) * 3 + 2] = double(acc[2]);
+    }
+}
+
+// z_p += xp (bsr.cpp:1083)
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_zp(int n, const int* __restrict__ rowSys, const TA* xp, double* z, const KScal* ks) {
+    for (int k = int(blockIdx.x * blockDim.x + threadIdx.x); k < n; k += int(gridDim.x * blockDim.x)) {
+        if (ks && ks[__ldg(rowSys + k)].status != ST_RUNNING) continue;
+        z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xp[k]));
+    }
+}
+
+template <class TA, class TT>
+int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, const TA* val, int mode, const double* r,
+             double* pv, const double* v, double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st) {
+    const int n = P.n, gn = grid_for(n, 256);
+    int launches = 0;
+    if (mode == IN_PUPDATE) k_gcpr_in<IN_PUPDATE, TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+    else if (mode == IN_SUPDATE) k_gcpr_in<IN_SUPDATE, TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+    else k_gcpr_in<IN_PLAIN, TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+    ++launches;
+    const auto& LB = G.levelRowBeg;
+    auto sweep = [&](int l, int phase, bool fwd, bool zero) {
+        const std::vector<int>& cb = G.colBeg[size_t(l)];
+        if (phase == 0 && cb.size() > 1) {                 // multicolour: a parallel pass per colour
+            const int nc = int(cb.size()) - 1;
+            for (int cc = 0; cc < nc; ++cc) {
+                const int c = fwd ? cc : nc - 1 - cc;
+                const int i0 = cb[size_t(c)], i1 = cb[size_t(c) + 1];
+                if (zero)
+                    k_gs_colour<TA, true><<<grid_for(i1 - i0, 256), 256, 0, st>>>(i0, i1, G.maxL, G.cpos, G.rowLv, G.lv, G.gsRows, G.wave,
+                                                                                 G.rp, G.ci, val, G.diag, C.b, C.x, ks);
+                else
+                    k_gs_colour<TA, false><<<grid_for(i1 - i0, 256), 256, 0, st>>>(i0, i1, G.maxL, G.cpos, G.rowLv, G.lv, G.gsRows, G.wave,
+                                                                                  G.rp, G.ci, val, G.diag, C.b, C.x, ks);
+                ++launches;
+            }
+            return;
+        }
+        const int q0 = LB[size_t(l)], q1 = LB[size_t(l) + 1];
+        int* flag = G.gsFlag + size_t(phase) * size_t(G.totRows);
+        unsigned* ctr = G.gsCtr + 4 * l + 2 * phase;
+        const int g = gs_grid(q1 - q0);
+        if (fwd && zero)
+            k_gs_grid<TA, true, true><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp, G.ci,
+                                                                       val, G.diag, C.b, C.x, flag, ctr, ks, err);
+        else if (fwd)
+            k_gs_grid<TA, true, false><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp, G.ci,
+                                                                        val, G.diag, C.b, C.x, flag, ctr, ks, err);
+        else
+            k_gs_grid<TA, false, false><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp, G.ci,
+                                                                         val, G.diag, C.b, C.x, flag, ctr, ks, err);
+        ++launches;
+    };
+    for (int l = 0; l + 1 < G.maxL; ++l) {                 // pre-smoothing and restriction, finest to coarsest
+        sweep(l, 0, true, true);
+        const int c0 = LB[size_t(l) + 1], c1 = LB[size_t(l) + 2];
+        k_gcpr_restrict<TA><<<grid_for(c1 - c0, 256), 256, 0, st>>>(c0, c1, G.maxL, G.rowLv, G.lv, G.rp, G.ci, val, G.memPtr, G.mem, C.b,
+                                                                    C.x, ks);
+        ++launches;
+    }
+    k_gcpr_coarse<TA><<<G.nsys, 256, 0, st>>>(C, ks);
+    ++launches;
+    for (int l : G.coarseGsLevels)                         // coarsest levels without dense LU (amg.cpp:313-315)
+        for (int it = 0; it < 20; ++it) {
+            sweep(l, 1, true, false);
+            sweep(l, 1, false, false);
+        }
+    for (int l = G.maxL - 2; l >= 0; --l) {                // prolongation and post-smoothing, coarsest to finest
+        const int q0 = LB[size_t(l)], q1 = LB[size_t(l) + 1];
+        k_gcpr_prolong<TA><<<grid_for(q1 - q0, 256), 256, 0, st>>>(q0, q1, G.maxL, G.rowLv, G.lv, G.agg, C.x, ks);
+        ++launches;
+        sweep(l, 0, false, false);
+    }
+    k_gcpr_t<TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, P.rowPtr, P.col, M.val, C.x, G.T, ks);
+    launch_ilu_grid_ks(P, M, G.T, z, ks, S, err, st);
+    k_gcpr_zp<TA><<<gn, 256, 0, st>>>(n, P.rowSys, C.x, z, ks);
+    return launches + 4;
+}
+
+}  // namespace
+
+int launch_cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, const double* r, double* pv, const double* v,
+                    double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st) {
+    if (M.kind == 0) {
+        const CprArgs<double> C = cpr_args<double>(G, G.val, G.slotVal, G.diagVal, G.lu, G.x, G.b, G.r, G.sp, G.spLov, G.spUov);
+        return cpr_grid<double, double>(P, M, G, C, G.val, mode, r, pv, v, z, ks, S, err, st);
+    }
+    const CprArgs<float> C = cpr_args<float>(G, G.valf, G.slotValf, G.diagValf, G.luf, G.xf, G.bf, G.rf, G.spf, G.spLovf, G.spUovf);
+    if (M.kind == 1) return cpr_grid<float, double>(P, M, G, C, G.valf, mode, r, pv, v, z, ks, S, err, st);
+    return cpr_grid<float, float>(P, M, G, C, G.valf, mode, r, pv, v, z, ks, S, err, st);
 }
 
 }  // namespace rsg

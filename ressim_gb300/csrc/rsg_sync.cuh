@@ -1,0 +1,69 @@
+// Synchronisation helpers of the sync-free (flag-driven) kernels, shared by the device translation units
+// (internal linkage in each): release stores and relaxed polls of per-row flags at GPU scope with one acquire
+// fence per row, the bounded waits, and the warp's claim of 32 consecutive positions from an atomic counter.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rsg_impl.h"
+
+namespace rsg {
+namespace {
+
+constexpr unsigned kSpinLimit = 1u << 22;   // x up to 256 ns back-off: about one second per wait
+
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// bounded wait for *f == want by relaxed polls (the caller fences once after all its waits): a short busy spin
+// first (most waits in a sweep are short), then exponential back-off up to 256 ns; on time-out sets ERR_TIMEOUT
+// and returns false (the caller then proceeds)
+__device__ __noinline__ bool spin_relaxed(const int* f, int want, int* err) {
+    for (int it = 0; it < 64; ++it)
+        if (ld_relaxed(f) == want) return true;
+    unsigned ns = 32;
+    for (unsigned it = 0; it < kSpinLimit; ++it) {
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+        if (ld_relaxed(f) == want) return true;
+        if ((it & 255u) == 255u && *(volatile int*)err != 0) return false;   // another wait already gave up
+    }
+    atomicOr(err, ERR_TIMEOUT);
+    return false;
+}
+
+// Wait until flag[idx(q)] == want for every q in [q0, q1) with need(q), then one acquire fence. A row's
+// dependencies are polled four at a time with relaxed loads that are in flight together, where an acquire load
+// per dependency would cost one round trip after another on the sweep's critical path.
+template <class Idx, class Need>
+__device__ __forceinline__ void wait_deps(const int* flag, int q0, int q1, int want, int* err, Idx idx, Need need) {
+    for (int q = q0; q < q1; q += 4) {
+        int k[4], v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) k[u] = (q + u < q1 && need(q + u)) ? idx(q + u) : -1;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = k[u] >= 0 ? ld_relaxed(flag + k[u]) : want;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (v[u] != want) spin_relaxed(flag + k[u], want, err);
+    }
+    fence_acquire();
+}
+// the common case: the dependencies are the columns col[p0 .. p1)
+__device__ __forceinline__ void wait_cols(const int* flag, const int* __restrict__ col, int p0, int p1, int want, int* err) {
+    wait_deps(flag, p0, p1, want, err, [&](int p) { return __ldg(col + p); }, [](int) { return true; });
+}
+__device__ __forceinline__ int warp_claim(unsigned* ctr) {
+    unsigned base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(ctr, 32u);
+    return int(__shfl_sync(0xffffffffu, base, 0));
+}
+
+}  // namespace
+}  // namespace rsg

@@ -217,30 +217,33 @@ def test_gpu_block_solver_adapter():
 
 
 # ---------------------------------------------------------------- CPR (AMG on the pressure system + BILU0)
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
-def test_cpr_apply_matches_reference(name):
+def test_cpr_apply_matches_reference(name, sweep):
     """BlockCPR::apply: weights, pressure matrix, aggregation hierarchy, Gauss-Seidel V-cycle and BILU0 are the
-    reference's arithmetic; only the back substitution of the coarsest dense LU runs column-wise (summation order)."""
+    reference's arithmetic; only the back substitution of the coarsest dense LU runs column-wise (summation order).
+    Both applications: one thread block per system, and grid-wide (sync-free sweeps, level by level)."""
     A, z = load_golden(name)
-    with dev(precond="cpr") as d:
+    with dev(precond="cpr", sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         assert d.stats().amg_levels == len(z["amg_rows"])
         assert rel(d.precond_apply(z["b"]), z["z_cpr"]) < 1e-10
     if "acc" in z.files:                                  # true-IMPES weights from the accumulation blocks
-        with dev(precond="cpr") as d:
+        with dev(precond="cpr", sweep=sweep) as d:
             d.set_matrix(A)
             d.setup(acc=z["acc"])
             assert rel(d.precond_apply(z["b"]), z["z_cpr_acc"]) < 1e-10
 
 
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("precision", ["mixed", "mixed_f32"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
-def test_cpr_multicolour_apply_matches_oracle(name, precision, oracle):
+def test_cpr_multicolour_apply_matches_oracle(name, precision, sweep, oracle):
     """FP32 precision forms: FP32 hierarchy smoothed by multicolour Gauss-Seidel; against the oracle's FP64
     restatement of the same algorithm (float rounding of factors, hierarchy, coarse LU and sweeps)."""
     A, z = load_golden(name)
-    with dev(precond="cpr", precision=precision) as d:
+    with dev(precond="cpr", precision=precision, sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         zd = d.precond_apply(z["b"])
@@ -254,10 +257,11 @@ def test_cpr_multicolour_apply_matches_oracle(name, precision, oracle):
     assert rel(zd, zo) < 1e-3
 
 
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
-def test_cpr_bicgstab_matches_reference(name):
+def test_cpr_bicgstab_matches_reference(name, sweep):
     A, z = load_golden(name)
-    with dev(precond="cpr", check_every=2) as d:
+    with dev(precond="cpr", check_every=2, sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         x, res = d.solve(z["b"], tol=1e-6, maxit=120)
@@ -285,11 +289,12 @@ def test_cpr_refresh_equals_fresh_setup():
     assert rel(z1, z2) < 1e-12
 
 
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
-def test_cpr_batched_ensemble(precision):
+def test_cpr_batched_ensemble(precision, sweep):
     from ressim_gb300 import synth
     systems = synth.ensemble(n_real=6, nx=24, ny=24, nz=6, sigma=1.5)
-    with dev(precond="cpr", precision=precision, check_every=4) as d:
+    with dev(precond="cpr", precision=precision, check_every=4, sweep=sweep) as d:
         d.set_batch([s.A for s in systems])
         d.setup()
         x, res = d.solve(np.concatenate([s.b for s in systems]), tol=1e-6, maxit=300)
@@ -337,6 +342,29 @@ def test_cpr_large_systems(precision, oracle):
         off += N
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed_f32"])
+def test_cpr_single_large_system(precision, oracle):
+    """One system too large for one SM (73,728 cells): the grid-wide CPR application against the oracle, and the
+    CPR-BiCGSTAB solve (which takes the grid path by itself) to the true residual."""
+    from ressim_gb300 import synth
+    s = synth.make_system(48, 48, 32, sigma=2.0, seed=11, dt=5.0, wells="random", n_wells=4)
+    A = s.A
+    assert A.n > 65536
+    r = np.random.default_rng(6).standard_normal(A.n * 3)
+    with dev(precond="cpr", precision=precision) as d:
+        d.set_matrix(A)
+        d.setup()
+        z = d.precond_apply(r)
+        x, res = d.solve(s.b, tol=1e-6, maxit=300)
+    oracle.set_mc_smoother(precision != "fp64")
+    try:
+        zo = oracle.prec_apply(A, r, prec=1)
+    finally:
+        oracle.set_mc_smoother(False)
+    assert rel(z, zo) < (1e-10 if precision == "fp64" else 1e-3)
+    assert res.converged and true_res(A, x, s.b) <= 1e-5
+
+
 # ---------------------------------------------------------------- GMRES (flexible, restarted; linsolve.cpp:218-273)
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS + ["singular_pivots.npz"])
 def test_gmres_bilu0_matches_reference(name):
@@ -354,9 +382,10 @@ def test_gmres_bilu0_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
-def test_gmres_cpr_matches_reference(name):
+@pytest.mark.parametrize("sweep", ["cta", "grid"])
+def test_gmres_cpr_matches_reference(name, sweep):
     A, z = load_golden(name)
-    with dev(krylov="gmres", precond="cpr", restart=30) as d:
+    with dev(krylov="gmres", precond="cpr", restart=30, sweep=sweep) as d:
         d.set_matrix(A)
         d.setup()
         x, res = d.solve(z["b"], tol=1e-6, maxit=300)
