@@ -63,6 +63,8 @@ typedef struct rsg_options {
     int fma;                /* 1 (default): the SpMV accumulates with fused multiply-adds (half the FP64
                                instructions; results within rounding of the reference); 0: the reference's separately
                                rounded products and sums, bit for bit (engine/src/bsr.cpp:109-117) */
+    int sweep_inflight;     /* sync-free grid sweeps (BILU0, factorisation, Gauss-Seidel): levels in flight, which sizes
+                               the persistent grid; 0 = auto (the full grid) */
 } rsg_options;
 
 typedef struct rsg_stats {
@@ -76,6 +78,8 @@ typedef struct rsg_stats {
     int amg_levels;         /* CPR: levels of the pressure AMG hierarchy */
     size_t device_bytes;    /* device memory held by the handle */
     long long kernel_launches; /* kernels launched by this handle since creation (graph nodes included) */
+    int escalated_systems;  /* precision form: systems of the last solve that diverged or stalled with the all-FP32
+                               preconditioner and were solved again with its FP64-vector sweeps */
 } rsg_stats;
 
 typedef struct rsg_solver rsg_solver;
@@ -121,6 +125,8 @@ int rsg_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, 
 
 /* Per-system results of the last (batched) solve: its[nsys], relres[nsys] (host arrays, may be NULL). */
 int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relres);
+/* Per system of the last solve: RSG_OK (converged), RSG_ENOTCONV or RSG_EBREAKDOWN. */
+int rsg_batch_status(rsg_solver* h, int* status);
 
 /* y = A x with host / device vectors. Replaces BSR::spmv (engine/src/bsr.cpp:109-126). */
 int rsg_spmv(rsg_solver* h, const double* x, double* y);
@@ -195,6 +201,7 @@ typedef struct rsg_result {
     double start_ms, end_ms;  /* admitted / done, ms since the server was created (one clock for all requests) */
     int slot;                 /* worker that ran it */
     int precond;              /* preconditioner used (RSG_PREC_*; CPR requests whose pattern is not structurally symmetric run BILU0) */
+    int batch;                /* requests solved together in the request's launch (small systems are batched) */
 } rsg_result;
 
 /* opts: solver options of every slot (device, precision, preconditioner, Krylov method); slots >= 1;

@@ -21,7 +21,7 @@ SWEEP = {"auto": 0, "cta": 1, "grid": 2}
 # every symbol include/rsg.h declares
 EXPORTS = [
     "rsg_default_options", "rsg_last_error", "rsg_version", "rsg_create", "rsg_destroy", "rsg_set_matrix", "rsg_set_batch",
-    "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
+    "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_batch_status", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
     "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
     "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes",
@@ -31,19 +31,19 @@ EXPORTS = [
 class Options(C.Structure):
     _fields_ = [("precond", C.c_int), ("krylov", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("gmres_fallback", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
-                ("mem_budget", C.c_size_t), ("sweep", C.c_int), ("fma", C.c_int)]
+                ("mem_budget", C.c_size_t), ("sweep", C.c_int), ("fma", C.c_int), ("sweep_inflight", C.c_int)]
 
 
 class Result(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
                 ("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double), ("device_bytes", C.c_size_t),
-                ("start_ms", C.c_double), ("end_ms", C.c_double), ("slot", C.c_int), ("precond", C.c_int)]
+                ("start_ms", C.c_double), ("end_ms", C.c_double), ("slot", C.c_int), ("precond", C.c_int), ("batch", C.c_int)]
 
 
 class Stats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("regularised_blocks", C.c_int), ("amg_levels", C.c_int),
-                ("device_bytes", C.c_size_t), ("kernel_launches", C.c_longlong)]
+                ("device_bytes", C.c_size_t), ("kernel_launches", C.c_longlong), ("escalated_systems", C.c_int)]
 
 
 class RsgError(RuntimeError):
@@ -78,6 +78,7 @@ def load(build_if_missing: bool = True):
     L.rsg_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
     L.rsg_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
     L.rsg_batch_results.argtypes = [vp, vp, vp, vp]
+    L.rsg_batch_status.argtypes = [vp, vp]
     L.rsg_spmv.argtypes = [vp, vp, vp]
     L.rsg_spmv_device.argtypes = [vp, vp, vp]
     L.rsg_precond_apply.argtypes = [vp, vp, vp]

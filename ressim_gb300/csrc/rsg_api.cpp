@@ -97,6 +97,7 @@ struct rsg_solver {
     SplitFactors<double> s64;
     SplitFactors<float> s32;
     bool cta = false;
+    bool escalated = false;      // precision form: failed systems re-solved with FP64 sweep vectors (until the next set-up)
     // CPR: device AMG of the batch (allocated in pmem; built at the first CPR set-up of a pattern)
     DevAmg amg;
     bool haveAmg = false;
@@ -190,6 +191,11 @@ int alloc_plan(rsg_solver* h) {
     D.nLov = int(P.LovCol.size());
     D.nUov = int(P.UovCol.size());
     D.maxSysRows = P.maxSysRows;
+    {
+        int maxLv = 1;
+        for (int s = 0; s < P.nsys; ++s) maxLv = std::max(maxLv, P.sysLvl0[size_t(s) + 1] - P.sysLvl0[size_t(s)] - 1);
+        D.sweepBlocks = sweep_blocks_for(double(P.n) / double(maxLv), h->opt.sweep_inflight);
+    }
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
     if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
@@ -249,7 +255,7 @@ PrecDev prec_dev(rsg_solver* h) {
     PrecDev M;
     if (h->opt.precond == RSG_PREC_JACOBI) { M.kind = 2; M.dinv = h->dinv; }
     else if (h->opt.precision == RSG_MIXED) { M.kind = 1; M.luf = h->luf; }
-    else if (h->opt.precision == RSG_MIXED_F32) { M.kind = 3; M.luf = h->luf; }
+    else if (h->opt.precision == RSG_MIXED_F32) { M.kind = h->escalated ? 1 : 3; M.luf = h->luf; }
     else { M.kind = 0; M.lu = h->lu; }
     M.val = h->val;
     M.y32 = h->V.y32;
@@ -516,28 +522,76 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         }
         if (gsCoarse) G.coarseGsLevels.push_back(l);
     }
-    // colour-major positions of every level (multicolour schedule only): colour c of every system, then c + 1
-    std::vector<int> cpos(static_cast<size_t>(std::max(rows, 1)), 0);
+    // the sync-free sweeps may take "updated before" from the entry position when it agrees with the waves everywhere
+    G.posOrder = true;
+    for (int l = 0; l < maxL && G.posOrder; ++l)
+        for (int s = 0; s < nsys && G.posOrder; ++s) {
+            if (l >= int(H[size_t(s)].lv.size())) continue;
+            const AmgSysLv& d = lv[size_t(s) * maxL + l];
+            const AmgLevel& A = H[size_t(s)].lv[size_t(l)];
+            for (int k = 0; k < A.n && G.posOrder; ++k) {
+                const int wk = wave[size_t(d.rowOff + k)], pd = A.diag[size_t(k)];
+                for (int p = A.rp[size_t(k)]; p < A.rp[size_t(k) + 1]; ++p) {
+                    if (p == pd) continue;
+                    const bool earlier = wave[size_t(d.rowOff + A.ci[size_t(p)])] < wk;
+                    if (earlier != (p < pd)) { G.posOrder = false; break; }
+                }
+            }
+        }
+    G.gsBlocks.assign(size_t(maxL), 1);
+    for (int l = 0; l < maxL; ++l) {
+        int maxNl = 1;
+        for (int s = 0; s < nsys; ++s)
+            if (l < int(H[size_t(s)].lv.size())) maxNl = std::max(maxNl, lv[size_t(s) * maxL + l].nl);
+        G.gsBlocks[size_t(l)] = sweep_blocks_for(double(G.levelRowBeg[size_t(l) + 1] - G.levelRowBeg[size_t(l)]) / maxNl, h->opt.sweep_inflight);
+    }
+    // colour-major rows of every level that is smoothed (multicolour schedule only): colour c of every system, then
+    // c + 1; colours from colTail on (all of them small) go to one thread block
+    constexpr int kTailRows = 2048;
+    std::vector<int4> cdesc;
+    std::vector<int> cbeg;
     G.colBeg.assign(size_t(maxL), std::vector<int>());
+    G.cbegOff.assign(size_t(maxL), 0);
+    G.colTail.assign(size_t(maxL), 0);
     if (mc)
         for (int l = 0; l < maxL; ++l) {
             int ncol = 0;
             for (int s = 0; s < nsys; ++s)
-                if (l < int(H[size_t(s)].lv.size())) ncol = std::max(ncol, lv[size_t(s) * maxL + l].nl);
+                if (l < int(H[size_t(s)].lv.size()) && !lv[size_t(s) * maxL + l].coarse) ncol = std::max(ncol, lv[size_t(s) * maxL + l].nl);
             std::vector<int>& cb = G.colBeg[size_t(l)];
-            cb.assign(size_t(ncol) + 1, G.levelRowBeg[size_t(l)]);
-            int q = G.levelRowBeg[size_t(l)];
+            cb.assign(size_t(ncol) + 1, int(cdesc.size()));
             for (int c = 0; c < ncol; ++c) {
-                cb[size_t(c)] = q;
+                cb[size_t(c)] = int(cdesc.size());
                 for (int s = 0; s < nsys; ++s) {
                     if (l >= int(H[size_t(s)].lv.size())) continue;
                     const AmgSysLv& d = lv[size_t(s) * maxL + l];
-                    if (c >= d.nl) continue;
+                    if (d.coarse || c >= d.nl) continue;
+                    const AmgLevel& A = H[size_t(s)].lv[size_t(l)];
                     const std::vector<int>& st0 = schStart[size_t(s) * maxL + l];
-                    for (int g = st0[size_t(c)]; g < st0[size_t(c) + 1]; ++g) cpos[size_t(q++)] = d.rowOff + g;
+                    const std::vector<int>& rw = schRows[size_t(s) * maxL + l];
+                    for (int g = st0[size_t(c)]; g < st0[size_t(c) + 1]; ++g) {
+                        const int k = rw[size_t(g)];
+                        cdesc.push_back(make_int4(d.rowOff + k, d.entOff + A.rp[size_t(k)], d.entOff + A.rp[size_t(k) + 1],
+                                                  d.entOff + A.diag[size_t(k)]));
+                    }
                 }
             }
-            cb[size_t(ncol)] = q;
+            cb[size_t(ncol)] = int(cdesc.size());
+            int tail = ncol;
+            while (tail > 0 && cb[size_t(tail)] - cb[size_t(tail) - 1] < kTailRows) --tail;
+            G.colTail[size_t(l)] = tail;
+            G.cbegOff[size_t(l)] = int(cbeg.size());
+            cbeg.insert(cbeg.end(), cb.begin(), cb.end());
+        }
+    if (cdesc.empty()) cdesc.push_back(make_int4(0, 0, 0, 0));
+    if (cbeg.empty()) cbeg.push_back(0);
+    std::vector<int> gci(static_cast<size_t>(std::max(ents, 1)), 0);
+    for (int l = 0; l < maxL; ++l)
+        for (int s = 0; s < nsys; ++s) {
+            if (l >= int(H[size_t(s)].lv.size())) continue;
+            const AmgSysLv& d = lv[size_t(s) * maxL + l];
+            const AmgLevel& A = H[size_t(s)].lv[size_t(l)];
+            for (int e = 0; e < d.nnz; ++e) gci[size_t(d.entOff + e)] = d.rowOff + A.ci[size_t(e)];
         }
     // pointer arrays are prefix sums over the level-major order: fill gaps (levels absent for some systems)
     for (size_t e = 1; e < apPtr.size(); ++e) apPtr[e] = std::max(apPtr[e], apPtr[e - 1]);
@@ -552,7 +606,8 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = upload(M, &G.apSrc, apSrc, st)) || (rc = upload(M, &G.acPtr, acPtr, st)) || (rc = upload(M, &G.acSrc, acSrc, st)) ||
         (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)) ||
         (rc = upload(M, &G.slotSrc, slotSrc, st)) || (rc = upload(M, &G.slotCol, slotCol, st)) || (rc = upload(M, &G.gsRows, gsRows, st)) ||
-        (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)) || (rc = upload(M, &G.rowLv, rowLv, st)) || (rc = upload(M, &G.cpos, cpos, st)) ||
+        (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)) || (rc = upload(M, &G.rowLv, rowLv, st)) || (rc = upload(M, &G.cdesc, cdesc, st)) || (rc = upload(M, &G.gci, gci, st)) ||
+        (rc = upload(M, &G.cbeg, cbeg, st)) ||
         (rc = upload(M, &G.wave, wave, st)) || (rc = dalloc(M, &G.gsFlag, 2 * size_t(std::max(rows, 1)))) ||
         (rc = dalloc(M, &G.gsCtr, 4 * size_t(std::max(maxL, 1)))) || (rc = dalloc(M, &G.coarse64, size_t(std::max(nsys, 1)))))
         return rc;
@@ -648,6 +703,8 @@ int setup_cpr(rsg_solver* h, const double* acc) {
 
 int do_setup(rsg_solver* h, const double* acc) {
     if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
+    h->escalated = false;
+    h->st.escalated_systems = 0;
     if (h->opt.precond == RSG_PREC_CPR && !h->plan.symmetric)
         return fail(RSG_EINVAL, "the CPR preconditioner needs structurally symmetric systems");
     int rc = ensure_precond_storage(h);
@@ -709,8 +766,9 @@ int launch_iterations(rsg_solver* h, int k) {
 
 
 // BiCGSTAB of every system from the gathered right-hand side h->b into h->V.x
-int run_bicgstab(rsg_solver* h, double tol, int maxIt) {
-    launch_bicg_init(h->dp, h->b, h->V, h->ks, h->R, tol, maxIt, h->d_active, h->stream);
+int run_bicgstab(rsg_solver* h, double tol, int maxIt, bool onlyFailed = false) {
+    const bool guard = h->opt.precision == RSG_MIXED_F32 && !h->escalated;
+    launch_bicg_init(h->dp, h->b, h->V, h->ks, h->R, tol, maxIt, h->d_active, guard, onlyFailed, h->stream);
     h->launches += 1;
     RSG_CUDA(cudaGetLastError());
     const int chunk = h->opt.check_every > 0 ? h->opt.check_every : 4;
@@ -808,6 +866,29 @@ int run_gmres(rsg_solver* h, double tol, int maxIt, bool onlyFailed) {
 }
 
 // d_b, d_x: caller's vectors in the original row order; the solve runs in level space (h->b, h->V.x)
+// Precision escalation of the all-FP32 preconditioner: on systems with extreme coefficient contrasts its FP32
+// triangular sweeps can diverge (the divergence guard stops them early). The systems that did not converge are
+// solved again from x = 0 with the same FP32 factors -- eliminated in FP64 on the thread-block path, as the grid
+// path already has them -- and the sweep vector in FP64 (the mixed form); the converged systems keep their result.
+int escalate(rsg_solver* h, double tol, int maxIt) {
+    std::vector<KScal> k0(size_t(h->plan.nsys));
+    RSG_CUDA(cudaMemcpyAsync(k0.data(), h->ks, sizeof(KScal) * k0.size(), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    int failed = 0;
+    for (const KScal& k : k0) failed += k.status != ST_CONV;
+    if (!failed) return RSG_OK;
+    if (h->cta) {
+        ++h->epoch;
+        launch_factor_lean(h->dp, h->val, h->luf, h->work, h->S, h->epoch, h->d_nreg, h->d_err, h->stream);
+        launch_pack_f32(h->dp, h->luf, h->s32, h->stream);
+        h->launches += 2;
+        RSG_CUDA(cudaGetLastError());
+    }
+    h->escalated = true;
+    h->st.escalated_systems = failed;
+    return run_bicgstab(h, tol, maxIt, true);
+}
+
 int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
     if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
     if (!(tol > 0) || maxIt < 0) return fail(RSG_EINVAL, "tol must be > 0 and maxIt >= 0");
@@ -820,6 +901,7 @@ int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, i
         if ((rc = run_gmres(h, tol, maxIt, false))) return rc;
     } else {
         if ((rc = run_bicgstab(h, tol, maxIt))) return rc;
+        if (h->opt.precision == RSG_MIXED_F32 && !h->escalated && (rc = escalate(h, tol, maxIt))) return rc;
         if (h->opt.gmres_fallback) {
             // systems that did not converge are solved again with GMRES from x = 0; per system the result with the
             // smaller recursive residual is kept (engine/src/simulator.cpp:3388-3398)
@@ -1012,6 +1094,15 @@ int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relr
         if (its) its[s] = h->hks[s].its;
         if (relres) relres[s] = h->hks[s].relres;
         if (true_relres) true_relres[s] = h->htrue[s];
+    }
+    return RSG_OK;
+}
+
+int rsg_batch_status(rsg_solver* h, int* status) {
+    if (!h || !status) return fail(RSG_EINVAL, "null argument");
+    for (size_t s = 0; s < h->hks.size(); ++s) {
+        const int st = h->hks[s].status;
+        status[s] = st == ST_CONV ? RSG_OK : (st == ST_BREAKDOWN ? RSG_EBREAKDOWN : RSG_ENOTCONV);
     }
     return RSG_OK;
 }

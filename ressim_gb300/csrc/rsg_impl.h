@@ -19,7 +19,8 @@ constexpr int UREC = 36;              // per row record of U and D: SLOTS blocks
 constexpr int SPREC = 24;             // CPR pressure columns of S per row: (SLOTS + 1 + SLOTS) blocks x 3 + 3 pad
 
 // Krylov status per system (device int)
-enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3, ST_CYCLE = 4 /* GMRES: restart cycle ended */ };
+enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3, ST_CYCLE = 4 /* GMRES: restart cycle ended */,
+             ST_DIVERGED = 5 /* FP32 preconditioner: the residual grew past the divergence guard */ };
 
 // Error bits written by kernels (device int, OR-ed)
 enum : int { ERR_TIMEOUT = 1, ERR_NONFINITE = 2 };
@@ -30,10 +31,11 @@ struct KScal {
     double bn;                        // ||b||
     double relres;                    // recursive relative residual of the last completed iteration
     double sn;                        // ||s|| of the current iteration
-    int status, its, maxit, pad;
+    int status, its, maxit, guard;    // guard: stop when the residual diverges (FP32 preconditioner; the solve escalates)
     double tol;
-    double hn;                        // GMRES: norm of the last orthogonalised vector
-    int gj, gend;                     // GMRES: inner steps of the current cycle; cycle ended by convergence
+    double hn;                        // GMRES: norm of the last orthogonalised vector; BiCGSTAB guard: best residual
+    int gj, gend;                     // GMRES: inner steps of the current cycle (BiCGSTAB guard: iteration of the best
+                                      // residual); cycle ended by convergence
 };
 
 // Host-built, pattern-only plan of the device solve. Everything on the device runs in "level space": inside
@@ -165,11 +167,20 @@ struct DevAmg {
     int* gsFlag = nullptr;             // 2 x totRows
     unsigned* gsCtr = nullptr;         // maxL x 4
     std::vector<int> coarseGsLevels;   // host: levels that are some system's coarsest without a dense LU
-    // multicolour schedule (FP32 forms), grid-wide: per level the schedule positions of every system ordered colour
-    // by colour (cpos), and per level the position range of colour c at colBeg[l][c] .. colBeg[l][c + 1]
-    int* cpos = nullptr;
+    // multicolour schedule (FP32 forms), grid-wide: per level the rows of every system that smooths it, colour by
+    // colour, as {row, first entry, end of entries, diagonal entry} (global indices); colour c of level l at
+    // colBeg[l][c] .. colBeg[l][c + 1] (host) and cbeg[cbegOff[l] + c] (device). Colours from colTail[l] on hold
+    // few rows (the cliques of perforated cells that the well Schur fill creates) and go to one thread block.
+    int4* cdesc = nullptr;
+    int* gci = nullptr;                // global column of every entry (rowOff + local column)
+    int* cbeg = nullptr;
     std::vector<std::vector<int>> colBeg;
+    std::vector<int> cbegOff, colTail;
+    std::vector<int> gsBlocks;         // host: persistent grid of the sync-free Gauss-Seidel sweeps of each level
+    bool posOrder = false;             // host: in every row the entries before the diagonal are exactly its earlier-wave neighbours
 };
+// blocks of 4 warps for a sync-free sweep that keeps `inflight` of its levels (avgRows rows each) in flight
+int sweep_blocks_for(double avgRows, int inflight);
 // CPR set-up kernels (rsg_cpr.cu)
 void launch_cpr_weights(const DevPlan& P, const double* val, const double* accLev, double* w, int* nfallback, cudaStream_t st);
 void launch_cpr_pressure(const DevPlan& P, const double* val, const double* w, double* ap, cudaStream_t st);
@@ -191,8 +202,10 @@ int launch_cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mod
                     double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st);
 inline int cpr_grid_launches(const DevAmg& G) {
     int n = 6 + 2 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
-    for (int l = 0; l + 1 < G.maxL; ++l)            // pre- and post-smoothing: one sweep, or one launch per colour
-        n += 2 * (l < int(G.colBeg.size()) && G.colBeg[size_t(l)].size() > 1 ? int(G.colBeg[size_t(l)].size()) - 1 : 1);
+    for (int l = 0; l + 1 < G.maxL; ++l) {          // pre- and post-smoothing: one sweep, or a launch per large colour + the tail
+        const int nc = l < int(G.colBeg.size()) ? int(G.colBeg[size_t(l)].size()) - 1 : 0;
+        n += 2 * (nc > 0 ? G.colTail[size_t(l)] + (G.colTail[size_t(l)] < nc ? 1 : 0) : 1);
+    }
     return n;
 }
 
@@ -215,6 +228,7 @@ struct DevPlan {
     int *LslotSrc = nullptr, *UslotSrc = nullptr, *LovCol = nullptr, *LovSrc = nullptr, *UovCol = nullptr, *UovSrc = nullptr;
     int* Dsrc = nullptr;
     int nLov = 0, nUov = 0, maxSysRows = 0;
+    int sweepBlocks = 0;              // persistent grid of the sync-free sweeps (0: sized from n)
     bool spmvFma = true;              // SpMV with fused multiply-adds (else the reference's rounding, bitwise)
 };
 
@@ -270,7 +284,8 @@ struct BicgVecs {
     float* y32;                       // FP32 sweep intermediate (mixed precision)
 };
 void launch_bicg_init(const DevPlan& P, const double* b, BicgVecs& V, KScal* ks, ReduceState& R, double tol, int maxit,
-                      int* active, cudaStream_t st);
+                      int* active, bool guard, bool onlyFailed,
+                      cudaStream_t st);
 // one BiCGSTAB iteration (engine/src/linsolve.cpp:166-214) with the preconditioner given by prec:
 // 0 = BILU0 FP64, 1 = BILU0 FP32 (mixed), 2 = block Jacobi
 struct PrecDev {

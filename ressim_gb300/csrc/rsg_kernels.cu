@@ -457,17 +457,19 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_tile(int ntiles, int nsys
 __global__ void __launch_bounds__(kTileThreads) k_bicg_init(int ntiles, int nsys, const int* __restrict__ tileRow0,
                                                            const int* __restrict__ tileSys, const int* __restrict__ sysTile0,
                                                            const double* __restrict__ b, double* x, double* r, double* rh, double* p,
-                                                           double* v, KScal* ks, double tol, int maxit, double* part,
-                                                           unsigned* done, double* sysdot, int* active) {
+                                                           double* v, KScal* ks, double tol, int maxit, int guard, int onlyFailed,
+                                                           double* part, unsigned* done, double* sysdot, int* active) {
     __shared__ double sh[MAX_DOTS * kTileThreads];
     const int tile = blockIdx.x;
     const size_t q0 = size_t(__ldg(tileRow0 + tile)) * 3, q1 = size_t(__ldg(tileRow0 + tile + 1)) * 3;
     double acc[MAX_DOTS] = {0, 0, 0, 0};
-    for (size_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-        const double bq = __ldg(b + q);
-        x[q] = 0; r[q] = bq; rh[q] = bq; p[q] = 0; v[q] = 0;
-        acc[0] += bq * bq;
-    }
+    // onlyFailed: the systems that converged keep their solution and status (a restart of the others)
+    if (!onlyFailed || ks[__ldg(tileSys + tile)].status != ST_CONV)
+        for (size_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+            const double bq = __ldg(b + q);
+            x[q] = 0; r[q] = bq; rh[q] = bq; p[q] = 0; v[q] = 0;
+            acc[0] += bq * bq;
+        }
     block_reduce<1>(acc, sh);
     if (threadIdx.x == 0) part[size_t(tile) * MAX_DOTS] = acc[0];
     if (!last_tile_reduce<1>(ntiles, nsys, sysTile0, part, done, sysdot, sh)) return;
@@ -476,7 +478,11 @@ __global__ void __launch_bounds__(kTileThreads) k_bicg_init(int ntiles, int nsys
     int nact = 0;
     for (int s = threadIdx.x; s < nsys; s += blockDim.x) {
         KScal& K = ks[s];
+        if (onlyFailed && K.status == ST_CONV) continue;
         const double bb = sysdot[size_t(s) * MAX_DOTS];
+        K.guard = guard;
+        K.hn = 1e300;           // the guard's best residual so far and its iteration
+        K.gj = 0;
         K.bn = sqrt(bb);
         K.tol = tol; K.maxit = maxit; K.its = 0; K.relres = 0; K.sn = 0;
         K.alpha = 1; K.omega = 1; K.rho = bb; K.beta = bb;   // rhoN of iteration 1 = <rh, r> = <b, b>
@@ -537,6 +543,10 @@ __global__ void __launch_bounds__(kTileThreads) k_bicg_update(int ntiles, int ns
         if (k.omega == 0 || !isfinite(rn)) { k.status = ST_BREAKDOWN; atomicSub(active, 1); continue; }
         if (fabs(rhoN) < 1e-300) { k.status = ST_BREAKDOWN; atomicSub(active, 1); continue; }   // next iteration's test
         if (it >= k.maxit) { k.status = ST_MAXIT; atomicSub(active, 1); continue; }
+        if (k.guard) {          // FP32 preconditioner: diverging, or no new best residual for 40 iterations (stalled)
+            if (k.relres < k.hn) { k.hn = k.relres; k.gj = it; }
+            if ((it >= 8 && k.relres > 1e4) || it - k.gj >= 40) { k.status = ST_DIVERGED; atomicSub(active, 1); continue; }
+        }
         k.beta = (rhoN / k.rho) * (k.alpha / k.omega);
         k.rho = rhoN;
     }
@@ -624,7 +634,20 @@ int sweep_grid(int n) {
     return blocks;
 }
 
+// the plan's grid when it was sized from the level widths, else one from n
+int sweep_blocks(const DevPlan& P) { return P.sweepBlocks > 0 ? P.sweepBlocks : sweep_grid(P.n); }
+
 }  // namespace
+
+// Warps that poll flags of levels far ahead of the sweep front only add memory traffic to the critical path:
+// keep about `inflight` levels' rows in flight (a warp per 32 rows), at most 8 blocks of 4 warps per SM.
+int sweep_blocks_for(double avgRows, int inflight) {
+    if (inflight <= 0) return 8 * device_sm_count();              // auto: the full grid (measured no slower)
+    const double warps = double(inflight) * avgRows / 32.0;
+    const long long blocks = (long long)((warps + 3.0) / 4.0);
+    const long long cap = 8LL * device_sm_count();
+    return int(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+}
 
 int device_sm_count() {
     if (g_sm_count == 0) {
@@ -650,20 +673,20 @@ void launch_factor_f64(const DevPlan& P, const double* val, double* lu, SweepSta
                        cudaStream_t st) {
     cudaMemcpyAsync(lu, val, size_t(P.nnzb) * 9 * sizeof(double), cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(S.ctr + 2, 0, sizeof(unsigned), st);
-    k_factor_f64<<<sweep_grid(P.n), kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, P.elimPtr, P.elimT, P.elimQ, lu,
+    k_factor_f64<<<sweep_blocks(P), kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, P.elimPtr, P.elimT, P.elimQ, lu,
                                                            S.flagL, epoch, S.ctr + 2, nreg, err);
 }
 
 void launch_factor_lean(const DevPlan& P, const double* val, float* luf, double* work, SweepState& S, int epoch, int* nreg,
                         int* err, cudaStream_t st) {
     cudaMemsetAsync(S.ctr + 2, 0, sizeof(unsigned), st);
-    k_factor_lean<<<sweep_grid(P.n), kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, P.elimPtr, P.elimT, P.elimQ,
+    k_factor_lean<<<sweep_blocks(P), kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, P.elimPtr, P.elimT, P.elimQ,
                                                             val, luf, work, S.flagL, epoch, S.ctr + 2, nreg, err);
 }
 
 void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, double* z, SweepState& S, int* err,
                           cudaStream_t st) {
-    const int g = sweep_grid(P.n);
+    const int g = sweep_blocks(P);
     k_fwd_f64<double, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, lu, r, nullptr, nullptr, z, P.rowSys,
                                                      nullptr, S.flagF, S.flagB, S.ctr, err);
     k_bwd_f64<double><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, lu, z, P.rowSys, nullptr, S.flagF, S.flagB, S.ctr,
@@ -672,7 +695,7 @@ void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, d
 
 void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r, double* z, SweepState& S, int* err,
                             cudaStream_t st) {
-    const int g = sweep_grid(P.n);
+    const int g = sweep_blocks(P);
     k_fwd_f64<float, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, luf, r, nullptr, nullptr, z, P.rowSys,
                                                            nullptr, S.flagF, S.flagB, S.ctr, err);
     k_bwd_f64<float><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, luf, z, P.rowSys, nullptr, S.flagF, S.flagB, S.ctr,
@@ -681,7 +704,7 @@ void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r,
 
 void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S, int* err,
                           cudaStream_t st) {
-    const int g = sweep_grid(P.n);
+    const int g = sweep_blocks(P);
     k_fwd_f32<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, luf, r, nullptr, nullptr, y32, P.rowSys,
                                                      nullptr, S.flagF, S.flagB, S.ctr, err);
     k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, luf, y32, z, P.rowSys, nullptr, S.flagF, S.flagB,
@@ -690,7 +713,7 @@ void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, d
 
 void launch_ilu_grid_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
                         cudaStream_t st) {
-    const int g = sweep_grid(P.n);
+    const int g = sweep_blocks(P);
     if (M.kind == 0) {
         k_fwd_f64<double, IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.lu, r, nullptr, nullptr, z,
                                                                  P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
@@ -752,16 +775,16 @@ void launch_block_jacobi_apply(const DevPlan& P, const double* dinv, const doubl
 }
 
 void launch_bicg_init(const DevPlan& P, const double* b, BicgVecs& V, KScal* ks, ReduceState& R, double tol, int maxit,
-                      int* active, cudaStream_t st) {
+                      int* active, bool guard, bool onlyFailed, cudaStream_t st) {
     k_bicg_init<<<P.ntiles, kTileThreads, 0, st>>>(P.ntiles, P.nsys, P.tileRow0, P.tileSys, P.sysTile0, b, V.x, V.r, V.rh, V.p, V.v,
-                                                   ks, tol, maxit, R.part, R.done, R.sysdot, active);
+                                                   ks, tol, maxit, guard ? 1 : 0, onlyFailed ? 1 : 0, R.part, R.done, R.sysdot, active);
 }
 
 // one iteration: (a) p-update fused into M p, (c) v = A ph + <rh,v>, (d) s-update fused into M s,
 // (f) t = A sh + <t,t>, <t,s>, <s,s>, (g) x / r update + ||r||, <rh,r>
 void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M, BicgVecs& V, KScal* ks, ReduceState& R,
                            SweepState& S, int* active, int* err, cudaStream_t st) {
-    const int g = sweep_grid(P.n);
+    const int g = sweep_blocks(P);
     auto prec = [&](bool pupd, double* out) {
         if (M.cpr && M.cta) {
             launch_cpr_cta(P, M, *M.amg, pupd ? 1 : 2, M.kind != 0, V.r, pupd ? V.p : V.s, V.v, out, ks, st);

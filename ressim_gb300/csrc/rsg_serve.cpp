@@ -2,7 +2,8 @@
 //
 // Each slot is a host thread with its own solver handle (own CUDA stream, own device memory). Requests wait in
 // arrival order; the head of the queue is admitted as soon as a slot is free and its estimated device footprint
-// fits in what the admitted requests leave of the budget. Admitted requests run concurrently on their slots'
+// fits in what the admitted requests leave of the budget. A small head (one SM's worth of rows) takes the small
+// requests queued behind it along, up to 64, and the slot solves them in one block-diagonal batch. Admitted requests run concurrently on their slots'
 // streams, so a request that arrives while others are on the GPU overlaps with them on the device; its matrix,
 // factors, hierarchy and Krylov state stay resident until it completes and are then freed (stream-ordered, no
 // device-wide synchronisation). A request is solved exactly as it would be alone: its own plan, deterministic
@@ -114,9 +115,70 @@ void run_request(rsg_server* S, int slot, Request& R) {
     rsg_release(h);                                               // the request's state leaves the device
 }
 
+constexpr int kBatchRows = 65536;      // a request this small runs on one SM: batch it with its neighbours in the queue
+constexpr int kMaxBatch = 64;
+constexpr long long kMaxBatchRowsTotal = 1 << 21;
+
+// Small requests of a batch: one block-diagonal solve (every system's kernels and reductions are its own, so each
+// result is the one it has alone). Patterns the batch cannot take (CPR on a pattern that is not structurally
+// symmetric) fall back to one request at a time.
+void run_batch(rsg_server* S, int slot, std::vector<std::shared_ptr<Request>>& B) {
+    rsg_solver* h = S->handles[size_t(slot)];
+    const int ns = int(B.size());
+    const size_t nsz = static_cast<size_t>(ns);
+    std::vector<int> n(nsz);
+    std::vector<const int*> rp(nsz), ci(nsz);
+    std::vector<const double*> val(nsz);
+    std::vector<double> b, x;
+    for (int k = 0; k < ns; ++k) {
+        Request& R = *B[size_t(k)];
+        n[size_t(k)] = R.n;
+        rp[size_t(k)] = R.rp.data();
+        ci[size_t(k)] = R.ci.data();
+        val[size_t(k)] = R.val.data();
+        b.insert(b.end(), R.b.begin(), R.b.end());
+    }
+    int rc = rsg_set_batch(h, ns, rsg::NB, n.data(), rp.data(), ci.data(), val.data());
+    if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
+    if (rc != RSG_OK) {
+        rsg_release(h);
+        for (auto& R : B) run_request(S, slot, *R);
+        return;
+    }
+    x.assign(b.size(), 0.0);
+    int its = 0;
+    double rr = 0;
+    rc = rsg_solve(h, b.data(), x.data(), B[0]->tol, B[0]->maxit, &its, &rr);
+    std::vector<int> sits(nsz), sst(nsz, rc < 0 ? rc : RSG_OK);
+    std::vector<double> srr(nsz), strue(nsz, -1.0);
+    if (rc >= 0) {
+        rsg_batch_results(h, sits.data(), srr.data(), strue.data());
+        rsg_batch_status(h, sst.data());
+    }
+    rsg_stats st{};
+    rsg_get_stats(h, &st);
+    size_t off = 0;
+    for (int k = 0; k < ns; ++k) {
+        Request& R = *B[size_t(k)];
+        const size_t N = R.b.size();
+        R.x.assign(x.begin() + long(off), x.begin() + long(off + N));
+        off += N;
+        R.res.status = sst[size_t(k)];
+        R.res.iterations = sits[size_t(k)];
+        R.res.rel_residual = srr[size_t(k)];
+        R.res.true_rel_residual = strue[size_t(k)];
+        R.res.device_bytes = st.device_bytes;
+        R.res.precond = S->opt.precond;
+        R.res.slot = slot;
+        R.res.batch = ns;
+    }
+    rsg_release(h);
+}
+
 void worker(rsg_server* S, int slot) {
     for (;;) {
-        std::shared_ptr<Request> R;
+        std::vector<std::shared_ptr<Request>> B;
+        size_t est = 0;
         {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cvWork.wait(lk, [&] {
@@ -126,25 +188,47 @@ void worker(rsg_server* S, int slot) {
                 return S->budget == 0 || S->inUse + e <= S->budget || S->running == 0;
             });
             if (S->stop) return;
-            R = S->queue.front();
+            B.push_back(S->queue.front());
             S->queue.pop_front();
-            S->inUse += R->est;
-            ++S->running;
+            est = B[0]->est;
+            if (B[0]->n <= kBatchRows) {                         // gather the small requests queued behind it
+                long long rows = B[0]->n;
+                while (!S->queue.empty() && int(B.size()) < kMaxBatch) {
+                    const auto& F = S->queue.front();
+                    if (F->n > kBatchRows || F->tol != B[0]->tol || F->maxit != B[0]->maxit || rows + F->n > kMaxBatchRowsTotal) break;
+                    if (S->budget && S->inUse + est + F->est > S->budget) break;
+                    rows += F->n;
+                    est += F->est;
+                    B.push_back(F);
+                    S->queue.pop_front();
+                }
+            }
+            S->inUse += est;
+            S->running += int(B.size());
         }
         S->cvWork.notify_all();                                   // the next head may fit as well
-        R->tStart = Clock::now();
-        run_request(S, slot, *R);
-        R->tEnd = Clock::now();
-        R->res.queue_ms = ms_between(R->tSubmit, R->tStart);
-        R->res.run_ms = ms_between(R->tStart, R->tEnd);
-        R->res.total_ms = ms_between(R->tSubmit, R->tEnd);
-        R->res.start_ms = ms_between(S->t0, R->tStart);
-        R->res.end_ms = ms_between(S->t0, R->tEnd);
+        const Clock::time_point t0 = Clock::now();
+        if (B.size() == 1) {
+            run_request(S, slot, *B[0]);
+            B[0]->res.batch = 1;
+        } else {
+            run_batch(S, slot, B);
+        }
+        const Clock::time_point t1 = Clock::now();
+        for (auto& R : B) {
+            R->tStart = t0;
+            R->tEnd = t1;
+            R->res.queue_ms = ms_between(R->tSubmit, t0);
+            R->res.run_ms = ms_between(t0, t1);
+            R->res.total_ms = ms_between(R->tSubmit, t1);
+            R->res.start_ms = ms_between(S->t0, t0);
+            R->res.end_ms = ms_between(S->t0, t1);
+        }
         {
             std::lock_guard<std::mutex> lk(S->mu);
-            S->inUse -= R->est;
-            --S->running;
-            R->done = true;
+            S->inUse -= est;
+            S->running -= int(B.size());
+            for (auto& R : B) R->done = true;
         }
         S->cvDone.notify_all();
         S->cvWork.notify_all();

@@ -1183,11 +1183,6 @@ int grid_for(long long n, int threads) {
     const long long b = (n + threads - 1) / threads, cap = 16LL * device_sm_count();
     return int(b < 1 ? 1 : (b < cap ? b : cap));
 }
-// persistent sweep grid: a warp per 32 rows, at most 8 blocks of 4 warps per SM
-int gs_grid(int n) {
-    const int blocks = ((n + 31) / 32 + 3) / 4, cap = 8 * device_sm_count();
-    return blocks < 1 ? 1 : (blocks < cap ? blocks : cap);
-}
 
 // input (the fused Krylov update of the mode), T = input (FP64), level-0 right-hand side b0 = w . input
 // (bsr.cpp:1064-1067; TT: the arithmetic of the restriction, FP32 in the all-FP32 form)
@@ -1221,7 +1216,7 @@ __global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ 
 // coarsest skip); phase 1: the symmetric GS solve of a coarsest level without dense LU. ZERO: pre-smoothing from
 // x = 0 (the terms of the neighbours not yet updated vanish and are not read). Flags of skipped rows are set all
 // the same: after every forward sweep of a (level, phase) all its flags are 1, after every backward sweep 0.
-template <class TA, bool FWD, bool ZERO>
+template <class TA, bool FWD, bool ZERO, bool POS>
 __global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int maxL, int phase, const int* __restrict__ rowLv,
                                                           const AmgSysLv* __restrict__ lv, const int* __restrict__ gsRows,
                                                           const int* __restrict__ wave, const int* __restrict__ rp,
@@ -1248,19 +1243,23 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int ma
                 const int p0 = __ldg(rp + rpOff + k), p1 = __ldg(rp + rpOff + k + 1), pd = __ldg(diag + row);
                 const int* cl = ci + entOff;
                 const TA* vl = val + entOff;
-                const int wi = __ldg(wave + row);
-                // the neighbours updated before this row in the sweep: of an earlier wave (forward), a later one (backward)
+                const int wi = POS ? 0 : __ldg(wave + row);
+                // the neighbours updated before this row in the sweep: of an earlier wave (forward), a later one
+                // (backward); POS: the entries before (after) the diagonal, which the plan checked to be the same
                 auto dep = [&](int p) {
                     if (p == pd) return false;
+                    if (POS) return FWD ? p < pd : p > pd;
                     const int w = __ldg(wave + rowOff + __ldg(cl + p));
                     return FWD ? w < wi : w > wi;
                 };
-                wait_deps(flag, p0, p1, FWD ? 1 : 0, err, [&](int p) { return rowOff + __ldg(cl + p); }, dep);
+                const int w0 = POS ? (FWD ? p0 : pd + 1) : p0, w1 = POS ? (FWD ? pd : p1) : p1;
+                wait_deps(flag, w0, w1, FWD ? 1 : 0, err, [&](int p) { return rowOff + __ldg(cl + p); }, dep);
                 TA s = b[row];
-                for (int p = p0; p < p1; ++p) {
+                const int e1 = (FWD && ZERO && POS) ? pd : p1;         // from zero: only the updated neighbours count
+                for (int p = p0; p < e1; ++p) {
                     if (p == pd) continue;
                     const int j = rowOff + __ldg(cl + p);
-                    if (FWD && ZERO && __ldg(wave + j) > wi) continue;   // x_j is still zero: the term vanishes
+                    if (FWD && ZERO && !POS && __ldg(wave + j) > wi) continue;   // x_j is still zero: the term vanishes
                     s = asub(s, amul(__ldg(vl + p), x[j]));
                 }
                 x[row] = adiv(s, __ldg(vl + pd));
@@ -1270,34 +1269,62 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int ma
     }
 }
 
-// one colour of a multicolour Gauss-Seidel sweep of level l over every system (FP32 forms): the positions
-// cpos[i0, i1) hold the colour's rows, which are independent, so this is a plain parallel pass. ZERO: pre-smoothing
-// from x = 0 (the terms of later colours vanish and are not read).
+// Multicolour Gauss-Seidel (FP32 forms) on the colour-major row descriptors {row, first entry, end, diagonal}:
+// the rows of a colour are independent. ZERO: pre-smoothing from x = 0 (the terms of later colours vanish and are
+// not read).
 template <class TA, bool ZERO>
-__global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, const int* __restrict__ cpos, const int* __restrict__ rowLv,
-                                                   const AmgSysLv* __restrict__ lv, const int* __restrict__ gsRows,
-                                                   const int* __restrict__ wave, const int* __restrict__ rp, const int* __restrict__ ci,
-                                                   const TA* __restrict__ val, const int* __restrict__ diag, const TA* b, TA* x,
-                                                   const KScal* ks) {
+__device__ __forceinline__ void gs_colour_row(const int4 d, const int* __restrict__ gci, const TA* __restrict__ val,
+                                              const int* __restrict__ wave, const TA* b, TA* x) {
+    const int wi = ZERO ? __ldg(wave + d.x) : 0;
+    TA s = b[d.x];
+    for (int p = d.y; p < d.z; ++p) {
+        if (p == d.w) continue;
+        const int j = __ldg(gci + p);
+        if (ZERO && __ldg(wave + j) > wi) continue;
+        s = asub(s, amul(__ldg(val + p), x[j]));
+    }
+    x[d.x] = adiv(s, __ldg(val + d.w));
+}
+// one large colour: a parallel pass over the descriptors [i0, i1)
+template <class TA, bool ZERO>
+__global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, const int4* __restrict__ cdesc, const int* __restrict__ gci,
+                                                   const TA* __restrict__ val, const int* __restrict__ wave, const int* __restrict__ rowLv,
+                                                   const TA* b, TA* x, const KScal* ks) {
     for (int i = i0 + int(blockIdx.x * blockDim.x + threadIdx.x); i < i1; i += int(gridDim.x * blockDim.x)) {
-        const int g = __ldg(cpos + i);
-        const int sl = __ldg(rowLv + g);
-        const AmgSysLv* A = lv + sl;
-        if (__ldg(&A->coarse) || (ks && ks[sl / maxL].status != ST_RUNNING)) continue;
-        const int rowOff = __ldg(&A->rowOff), k = __ldg(gsRows + g), row = rowOff + k;
-        const int rpOff = __ldg(&A->rpOff), entOff = __ldg(&A->entOff);
-        const int p0 = __ldg(rp + rpOff + k), p1 = __ldg(rp + rpOff + k + 1), pd = __ldg(diag + row);
-        const int* cl = ci + entOff;
-        const TA* vl = val + entOff;
-        const int wi = ZERO ? __ldg(wave + row) : 0;
-        TA s = b[row];
-        for (int p = p0; p < p1; ++p) {
-            if (p == pd) continue;
-            const int j = rowOff + __ldg(cl + p);
-            if (ZERO && __ldg(wave + j) > wi) continue;
-            s = asub(s, amul(__ldg(vl + p), x[j]));
+        const int4 d = __ldg(cdesc + i);
+        if (ks && ks[__ldg(rowLv + d.x) / maxL].status != ST_RUNNING) continue;
+        gs_colour_row<TA, ZERO>(d, gci, val, wave, b, x);
+    }
+}
+// the small colours [c0, c1) of a level, one after another in one thread block (ascending forward, descending
+// backward), a barrier between colours
+// (a warp per row: the rows of the small colours are the long rows of the well cliques; the lanes split the
+// entries and the partial sums meet in a fixed shuffle tree)
+template <class TA, bool ZERO>
+__global__ void __launch_bounds__(256) k_gs_tail(const int* __restrict__ cb, int c0, int c1, int fwd, int maxL,
+                                                 const int4* __restrict__ cdesc, const int* __restrict__ gci, const TA* __restrict__ val,
+                                                 const int* __restrict__ wave, const int* __restrict__ rowLv, const TA* b, TA* x,
+                                                 const KScal* ks) {
+    const int lane = int(threadIdx.x & 31), wid = int(threadIdx.x >> 5), nw = int(blockDim.x >> 5);
+    for (int cc = 0; cc < c1 - c0; ++cc) {
+        const int c = fwd ? c0 + cc : c1 - 1 - cc;
+        const int i1 = __ldg(cb + c + 1);
+        for (int i = __ldg(cb + c) + wid; i < i1; i += nw) {
+            const int4 d = __ldg(cdesc + i);
+            if (ks && ks[__ldg(rowLv + d.x) / maxL].status != ST_RUNNING) continue;
+            const int wi = ZERO ? __ldg(wave + d.x) : 0;
+            TA t = TA(0);
+            for (int p = d.y + lane; p < d.z; p += 32) {
+                if (p == d.w) continue;
+                const int j = __ldg(gci + p);
+                if (ZERO && __ldg(wave + j) > wi) continue;
+                t = aadd(t, amul(__ldg(val + p), x[j]));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t = aadd(t, __shfl_xor_sync(0xffffffffu, t, o));
+            if (lane == 0) x[d.x] = adiv(asub(b[d.x], t), __ldg(val + d.w));
         }
-        x[row] = adiv(s, __ldg(vl + pd));
+        __syncthreads();
     }
 }
 
@@ -1322,10 +1349,14 @@ __global__ void __launch_bounds__(256) k_gcpr_restrict(int c0, int c1, int maxL,
         const int* fci = ci + __ldg(&F->entOff);
         const TA* fv = val + __ldg(&F->entOff);
         TA t = TA(0);
-        for (int q = __ldg(mp + I); q < __ldg(mp + I + 1); ++q) {
+        const int q1 = __ldg(mp + I + 1);
+#pragma unroll 2
+        for (int q = __ldg(mp + I); q < q1; ++q) {
             const int m = __ldg(mm + q);
+            const int pe = __ldg(frp + m + 1);
             TA acc = TA(0);
-            for (int p = __ldg(frp + m); p < __ldg(frp + m + 1); ++p) acc = aadd(acc, amul(__ldg(fv + p), x[fOff + __ldg(fci + p)]));
+#pragma unroll 4
+            for (int p = __ldg(frp + m); p < pe; ++p) acc = aadd(acc, amul(__ldg(fv + p), x[fOff + __ldg(fci + p)]));
             t = aadd(t, asub(b[fOff + m], acc));
         }
         b[c] = t;
@@ -1409,34 +1440,56 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
     const auto& LB = G.levelRowBeg;
     auto sweep = [&](int l, int phase, bool fwd, bool zero) {
         const std::vector<int>& cb = G.colBeg[size_t(l)];
-        if (phase == 0 && cb.size() > 1) {                 // multicolour: a parallel pass per colour
-            const int nc = int(cb.size()) - 1;
-            for (int cc = 0; cc < nc; ++cc) {
-                const int c = fwd ? cc : nc - 1 - cc;
+        if (phase == 0 && cb.size() > 1) {                 // multicolour: a parallel pass per large colour, the small ones in one block
+            const int nc = int(cb.size()) - 1, tail = G.colTail[size_t(l)];
+            const int* cbd = G.cbeg + G.cbegOff[size_t(l)];
+            auto big = [&](int c) {
                 const int i0 = cb[size_t(c)], i1 = cb[size_t(c) + 1];
                 if (zero)
-                    k_gs_colour<TA, true><<<grid_for(i1 - i0, 256), 256, 0, st>>>(i0, i1, G.maxL, G.cpos, G.rowLv, G.lv, G.gsRows, G.wave,
-                                                                                 G.rp, G.ci, val, G.diag, C.b, C.x, ks);
+                    k_gs_colour<TA, true><<<grid_for(i1 - i0, 256), 256, 0, st>>>(i0, i1, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
+                                                                                 C.x, ks);
                 else
-                    k_gs_colour<TA, false><<<grid_for(i1 - i0, 256), 256, 0, st>>>(i0, i1, G.maxL, G.cpos, G.rowLv, G.lv, G.gsRows, G.wave,
-                                                                                  G.rp, G.ci, val, G.diag, C.b, C.x, ks);
+                    k_gs_colour<TA, false><<<grid_for(i1 - i0, 256), 256, 0, st>>>(i0, i1, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv,
+                                                                                  C.b, C.x, ks);
                 ++launches;
+            };
+            auto small = [&]() {
+                if (tail >= nc) return;
+                if (zero)
+                    k_gs_tail<TA, true><<<1, 256, 0, st>>>(cbd, tail, nc, fwd ? 1 : 0, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
+                                                          C.x, ks);
+                else
+                    k_gs_tail<TA, false><<<1, 256, 0, st>>>(cbd, tail, nc, fwd ? 1 : 0, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
+                                                           C.x, ks);
+                ++launches;
+            };
+            if (fwd) {
+                for (int c = 0; c < tail; ++c) big(c);
+                small();
+            } else {
+                small();
+                for (int c = tail - 1; c >= 0; --c) big(c);
             }
             return;
         }
         const int q0 = LB[size_t(l)], q1 = LB[size_t(l) + 1];
         int* flag = G.gsFlag + size_t(phase) * size_t(G.totRows);
         unsigned* ctr = G.gsCtr + 4 * l + 2 * phase;
-        const int g = gs_grid(q1 - q0);
-        if (fwd && zero)
-            k_gs_grid<TA, true, true><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp, G.ci,
-                                                                       val, G.diag, C.b, C.x, flag, ctr, ks, err);
-        else if (fwd)
-            k_gs_grid<TA, true, false><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp, G.ci,
-                                                                        val, G.diag, C.b, C.x, flag, ctr, ks, err);
-        else
-            k_gs_grid<TA, false, false><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp, G.ci,
-                                                                         val, G.diag, C.b, C.x, flag, ctr, ks, err);
+        const int g = G.gsBlocks[size_t(l)];
+        auto go = [&](auto pos) {
+            constexpr bool POS = decltype(pos)::value;
+            if (fwd && zero)
+                k_gs_grid<TA, true, true, POS><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp,
+                                                                            G.ci, val, G.diag, C.b, C.x, flag, ctr, ks, err);
+            else if (fwd)
+                k_gs_grid<TA, true, false, POS><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp,
+                                                                             G.ci, val, G.diag, C.b, C.x, flag, ctr, ks, err);
+            else
+                k_gs_grid<TA, false, false, POS><<<g, kGridThreads, 0, st>>>(q0, q1, G.maxL, phase, G.rowLv, G.lv, G.gsRows, G.wave, G.rp,
+                                                                              G.ci, val, G.diag, C.b, C.x, flag, ctr, ks, err);
+        };
+        if (G.posOrder) go(std::true_type());
+        else go(std::false_type());
         ++launches;
     };
     for (int l = 0; l + 1 < G.maxL; ++l) {                 // pre-smoothing and restriction, finest to coarsest

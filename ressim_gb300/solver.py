@@ -36,7 +36,8 @@ class DeviceSolver:
 
     def __init__(self, precond: str = "bilu0", krylov: str = "bicgstab", precision: str = "fp64", restart: int = 40,
                  check_every: int = 4, use_graphs: bool = True, device: int = 0, mem_budget: int = 0,
-                 gmres_fallback: bool = False, sweep: str = "auto", fma: bool = True):
+                 gmres_fallback: bool = False, sweep: str = "auto", fma: bool = True,
+                 sweep_inflight: int = 0):
         self.L = _lib.load()
         o = _lib.Options()
         self.L.rsg_default_options(C.byref(o))
@@ -51,6 +52,7 @@ class DeviceSolver:
         o.gmres_fallback = 1 if gmres_fallback else 0
         o.fma = 1 if fma else 0
         o.sweep = _lib.SWEEP[sweep]
+        o.sweep_inflight = sweep_inflight
         self.opts = o
         h = C.c_void_p()
         _lib.check(self.L.rsg_create(C.byref(h), C.byref(o)))

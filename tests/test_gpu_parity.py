@@ -365,6 +365,45 @@ def test_cpr_single_large_system(precision, oracle):
     assert res.converged and true_res(A, x, s.b) <= 1e-5
 
 
+def _hard_request():
+    """A serving request with extreme permeability contrast (sigma ln k near 3) on which the all-FP32 preconditioner
+    diverges (60,372 cells): the tenth of the stratified serving pool."""
+    from ressim_gb300 import synth
+    rng = np.random.default_rng(4242)
+    for i in range(10):
+        cells = 1e3 * 1000.0 ** ((i + 0.5) / 16)
+        s = synth.serving_request(rng, cells_lo=cells, cells_hi=cells)
+    return s
+
+
+def test_precision_escalation():
+    """All-FP32 preconditioner on a system where its FP32 sweeps diverge: the divergence guard stops it, the system
+    is solved again with FP64 sweep vectors and converges to the true residual; in a batch, the easy system that
+    converged in FP32 keeps exactly the result it has alone."""
+    hard = _hard_request()
+    easy = load_golden("waterflood_sys1.npz")
+    with dev(precond="cpr", precision="mixed_f32") as d:
+        d.set_matrix(hard.A)
+        d.setup()
+        x, res = d.solve(hard.b, tol=1e-6, maxit=500)
+        assert d.stats().escalated_systems == 1
+    assert res.converged and true_res(hard.A, x, hard.b) <= 1e-5
+    with dev(precond="cpr", precision="mixed_f32") as d:
+        d.set_matrix(easy[0])
+        d.setup()
+        xe, re_ = d.solve(easy[1]["b"], tol=1e-6, maxit=500)
+        assert d.stats().escalated_systems == 0
+    with dev(precond="cpr", precision="mixed_f32") as d:
+        d.set_batch([easy[0], hard.A])
+        d.setup()
+        xb, rb = d.solve(np.concatenate([easy[1]["b"], hard.b]), tol=1e-6, maxit=500)
+        its, rr, tr = d.batch_results()
+        assert d.stats().escalated_systems == 1
+    Ne = easy[0].n * 3
+    assert np.array_equal(xb[:Ne], xe) and its[0] == re_.iterations
+    assert true_res(hard.A, xb[Ne:], hard.b) <= 1e-5
+
+
 # ---------------------------------------------------------------- GMRES (flexible, restarted; linsolve.cpp:218-273)
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS + ["singular_pivots.npz"])
 def test_gmres_bilu0_matches_reference(name):

@@ -29,7 +29,7 @@ def test_result_is_the_same_alone_and_in_the_mix(precond, precision):
     with Server(slots=4, precond=precond, precision=precision) as s:
         ids = [s.submit(r.A, r.b, tol=1e-6, maxit=500) for r in reqs]       # all arrive while others run
         mix = [s.poll(i) for i in ids]
-    slots, conv = set(), 0
+    slots, conv, shared = set(), 0, 0
     for r, (xa, ra), (xm, rm) in zip(reqs, alone, mix):
         # same status, iterations and iterate bit for bit (also for a request that does not converge: the generator
         # draws some that FP64 CPR / BILU0 with BiCGSTAB or GMRES cannot solve either, e.g. the second one here)
@@ -39,8 +39,26 @@ def test_result_is_the_same_alone_and_in_the_mix(precond, precision):
             assert true_res(r.A, xm, r.b) <= 1e-5
             conv += 1
         slots.add(rm["slot"])
+        shared += rm["batch"] > 1
     assert conv >= 5
-    assert len(slots) > 1                                               # the mix really ran on several slots
+    assert len(slots) > 1 or shared > 1                                 # the mix really shared the device
+
+
+def test_small_requests_are_batched():
+    """Small requests queued together are solved in one block-diagonal launch; each result is bit for bit the one it
+    has alone, and the batch really formed."""
+    from ressim_gb300.solver import Server
+    reqs = requests(8, seed=21, lo=1e3, hi=1.5e4)
+    with Server(slots=1, precond="cpr", precision="mixed_f32") as s:
+        alone = [s.poll(s.submit(r.A, r.b, tol=1e-6, maxit=500)) for r in reqs]
+    with Server(slots=1, precond="cpr", precision="mixed_f32") as s:
+        ids = [s.submit(r.A, r.b, tol=1e-6, maxit=500) for r in reqs]
+        mix = [s.poll(i) for i in ids]
+    assert max(rm["batch"] for _, rm in mix) > 1
+    for (xa, ra), (xm, rm) in zip(alone, mix):
+        assert ra["batch"] == 1
+        assert ra["status"] == rm["status"] and ra["iterations"] == rm["iterations"]
+        assert np.array_equal(xa, xm, equal_nan=True)
 
 
 def test_admission_respects_the_budget():
