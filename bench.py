@@ -202,12 +202,12 @@ def serving_leg(local, pool, arrivals, precision):
         T = time.perf_counter() - t0
     lat = np.array([r["total_ms"] for r, _ in res])
     ok = [r["status"] == 0 and 0 <= r["true_rel_residual"] <= TOL for r, _ in res]
-    big = [r for r, k in res if pool[k].A.n > 65536]
     return {"throughput": len(res) / T, "unit": "solves/s", "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "mean_run_ms": float(np.mean([r["run_ms"] for r, _ in res])),
             "converged": int(sum(ok)), "requests": len(res), "max_submit_lag_ms": 1e3 * late,
             "cells_per_s": float(sum(pool[k].A.n for _, k in res) / T),
-            "over_64k_rows_precond": sorted({int(r["precond"]) for r in big})}
+            "batched_requests": int(sum(r["batch"] > 1 for r, _ in res)),
+            "mean_batch": float(np.mean([r["batch"] for r, _ in res]))}
 
 
 def run_reference(args, rank, world):
@@ -273,7 +273,7 @@ def main():
     from ressim_gb300.solver import DeviceSolver
 
     serving = None
-    if args.serving != "off":
+    if args.serving != "off" and world == 1:               # the serving stream is a one-GPU measurement
         pool = serving_pool()
         arr = serving_arrivals()
         serving = {"rate_per_s": SERVE_RATE, "requests": SERVE_N, "pool": SERVE_POOL, "slots": SERVE_SLOTS,

@@ -234,6 +234,7 @@ int check_device_errors(rsg_solver* h) {
         cudaMemsetAsync(h->S.flagB, 0, sizeof(int) * size_t(h->plan.n), h->stream);
         cudaMemsetAsync(h->S.ctr, 0, sizeof(unsigned) * 4, h->stream);
         cudaMemsetAsync(h->R.done, 0, sizeof(unsigned), h->stream);
+        if (h->V.yt) cudaMemsetAsync(h->V.yt, 0, size_t(h->plan.n) * NB * sizeof(unsigned long long), h->stream);
         if (h->amg.gsFlag) {
             cudaMemsetAsync(h->amg.gsFlag, 0, 2 * size_t(std::max(h->amg.totRows, 1)) * sizeof(int), h->stream);
             cudaMemsetAsync(h->amg.gsCtr, 0, 4 * size_t(std::max(h->amg.maxL, 1)) * sizeof(unsigned), h->stream);
@@ -259,6 +260,7 @@ PrecDev prec_dev(rsg_solver* h) {
     else { M.kind = 0; M.lu = h->lu; }
     M.val = h->val;
     M.y32 = h->V.y32;
+    M.yt = h->V.yt;
     if (h->opt.precond == RSG_PREC_CPR && h->haveAmg) { M.cpr = true; M.amg = &h->amg; }
     if (M.kind != 2 && h->cta) {
         M.smem = cta_sweep_smem(h->dp, M.kind == 3);
@@ -344,6 +346,10 @@ int ensure_precond_storage(rsg_solver* h) {
         if (!h->luf && (rc = dalloc(h->pmem, &h->luf, E))) return rc;
         if (!h->work && (rc = dalloc(h->pmem, &h->work, E))) return rc;
         if (h->opt.precision == RSG_MIXED_F32 && !h->V.y32 && (rc = dalloc(h->pmem, &h->V.y32, size_t(h->plan.n) * NB))) return rc;
+        if (h->opt.precision == RSG_MIXED_F32 && !h->V.yt) {
+            if ((rc = dalloc(h->pmem, &h->V.yt, size_t(h->plan.n) * NB))) return rc;
+            RSG_CUDA(cudaMemsetAsync(h->V.yt, 0, size_t(h->plan.n) * NB * sizeof(unsigned long long), h->stream));
+        }
         if (h->cta && !h->s32.L && (rc = alloc_split(h, h->s32))) return rc;
     } else {
         if (!h->lu && (rc = dalloc(h->pmem, &h->lu, E))) return rc;
@@ -1154,7 +1160,7 @@ static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
     else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
     else if (M.kind == 1) { launch_ilu_apply_mixed(h->dp, h->luf, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
-    else if (M.kind == 3) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.y32, h->S, h->d_err, h->stream); h->launches += 2; }
+    else if (M.kind == 3) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.yt, h->S, h->d_err, h->stream); h->launches += 2; }
     else { launch_block_jacobi_apply(h->dp, h->dinv, d_r, d_z, h->stream); h->launches += 1; }
     RSG_CUDA(cudaGetLastError());
     return RSG_OK;

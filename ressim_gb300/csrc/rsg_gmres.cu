@@ -339,7 +339,7 @@ void launch_precond_gm(const DevPlan& P, const PrecDev& M, const double* r, doub
     else if (M.cta) launch_ilu_cta_apply_ks(P, M, r, z, ks, st);
     else if (M.kind == 0) launch_ilu_apply_f64(P, M.lu, r, z, S, err, st);
     else if (M.kind == 1) launch_ilu_apply_mixed(P, M.luf, r, z, S, err, st);
-    else if (M.kind == 3) launch_ilu_apply_f32(P, M.luf, r, z, M.y32, S, err, st);
+    else if (M.kind == 3) launch_ilu_apply_f32(P, M.luf, r, z, M.yt, S, err, st);
     else launch_block_jacobi_apply(P, M.dinv, r, z, st);
 }
 

@@ -263,7 +263,7 @@ void launch_factor_lean(const DevPlan& P, const double* val, float* luf, double*
 // z = U^-1 L^-1 r (FP64 factors, FP64 vectors) or with FP32 factors / FP32 vectors and accumulation.
 void launch_ilu_apply_f64(const DevPlan& P, const double* lu, const double* r, double* z, SweepState& S, int* err,
                           cudaStream_t st);
-void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S,
+void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, unsigned long long* yt, SweepState& S,
                           int* err, cudaStream_t st);
 // FP32 factors, FP64 vector and accumulation (the reference's float-factor sweeps)
 void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r, double* z, SweepState& S, int* err,
@@ -281,7 +281,8 @@ void launch_block_jacobi_apply(const DevPlan& P, const double* dinv, const doubl
 // BiCGSTAB building blocks (per-system scalars on the device).
 struct BicgVecs {
     double *x, *r, *rh, *p, *v, *s, *t, *ph, *sh;
-    float* y32;                       // FP32 sweep intermediate (mixed precision)
+    float* y32;                       // FP32 sweep intermediate of the thread-block sweeps (systems that do not fit on chip)
+    unsigned long long* yt;           // the grid-wide all-FP32 sweeps' vector: tagged words {float, sweep tag}
 };
 void launch_bicg_init(const DevPlan& P, const double* b, BicgVecs& V, KScal* ks, ReduceState& R, double tol, int maxit,
                       int* active, bool guard, bool onlyFailed,
@@ -299,6 +300,7 @@ struct PrecDev {
     SplitFactors<float> s32;
     size_t smem = 0;                  // dynamic shared memory of the CTA sweep (systems whose vector fits keep it there)
     float* y32 = nullptr;             // all-FP32 sweep vector in global memory (systems that do not fit on chip)
+    unsigned long long* yt = nullptr; // grid-wide all-FP32 sweeps: tagged sweep vector
     bool cpr = false;                 // CPR two-stage preconditioner (AMG on the pressure system + BILU0)
     const DevAmg* amg = nullptr;
 };

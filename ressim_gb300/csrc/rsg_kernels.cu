@@ -135,6 +135,31 @@ __device__ __forceinline__ void ldf9(const float* p, double* a) {
     for (int e = 0; e < 9; ++e) a[e] = double(__ldg(p + e));
 }
 
+// yi -= sum_p B_p y_col(p) over the entries [p0, p1) of a row, in order (FP64 explicitly rounded, the reference's
+// sweep arithmetic). Four blocks at a time: their factor blocks are loaded before the wait (read-only: they need
+// not wait for anything), the four dependency flags are polled together, then one acquire fence and the values.
+template <class TF>
+__device__ __forceinline__ void sub_flagged(double (&yi)[3], const int* __restrict__ col, const TF* __restrict__ lu, int p0, int p1,
+                                            const double* y, const int* flag, int* err) {
+    for (int q = p0; q < p1; q += 4) {
+        const int q1 = q + 4 < p1 ? q + 4 : p1;
+        double a[4][9];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (q + u < q1) ldf9(lu + size_t(q + u) * 9, a[u]);
+        wait_cols(flag, col, q, q1, 1, err);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (q + u >= q1) break;
+            const int k = __ldg(col + q + u);
+            const double yk[3] = {y[size_t(k) * 3 + 0], y[size_t(k) * 3 + 1], y[size_t(k) * 3 + 2]};
+            yi[0] = ds(yi[0], dot3(a[u], yk));
+            yi[1] = ds(yi[1], dot3(a[u] + 3, yk));
+            yi[2] = ds(yi[2], dot3(a[u] + 6, yk));
+        }
+    }
+}
+
 template <class TF, int MODE>
 __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                           const int* __restrict__ diag, const int* __restrict__ ford,
@@ -177,17 +202,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f64(int n, const int* __r
                 for (int e = 0; e < 3; ++e) yi[e] = r[size_t(i) * 3 + e];
             }
             if (run) {
-                const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
-                wait_cols(flagF, col, r0, d, 1, err);
-                for (int p = r0; p < d; ++p) {
-                    const int k = __ldg(col + p);
-                    double a[9], yk[3];
-                    ldf9(lu + size_t(p) * 9, a);
-                    yk[0] = y[size_t(k) * 3 + 0]; yk[1] = y[size_t(k) * 3 + 1]; yk[2] = y[size_t(k) * 3 + 2];
-                    yi[0] = ds(yi[0], dot3(a, yk));
-                    yi[1] = ds(yi[1], dot3(a + 3, yk));
-                    yi[2] = ds(yi[2], dot3(a + 6, yk));
-                }
+                sub_flagged(yi, col, lu, __ldg(rowPtr + i), __ldg(diag + i), y, flagF, err);
             }
             y[size_t(i) * 3 + 0] = yi[0]; y[size_t(i) * 3 + 1] = yi[1]; y[size_t(i) * 3 + 2] = yi[2];
             flagB[i] = 0;
@@ -213,19 +228,10 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __r
             const int i = __ldg(bord + idx);
             if (sys_running(ks, rowSys, i)) {
                 double yi[3] = {y[size_t(i) * 3 + 0], y[size_t(i) * 3 + 1], y[size_t(i) * 3 + 2]};
-                const int d = __ldg(diag + i), r1 = __ldg(rowPtr + i + 1);
-                wait_cols(flagB, col, d + 1, r1, 1, err);
-                for (int p = d + 1; p < r1; ++p) {
-                    const int j = __ldg(col + p);
-                    double a[9], zj[3];
-                    ldf9(lu + size_t(p) * 9, a);
-                    zj[0] = y[size_t(j) * 3 + 0]; zj[1] = y[size_t(j) * 3 + 1]; zj[2] = y[size_t(j) * 3 + 2];
-                    yi[0] = ds(yi[0], dot3(a, zj));
-                    yi[1] = ds(yi[1], dot3(a + 3, zj));
-                    yi[2] = ds(yi[2], dot3(a + 6, zj));
-                }
+                const int d = __ldg(diag + i);
                 double D[9];
                 ldf9(lu + size_t(d) * 9, D);
+                sub_flagged(yi, col, lu, d + 1, __ldg(rowPtr + i + 1), y, flagB, err);
                 y[size_t(i) * 3 + 0] = dot3(D, yi);
                 y[size_t(i) * 3 + 1] = dot3(D + 3, yi);
                 y[size_t(i) * 3 + 2] = dot3(D + 6, yi);
@@ -236,14 +242,85 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f64(int n, const int* __r
     }
 }
 
-// FP32 factors, FP32 vectors and accumulation (BILU0f, engine/src/bsr.cpp:1100-1121); y32 holds the float
-// intermediate, the result is written to z in double.
+// FP32 factors, FP32 vectors and accumulation (BILU0f, engine/src/bsr.cpp:1100-1121), the result written to z in
+// double. The sweep vector is a tagged word per component: {float value, sweep tag} in 64 bits (tag 1 once the
+// forward sweep wrote it, 2 once the backward sweep did). A 64-bit access is single-copy atomic, so a poll that
+// sees the tag already holds the value: a dependency costs one round trip, with no flag, no fence and no second
+// load. Every row is written by both sweeps (rows of systems that are not running carry their value along), so
+// the tags alternate and a word never shows the awaited tag before its new value.
+constexpr unsigned kTagF = 1u, kTagB = 2u;
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_word(unsigned long long* p, float v, unsigned tag) {
+    const unsigned long long w = (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(w) : "memory");
+}
+__device__ __forceinline__ float word_val(unsigned long long w) { return __uint_as_float(unsigned(w & 0xffffffffull)); }
+__device__ __forceinline__ bool word_has(unsigned long long w, unsigned tag) { return unsigned(w >> 32) == tag; }
+// yi -= sum_p B_p y_col(p) over the entries [p0, p1) of a row (in order). The y words of four blocks are awaited
+// together: every poll round re-issues the loads of all words still without the tag (one round trip per round),
+// a short busy phase, then back-off up to 256 ns, bounded (ERR_TIMEOUT).
+__device__ __forceinline__ void sub_tagged(float (&yi)[3], const int* __restrict__ col, const float* __restrict__ lu, int p0, int p1,
+                                           const unsigned long long* y, unsigned tag, int* err) {
+    for (int q = p0; q < p1; q += 4) {
+        int k[4];
+        unsigned long long w[4][3];
+        float a[4][9];                                            // the factor blocks, loaded before the wait
+        unsigned pending = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            k[u] = q + u < p1 ? __ldg(col + q + u) : -1;
+            if (k[u] >= 0) pending |= 7u << (3 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[u][e] = k[u] >= 0 ? __ldg(lu + size_t(q + u) * 9 + e) : 0.f;
+        unsigned ns = 0;
+        for (unsigned it = 0; pending; ++it) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int e = 0; e < 3; ++e)
+                    if ((pending >> (3 * u + e)) & 1u) w[u][e] = ld_word(y + size_t(k[u]) * 3 + e);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int e = 0; e < 3; ++e)
+                    if (((pending >> (3 * u + e)) & 1u) && word_has(w[u][e], tag)) pending &= ~(1u << (3 * u + e));
+            if (!pending) break;
+            if (it >= 64) {
+                __nanosleep(ns);
+                ns = ns < 32 ? 32 : (ns < 256 ? 2 * ns : 256);
+                if (it >= 64 + kSpinLimit) { atomicOr(err, ERR_TIMEOUT); break; }
+                if ((it & 255u) == 255u && *(volatile int*)err != 0) break;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (k[u] < 0) break;
+            const float y0 = word_val(w[u][0]), y1 = word_val(w[u][1]), y2 = word_val(w[u][2]);
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                float s = 0.f;
+                s += a[u][e * 3 + 0] * y0;
+                s += a[u][e * 3 + 1] * y1;
+                s += a[u][e * 3 + 2] * y2;
+                yi[e] -= s;
+            }
+        }
+    }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kSweepThreads) k_fwd_f32(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                           const int* __restrict__ diag, const int* __restrict__ ford,
                                                           const float* __restrict__ lu, const double* r, double* pv,
-                                                          const double* v, float* y, const int* __restrict__ rowSys,
-                                                          const KScal* ks, int* flagF, int* flagB, unsigned* ctr, int* err) {
+                                                          const double* v, unsigned long long* y, const int* __restrict__ rowSys,
+                                                          const KScal* ks, unsigned* ctr, int* err) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1] = 0u;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -279,35 +356,17 @@ __global__ void __launch_bounds__(kSweepThreads) k_fwd_f32(int n, const int* __r
 #pragma unroll
                 for (int e = 0; e < 3; ++e) yi[e] = float(r[size_t(i) * 3 + e]);
             }
-            if (run) {
-                const int r0 = __ldg(rowPtr + i), d = __ldg(diag + i);
-                wait_cols(flagF, col, r0, d, 1, err);
-                for (int p = r0; p < d; ++p) {
-                    const int k = __ldg(col + p);
-                    const float* a = lu + size_t(p) * 9;
-                    const float y0 = y[size_t(k) * 3 + 0], y1 = y[size_t(k) * 3 + 1], y2 = y[size_t(k) * 3 + 2];
+            if (run) sub_tagged(yi, col, lu, __ldg(rowPtr + i), __ldg(diag + i), y, kTagF, err);
 #pragma unroll
-                    for (int e = 0; e < 3; ++e) {
-                        float s = 0.f;
-                        s += __ldg(a + e * 3 + 0) * y0;
-                        s += __ldg(a + e * 3 + 1) * y1;
-                        s += __ldg(a + e * 3 + 2) * y2;
-                        yi[e] -= s;
-                    }
-                }
-            }
-            y[size_t(i) * 3 + 0] = yi[0]; y[size_t(i) * 3 + 1] = yi[1]; y[size_t(i) * 3 + 2] = yi[2];
-            flagB[i] = 0;
-            st_release(flagF + i, 1);
+            for (int e = 0; e < 3; ++e) st_word(y + size_t(i) * 3 + e, yi[e], kTagF);
         }
     }
 }
 
 __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __restrict__ rowPtr, const int* __restrict__ col,
                                                           const int* __restrict__ diag, const int* __restrict__ bord,
-                                                          const float* __restrict__ lu, float* y, double* z,
-                                                          const int* __restrict__ rowSys, const KScal* ks, int* flagF, int* flagB,
-                                                          unsigned* ctr, int* err) {
+                                                          const float* __restrict__ lu, unsigned long long* y, double* z,
+                                                          const int* __restrict__ rowSys, const KScal* ks, unsigned* ctr, int* err) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctr[0] = 0u;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -317,23 +376,11 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __r
         const int idx = base + lane;
         if (idx < n) {
             const int i = __ldg(bord + idx);
+            float yi[3] = {word_val(ld_word(y + size_t(i) * 3 + 0)), word_val(ld_word(y + size_t(i) * 3 + 1)),
+                           word_val(ld_word(y + size_t(i) * 3 + 2))};
             if (sys_running(ks, rowSys, i)) {
-                float yi[3] = {y[size_t(i) * 3 + 0], y[size_t(i) * 3 + 1], y[size_t(i) * 3 + 2]};
-                const int d = __ldg(diag + i), r1 = __ldg(rowPtr + i + 1);
-                wait_cols(flagB, col, d + 1, r1, 1, err);
-                for (int p = d + 1; p < r1; ++p) {
-                    const int j = __ldg(col + p);
-                    const float* a = lu + size_t(p) * 9;
-                    const float z0 = y[size_t(j) * 3 + 0], z1 = y[size_t(j) * 3 + 1], z2 = y[size_t(j) * 3 + 2];
-#pragma unroll
-                    for (int e = 0; e < 3; ++e) {
-                        float s = 0.f;
-                        s += __ldg(a + e * 3 + 0) * z0;
-                        s += __ldg(a + e * 3 + 1) * z1;
-                        s += __ldg(a + e * 3 + 2) * z2;
-                        yi[e] -= s;
-                    }
-                }
+                const int d = __ldg(diag + i);
+                sub_tagged(yi, col, lu, d + 1, __ldg(rowPtr + i + 1), y, kTagB, err);
                 const float* D = lu + size_t(d) * 9;
                 float t[3];
 #pragma unroll
@@ -344,11 +391,14 @@ __global__ void __launch_bounds__(kSweepThreads) k_bwd_f32(int n, const int* __r
                     s += __ldg(D + e * 3 + 2) * yi[2];
                     t[e] = s;
                 }
-                y[size_t(i) * 3 + 0] = t[0]; y[size_t(i) * 3 + 1] = t[1]; y[size_t(i) * 3 + 2] = t[2];
-                z[size_t(i) * 3 + 0] = double(t[0]); z[size_t(i) * 3 + 1] = double(t[1]); z[size_t(i) * 3 + 2] = double(t[2]);
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    yi[e] = t[e];
+                    z[size_t(i) * 3 + e] = double(t[e]);
+                }
             }
-            flagF[i] = 0;
-            st_release(flagB + i, 1);
+#pragma unroll
+            for (int e = 0; e < 3; ++e) st_word(y + size_t(i) * 3 + e, yi[e], kTagB);
         }
     }
 }
@@ -702,13 +752,12 @@ void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r,
                                                  err);
 }
 
-void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, float* y32, SweepState& S, int* err,
+void launch_ilu_apply_f32(const DevPlan& P, const float* luf, const double* r, double* z, unsigned long long* y32, SweepState& S, int* err,
                           cudaStream_t st) {
     const int g = sweep_blocks(P);
     k_fwd_f32<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, luf, r, nullptr, nullptr, y32, P.rowSys,
-                                                     nullptr, S.flagF, S.flagB, S.ctr, err);
-    k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, luf, y32, z, P.rowSys, nullptr, S.flagF, S.flagB,
-                                          S.ctr, err);
+                                                     nullptr, S.ctr, err);
+    k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, luf, y32, z, P.rowSys, nullptr, S.ctr, err);
 }
 
 void launch_ilu_grid_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
@@ -725,10 +774,9 @@ void launch_ilu_grid_ks(const DevPlan& P, const PrecDev& M, const double* r, dou
         k_bwd_f64<float><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, z, P.rowSys, ks, S.flagF, S.flagB,
                                                       S.ctr, err);
     } else {
-        k_fwd_f32<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, r, nullptr, nullptr, M.y32,
-                                                         P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
-        k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, M.y32, z, P.rowSys, ks, S.flagF, S.flagB,
-                                               S.ctr, err);
+        k_fwd_f32<IN_PLAIN><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, r, nullptr, nullptr, M.yt,
+                                                         P.rowSys, ks, S.ctr, err);
+        k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, M.yt, z, P.rowSys, ks, S.ctr, err);
     }
 }
 
@@ -812,13 +860,12 @@ void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M
                                                          S.flagB, S.ctr, err);
         } else if (M.kind == 3) {      // all-FP32 sweep
             if (pupd)
-                k_fwd_f32<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.p, V.v, V.y32,
-                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
+                k_fwd_f32<IN_PUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.p, V.v, V.yt,
+                                                                   P.rowSys, ks, S.ctr, err);
             else
-                k_fwd_f32<IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.s, V.v, V.y32,
-                                                                   P.rowSys, ks, S.flagF, S.flagB, S.ctr, err);
-            k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, V.y32, out, P.rowSys, ks, S.flagF,
-                                                  S.flagB, S.ctr, err);
+                k_fwd_f32<IN_SUPDATE><<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.ford, M.luf, V.r, V.s, V.v, V.yt,
+                                                                   P.rowSys, ks, S.ctr, err);
+            k_bwd_f32<<<g, kSweepThreads, 0, st>>>(P.n, P.rowPtr, P.col, P.diag, P.bord, M.luf, V.yt, out, P.rowSys, ks, S.ctr, err);
         } else {
             const int gb = (P.n + 127) / 128;
             if (pupd)

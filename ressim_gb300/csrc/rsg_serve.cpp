@@ -72,14 +72,23 @@ struct rsg_server {
     long long nextId = 0;
     bool stop = false;
     std::vector<std::thread> workers;
-    std::vector<rsg_solver*> handles, bilu;   // per slot: the configured handle, a BILU0 handle for patterns CPR cannot take
+    std::vector<rsg_solver*> handles, grid, bilu;   // per slot: the configured handle (batches of small requests), one
+                                                    // with the grid-wide sweeps (larger requests), a BILU0 handle for
+                                                    // patterns CPR cannot take
     Clock::time_point t0 = Clock::now();      // the server's clock origin (start_ms / end_ms of the results)
 };
 
 namespace {
 
+// A request of at most kBatchRows block rows runs on one SM (thread-block sweeps) and is batched with the small
+// requests queued behind it; a larger one is solved alone by the grid-wide sweeps, where a lone system gets the whole
+// GPU. The choice depends on the request alone, so its result does not depend on what else is queued.
+constexpr int kBatchRows = 32768;
+constexpr int kMaxBatch = 64;
+constexpr long long kMaxBatchRowsTotal = 1 << 21;
+
 void run_request(rsg_server* S, int slot, Request& R) {
-    rsg_solver* h = S->handles[size_t(slot)];
+    rsg_solver* h = R.n > kBatchRows && S->grid[size_t(slot)] ? S->grid[size_t(slot)] : S->handles[size_t(slot)];
     int prec = S->opt.precond;
     int rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
     if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
@@ -115,9 +124,6 @@ void run_request(rsg_server* S, int slot, Request& R) {
     rsg_release(h);                                               // the request's state leaves the device
 }
 
-constexpr int kBatchRows = 65536;      // a request this small runs on one SM: batch it with its neighbours in the queue
-constexpr int kMaxBatch = 64;
-constexpr long long kMaxBatchRowsTotal = 1 << 21;
 
 // Small requests of a batch: one block-diagonal solve (every system's kernels and reductions are its own, so each
 // result is the one it has alone). Patterns the batch cannot take (CPR on a pattern that is not structurally
@@ -251,11 +257,16 @@ int rsg_server_create(rsg_server** out, const rsg_options* opts, int slots, size
     S->slots = slots;
     S->budget = mem_budget;
     S->handles.assign(size_t(slots), nullptr);
+    S->grid.assign(size_t(slots), nullptr);
     S->bilu.assign(size_t(slots), nullptr);
+    rsg_options og = S->opt;
+    og.sweep = 2;
     for (int i = 0; i < slots; ++i) {
-        const int rc = rsg_create(&S->handles[size_t(i)], &S->opt);
+        int rc = rsg_create(&S->handles[size_t(i)], &S->opt);
+        if (rc == RSG_OK) rc = rsg_create(&S->grid[size_t(i)], &og);
         if (rc != RSG_OK) {
             for (rsg_solver* h : S->handles) rsg_destroy(h);
+            for (rsg_solver* h : S->grid) rsg_destroy(h);
             delete S;
             return rc;                                            // the handle's message stays in rsg_last_error
         }
@@ -281,6 +292,7 @@ int rsg_server_destroy(rsg_server* S) {
     S->cvWork.notify_all();
     for (auto& t : S->workers) t.join();
     for (rsg_solver* h : S->handles) rsg_destroy(h);
+    for (rsg_solver* h : S->grid) rsg_destroy(h);
     for (rsg_solver* h : S->bilu) rsg_destroy(h);
     delete S;
     return RSG_OK;

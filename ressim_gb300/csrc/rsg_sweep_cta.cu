@@ -1253,16 +1253,32 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int ma
                     return FWD ? w < wi : w > wi;
                 };
                 const int w0 = POS ? (FWD ? p0 : pd + 1) : p0, w1 = POS ? (FWD ? pd : p1) : p1;
+                const int e1 = (FWD && ZERO && POS) ? pd : p1;         // from zero: only the updated neighbours count
+                TA vp[8];                                              // the row's first values and columns, loaded
+                int jp[8];                                             // before the wait (read-only)
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    vp[u] = p0 + u < e1 ? __ldg(vl + p0 + u) : TA(0);
+                    jp[u] = p0 + u < e1 ? rowOff + __ldg(cl + p0 + u) : 0;
+                }
+                const TA dv = __ldg(vl + pd);
                 wait_deps(flag, w0, w1, FWD ? 1 : 0, err, [&](int p) { return rowOff + __ldg(cl + p); }, dep);
                 TA s = b[row];
-                const int e1 = (FWD && ZERO && POS) ? pd : p1;         // from zero: only the updated neighbours count
-                for (int p = p0; p < e1; ++p) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int p = p0 + u;
+                    if (p >= e1) break;
+                    if (p == pd) continue;
+                    if (FWD && ZERO && !POS && __ldg(wave + jp[u]) > wi) continue;   // x_j is still zero: the term vanishes
+                    s = asub(s, amul(vp[u], x[jp[u]]));
+                }
+                for (int p = p0 + 8; p < e1; ++p) {
                     if (p == pd) continue;
                     const int j = rowOff + __ldg(cl + p);
-                    if (FWD && ZERO && !POS && __ldg(wave + j) > wi) continue;   // x_j is still zero: the term vanishes
+                    if (FWD && ZERO && !POS && __ldg(wave + j) > wi) continue;
                     s = asub(s, amul(__ldg(vl + p), x[j]));
                 }
-                x[row] = adiv(s, __ldg(vl + pd));
+                x[row] = adiv(s, dv);
             }
             st_release(flag + row, FWD ? 1 : 0);
         }

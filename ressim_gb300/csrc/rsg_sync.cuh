@@ -21,37 +21,36 @@ __device__ __forceinline__ int ld_relaxed(const int* p) {
 }
 __device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
-// bounded wait for *f == want by relaxed polls (the caller fences once after all its waits): a short busy spin
-// first (most waits in a sweep are short), then exponential back-off up to 256 ns; on time-out sets ERR_TIMEOUT
-// and returns false (the caller then proceeds)
-__device__ __noinline__ bool spin_relaxed(const int* f, int want, int* err) {
-    for (int it = 0; it < 64; ++it)
-        if (ld_relaxed(f) == want) return true;
-    unsigned ns = 32;
-    for (unsigned it = 0; it < kSpinLimit; ++it) {
-        __nanosleep(ns);
-        if (ns < 256) ns <<= 1;
-        if (ld_relaxed(f) == want) return true;
-        if ((it & 255u) == 255u && *(volatile int*)err != 0) return false;   // another wait already gave up
-    }
-    atomicOr(err, ERR_TIMEOUT);
-    return false;
-}
-
 // Wait until flag[idx(q)] == want for every q in [q0, q1) with need(q), then one acquire fence. A row's
-// dependencies are polled four at a time with relaxed loads that are in flight together, where an acquire load
-// per dependency would cost one round trip after another on the sweep's critical path.
+// dependencies are polled four at a time, and every poll round re-issues the loads of all those still pending
+// together (relaxed loads, in flight at once): a round costs one memory round trip however many are pending.
+// Bounded: a short busy phase, then back-off up to 256 ns; on time-out ERR_TIMEOUT is set and the wait ends.
 template <class Idx, class Need>
 __device__ __forceinline__ void wait_deps(const int* flag, int q0, int q1, int want, int* err, Idx idx, Need need) {
     for (int q = q0; q < q1; q += 4) {
-        int k[4], v[4];
+        int k[4];
+        unsigned pending = 0;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) k[u] = (q + u < q1 && need(q + u)) ? idx(q + u) : -1;
+        for (int u = 0; u < 4; ++u) {
+            k[u] = (q + u < q1 && need(q + u)) ? idx(q + u) : -1;
+            if (k[u] >= 0) pending |= 1u << u;
+        }
+        unsigned ns = 0;
+        for (unsigned it = 0; pending; ++it) {
+            int v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = k[u] >= 0 ? ld_relaxed(flag + k[u]) : want;
+            for (int u = 0; u < 4; ++u) v[u] = (pending >> u) & 1u ? ld_relaxed(flag + k[u]) : want;
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (v[u] != want) spin_relaxed(flag + k[u], want, err);
+            for (int u = 0; u < 4; ++u)
+                if (v[u] == want) pending &= ~(1u << u);
+            if (!pending) break;
+            if (it >= 64) {
+                __nanosleep(ns);
+                ns = ns < 32 ? 32 : (ns < 256 ? 2 * ns : 256);
+                if (it >= 64 + kSpinLimit) { atomicOr(err, ERR_TIMEOUT); break; }
+                if ((it & 255u) == 255u && *(volatile int*)err != 0) break;   // another wait already gave up
+            }
+        }
     }
     fence_acquire();
 }
