@@ -552,12 +552,10 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         G.gsBlocks[size_t(l)] = sweep_blocks_for(double(G.levelRowBeg[size_t(l) + 1] - G.levelRowBeg[size_t(l)]) / maxNl, h->opt.sweep_inflight);
     }
     // colour-major rows of every level that is smoothed (multicolour schedule only): colour c of every system, then
-    // c + 1; colours from colTail on (all of them small) go to one thread block
+    // c + 1; colours from colTail on (all of them small) are swept together by one sync-free pass
     constexpr int kTailRows = 2048;
     std::vector<int4> cdesc;
-    std::vector<int> cbeg;
     G.colBeg.assign(size_t(maxL), std::vector<int>());
-    G.cbegOff.assign(size_t(maxL), 0);
     G.colTail.assign(size_t(maxL), 0);
     if (mc)
         for (int l = 0; l < maxL; ++l) {
@@ -586,11 +584,8 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             int tail = ncol;
             while (tail > 0 && cb[size_t(tail)] - cb[size_t(tail) - 1] < kTailRows) --tail;
             G.colTail[size_t(l)] = tail;
-            G.cbegOff[size_t(l)] = int(cbeg.size());
-            cbeg.insert(cbeg.end(), cb.begin(), cb.end());
         }
     if (cdesc.empty()) cdesc.push_back(make_int4(0, 0, 0, 0));
-    if (cbeg.empty()) cbeg.push_back(0);
     std::vector<int> gci(static_cast<size_t>(std::max(ents, 1)), 0);
     for (int l = 0; l < maxL; ++l)
         for (int s = 0; s < nsys; ++s) {
@@ -613,7 +608,6 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = upload(M, &G.diagGlob, dgG, st)) || (rc = upload(M, &G.luPerm, luPerm, st)) ||
         (rc = upload(M, &G.slotSrc, slotSrc, st)) || (rc = upload(M, &G.slotCol, slotCol, st)) || (rc = upload(M, &G.gsRows, gsRows, st)) ||
         (rc = upload(M, reinterpret_cast<int**>(&G.rowMeta), meta, st)) || (rc = upload(M, &G.rowLv, rowLv, st)) || (rc = upload(M, &G.cdesc, cdesc, st)) || (rc = upload(M, &G.gci, gci, st)) ||
-        (rc = upload(M, &G.cbeg, cbeg, st)) ||
         (rc = upload(M, &G.wave, wave, st)) || (rc = dalloc(M, &G.gsFlag, 2 * size_t(std::max(rows, 1)))) ||
         (rc = dalloc(M, &G.gsCtr, 4 * size_t(std::max(maxL, 1)))) || (rc = dalloc(M, &G.coarse64, size_t(std::max(nsys, 1)))))
         return rc;

@@ -169,13 +169,12 @@ struct DevAmg {
     std::vector<int> coarseGsLevels;   // host: levels that are some system's coarsest without a dense LU
     // multicolour schedule (FP32 forms), grid-wide: per level the rows of every system that smooths it, colour by
     // colour, as {row, first entry, end of entries, diagonal entry} (global indices); colour c of level l at
-    // colBeg[l][c] .. colBeg[l][c + 1] (host) and cbeg[cbegOff[l] + c] (device). Colours from colTail[l] on hold
-    // few rows (the cliques of perforated cells that the well Schur fill creates) and go to one thread block.
+    // colBeg[l][c] .. colBeg[l][c + 1]. Colours from colTail[l] on hold few rows each (the cliques of perforated
+    // cells that the well Schur fill creates) and are swept together by one sync-free pass.
     int4* cdesc = nullptr;
     int* gci = nullptr;                // global column of every entry (rowOff + local column)
-    int* cbeg = nullptr;
     std::vector<std::vector<int>> colBeg;
-    std::vector<int> cbegOff, colTail;
+    std::vector<int> colTail;
     std::vector<int> gsBlocks;         // host: persistent grid of the sync-free Gauss-Seidel sweeps of each level
     bool posOrder = false;             // host: in every row the entries before the diagonal are exactly its earlier-wave neighbours
 };

@@ -1312,35 +1312,72 @@ __global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, con
         gs_colour_row<TA, ZERO>(d, gci, val, wave, b, x);
     }
 }
-// the small colours [c0, c1) of a level, one after another in one thread block (ascending forward, descending
-// backward), a barrier between colours
-// (a warp per row: the rows of the small colours are the long rows of the well cliques; the lanes split the
-// entries and the partial sums meet in a fixed shuffle tree)
-template <class TA, bool ZERO>
-__global__ void __launch_bounds__(256) k_gs_tail(const int* __restrict__ cb, int c0, int c1, int fwd, int maxL,
-                                                 const int4* __restrict__ cdesc, const int* __restrict__ gci, const TA* __restrict__ val,
-                                                 const int* __restrict__ wave, const int* __restrict__ rowLv, const TA* b, TA* x,
-                                                 const KScal* ks) {
-    const int lane = int(threadIdx.x & 31), wid = int(threadIdx.x >> 5), nw = int(blockDim.x >> 5);
-    for (int cc = 0; cc < c1 - c0; ++cc) {
-        const int c = fwd ? c0 + cc : c1 - 1 - cc;
-        const int i1 = __ldg(cb + c + 1);
-        for (int i = __ldg(cb + c) + wid; i < i1; i += nw) {
-            const int4 d = __ldg(cdesc + i);
-            if (ks && ks[__ldg(rowLv + d.x) / maxL].status != ST_RUNNING) continue;
-            const int wi = ZERO ? __ldg(wave + d.x) : 0;
+// The small colours (from colour `tail` on) of a level in one sync-free pass. Their rows are the long rows of the
+// well cliques, so a warp takes one row: rows are claimed in colour order (forward ascending, backward
+// descending), the lanes split the row's entries, poll together the flags of its neighbours of an earlier colour
+// inside the tail (forward; a later one backward) until the whole warp sees them set, then sum their terms and
+// meet in a shuffle tree. The large colours are done before (forward) or after (backward) by their own passes, so
+// their values are final or old as the multicolour order wants. Flags: 1 after the forward pass, 0 after the
+// backward one; bounded waits (ERR_TIMEOUT).
+template <class TA, bool FWD, bool ZERO>
+__global__ void __launch_bounds__(kGridThreads) k_gs_tail(int i0, int i1, int tail, int maxL, const int4* __restrict__ cdesc,
+                                                          const int* __restrict__ gci, const TA* __restrict__ val,
+                                                          const int* __restrict__ wave, const int* __restrict__ rowLv, const TA* b, TA* x,
+                                                          int* flag, unsigned* ctr, const KScal* ks, int* err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr[FWD ? 1 : 0] = 0u;   // the opposite direction's counter, for its next pass
+    const int n = i1 - i0, lane = int(threadIdx.x & 31);
+    const int want = FWD ? 1 : 0;
+    for (;;) {
+        unsigned got = 0;
+        if (lane == 0) got = atomicAdd(ctr + (FWD ? 0 : 1), 1u);
+        const int idx = int(__shfl_sync(0xffffffffu, got, 0));
+        if (idx >= n) break;
+        const int4 d = __ldg(cdesc + (FWD ? i0 + idx : i1 - 1 - idx));
+        const bool run = !ks || ks[__ldg(rowLv + d.x) / maxL].status == ST_RUNNING;
+        if (run) {
+            const int wi = __ldg(wave + d.x);
+            // this lane's entries: up to four polled at once per round (longer rows: the rest in later passes)
+            for (int p0 = d.y; p0 < d.z; p0 += 128) {
+                int k[4];
+                unsigned pending = 0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int p = p0 + lane + 32 * u;
+                    k[u] = -1;
+                    if (p < d.z && p != d.w) {
+                        const int j = __ldg(gci + p);
+                        const int w = __ldg(wave + j);
+                        if (FWD ? (w < wi && w >= tail) : w > wi) { k[u] = j; pending |= 1u << u; }
+                    }
+                }
+                unsigned ns = 0;
+                for (unsigned it = 0;; ++it) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (((pending >> u) & 1u) && ld_relaxed(flag + k[u]) == want) pending &= ~(1u << u);
+                    if (!__any_sync(0xffffffffu, pending != 0)) break;
+                    if (it >= 64) {
+                        __nanosleep(ns);
+                        ns = ns < 32 ? 32 : (ns < 256 ? 2 * ns : 256);
+                        if (it >= 64 + kSpinLimit) { if (pending) atomicOr(err, ERR_TIMEOUT); break; }
+                        if ((it & 255u) == 255u && *(volatile int*)err != 0) break;
+                    }
+                }
+            }
+            fence_acquire();
             TA t = TA(0);
             for (int p = d.y + lane; p < d.z; p += 32) {
                 if (p == d.w) continue;
                 const int j = __ldg(gci + p);
-                if (ZERO && __ldg(wave + j) > wi) continue;
+                if (ZERO && __ldg(wave + j) > wi) continue;            // x_j is still zero: the term vanishes
                 t = aadd(t, amul(__ldg(val + p), x[j]));
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) t = aadd(t, __shfl_xor_sync(0xffffffffu, t, o));
             if (lane == 0) x[d.x] = adiv(asub(b[d.x], t), __ldg(val + d.w));
         }
-        __syncthreads();
+        __syncwarp();
+        if (lane == 0) st_release(flag + d.x, want);
     }
 }
 
@@ -1458,7 +1495,6 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
         const std::vector<int>& cb = G.colBeg[size_t(l)];
         if (phase == 0 && cb.size() > 1) {                 // multicolour: a parallel pass per large colour, the small ones in one block
             const int nc = int(cb.size()) - 1, tail = G.colTail[size_t(l)];
-            const int* cbd = G.cbeg + G.cbegOff[size_t(l)];
             auto big = [&](int c) {
                 const int i0 = cb[size_t(c)], i1 = cb[size_t(c) + 1];
                 if (zero)
@@ -1471,12 +1507,19 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
             };
             auto small = [&]() {
                 if (tail >= nc) return;
-                if (zero)
-                    k_gs_tail<TA, true><<<1, 256, 0, st>>>(cbd, tail, nc, fwd ? 1 : 0, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
-                                                          C.x, ks);
+                const int i0 = cb[size_t(tail)], i1 = cb[size_t(nc)];
+                const int g = std::max(1, std::min(G.gsBlocks[size_t(l)], (i1 - i0 + kGridThreads / 32 - 1) / (kGridThreads / 32)));
+                int* flag = G.gsFlag;                               // phase-0 flags: unused otherwise on multicolour levels
+                unsigned* ctr = G.gsCtr + 4 * l;
+                if (fwd && zero)
+                    k_gs_tail<TA, true, true><<<g, kGridThreads, 0, st>>>(i0, i1, tail, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
+                                                                          C.x, flag, ctr, ks, err);
+                else if (fwd)
+                    k_gs_tail<TA, true, false><<<g, kGridThreads, 0, st>>>(i0, i1, tail, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
+                                                                           C.x, flag, ctr, ks, err);
                 else
-                    k_gs_tail<TA, false><<<1, 256, 0, st>>>(cbd, tail, nc, fwd ? 1 : 0, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv, C.b,
-                                                           C.x, ks);
+                    k_gs_tail<TA, false, false><<<g, kGridThreads, 0, st>>>(i0, i1, tail, G.maxL, G.cdesc, G.gci, val, G.wave, G.rowLv,
+                                                                            C.b, C.x, flag, ctr, ks, err);
                 ++launches;
             };
             if (fwd) {
