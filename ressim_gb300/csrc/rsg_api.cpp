@@ -174,8 +174,7 @@ int alloc_plan(rsg_solver* h) {
     cudaStream_t st = h->stream;
     D.n = P.n; D.nnzb = P.nnzb; D.nsys = P.nsys; D.ntiles = int(P.tileSys.size());
     int rc;
-    // col and the values carry 64 bytes of padding: the staged SpMV copies whole 16-byte granules
-    if ((rc = upload(M, &D.rowPtr, P.rowPtr, st)) || (rc = upload(M, &D.col, P.col, st, 16)) || (rc = upload(M, &D.diag, P.diag, st)) ||
+    if ((rc = upload(M, &D.rowPtr, P.rowPtr, st)) || (rc = upload(M, &D.col, P.col, st)) || (rc = upload(M, &D.diag, P.diag, st)) ||
         (rc = upload(M, &D.ford, P.ford, st)) || (rc = upload(M, &D.bord, P.bord, st)) || (rc = upload(M, &D.elimPtr, P.elimPtr, st)) ||
         (rc = upload(M, &D.elimT, P.elimT, st)) || (rc = upload(M, &D.elimQ, P.elimQ, st)) || (rc = upload(M, &D.rowSys, P.rowSys, st)) ||
         (rc = upload(M, &D.tileRow0, P.tileRow0, st)) || (rc = upload(M, &D.tileSys, P.tileSys, st)) ||
@@ -199,7 +198,7 @@ int alloc_plan(rsg_solver* h) {
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
     if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
-    if ((rc = dalloc(M, &h->val, E + 8)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
+    if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
         (rc = dalloc(M, &h->tmp, N)))
         return rc;
     double** vecs[] = {&h->V.x, &h->V.r, &h->V.rh, &h->V.p, &h->V.v, &h->V.s, &h->V.t, &h->V.ph, &h->V.sh};

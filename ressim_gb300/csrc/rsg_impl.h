@@ -70,7 +70,6 @@ struct HostPlan {
     std::vector<int> Uslot, UslotSrc, UovCol, UovSrc;
     std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of row k
     int maxSysRows = 0;
-    // bulk-staged SpMV: bytes of one stage (values, columns) covering the largest 64-row chunk of any tile
 };
 
 struct PrecDev;
