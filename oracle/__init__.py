@@ -80,6 +80,16 @@ class Oracle:
         L.orc_refine_float.restype = C.c_int
         L.orc_cpr_setup.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_void_p, C.c_int]
         L.orc_cpr_setup.restype = C.c_void_p
+        L.orc_devcpr_setup.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p]
+        L.orc_devcpr_setup.restype = C.c_void_p
+        L.orc_devcpr_apply.argtypes = [C.c_void_p, _f32p, _f32p]
+        L.orc_devcpr_apply.restype = None
+        L.orc_devcpr_levels.argtypes = [C.c_void_p]
+        L.orc_devcpr_levels.restype = C.c_int
+        L.orc_devcpr_has_inverse.argtypes = [C.c_void_p]
+        L.orc_devcpr_has_inverse.restype = C.c_int
+        L.orc_devcpr_free.argtypes = [C.c_void_p]
+        L.orc_devcpr_free.restype = None
         L.orc_cpr_weights.argtypes = [C.c_void_p]
         L.orc_cpr_weights.restype = C.POINTER(C.c_double)
         L.orc_cpr_amg.argtypes = [C.c_void_p]
@@ -173,6 +183,17 @@ class Oracle:
                                        C.byref(its), C.byref(rr))
         return x, bool(conv), its.value, rr.value
 
+    def devcpr_apply(self, A, r):
+        """GPU-shaped float CPR-AMG (engine/src/bsr.cpp:1217-1371): z = M^-1 r in float32."""
+        rf = np.ascontiguousarray(r, dtype=np.float32)
+        z = np.zeros(A.n * A.nb, dtype=np.float32)
+        h = self.L.orc_devcpr_setup(A.n, A.nb, A.rowPtr, A.col, A.val)
+        try:
+            self.L.orc_devcpr_apply(h, rf, z)
+        finally:
+            self.L.orc_devcpr_free(h)
+        return z
+
     def cpr_info(self, A, acc=None):
         """CPR weights and the AMG hierarchy: (w, [(rows, nnz)], [level CSR + aggregates])."""
         accv = None if acc is None else _arr(acc, np.float64)
@@ -251,6 +272,8 @@ class RefShim:
         L.ref_refine_float.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.c_double, C.c_int, C.c_int,
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.ref_refine_float.restype = C.c_int
+        L.ref_devcpr_apply.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f32p, _f32p]
+        L.ref_devcpr_apply.restype = C.c_int
         L.ref_set_threads(1)
 
     @staticmethod
@@ -291,6 +314,12 @@ class RefShim:
         conv = self.L.ref_solve(A.n, A.nb, A.rowPtr, A.col, A.val, None if accv is None else accv.ctypes.data_as(C.c_void_p), prec,
                                 method, restart, _arr(b, np.float64), x, tol, maxit, C.byref(its), C.byref(rr))
         return x, bool(conv), its.value, rr.value
+
+    def devcpr_apply(self, A, r):
+        rf = np.ascontiguousarray(r, dtype=np.float32)
+        z = np.zeros(A.n * A.nb, dtype=np.float32)
+        self.L.ref_devcpr_apply(A.n, A.nb, A.rowPtr, A.col, A.val, rf, z)
+        return z
 
     def cpr_info(self, A, acc=None):
         accv = None if acc is None else _arr(acc, np.float64)

@@ -14,6 +14,7 @@
 //   bicgstab / gmres             engine/src/linsolve.cpp:159-273
 //   WellSchur build/reduce/recover engine/src/bsr.cpp:733-990
 //   CpuFloatBlockSolver, refineWithDevice engine/src/bsr.cpp:1130-1215,1373-1396
+//   DeviceCprAmg build / apply   engine/src/bsr.cpp:1217-1371
 #define private public      // read the factor storage of BILU0 (layout is unchanged by access specifiers)
 #include "ressim/bsr.h"
 #undef private
@@ -165,6 +166,17 @@ int ref_refine_float(int n, int nb, const int* rowPtr, const int* col, const dou
     std::memcpy(x, xv.data(), sizeof(double) * xv.size());
     *its = r.iterations; *relres = r.relResidual;
     return r.converged ? 1 : 0;
+}
+
+// GPU-shaped float CPR-AMG (DeviceCprAmg::build / apply, engine/src/bsr.cpp:1217-1371): z = M^-1 r in float
+int ref_devcpr_apply(int n, int nb, const int* rowPtr, const int* col, const double* val, const float* r, float* z) {
+    const BSR A = makeBsr(n, nb, rowPtr, col, val);
+    DeviceCprAmg D;
+    if (!D.build(A)) return 0;
+    std::vector<float> Av(A.val.size());
+    for (size_t e = 0; e < Av.size(); ++e) Av[e] = float(A.val[e]);
+    D.apply(A, Av, r, z);
+    return int(D.lv.size());
 }
 
 }  // extern "C"

@@ -1109,6 +1109,208 @@ void orc_cpr_free(orc_cpr* h) {
     free(h);
 }
 
+/* ================================================================== GPU-shaped float CPR-AMG
+ * engine/src/bsr.cpp:1217-1371 (DeviceCprAmg::build / apply): the BlockCPR hierarchy with float values, damped Jacobi
+ * V(1,1) (omega = 0.6667, one sweep each way, the first from x = 0), the coarsest level by an explicit inverse
+ * (Gauss-Jordan in double, at most 1500 rows; else 31 Jacobi sweeps), the second stage block-Jacobi on r - S E x.
+ * Float operations in the reference's order (this file is built with -ffp-contract=off). */
+struct orc_devcpr {
+    int n, nb, L;
+    const int *rowPtr, *col;
+    orc_cpr* cpr;             /* weights and hierarchy, as BlockCPR::setup builds them */
+    float *w, *Av, *bj;       /* weights (n*nb), float values of S, block-diagonal inverses (n*nb*nb) */
+    float *A[14], *P[14], *R[14], *dinv[14];
+    float *x[14], *b[14], *t[14];
+    int m;                    /* coarsest rows */
+    float* cinv;              /* explicit inverse of the coarsest level (m*m, natural order) or NULL */
+    float *z1, *tt;
+};
+
+static float* f32_copy(const double* v, size_t n) {
+    float* f = (float*)xmalloc(sizeof(float) * (n > 0 ? n : 1));
+    for (size_t k = 0; k < n; ++k) f[k] = (float)v[k];
+    return f;
+}
+
+orc_devcpr* orc_devcpr_setup(int n, int nb, const int* rowPtr, const int* col, const double* val) {
+    orc_devcpr* h = (orc_devcpr*)xcalloc(1, sizeof(orc_devcpr));
+    const int N = n * nb, b2 = nb * nb, nnzb = rowPtr[n];
+    h->n = n; h->nb = nb; h->rowPtr = rowPtr; h->col = col;
+    h->cpr = orc_cpr_setup(n, nb, rowPtr, col, val, NULL, 0);
+    const orc_amg* G = h->cpr->amg;
+    h->L = G->L;
+    h->w = f32_copy(h->cpr->w, (size_t)N);
+    h->Av = f32_copy(val, (size_t)nnzb * b2);
+    for (int l = 0; l < h->L; ++l) {
+        const amg_level* V = &G->lv[l];
+        const int nl = V->A.nr;
+        h->A[l] = f32_copy(V->A.v, (size_t)V->A.rp[nl]);
+        h->dinv[l] = (float*)xmalloc(sizeof(float) * (size_t)(nl > 0 ? nl : 1));
+        for (int i = 0; i < nl; ++i) {
+            double d = 0;
+            for (int k = V->A.rp[i]; k < V->A.rp[i + 1]; ++k)
+                if (V->A.ci[k] == i) d = V->A.v[k];
+            h->dinv[l][i] = fabs(d) > 1e-300 ? (float)(1.0 / d) : 0.0f;
+        }
+        if (l + 1 < h->L) {
+            h->P[l] = f32_copy(V->P.v, (size_t)V->P.rp[V->P.nr]);
+            h->R[l] = f32_copy(V->R.v, (size_t)V->R.rp[V->R.nr]);
+        }
+        h->x[l] = (float*)xcalloc((size_t)(nl > 0 ? nl : 1), sizeof(float));
+        h->b[l] = (float*)xcalloc((size_t)(nl > 0 ? nl : 1), sizeof(float));
+        h->t[l] = (float*)xcalloc((size_t)(nl > 0 ? nl : 1), sizeof(float));
+    }
+    /* explicit inverse of the coarsest operator: Gauss-Jordan in double, pivot = first strictly largest |a_ik| */
+    const sp_t* Cc = &G->lv[h->L - 1].A;
+    const int m = Cc->nr;
+    h->m = m;
+    if (m > 0 && m <= 1500) {
+        const size_t w2 = 2 * (size_t)m;
+        double* M = (double*)xcalloc((size_t)m * w2, sizeof(double));
+        for (int i = 0; i < m; ++i) {
+            for (int k = Cc->rp[i]; k < Cc->rp[i + 1]; ++k) M[(size_t)i * w2 + (size_t)Cc->ci[k]] += Cc->v[k];
+            M[(size_t)i * w2 + (size_t)(m + i)] = 1.0;
+        }
+        int ok = 1;
+        for (int k = 0; k < m && ok; ++k) {
+            int pr = k;
+            for (int i = k + 1; i < m; ++i)
+                if (fabs(M[(size_t)i * w2 + k]) > fabs(M[(size_t)pr * w2 + k])) pr = i;
+            if (fabs(M[(size_t)pr * w2 + k]) < 1e-300) { ok = 0; break; }
+            if (pr != k)
+                for (size_t j = 0; j < w2; ++j) {
+                    const double t = M[(size_t)k * w2 + j];
+                    M[(size_t)k * w2 + j] = M[(size_t)pr * w2 + j];
+                    M[(size_t)pr * w2 + j] = t;
+                }
+            const double piv = 1.0 / M[(size_t)k * w2 + k];
+            for (size_t j = 0; j < w2; ++j) M[(size_t)k * w2 + j] *= piv;
+            for (int i = 0; i < m; ++i) {
+                if (i == k) continue;
+                const double f = M[(size_t)i * w2 + k];
+                if (f == 0) continue;
+                for (size_t j = 0; j < w2; ++j) M[(size_t)i * w2 + j] -= f * M[(size_t)k * w2 + j];
+            }
+        }
+        if (ok) {
+            h->cinv = (float*)xmalloc(sizeof(float) * (size_t)m * m);
+            for (int i = 0; i < m; ++i)
+                for (int j = 0; j < m; ++j) h->cinv[(size_t)i * m + j] = (float)M[(size_t)i * w2 + (size_t)(m + j)];
+        }
+        free(M);
+    }
+    /* block-Jacobi second stage: inverse diagonal blocks, 1 / max(1e-30, |D_ee|) on the diagonal when singular */
+    h->bj = (float*)xmalloc(sizeof(float) * (size_t)n * b2);
+    double blk[KMAXB * KMAXB];
+    for (int i = 0; i < n; ++i) {
+        int dp = -1;
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (col[k] == i) dp = k;
+        const double* D = val + (size_t)dp * b2;
+        for (int e = 0; e < b2; ++e) blk[e] = D[e];
+        if (!orc_invert_block(blk, nb)) {
+            for (int e = 0; e < b2; ++e) blk[e] = 0.0;
+            for (int e = 0; e < nb; ++e) blk[e * nb + e] = 1.0 / fmax(1e-30, fabs(D[e * nb + e]));
+        }
+        for (int e = 0; e < b2; ++e) h->bj[(size_t)i * b2 + e] = (float)blk[e];
+    }
+    h->z1 = (float*)xcalloc((size_t)(N > 0 ? N : 1), sizeof(float));
+    h->tt = (float*)xcalloc((size_t)(N > 0 ? N : 1), sizeof(float));
+    return h;
+}
+
+static void f32_spmv(const sp_t* S, const float* v, const float* x, float* y) {
+    for (int i = 0; i < S->nr; ++i) {
+        float acc = 0;
+        for (int k = S->rp[i]; k < S->rp[i + 1]; ++k) acc += v[k] * x[S->ci[k]];
+        y[i] = acc;
+    }
+}
+
+void orc_devcpr_apply(const orc_devcpr* h, const float* r, float* z) {
+    const int n = h->n, nb = h->nb, b2 = nb * nb, L = h->L;
+    const orc_amg* G = h->cpr->amg;
+    const float omega = 0.6667f;
+    for (int i = 0; i < n; ++i) {                                  /* W r */
+        float acc = 0;
+        for (int e = 0; e < nb; ++e) acc += h->w[(size_t)i * nb + e] * r[(size_t)i * nb + e];
+        h->b[0][i] = acc;
+    }
+    for (int l = 0; l + 1 < L; ++l) {
+        const sp_t* A = &G->lv[l].A;
+        float *x = h->x[l], *b = h->b[l], *t = h->t[l];
+        const float* dinv = h->dinv[l];
+        for (int i = 0; i < A->nr; ++i) x[i] = omega * dinv[i] * b[i];   /* one sweep from x = 0 */
+        f32_spmv(A, h->A[l], x, t);
+        for (int i = 0; i < A->nr; ++i) t[i] = b[i] - t[i];
+        f32_spmv(&G->lv[l].R, h->R[l], t, h->b[l + 1]);
+    }
+    {                                                              /* coarsest */
+        const sp_t* A = &G->lv[L - 1].A;
+        float *x = h->x[L - 1], *b = h->b[L - 1], *t = h->t[L - 1];
+        const float* dinv = h->dinv[L - 1];
+        if (h->cinv) {
+            const int m = h->m;
+            for (int i = 0; i < m; ++i) {
+                float acc = 0;
+                for (int j = 0; j < m; ++j) acc += h->cinv[(size_t)i * m + j] * b[j];
+                x[i] = acc;
+            }
+        } else {
+            for (int i = 0; i < A->nr; ++i) x[i] = omega * dinv[i] * b[i];
+            for (int s = 0; s < 30; ++s) {
+                f32_spmv(A, h->A[L - 1], x, t);
+                for (int i = 0; i < A->nr; ++i) x[i] += omega * dinv[i] * (b[i] - t[i]);
+            }
+        }
+    }
+    for (int l = L - 2; l >= 0; --l) {
+        const sp_t* A = &G->lv[l].A;
+        float *x = h->x[l], *b = h->b[l], *t = h->t[l];
+        const float* dinv = h->dinv[l];
+        f32_spmv(&G->lv[l].P, h->P[l], h->x[l + 1], t);
+        for (int i = 0; i < A->nr; ++i) x[i] += t[i];
+        f32_spmv(A, h->A[l], x, t);                                /* one sweep after */
+        for (int i = 0; i < A->nr; ++i) x[i] += omega * dinv[i] * (b[i] - t[i]);
+    }
+    for (int i = 0; i < n; ++i)                                    /* E x: the pressure of each block (a CSR row */
+        for (int e = 0; e < nb; ++e)                               /* with one unit entry, or none)             */
+            h->z1[(size_t)i * nb + e] = e == 0 ? 0.0f + 1.0f * h->x[0][i] : 0.0f;
+    for (int i = 0; i < n; ++i) {                                  /* second stage: z = z1 + D^-1 (r - S z1) */
+        float acc[KMAXB];
+        for (int e = 0; e < nb; ++e) acc[e] = 0;
+        for (int k = h->rowPtr[i]; k < h->rowPtr[i + 1]; ++k) {
+            const float* B = h->Av + (size_t)k * b2;
+            const float* xk = h->z1 + (size_t)h->col[k] * nb;
+            for (int e = 0; e < nb; ++e)
+                for (int f = 0; f < nb; ++f) acc[e] += B[e * nb + f] * xk[f];
+        }
+        for (int e = 0; e < nb; ++e) h->tt[(size_t)i * nb + e] = r[(size_t)i * nb + e] - acc[e];
+    }
+    for (int i = 0; i < n; ++i) {
+        const float* D = h->bj + (size_t)i * b2;
+        for (int e = 0; e < nb; ++e) {
+            float s2 = 0;
+            for (int f = 0; f < nb; ++f) s2 += D[e * nb + f] * h->tt[(size_t)i * nb + f];
+            z[(size_t)i * nb + e] = h->z1[(size_t)i * nb + e] + s2;
+        }
+    }
+}
+
+int orc_devcpr_levels(const orc_devcpr* h) { return h ? h->L : 0; }
+int orc_devcpr_has_inverse(const orc_devcpr* h) { return h && h->cinv ? 1 : 0; }
+
+void orc_devcpr_free(orc_devcpr* h) {
+    if (!h) return;
+    orc_cpr_free(h->cpr);
+    free(h->w); free(h->Av); free(h->bj); free(h->cinv); free(h->z1); free(h->tt);
+    for (int l = 0; l < h->L; ++l) {
+        free(h->A[l]); free(h->dinv[l]); free(h->x[l]); free(h->b[l]); free(h->t[l]);
+        if (l + 1 < h->L) { free(h->P[l]); free(h->R[l]); }
+    }
+    free(h);
+}
+
 /* ================================================================== Krylov (engine/src/linsolve.cpp:147-273) */
 static double dot(const double* a, const double* b, int n) {
     double s = 0;

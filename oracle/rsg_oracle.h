@@ -69,6 +69,14 @@ const double* orc_cpr_weights(const orc_cpr* h);
 const orc_amg* orc_cpr_amg(const orc_cpr* h);
 void orc_cpr_free(orc_cpr* h);
 
+/* GPU-shaped float CPR-AMG (engine/src/bsr.cpp:1217-1371): r, z float of size n*nb */
+typedef struct orc_devcpr orc_devcpr;
+orc_devcpr* orc_devcpr_setup(int n, int nb, const int* rowPtr, const int* col, const double* val);
+void orc_devcpr_apply(const orc_devcpr* h, const float* r, float* z);
+int orc_devcpr_levels(const orc_devcpr* h);
+int orc_devcpr_has_inverse(const orc_devcpr* h);
+void orc_devcpr_free(orc_devcpr* h);
+
 /* ---- Krylov (engine/src/linsolve.cpp:159-273). Callback operator / preconditioner. */
 typedef void (*orc_apply_fn)(void* ctx, const double* x, double* y);
 int orc_bicgstab(int N, orc_apply_fn A, void* actx, orc_apply_fn M, void* mctx, const double* b, double* x, double tol, int maxIt,

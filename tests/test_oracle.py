@@ -67,6 +67,14 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", ALL_GOLDEN)
+def test_device_cpr_amg(oracle, name):
+    """GPU-shaped float CPR-AMG (DeviceCprAmg::build / apply, engine/src/bsr.cpp:1217-1371): the restatement in
+    float, bit for bit the reference's output for the right-hand side rounded to float."""
+    A, z = load_golden(name)
+    assert np.array_equal(oracle.devcpr_apply(A, z["b"].astype(np.float32)), z["z_devcpr"])
+
+
+@pytest.mark.parametrize("name", ALL_GOLDEN)
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_krylov(oracle, name, case):
     A, z = load_golden(name)
