@@ -32,6 +32,9 @@ extern "C" {
 #define RSG_PREC_BILU0 0    /* block ILU(0), natural-order exact (ressim::BILU0, engine/include/ressim/bsr.h:50-94) */
 #define RSG_PREC_CPR 1      /* two-stage CPR: AMG on the pressure system + BILU0 (ressim::BlockCPR, bsr.h:224-250) */
 #define RSG_PREC_JACOBI 2   /* block Jacobi (diagonal-block inverses) */
+#define RSG_PREC_CPR_DEVICE 3 /* the reference's GPU-shaped float CPR-AMG (ressim::DeviceCprAmg, engine/src/bsr.cpp:1217-1371):
+                                 damped-Jacobi V-cycle, explicit coarse inverse, block-Jacobi second stage, in float;
+                                 the precision option does not apply */
 /* Krylov methods */
 #define RSG_KRYLOV_BICGSTAB 0 /* ressim::bicgstab, engine/include/ressim/linsolve.h:99-100 */
 #define RSG_KRYLOV_GMRES 1    /* ressim::gmres (flexible, restarted), linsolve.h:101-102 */

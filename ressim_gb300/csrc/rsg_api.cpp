@@ -247,6 +247,7 @@ int check_device_errors(rsg_solver* h) {
 
 // kernel launches of one preconditioner application
 int precond_launches(const PrecDev& M) {
+    if (M.devcpr) return devcpr_launches(*M.amg);
     if (M.cpr && !M.cta) return cpr_grid_launches(*M.amg);
     return M.cpr || M.cta || M.kind == 2 ? 1 : 2;
 }
@@ -261,6 +262,7 @@ PrecDev prec_dev(rsg_solver* h) {
     M.y32 = h->V.y32;
     M.yt = h->V.yt;
     if (h->opt.precond == RSG_PREC_CPR && h->haveAmg) { M.cpr = true; M.amg = &h->amg; }
+    if (h->opt.precond == RSG_PREC_CPR_DEVICE) { M.devcpr = true; M.kind = 4; M.amg = &h->amg; return M; }
     if (M.kind != 2 && h->cta) {
         M.smem = cta_sweep_smem(h->dp, M.kind == 3);
         M.cta = true;
@@ -339,6 +341,7 @@ int alloc_split(rsg_solver* h, SplitFactors<T>& F) {
 int ensure_precond_storage(rsg_solver* h) {
     const size_t E = size_t(h->plan.nnzb) * NB2;
     int rc;
+    if (h->opt.precond == RSG_PREC_CPR_DEVICE) return RSG_OK;    // its arrays live with the hierarchy
     if (h->opt.precond == RSG_PREC_JACOBI) {
         if (!h->dinv && (rc = dalloc(h->pmem, &h->dinv, size_t(h->plan.n) * NB2))) return rc;
     } else if (h->opt.precision == RSG_MIXED || h->opt.precision == RSG_MIXED_F32) {
@@ -611,6 +614,20 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = dalloc(M, &G.gsCtr, 4 * size_t(std::max(maxL, 1)))) || (rc = dalloc(M, &G.coarse64, size_t(std::max(nsys, 1)))))
         return rc;
     RSG_CUDA(cudaMemsetAsync(G.coarse64, 0, size_t(std::max(nsys, 1)) * sizeof(int), st));
+    if (h->opt.precond == RSG_PREC_CPR_DEVICE) {              // the float CPR-AMG's arrays
+        std::vector<size_t> woff(size_t(nsys), 0);
+        size_t wtot = 0;
+        for (int s = 0; s < nsys; ++s) {
+            woff[size_t(s)] = wtot;
+            const int L = int(H[size_t(s)].lv.size());
+            const AmgSysLv& d = lv[size_t(s) * maxL + L - 1];
+            if (d.dense) wtot += 2 * size_t(d.n) * size_t(d.n);
+        }
+        if ((rc = dalloc(M, &G.dinvf, size_t(std::max(rows, 1)))) || (rc = dalloc(M, &G.bjf, size_t(h->plan.n) * NB2)) ||
+            (rc = dalloc(M, &G.dcOk, size_t(std::max(nsys, 1)))) || (rc = dalloc(M, &G.dcWork, std::max<size_t>(wtot, 1))) ||
+            (rc = upload(M, &G.dcWorkOff, woff, st)))
+            return rc;
+    }
     RSG_CUDA(cudaMemsetAsync(G.gsFlag, 0, 2 * size_t(std::max(rows, 1)) * sizeof(int), st));
     RSG_CUDA(cudaMemsetAsync(G.gsCtr, 0, 4 * size_t(std::max(maxL, 1)) * sizeof(unsigned), st));
     {
@@ -688,6 +705,12 @@ int setup_cpr(rsg_solver* h, const double* acc) {
     }
     launch_cpr_pressure(D, h->val, G.w, G.val, st);          // level 0 of every system = the block pattern
     launch_amg_refresh(G, st);
+    if (h->opt.precond == RSG_PREC_CPR_DEVICE) {              // the float CPR-AMG: float values, its own set-up
+        launch_amg_round(G, st);
+        h->launches += 2 + 3 * std::max(0, G.maxL - 1) + launch_devcpr_setup(D, h->val, G, st);
+        RSG_CUDA(cudaGetLastError());
+        return RSG_OK;
+    }
     launch_amg_coarse_lu(G, h->opt.precision != RSG_FP64, st);
     if (h->opt.precision != RSG_FP64) launch_amg_round(G, st);
     if (h->cta) {                                              // row slots of the thread-block application
@@ -704,15 +727,18 @@ int do_setup(rsg_solver* h, const double* acc) {
     if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
     h->escalated = false;
     h->st.escalated_systems = 0;
-    if (h->opt.precond == RSG_PREC_CPR && !h->plan.symmetric)
-        return fail(RSG_EINVAL, "the CPR preconditioner needs structurally symmetric systems");
+    const bool amgPrec = h->opt.precond == RSG_PREC_CPR || h->opt.precond == RSG_PREC_CPR_DEVICE;
+    if (amgPrec && !h->plan.symmetric)
+        return fail(RSG_EINVAL, "the CPR preconditioners need structurally symmetric systems");
     int rc = ensure_precond_storage(h);
     if (rc) return rc;
     RSG_CUDA(cudaMemsetAsync(h->d_nreg, 0, sizeof(int), h->stream));
     RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
-    if (h->opt.precond == RSG_PREC_CPR && (rc = setup_cpr(h, acc))) return rc;
+    if (amgPrec && (rc = setup_cpr(h, acc))) return rc;
     h->launches += 1;
-    if (h->opt.precond == RSG_PREC_JACOBI) {
+    if (h->opt.precond == RSG_PREC_CPR_DEVICE) {
+        // no BILU0: the second stage is block Jacobi (set up with the hierarchy)
+    } else if (h->opt.precond == RSG_PREC_JACOBI) {
         launch_block_jacobi_setup(h->dp, h->val, h->dinv, h->d_nreg, h->stream);
     } else {
         ++h->epoch;
@@ -733,7 +759,7 @@ int do_setup(rsg_solver* h, const double* acc) {
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->st.setup_ms = ms;
     h->st.regularised_blocks = h->h_pin[2];
-    h->st.amg_levels = h->opt.precond == RSG_PREC_CPR ? h->amgLevels : 0;
+    h->st.amg_levels = amgPrec ? h->amgLevels : 0;
     h->haveSetup = true;
     return RSG_OK;
 }
@@ -766,7 +792,8 @@ int launch_iterations(rsg_solver* h, int k) {
 
 // BiCGSTAB of every system from the gathered right-hand side h->b into h->V.x
 int run_bicgstab(rsg_solver* h, double tol, int maxIt, bool onlyFailed = false) {
-    const bool guard = h->opt.precision == RSG_MIXED_F32 && !h->escalated;
+    const bool guard = h->opt.precision == RSG_MIXED_F32 && !h->escalated && h->opt.precond != RSG_PREC_CPR_DEVICE &&
+                       h->opt.precond != RSG_PREC_JACOBI;
     launch_bicg_init(h->dp, h->b, h->V, h->ks, h->R, tol, maxIt, h->d_active, guard, onlyFailed, h->stream);
     h->launches += 1;
     RSG_CUDA(cudaGetLastError());
@@ -900,7 +927,9 @@ int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, i
         if ((rc = run_gmres(h, tol, maxIt, false))) return rc;
     } else {
         if ((rc = run_bicgstab(h, tol, maxIt))) return rc;
-        if (h->opt.precision == RSG_MIXED_F32 && !h->escalated && (rc = escalate(h, tol, maxIt))) return rc;
+        if (h->opt.precision == RSG_MIXED_F32 && h->opt.precond != RSG_PREC_CPR_DEVICE && h->opt.precond != RSG_PREC_JACOBI &&
+            !h->escalated && (rc = escalate(h, tol, maxIt)))
+            return rc;
         if (h->opt.gmres_fallback) {
             // systems that did not converge are solved again with GMRES from x = 0; per system the result with the
             // smaller recursive residual is kept (engine/src/simulator.cpp:3388-3398)
@@ -986,7 +1015,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     rsg_options o;
     rsg_default_options(&o);
     if (opts) o = *opts;
-    if (o.precond < 0 || o.precond > 2 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 2)
+    if (o.precond < 0 || o.precond > 3 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 2)
         return fail(RSG_EINVAL, "invalid options");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
@@ -1148,7 +1177,8 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
 // level-space r -> level-space z
 static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     const PrecDev M = prec_dev(h);
-    if (M.cpr && M.cta) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
+    if (M.devcpr) h->launches += launch_devcpr(h->dp, h->amg, h->val, 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream);
+    else if (M.cpr && M.cta) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
     else if (M.cpr) h->launches += launch_cpr_grid(h->dp, M, *M.amg, 0, d_r, nullptr, nullptr, d_z, nullptr, h->S, h->d_err, h->stream);
     else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
     else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }

@@ -161,6 +161,13 @@ struct DevAmg {
     // sweep), sync-free sweep flags (phase 0: the smoothing sweeps, phase 1: the GS solve of a coarsest level
     // without dense LU) and claim counters (per level and phase: forward, backward)
     int* coarse64 = nullptr;           // FP32 forms, per system: 1 = coarsest level solved in FP64 (LU), the FP32 inverse too inexact
+    // the GPU-shaped float CPR-AMG (RSG_PREC_CPR_DEVICE): float inverse diagonal of every AMG row, float block-Jacobi
+    // inverses (n * 9), per system whether the coarsest inverse exists, the double Gauss-Jordan work matrices
+    float* dinvf = nullptr;
+    float* bjf = nullptr;
+    int* dcOk = nullptr;
+    double* dcWork = nullptr;
+    size_t* dcWorkOff = nullptr;
     int* rowLv = nullptr;
     int* wave = nullptr;
     int* gsFlag = nullptr;             // 2 x totRows
@@ -198,6 +205,12 @@ void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mod
 // sweeps, z_p += xp. Returns the number of kernel launches.
 int launch_cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, const double* r, double* pv, const double* v,
                     double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st);
+// the reference's GPU-shaped float CPR-AMG (rsg_devcpr.cu): set-up (coarse inverse, inverse diagonals, block
+// inverses) after the hierarchy refresh, and one application (mode: plain, p-update, s-update); both return launches
+int launch_devcpr_setup(const DevPlan& P, const double* val, DevAmg& G, cudaStream_t st);
+int launch_devcpr(const DevPlan& P, const DevAmg& G, const double* val, int mode, const double* r, double* pv, const double* v, double* z,
+                  const KScal* ks, cudaStream_t st);
+int devcpr_launches(const DevAmg& G);
 inline int cpr_grid_launches(const DevAmg& G) {
     int n = 6 + 2 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
     for (int l = 0; l + 1 < G.maxL; ++l) {          // pre- and post-smoothing: one sweep, or a launch per large colour + the tail
@@ -300,6 +313,7 @@ struct PrecDev {
     float* y32 = nullptr;             // all-FP32 sweep vector in global memory (systems that do not fit on chip)
     unsigned long long* yt = nullptr; // grid-wide all-FP32 sweeps: tagged sweep vector
     bool cpr = false;                 // CPR two-stage preconditioner (AMG on the pressure system + BILU0)
+    bool devcpr = false;              // the reference's GPU-shaped float CPR-AMG
     const DevAmg* amg = nullptr;
 };
 // all-FP32 factorisation (FP32 elimination, FP64 pivot inversion), one thread block per system

@@ -51,34 +51,21 @@ __device__ bool last_tile_reduce(int ntiles, int nsys, const int* __restrict__ s
     __syncthreads();
     if (!amLast) return false;
     __threadfence();
+    // one warp per system, the same order whatever the batch: a system's inner products do not depend on the
+    // systems solved with it (lane-strided partial sums over its tiles, then a shuffle tree)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (nsys <= 4) {
-        for (int s = 0; s < nsys; ++s) {
-            double v[MAX_DOTS] = {0, 0, 0, 0};
-            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
-            for (int t = t0 + int(threadIdx.x); t < t1; t += blockDim.x)
+    for (int s = w; s < nsys; s += nw) {
+        double v[MAX_DOTS] = {0, 0, 0, 0};
+        const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
+        for (int t = t0 + lane; t < t1; t += 32)
 #pragma unroll
-                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
-            block_reduce<ND>(v, sh);
-            if (threadIdx.x == 0)
+            for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
 #pragma unroll
-                for (int j = 0; j < ND; ++j) sysdot[size_t(s) * MAX_DOTS + j] = v[j];
-            __syncthreads();
-        }
-    } else {
-        for (int s = w; s < nsys; s += nw) {
-            double v[MAX_DOTS] = {0, 0, 0, 0};
-            const int t0 = sysTile0[s], t1 = sysTile0[s + 1];
-            for (int t = t0 + lane; t < t1; t += 32)
+        for (int j = 0; j < ND; ++j) {
+            double x = v[j];
 #pragma unroll
-                for (int j = 0; j < ND; ++j) v[j] += ((volatile const double*)part)[size_t(t) * MAX_DOTS + j];
-#pragma unroll
-            for (int j = 0; j < ND; ++j) {
-                double x = v[j];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                if (lane == 0) sysdot[size_t(s) * MAX_DOTS + j] = x;
-            }
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) sysdot[size_t(s) * MAX_DOTS + j] = x;
         }
     }
     __syncthreads();

@@ -52,7 +52,7 @@ size_t footprint(int n, long long nnzb, const rsg_options& o) {
     double bytes = E * (2 * 72.0 + 100.0) + N * 700.0;           // values + staging, plan arrays, level / slot plan
     bytes += o.precision == RSG_FP64 ? E * 72.0 + N * 512.0 : E * 108.0 + N * 256.0;   // factors (+ lean work)
     bytes += N * 3 * 8 * 14;                                      // Krylov and staging vectors
-    if (o.precond == RSG_PREC_CPR) bytes += E * 40.0 + N * 600.0;
+    if (o.precond == RSG_PREC_CPR || o.precond == RSG_PREC_CPR_DEVICE) bytes += E * 40.0 + N * 600.0;
     if (o.krylov == RSG_KRYLOV_GMRES || o.gmres_fallback) bytes += N * 3 * 8 * (2.0 * (o.restart > 0 ? o.restart : 40) + 3);
     return size_t(bytes) + (size_t(16) << 20);
 }
@@ -92,7 +92,7 @@ void run_request(rsg_server* S, int slot, Request& R) {
     int prec = S->opt.precond;
     int rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
     if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
-    if (rc == RSG_EINVAL && prec == RSG_PREC_CPR) {               // CPR needs a structurally symmetric pattern: BILU0
+    if (rc == RSG_EINVAL && (prec == RSG_PREC_CPR || prec == RSG_PREC_CPR_DEVICE)) {   // CPR needs a structurally symmetric pattern: BILU0
         rsg_release(h);
         if (!S->bilu[size_t(slot)]) {
             rsg_options o = S->opt;
