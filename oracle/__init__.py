@@ -80,6 +80,8 @@ class Oracle:
         L.orc_refine_float.restype = C.c_int
         L.orc_cpr_setup.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_void_p, C.c_int]
         L.orc_cpr_setup.restype = C.c_void_p
+        L.orc_mcbilu0_apply.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.orc_mcbilu0_apply.restype = C.c_int
         L.orc_devcpr_setup.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p]
         L.orc_devcpr_setup.restype = C.c_void_p
         L.orc_devcpr_apply.argtypes = [C.c_void_p, _f32p, _f32p]
@@ -183,6 +185,12 @@ class Oracle:
                                        C.byref(its), C.byref(rr))
         return x, bool(conv), its.value, rr.value
 
+    def mcbilu0_apply(self, A, r):
+        """Multicolour BILU0 (engine/src/bsr.cpp:599-730): z = M^-1 r."""
+        z = np.zeros(A.n * A.nb)
+        self.L.orc_mcbilu0_apply(A.n, A.nb, A.rowPtr, A.col, A.val, _arr(r, np.float64), z)
+        return z
+
     def devcpr_apply(self, A, r):
         """GPU-shaped float CPR-AMG (engine/src/bsr.cpp:1217-1371): z = M^-1 r in float32."""
         rf = np.ascontiguousarray(r, dtype=np.float32)
@@ -272,6 +280,8 @@ class RefShim:
         L.ref_refine_float.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p, C.c_double, C.c_int, C.c_int,
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.ref_refine_float.restype = C.c_int
+        L.ref_mcbilu0_apply.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.ref_mcbilu0_apply.restype = C.c_int
         L.ref_devcpr_apply.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f32p, _f32p]
         L.ref_devcpr_apply.restype = C.c_int
         L.ref_set_threads(1)
@@ -314,6 +324,11 @@ class RefShim:
         conv = self.L.ref_solve(A.n, A.nb, A.rowPtr, A.col, A.val, None if accv is None else accv.ctypes.data_as(C.c_void_p), prec,
                                 method, restart, _arr(b, np.float64), x, tol, maxit, C.byref(its), C.byref(rr))
         return x, bool(conv), its.value, rr.value
+
+    def mcbilu0_apply(self, A, r):
+        z = np.zeros(A.n * A.nb)
+        self.L.ref_mcbilu0_apply(A.n, A.nb, A.rowPtr, A.col, A.val, _arr(r, np.float64), z)
+        return z
 
     def devcpr_apply(self, A, r):
         rf = np.ascontiguousarray(r, dtype=np.float32)

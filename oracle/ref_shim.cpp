@@ -15,6 +15,7 @@
 //   WellSchur build/reduce/recover engine/src/bsr.cpp:733-990
 //   CpuFloatBlockSolver, refineWithDevice engine/src/bsr.cpp:1130-1215,1373-1396
 //   DeviceCprAmg build / apply   engine/src/bsr.cpp:1217-1371
+//   MCBILU0 factor / apply       engine/src/bsr.cpp:599-730
 #define private public      // read the factor storage of BILU0 (layout is unchanged by access specifiers)
 #include "ressim/bsr.h"
 #undef private
@@ -166,6 +167,15 @@ int ref_refine_float(int n, int nb, const int* rowPtr, const int* col, const dou
     std::memcpy(x, xv.data(), sizeof(double) * xv.size());
     *its = r.iterations; *relres = r.relResidual;
     return r.converged ? 1 : 0;
+}
+
+// multicolour BILU0 (MCBILU0::factor / apply, engine/src/bsr.cpp:599-730): z = M^-1 r, returns the colours
+int ref_mcbilu0_apply(int n, int nb, const int* rowPtr, const int* col, const double* val, const double* r, double* z) {
+    const BSR A = makeBsr(n, nb, rowPtr, col, val);
+    MCBILU0 M;
+    M.factor(A);
+    M.apply(r, z);
+    return M.colours();
 }
 
 // GPU-shaped float CPR-AMG (DeviceCprAmg::build / apply, engine/src/bsr.cpp:1217-1371): z = M^-1 r in float

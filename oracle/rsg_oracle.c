@@ -1109,6 +1109,109 @@ void orc_cpr_free(orc_cpr* h) {
     free(h);
 }
 
+/* ================================================================== multicolour BILU0
+ * engine/src/bsr.cpp:599-730 (colourBlocks, permuteBsr, MCBILU0::factor / apply): largest-degree-first greedy
+ * colouring of the symmetric block graph, P A P^T with sorted columns, block ILU(0) of it in its natural order (rows of
+ * a colour depend on earlier colours only; the row arithmetic and singular-pivot shift are bilu0Row's), and the
+ * sweeps on the permuted vectors. */
+static int int_cmp(const void* a, const void* b);
+typedef struct { int d, i; } deg_t;
+static int deg_cmp(const void* a, const void* b) {               /* degree descending, index ascending (stable) */
+    const deg_t* x = (const deg_t*)a;
+    const deg_t* y = (const deg_t*)b;
+    if (x->d != y->d) return x->d > y->d ? -1 : 1;
+    return x->i < y->i ? -1 : (x->i > y->i ? 1 : 0);
+}
+
+int orc_colour_blocks(int n, const int* rowPtr, const int* col, int* colour, int* perm) {
+    int* cnt = (int*)xcalloc((size_t)n + 1, sizeof(int));
+    for (int i = 0; i < n; ++i)
+        for (int p = rowPtr[i]; p < rowPtr[i + 1]; ++p)
+            if (col[p] != i) { cnt[i + 1]++; cnt[col[p] + 1]++; }
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    int* adj = (int*)xmalloc(sizeof(int) * (size_t)(cnt[n] > 0 ? cnt[n] : 1));
+    int* fill = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) fill[i] = cnt[i];
+    for (int i = 0; i < n; ++i)
+        for (int p = rowPtr[i]; p < rowPtr[i + 1]; ++p)
+            if (col[p] != i) { adj[fill[i]++] = col[p]; adj[fill[col[p]]++] = i; }
+    int* deg = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) {                                 /* sorted, unique */
+        int* a = adj + cnt[i];
+        const int m = fill[i] - cnt[i];
+        qsort(a, (size_t)m, sizeof(int), int_cmp);
+        int u = 0;
+        for (int k = 0; k < m; ++k)
+            if (u == 0 || a[k] != a[u - 1]) a[u++] = a[k];
+        deg[i] = u;
+    }
+    deg_t* ord = (deg_t*)xmalloc(sizeof(deg_t) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) { ord[i].d = deg[i]; ord[i].i = i; }
+    qsort(ord, (size_t)n, sizeof(deg_t), deg_cmp);
+    for (int i = 0; i < n; ++i) colour[i] = -1;
+    int colours = 0;
+    char* mark = (char*)xmalloc((size_t)n + 2);
+    for (int t = 0; t < n; ++t) {
+        const int i = ord[t].i, m = deg[i];
+        memset(mark, 0, (size_t)m + 2);
+        for (int k = 0; k < m; ++k) {
+            const int cj = colour[adj[cnt[i] + k]];
+            if (cj >= 0 && cj < m + 2) mark[cj] = 1;
+        }
+        int c = 0;
+        while (mark[c]) ++c;
+        colour[i] = c;
+        if (c + 1 > colours) colours = c + 1;
+    }
+    int* start = (int*)xcalloc((size_t)colours + 1, sizeof(int));
+    for (int i = 0; i < n; ++i) start[colour[i] + 1]++;
+    for (int c = 0; c < colours; ++c) start[c + 1] += start[c];
+    for (int i = 0; i < n; ++i) perm[start[colour[i]]++] = i;     /* new index -> original, cells grouped by colour */
+    free(start); free(mark); free(ord); free(deg); free(fill); free(adj); free(cnt);
+    return colours;
+}
+
+typedef struct { int c, p; } colpos_t;
+static int colpos_cmp(const void* a, const void* b) {
+    const colpos_t* x = (const colpos_t*)a;
+    const colpos_t* y = (const colpos_t*)b;
+    if (x->c != y->c) return x->c < y->c ? -1 : 1;
+    return x->p < y->p ? -1 : (x->p > y->p);
+}
+
+int orc_mcbilu0_apply(int n, int nb, const int* rowPtr, const int* col, const double* val, const double* r, double* z) {
+    const int b2 = nb * nb, nnzb = rowPtr[n];
+    int* colour = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int* perm = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int* iperm = (int*)xmalloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    const int colours = orc_colour_blocks(n, rowPtr, col, colour, perm);
+    for (int k = 0; k < n; ++k) iperm[perm[k]] = k;
+    int* prp = (int*)xcalloc((size_t)n + 1, sizeof(int));
+    int* pci = (int*)xmalloc(sizeof(int) * (size_t)(nnzb > 0 ? nnzb : 1));
+    double* pv = (double*)xmalloc(sizeof(double) * (size_t)(nnzb > 0 ? nnzb : 1) * b2);
+    colpos_t* row = (colpos_t*)xmalloc(sizeof(colpos_t) * (size_t)(nnzb > 0 ? nnzb : 1));
+    for (int k = 0; k < n; ++k) {
+        const int i = perm[k], m = rowPtr[i + 1] - rowPtr[i];
+        for (int q = 0; q < m; ++q) { row[q].c = iperm[col[rowPtr[i] + q]]; row[q].p = rowPtr[i] + q; }
+        qsort(row, (size_t)m, sizeof(colpos_t), colpos_cmp);
+        prp[k + 1] = prp[k] + m;
+        for (int q = 0; q < m; ++q) {
+            pci[prp[k] + q] = row[q].c;
+            memcpy(pv + (size_t)(prp[k] + q) * b2, val + (size_t)row[q].p * b2, sizeof(double) * (size_t)b2);
+        }
+    }
+    double* lu = (double*)xmalloc(sizeof(double) * (size_t)(nnzb > 0 ? nnzb : 1) * b2);
+    const int nreg = orc_bilu0_factor(n, nb, prp, pci, pv, lu);
+    double* rp = (double*)xmalloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * nb);
+    double* zp = (double*)xmalloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * nb);
+    for (int k = 0; k < n; ++k) memcpy(rp + (size_t)k * nb, r + (size_t)perm[k] * nb, sizeof(double) * (size_t)nb);
+    orc_bilu0_apply(n, nb, prp, pci, lu, rp, zp);
+    for (int k = 0; k < n; ++k) memcpy(z + (size_t)perm[k] * nb, zp + (size_t)k * nb, sizeof(double) * (size_t)nb);
+    free(zp); free(rp); free(lu); free(row); free(pv); free(pci); free(prp); free(iperm); free(perm); free(colour);
+    (void)nreg;
+    return colours;
+}
+
 /* ================================================================== GPU-shaped float CPR-AMG
  * engine/src/bsr.cpp:1217-1371 (DeviceCprAmg::build / apply): the BlockCPR hierarchy with float values, damped Jacobi
  * V(1,1) (omega = 0.6667, one sweep each way, the first from x = 0), the coarsest level by an explicit inverse

@@ -69,6 +69,11 @@ const double* orc_cpr_weights(const orc_cpr* h);
 const orc_amg* orc_cpr_amg(const orc_cpr* h);
 void orc_cpr_free(orc_cpr* h);
 
+/* multicolour BILU0 (engine/src/bsr.cpp:599-730): colouring (colour per cell, perm: new index -> cell; returns the
+ * number of colours) and z = M^-1 r of the colour-permuted block ILU(0) */
+int orc_colour_blocks(int n, const int* rowPtr, const int* col, int* colour, int* perm);
+int orc_mcbilu0_apply(int n, int nb, const int* rowPtr, const int* col, const double* val, const double* r, double* z);
+
 /* GPU-shaped float CPR-AMG (engine/src/bsr.cpp:1217-1371): r, z float of size n*nb */
 typedef struct orc_devcpr orc_devcpr;
 orc_devcpr* orc_devcpr_setup(int n, int nb, const int* rowPtr, const int* col, const double* val);

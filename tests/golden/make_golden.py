@@ -81,6 +81,7 @@ def golden_for(R: RefShim, A: BSR, b, acc=None, with_factors=False, label=""):
     out["z_bilu0f"] = R.bilu0f_apply(A, b)
     out["z_cpr"] = R.prec_apply(A, b, prec=1, acc=None)
     out["z_devcpr"] = R.devcpr_apply(A, b.astype(np.float32))   # DeviceCprAmg::apply (float), input rounded to float
+    out["z_mcbilu0"] = R.mcbilu0_apply(A, b)                     # MCBILU0::factor / apply
     w, info, levels = R.cpr_info(A, acc=None)
     out["cpr_w"] = w
     out["amg_rows"] = np.array([r for r, _ in info], dtype=np.int32)

@@ -67,6 +67,13 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", ALL_GOLDEN)
+def test_multicolour_bilu0(oracle, name):
+    """MCBILU0 (engine/src/bsr.cpp:599-730): colouring, P A P^T, its block ILU(0) and sweeps, bit for bit."""
+    A, z = load_golden(name)
+    assert np.array_equal(oracle.mcbilu0_apply(A, z["b"]), z["z_mcbilu0"])
+
+
+@pytest.mark.parametrize("name", ALL_GOLDEN)
 def test_device_cpr_amg(oracle, name):
     """GPU-shaped float CPR-AMG (DeviceCprAmg::build / apply, engine/src/bsr.cpp:1217-1371): the restatement in
     float, bit for bit the reference's output for the right-hand side rounded to float."""
