@@ -32,6 +32,8 @@ extern "C" {
 #define RSG_PREC_BILU0 0    /* block ILU(0), natural-order exact (ressim::BILU0, engine/include/ressim/bsr.h:50-94) */
 #define RSG_PREC_CPR 1      /* two-stage CPR: AMG on the pressure system + BILU0 (ressim::BlockCPR, bsr.h:224-250) */
 #define RSG_PREC_JACOBI 2   /* block Jacobi (diagonal-block inverses) */
+#define RSG_PREC_MCBILU0 4   /* multicolour block ILU(0) (ressim::MCBILU0, engine/src/bsr.cpp:599-730): the natural-order BILU0
+                                 of P A P^T, P the largest-degree-first greedy colouring; few levels, so short sweeps */
 #define RSG_PREC_CPR_DEVICE 3 /* the reference's GPU-shaped float CPR-AMG (ressim::DeviceCprAmg, engine/src/bsr.cpp:1217-1371):
                                  damped-Jacobi V-cycle, explicit coarse inverse, block-Jacobi second stage, in float;
                                  the precision option does not apply */

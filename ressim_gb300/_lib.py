@@ -13,7 +13,7 @@ import numpy as np
 from . import _build
 
 RSG_OK, RSG_EINVAL, RSG_ECUDA, RSG_ENOMEM, RSG_ESTATE, RSG_ETIMEOUT, RSG_EBREAKDOWN, RSG_ENOTCONV = 0, -1, -2, -3, -4, -5, -6, 1
-PREC = {"bilu0": 0, "cpr": 1, "jacobi": 2, "cpr_device": 3}
+PREC = {"bilu0": 0, "cpr": 1, "jacobi": 2, "cpr_device": 3, "mcbilu0": 4}
 KRYLOV = {"bicgstab": 0, "gmres": 1}
 PRECISION = {"fp64": 0, "mixed": 1, "mixed_f32": 2}
 SWEEP = {"auto": 0, "cta": 1, "grid": 2}

@@ -320,7 +320,21 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
     if (!same) {
         free_plan(h);
         std::string err;
-        if (!build_plan(h->plan, nsys, sysRow0, rp, ci, err)) return fail(RSG_EINVAL, err);
+        if (h->opt.precond == RSG_PREC_MCBILU0) {
+            // multicolour BILU0: the plan of P A P^T (its natural-order BILU0 is the multicolour one), mapped back to the
+            // caller's rows and blocks
+            std::vector<int> rp2, ci2, rowOrig, blockOrig;
+            multicolour_batch(nsys, sysRow0, rp, ci, rp2, ci2, rowOrig, blockOrig);
+            if (!build_plan(h->plan, nsys, sysRow0, rp2, ci2, err)) return fail(RSG_EINVAL, err);
+            HostPlan& P = h->plan;
+            for (auto& v : P.perm) v = rowOrig[size_t(v)];
+            for (int k = 0; k < P.n; ++k) P.iperm[size_t(P.perm[size_t(k)])] = k;
+            for (auto& v : P.valSrc) v = blockOrig[size_t(v)];
+            P.rowPtr0 = rp;
+            P.col0 = ci;
+        } else if (!build_plan(h->plan, nsys, sysRow0, rp, ci, err)) {
+            return fail(RSG_EINVAL, err);
+        }
         int rc = alloc_plan(h);
         if (rc) { free_plan(h); return rc; }
         h->nsys = nsys;
@@ -1015,7 +1029,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     rsg_options o;
     rsg_default_options(&o);
     if (opts) o = *opts;
-    if (o.precond < 0 || o.precond > 3 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 2)
+    if (o.precond < 0 || o.precond > 4 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 2)
         return fail(RSG_EINVAL, "invalid options");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");

@@ -78,6 +78,10 @@ struct SweepState;
 // Builds the plan of a (block-diagonal batch of) BSR pattern(s). Returns false with a message on bad input.
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
                 const std::vector<int>& col, std::string& err);
+// multicolour ordering of every system (MCBILU0, engine/src/bsr.cpp:599-653): permuted pattern and the original row /
+// block of every permuted row / block
+void multicolour_batch(int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rp, const std::vector<int>& ci,
+                       std::vector<int>& rp2, std::vector<int>& ci2, std::vector<int>& rowOrig, std::vector<int>& blockOrig);
 
 // ---- CPR pressure AMG of one system (host plan; engine/src/amg.cpp:137-295). Every level is kept in its own level
 // space: rows renumbered by forward Gauss-Seidel level, entries of a row in their natural order.

@@ -21,6 +21,71 @@ void order_by_level(const std::vector<int>& lev, int nl, std::vector<int>& ord) 
 }
 }  // namespace
 
+// Multicolour ordering of every system of a batch (MCBILU0's colouring and P A P^T, engine/src/bsr.cpp:599-653): the
+// symmetric block graph of the system coloured greedily in largest-degree-first order (ties by index, as a stable
+// sort leaves them; a colour is taken if none of the row's neighbours has it), rows renumbered colour by colour
+// (ascending original index inside a colour), every row's entries sorted by their new column. Output: the permuted
+// block-diagonal pattern, the original row of every permuted row and the original block of every permuted block.
+void multicolour_batch(int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rp, const std::vector<int>& ci,
+                       std::vector<int>& rp2, std::vector<int>& ci2, std::vector<int>& rowOrig, std::vector<int>& blockOrig) {
+    const int n = int(rp.size()) - 1;
+    rp2.assign(size_t(n) + 1, 0);
+    ci2.assign(ci.size(), 0);
+    rowOrig.assign(size_t(n), 0);
+    blockOrig.assign(ci.size(), 0);
+    std::vector<int> iperm(size_t(n), 0);
+    for (int s = 0; s < nsys; ++s) {
+        const int r0 = sysRow0[size_t(s)], m = sysRow0[size_t(s) + 1] - r0;
+        std::vector<std::vector<int>> adj(static_cast<size_t>(m));
+        for (int i = 0; i < m; ++i)
+            for (int p = rp[size_t(r0 + i)]; p < rp[size_t(r0 + i) + 1]; ++p) {
+                const int j = ci[size_t(p)] - r0;
+                if (j != i) { adj[size_t(i)].push_back(j); adj[size_t(j)].push_back(i); }
+            }
+        for (auto& v : adj) { std::sort(v.begin(), v.end()); v.erase(std::unique(v.begin(), v.end()), v.end()); }
+        std::vector<int> order(static_cast<size_t>(m));
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return adj[size_t(a)].size() > adj[size_t(b)].size(); });
+        std::vector<int> colour(static_cast<size_t>(m), -1);
+        std::vector<char> taken;
+        int colours = 0;
+        for (int i : order) {
+            const size_t deg = adj[size_t(i)].size();
+            taken.assign(deg + 2, 0);
+            for (int j : adj[size_t(i)]) {
+                const int c = colour[size_t(j)];
+                if (c >= 0 && size_t(c) < taken.size()) taken[size_t(c)] = 1;
+            }
+            int c = 0;
+            while (taken[size_t(c)]) ++c;
+            colour[size_t(i)] = c;
+            colours = std::max(colours, c + 1);
+        }
+        std::vector<int> start(size_t(colours) + 1, 0);
+        for (int i = 0; i < m; ++i) start[size_t(colour[size_t(i)]) + 1]++;
+        for (int c = 0; c < colours; ++c) start[size_t(c) + 1] += start[size_t(c)];
+        for (int i = 0; i < m; ++i) {
+            const int k = start[size_t(colour[size_t(i)])]++;
+            rowOrig[size_t(r0 + k)] = r0 + i;
+            iperm[size_t(r0 + i)] = r0 + k;
+        }
+    }
+    std::vector<std::pair<int, int>> row;
+    for (int k = 0; k < n; ++k) {
+        const int i = rowOrig[size_t(k)];
+        row.clear();
+        for (int p = rp[size_t(i)]; p < rp[size_t(i) + 1]; ++p) row.push_back({iperm[size_t(ci[size_t(p)])], p});
+        std::sort(row.begin(), row.end());
+        rp2[size_t(k) + 1] = rp2[size_t(k)] + int(row.size());
+        int q = rp2[size_t(k)];
+        for (const auto& e : row) {
+            ci2[size_t(q)] = e.first;
+            blockOrig[size_t(q)] = e.second;
+            ++q;
+        }
+    }
+}
+
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr0,
                 const std::vector<int>& col0, std::string& err) {
     const int n = int(rowPtr0.size()) - 1;
