@@ -491,7 +491,9 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
                 }
             }
         }
-    std::vector<int> rp(static_cast<size_t>(rps)), ci(static_cast<size_t>(ents)), dg(static_cast<size_t>(rows)),
+    // ci (and the value arrays) carry OV_CHUNK - 1 entries past the last row: the sweeps read a row's entries
+    // after its slots in chunks of OV_CHUNK
+    std::vector<int> rp(static_cast<size_t>(rps)), ci(static_cast<size_t>(ents) + OV_CHUNK - 1, 0), dg(static_cast<size_t>(rows)),
         lvl(static_cast<size_t>(lvls)), agg(static_cast<size_t>(rows), 0), memPtr(static_cast<size_t>(rps), 0),
         mem(static_cast<size_t>(mems)), dgG(static_cast<size_t>(rows)), luPerm(static_cast<size_t>(std::max(lurows, 1)), 0),
         gsRows(static_cast<size_t>(std::max(rows, 1)), 0);
@@ -654,7 +656,7 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
             return rc;
     }
     RSG_CUDA(cudaMemcpyAsync(G.lv, lv.data(), lv.size() * sizeof(AmgSysLv), cudaMemcpyHostToDevice, st));
-    if ((rc = dalloc(M, &G.val, size_t(ents))) || (rc = dalloc(M, &G.valf, size_t(ents))) || (rc = dalloc(M, &G.apVal, size_t(std::max(aps, 1)))) ||
+    if ((rc = dalloc(M, &G.val, size_t(ents) + OV_CHUNK - 1)) || (rc = dalloc(M, &G.valf, size_t(ents) + OV_CHUNK - 1)) || (rc = dalloc(M, &G.apVal, size_t(std::max(aps, 1)))) ||
         (rc = dalloc(M, &G.lu, size_t(std::max(lus, 1)))) || (rc = dalloc(M, &G.luf, size_t(std::max(lus, 1)))) ||
         (rc = dalloc(M, &G.invf, size_t(std::max(lus, 1)))) ||
         (rc = dalloc(M, &G.piv, size_t(std::max(lurows, 1)))) || (rc = dalloc(M, &G.x, size_t(rows))) || (rc = dalloc(M, &G.b, size_t(rows))) ||

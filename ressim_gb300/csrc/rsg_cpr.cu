@@ -266,14 +266,22 @@ __global__ void __launch_bounds__(256) k_coarse_inv(int maxL, const AmgSysLv* __
 }
 
 // FP32 forms: the coarsest inverse directly, by Gauss-Jordan elimination with partial pivoting on the dense matrix
-// in its natural numbering, in shared memory (m <= kInvSmemRows): thread j owns column j, column k of every step is
-// staged for all threads; the inverse is written as the V-cycle reads it, inv[j * m + I] = (A^-1)[I][nat(j)].
-// Larger levels take the LU (k_coarse_lu<float>) and k_coarse_inv instead.
-__global__ void __launch_bounds__(256) k_coarse_gj(int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
-                                                   const int* __restrict__ ci, const double* __restrict__ val,
-                                                   const int* __restrict__ luPerm, float* invAll) {
+// in its natural numbering (m <= kInvSmemRows); the inverse is written as the V-cycle reads it,
+// inv[j * m + I] = (A^-1)[I][nat(j)]. Larger levels take the LU (k_coarse_lu<float>) and k_coarse_inv instead.
+// The work matrix lives in registers: 16 warps, row i in warp i % 16, column j in lane j % 32, so a thread holds
+// a 14 x 7 tile and a step's rank-1 update is register arithmetic. Per step, the pivot column (staged in shared
+// memory by its owning lane during the previous update) is searched by every warp on its own; the pivot row and
+// row k go through shared memory for the interchange and the scaled pivot row. Every element gets the same
+// separately rounded operations as a column-per-thread elimination in shared memory.
+constexpr int kGjThreads = 512;
+constexpr int kGjWarps = kGjThreads / 32;
+constexpr int kGjRows = (kInvSmemRows + kGjWarps - 1) / kGjWarps;   // register rows per thread
+constexpr int kGjCols = (kInvSmemRows + 31) / 32;                  // register columns per thread
+__global__ void __launch_bounds__(kGjThreads, 1) k_coarse_gj(int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                            const int* __restrict__ ci, const double* __restrict__ val,
+                                                            const int* __restrict__ luPerm, float* invAll) {
     extern __shared__ float W[];
-    const int s = blockIdx.x;
+    const int s = blockIdx.x, tid = int(threadIdx.x), nt = int(blockDim.x), lane = tid & 31, wg = tid >> 5;
     AmgSysLv L;
     bool found = false;
     for (int l = 0; l < maxL; ++l) {
@@ -282,56 +290,120 @@ __global__ void __launch_bounds__(256) k_coarse_gj(int maxL, const AmgSysLv* __r
     }
     if (!found || !L.dense) return;
     const int m = L.n;
-    if (m > kInvSmemRows || m > int(blockDim.x)) return;         // left to the LU path
-    float* col = W + m * m;                                      // column k of the current step
-    __shared__ float pv[256];
-    __shared__ int pi[256];
+    if (m > kInvSmemRows || nt != kGjThreads) return;          // left to the LU path
+    __shared__ float colk[2][kGjWarps * kGjRows];               // column k of the current step, then of the next
+    __shared__ float rowK[32 * kGjCols], rowP[32 * kGjCols];   // rows k and p before the interchange
     __shared__ int perm[kInvSmemRows];
     const int* nat = luPerm + L.luRowOff;
-    for (int q = threadIdx.x; q < m * m; q += blockDim.x) W[q] = 0.f;
+    for (int q = tid; q < m * m; q += nt) W[q] = 0.f;
     __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    for (int k = tid; k < m; k += nt) {
         const int I = __ldg(nat + k);
         for (int p = __ldg(rp + L.rpOff + k); p < __ldg(rp + L.rpOff + k + 1); ++p)
             W[I * m + __ldg(nat + __ldg(ci + L.entOff + p))] = float(val[L.entOff + p]);
     }
-    const int j = threadIdx.x;
+    __syncthreads();
+    float R[kGjRows][kGjCols];
+#pragma unroll
+    for (int r = 0; r < kGjRows; ++r)
+#pragma unroll
+        for (int c = 0; c < kGjCols; ++c) {
+            const int i = wg + kGjWarps * r, j = lane + 32 * c;
+            R[r][c] = (i < m && j < m) ? W[i * m + j] : 0.f;
+        }
+    for (int i = tid; i < kGjWarps * kGjRows; i += nt) colk[0][i] = i < m ? W[i * m] : 0.f;
     for (int k = 0; k < m; ++k) {
+        const float* ck = colk[k & 1];
         __syncthreads();
-        // pivot: largest |a_ik|, i >= k (first on ties)
+        // pivot: largest |a_ik|, i >= k (first on ties), found by every warp
         float best = -1.f;
         int bi = m;
-        for (int i = k + int(threadIdx.x); i < m; i += blockDim.x) {
-            const float a = fabsf(W[i * m + k]);
+        for (int i = k + lane; i < m; i += 32) {
+            const float a = fabsf(ck[i]);
             if (a > best) { best = a; bi = i; }
         }
-        pv[threadIdx.x] = best;
-        pi[threadIdx.x] = bi;
-        __syncthreads();
-        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-            if (int(threadIdx.x) < o) {
-                const float b2 = pv[threadIdx.x + o];
-                const int i2 = pi[threadIdx.x + o];
-                if (b2 > pv[threadIdx.x] || (b2 == pv[threadIdx.x] && i2 < pi[threadIdx.x])) { pv[threadIdx.x] = b2; pi[threadIdx.x] = i2; }
-            }
-            __syncthreads();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float b2 = __shfl_xor_sync(0xffffffffu, best, o);
+            const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (b2 > best || (b2 == best && i2 < bi)) { best = b2; bi = i2; }
         }
-        const int p = pi[0];
-        if (j < m && p != k) { const float t = W[k * m + j]; W[k * m + j] = W[p * m + j]; W[p * m + j] = t; }
-        if (threadIdx.x == 0) perm[k] = p;
+        const int p = bi < m ? bi : k;                          // no comparable entry (NaN column): no interchange
+        // (register rows and columns are picked by select chains: an indexed access would move the tile to local
+        // memory)
+        if (wg == k % kGjWarps) {
+            const int rk = k / kGjWarps;
+#pragma unroll
+            for (int c = 0; c < kGjCols; ++c) {
+                float v = R[0][c];
+#pragma unroll
+                for (int r = 1; r < kGjRows; ++r) v = rk == r ? R[r][c] : v;
+                rowK[lane + 32 * c] = v;
+            }
+        }
+        if (wg == p % kGjWarps) {
+            const int rp = p / kGjWarps;
+#pragma unroll
+            for (int c = 0; c < kGjCols; ++c) {
+                float v = R[0][c];
+#pragma unroll
+                for (int r = 1; r < kGjRows; ++r) v = rp == r ? R[r][c] : v;
+                rowP[lane + 32 * c] = v;
+            }
+        }
+        if (tid == 0) perm[k] = p;
         __syncthreads();
-        for (int i = threadIdx.x; i < m; i += blockDim.x) col[i] = W[i * m + k];
-        __syncthreads();
-        if (j < m) {
-            float d = col[k];
-            if (fabsf(d) < 1.17549435e-38f) d = 1.17549435e-38f;                 // singular: smallest normal pivot
-            const float akj = j == k ? __fdiv_rn(1.f, d) : __fdiv_rn(W[k * m + j], d);
-            W[k * m + j] = akj;
-            for (int i = 0; i < m; ++i)
-                if (i != k) W[i * m + j] = __fsub_rn(j == k ? 0.f : W[i * m + j], __fmul_rn(col[i], akj));
+        float d = ck[p];
+        if (fabsf(d) < 1.17549435e-38f) d = 1.17549435e-38f;                     // singular: smallest normal pivot
+        float akj[kGjCols];                                                       // the scaled pivot row
+#pragma unroll
+        for (int c = 0; c < kGjCols; ++c) {
+            const int j = lane + 32 * c;
+            akj[c] = j == k ? __fdiv_rn(1.f, d) : __fdiv_rn(rowP[j], d);
+        }
+        if (p != k && wg == p % kGjWarps) {                                       // row p takes row k
+            const int rp = p / kGjWarps;
+#pragma unroll
+            for (int c = 0; c < kGjCols; ++c) {
+                const float v = rowK[lane + 32 * c];
+#pragma unroll
+                for (int r = 0; r < kGjRows; ++r) R[r][c] = rp == r ? v : R[r][c];
+            }
+        }
+        const float ckk = ck[k];
+#pragma unroll
+        for (int r = 0; r < kGjRows; ++r) {
+            const int i = wg + kGjWarps * r;
+            const float cik = i == p ? ckk : ck[i];                              // column k after the interchange
+#pragma unroll
+            for (int c = 0; c < kGjCols; ++c) {
+                const int j = lane + 32 * c;
+                R[r][c] = i == k ? akj[c] : __fsub_rn(j == k ? 0.f : R[r][c], __fmul_rn(cik, akj[c]));
+            }
+        }
+        const int kn = k + 1;                                   // the next pivot column, by its owning lane
+        if (kn < m && lane == kn % 32) {
+            float* cn = colk[kn & 1];
+            const int kc = kn / 32;
+#pragma unroll
+            for (int r = 0; r < kGjRows; ++r) {
+                float v = R[r][0];
+#pragma unroll
+                for (int c = 1; c < kGjCols; ++c) v = kc == c ? R[r][c] : v;
+                cn[wg + kGjWarps * r] = v;
+            }
         }
     }
     __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kGjRows; ++r)
+#pragma unroll
+        for (int c = 0; c < kGjCols; ++c) {
+            const int i = wg + kGjWarps * r, j = lane + 32 * c;
+            if (i < m && j < m) W[i * m + j] = R[r][c];
+        }
+    __syncthreads();
+    const int j = tid;
     // the row interchanges of the elimination become column interchanges of the inverse, in reverse order
     if (j < m)
         for (int k = m - 1; k >= 0; --k) {
@@ -493,7 +565,7 @@ void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st) {
     if (fp32) {
         const int smem = int(sizeof(float)) * (kInvSmemRows * kInvSmemRows + kInvSmemRows);
         raise_smem_limit(reinterpret_cast<const void*>(k_coarse_gj), smem);
-        k_coarse_gj<<<G.nsys, 256, smem, st>>>(G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.invf);
+        k_coarse_gj<<<G.nsys, kGjThreads, smem, st>>>(G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.invf);
         if (G.maxCoarse > kInvSmemRows) {                        // levels too large for shared memory: LU, then columns
             raise_smem_limit(reinterpret_cast<const void*>(k_coarse_inv), smem);
             k_coarse_lu<float><<<G.nsys, 256, 0, st>>>(G.nsys, G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.luf, G.piv, G.cin,

@@ -17,6 +17,7 @@ constexpr int SLOTS = 3;              // factor block slots per row and triangle
 constexpr int LREC = 28;              // factor values per row record of L: SLOTS blocks + 1 pad (16-byte multiple)
 constexpr int UREC = 36;              // per row record of U and D: SLOTS blocks + the inverted diagonal block
 constexpr int SPREC = 24;             // CPR pressure columns of S per row: (SLOTS + 1 + SLOTS) blocks x 3 + 3 pad
+constexpr int OV_CHUNK = 4;           // overflow entries a sweep reads at once (the lists are padded to allow it)
 
 // Krylov status per system (device int)
 enum : int { ST_RUNNING = 0, ST_CONV = 1, ST_BREAKDOWN = 2, ST_MAXIT = 3, ST_CYCLE = 4 /* GMRES: restart cycle ended */,
@@ -65,7 +66,9 @@ struct HostPlan {
     // further blocks continue in an overflow list, terminated by a column of -1.
     //   Lslot[4k + j], j < SLOTS: local column of slot j (-1 empty); Lslot[4k + 3]: overflow start (-1 none)
     //   LslotSrc[SLOTS k + j]: source block position of slot j (-1 empty)
-    //   LovCol / LovSrc: overflow entries (local column, source block; -1 / -1 ends a row's list)
+    //   LovCol / LovSrc: overflow entries (local column, source block; -1 / -1 ends a row's list). OV_CHUNK - 1
+    //   further -1 / -1 entries follow the last list, so OV_CHUNK entries from any position up to a terminator
+    //   are readable.
     std::vector<int> Lslot, LslotSrc, LovCol, LovSrc;
     std::vector<int> Uslot, UslotSrc, UovCol, UovSrc;
     std::vector<int> Dsrc;               // diagonal (U_ii^-1) block of row k

@@ -255,6 +255,8 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
         fill(k, P.diag[size_t(k)] + 1, P.rowPtr[size_t(k) + 1], base, P.Uslot, P.UslotSrc, P.UovCol, P.UovSrc);
         P.Dsrc[size_t(k)] = P.diag[size_t(k)];
     }
+    for (auto* v : {&P.LovCol, &P.LovSrc, &P.UovCol, &P.UovSrc})
+        if (!v->empty()) v->insert(v->end(), size_t(OV_CHUNK - 1), -1);
     return true;
 }
 

@@ -153,6 +153,29 @@ __device__ __forceinline__ void sub_block(TV (&yi)[3], const TF* a, const TV* y,
     yi[2] = vsub(yi[2], rdot(a + 6, yc));
 }
 
+// yi -= sum over the overflow list from position q (columns oc, blocks ov) in list order. The entries come in
+// chunks of OV_CHUNK whose columns and blocks are all loaded before the first is used: a row with many
+// couplings (a well cell) costs one memory latency per chunk, not two per entry. Entries past a row's
+// terminator are read but not used (the lists are padded so that they exist).
+template <class TF, class TV>
+__device__ __forceinline__ void ov_sub(TV (&yi)[3], const int* __restrict__ oc, const TF* __restrict__ ov, int q, const TV* y) {
+    for (;; q += OV_CHUNK) {
+        int c[OV_CHUNK];
+        TF a[OV_CHUNK][9];
+#pragma unroll
+        for (int u = 0; u < OV_CHUNK; ++u) c[u] = __ldg(oc + q + u);
+#pragma unroll
+        for (int u = 0; u < OV_CHUNK; ++u)
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[u][e] = __ldg(ov + size_t(q + u) * 9 + e);
+#pragma unroll
+        for (int u = 0; u < OV_CHUNK; ++u) {
+            if (c[u] < 0) return;
+            sub_block(yi, a[u], y, c[u]);
+        }
+    }
+}
+
 // y_i = in_i - sum_{k<i} L_ik y_k (engine/src/bsr.cpp:568-575): slots, then the overflow list, in row order
 template <class TF, class TV, class TI, int MODE>
 __device__ __forceinline__ void fwd_step(const FwdRow<TF, TI, MODE>& R, const IluArgs<TF>& F, int row0, TV* y, double* pv, double beta,
@@ -179,15 +202,7 @@ __device__ __forceinline__ void fwd_step(const FwdRow<TF, TI, MODE>& R, const Il
         const int c = slot_col(R.c, j);
         if (c >= 0) sub_block(yi, R.a + 9 * j, y, c);
     }
-    if (R.c.w >= 0)
-        for (int q = R.c.w;; ++q) {
-            const int c = __ldg(F.LovCol + q);
-            if (c < 0) break;
-            TF a[9];
-#pragma unroll
-            for (int e = 0; e < 9; ++e) a[e] = __ldg(F.Lov + size_t(q) * 9 + e);
-            sub_block(yi, a, y, c);
-        }
+    if (R.c.w >= 0) ov_sub(yi, F.LovCol, F.Lov, R.c.w, y);
     const int li = k - row0;
     y[li * 3 + 0] = yi[0]; y[li * 3 + 1] = yi[1]; y[li * 3 + 2] = yi[2];
 }
@@ -203,15 +218,7 @@ __device__ __forceinline__ void bwd_step(const BwdRow<TF>& R, const IluArgs<TF>&
         const int c = slot_col(R.c, j);
         if (c >= 0) sub_block(yi, R.a + 9 * j, y, c);
     }
-    if (R.c.w >= 0)
-        for (int q = R.c.w;; ++q) {
-            const int c = __ldg(F.UovCol + q);
-            if (c < 0) break;
-            TF a[9];
-#pragma unroll
-            for (int e = 0; e < 9; ++e) a[e] = __ldg(F.Uov + size_t(q) * 9 + e);
-            sub_block(yi, a, y, c);
-        }
+    if (R.c.w >= 0) ov_sub(yi, F.UovCol, F.Uov, R.c.w, y);
     const TF* d = R.a + 9 * SLOTS;
     const TV t0 = rdot(d, yi), t1 = rdot(d + 3, yi), t2 = rdot(d + 6, yi);
     y[li * 3 + 0] = t0; y[li * 3 + 1] = t1; y[li * 3 + 2] = t2;
@@ -422,13 +429,21 @@ __device__ __forceinline__ void gs_step(const GsRow<TA, W>& R, const AmgSysLv& A
 #pragma unroll
     for (int j = 0; j < W; ++j)
         if (j < lim) s = asub(s, amul(R.v[j], x[R.c[j]]));
-    if (lim > W) {
+    if (lim > W) {                    // entries after the slots, in chunks as ov_sub (the arrays are padded)
         const int* ci = C.ci + A.entOff;
         const TA* val = C.val + A.entOff;
-        for (int p = R.m.z, jo = W; jo < lim; ++p) {
-            if (p == R.m.w) continue;
-            s = asub(s, amul(val[p], x[__ldg(ci + p)]));
-            ++jo;
+        int jo = W;
+        for (int p = R.m.z; jo < lim; p += OV_CHUNK) {
+            int c[OV_CHUNK];
+            TA a[OV_CHUNK];
+#pragma unroll
+            for (int u = 0; u < OV_CHUNK; ++u) { c[u] = __ldg(ci + p + u); a[u] = val[p + u]; }
+#pragma unroll
+            for (int u = 0; u < OV_CHUNK; ++u)
+                if (jo < lim && p + u != R.m.w) {
+                    s = asub(s, amul(a[u], x[c[u]]));
+                    ++jo;
+                }
         }
     }
     x[R.k] = adiv(s, R.d);
@@ -827,6 +842,26 @@ __device__ __forceinline__ void sub_p(float (&acc)[3], const float* s3, float xk
     for (int e = 0; e < 3; ++e) acc[e] = acc[e] - s3[e] * xk;
 }
 
+// acc -= the overflow list's pressure columns times xp, from position q in list order, in chunks as ov_sub
+template <class TV, class TA>
+__device__ __forceinline__ void ov_sub_p(TV (&acc)[3], const int* __restrict__ oc, const TA* __restrict__ s3v, int q, const TA* xp) {
+    for (;; q += OV_CHUNK) {
+        int c[OV_CHUNK];
+        TA s3[OV_CHUNK][3];
+#pragma unroll
+        for (int u = 0; u < OV_CHUNK; ++u) {
+            c[u] = __ldg(oc + q + u);
+#pragma unroll
+            for (int e = 0; e < 3; ++e) s3[u][e] = __ldg(s3v + size_t(q + u) * 3 + e);
+        }
+#pragma unroll
+        for (int u = 0; u < OV_CHUNK; ++u) {
+            if (c[u] < 0) return;
+            sub_p(acc, s3[u], TV(xp[c[u]]));
+        }
+    }
+}
+
 // One CPR application per system. The second-stage input t lives in C.T with the sweep vector's type TV: FP64
 // for the FP64 and mixed forms, FP32 for the all-FP32 preconditioner, whose restriction w . r, t = r - S[:,p] xp
 // and sweeps then run in FP32 arithmetic (the FP64 unit is a small fraction of the FP32 rate on this part).
@@ -899,34 +934,37 @@ __global__ void __launch_bounds__(NT) k_cpr_cta(IluArgs<TF> F, CprArgs<TA> C, co
     // memory for the final correction when it lived on chip
     const TA* xp = V.x(A0, C);
     TA* xpg = C.x + A0.rowOff;
-    for (int k = row0 + tid; k < row0 + ns; k += nt) {
-        const int4 lc = __ldg(F.Lslot + k), uc = __ldg(F.Uslot + k);
-        TA sp[SPREC];
-        ldrec(sp, C.sp + size_t(k) * SPREC);
-        TV acc[3] = {T[size_t(k) * 3], T[size_t(k) * 3 + 1], T[size_t(k) * 3 + 2]};
+    // rows in batches of TB (all record loads of a batch issued before any use)
+    constexpr int TB = 2;
+    for (int base = row0 + tid; base < row0 + ns; base += TB * nt) {
+        int4 lc[TB], uc[TB];
+        TA sp[TB][SPREC];
+        TV acc[TB][3];
 #pragma unroll
-        for (int j = 0; j < SLOTS; ++j)
-            if (slot_col(lc, j) >= 0) sub_p(acc, sp + 3 * j, TV(xp[slot_col(lc, j)]));
-        if (lc.w >= 0)
-            for (int q = lc.w;; ++q) {
-                const int c = __ldg(F.LovCol + q);
-                if (c < 0) break;
-                const TA s3[3] = {__ldg(C.spLov + size_t(q) * 3), __ldg(C.spLov + size_t(q) * 3 + 1), __ldg(C.spLov + size_t(q) * 3 + 2)};
-                sub_p(acc, s3, TV(xp[c]));
-            }
-        sub_p(acc, sp + 3 * SLOTS, TV(xp[k - row0]));
+        for (int u = 0; u < TB; ++u) {
+            const int k = min(base + u * nt, row0 + ns - 1);    // past the end: re-read the last row, not stored
+            lc[u] = __ldg(F.Lslot + k);
+            uc[u] = __ldg(F.Uslot + k);
+            ldrec(sp[u], C.sp + size_t(k) * SPREC);
 #pragma unroll
-        for (int j = 0; j < SLOTS; ++j)
-            if (slot_col(uc, j) >= 0) sub_p(acc, sp + 3 * (SLOTS + 1 + j), TV(xp[slot_col(uc, j)]));
-        if (uc.w >= 0)
-            for (int q = uc.w;; ++q) {
-                const int c = __ldg(F.UovCol + q);
-                if (c < 0) break;
-                const TA s3[3] = {__ldg(C.spUov + size_t(q) * 3), __ldg(C.spUov + size_t(q) * 3 + 1), __ldg(C.spUov + size_t(q) * 3 + 2)};
-                sub_p(acc, s3, TV(xp[c]));
-            }
-        T[size_t(k) * 3] = acc[0]; T[size_t(k) * 3 + 1] = acc[1]; T[size_t(k) * 3 + 2] = acc[2];
-        if (V.xs) xpg[k - row0] = xp[k - row0];
+            for (int e = 0; e < 3; ++e) acc[u][e] = T[size_t(k) * 3 + e];
+        }
+#pragma unroll
+        for (int u = 0; u < TB; ++u) {
+            const int k = base + u * nt;
+            if (k >= row0 + ns) break;
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+                if (slot_col(lc[u], j) >= 0) sub_p(acc[u], sp[u] + 3 * j, TV(xp[slot_col(lc[u], j)]));
+            if (lc[u].w >= 0) ov_sub_p(acc[u], F.LovCol, C.spLov, lc[u].w, xp);
+            sub_p(acc[u], sp[u] + 3 * SLOTS, TV(xp[k - row0]));
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+                if (slot_col(uc[u], j) >= 0) sub_p(acc[u], sp[u] + 3 * (SLOTS + 1 + j), TV(xp[slot_col(uc[u], j)]));
+            if (uc[u].w >= 0) ov_sub_p(acc[u], F.UovCol, C.spUov, uc[u].w, xp);
+            T[size_t(k) * 3] = acc[u][0]; T[size_t(k) * 3 + 1] = acc[u][1]; T[size_t(k) * 3 + 2] = acc[u][2];
+            if (V.xs) xpg[k - row0] = xp[k - row0];
+        }
     }
     __syncthreads();
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
@@ -963,6 +1001,7 @@ __device__ __forceinline__ void gemm3f(const float* a, const float* b, float* c)
         c[i * 3 + 0] = r0; c[i * 3 + 1] = r1; c[i * 3 + 2] = r2;
     }
 }
+constexpr int kFacChunk = 4;       // elimination targets of one entry loaded at once
 __device__ __forceinline__ void gemm3f_sub(const float* a, const float* b, float* c) {
     float t[9];
     gemm3f(a, b, t);
@@ -983,27 +1022,51 @@ __global__ void __launch_bounds__(kCtaThreads) k_factor_cta_f32(const int* __res
     __syncthreads();
     const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
     int reg = 0;
+    float Lb[9];
     for (int L = 0; L < nl; ++L) {
         const int k1 = __ldg(lvlStart + l0 + L + 1);
         for (int i = __ldg(lvlStart + l0 + L) + tid; i < k1; i += nt) {
             const int p0 = __ldg(rowPtr + i), d = __ldg(diag + i);
+            // the indices of entry p (column k, elimination list [q0, q1)) are loaded one entry ahead, so an entry
+            // costs two dependent loads (diag[k] with its first elimination targets, then every block it touches)
+            int k = 0, q0 = 0, q1 = 0;
+            if (p0 < d) { k = __ldg(col + p0); q0 = __ldg(elimPtr + p0); q1 = __ldg(elimPtr + p0 + 1); }
             for (int p = p0; p < d; ++p) {
-                const int k = __ldg(col + p);
-                float a[9], u[9], Lb[9];
+                const int kn = p + 1 < d ? __ldg(col + p + 1) : 0;
+                const int q2 = p + 1 < d ? __ldg(elimPtr + p + 2) : 0;
+                const int dk = __ldg(diag + k);
+                for (int qc = q0; qc == q0 || qc < q1; qc += kFacChunk) {
+                    int t[kFacChunk], uq[kFacChunk];
 #pragma unroll
-                for (int e = 0; e < 9; ++e) { a[e] = F[size_t(p) * 9 + e]; u[e] = F[size_t(__ldg(diag + k)) * 9 + e]; }
-                gemm3f(a, u, Lb);                                     // L_ik = A_ik U_kk^-1
+                    for (int v = 0; v < kFacChunk; ++v) {
+                        const bool ok = qc + v < q1;
+                        t[v] = ok ? __ldg(elimT + qc + v) : -1;
+                        uq[v] = ok ? __ldg(elimQ + qc + v) : 0;
+                    }
+                    float U[kFacChunk][9], Cb[kFacChunk][9];
 #pragma unroll
-                for (int e = 0; e < 9; ++e) F[size_t(p) * 9 + e] = Lb[e];
-                for (int q = __ldg(elimPtr + p); q < __ldg(elimPtr + p + 1); ++q) {
-                    const int t = __ldg(elimT + q), uq = __ldg(elimQ + q);
-                    float U[9], Cb[9];
+                    for (int v = 0; v < kFacChunk; ++v)
+                        if (t[v] >= 0) {
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) { U[e] = F[size_t(uq) * 9 + e]; Cb[e] = F[size_t(t) * 9 + e]; }
-                    gemm3f_sub(Lb, U, Cb);                            // A_it -= L_ik U_kq
+                            for (int e = 0; e < 9; ++e) { U[v][e] = F[size_t(uq[v]) * 9 + e]; Cb[v][e] = F[size_t(t[v]) * 9 + e]; }
+                        }
+                    if (qc == q0) {                                   // L_ik = A_ik U_kk^-1, once per entry
+                        float a[9], u[9];
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) F[size_t(t) * 9 + e] = Cb[e];
+                        for (int e = 0; e < 9; ++e) { a[e] = F[size_t(p) * 9 + e]; u[e] = F[size_t(dk) * 9 + e]; }
+                        gemm3f(a, u, Lb);
+#pragma unroll
+                        for (int e = 0; e < 9; ++e) F[size_t(p) * 9 + e] = Lb[e];
+                    }
+#pragma unroll
+                    for (int v = 0; v < kFacChunk; ++v)
+                        if (t[v] >= 0) {
+                            gemm3f_sub(Lb, U[v], Cb[v]);                 // A_it -= L_ik U_kq (targets of one entry differ)
+#pragma unroll
+                            for (int e = 0; e < 9; ++e) F[size_t(t[v]) * 9 + e] = Cb[v][e];
+                        }
                 }
+                k = kn; q0 = q1; q1 = q2;
             }
             double D[9];
 #pragma unroll
