@@ -64,7 +64,10 @@ typedef struct rsg_options {
     int device;             /* CUDA device ordinal */
     size_t mem_budget;      /* bytes this handle may hold on the device (0 = no limit) */
     int sweep;              /* BILU0 sweep scheduling: 0 auto, 1 one thread block per system (level barriers,
-                               shared-memory vector), 2 grid-wide sync-free (per-row flags) */
+                               shared-memory vector), 2 grid-wide sync-free (per-row flags), 3 split CPR: the
+                               V-cycle's passes grid-wide over all systems, the BILU0 sweeps one thread block per
+                               system (same results as 1). Auto takes 3 for CPR and 1 for BILU0 where the thread-block
+                               sweeps apply, else 2 */
     int fma;                /* 1 (default): the SpMV accumulates with fused multiply-adds (half the FP64
                                instructions; results within rounding of the reference); 0: the reference's separately
                                rounded products and sums, bit for bit (engine/src/bsr.cpp:109-117) */

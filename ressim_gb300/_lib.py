@@ -16,7 +16,7 @@ RSG_OK, RSG_EINVAL, RSG_ECUDA, RSG_ENOMEM, RSG_ESTATE, RSG_ETIMEOUT, RSG_EBREAKD
 PREC = {"bilu0": 0, "cpr": 1, "jacobi": 2, "cpr_device": 3, "mcbilu0": 4}
 KRYLOV = {"bicgstab": 0, "gmres": 1}
 PRECISION = {"fp64": 0, "mixed": 1, "mixed_f32": 2}
-SWEEP = {"auto": 0, "cta": 1, "grid": 2}
+SWEEP = {"auto": 0, "cta": 1, "grid": 2, "split": 3}
 
 # every symbol include/rsg.h declares
 EXPORTS = [

@@ -97,6 +97,7 @@ struct rsg_solver {
     SplitFactors<double> s64;
     SplitFactors<float> s32;
     bool cta = false;
+    bool splitCpr = false;       // CPR on the thread-block path: V-cycle grid-wide (PrecDev::split)
     bool escalated = false;      // precision form: failed systems re-solved with FP64 sweep vectors (until the next set-up)
     // CPR: device AMG of the batch (allocated in pmem; built at the first CPR set-up of a pattern)
     DevAmg amg;
@@ -196,7 +197,12 @@ int alloc_plan(rsg_solver* h) {
         D.sweepBlocks = sweep_blocks_for(double(P.n) / double(maxLv), h->opt.sweep_inflight);
     }
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
-    if (h->opt.sweep == 1 && !h->cta) return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
+    if ((h->opt.sweep == 1 || h->opt.sweep == 3) && !h->cta)
+        return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
+    // CPR on the thread-block path: the V-cycle's parallel passes grid-wide (all systems at once, the whole GPU's
+    // loads in flight) unless the one-kernel form is asked for. The choice does not depend on the batch, so a
+    // system's result does not either.
+    h->splitCpr = h->cta && (h->opt.sweep == 3 || h->opt.sweep == 0);
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
     if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
         (rc = dalloc(M, &h->tmp, N)))
@@ -248,7 +254,7 @@ int check_device_errors(rsg_solver* h) {
 // kernel launches of one preconditioner application
 int precond_launches(const PrecDev& M) {
     if (M.devcpr) return devcpr_launches(*M.amg);
-    if (M.cpr && !M.cta) return cpr_grid_launches(*M.amg);
+    if (M.cpr && (!M.cta || M.split)) return cpr_grid_launches(*M.amg, M.split);
     return M.cpr || M.cta || M.kind == 2 ? 1 : 2;
 }
 
@@ -268,6 +274,7 @@ PrecDev prec_dev(rsg_solver* h) {
         M.cta = true;
         M.s64 = h->s64;
         M.s32 = h->s32;
+        M.split = M.cpr && h->splitCpr;
     }
     return M;
 }
@@ -1031,7 +1038,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     rsg_options o;
     rsg_default_options(&o);
     if (opts) o = *opts;
-    if (o.precond < 0 || o.precond > 4 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 2)
+    if (o.precond < 0 || o.precond > 4 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 3)
         return fail(RSG_EINVAL, "invalid options");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
@@ -1194,7 +1201,7 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
 static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
     const PrecDev M = prec_dev(h);
     if (M.devcpr) h->launches += launch_devcpr(h->dp, h->amg, h->val, 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream);
-    else if (M.cpr && M.cta) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
+    else if (M.cpr && M.cta && !M.split) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
     else if (M.cpr) h->launches += launch_cpr_grid(h->dp, M, *M.amg, 0, d_r, nullptr, nullptr, d_z, nullptr, h->S, h->d_err, h->stream);
     else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
     else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }

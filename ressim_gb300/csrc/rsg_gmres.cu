@@ -335,7 +335,7 @@ void launch_gm_pick(const DevPlan& P, double* x, const double* xPrev, const KSca
 void launch_precond_gm(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
                        cudaStream_t st) {
     if (M.devcpr) launch_devcpr(P, *M.amg, M.val, 0, r, nullptr, nullptr, z, ks, st);
-    else if (M.cpr && M.cta) launch_cpr_cta(P, M, *M.amg, 0, M.kind != 0, r, nullptr, nullptr, z, ks, st);
+    else if (M.cpr && M.cta && !M.split) launch_cpr_cta(P, M, *M.amg, 0, M.kind != 0, r, nullptr, nullptr, z, ks, st);
     else if (M.cpr) launch_cpr_grid(P, M, *M.amg, 0, r, nullptr, nullptr, z, ks, S, err, st);
     else if (M.cta) launch_ilu_cta_apply_ks(P, M, r, z, ks, st);
     else if (M.kind == 0) launch_ilu_apply_f64(P, M.lu, r, z, S, err, st);

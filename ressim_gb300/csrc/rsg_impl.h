@@ -209,7 +209,8 @@ void launch_cpr_cta(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mod
                     const double* v, double* z, const KScal* ks, cudaStream_t st);
 // the same application grid-wide for systems of any size (rsg_sweep_cta.cu): input and restriction, the V-cycle one
 // level at a time with sync-free Gauss-Seidel sweeps, coarse solve per system, t = r - S[:,p] xp, the grid BILU0
-// sweeps, z_p += xp. Returns the number of kernel launches.
+// sweeps, z_p += xp; with M.split the second stage (t, the BILU0 sweeps, z_p += xp) is the thread-block kernel's,
+// on the split factors, so that the result is the thread-block application's. Returns the number of kernel launches.
 int launch_cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, const double* r, double* pv, const double* v,
                     double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st);
 // the reference's GPU-shaped float CPR-AMG (rsg_devcpr.cu): set-up (coarse inverse, inverse diagonals, block
@@ -218,8 +219,8 @@ int launch_devcpr_setup(const DevPlan& P, const double* val, DevAmg& G, cudaStre
 int launch_devcpr(const DevPlan& P, const DevAmg& G, const double* val, int mode, const double* r, double* pv, const double* v, double* z,
                   const KScal* ks, cudaStream_t st);
 int devcpr_launches(const DevAmg& G);
-inline int cpr_grid_launches(const DevAmg& G) {
-    int n = 6 + 2 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
+inline int cpr_grid_launches(const DevAmg& G, bool split = false) {
+    int n = (split ? 4 : 6) + 2 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
     for (int l = 0; l + 1 < G.maxL; ++l) {          // pre- and post-smoothing: one sweep, or a launch per large colour + the tail
         const int nc = l < int(G.colBeg.size()) ? int(G.colBeg[size_t(l)].size()) - 1 : 0;
         n += 2 * (nc > 0 ? G.colTail[size_t(l)] + (G.colTail[size_t(l)] < nc ? 1 : 0) : 1);
@@ -321,6 +322,8 @@ struct PrecDev {
     unsigned long long* yt = nullptr; // grid-wide all-FP32 sweeps: tagged sweep vector
     bool cpr = false;                 // CPR two-stage preconditioner (AMG on the pressure system + BILU0)
     bool devcpr = false;              // the reference's GPU-shaped float CPR-AMG
+    bool split = false;               // CPR with cta: V-cycle and second-stage input grid-wide (all systems at once),
+                                      // the BILU0 sweeps one thread block per system
     const DevAmg* amg = nullptr;
 };
 // all-FP32 factorisation (FP32 elimination, FP64 pivot inversion), one thread block per system

@@ -836,7 +836,7 @@ void launch_bicg_iteration(const DevPlan& P, const double* val, const PrecDev& M
     auto prec = [&](bool pupd, double* out) {
         if (M.devcpr) {
             launch_devcpr(P, *M.amg, val, pupd ? 1 : 2, V.r, pupd ? V.p : V.s, V.v, out, ks, st);
-        } else if (M.cpr && M.cta) {
+        } else if (M.cpr && M.cta && !M.split) {
             launch_cpr_cta(P, M, *M.amg, pupd ? 1 : 2, M.kind != 0, V.r, pupd ? V.p : V.s, V.v, out, ks, st);
         } else if (M.cpr) {
             launch_cpr_grid(P, M, *M.amg, pupd ? 1 : 2, V.r, pupd ? V.p : V.s, V.v, out, ks, S, err, st);

@@ -1247,11 +1247,12 @@ int grid_for(long long n, int threads) {
     return int(b < 1 ? 1 : (b < cap ? b : cap));
 }
 
-// input (the fused Krylov update of the mode), T = input (FP64), level-0 right-hand side b0 = w . input
-// (bsr.cpp:1064-1067; TT: the arithmetic of the restriction, FP32 in the all-FP32 form)
-template <int MODE, class TA, class TT>
+// input (the fused Krylov update of the mode), T = input (TS: FP64, or the split form's second-stage type),
+// level-0 right-hand side b0 = w . input (bsr.cpp:1064-1067; TT: the arithmetic of the restriction, FP32 in the
+// all-FP32 form)
+template <int MODE, class TA, class TT, class TS>
 __global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ rowSys, const double* r, double* pv, const double* v,
-                                                 const double* __restrict__ w, double* T, TA* b0, const KScal* ks) {
+                                                 const double* __restrict__ w, TS* T, TA* b0, const KScal* ks) {
     for (int k = int(blockIdx.x * blockDim.x + threadIdx.x); k < n; k += int(gridDim.x * blockDim.x)) {
         double beta = 0, omega = 0, alpha = 0;
         if (ks) {
@@ -1266,7 +1267,7 @@ __global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ 
             if (MODE == IN_PUPDATE) { in[e] = da(r[q], dm(beta, ds(pv[q], dm(omega, v[q])))); pv[q] = in[e]; }
             else if (MODE == IN_SUPDATE) { in[e] = ds(r[q], dm(alpha, v[q])); pv[q] = in[e]; }
             else in[e] = r[q];
-            T[q] = in[e];
+            T[q] = TS(in[e]);
         }
         const double w0 = __ldg(w + size_t(k) * 3), w1 = __ldg(w + size_t(k) * 3 + 1), w2 = __ldg(w + size_t(k) * 3 + 2);
         if (sizeof(TT) == 4) b0[k] = TA(float(w0) * float(in[0]) + float(w1) * float(in[1]) + float(w2) * float(in[2]));
@@ -1378,8 +1379,8 @@ __global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, con
 // The small colours (from colour `tail` on) of a level in one sync-free pass. Their rows are the long rows of the
 // well cliques, so a warp takes one row: rows are claimed in colour order (forward ascending, backward
 // descending), the lanes split the row's entries, poll together the flags of its neighbours of an earlier colour
-// inside the tail (forward; a later one backward) until the whole warp sees them set, then sum their terms and
-// meet in a shuffle tree. The large colours are done before (forward) or after (backward) by their own passes, so
+// inside the tail (forward; a later one backward) until the whole warp sees them set, then take the terms in entry
+// order. The large colours are done before (forward) or after (backward) by their own passes, so
 // their values are final or old as the multicolour order wants. Flags: 1 after the forward pass, 0 after the
 // backward one; bounded waits (ERR_TIMEOUT).
 template <class TA, bool FWD, bool ZERO>
@@ -1428,16 +1429,27 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_tail(int i0, int i1, int ta
                 }
             }
             fence_acquire();
-            TA t = TA(0);
-            for (int p = d.y + lane; p < d.z; p += 32) {
-                if (p == d.w) continue;
-                const int j = __ldg(gci + p);
-                if (ZERO && __ldg(wave + j) > wi) continue;            // x_j is still zero: the term vanishes
-                t = aadd(t, amul(__ldg(val + p), x[j]));
+            // s = b - sum a_p x_p in entry order, one rounding after another as the thread-per-row passes and the
+            // thread-block sweeps do (the lanes load a chunk's terms, every lane runs the chain on the broadcasts),
+            // so a row's value does not depend on which pass took its colour
+            TA s = b[d.x];
+            for (int p0 = d.y; p0 < d.z; p0 += 32) {
+                const int p = p0 + lane;
+                TA a = TA(0), xv = TA(0);
+                bool use = false;
+                if (p < d.z && p != d.w) {
+                    const int j = __ldg(gci + p);
+                    use = !(ZERO && __ldg(wave + j) > wi);              // x_j still zero: the term is not taken
+                    if (use) { a = __ldg(val + p); xv = x[j]; }
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, use);
+                const int cnt = min(32, d.z - p0);
+                for (int u = 0; u < cnt; ++u) {
+                    const TA au = __shfl_sync(0xffffffffu, a, u), xu = __shfl_sync(0xffffffffu, xv, u);
+                    if ((m >> u) & 1u) s = asub(s, amul(au, xu));
+                }
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t = aadd(t, __shfl_xor_sync(0xffffffffu, t, o));
-            if (lane == 0) x[d.x] = adiv(asub(b[d.x], t), __ldg(val + d.w));
+            if (lane == 0) x[d.x] = adiv(s, __ldg(val + d.w));
         }
         __syncwarp();
         if (lane == 0) st_release(flag + d.x, want);
@@ -1544,14 +1556,74 @@ __global__ void __launch_bounds__(256) k_gcpr_zp(int n, const int* __restrict__ 
     }
 }
 
+// split form, second-stage input: t = T - S[:,p] xp in the thread-block kernel's slot order and arithmetic
+// (bsr.cpp:1071-1081), one row per thread over every system; xp = the level-0 V-cycle solution of the row's system
+template <class TA, class TV>
+__global__ void __launch_bounds__(256) k_gcpr_tsp(int n, const int* __restrict__ rowSys, const int* __restrict__ sysRow0, int maxL,
+                                                  const AmgSysLv* __restrict__ lv, const int4* __restrict__ Lslot,
+                                                  const int4* __restrict__ Uslot, const int* __restrict__ LovCol,
+                                                  const int* __restrict__ UovCol, const TA* __restrict__ sp, const TA* __restrict__ spLov,
+                                                  const TA* __restrict__ spUov, const TA* x, TV* T, const KScal* ks) {
+    for (int k = int(blockIdx.x * blockDim.x + threadIdx.x); k < n; k += int(gridDim.x * blockDim.x)) {
+        const int s = __ldg(rowSys + k);
+        if (ks && ks[s].status != ST_RUNNING) continue;
+        const int li = k - __ldg(sysRow0 + s);
+        const TA* xp = x + __ldg(&lv[s * maxL].rowOff);
+        const int4 lc = __ldg(Lslot + k), uc = __ldg(Uslot + k);
+        TA spr[SPREC];
+        ldrec(spr, sp + size_t(k) * SPREC);
+        TV acc[3] = {T[size_t(k) * 3], T[size_t(k) * 3 + 1], T[size_t(k) * 3 + 2]};
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (slot_col(lc, j) >= 0) sub_p(acc, spr + 3 * j, TV(xp[slot_col(lc, j)]));
+        if (lc.w >= 0) ov_sub_p(acc, LovCol, spLov, lc.w, xp);
+        sub_p(acc, spr + 3 * SLOTS, TV(xp[li]));
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (slot_col(uc, j) >= 0) sub_p(acc, spr + 3 * (SLOTS + 1 + j), TV(xp[slot_col(uc, j)]));
+        if (uc.w >= 0) ov_sub_p(acc, UovCol, spUov, uc.w, xp);
+        T[size_t(k) * 3] = acc[0]; T[size_t(k) * 3 + 1] = acc[1]; T[size_t(k) * 3 + 2] = acc[2];
+    }
+}
+
+// split form, second stage: the BILU0 sweeps of one system per thread block on t, z_p += xp as z is written (the
+// tail of k_cpr_cta)
+template <class TF, class TV, class TA, int NT = cta_threads<TF, TV>()>
+__global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const AmgSysLv* __restrict__ lv, const TA* x, const TV* T,
+                                                 double* z, TV* yglob, size_t smemBytes, const KScal* ks) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int s = blockIdx.x, tid = int(threadIdx.x), nt = int(blockDim.x);
+    if (ks && ks[s].status != ST_RUNNING) return;
+    const int row0 = __ldg(F.sysRow0 + s), ns = __ldg(F.sysRow0 + s + 1) - row0;
+    const TA* xpg = x + __ldg(&lv[s * maxL].rowOff);
+    const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
+    TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
+    const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
+    if (onchip || sizeof(TV) != sizeof(double)) {
+        ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
+    } else {
+        ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
+        for (int k = row0 + tid; k < row0 + ns; k += nt) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xpg[k - row0]));
+    }
+}
+
 template <class TA, class TT>
 int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, const TA* val, int mode, const double* r,
              double* pv, const double* v, double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st) {
     const int n = P.n, gn = grid_for(n, 256);
     int launches = 0;
-    if (mode == IN_PUPDATE) k_gcpr_in<IN_PUPDATE, TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
-    else if (mode == IN_SUPDATE) k_gcpr_in<IN_SUPDATE, TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
-    else k_gcpr_in<IN_PLAIN, TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+    // the split form keeps t in the second stage's sweep type (TT: FP32 in the all-FP32 form), as the thread-block
+    // kernel does
+    TT* Tsplit = reinterpret_cast<TT*>(G.T);
+    if (M.split) {
+        if (mode == IN_PUPDATE) k_gcpr_in<IN_PUPDATE, TA, TT, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, Tsplit, C.b, ks);
+        else if (mode == IN_SUPDATE) k_gcpr_in<IN_SUPDATE, TA, TT, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, Tsplit, C.b, ks);
+        else k_gcpr_in<IN_PLAIN, TA, TT, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, Tsplit, C.b, ks);
+    } else {
+        if (mode == IN_PUPDATE) k_gcpr_in<IN_PUPDATE, TA, TT, double><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+        else if (mode == IN_SUPDATE) k_gcpr_in<IN_SUPDATE, TA, TT, double><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+        else k_gcpr_in<IN_PLAIN, TA, TT, double><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, G.T, C.b, ks);
+    }
     ++launches;
     const auto& LB = G.levelRowBeg;
     auto sweep = [&](int l, int phase, bool fwd, bool zero) {
@@ -1633,6 +1705,28 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
         k_gcpr_prolong<TA><<<grid_for(q1 - q0, 256), 256, 0, st>>>(q0, q1, G.maxL, G.rowLv, G.lv, G.agg, C.x, ks);
         ++launches;
         sweep(l, 0, false, false);
+    }
+    if (M.split) {
+        k_gcpr_tsp<TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, P.sysRow0, G.maxL, G.lv, P.Lslot, P.Uslot, P.LovCol, P.UovCol, C.sp, C.spLov,
+                                              C.spUov, C.x, Tsplit, ks);
+        // second stage: TF = TA (FP64 factors in the FP64 form, FP32 otherwise), TV = TT
+        if constexpr (sizeof(TA) == 8) {
+            const IluArgs<double> F = ilu_args(P, M.s64);
+            raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<double, double, TA>), int(M.smem));
+            k_cpr2_cta<double, double, TA><<<P.nsys, cta_threads<double, double>(), M.smem, st>>>(F, G.maxL, G.lv, C.x, Tsplit, z, z,
+                                                                                                  M.smem, ks);
+        } else if constexpr (sizeof(TT) == 8) {
+            const IluArgs<float> F = ilu_args(P, M.s32);
+            raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<float, double, TA>), int(M.smem));
+            k_cpr2_cta<float, double, TA><<<P.nsys, cta_threads<float, double>(), M.smem, st>>>(F, G.maxL, G.lv, C.x, Tsplit, z, z,
+                                                                                                M.smem, ks);
+        } else {
+            const IluArgs<float> F = ilu_args(P, M.s32);
+            raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<float, float, TA>), int(M.smem));
+            k_cpr2_cta<float, float, TA><<<P.nsys, cta_threads<float, float>(), M.smem, st>>>(F, G.maxL, G.lv, C.x, Tsplit, z, M.y32,
+                                                                                              M.smem, ks);
+        }
+        return launches + 2;
     }
     k_gcpr_t<TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, P.rowPtr, P.col, M.val, C.x, G.T, ks);
     launch_ilu_grid_ks(P, M, G.T, z, ks, S, err, st);

@@ -217,7 +217,7 @@ def test_gpu_block_solver_adapter():
 
 
 # ---------------------------------------------------------------- CPR (AMG on the pressure system + BILU0)
-@pytest.mark.parametrize("sweep", ["cta", "grid"])
+@pytest.mark.parametrize("sweep", ["cta", "split", "grid"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
 def test_cpr_apply_matches_reference(name, sweep):
     """BlockCPR::apply: weights, pressure matrix, aggregation hierarchy, Gauss-Seidel V-cycle and BILU0 are the
@@ -236,7 +236,7 @@ def test_cpr_apply_matches_reference(name, sweep):
             assert rel(d.precond_apply(z["b"]), z["z_cpr_acc"]) < 1e-10
 
 
-@pytest.mark.parametrize("sweep", ["cta", "grid"])
+@pytest.mark.parametrize("sweep", ["cta", "split", "grid"])
 @pytest.mark.parametrize("precision", ["mixed", "mixed_f32"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
 def test_cpr_multicolour_apply_matches_oracle(name, precision, sweep, oracle):
@@ -257,7 +257,7 @@ def test_cpr_multicolour_apply_matches_oracle(name, precision, sweep, oracle):
     assert rel(zd, zo) < 1e-3
 
 
-@pytest.mark.parametrize("sweep", ["cta", "grid"])
+@pytest.mark.parametrize("sweep", ["cta", "split", "grid"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
 def test_cpr_bicgstab_matches_reference(name, sweep):
     A, z = load_golden(name)
@@ -289,7 +289,7 @@ def test_cpr_refresh_equals_fresh_setup():
     assert rel(z1, z2) < 1e-12
 
 
-@pytest.mark.parametrize("sweep", ["cta", "grid"])
+@pytest.mark.parametrize("sweep", ["cta", "split", "grid"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
 def test_cpr_batched_ensemble(precision, sweep):
     from ressim_gb300 import synth
@@ -306,6 +306,27 @@ def test_cpr_batched_ensemble(precision, sweep):
         N = s.A.n * 3
         assert true_res(s.A, x[off:off + N], s.b) <= 1e-5
         off += N
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
+def test_split_cpr_equals_thread_block(precision):
+    """The split CPR (V-cycle passes grid-wide over every system, BILU0 sweeps one thread block per system) gives
+    the one-kernel thread-block application's results: same preconditioner output and same solve, on a batch with
+    well cliques (the small colours of the multicolour smoother)."""
+    from ressim_gb300 import synth
+    systems = synth.ensemble(n_real=6, nx=24, ny=24, nz=6, sigma=1.5)
+    b = np.concatenate([s.b for s in systems])
+    out = {}
+    for sweep in ("cta", "split"):
+        with dev(precond="cpr", precision=precision, check_every=4, sweep=sweep) as d:
+            d.set_batch([s.A for s in systems])
+            d.setup()
+            z = d.precond_apply(b)
+            x, res = d.solve(b, tol=1e-6, maxit=300)
+            out[sweep] = (z, x, d.batch_results()[0])
+    assert np.array_equal(out["cta"][0], out["split"][0])
+    assert np.array_equal(out["cta"][1], out["split"][1])
+    assert np.array_equal(out["cta"][2], out["split"][2])
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
@@ -529,7 +550,7 @@ def test_gmres_bilu0_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
-@pytest.mark.parametrize("sweep", ["cta", "grid"])
+@pytest.mark.parametrize("sweep", ["cta", "split", "grid"])
 def test_gmres_cpr_matches_reference(name, sweep):
     A, z = load_golden(name)
     with dev(krylov="gmres", precond="cpr", restart=30, sweep=sweep) as d:
