@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(256) k_coarse_lu(int nsys, int maxL, const Amg
 
 // Explicit inverse of every coarsest level for the FP32 precision forms (the reference's device-shaped CPR keeps an
 // explicit coarse inverse, engine/src/bsr.cpp:1235-1317): column j = LU^-1 e_j of the level-space unit vector,
-// stored in natural row order: inv[j * m + nat(k)] = (A^-1)_{k j}. All m columns are eliminated together by the
+// stored in natural row order: inv[j * m + nat(k)] = (A^-1)_{k j} (k_coarse_perm then moves it to the V-cycle's
+// level-space layout). All m columns are eliminated together by the
 // block, column-oriented, in an m x m shared-memory work matrix (m <= kInvSmemRows), else one column per thread in
 // global memory.
 constexpr int kInvSmemRows = 224;
@@ -266,8 +267,8 @@ __global__ void __launch_bounds__(256) k_coarse_inv(int maxL, const AmgSysLv* __
 }
 
 // FP32 forms: the coarsest inverse directly, by Gauss-Jordan elimination with partial pivoting on the dense matrix
-// in its natural numbering (m <= kInvSmemRows); the inverse is written as the V-cycle reads it,
-// inv[j * m + I] = (A^-1)[I][nat(j)]. Larger levels take the LU (k_coarse_lu<float>) and k_coarse_inv instead.
+// in its natural numbering (m <= kInvSmemRows); the inverse is written as inv[j * m + I] = (A^-1)[I][nat(j)], which
+// k_coarse_perm turns into the V-cycle's layout. Larger levels take the LU (k_coarse_lu<float>) and k_coarse_inv.
 // The work matrix lives in registers: 16 warps, row i in warp i % 16, column j in lane j % 32, so a thread holds
 // a 14 x 7 tile and a step's rank-1 update is register arithmetic. Per step, the pivot column (staged in shared
 // memory by its owning lane during the previous update) is searched by every warp on its own; the pivot row and
@@ -504,6 +505,32 @@ void launch_amg_refresh(const DevAmg& G, cudaStream_t st) {
         k_diag_fix<<<grid_for(size_t(r1 - r0)), 256, 0, st>>>(r0, r1, G.diagGlob, G.val);
     }
 }
+// FP32 forms: the explicit inverses from the natural-row layout inv[j * m + I] = (A^-1)[I][nat(j)] to the layout the
+// V-cycle reads, inv[j * m + k] = (A^-1)[nat(k)][nat(j)] (k, j level-space): the threads of consecutive rows k then
+// read consecutive words of a column. One column at a time through shared memory, in place.
+__global__ void __launch_bounds__(256) k_coarse_perm(int maxL, const AmgSysLv* __restrict__ lv, const int* __restrict__ luPerm,
+                                                     float* invAll) {
+    extern __shared__ float colbuf[];
+    const int s = blockIdx.x;
+    AmgSysLv L;
+    bool found = false;
+    for (int l = 0; l < maxL; ++l) {
+        const AmgSysLv c = lv[s * maxL + l];
+        if (c.n > 0 && c.coarse) { L = c; found = true; break; }
+    }
+    if (!found || !L.dense) return;
+    const int m = L.n;
+    const int* nat = luPerm + L.luRowOff;
+    float* inv = invAll + L.luOff;
+    for (int j = 0; j < m; ++j) {
+        float* col = inv + size_t(j) * m;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) colbuf[i] = col[i];
+        __syncthreads();
+        for (int k = threadIdx.x; k < m; k += blockDim.x) col[k] = colbuf[__ldg(nat + k)];
+        __syncthreads();
+    }
+}
+
 // FP32 forms: how well the explicit FP32 inverse solves the coarsest level. x_t deterministic in [-1, 1), b = A x_t
 // in FP64, x = inv float(b) as the V-cycle applies it; a system whose relative error exceeds kCoarseTol (or is not
 // finite) solves its coarsest level in FP64 with the LU instead: extreme permeability contrasts (sigma ln k ~ 3)
@@ -539,8 +566,9 @@ __global__ void __launch_bounds__(256) k_coarse_check(int maxL, const AmgSysLv* 
     const int* nat = luPerm + L.luRowOff;
     double e2 = 0, r2 = 0;
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        const float* col = inv + __ldg(nat + k);
+        const float* col = inv + k;                              // the V-cycle's layout (k_coarse_perm)
         float acc = 0.f;
+#pragma unroll 16
         for (int j = 0; j < m; ++j) acc = fmaf(col[size_t(j) * m], float(b[j]), acc);
         const double d = double(acc) - x[k];
         e2 += d * d;
@@ -572,6 +600,7 @@ void launch_amg_coarse_lu(const DevAmg& G, bool fp32, cudaStream_t st) {
                                                        kInvSmemRows, nullptr);
             k_coarse_inv<<<G.nsys, 256, smem, st>>>(G.maxL, G.lv, G.cin, G.luf, G.invf, kInvSmemRows);
         }
+        k_coarse_perm<<<G.nsys, 256, size_t(std::max(G.maxCoarse, 1)) * sizeof(float), st>>>(G.maxL, G.lv, G.luPerm, G.invf);
         // the FP32 inverse checked per system; the FP64 LU (after the FP32 one: pivots and gather order are its own)
         // only for the systems that need it
         k_coarse_check<<<G.nsys, 256, 0, st>>>(G.maxL, G.lv, G.rp, G.ci, G.val, G.luPerm, G.invf, G.x, G.b, G.coarse64);

@@ -220,7 +220,7 @@ int launch_devcpr(const DevPlan& P, const DevAmg& G, const double* val, int mode
                   const KScal* ks, cudaStream_t st);
 int devcpr_launches(const DevAmg& G);
 inline int cpr_grid_launches(const DevAmg& G, bool split = false) {
-    int n = (split ? 4 : 6) + 2 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
+    int n = (split ? 4 : 6) + 3 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
     for (int l = 0; l + 1 < G.maxL; ++l) {          // pre- and post-smoothing: one sweep, or a launch per large colour + the tail
         const int nc = l < int(G.colBeg.size()) ? int(G.colBeg[size_t(l)].size()) - 1 : 0;
         n += 2 * (nc > 0 ? G.colTail[size_t(l)] + (G.colTail[size_t(l)] < nc ? 1 : 0) : 1);

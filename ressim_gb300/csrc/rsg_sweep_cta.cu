@@ -232,7 +232,7 @@ __device__ __forceinline__ void bwd_step(const BwdRow<TF>& R, const IluArgs<TF>&
 template <class TF, class TI, int MODE>
 __device__ __forceinline__ void prefetch_fwd_level(const IluArgs<TF>& F, const int* lv, int L, const TI* r, const double* pv,
                                                    const double* v) {
-    const size_t s = size_t(__ldg(lv + L)), e = size_t(__ldg(lv + L + 1));
+    const size_t s = size_t(lv[L]), e = size_t(lv[L + 1]);
     l2_prefetch(F.L, s * LREC * sizeof(TF), e * LREC * sizeof(TF));
     l2_prefetch(F.Lslot, s * sizeof(int4), e * sizeof(int4));
     l2_prefetch(r, s * 3 * sizeof(TI), e * 3 * sizeof(TI));
@@ -241,7 +241,7 @@ __device__ __forceinline__ void prefetch_fwd_level(const IluArgs<TF>& F, const i
 }
 template <class TF>
 __device__ __forceinline__ void prefetch_bwd_level(const IluArgs<TF>& F, const int* lv, int L) {
-    const size_t s = size_t(__ldg(lv + L)), e = size_t(__ldg(lv + L + 1));
+    const size_t s = size_t(lv[L]), e = size_t(lv[L + 1]);
     l2_prefetch(F.UD, s * UREC * sizeof(TF), e * UREC * sizeof(TF));
     l2_prefetch(F.Uslot, s * sizeof(int4), e * sizeof(int4));
 }
@@ -260,10 +260,10 @@ template <class TF, class TV, class TI, int MODE, int NSET>
 __device__ __forceinline__ void fwd_level(const IluArgs<TF>& F, const int* lv, int L, int nl, FwdRow<TF, TI, MODE>* cur,
                                           FwdRow<TF, TI, MODE>* nxt, int row0, const TI* r, double* pv, const double* v, TV* y,
                                           double beta, double omega, double alpha) {
-    const int s = __ldg(lv + L), e = __ldg(lv + L + 1);
+    const int s = lv[L], e = lv[L + 1];
     if (threadIdx.x == 0 && L + kAhead < nl) prefetch_fwd_level<TF, TI, MODE>(F, lv, L + kAhead, r, pv, v);
     if (L + 1 < nl) {
-        const int e1 = __ldg(lv + L + 2);
+        const int e1 = lv[L + 2];
 #pragma unroll
         for (int j = 0; j < NSET; ++j) load_fwd(nxt[j], row_of<NSET>(e, e1, j), F, r, pv, v);
     }
@@ -285,10 +285,10 @@ __device__ __forceinline__ void fwd_level(const IluArgs<TF>& F, const int* lv, i
 template <class TF, class TV, bool XP, int NSET, class TX>
 __device__ __forceinline__ void bwd_level(const IluArgs<TF>& F, const int* lv, int L, BwdRow<TF>* cur, BwdRow<TF>* nxt, int row0,
                                           const TX* xp, TV* y, double* z, bool writeZ) {
-    const int s = __ldg(lv + L), e = __ldg(lv + L + 1);
+    const int s = lv[L], e = lv[L + 1];
     if (threadIdx.x == 0 && L - kAhead >= 0) prefetch_bwd_level(F, lv, L - kAhead);
     if (L > 0) {
-        const int s1 = __ldg(lv + L - 1);
+        const int s1 = lv[L - 1];
 #pragma unroll
         for (int j = 0; j < NSET; ++j) load_bwd(nxt[j], row_of<NSET>(s1, s, j), F, xp, row0);
     }
@@ -307,19 +307,30 @@ __device__ __forceinline__ void bwd_level(const IluArgs<TF>& F, const int* lv, i
     __syncthreads();
 }
 
+// The level starts of a system are read at every level step by every thread. The streaming factor records keep the
+// small L1 of these kernels (most of the SM's memory is shared memory) from holding them, so each step would
+// begin with an L2 round trip: a block copies them to shared memory when they fit.
+constexpr int kLvCache = 512;
+constexpr size_t kCtaStaticSmem = 4096;    // static shared memory of the sweep kernels (level starts), off the dynamic cap
+__device__ __forceinline__ const int* level_starts(const int* g, int nl, int* cache) {
+    if (nl + 1 > kLvCache) return g;
+    for (int i = int(threadIdx.x); i <= nl; i += int(blockDim.x)) cache[i] = __ldg(g + i);
+    __syncthreads();
+    return cache;
+}
+
 // Both sweeps of one system by the calling thread block (y: the sweep vector of this system, on chip or in z;
 // xp: with XP, the CPR pressure correction added to z_p as z is written)
 template <class TF, class TV, class TI, int MODE, bool XP, class TX, int NT>
-__device__ void ilu_body(const IluArgs<TF>& F, int row0, int l0, int nl, const TI* r, double* pv, const double* v, double* z, TV* y,
+__device__ void ilu_body(const IluArgs<TF>& F, int row0, const int* lv, int nl, const TI* r, double* pv, const double* v, double* z, TV* y,
                          bool writeZ, double beta, double omega, double alpha, const TX* xp) {
     constexpr int NSET = (NT < 512 && sizeof(TF) == 4 && MODE == IN_PLAIN) ? 2 : 1;
-    const int* lv = F.lvlStart + l0;
     if (threadIdx.x == 0)
         for (int L = 0; L < kAhead && L < nl; ++L) prefetch_fwd_level<TF, TI, MODE>(F, lv, L, r, pv, v);
     {
         FwdRow<TF, TI, MODE> A[NSET], B[NSET];
         if (nl > 0) {
-            const int s = __ldg(lv), e = __ldg(lv + 1);
+            const int s = lv[0], e = lv[1];
 #pragma unroll
             for (int j = 0; j < NSET; ++j) load_fwd(A[j], row_of<NSET>(s, e, j), F, r, pv, v);
         }
@@ -334,13 +345,80 @@ __device__ void ilu_body(const IluArgs<TF>& F, int row0, int l0, int nl, const T
         const TX* xq = XP ? xp : nullptr;
         BwdRow<TF> A[NSET], B[NSET];
         if (nl > 0) {
-            const int s = __ldg(lv + nl - 1), e = __ldg(lv + nl);
+            const int s = lv[nl - 1], e = lv[nl];
 #pragma unroll
             for (int j = 0; j < NSET; ++j) load_bwd(A[j], row_of<NSET>(s, e, j), F, xq, row0);
         }
         for (int L = nl - 1; L >= 0; L -= 2) {
             bwd_level<TF, TV, XP, NSET>(F, lv, L, A, B, row0, xq, y, z, writeZ);
             if (L - 1 >= 0) bwd_level<TF, TV, XP, NSET>(F, lv, L - 1, B, A, row0, xq, y, z, writeZ);
+        }
+    }
+}
+
+// The same sweeps with three register buffers and one row per thread per buffer: a level's rows are loaded two
+// levels ahead (at the start of level L, the rows of level L + 2), so a load has two level steps to arrive. Rows past
+// blockDim in a level load when they are reached. For FP32 factor records (three FP64 records do not fit the
+// registers of a 256-thread block).
+template <class TF, class TV, class TI, bool XP, class TX>
+__device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl, const TI* r, double* z, TV* y, bool writeZ, const TX* xp) {
+    const int nt = int(blockDim.x);
+    if (threadIdx.x == 0)
+        for (int L = 0; L < kAhead && L < nl; ++L) prefetch_fwd_level<TF, TI, IN_PLAIN>(F, lv, L, r, nullptr, nullptr);
+    {
+        FwdRow<TF, TI, IN_PLAIN> R[3];
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+            if (b < nl) load_fwd(R[b], row_of<1>(lv[b], lv[b + 1], 0), F, r, nullptr, nullptr);
+        for (int L0 = 0; L0 < nl; L0 += 3) {
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {                    // level L0 + b works on R[b], loads level + 2 into R[(b + 2) % 3]
+                const int L = L0 + b;
+                if (L >= nl) break;
+                const int s = lv[L], e = lv[L + 1];
+                if (threadIdx.x == 0 && L + kAhead < nl) prefetch_fwd_level<TF, TI, IN_PLAIN>(F, lv, L + kAhead, r, nullptr, nullptr);
+                if (L + 2 < nl) load_fwd(R[(b + 2) % 3], row_of<1>(lv[L + 2], lv[L + 3], 0), F, r, nullptr, nullptr);
+                const int k = row_of<1>(s, e, 0);
+                if (k >= 0) {
+                    if (R[b].k != k) load_fwd(R[b], k, F, r, nullptr, nullptr);
+                    fwd_step<TF, TV, TI, IN_PLAIN>(R[b], F, row0, y, nullptr, 0, 0, 0);
+                }
+                for (int k2 = s + int(threadIdx.x) + nt; k2 < e; k2 += nt) {
+                    load_fwd(R[b], k2, F, r, nullptr, nullptr);
+                    fwd_step<TF, TV, TI, IN_PLAIN>(R[b], F, row0, y, nullptr, 0, 0, 0);
+                }
+                __syncthreads();
+            }
+        }
+    }
+    if (threadIdx.x == 0)
+        for (int L = nl - 1; L >= 0 && L >= nl - kAhead; --L) prefetch_bwd_level(F, lv, L);
+    {
+        const TX* xq = XP ? xp : nullptr;
+        BwdRow<TF> R[3];
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+            if (b < nl) load_bwd(R[b], row_of<1>(lv[nl - 1 - b], lv[nl - b], 0), F, xq, row0);
+        for (int g0 = 0; g0 < nl; g0 += 3) {
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const int g = g0 + b;
+                if (g >= nl) break;
+                const int L = nl - 1 - g;
+                const int s = lv[L], e = lv[L + 1];
+                if (threadIdx.x == 0 && L - kAhead >= 0) prefetch_bwd_level(F, lv, L - kAhead);
+                if (L - 2 >= 0) load_bwd(R[(b + 2) % 3], row_of<1>(lv[L - 2], lv[L - 1], 0), F, xq, row0);
+                const int k = row_of<1>(s, e, 0);
+                if (k >= 0) {
+                    if (R[b].k != k) load_bwd(R[b], k, F, xq, row0);
+                    bwd_step<TF, TV, XP>(R[b], F, row0, y, z, writeZ);
+                }
+                for (int k2 = s + int(threadIdx.x) + nt; k2 < e; k2 += nt) {
+                    load_bwd(R[b], k2, F, xq, row0);
+                    bwd_step<TF, TV, XP>(R[b], F, row0, y, z, writeZ);
+                }
+                __syncthreads();
+            }
         }
     }
 }
@@ -361,7 +439,9 @@ __global__ void __launch_bounds__(NT) k_ilu_cta(IluArgs<TF> F, const double* r, 
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
     TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
     const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
-    ilu_body<TF, TV, double, MODE, false, double, NT>(F, row0, l0, nl, r, pv, v, z, y, onchip || sizeof(TV) != sizeof(double), beta, omega,
+    __shared__ int lvc[kLvCache];
+    const int* lv = level_starts(F.lvlStart + l0, nl, lvc);
+    ilu_body<TF, TV, double, MODE, false, double, NT>(F, row0, lv, nl, r, pv, v, z, y, onchip || sizeof(TV) != sizeof(double), beta, omega,
                                                   alpha, nullptr);
 }
 
@@ -694,16 +774,15 @@ template <class TA, int W, int NT>
 __device__ __forceinline__ void residual(const AmgSysLv& A, const CprArgs<TA>& C, const TA* x, const TA* b, TA* r) {
     residual_call<TA, W>(A, C, x, b, r);
 }
-// FP32 forms: x = A^-1 b with the explicit inverse; thread k accumulates row k (natural index nat(k)) over the
-// columns, whose entries for consecutive k sit close together
+// FP32 forms: x = A^-1 b with the explicit inverse in the level-space layout inv[j * m + k] = (A^-1)[nat(k)][nat(j)];
+// thread k accumulates row k over the columns (consecutive k: consecutive words), many loads in flight
 __device__ __noinline__ void coarse_inverse(const AmgSysLv& A, const CprArgs<float>& C, float* x, const float* b) {
     const int m = A.n;
     const float* inv = C.inv + A.luOff;
-    const int* nat = C.luPerm + A.luRowOff;
     for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        const float* col = inv + __ldg(nat + k);
+        const float* col = inv + k;
         float acc = 0.f;
-#pragma unroll 8
+#pragma unroll 32
         for (int j = 0; j < m; ++j) acc = fmaf(__ldg(col + size_t(j) * m), b[j], acc);
         x[k] = acc;
     }
@@ -970,11 +1049,13 @@ __global__ void __launch_bounds__(NT) k_cpr_cta(IluArgs<TF> F, CprArgs<TA> C, co
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
     TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
     const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
+    __shared__ int lvc[kLvCache];
+    const int* lv = level_starts(F.lvlStart + l0, nl, lvc);
     const bool writeZ = onchip || sizeof(TV) != sizeof(double);
     if (writeZ) {   // y is not z: z_p += xp (bsr.cpp:1083) as z is written
-        ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
+        ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, lv, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
     } else {        // y is z itself: the correction after the sweeps
-        ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
+        ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, lv, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
         for (int k = row0 + tid; k < row0 + ns; k += nt) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xpg[k - row0]));
     }
 }
@@ -1021,11 +1102,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_factor_cta_f32(const int* __res
     for (size_t e = e0 + size_t(tid); e < e1; e += size_t(nt)) F[e] = float(__ldg(val + e));
     __syncthreads();
     const int l0 = __ldg(sysLvl0 + s), nl = __ldg(sysLvl0 + s + 1) - l0 - 1;
+    __shared__ int lvc[kLvCache];
+    const int* lv = level_starts(lvlStart + l0, nl, lvc);
     int reg = 0;
     float Lb[9];
     for (int L = 0; L < nl; ++L) {
-        const int k1 = __ldg(lvlStart + l0 + L + 1);
-        for (int i = __ldg(lvlStart + l0 + L) + tid; i < k1; i += nt) {
+        const int k1 = lv[L + 1];
+        for (int i = lv[L] + tid; i < k1; i += nt) {
             const int p0 = __ldg(rowPtr + i), d = __ldg(diag + i);
             // the indices of entry p (column k, elimination list [q0, q1)) are loaded one entry ahead, so an entry
             // costs two dependent loads (diag[k] with its first elimination targets, then every block it touches)
@@ -1145,7 +1228,7 @@ void dispatch(const DevPlan& P, const PrecDev& M, const double* r, double* pv, c
 size_t cta_sweep_smem(const DevPlan& P, bool vec32) {
     // the largest system's vector if it fits, else all the opt-in shared memory (systems that fit use it)
     const size_t need = size_t(P.maxSysRows) * 3 * (vec32 ? sizeof(float) : sizeof(double));
-    const size_t cap = size_t(max_smem_optin());
+    const size_t cap = size_t(max_smem_optin()) - kCtaStaticSmem;
     return need <= cap ? need : cap;
 }
 
@@ -1197,7 +1280,7 @@ template <class TF, class TV, class TA, int MODE>
 void launch_cpr_t(const DevPlan& P, const SplitFactors<TF>& S, size_t smem, const CprArgs<TA>& C, const DevAmg& G, const double* r,
                   double* pv, const double* v, double* z, TV* yglob, const KScal* ks, cudaStream_t st) {
     // shared memory: the larger of the sweep vector and the V-cycle vectors of the largest system, within the cap
-    const size_t cap = size_t(max_smem_optin());
+    const size_t cap = size_t(max_smem_optin()) - kCtaStaticSmem;
     smem = std::max(smem, std::min(cap, size_t(G.maxSysAmgRows) * 3 * sizeof(TA)));
     raise_smem_limit(reinterpret_cast<const void*>(k_cpr_cta<TF, TV, TA, MODE>), int(smem));
     k_cpr_cta<TF, TV, TA, MODE><<<P.nsys, cta_threads<TF, TV>(), smem, st>>>(ilu_args(P, S), C, r, pv, v, z, yglob, smem, ks);
@@ -1357,11 +1440,28 @@ __device__ __forceinline__ void gs_colour_row(const int4 d, const int* __restric
                                               const int* __restrict__ wave, const TA* b, TA* x) {
     const int wi = ZERO ? __ldg(wave + d.x) : 0;
     TA s = b[d.x];
-    for (int p = d.y; p < d.z; ++p) {
-        if (p == d.w) continue;
-        const int j = __ldg(gci + p);
-        if (ZERO && __ldg(wave + j) > wi) continue;
-        s = asub(s, amul(__ldg(val + p), x[j]));
+    // entries in chunks whose loads are all issued before the terms are taken (in entry order): a row costs two
+    // dependent loads per chunk, not per entry
+    constexpr int CH = 8;
+    for (int p0 = d.y; p0 < d.z; p0 += CH) {
+        int j[CH];
+        TA a[CH], xv[CH];
+        bool use[CH];
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+            const int p = p0 + u;
+            use[u] = p < d.z && p != d.w;
+            j[u] = use[u] ? __ldg(gci + p) : 0;
+            a[u] = use[u] ? __ldg(val + p) : TA(0);
+        }
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+            if (ZERO && use[u] && __ldg(wave + j[u]) > wi) use[u] = false;   // x_j still zero: the term is not taken
+            xv[u] = use[u] ? x[j[u]] : TA(0);
+        }
+#pragma unroll
+        for (int u = 0; u < CH; ++u)
+            if (use[u]) s = asub(s, amul(a[u], xv[u]));
     }
     x[d.x] = adiv(s, __ldg(val + d.w));
 }
@@ -1456,36 +1556,67 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_tail(int i0, int i1, int ta
     }
 }
 
-// b_{l+1} = R (b_l - A_l x_l) for the coarse rows [c0, c1) of level l + 1: the residual of each member from zero in
-// entry order, the members in restriction order (engine/src/amg.cpp:321-324)
+// r = b - A x on the rows [q0, q1) of one level of every system (engine/src/amg.cpp:321-322: the row sum from
+// zero in entry order, the diagonal at its place); rows of a system's coarsest level are skipped
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_resid(int q0, int q1, int maxL, const int* __restrict__ rowLv,
+                                                    const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                    const int* __restrict__ ci, const TA* __restrict__ val, const TA* b, const TA* x, TA* r,
+                                                    const KScal* ks) {
+    for (int g = q0 + int(blockIdx.x * blockDim.x + threadIdx.x); g < q1; g += int(gridDim.x * blockDim.x)) {
+        const int sl = __ldg(rowLv + g);
+        if (ks && ks[sl / maxL].status != ST_RUNNING) continue;
+        const AmgSysLv* F = lv + sl;
+        if (__ldg(&F->coarse)) continue;
+        const int fOff = __ldg(&F->rowOff), k = g - fOff;
+        const int* frp = rp + __ldg(&F->rpOff);
+        const int* fci = ci + __ldg(&F->entOff);
+        const TA* fv = val + __ldg(&F->entOff);
+        const int p0 = __ldg(frp + k), p1 = __ldg(frp + k + 1);
+        TA acc = TA(0);
+        constexpr int CH = 8;                     // loads of a chunk issued before its terms are summed in order
+        for (int q = p0; q < p1; q += CH) {
+            int c[CH];
+            TA a[CH], xv[CH];
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                c[u] = q + u < p1 ? __ldg(fci + q + u) : 0;
+                a[u] = q + u < p1 ? __ldg(fv + q + u) : TA(0);
+            }
+#pragma unroll
+            for (int u = 0; u < CH; ++u) xv[u] = q + u < p1 ? x[fOff + c[u]] : TA(0);
+#pragma unroll
+            for (int u = 0; u < CH; ++u)
+                if (q + u < p1) acc = aadd(acc, amul(a[u], xv[u]));
+        }
+        r[g] = asub(b[g], acc);
+    }
+}
+
+// restriction b_{l+1} = R r for the coarse rows [c0, c1) of every system: members in ascending natural order
+// (engine/src/amg.cpp:324)
 template <class TA>
 __global__ void __launch_bounds__(256) k_gcpr_restrict(int c0, int c1, int maxL, const int* __restrict__ rowLv,
-                                                       const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
-                                                       const int* __restrict__ ci, const TA* __restrict__ val,
-                                                       const int* __restrict__ memPtr, const int* __restrict__ mem, TA* b, const TA* x,
-                                                       const KScal* ks) {
+                                                       const AmgSysLv* __restrict__ lv, const int* __restrict__ memPtr,
+                                                       const int* __restrict__ mem, TA* b, const TA* r, const KScal* ks) {
     for (int c = c0 + int(blockIdx.x * blockDim.x + threadIdx.x); c < c1; c += int(gridDim.x * blockDim.x)) {
         const int sl = __ldg(rowLv + c);
         if (ks && ks[sl / maxL].status != ST_RUNNING) continue;
         const AmgSysLv* Cl = lv + sl;
-        const AmgSysLv* F = lv + sl - 1;
         const int I = c - __ldg(&Cl->rowOff);
         const int* mp = memPtr + __ldg(&Cl->rpOff);
         const int* mm = mem + __ldg(&Cl->memOff);
-        const int fOff = __ldg(&F->rowOff);
-        const int* frp = rp + __ldg(&F->rpOff);
-        const int* fci = ci + __ldg(&F->entOff);
-        const TA* fv = val + __ldg(&F->entOff);
+        const TA* rf = r + __ldg(&lv[sl - 1].rowOff);
+        const int q0 = __ldg(mp + I), q1 = __ldg(mp + I + 1);
         TA t = TA(0);
-        const int q1 = __ldg(mp + I + 1);
-#pragma unroll 2
-        for (int q = __ldg(mp + I); q < q1; ++q) {
-            const int m = __ldg(mm + q);
-            const int pe = __ldg(frp + m + 1);
-            TA acc = TA(0);
-#pragma unroll 4
-            for (int p = __ldg(frp + m); p < pe; ++p) acc = aadd(acc, amul(__ldg(fv + p), x[fOff + __ldg(fci + p)]));
-            t = aadd(t, asub(b[fOff + m], acc));
+        constexpr int CH = 8;
+        for (int q = q0; q < q1; q += CH) {
+            TA v[CH];
+#pragma unroll
+            for (int u = 0; u < CH; ++u) v[u] = q + u < q1 ? rf[__ldg(mm + q + u)] : TA(0);
+#pragma unroll
+            for (int u = 0; u < CH; ++u)
+                if (q + u < q1) t = aadd(t, v[u]);
         }
         b[c] = t;
     }
@@ -1599,10 +1730,14 @@ __global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const 
     const bool onchip = size_t(ns) * 3 * sizeof(TV) <= smemBytes;
     TV* y = onchip ? reinterpret_cast<TV*>(smraw) : yglob + size_t(row0) * 3;
     const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
+    __shared__ int lvc[kLvCache];
+    const int* ls = level_starts(F.lvlStart + l0, nl, lvc);
     if (onchip || sizeof(TV) != sizeof(double)) {
-        ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
+        if constexpr (sizeof(TF) == 4) ilu_body3<TF, TV, TV, true, TA>(F, row0, ls, nl, T, z, y, true, xpg);
+        else ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, ls, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
     } else {
-        ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, l0, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
+        if constexpr (sizeof(TF) == 4) ilu_body3<TF, TV, TV, false, TA>(F, row0, ls, nl, T, z, y, false, (const TA*)nullptr);
+        else ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, ls, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
         for (int k = row0 + tid; k < row0 + ns; k += nt) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xpg[k - row0]));
     }
 }
@@ -1688,10 +1823,10 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
     };
     for (int l = 0; l + 1 < G.maxL; ++l) {                 // pre-smoothing and restriction, finest to coarsest
         sweep(l, 0, true, true);
-        const int c0 = LB[size_t(l) + 1], c1 = LB[size_t(l) + 2];
-        k_gcpr_restrict<TA><<<grid_for(c1 - c0, 256), 256, 0, st>>>(c0, c1, G.maxL, G.rowLv, G.lv, G.rp, G.ci, val, G.memPtr, G.mem, C.b,
-                                                                    C.x, ks);
-        ++launches;
+        const int f0 = LB[size_t(l)], f1 = LB[size_t(l) + 1], c0 = LB[size_t(l) + 1], c1 = LB[size_t(l) + 2];
+        k_gcpr_resid<TA><<<grid_for(f1 - f0, 256), 256, 0, st>>>(f0, f1, G.maxL, G.rowLv, G.lv, G.rp, G.ci, val, C.b, C.x, C.r, ks);
+        k_gcpr_restrict<TA><<<grid_for(c1 - c0, 256), 256, 0, st>>>(c0, c1, G.maxL, G.rowLv, G.lv, G.memPtr, G.mem, C.b, C.r, ks);
+        launches += 2;
     }
     k_gcpr_coarse<TA><<<G.nsys, 256, 0, st>>>(C, ks);
     ++launches;
