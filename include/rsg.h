@@ -66,8 +66,8 @@ typedef struct rsg_options {
     int sweep;              /* BILU0 sweep scheduling: 0 auto, 1 one thread block per system (level barriers,
                                shared-memory vector), 2 grid-wide sync-free (per-row flags), 3 split CPR: the
                                V-cycle's passes grid-wide over all systems, the BILU0 sweeps one thread block per
-                               system (same results as 1). Auto takes 3 for CPR and 1 for BILU0 where the thread-block
-                               sweeps apply, else 2 */
+                               system (same results as 1). Auto takes 3 for CPR on a batch, 1 for a single system and
+                               for BILU0 where the thread-block sweeps apply, else 2 */
     int fma;                /* 1 (default): the SpMV accumulates with fused multiply-adds (half the FP64
                                instructions; results within rounding of the reference); 0: the reference's separately
                                rounded products and sums, bit for bit (engine/src/bsr.cpp:109-117) */
@@ -135,6 +135,11 @@ int rsg_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, 
 int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relres);
 /* Per system of the last solve: RSG_OK (converged), RSG_ENOTCONV or RSG_EBREAKDOWN. */
 int rsg_batch_status(rsg_solver* h, int* status);
+/* CPR: sizes of the pressure hierarchy after rsg_setup, summed over the systems of the batch. For level l < returned
+   count (at most maxlev): rows[l] and nnz[l] of the level matrices A_l (rows of a system's coarsest level
+   included); *dense = entries of the coarsest levels kept dense (sum of m^2). Returns the number of levels, or -1
+   (no CPR hierarchy). Lets a caller size the algorithmic bytes of an application. */
+int rsg_amg_level_sizes(rsg_solver* h, int maxlev, long long* rows, long long* nnz, long long* dense);
 
 /* y = A x with host / device vectors. Replaces BSR::spmv (engine/src/bsr.cpp:109-126). */
 int rsg_spmv(rsg_solver* h, const double* x, double* y);

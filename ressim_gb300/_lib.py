@@ -21,7 +21,7 @@ SWEEP = {"auto": 0, "cta": 1, "grid": 2, "split": 3}
 # every symbol include/rsg.h declares
 EXPORTS = [
     "rsg_default_options", "rsg_last_error", "rsg_version", "rsg_create", "rsg_destroy", "rsg_set_matrix", "rsg_set_batch",
-    "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_batch_status", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
+    "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_batch_results", "rsg_batch_status", "rsg_amg_level_sizes", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
     "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
     "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes",
@@ -79,6 +79,7 @@ def load(build_if_missing: bool = True):
     L.rsg_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
     L.rsg_batch_results.argtypes = [vp, vp, vp, vp]
     L.rsg_batch_status.argtypes = [vp, vp]
+    L.rsg_amg_level_sizes.argtypes = [vp, C.c_int, vp, vp, vp]
     L.rsg_spmv.argtypes = [vp, vp, vp]
     L.rsg_spmv_device.argtypes = [vp, vp, vp]
     L.rsg_precond_apply.argtypes = [vp, vp, vp]

@@ -199,10 +199,10 @@ int alloc_plan(rsg_solver* h) {
     h->cta = h->opt.sweep != 2 && cta_sweep_supported(D, P);
     if ((h->opt.sweep == 1 || h->opt.sweep == 3) && !h->cta)
         return fail(RSG_EINVAL, "thread-block sweeps need a structurally symmetric pattern of <= 32768 block rows per system");
-    // CPR on the thread-block path: the V-cycle's parallel passes grid-wide (all systems at once, the whole GPU's
-    // loads in flight) unless the one-kernel form is asked for. The choice does not depend on the batch, so a
-    // system's result does not either.
-    h->splitCpr = h->cta && (h->opt.sweep == 3 || h->opt.sweep == 0);
+    // CPR on the thread-block path: for a batch, the V-cycle's passes grid-wide (all systems at once, the whole
+    // GPU's loads in flight); a single system keeps the one-kernel form (one launch per application instead of a
+    // launch per pass). Both give the same results bit for bit, so a system's result does not depend on its batch.
+    h->splitCpr = h->cta && (h->opt.sweep == 3 || (h->opt.sweep == 0 && P.nsys > 1));
     const size_t N = size_t(P.n) * NB, E = size_t(P.nnzb) * NB2;
     if ((rc = dalloc(M, &h->val, E)) || (rc = dalloc(M, &h->val0, E)) || (rc = dalloc(M, &h->b, N)) || (rc = dalloc(M, &h->xout, N)) ||
         (rc = dalloc(M, &h->tmp, N)))
@@ -1156,6 +1156,23 @@ int rsg_batch_status(rsg_solver* h, int* status) {
         status[s] = st == ST_CONV ? RSG_OK : (st == ST_BREAKDOWN ? RSG_EBREAKDOWN : RSG_ENOTCONV);
     }
     return RSG_OK;
+}
+
+int rsg_amg_level_sizes(rsg_solver* h, int maxlev, long long* rows, long long* nnz, long long* dense) {
+    if (!h || maxlev < 0 || (maxlev > 0 && (!rows || !nnz))) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->haveAmg) {
+        fail(RSG_ESTATE, "no CPR hierarchy (setup not run, or not a CPR preconditioner)");
+        return -1;
+    }
+    const DevAmg& G = h->amg;
+    const int nl = std::min(maxlev, G.maxL);
+    for (int l = 0; l < nl; ++l) {
+        rows[l] = G.levelRowBeg[size_t(l) + 1] - G.levelRowBeg[size_t(l)];
+        nnz[l] = G.levelEntBeg[size_t(l) + 1] - G.levelEntBeg[size_t(l)];
+    }
+    if (dense) *dense = G.totLu;
+    return G.maxL;
 }
 
 int rsg_spmv_device(rsg_solver* h, const double* d_x, double* d_y) {

@@ -154,6 +154,18 @@ class DeviceSolver:
         _lib.check(self.L.rsg_get_stats(self.h, C.byref(st)))
         return st
 
+    def amg_level_sizes(self, maxlev: int = 16):
+        """CPR hierarchy after setup(), summed over the batch: (rows per level, entries per level, dense coarse
+        entries), or None without a CPR hierarchy."""
+        rows = np.zeros(maxlev, dtype=np.int64)
+        nnz = np.zeros(maxlev, dtype=np.int64)
+        dense = C.c_longlong(0)
+        nl = self.L.rsg_amg_level_sizes(self.h, maxlev, _lib.ptr(rows), _lib.ptr(nnz), C.byref(dense))
+        if nl < 0:
+            return None
+        nl = min(nl, maxlev)
+        return rows[:nl], nnz[:nl], int(dense.value)
+
     @property
     def stream(self) -> int:
         return int(self.L.rsg_stream(self.h) or 0)

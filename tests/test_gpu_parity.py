@@ -236,6 +236,28 @@ def test_cpr_apply_matches_reference(name, sweep):
             assert rel(d.precond_apply(z["b"]), z["z_cpr_acc"]) < 1e-10
 
 
+@pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
+def test_amg_level_sizes_match_reference(name):
+    """rsg_amg_level_sizes reports the reference hierarchy's level sizes (rows, entries); for a batch, their sums."""
+    A, z = load_golden(name)
+    with dev(precond="cpr") as d:
+        d.set_matrix(A)
+        d.setup()
+        rows, nnz, dense = d.amg_level_sizes()
+    assert list(rows) == list(z["amg_rows"]) and list(nnz) == list(z["amg_nnz"])
+    assert dense in (0, int(z["amg_rows"][-1]) ** 2)
+    with dev(precond="cpr") as d:
+        d.set_batch([A, A])
+        d.setup()
+        rows2, nnz2, dense2 = d.amg_level_sizes()
+    assert list(rows2) == [2 * int(r) for r in z["amg_rows"]] and list(nnz2) == [2 * int(q) for q in z["amg_nnz"]]
+    assert dense2 == 2 * dense
+    with dev(precond="bilu0") as d:
+        d.set_matrix(A)
+        d.setup()
+        assert d.amg_level_sizes() is None
+
+
 @pytest.mark.parametrize("sweep", ["cta", "split", "grid"])
 @pytest.mark.parametrize("precision", ["mixed", "mixed_f32"])
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
