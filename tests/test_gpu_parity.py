@@ -2,8 +2,8 @@
 
 Tolerances: integer / structural results and the FP64 kernels that follow the reference's serial arithmetic
 (SpMV, BILU0 factors, BILU0 sweeps) are compared bit for bit; Krylov solutions, whose inner products are
-reduced in a different (tree) order, must match the reference solution within 1e-8 relative (the north-star
-bar) at the same iteration count; FP32 preconditioner outputs within 1e-5 relative of the oracle's float
+reduced in a different (tree) order, must match the reference solution within 1e-8 relative (the plain FP64
+path's accuracy bar) at the same iteration count; FP32 preconditioner outputs within 1e-5 relative of the oracle's float
 restatement; every solve's true residual ||b - A x|| / ||b|| is recomputed in FP64 on the host.
 """
 import numpy as np
