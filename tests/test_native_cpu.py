@@ -42,6 +42,16 @@ def test_create_without_gpu_fails_cleanly():
     rc = L.rsg_create(C.byref(h), None)
     assert rc == _lib.RSG_ECUDA
     assert "CUDA" in _lib.last_error() or "device" in _lib.last_error()
+    # options are checked before the device: every sweep form (0-3) passes to the device check, 4 does not
+    o = _lib.Options()
+    L.rsg_default_options(C.byref(o))
+    for sweep, want in ((0, _lib.RSG_ECUDA), (3, _lib.RSG_ECUDA), (4, _lib.RSG_EINVAL)):
+        o.sweep = sweep
+        assert L.rsg_create(C.byref(h), C.byref(o)) == want
+    # entry points without a handle fail cleanly
+    rows = np.zeros(4, dtype=np.int64)
+    assert L.rsg_amg_level_sizes(None, 4, _lib.ptr(rows), _lib.ptr(rows), None) == _lib.RSG_EINVAL
+    assert L.rsg_batch_status(None, None) == _lib.RSG_EINVAL
 
 
 def test_server_without_gpu_fails_cleanly_and_footprint_is_monotone():
