@@ -138,7 +138,8 @@ int rsg_batch_status(rsg_solver* h, int* status);
 /* CPR: sizes of the pressure hierarchy after rsg_setup, summed over the systems of the batch. For level l < returned
    count (at most maxlev): rows[l] and nnz[l] of the level matrices A_l (rows of a system's coarsest level
    included); *dense = entries of the coarsest levels kept dense (sum of m^2). Returns the number of levels, or -1
-   (no CPR hierarchy). Lets a caller size the algorithmic bytes of an application. */
+   (no CPR hierarchy). Replaces AMG::levels / coarsestSize / operatorComplexity (engine/include/ressim/
+   linsolve.h:54-56) for the device hierarchy, and lets a caller size the algorithmic bytes of an application. */
 int rsg_amg_level_sizes(rsg_solver* h, int maxlev, long long* rows, long long* nnz, long long* dense);
 
 /* y = A x with host / device vectors. Replaces BSR::spmv (engine/src/bsr.cpp:109-126). */
