@@ -87,33 +87,58 @@ struct Galerkin {
     std::vector<int> apPtr, apSrc;   // AP entry -> A positions
     std::vector<int> acPtr, acSrc;   // A_c entry -> AP entries
 };
+// One output row of a sparse product in the reference's order. The row's contributions arrive in order as
+// (column J, value, source); take() sums the values of each J in arrival order, then emit() writes the columns in
+// ascending J with their sums and, per column, the sources in arrival order. The buffers live across rows (the
+// plan of a large system has millions of rows).
+struct RowAccumulator {
+    std::vector<int> mark;                      // J -> slot in this row, -1 outside
+    std::vector<std::pair<int, int>> cols;      // (J, slot) in first-appearance order
+    std::vector<double> vals;                   // per slot
+    std::vector<int> srcSlot, src;              // arrivals: slot and source
+    std::vector<int> rank, off;                 // per slot: position of its column, first output source
+    explicit RowAccumulator(int ncols) : mark(size_t(ncols), -1) {}
+    void take(int J, double v, int source) {
+        int& m = mark[size_t(J)];
+        if (m < 0) { m = int(cols.size()); cols.push_back({J, m}); vals.push_back(v); }
+        else vals[size_t(m)] += v;
+        srcSlot.push_back(m);
+        src.push_back(source);
+    }
+    // cols sorted by J; sources bucketed by slot, arrival order kept within a bucket
+    template <class Emit>
+    void emit(std::vector<int>& outSrc, Emit&& emitCol) {
+        for (auto& c : cols) mark[size_t(c.first)] = -1;
+        std::sort(cols.begin(), cols.end());
+        const size_t ns = cols.size();
+        rank.assign(ns, 0);
+        off.assign(ns + 1, 0);
+        for (size_t r = 0; r < ns; ++r) rank[size_t(cols[r].second)] = int(r);
+        for (int sl : srcSlot) off[size_t(rank[size_t(sl)]) + 1]++;
+        for (size_t r = 0; r < ns; ++r) off[r + 1] += off[r];
+        const size_t base = outSrc.size();
+        outSrc.resize(base + src.size());
+        std::vector<int>& pos = rank;           // reused: next free place per column
+        for (size_t r = 0; r < ns; ++r) pos[size_t(cols[r].second)] = off[r];
+        for (size_t q = 0; q < src.size(); ++q) outSrc[base + size_t(pos[size_t(srcSlot[q])]++)] = src[q];
+        for (size_t r = 0; r < ns; ++r) emitCol(cols[r].first, vals[size_t(cols[r].second)], int(base) + off[r + 1]);
+        cols.clear(); vals.clear(); srcSlot.clear(); src.clear();
+    }
+};
+
 void galerkin(const Csr& A, const std::vector<int>& agg, int na, Galerkin& G) {
     const int n = A.n;
     Csr& AP = G.AP;
     AP.n = n;
     AP.rp.assign(size_t(n) + 1, 0);
     AP.ci.clear(); AP.v.clear();
+    AP.ci.reserve(A.ci.size()); AP.v.reserve(A.ci.size());
     G.apPtr.assign(1, 0); G.apSrc.clear();
-    std::vector<int> mark(size_t(na), -1);
-    std::vector<std::vector<int>> lists;
+    G.apPtr.reserve(A.ci.size() + 1); G.apSrc.reserve(A.ci.size());
+    RowAccumulator acc(na);
     for (int i = 0; i < n; ++i) {
-        std::vector<std::pair<int, int>> cols;   // (J, slot in first-appearance order)
-        lists.clear();
-        std::vector<double> vals;
-        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) {
-            const int J = agg[size_t(A.ci[size_t(p)])];
-            if (mark[size_t(J)] < 0) { mark[size_t(J)] = int(cols.size()); cols.push_back({J, int(cols.size())}); lists.push_back({}); vals.push_back(A.v[size_t(p)]); }
-            else vals[size_t(mark[size_t(J)])] += A.v[size_t(p)];
-            lists[size_t(mark[size_t(J)])].push_back(p);
-        }
-        for (auto& c : cols) mark[size_t(c.first)] = -1;
-        std::sort(cols.begin(), cols.end());
-        for (auto& c : cols) {
-            AP.ci.push_back(c.first);
-            AP.v.push_back(vals[size_t(c.second)]);
-            for (int p : lists[size_t(c.second)]) G.apSrc.push_back(p);
-            G.apPtr.push_back(int(G.apSrc.size()));
-        }
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) acc.take(agg[size_t(A.ci[size_t(p)])], A.v[size_t(p)], p);
+        acc.emit(G.apSrc, [&](int J, double v, int end) { AP.ci.push_back(J); AP.v.push_back(v); G.apPtr.push_back(end); });
         AP.rp[size_t(i) + 1] = int(AP.ci.size());
     }
     // members of every aggregate in ascending row order (the rows of R = P^T)
@@ -129,32 +154,22 @@ void galerkin(const Csr& A, const std::vector<int>& agg, int na, Galerkin& G) {
     Ac.rp.assign(size_t(na) + 1, 0);
     Ac.ci.clear(); Ac.v.clear();
     G.acPtr.assign(1, 0); G.acSrc.clear();
+    G.acSrc.reserve(AP.ci.size());
     for (int I = 0; I < na; ++I) {
-        std::vector<std::pair<int, int>> cols;
-        lists.clear();
-        std::vector<double> vals;
         for (int q = mPtr[size_t(I)]; q < mPtr[size_t(I) + 1]; ++q) {
             const int i = mem[size_t(q)];
-            for (int e = AP.rp[size_t(i)]; e < AP.rp[size_t(i) + 1]; ++e) {
-                const int J = AP.ci[size_t(e)];
-                if (mark[size_t(J)] < 0) { mark[size_t(J)] = int(cols.size()); cols.push_back({J, int(cols.size())}); lists.push_back({}); vals.push_back(AP.v[size_t(e)]); }
-                else vals[size_t(mark[size_t(J)])] += AP.v[size_t(e)];
-                lists[size_t(mark[size_t(J)])].push_back(e);
-            }
+            for (int e = AP.rp[size_t(i)]; e < AP.rp[size_t(i) + 1]; ++e) acc.take(AP.ci[size_t(e)], AP.v[size_t(e)], e);
         }
-        for (auto& c : cols) mark[size_t(c.first)] = -1;
-        std::sort(cols.begin(), cols.end());
         bool haveDiag = false;
-        for (auto& c : cols) {
-            if (!haveDiag && c.first > I) {                  // inserted zero diagonal (engine/src/amg.cpp:83-91)
-                Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(int(G.acSrc.size())); haveDiag = true;
+        acc.emit(G.acSrc, [&](int J, double v, int end) {
+            if (!haveDiag && J > I) {                        // inserted zero diagonal (engine/src/amg.cpp:83-91)
+                Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(G.acPtr.back()); haveDiag = true;
             }
-            if (c.first == I) haveDiag = true;
-            Ac.ci.push_back(c.first);
-            Ac.v.push_back(vals[size_t(c.second)]);
-            for (int e : lists[size_t(c.second)]) G.acSrc.push_back(e);
-            G.acPtr.push_back(int(G.acSrc.size()));
-        }
+            if (J == I) haveDiag = true;
+            Ac.ci.push_back(J);
+            Ac.v.push_back(v);
+            G.acPtr.push_back(end);
+        });
         if (!haveDiag) { Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(int(G.acSrc.size())); }
         Ac.rp[size_t(I) + 1] = int(Ac.ci.size());
     }
@@ -201,7 +216,11 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
     Csr A;
     A.n = n0;
     A.rp.assign(size_t(n0) + 1, 0);
+    const size_t nnz0 = size_t(P.rowPtr[size_t(r1)] - b0);
+    A.ci.reserve(nnz0);
+    A.v.reserve(nnz0);
     std::vector<int> natPos;                     // natural position -> level-space position (relative to b0)
+    natPos.reserve(nnz0);
     for (int io = 0; io < n0; ++io) {
         const int k = P.iperm[size_t(r0 + io)];
         for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p) {
@@ -221,6 +240,8 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
         AmgLevel L0;
         L0.n = n0;
         L0.rp.assign(size_t(n0) + 1, 0);
+        L0.ci.reserve(nnz0);
+        L0.diag.reserve(size_t(n0));
         for (int k = r0; k < r1; ++k) {
             for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p) L0.ci.push_back(P.col[size_t(p)] - r0);
             L0.rp[size_t(k - r0) + 1] = int(L0.ci.size());
@@ -235,9 +256,9 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
             if (std::fabs(L0.val[size_t(L0.diag[size_t(k)])]) < 1e-300) L0.val[size_t(L0.diag[size_t(k)])] = 1.0;
         out.lv.push_back(std::move(L0));
     }
-    std::vector<int> natToLev0 = natPos;        // natural position -> level-space position of the current level
-    Csr cur = A;
-    std::vector<int> curDiag = dg;
+    std::vector<int> natToLev0 = std::move(natPos);   // natural position -> level-space position of the current level
+    Csr cur = std::move(A);
+    std::vector<int> curDiag = std::move(dg);
     while (true) {
         if (cur.n <= 400 || int(out.lv.size()) >= 14) break;          // engine/src/amg.cpp:153
         std::vector<int> agg;
@@ -254,6 +275,9 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
         // coarse level-space CSR (entries in natural order), values, diagonal positions
         std::vector<int> cNat2Lev(G.Ac.ci.size());
         C.rp.assign(size_t(na) + 1, 0);
+        C.ci.reserve(G.Ac.ci.size());
+        C.val.reserve(G.Ac.ci.size());
+        C.diag.reserve(size_t(na));
         for (int k = 0; k < na; ++k) {
             const int I = C.perm[size_t(k)];
             for (int p = G.Ac.rp[size_t(I)]; p < G.Ac.rp[size_t(I) + 1]; ++p) {
@@ -283,6 +307,7 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
         for (size_t q = 0; q < G.apSrc.size(); ++q) C.apSrc[q] = natToLev0[size_t(G.apSrc[q])];
         C.acPtr.assign(G.Ac.ci.size() + 1, 0);
         C.acSrc.clear();
+        C.acSrc.reserve(G.acSrc.size());
         {
             std::vector<int> order(G.Ac.ci.size());
             for (size_t p = 0; p < order.size(); ++p) order[size_t(cNat2Lev[p])] = int(p);
@@ -292,9 +317,9 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
                 C.acPtr[e + 1] = int(C.acSrc.size());
             }
         }
-        natToLev0 = cNat2Lev;
-        cur = G.Ac;
-        curDiag = cd;
+        natToLev0 = std::move(cNat2Lev);
+        cur = std::move(G.Ac);
+        curDiag = std::move(cd);
         out.lv.push_back(std::move(C));
     }
     out.coarseDense = cur.n <= 800;

@@ -7,7 +7,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT, load_golden
+from conftest import GOLDEN_SYSTEMS, ROOT, load_golden
 
 
 def declared_symbols():
@@ -131,3 +131,40 @@ def test_reference_tools_compile_against_the_adapters():
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", *inc, "-x", "c++", os.path.join(ROOT, "include", "rsg_ressim_adapter.hpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
+def test_host_amg_plan_matches_oracle(name, oracle):
+    """The host AMG plan (aggregation, then Galerkin products summed in the reference's order) is the oracle's
+    hierarchy: level sizes, the level-0 aggregates and every coarse operator bit for bit. Host code only
+    (rsg_debug_amg_plan builds the plan of one system from its pressure matrix; no GPU)."""
+    from ressim_gb300 import _build
+    L = C.CDLL(_build.LIB)
+    L.rsg_debug_amg_plan.argtypes = [C.c_int] + [C.c_void_p] * 3 + [C.c_int] + [C.c_void_p] * 3 + [C.c_int] + [C.c_void_p] * 4
+    A, _ = load_golden(name)
+    w, info, levels = oracle.cpr_info(A)
+    rp0, ci0, v0, agg0 = levels[0]
+    assert np.array_equal(rp0, A.rowPtr) and np.array_equal(ci0, A.col)     # the pressure matrix has S's pattern
+    ap = np.ascontiguousarray(v0, dtype=np.float64)
+    nlev = C.c_int(0)
+    rows = np.zeros(16, np.int32)
+    nnz = np.zeros(16, np.int32)
+    agg = np.zeros(A.n, np.int32)
+    m = np.zeros(A.n + 1, np.int32)
+    assert L.rsg_debug_amg_plan(A.n, A.rowPtr.ctypes.data, A.col.ctypes.data, ap.ctypes.data, 0, C.byref(nlev), rows.ctypes.data,
+                                nnz.ctypes.data, 16, m.ctypes.data, np.zeros(len(ci0), np.int32).ctypes.data,
+                                np.zeros(len(ci0)).ctypes.data, agg.ctypes.data) == 0
+    assert nlev.value == len(info)
+    assert [int(r) for r in rows[:nlev.value]] == [r for r, _ in info]
+    assert [int(q) for q in nnz[:nlev.value]] == [q for _, q in info]
+    if len(info) > 1:
+        assert np.array_equal(agg, agg0)
+    for lv in range(1, len(info)):                    # every coarse operator, pattern and values
+        rpl, cil, vl, _ = levels[lv]
+        rp = np.zeros(len(rpl), np.int32)
+        ci = np.zeros(len(cil), np.int32)
+        v = np.zeros(len(vl))
+        assert L.rsg_debug_amg_plan(A.n, A.rowPtr.ctypes.data, A.col.ctypes.data, ap.ctypes.data, lv, C.byref(nlev), rows.ctypes.data,
+                                    nnz.ctypes.data, 16, rp.ctypes.data, ci.ctypes.data, v.ctypes.data, None) == 0
+        assert np.array_equal(rp, rpl) and np.array_equal(ci, cil)
+        assert np.array_equal(v, vl)
