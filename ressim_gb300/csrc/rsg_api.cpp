@@ -303,6 +303,13 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
         if (n[s] < 1 || !rowPtr[s] || !col[s] || !val[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " is empty");
         sysRow0[size_t(s) + 1] = sysRow0[size_t(s)] + n[s];
     }
+    // the pattern of the current plan (a new Newton iteration or time step): values only, no pattern copy
+    if (h->havePlan && same_batch_pattern(h->plan, nsys, n, rowPtr, col)) {
+        std::vector<int> nnzbs(static_cast<size_t>(nsys));
+        for (int s = 0; s < nsys; ++s) nnzbs[size_t(s)] = rowPtr[s][n[s]];
+        std::vector<const double*> vals(val, val + nsys);
+        return set_values(h, vals, nnzbs);
+    }
     const int ntot = sysRow0[size_t(nsys)];
     // concatenated pattern of the block-diagonal batch
     std::vector<int> rp(size_t(ntot) + 1, 0), ci;

@@ -79,6 +79,9 @@ struct PrecDev;
 struct DevPlan;
 struct SweepState;
 // Builds the plan of a (block-diagonal batch of) BSR pattern(s). Returns false with a message on bad input.
+// True when a batch (per system: n[s] rows, rowPtr[s], col[s]) has exactly the pattern the plan was built from,
+// compared in place (no concatenated copy).
+bool same_batch_pattern(const HostPlan& P, int nsys, const int* n, const int* const* rowPtr, const int* const* col);
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
                 const std::vector<int>& col, std::string& err);
 // multicolour ordering of every system (MCBILU0, engine/src/bsr.cpp:599-653): permuted pattern and the original row /

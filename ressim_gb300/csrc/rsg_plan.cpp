@@ -260,6 +260,24 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     return true;
 }
 
+bool same_batch_pattern(const HostPlan& P, int nsys, const int* n, const int* const* rowPtr, const int* const* col) {
+    if (P.nsys != nsys || int(P.sysRow0.size()) != nsys + 1) return false;
+    for (int s = 0; s < nsys; ++s)
+        if (P.sysRow0[size_t(s) + 1] - P.sysRow0[size_t(s)] != n[s]) return false;
+    for (int s = 0; s < nsys; ++s) {
+        const int r0 = P.sysRow0[size_t(s)];
+        const int base = P.rowPtr0[size_t(r0)];
+        const int* rp = rowPtr[s];
+        for (int i = 0; i <= n[s]; ++i)
+            if (P.rowPtr0[size_t(r0 + i)] - base != rp[i]) return false;
+        const int* pc = P.col0.data() + base;
+        const int* c = col[s];
+        for (int p = 0; p < rp[n[s]]; ++p)
+            if (pc[p] - r0 != c[p]) return false;
+    }
+    return true;
+}
+
 // ====================================================================== well Schur complement
 namespace {
 struct WellParts {
@@ -387,3 +405,24 @@ int wellschur_recover(int nrows, const int* rowPtr, const int* col, const double
 }
 
 }  // namespace rsg
+
+// Diagnostics: whether a batch (b) has the pattern of the plan built from another batch (a), as rsg_set_batch decides
+// it (1 same, 0 different, -1 batch a rejected). Host code only.
+extern "C" int rsg_debug_same_pattern(int nsys, const int* na, const int* const* rpa, const int* const* cia, int nsysB, const int* nb,
+                                      const int* const* rpb, const int* const* cib) {
+    using namespace rsg;
+    std::vector<int> sysRow0(size_t(nsys) + 1, 0), rp, ci;
+    for (int s = 0; s < nsys; ++s) sysRow0[size_t(s) + 1] = sysRow0[size_t(s)] + na[s];
+    rp.assign(size_t(sysRow0[size_t(nsys)]) + 1, 0);
+    for (int s = 0; s < nsys; ++s) {
+        const int r0 = sysRow0[size_t(s)];
+        for (int i = 0; i < na[s]; ++i) {
+            rp[size_t(r0 + i) + 1] = rp[size_t(r0)] + rpa[s][i + 1];
+            for (int p = rpa[s][i]; p < rpa[s][i + 1]; ++p) ci.push_back(cia[s][p] + r0);
+        }
+    }
+    HostPlan P;
+    std::string err;
+    if (!build_plan(P, nsys, sysRow0, rp, ci, err)) return -1;
+    return same_batch_pattern(P, nsysB, nb, rpb, cib) ? 1 : 0;
+}

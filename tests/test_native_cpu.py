@@ -168,3 +168,46 @@ def test_host_amg_plan_matches_oracle(name, oracle):
                                     nnz.ctypes.data, 16, rp.ctypes.data, ci.ctypes.data, v.ctypes.data, None) == 0
         assert np.array_equal(rp, rpl) and np.array_equal(ci, cil)
         assert np.array_equal(v, vl)
+
+
+def test_same_pattern_check_of_set_batch():
+    """rsg_set_batch reuses its plan when the batch has the plan's pattern, compared in place: the same batch is
+    the same; a moved column, a row of another length, another system count are not. Host code only."""
+    from ressim_gb300 import _build, synth
+    L = C.CDLL(_build.LIB)
+    L.rsg_debug_same_pattern.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+
+    class Pattern:
+        def __init__(self, n, rowPtr, col):
+            self.n = n
+            self.rowPtr = np.ascontiguousarray(rowPtr, np.int32)
+            self.col = np.ascontiguousarray(col, np.int32)
+
+    mats = [Pattern(s.A.n, s.A.rowPtr, s.A.col) for s in synth.ensemble(n_real=3, nx=8, ny=7, nz=3)]
+
+    def same(a, b):
+        na, nb = np.array([m.n for m in a], np.int32), np.array([m.n for m in b], np.int32)
+        ra, ca = (C.c_void_p * len(a))(*[m.rowPtr.ctypes.data for m in a]), (C.c_void_p * len(a))(*[m.col.ctypes.data for m in a])
+        rb, cb = (C.c_void_p * len(b))(*[m.rowPtr.ctypes.data for m in b]), (C.c_void_p * len(b))(*[m.col.ctypes.data for m in b])
+        return L.rsg_debug_same_pattern(len(a), na.ctypes.data, ra, ca, len(b), nb.ctypes.data, rb, cb)
+
+    assert same(mats, mats) == 1
+    assert same(mats, [Pattern(m.n, m.rowPtr.copy(), m.col.copy()) for m in mats]) == 1     # equal copies
+    assert same(mats, mats[:2]) == 0                                                       # another system count
+    B = mats[1]
+    # a column moved one place right in a row whose last entry has a free column after it (still sorted)
+    col = B.col.copy()
+    moved = False
+    for i in range(B.n):
+        p = B.rowPtr[i + 1] - 1
+        if col[p] > i and col[p] + 1 < B.n:
+            col[p] += 1
+            moved = True
+            break
+    assert moved
+    assert same(mats, [mats[0], Pattern(B.n, B.rowPtr, col), mats[2]]) == 0
+    # a row of another length: the last off-diagonal entry of a row dropped
+    i = next(i for i in range(B.n) if B.col[B.rowPtr[i + 1] - 1] > i)
+    rp2 = B.rowPtr.copy()
+    rp2[i + 1:] -= 1
+    assert same(mats, [mats[0], Pattern(B.n, rp2, np.delete(B.col, B.rowPtr[i + 1] - 1)), mats[2]]) == 0
