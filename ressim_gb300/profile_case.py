@@ -5,6 +5,7 @@ workload, for ncu captures of single kernels or of one step's launch list (the b
     python -m ressim_gb300.profile_case bilu0_grid180k --precision mixed_f32 --applications 3
     python -m ressim_gb300.profile_case ensemble64 --applications 3
     python -m ressim_gb300.profile_case ensemble64 --steps 2
+    python -m ressim_gb300.profile_case ensemble64 --steps 1 --sweep cta     # the one-kernel CPR application
 
 cpr_grid810k: 180x90x50 cells (810,000 block rows, sigma ln k = 1.5, 4 wells), CPR applied grid-wide (a system
 this size does not fit one SM). bilu0_grid180k: 100x60x30 cells (180,000 block rows), BILU0 with the grid-wide
@@ -30,6 +31,8 @@ def main(argv=None):
     ap.add_argument("--precision", default="mixed_f32", choices=["fp64", "mixed", "mixed_f32"])
     ap.add_argument("--applications", type=int, default=2)
     ap.add_argument("--steps", type=int, default=0, help="ensemble64: whole set-up + solve steps instead of applications")
+    ap.add_argument("--sweep", default=None, choices=["auto", "cta", "split", "grid"],
+                    help="sweep / CPR form (default: the case's; cta = the one-kernel CPR application)")
     args = ap.parse_args(argv)
     from ressim_gb300 import synth
     from ressim_gb300.solver import DeviceSolver
@@ -40,8 +43,8 @@ def main(argv=None):
     else:
         s = synth.make_system(*c["shape"], sigma=1.5, seed=3, dt=5.0, wells="random", n_wells=4)
         mats, b = [s.A], s.b
-    d = DeviceSolver(precond=c["precond"], precision=args.precision, sweep=c["sweep"], krylov="bicgstab", check_every=4,
-                     use_graphs=True)
+    d = DeviceSolver(precond=c["precond"], precision=args.precision, sweep=args.sweep or c["sweep"], krylov="bicgstab",
+                     check_every=4, use_graphs=True)
     if len(mats) > 1:
         d.set_batch(mats)
     else:
