@@ -31,6 +31,7 @@ def main(argv=None):
     ap.add_argument("--precision", default="mixed_f32", choices=["fp64", "mixed", "mixed_f32"])
     ap.add_argument("--applications", type=int, default=2)
     ap.add_argument("--steps", type=int, default=0, help="ensemble64: whole set-up + solve steps instead of applications")
+    ap.add_argument("--systems", type=int, default=64, help="ensemble64: realisations of the ensemble (the bench's 64)")
     ap.add_argument("--sweep", default=None, choices=["auto", "cta", "split", "grid"],
                     help="sweep / CPR form (default: the case's; cta = the one-kernel CPR application)")
     args = ap.parse_args(argv)
@@ -38,7 +39,7 @@ def main(argv=None):
     from ressim_gb300.solver import DeviceSolver
     c = CASES[args.case]
     if c["shape"] is None:
-        systems = synth.ensemble(n_real=64)
+        systems = synth.ensemble(n_real=args.systems)
         mats, b = [s.A for s in systems], np.concatenate([s.b for s in systems])
     else:
         s = synth.make_system(*c["shape"], sigma=1.5, seed=3, dt=5.0, wells="random", n_wells=4)
