@@ -10,10 +10,15 @@ products / true residual, FP32 preconditioner).
 Reported besides ``value`` (device-resident inputs, CUDA events on the solver stream):
 * ``e2e``: the same step through the C ABI with host buffers (matrix values and right-hand sides copied in,
   solutions copied out, every step);
+* ``fp64_batched``: the same batch and CPR in plain FP64, timed the same way (the precision form's gain);
 * ``fp64_plain``: the plain FP64 GPU path, the 64 systems solved one after another (one handle each);
+* ``error_vs_fp64``: each result's distance to its system's FP64 solution (plain FP64 at 1e-12);
 * ``roofline`` of the dominant kernel and ``kernels`` (per-launch device time and algorithmic bytes);
-* ``cpu_baseline``: the C restatement (oracle/) of the reference FP64 CPR-BiCGSTAB on the host cores,
-  on a bounded sample of the same systems.
+* ``cpu_baseline``: the reference engine's own FP64 CPR-BiCGSTAB (compiled on this host from its staged sources,
+  oracle/_ref) on the host cores, on a bounded sample of the same systems; the C restatement (oracle/) where the
+  reference build is absent.
+
+``--impl reference`` times the same reference CPU path on every step's 64 systems (rank 0 only).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--serving on|off|only] [--spe10]
 """
@@ -155,8 +160,64 @@ def cpr_bytes(nnzb, n, levels, sv, sx):
     return int(b + n * (3 * sx * 2) + nnzb * (3 * sv + 4))
 
 
-def cpu_baseline(systems, budget_s=20.0):
-    """Oracle (C restatement of the reference FP64 CPR + BiCGSTAB) on the host cores, bounded sample."""
+class RefEnsemble:
+    """The reference engine's own CPU path over the ensemble (oracle/_ref/libressim_ref.so, compiled on this host from
+    the reference's staged sources): one BlockCPR per realisation with the AMG aggregates reused after the first
+    set-up, BiCGSTAB to the tolerance. Two ways to use the host's cores: one system after another with the reference's
+    OpenMP on all physical cores, or one system per core at once (how a study runs one simulator per realisation)."""
+
+    def __init__(self, systems):
+        import ctypes as C
+        from oracle import REF_LIB
+        L = C.CDLL(REF_LIB)
+        L.ref_ens_create.restype = C.c_void_p
+        L.ref_ens_create.argtypes = [C.c_int]
+        L.ref_ens_set.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_ens_step.restype = C.c_double
+        L.ref_ens_step.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int]
+        L.ref_ens_result.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_ens_free.argtypes = [C.c_void_p]
+        L.ref_physical_cores.restype = C.c_int
+        self.L, self.n = L, len(systems)
+        self.h = L.ref_ens_create(len(systems))
+        for k, s in enumerate(systems):
+            L.ref_ens_set(self.h, k, s.A.n, s.A.nb, s.A.rowPtr.ctypes.data, s.A.col.ctypes.data, s.A.val.ctypes.data, s.b.ctypes.data)
+        self.cores = int(L.ref_physical_cores())
+
+    def step(self, concurrent):
+        return float(self.L.ref_ens_step(self.h, TOL, MAXIT, self.cores if concurrent else 1, 0))
+
+    def converged(self):
+        return all(self.L.ref_ens_result(self.h, k, None, None, None) == 1 for k in range(self.n))
+
+    def close(self):
+        self.L.ref_ens_free(self.h)
+
+
+def reference_available():
+    from oracle import RefShim
+    return RefShim.available()
+
+
+def cpu_baseline(systems):
+    """The reference CPU path on the host cores, on a bounded sample: one untimed pass over the ensemble (first
+    set-up of every realisation's AMG), then one timed pass in each way of using the cores; the faster is reported.
+    Without the reference build, the C restatement (oracle/) of the same path, one system after another."""
+    if reference_available():
+        R = RefEnsemble(systems)
+        try:
+            R.step(True)
+            t_omp, t_con = R.step(False), R.step(True)
+            ok = R.converged()
+        finally:
+            R.close()
+        best = min(t_omp, t_con)
+        return {"value": len(systems) / best, "unit": "solves/s", "cores": R.cores, "kind": "reference",
+                "mode": "one system per core" if t_con <= t_omp else "OpenMP per system",
+                "modes_solves_per_s": {"openmp_per_system": len(systems) / t_omp, "system_per_core": len(systems) / t_con},
+                "all_converged": bool(ok),
+                "sample": f"one pass over the {len(systems)} ensemble systems after a warm-up pass (reference BlockCPR + BiCGSTAB, "
+                          f"FP64, AMG reused), faster of the two ways of using {R.cores} cores"}
     from oracle import Oracle
     o = Oracle()
     threads = os.cpu_count() or 1
@@ -164,9 +225,9 @@ def cpu_baseline(systems, budget_s=20.0):
     t0 = time.perf_counter()
     done = 0
     for s in systems:
-        x, conv, its, rr, ts, tv = o.solve(s.A, s.b, prec=CPU_PREC, method=0, tol=TOL, maxit=MAXIT)
+        o.solve(s.A, s.b, prec=CPU_PREC, method=0, tol=TOL, maxit=MAXIT)
         done += 1
-        if time.perf_counter() - t0 > budget_s:
+        if time.perf_counter() - t0 > 20.0:
             break
     dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": "solves/s", "cores": threads, "kind": "port",
@@ -257,33 +318,51 @@ def spe10_report(local):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference engine's own CPU solve of the whole ensemble per step (every realisation's
+    BlockCPR set-up with AMG reuse, then BiCGSTAB to 1e-6, FP64), on all host cores, in the faster of its two ways of
+    using them (chosen in the warm-up). Rank 0 only; without the reference build, the C restatement."""
     if rank != 0:
         return 0
     systems = ensemble(0)
-    per_step = max(1, int(os.environ.get("RSG_REF_SYSTEMS_PER_STEP", "4")))
-    from oracle import Oracle
-    o = Oracle()
-    threads = os.cpu_count() or 1
-    o.set_threads(threads)
-    times = []
-    k = 0
-    for step in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        for _ in range(per_step):
-            s = systems[k % len(systems)]
-            k += 1
-            o.solve(s.A, s.b, prec=CPU_PREC, method=0, tol=TOL, maxit=MAXIT)
-        if step >= args.warmup:
-            times.append(time.perf_counter() - t0)
-    T = sum(times)
-    v = per_step * len(times) / T
-    line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * T / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (ressim_gb300.synth, seeded)", "impl": "reference",
-            "config": {"workload": workload(), "systems_per_step": per_step, "solver": "CPR-BiCGSTAB FP64 (reference CPU algorithm)"},
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": f"{per_step} ensemble systems per step (C restatement of the reference CPU path)"},
-            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line = {"metric": METRIC, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (ressim_gb300.synth, seeded)", "impl": "reference"}
+    if reference_available():
+        R = RefEnsemble(systems)
+        R.step(True)                               # first set-up of every realisation's AMG hierarchy
+        warm = {True: [], False: []}
+        for w in range(max(2, args.warmup)):
+            warm[w % 2 == 0].append(R.step(w % 2 == 0))
+        concurrent = min(warm[True]) <= min(warm[False])
+        times = [R.step(concurrent) for _ in range(args.steps)]
+        ok = R.converged()
+        R.close()
+        T = sum(times)
+        v = len(systems) * len(times) / T
+        mode = "one system per core (one OpenMP thread each)" if concurrent else "one system after another, OpenMP on all cores"
+        line.update({"value": v, "ms_per_step": 1e3 * T / len(times),
+                     "config": {"workload": workload(), "systems_per_step": len(systems), "solver": "reference BlockCPR + BiCGSTAB, FP64",
+                                "mode": mode, "all_converged": bool(ok)},
+                     "cpu_baseline": {"value": v, "unit": "solves/s", "cores": R.cores, "kind": "reference",
+                                      "sample": f"all {len(systems)} ensemble systems per step, {mode}"}})
+    else:
+        from oracle import Oracle
+        o = Oracle()
+        threads = os.cpu_count() or 1
+        o.set_threads(threads)
+        times = []
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            for s in systems:
+                o.solve(s.A, s.b, prec=CPU_PREC, method=0, tol=TOL, maxit=MAXIT)
+            if step >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        T = sum(times)
+        v = len(systems) * len(times) / T
+        line.update({"value": v, "ms_per_step": 1e3 * T / len(times),
+                     "config": {"workload": workload(), "systems_per_step": len(systems), "solver": "CPR-BiCGSTAB FP64 (C restatement)"},
+                     "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                                      "sample": f"all {len(systems)} ensemble systems per step (C restatement of the reference CPU path)"}})
+    line["e2e"] = {"value": line["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     print(json.dumps(line))
     return 0
 
@@ -386,6 +465,52 @@ def main():
     value = world * N_REAL * args.steps / T
     ok = all(r.converged for r in results) and float(np.max(tr)) <= TOL
 
+    # ---------------- the same batch in plain FP64 (same CPR, FP64 factors, hierarchy and sweeps): the precision gain
+    dev64 = DeviceSolver(krylov="bicgstab", check_every=4, use_graphs=True, device=local, **PLAIN_PREC)
+    dev64.set_batch(mats)
+    s64 = torch.cuda.ExternalStream(dev64.stream)
+    d_x64 = torch.zeros_like(d_b)
+
+    def step64():
+        dev64.setup()
+        return dev64.solve_device(d_b.data_ptr(), d_x64.data_ptr(), tol=TOL, maxit=MAXIT)
+
+    for _ in range(args.warmup):
+        step64()
+    barrier()
+    ev64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ok64 = True
+    for k in range(args.steps):
+        ev64[k][0].record(s64)
+        r64 = step64()
+        ev64[k][1].record(s64)
+        ok64 &= r64.converged
+    barrier()
+    T64 = sum(a.elapsed_time(b) for a, b in ev64) / 1e3
+    if dist:
+        T64 = max_over_ranks(T64, dist, f"cuda:{local}")
+    its64, _, tr64 = dev64.batch_results()
+    fp64_batched = {"value": world * N_REAL * args.steps / T64, "unit": "solves/s", "ms_per_step": 1e3 * T64 / args.steps,
+                    "iterations": {"mean": float(np.mean(its64)), "max": int(np.max(its64))},
+                    "all_converged": bool(ok64 and float(np.max(tr64)) <= TOL)}
+    # error of every result against the FP64 solution of its system (plain FP64 path at 1e-12, pinned to the
+    # reference's solution by the parity tests): the precision form at 1e-6, and the plain FP64 solve at 1e-6 beside it
+    x64 = d_x64.cpu().numpy()
+    dev64.solve_device(d_b.data_ptr(), d_x64.data_ptr(), tol=1e-12, maxit=MAXIT)
+    xref = d_x64.cpu().numpy()
+    dev64.close()
+    err32, err64 = [], []
+    off = 0
+    for A in mats:
+        sl = slice(off, off + 3 * A.n)
+        nr = np.linalg.norm(xref[sl])
+        err32.append(float(np.linalg.norm(x_dev[sl] - xref[sl]) / nr))
+        err64.append(float(np.linalg.norm(x64[sl] - xref[sl]) / nr))
+        off += 3 * A.n
+    error_vs_fp64 = {"reference": "plain FP64 GPU solution at 1e-12 of each system",
+                     "precision_form_max": max(err32), "precision_form_median": float(np.median(err32)),
+                     "fp64_at_same_tol_max": max(err64), "fp64_at_same_tol_median": float(np.median(err64))}
+
     # ---------------- per-kernel device time (events on the solver stream) for the roofline
     reps = 20
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -477,7 +602,8 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "mixed f32/f64 (FP32 preconditioner, FP64 Krylov vectors, inner products and true residual)",
             "data": "synthetic (ressim_gb300.synth: seeded black-oil Jacobians of the named shapes)",
             "config": {"workload": workload(), "systems": N_REAL, "grid": f"{NX}x{NY}x{NZ}", "sigma_lnk": SIGMA,
                        "active_cells": [int(min(A.n for A in mats)), int(max(A.n for A in mats))], "block_rows": n_rows,
@@ -489,7 +615,10 @@ def main():
                            "note": "batched step: all 64 systems complete together"},
             "iterations": {"mean": mean_its, "max": int(np.max(its))}, "max_true_relres": float(np.max(tr)), "all_converged": bool(ok),
             "last_step_device_ms": {"setup": st_last.setup_ms, "solve": st_last.solve_ms},
-            "fp64_plain": fp64_plain, "batched_mixed_over_plain_fp64": value / world / fp64_plain["value"],
+            "fp64_plain": fp64_plain, "fp64_batched": fp64_batched, "max_rel_err_vs_fp64": error_vs_fp64["precision_form_max"],
+            "error_vs_fp64": error_vs_fp64,
+            "batched_mixed_over_plain_fp64": value / world / fp64_plain["value"],
+            "batched_mixed_over_batched_fp64": value / fp64_batched["value"],
             "e2e": e2e, "roofline": roofline, "roofline_spmv": roofline_spmv, "kernels": kernels, "gpu_launches": int(launches),
             "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving,
         }

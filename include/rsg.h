@@ -172,8 +172,9 @@ int rsg_precond_level_probe(rsg_solver* h, int reps);
  * 129 KiB array in the library's device memory, present on every device that loads the library; hence the limit of
  * n <= 4,194,304 block rows (larger n returns RSG_EINVAL). The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress): make that first call before any stream capture. All calls share the array; the
- * call clears its counter first, but calls that overlap on the GPU race: order them on one stream. It calls no
- * cudaMalloc / cudaFree or other allocating routine. */
+ * call clears its counter first, but calls that overlap on the GPU race: order them on one stream. d_y must not
+ * alias d_x or d_w (RSG_EINVAL). The looked-up address does not survive cudaDeviceReset: do not call this entry point
+ * again on a device the process has reset. It calls no cudaMalloc / cudaFree or other allocating routine. */
 int rsg_spmv_dot_noalloc(int n, int nb, const int* d_rowPtr, const int* d_col, const double* d_val, const double* d_x,
                          double* d_y, const double* d_w, double* d_dot, void* stream);
 

@@ -7,7 +7,9 @@
 //    ressim::setDistributedSolver() for the FP64 path (the Newton loop trusts its result at the linear tolerance,
 //    engine/src/simulator.cpp:3358-3367) or with ressim::setGpuBlockSolver() for the mixed-precision path that
 //    the engine wraps in its own FP64 refinement (refineWithDevice, engine/src/simulator.cpp:3368-3378).
-//    solve() returns false on any device error or non-finite result, so the engine falls back to its CPU path.
+//    By default it chooses the preconditioner as the engine does (CPR from 500 cells, else BILU0) and its GMRES
+//    fallback is GMRES(60), the engine's. solve() returns false on any device error or non-finite result (and, in
+//    the FP64 role, on a solve that missed the tolerance), so the engine falls back to its CPU path.
 //  * rsg::RsgBlockSolver -- the BlockSolver interface that tools/lsbench.cpp:65-81 expects from the (absent)
 //    header ressim/blocksolve.h: full scalar CSR with well rows -> well Schur complement -> device solve ->
 //    recovery of the BHPs.
@@ -24,29 +26,51 @@ namespace rsg {
 
 class RsgGpuBlockSolver : public ressim::GpuBlockSolver {
 public:
-    explicit RsgGpuBlockSolver(int precision = RSG_FP64, int precond = RSG_PREC_BILU0, int krylov = RSG_KRYLOV_BICGSTAB) {
+    // Preconditioner choice of the engine itself: CPR from 500 cells, BILU0 below (linearSolver 2,
+    // engine/src/simulator.cpp:224)
+    static constexpr int kEngineChoice = -1;
+    // Distributed: registered with setDistributedSolver, the result must meet the tolerance (false otherwise, and the
+    // engine solves the system on its CPU path). Refinement: registered with setGpuBlockSolver, the inner solve of
+    // the engine's FP64 defect correction (refineWithDevice, engine/src/bsr.cpp:1373-1396): an iterate that stopped at
+    // the iteration limit still corrects x, so only device errors and non-finite results return false.
+    enum class Role { Distributed, Refinement };
+
+    explicit RsgGpuBlockSolver(int precision = RSG_FP64, int precond = kEngineChoice, int krylov = RSG_KRYLOV_BICGSTAB,
+                               Role role = Role::Distributed)
+        : precond_(precond), role_(role) {
         rsg_options o;
         rsg_default_options(&o);
         o.precision = precision;
-        o.precond = precond;
+        o.precond = precond == kEngineChoice ? RSG_PREC_CPR : precond;
         o.krylov = krylov;
-        ok_ = rsg_create(&h_, &o) == RSG_OK;
+        o.restart = 60;   // the engine's GMRES fallback is GMRES(60) (engine/src/simulator.cpp:3390)
+        o.gmres_fallback = role == Role::Distributed ? 1 : 0;   // try it on the device before handing back to the CPU
+        ok_ = rsg_create(&cpr_, &o) == RSG_OK;
+        if (ok_ && precond == kEngineChoice) {
+            o.precond = RSG_PREC_BILU0;
+            ok_ = rsg_create(&ilu_, &o) == RSG_OK;
+        }
     }
-    ~RsgGpuBlockSolver() override { if (h_) rsg_destroy(h_); }
+    ~RsgGpuBlockSolver() override {
+        if (cpr_) rsg_destroy(cpr_);
+        if (ilu_) rsg_destroy(ilu_);
+    }
+    bool ok() const { return ok_; }
     const char* name() const override { return rsg_version(); }
     bool solve(const ressim::BSR& A, const std::vector<double>& b, std::vector<double>& x, double tol, int maxIt,
                int& iterations) override {
         std::lock_guard<std::mutex> lk(mu_);   // studies run several simulators at once: one solve per handle at a time
         iterations = 0;
         if (!ok_ || A.nb != 3) return false;
-        if (rsg_set_matrix(h_, A.n, A.nb, A.rowPtr.data(), A.col.data(), A.val.data()) != RSG_OK) return false;
-        if (rsg_setup(h_, nullptr) != RSG_OK) return false;
+        rsg_solver* h = (precond_ == kEngineChoice && A.n < 500) ? ilu_ : cpr_;
+        if (rsg_set_matrix(h, A.n, A.nb, A.rowPtr.data(), A.col.data(), A.val.data()) != RSG_OK) return false;
+        if (rsg_setup(h, nullptr) != RSG_OK) return false;
         x.assign(size_t(A.size()), 0.0);
         double rr = 0;
-        const int rc = rsg_solve(h_, b.data(), x.data(), tol, maxIt, &iterations, &rr);
+        const int rc = rsg_solve(h, b.data(), x.data(), tol, maxIt, &iterations, &rr);
         rsg_stats st;
-        if (rsg_get_stats(h_, &st) == RSG_OK) seconds_ += 1e-3 * (st.setup_ms + st.solve_ms);
-        if (rc != RSG_OK) return false;
+        if (rsg_get_stats(h, &st) == RSG_OK) seconds_ += 1e-3 * (st.setup_ms + st.solve_ms);
+        if (rc < 0 || (rc == RSG_ENOTCONV && role_ == Role::Distributed)) return false;
         for (double v : x)
             if (!std::isfinite(v)) return false;
         return true;
@@ -54,7 +78,10 @@ public:
     double deviceSeconds() const override { return seconds_; }
 
 private:
-    rsg_solver* h_ = nullptr;
+    rsg_solver* cpr_ = nullptr;
+    rsg_solver* ilu_ = nullptr;
+    int precond_;
+    Role role_;
     bool ok_ = false;
     double seconds_ = 0;
     std::mutex mu_;

@@ -225,6 +225,10 @@ class Oracle:
         finally:
             self.L.orc_cpr_free(h)
 
+    def cpr_handle(self, A, acc=None, lean=False):
+        """A set-up BlockCPR (engine/src/bsr.cpp:993-1084) kept for repeated applications: ``h.apply(r)``."""
+        return _CprHandle(self, A, acc, lean)
+
     def wellschur(self, J, na, nv, nw, b):
         """J: scalar CSR (rowPtr, col, val); returns (S as BSR-like dict, bc) or None."""
         rp, ci, v = (_arr(J[0], np.int32), _arr(J[1], np.int32), _arr(J[2], np.float64))
@@ -248,6 +252,30 @@ class Oracle:
         x = np.zeros(rp.size - 1)
         self.L.orc_wellschur_recover(rp.size - 1, rp, ci, v, na, nv, nw, _arr(b, np.float64), _arr(xc, np.float64), x)
         return x
+
+
+class _CprHandle:
+    """Owner of one ``orc_cpr`` set-up; freed with the object."""
+
+    def __init__(self, o: Oracle, A, acc, lean):
+        self.L = o.L
+        self.L.orc_cpr_apply.argtypes = [C.c_void_p, _f64p, _f64p]
+        self.L.orc_cpr_apply.restype = None
+        self.N = A.n * A.nb
+        accv = None if acc is None else _arr(acc, np.float64)
+        self._acc = accv
+        self.h = self.L.orc_cpr_setup(A.n, A.nb, A.rowPtr, A.col, A.val, None if accv is None else accv.ctypes.data_as(C.c_void_p),
+                                      1 if lean else 0)
+
+    def apply(self, r):
+        z = np.zeros(self.N)
+        self.L.orc_cpr_apply(self.h, _arr(r, np.float64), z)
+        return z
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_cpr_free(self.h)
+            self.h = None
 
 
 class RefShim:

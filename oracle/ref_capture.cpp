@@ -1,8 +1,7 @@
 // Golden-system capture harness (test infrastructure; runs only where the reference tree exists).
 //
-// Builds the 20x20x4 three-phase waterflood from the reference's own input generators
-// (generateGeometry / generateRock / makeCorrelationPVT / makeCoreySWOF / makeCoreySGOF,
-// engine/src/tools.cpp:13-245), runs the reference black-oil simulator, and records every
+// Builds the 20x20x4 three-phase waterflood from the reference's own input generators (oracle/ref_case.hpp),
+// runs the reference black-oil simulator, and records every
 // Schur-reduced Newton system (S, b) that the Newton loop hands to the double-precision solver
 // hook (engine/src/simulator.cpp:3358-3367, hook declared at engine/include/ressim/bsr.h:153-157).
 // The hook returns false, so the engine falls back to its own CPU solver and the run is the
@@ -15,10 +14,9 @@
 // System file format (little endian): int32 magic 0x42475352 ("RSGB"), int32 version 1, int32 n,
 // int32 nb, int32 nnzb, int32 maxIt, float64 tol, int32 rowPtr[n+1], int32 col[nnzb],
 // float64 val[nnzb*nb*nb], float64 b[n*nb].
+#include "ref_case.hpp"
 #include "ressim/bsr.h"
-#include "ressim/case.h"
 #include "ressim/simulator.h"
-#include "ressim/tools.h"
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -62,37 +60,7 @@ int main(int argc, char** argv) {
     const double sigma = argc > 8 ? std::atof(argv[8]) : 1.0;
     const unsigned seed = argc > 9 ? unsigned(std::atoi(argv[9])) : 0u;
 
-    // the demo case supplies fluids-in-place, equilibration and controls; grid, rock, PVT and rel-perm are
-    // replaced by the generator outputs of the 20x20x4 waterflood
-    Case c = makeDemoCase();
-    c.title = "golden capture: generated waterflood";
-    GeomInput gi; gi.nx = nx; gi.ny = ny; gi.nz = nz; gi.dx = 100; gi.dy = 100; gi.dz.assign(size_t(nz), 20.0); gi.top = 8325;
-    c.grid = GridInput{};
-    generateGeometry(gi, c.grid);
-    RockGenInput ri; ri.layerPerm = {100}; ri.layerPoro = {0.2}; ri.sigmaLn = sigma; ri.corrX = 5; ri.corrY = 5;
-    ri.poroPermExp = 0; ri.seed = seed;
-    generateRock(ri, c.grid);
-    CorrelationInput pvt;
-    makeCorrelationPVT(pvt, c.units, c.props);
-    CoreyInput cor; cor.swc = 0.2; cor.sorw = 0.2; cor.nw = 2; cor.now = 2;
-    makeCoreySWOF(cor, c.props.swof);
-    makeCoreySGOF(cor, c.props.sgof);
-    c.wells.clear();
-    WellInput prod; prod.name = "PROD"; prod.type = WellType::Producer; prod.i = nx - 1; prod.j = ny - 1;
-    { Completion cp; cp.i = nx - 1; cp.j = ny - 1; cp.k1 = 0; cp.k2 = nz - 1; prod.completions.push_back(cp); }
-    WellInput inj; inj.name = "INJ"; inj.type = WellType::WaterInjector; inj.i = 0; inj.j = 0;
-    { Completion cp; cp.i = 0; cp.j = 0; cp.k1 = 0; cp.k2 = nz - 1; inj.completions.push_back(cp); }
-    c.wells = {prod, inj};
-    WellControl wp; wp.well = "PROD"; wp.mode = Control::ORAT; wp.orat = 1500; wp.bhp = 1000;
-    WellControl wi; wi.well = "INJ"; wi.mode = Control::RATE; wi.rate = 2000; wi.bhp = 6000;
-    c.schedule.clear();
-    for (int s = 0; s < nsteps; ++s) {
-        ReportStep r; r.length = stepDays;
-        if (s == 0) r.controls = {wp, wi};
-        c.schedule.push_back(r);
-    }
-    c.tuning.linearSolver = linearSolver;
-    c.tuning.blockSolver = true;
+    const Case c = rsgref::waterfloodCase(nsteps, stepDays, linearSolver, nx, ny, nz, sigma, seed);
 
     Capture cap; cap.dir = dir;
     setDistributedSolver(&cap);

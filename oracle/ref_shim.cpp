@@ -190,3 +190,86 @@ int ref_devcpr_apply(int n, int nb, const int* rowPtr, const int* col, const dou
 }
 
 }  // extern "C"
+
+// ---- the reference CPU path over an ensemble (the timed CPU baseline): one BlockCPR per realisation, as one
+// simulator per realisation keeps its own (engine/src/simulator.cpp: bcpr_), set up on each new Jacobian with the AMG
+// aggregates reused from the first set-up (BlockCPR::setup reuseAmg, engine/src/bsr.cpp:993-1059), then BiCGSTAB
+// (engine/src/linsolve.cpp:159-216) from x0 = 0.
+#include <atomic>
+#include <chrono>
+#include <thread>
+
+namespace {
+struct RefMember {
+    BSR A;
+    std::vector<double> b, x;
+    BlockCPR cpr;
+    bool built = false;
+    int its = 0, conv = 0;
+    double relres = 0;
+};
+struct RefEnsemble {
+    std::vector<RefMember> m;
+};
+void solveMember(RefMember& s, double tol, int maxIt) {
+    s.cpr.setup(s.A, nullptr, s.built);
+    s.built = true;
+    BsrOperator op(s.A);
+    const LinResult r = bicgstab(op, s.cpr, s.b, s.x, tol, maxIt);
+    s.its = r.iterations;
+    s.relres = r.relResidual;
+    s.conv = r.converged ? 1 : 0;
+}
+}  // namespace
+
+extern "C" {
+
+int ref_physical_cores() { return physicalCores(); }
+
+void* ref_ens_create(int nsys) {
+    auto* e = new RefEnsemble;
+    e->m.resize(size_t(nsys));
+    return e;
+}
+
+void ref_ens_set(void* h, int s, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b) {
+    RefMember& m = static_cast<RefEnsemble*>(h)->m[size_t(s)];
+    m.A = makeBsr(n, nb, rowPtr, col, val);
+    m.b.assign(b, b + size_t(n) * nb);
+    m.built = false;
+}
+
+// One step over every member: set-up (AMG refresh after the first) and solve. workers <= 1: one member after another
+// with the reference's OpenMP on `threads` threads (<= 0: its default, one per physical core); workers > 1: that many
+// members at once, one OpenMP thread each. Returns the wall seconds of the step.
+double ref_ens_step(void* h, double tol, int maxIt, int workers, int threads) {
+    RefEnsemble& e = *static_cast<RefEnsemble*>(h);
+    unsetenv("RESSIM_LEVEL_ILU");   // the engine's own choice of BILU0 sweep (serial / contiguous levels)
+    const auto t0 = std::chrono::steady_clock::now();
+    if (workers <= 1) {
+        setNumThreads(threads);
+        for (RefMember& s : e.m) solveMember(s, tol, maxIt);
+    } else {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> pool;
+        for (int w = 0; w < workers; ++w)
+            pool.emplace_back([&] {
+                setNumThreads(1);
+                for (size_t k; (k = next.fetch_add(1)) < e.m.size();) solveMember(e.m[k], tol, maxIt);
+            });
+        for (auto& t : pool) t.join();
+    }
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int ref_ens_result(void* h, int s, double* x, int* its, double* relres) {
+    const RefMember& m = static_cast<RefEnsemble*>(h)->m[size_t(s)];
+    if (x) std::memcpy(x, m.x.data(), sizeof(double) * m.x.size());
+    if (its) *its = m.its;
+    if (relres) *relres = m.relres;
+    return m.conv;
+}
+
+void ref_ens_free(void* h) { delete static_cast<RefEnsemble*>(h); }
+
+}  // extern "C"

@@ -114,6 +114,25 @@ def read_dump(path: str):
     return ScalarCSR(rp, ci, v), b, na, nv, nw, acc
 
 
+def write_lsbench(path: str, J: ScalarCSR, rhs, na: int, nv: int, nw: int, acc=None):
+    """Write a full Jacobian in the layout tools/lsbench.cpp:22-40 reads: header ``[n, nnz, na, nv, nw]``, rowPtr,
+    col, val, rhs, then an int32 ``hasAcc`` and, if set, the na*nv*nv accumulation blocks. The simulator's own dump
+    (read_dump) orders its header ``[n, na, nv, nw, nnz]`` and keeps the blocks in a ``.acc`` side file; this writes
+    the same content in the benchmark's layout."""
+    rp = np.ascontiguousarray(J.rowPtr, dtype=np.int32)
+    n = rp.size - 1
+    nnz = int(rp[-1])
+    with open(path, "wb") as f:
+        f.write(struct.pack("<5i", n, nnz, na, nv, nw))
+        f.write(rp.tobytes())
+        f.write(np.ascontiguousarray(J.col, dtype=np.int32).tobytes())
+        f.write(np.ascontiguousarray(J.val, dtype=np.float64).tobytes())
+        f.write(np.ascontiguousarray(rhs, dtype=np.float64).tobytes())
+        f.write(struct.pack("<i", 0 if acc is None else 1))
+        if acc is not None:
+            f.write(np.ascontiguousarray(acc, dtype=np.float64).tobytes())
+
+
 def read_system(path: str) -> NewtonSystem:
     """Read a captured Schur-reduced system (format written by oracle/ref_capture.cpp)."""
     with open(path, "rb") as f:

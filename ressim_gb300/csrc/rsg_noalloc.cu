@@ -85,7 +85,10 @@ __global__ void __launch_bounds__(kThreads) k_spmv_dot_noalloc(int n, const int*
     }
 }
 
-// device address of the scratch array, looked up once per device (host code cannot use the symbol itself)
+// device address of the scratch array, looked up once per device (host code cannot use the symbol itself). The
+// address belongs to the device's context of the first call: after cudaDeviceReset the library's module is loaded
+// again in a new context, and this cache would hand the kernel the old address, so a process that resets a device
+// must not call this entry point on that device again.
 std::mutex g_mu;
 double* g_addr[64] = {nullptr};
 
@@ -122,6 +125,10 @@ extern "C" int rsg_spmv_dot_noalloc(int n, int nb, const int* d_rowPtr, const in
     }
     if (!d_rowPtr || !d_col || !d_val || !d_x || !d_y || !d_w || !d_dot) {
         rsg::set_last_error("rsg_spmv_dot_noalloc: null pointer");
+        return RSG_EINVAL;
+    }
+    if (d_x == d_y || d_w == d_y) {   // x and w are read through the read-only path while y is written
+        rsg::set_last_error("rsg_spmv_dot_noalloc: d_y must not alias d_x or d_w");
         return RSG_EINVAL;
     }
     double* scratch = nullptr;

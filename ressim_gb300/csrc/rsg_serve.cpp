@@ -73,8 +73,8 @@ struct rsg_server {
     bool stop = false;
     std::vector<std::thread> workers;
     std::vector<rsg_solver*> handles, grid, bilu;   // per slot: the configured handle (batches of small requests), one
-                                                    // with the grid-wide sweeps (larger requests), a BILU0 handle for
-                                                    // patterns CPR cannot take
+                                                    // with the grid-wide sweeps (larger requests), and two BILU0 handles
+                                                    // (thread-block and grid-wide sweeps) for patterns CPR cannot take
     Clock::time_point t0 = Clock::now();      // the server's clock origin (start_ms / end_ms of the results)
 };
 
@@ -94,13 +94,16 @@ void run_request(rsg_server* S, int slot, Request& R) {
     if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
     if (rc == RSG_EINVAL && (prec == RSG_PREC_CPR || prec == RSG_PREC_CPR_DEVICE)) {   // CPR needs a structurally symmetric pattern: BILU0
         rsg_release(h);
-        if (!S->bilu[size_t(slot)]) {
+        const bool large = R.n > kBatchRows;                      // the grid-wide sweeps for a large request, as for CPR
+        rsg_solver*& fb = S->bilu[size_t(2 * slot + (large ? 1 : 0))];
+        if (!fb) {
             rsg_options o = S->opt;
             o.precond = RSG_PREC_BILU0;
-            rsg_create(&S->bilu[size_t(slot)], &o);
+            if (large) o.sweep = 2;
+            rsg_create(&fb, &o);
         }
-        if (S->bilu[size_t(slot)]) {
-            h = S->bilu[size_t(slot)];
+        if (fb) {
+            h = fb;
             prec = RSG_PREC_BILU0;
             rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
             if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
@@ -258,7 +261,7 @@ int rsg_server_create(rsg_server** out, const rsg_options* opts, int slots, size
     S->budget = mem_budget;
     S->handles.assign(size_t(slots), nullptr);
     S->grid.assign(size_t(slots), nullptr);
-    S->bilu.assign(size_t(slots), nullptr);
+    S->bilu.assign(size_t(2 * slots), nullptr);
     rsg_options og = S->opt;
     og.sweep = 2;
     for (int i = 0; i < slots; ++i) {

@@ -369,14 +369,15 @@ def spe10_like(day: int = 1, seed: int = 0, nx=60, ny=220, nz=85) -> NewtonSyste
                        channels=(35, 84, 4, 100.0), wells="corners+center", dt=float(day))
 
 
+def ensemble_member(r: int, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0, dt: float = 10.0):
+    """Realisation r of the ensemble: permeability seed seed0 + r and a seeded inactive fraction U[0.1, 0.5]."""
+    frac = float(np.random.default_rng(10_000 + seed0 + r).uniform(0.1, 0.5))
+    return make_system(nx, ny, nz, sigma=sigma, seed=seed0 + r, actnum_fraction=frac, wells="corners+center", dt=dt)
+
+
 def ensemble(n_real: int = 64, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0, dt: float = 10.0):
     """Realisations with their own permeability seed and a seeded inactive fraction U[0.1, 0.5]."""
-    out = []
-    for r in range(n_real):
-        frac = float(np.random.default_rng(10_000 + seed0 + r).uniform(0.1, 0.5))
-        out.append(make_system(nx, ny, nz, sigma=sigma, seed=seed0 + r, actnum_fraction=frac, wells="corners+center",
-                               dt=dt))
-    return out
+    return [ensemble_member(r, nx, ny, nz, sigma, seed0, dt) for r in range(n_real)]
 
 
 def serving_request(rng: np.random.Generator, cells_lo=1e3, cells_hi=1e6, max_cells=None) -> NewtonSystem:

@@ -10,10 +10,12 @@ oracle/Makefile.ref). Steps:
 2. Two small synthetic systems from ressim_gb300.synth (one with singular pivot blocks) are added.
 3. For every system the reference's own classes (through oracle/ref_shim.cpp, single thread) produce:
    BSR::spmv, BILU0 factors and apply, BILU0f apply, BlockCPR weights / AMG hierarchy / apply,
-   BiCGSTAB and GMRES(30) solves with BILU0 and CPR, the float-device emulation with double refinement,
-   and (dump) WellSchur reduce / recover.
+   BiCGSTAB, GMRES(30) and GMRES(60) solves with BILU0 and CPR (at 1e-6, and tight: 1e-10 for BiCGSTAB,
+   1e-12 for GMRES), the float-device emulation with double refinement, and (dump) WellSchur reduce / recover.
+   For the tight solves, the solution's movement under a change of inner-product summation order alone
+   (``sens_<case>``) is recorded: the GPU parity bound is max(1e-8, 10 sens).
 
-    python tests/golden/make_golden.py
+    RESSIM_REFERENCE=<reference repository root> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -32,16 +34,18 @@ from oracle import RefShim  # noqa: E402
 from ressim_gb300 import synth  # noqa: E402
 from ressim_gb300.bsr import BSR, read_dump, read_system  # noqa: E402
 
-REF = os.environ.get("RESSIM_REFERENCE", "/root/reference")
+REF = os.environ.get("RESSIM_REFERENCE", "")
 
 
 def build_ref():
+    if not REF or not os.path.isdir(os.path.join(REF, "engine", "src")):
+        sys.exit("set RESSIM_REFERENCE to the reference repository's root (its engine/src is compiled into oracle/_ref)")
     subprocess.run(["make", "-f", "oracle/Makefile.ref", "-j8", "REF=" + REF], cwd=ROOT, check=True, capture_output=True)
 
 
-def pairwise_bicgstab(A: BSR, lu, b, tol, maxit):
-    """BiCGSTAB with the oracle's SpMV and BILU0 but numpy's pairwise inner products: how far the solution moves
-    under a change of summation order alone (the sensitivity the GPU parity bound allows for)."""
+def pairwise_bicgstab(A: BSR, M, b, tol, maxit):
+    """BiCGSTAB with the oracle's SpMV and preconditioner ``M`` but numpy's pairwise inner products: how far the
+    solution moves under a change of summation order alone (the sensitivity the GPU parity bound allows for)."""
     from oracle import Oracle
     o = Oracle()
     n = b.size
@@ -51,17 +55,94 @@ def pairwise_bicgstab(A: BSR, lu, b, tol, maxit):
         rhoN = np.dot(rh, r)
         beta = (rhoN / rho) * (alpha / omega); rho = rhoN
         p = r + beta * (p - omega * v)
-        ph = o.bilu0_apply(A, lu, p); v = o.spmv(A, ph)
+        ph = M(p); v = o.spmv(A, ph)
         alpha = rho / np.dot(rh, v)
         s = r - alpha * v
         if np.sqrt(np.dot(s, s)) / bn < tol:
             return x + alpha * ph
-        sh = o.bilu0_apply(A, lu, s); t = o.spmv(A, sh)
+        sh = M(s); t = o.spmv(A, sh)
         omega = np.dot(t, s) / np.dot(t, t)
         x = x + alpha * ph + omega * sh; r = s - omega * t
         if np.sqrt(np.dot(r, r)) / bn < tol:
             return x
     return x
+
+
+def pairwise_gmres(A: BSR, M, b, tol, maxit, m):
+    """Flexible GMRES(m) with the oracle's SpMV and preconditioner and numpy's pairwise inner products (same
+    recurrence as engine/src/linsolve.cpp:218-273): the solution's sensitivity to the summation order."""
+    from oracle import Oracle
+    o = Oracle()
+    n = b.size
+    x = np.zeros(n)
+    bn = np.linalg.norm(b)
+    total = 0
+    while total < maxit:
+        r = b - o.spmv(A, x)
+        beta = np.linalg.norm(r)
+        if beta / bn < tol:
+            break
+        V = [r / beta]; Z = []
+        H = np.zeros((m + 1, m)); cs = np.zeros(m); sn = np.zeros(m); g = np.zeros(m + 1); g[0] = beta
+        j = 0
+        done = False
+        while j < m and total < maxit:
+            Z.append(M(V[j])); w = o.spmv(A, Z[j])
+            for i in range(j + 1):
+                H[i, j] = np.dot(w, V[i]); w = w - H[i, j] * V[i]
+            H[j + 1, j] = np.linalg.norm(w)
+            V.append(w / H[j + 1, j] if H[j + 1, j] > 0 else w)
+            for i in range(j):
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]; H[i, j] = t
+            den = np.hypot(H[j, j], H[j + 1, j])
+            cs[j] = H[j, j] / den if den > 0 else 1.0; sn[j] = H[j + 1, j] / den if den > 0 else 0.0
+            H[j, j] = den; H[j + 1, j] = 0.0
+            g[j + 1] = -sn[j] * g[j]; g[j] = cs[j] * g[j]
+            j += 1; total += 1
+            if abs(g[j]) / bn < tol:
+                done = True
+                break
+        y = np.zeros(j)
+        for i in range(j - 1, -1, -1):
+            y[i] = (g[i] - np.dot(H[i, i + 1:j], y[i + 1:j])) / H[i, i]
+        for i in range(j):
+            x = x + y[i] * Z[i]
+        if done:
+            break
+    return x
+
+
+def oracle_preconditioner(A: BSR, prec):
+    """The oracle's BILU0 (prec 0) or BlockCPR (prec 1) as a callable r -> z."""
+    from oracle import Oracle
+    o = Oracle()
+    if prec == 0:
+        lu, _ = o.bilu0_factor(A)
+        return lambda r: o.bilu0_apply(A, lu, r)
+    h = o.cpr_handle(A)
+    return h.apply
+
+
+# Krylov cases solved by the reference for every golden system. The tight ones pin the GPU solution within 1e-8
+# of the reference's own solution of the same method and preconditioner; GMRES runs to 1e-12 because its
+# solution at 1e-10 can still be 1e-8 away from the exact one (measured: 1.4e-8 on waterflood system 2).
+# GMRES(60) is the engine's fallback (engine/src/simulator.cpp:3390-3398).
+CASES = {
+    "bicg_bilu0": dict(prec=0, method=0, tol=1e-6, maxit=120),
+    "bicg_bilu0_tight": dict(prec=0, method=0, tol=1e-10, maxit=1000),
+    "gmres_bilu0": dict(prec=0, method=1, restart=30, tol=1e-6, maxit=300),
+    "bicg_cpr": dict(prec=1, method=0, tol=1e-6, maxit=120),
+    "gmres_cpr": dict(prec=1, method=1, restart=30, tol=1e-6, maxit=300),
+    "bicg_cpr_tight": dict(prec=1, method=0, tol=1e-10, maxit=500),
+    "gmres_bilu0_tight": dict(prec=0, method=1, restart=30, tol=1e-12, maxit=1000),
+    "gmres_cpr_tight": dict(prec=1, method=1, restart=30, tol=1e-12, maxit=500),
+    "gmres60_bilu0_tight": dict(prec=0, method=1, restart=60, tol=1e-12, maxit=1000),
+    "gmres60_cpr_tight": dict(prec=1, method=1, restart=60, tol=1e-12, maxit=500),
+}
+# cases whose summation-order sensitivity is recorded (sens_<case>)
+SENS_CASES = ("bicg_bilu0", "bicg_bilu0_tight", "bicg_cpr_tight", "gmres_bilu0_tight", "gmres_cpr_tight", "gmres60_bilu0_tight",
+              "gmres60_cpr_tight")
 
 
 def golden_for(R: RefShim, A: BSR, b, acc=None, with_factors=False, label=""):
@@ -92,24 +173,21 @@ def golden_for(R: RefShim, A: BSR, b, acc=None, with_factors=False, label=""):
     if acc is not None:
         out["z_cpr_acc"] = R.prec_apply(A, b, prec=1, acc=acc)
         out["cpr_w_acc"] = R.cpr_info(A, acc=acc)[0]
-    cases = {
-        "bicg_bilu0": dict(prec=0, method=0, tol=1e-6, maxit=120),
-        "bicg_bilu0_tight": dict(prec=0, method=0, tol=1e-10, maxit=1000),
-        "gmres_bilu0": dict(prec=0, method=1, restart=30, tol=1e-6, maxit=300),
-        "bicg_cpr": dict(prec=1, method=0, tol=1e-6, maxit=120),
-        "gmres_cpr": dict(prec=1, method=1, restart=30, tol=1e-6, maxit=300),
-    }
-    for k, c in cases.items():
+    for k, c in CASES.items():
         xs, conv, its, rr = R.solve(A, b, **c)
         out["x_" + k] = xs
         out["its_" + k] = its
         out["rr_" + k] = rr
         out["conv_" + k] = int(conv)
-        if c["prec"] == 0 and c["method"] == 0 and conv:
-            lu0, _ = R.bilu0_factor(A)
-            xp = pairwise_bicgstab(A, lu0, b, c["tol"], c["maxit"])
+        if k in SENS_CASES and conv:
+            M = oracle_preconditioner(A, c["prec"])
+            if c["method"] == 0:
+                xp = pairwise_bicgstab(A, M, b, c["tol"], c["maxit"])
+            else:
+                xp = pairwise_gmres(A, M, b, c["tol"], c["maxit"], c["restart"])
             out["sens_" + k] = np.linalg.norm(xp - xs) / np.linalg.norm(xs)
-        print(f"  {label:10s} {k:18s} conv {conv} its {its:4d} relres {rr:.3e}")
+        print(f"  {label:10s} {k:18s} conv {conv} its {its:4d} relres {rr:.3e}"
+              + (f" sens {float(out['sens_' + k]):.1e}" if "sens_" + k in out else ""))
     xr, conv, its, rr = R.refine_float(A, b, tol=1e-8, max_outer=6, inner_it=120)
     out["x_refine"] = xr
     out["its_refine"] = its

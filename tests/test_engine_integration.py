@@ -1,0 +1,123 @@
+"""The GPU solver inside the reference engine itself, through the engine's own solver hooks (include/rsg_ressim_adapter.hpp).
+
+The reference engine is compiled from its staged, unmodified sources (oracle/Makefile.ref: ``stage`` copies them into
+the git-ignored oracle/_ref/src; the GPU host compiles them for its own architecture) and linked with librsg.so:
+
+* oracle/ref_trajectory runs the 20x20x4 waterflood (6 report steps of 30 days) stock, and with
+  rsg::RsgGpuBlockSolver registered through ressim::setDistributedSolver (engine/src/simulator.cpp:3358-3367) or, in the
+  precision form, through ressim::setGpuBlockSolver inside the engine's FP64 refinement (:3368-3378). The Newton
+  trajectory -- time steps, Newton iterations per step, each Newton iteration's CNV and material-balance residuals
+  (printed by the engine, RESSIM_DEBUG) and the well rates, totals and field pressure of every step -- is compared
+  between the stock run and the GPU run on the same host.
+* the reference's own linear-solver benchmark tools/lsbench.cpp, compiled unmodified against include/ressim/blocksolve.h,
+  solves the engine's dump of a full Jacobian with well rows (tests/golden/waterflood_dump.npz, written in the
+  benchmark's file layout).
+
+Tolerances: rates, totals and pressures within 1e-6 relative; CNV / MB residuals equal as printed (4 significant
+digits) or within 1e-6; Newton iterations per step equal; linear iterations of the run within 3 %.
+"""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+
+pytestmark = pytest.mark.gpu
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+STAGED = os.path.join(REF, "src", "engine", "src", "simulator.cpp")
+
+
+@pytest.fixture(scope="module")
+def harness():
+    if not os.path.exists(STAGED):
+        pytest.skip("reference engine sources not staged (make -f oracle/Makefile.ref stage REF=...)")
+    jobs = str(max(2, os.cpu_count() or 2))
+    r = subprocess.run(["make", "-f", "oracle/Makefile.ref", "-j" + jobs, "sim", "oracle/_ref/lsbench"], cwd=ROOT, capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    return REF
+
+
+def run_traj(harness, mode, linear_solver, nsteps=6, days=30):
+    env = dict(os.environ, RESSIM_DEBUG="1", OMP_NUM_THREADS="1")
+    r = subprocess.run([os.path.join(harness, "ref_trajectory"), mode, str(linear_solver), str(nsteps), str(days)], capture_output=True,
+                       text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    steps = []
+    for line in r.stdout.splitlines():
+        if line.startswith("ts "):
+            f = line.split()
+            d = {f[i]: float(f[i + 1]) for i in range(2, len(f) - 1, 2)}
+            steps.append(d)
+        elif line.startswith("run "):
+            f = line.split()
+            run = {f[i]: int(f[i + 1]) for i in range(1, len(f) - 1, 2)}
+    newton = re.findall(r"\bit (\d+) cnv (\S+) mb (\S+)", r.stderr)
+    return steps, run, newton
+
+
+def same_residual(a: str, b: str) -> bool:
+    return a == b or abs(float(a) - float(b)) <= 1e-6
+
+
+@pytest.mark.parametrize("linear_solver", [0, 2], ids=["ilu0", "cpr"])
+def test_newton_trajectory_gpu_matches_stock(harness, linear_solver):
+    """linear_solver 0: ILU(0)-BiCGSTAB (the GPU solver with BILU0); 2: the engine's automatic choice, CPR-AMG at
+    1,600 cells (the GPU solver with CPR)."""
+    s_cpu, run_cpu, nw_cpu = run_traj(harness, "cpu", linear_solver)
+    s_gpu, run_gpu, nw_gpu = run_traj(harness, "gpu", linear_solver)
+    assert run_gpu["dd_solves"] > 0 and run_gpu["dd_fallbacks"] == 0      # every Newton system solved on the GPU
+    assert len(s_cpu) == len(s_gpu) and len(s_cpu) >= 6
+    for a, b in zip(s_cpu, s_gpu):
+        assert a["time"] == b["time"] and a["dt"] == b["dt"]
+        assert a["newton"] == b["newton"]
+        for k in ("fopr", "fwpr", "fwir", "fopt", "fwpt", "fwit", "fpr"):
+            assert abs(a[k] - b[k]) <= 1e-6 * max(abs(a[k]), 1e-12) + 1e-12, (k, a[k], b[k])
+    assert run_cpu["newton"] == run_gpu["newton"]
+    assert abs(run_cpu["linear"] - run_gpu["linear"]) <= 0.03 * run_cpu["linear"]
+    assert len(nw_cpu) == len(nw_gpu)
+    for (i1, c1, m1), (i2, c2, m2) in zip(nw_cpu, nw_gpu):
+        assert i1 == i2 and same_residual(c1, c2) and same_residual(m1, m2), ((i1, c1, m1), (i2, c2, m2))
+
+
+def test_stock_run_reproduces_golden_trajectory(harness):
+    """The reference compiled on this host reproduces the committed trajectory of the stock ILU(0) run."""
+    s, run, _ = run_traj(harness, "cpu", 0)
+    gold = [ln.split() for ln in open(os.path.join(ROOT, "tests", "golden", "waterflood_trajectory.txt")) if ln.startswith("step")]
+    assert run["newton"] == int(gold[-1][3]) and run["linear"] == int(gold[-1][5])
+    assert abs(s[-1]["fopt"] - float(gold[-1][7])) <= 1e-8 * float(gold[-1][7])
+    assert abs(s[-1]["fpr"] - float(gold[-1][9])) <= 1e-8 * float(gold[-1][9])
+
+
+def test_precision_form_inside_engine_refinement(harness):
+    """The precision form (FP32 preconditioner, FP64 Krylov) as the inner solver of the engine's FP64 defect
+    correction: every device solve is used (no fallback), and the run ends where the stock run ends."""
+    s_cpu, run_cpu, _ = run_traj(harness, "cpu", 2)
+    s_ref, run_ref, _ = run_traj(harness, "refine", 2)
+    assert run_ref["gpu_solves"] > 0 and run_ref["gpu_fallbacks"] == 0
+    assert len(s_cpu) == len(s_ref)
+    for k in ("fopt", "fwpt", "fwit", "fpr"):
+        assert abs(s_cpu[-1][k] - s_ref[-1][k]) <= 1e-4 * abs(s_cpu[-1][k]), k
+
+
+def test_lsbench_on_engine_dump(harness, tmp_path):
+    """tools/lsbench.cpp, unmodified, linked with the rsg adapters: the four block-solver variants (CPR with and
+    without wells in the pressure system, BILU0, CPR without accumulation blocks) on the engine's dump of a full
+    Jacobian (1,600 cells x 3 + 2 BHP rows) converge to the benchmark's tolerance."""
+    from ressim_gb300.bsr import ScalarCSR, write_lsbench
+    _, z = load_golden("waterflood_dump.npz")
+    path = str(tmp_path / "j0.lsb")
+    write_lsbench(path, ScalarCSR(z["J_rowPtr"], z["J_col"], z["J_val"]), z["J_rhs"], int(z["na"]), int(z["nv"]), int(z["nw"]),
+                  z["acc"])
+    r = subprocess.run([os.path.join(harness, "lsbench"), path, "new", "1e-6"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "n 4802 nnz 90770 cells 1600 nv 3 wells 2 acc 1" in r.stdout
+    rows = re.findall(r"NEW v(\d) \(cpr (\d) wellsP (\d)\): setup \S+ solve \S+ its (\d+) res (\S+) conv (\d) levels (\d+)", r.stdout)
+    assert len(rows) == 4, r.stdout
+    for v, cpr, wp, its, res, conv, levels in rows:
+        assert conv == "1" and float(res) <= 1e-6, r.stdout
+        assert (int(levels) > 0) == (cpr == "1")

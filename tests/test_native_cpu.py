@@ -116,21 +116,23 @@ def test_synth_manufactured_rhs():
     assert np.allclose(S.val, s.A.val, rtol=1e-12, atol=1e-12 * np.abs(s.A.val).max())
 
 
-def test_reference_tools_compile_against_the_adapters():
-    """The reference's own tools/lsbench.cpp compiles with the supplied ressim/blocksolve.h, and the GpuBlockSolver
-    adapter compiles against the engine's own headers (only where the reference tree exists)."""
+def test_reference_tools_build_against_the_adapters():
+    """The reference's own tools/lsbench.cpp compiles and links, unmodified, with the supplied ressim/blocksolve.h,
+    librsg.so and the reference solver objects, and the GpuBlockSolver adapter compiles against the engine's own
+    headers (where the reference engine's sources are staged in oracle/_ref/src)."""
     import shutil
     import subprocess
-    ref = os.environ.get("RESSIM_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "engine", "include")) or not shutil.which("g++"):
-        pytest.skip("reference tree not present on this host")
-    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ref, "engine", "include")]
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", *inc, os.path.join(ref, "tools", "lsbench.cpp")],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
+    src = os.path.join(ROOT, "oracle", "_ref", "src")
+    if not os.path.isdir(os.path.join(src, "engine", "include")) or not shutil.which("g++"):
+        pytest.skip("reference engine sources not staged on this host")
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(src, "engine", "include")]
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", *inc, "-x", "c++", os.path.join(ROOT, "include", "rsg_ressim_adapter.hpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+    if not os.path.exists(os.path.join(ROOT, "ressim_gb300", "librsg.so")):
+        pytest.skip("librsg.so not built")
+    r = subprocess.run(["make", "-f", "oracle/Makefile.ref", "-j4", "oracle/_ref/lsbench"], cwd=ROOT, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
 
 
 @pytest.mark.parametrize("name", GOLDEN_SYSTEMS)

@@ -63,6 +63,11 @@ CASES = {
     "gmres_bilu0": dict(prec=0, method=1, restart=30, tol=1e-6, maxit=300),
     "bicg_cpr": dict(prec=1, method=0, tol=1e-6, maxit=120),
     "gmres_cpr": dict(prec=1, method=1, restart=30, tol=1e-6, maxit=300),
+    "bicg_cpr_tight": dict(prec=1, method=0, tol=1e-10, maxit=500),
+    "gmres_bilu0_tight": dict(prec=0, method=1, restart=30, tol=1e-12, maxit=1000),
+    "gmres_cpr_tight": dict(prec=1, method=1, restart=30, tol=1e-12, maxit=500),
+    "gmres60_bilu0_tight": dict(prec=0, method=1, restart=60, tol=1e-12, maxit=1000),
+    "gmres60_cpr_tight": dict(prec=1, method=1, restart=60, tol=1e-12, maxit=500),
 }
 
 
