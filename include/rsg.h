@@ -73,6 +73,12 @@ typedef struct rsg_options {
                                rounded products and sums, bit for bit (engine/src/bsr.cpp:109-117) */
     int sweep_inflight;     /* sync-free grid sweeps (BILU0, factorisation, Gauss-Seidel): levels in flight, which sizes
                                the persistent grid; 0 = auto (the full grid) */
+    int autotune;           /* 1 (default): the launch shapes left at 0 below are chosen by timing the candidates on the
+                               system at its first set-up (cached per pattern for the life of the process); 0: their
+                               defaults. Every shape gives the same results bit for bit. */
+    int vcycle_fused;       /* split CPR: 1 = its grid-wide passes as the phases of one cooperative kernel (grid barriers
+                               between them), 2 = one launch per pass; 0 = tuned (default 1) */
+    int cpr2_threads;       /* split CPR: threads per system of the BILU0 stage, 256 or 512; 0 = tuned (default 256) */
 } rsg_options;
 
 typedef struct rsg_stats {
@@ -131,6 +137,16 @@ int rsg_solve(rsg_solver* h, const double* b, double* x, double tol, int maxIt, 
 /* Same with device-resident vectors (b, x: device pointers of n*nb float64 on the handle's device). */
 int rsg_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres);
 
+/* FP64 iterative refinement (defect correction) around this handle's solver, per system of the batch, with host
+ * vectors: x = 0, r = b; while ||r|| / ||b|| > tol and at most maxOuter times, solve A d = r with the handle's
+ * preconditioned Krylov method (typically the RSG_MIXED_F32 precision form) to innerTol = clamp(10 tol, 1e-4, 1e-2) in at
+ * most innerIt iterations, then x += d and r = b - A x, the SpMV, residual and norms in FP64 on the device. Iterations
+ * (rsg_batch_results) are the sums of the inner iterations; the residual reported is the final FP64 one.
+ * Returns RSG_OK when every system is within tol, RSG_ENOTCONV otherwise.
+ * Replaces: refineWithDevice (engine/src/bsr.cpp:1373-1396) with this handle as its inner device solver. */
+int rsg_solve_refined(rsg_solver* h, const double* b, double* x, double tol, int maxOuter, int innerIt, int* iterations,
+                      double* relres);
+
 /* Per-system results of the last (batched) solve: its[nsys], relres[nsys] (host arrays, may be NULL). */
 int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relres);
 /* Per system of the last solve: RSG_OK (converged), RSG_ENOTCONV or RSG_EBREAKDOWN. */
@@ -180,6 +196,11 @@ int rsg_spmv_dot_noalloc(int n, int nb, const int* d_rowPtr, const int* d_col, c
 
 /* Statistics of the last setup / solve. */
 int rsg_get_stats(rsg_solver* h, rsg_stats* st);
+
+/* The launch shapes in use after rsg_setup and how they were chosen, as text ("vcycle_fused=1 cpr2_threads=512
+ * source=tuned ..." with the timed candidates), written NUL-terminated into buf (at most len bytes). No counterpart in
+ * the reference, whose device kernels have fixed 64-thread groups (app/src/gpu_compute.cpp:57-80). */
+int rsg_tuning(rsg_solver* h, char* buf, int len);
 
 /* Handle's CUDA stream (cudaStream_t as void*), for callers that order their own work with it. */
 void* rsg_stream(rsg_solver* h);

@@ -1,7 +1,10 @@
 // Newton-trajectory harness (test infrastructure): the reference black-oil simulator on the 20x20x4 waterflood
 // (oracle/ref_case.hpp), either stock or with this repository's GPU solver in the engine's own solver hooks.
 //
-//   ref_trajectory MODE LINEAR_SOLVER NSTEPS STEP_DAYS
+//   ref_trajectory MODE LINEAR_SOLVER NSTEPS STEP_DAYS [qimpes]
+//
+// qimpes: CPR with quasi-IMPES weights (tuning.cprWeights = 0) instead of the engine's default true-IMPES weights,
+// which need the accumulation blocks that the GpuBlockSolver hook does not pass on (engine/include/ressim/bsr.h:147).
 //
 // MODE
 //   cpu      the stock run: the engine's own CPU solver (ILU(0)- or CPR-BiCGSTAB, GMRES(60) fallback)
@@ -31,13 +34,14 @@ using namespace ressim;
 
 int main(int argc, char** argv) {
     if (argc < 5) {
-        std::fprintf(stderr, "usage: ref_trajectory cpu|gpu|refine LINEAR_SOLVER NSTEPS STEP_DAYS\n");
+        std::fprintf(stderr, "usage: ref_trajectory cpu|gpu|refine LINEAR_SOLVER NSTEPS STEP_DAYS [qimpes]\n");
         return 1;
     }
     const std::string mode = argv[1];
     const int linearSolver = std::atoi(argv[2]), nsteps = std::atoi(argv[3]);
     const double stepDays = std::atof(argv[4]);
     Case c = rsgref::waterfloodCase(nsteps, stepDays, linearSolver);
+    if (argc > 5 && std::strcmp(argv[5], "qimpes") == 0) c.tuning.cprWeights = 0;
 
     std::unique_ptr<rsg::RsgGpuBlockSolver> dev;
     if (mode == "gpu") {

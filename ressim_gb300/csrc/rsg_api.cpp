@@ -8,7 +8,9 @@
 #include <numeric>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -129,11 +131,20 @@ struct rsg_solver {
     int gmKind = -1;
     double* xPrev = nullptr;
     KScal* ksPrev = nullptr;
+    // FP64 defect correction (rsg_solve_refined): level-space b, accumulated x, residual, per-system relative residual
+    double *refB = nullptr, *refX = nullptr, *refR = nullptr, *refRel = nullptr;
     // results
     rsg_stats st{};
     long long launches = 0;
     std::vector<KScal> hks;
     std::vector<double> htrue;
+    // launch shapes (every choice gives the same results bit for bit) and how they were chosen
+    struct Tune {
+        bool fused = true;
+        int cpr2Threads = 256;
+        std::string desc = "defaults";
+    } tune;
+    unsigned long long patHash = 0;   // FNV-1a of the plan's pattern (0: not computed)
     std::mutex mu;
 };
 
@@ -146,6 +157,7 @@ void free_plan(rsg_solver* h) {
     drop_gm_graphs(h);
     h->gmExec.clear();
     h->gm = GmState{}; h->gmKind = -1; h->xPrev = nullptr; h->ksPrev = nullptr;
+    h->refB = h->refX = h->refR = h->refRel = nullptr;
     h->pmem.release_all();
     h->dp = DevPlan{};
     h->val = nullptr; h->lu = nullptr; h->luf = nullptr; h->work = nullptr; h->dinv = nullptr;
@@ -275,6 +287,8 @@ PrecDev prec_dev(rsg_solver* h) {
         M.s64 = h->s64;
         M.s32 = h->s32;
         M.split = M.cpr && h->splitCpr;
+        M.fused = M.split && h->tune.fused;
+        M.cpr2Threads = h->tune.cpr2Threads;
     }
     return M;
 }
@@ -677,6 +691,14 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
         (rc = dalloc(M, &G.r, size_t(rows))) || (rc = dalloc(M, &G.xf, size_t(rows))) || (rc = dalloc(M, &G.bf, size_t(rows))) ||
         (rc = dalloc(M, &G.rf, size_t(rows))))
         return rc;
+    // the fused V-cycle's phase table and barrier counter (the split CPR form)
+    {
+        std::vector<VPhase> ph;
+        vcycle_phases(G, ph);
+        G.nPhases = int(ph.size());
+        G.coarseChunks = std::max(1, (G.maxCoarse + 255) / 256);
+        if (!ph.empty() && ((rc = upload(M, &G.phases, ph, st)) || (rc = dalloc(M, &G.vbar, 1)))) return rc;
+    }
     h->amgLevels = maxL;
     return RSG_OK;
 }
@@ -753,6 +775,121 @@ int setup_cpr(rsg_solver* h, const double* acc) {
     return RSG_OK;
 }
 
+int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
+    const PrecDev M = prec_dev(h);
+    if (M.devcpr) h->launches += launch_devcpr(h->dp, h->amg, h->val, 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream);
+    else if (M.cpr && M.cta && !M.split) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
+    else if (M.cpr) h->launches += launch_cpr_grid(h->dp, M, *M.amg, 0, d_r, nullptr, nullptr, d_z, nullptr, h->S, h->d_err, h->stream);
+    else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
+    else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
+    else if (M.kind == 1) { launch_ilu_apply_mixed(h->dp, h->luf, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
+    else if (M.kind == 3) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.yt, h->S, h->d_err, h->stream); h->launches += 2; }
+    else { launch_block_jacobi_apply(h->dp, h->dinv, d_r, d_z, h->stream); h->launches += 1; }
+    RSG_CUDA(cudaGetLastError());
+    return RSG_OK;
+}
+
+// ---- launch-shape autotuner. The candidates are timed on the handle's own system right after its first set-up
+// (CUDA events on its stream, the preconditioner applied to a zero vector: the same work as any other), the fastest
+// is kept and cached per (pattern, options) for the life of the process. Every candidate computes the same values
+// bit for bit, so the choice changes time only.
+unsigned long long pattern_hash(rsg_solver* h) {
+    if (h->patHash) return h->patHash;
+    unsigned long long x = 1469598103934665603ULL;
+    auto mix = [&x](const std::vector<int>& v) {
+        x ^= (unsigned long long)v.size() + 0x9e3779b97f4a7c15ULL;
+        x *= 1099511628211ULL;
+        for (int q : v) { x ^= (unsigned long long)(unsigned)q; x *= 1099511628211ULL; }
+    };
+    mix(h->plan.rowPtr0);
+    mix(h->plan.col0);
+    mix(h->plan.sysRow0);
+    h->patHash = x ? x : 1;
+    return h->patHash;
+}
+
+std::mutex g_tune_mu;
+std::map<std::pair<unsigned long long, int>, rsg_solver::Tune> g_tune_cache;
+
+// true when one fused application can be captured into a CUDA graph on this device (a cooperative kernel node)
+bool fused_capturable(rsg_solver* h, const double* d_r, double* d_z) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return false; }
+    precond_apply_dev(h, d_r, d_z);
+    const cudaError_t e1 = cudaStreamEndCapture(h->stream, &g);
+    bool ok = e1 == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return ok;
+}
+
+int tune_shapes(rsg_solver* h) {
+    rsg_solver::Tune t;
+    const bool split = h->opt.precond == RSG_PREC_CPR && h->cta && h->splitCpr && h->haveAmg && h->amg.nPhases > 0;
+    t.fused = h->opt.vcycle_fused != 2;
+    t.cpr2Threads = h->opt.cpr2_threads ? h->opt.cpr2_threads : 256;
+    const bool free_fused = h->opt.vcycle_fused == 0, free_thr = h->opt.cpr2_threads == 0;
+    if (!split) { t.desc = "no split CPR: fixed shapes"; h->tune = t; return RSG_OK; }
+    if (!h->opt.autotune || (!free_fused && !free_thr)) {
+        t.desc = std::string("vcycle_fused=") + (t.fused ? "1" : "2") + " cpr2_threads=" + std::to_string(t.cpr2Threads) +
+                 (h->opt.autotune ? " source=options" : " source=defaults");
+        h->tune = t;
+        return RSG_OK;
+    }
+    const int key2 = h->opt.precision * 1000 + h->opt.vcycle_fused * 10000 + h->opt.cpr2_threads + h->device * 100000;
+    const auto key = std::make_pair(pattern_hash(h), key2);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) { h->tune = it->second; return RSG_OK; }
+    }
+    const size_t N = size_t(h->plan.n) * NB;
+    RSG_CUDA(cudaMemsetAsync(h->tmp, 0, N * sizeof(double), h->stream));
+    std::vector<rsg_solver::Tune> cand;
+    for (int f : {1, 0})
+        for (int thr : {256, 512}) {
+            if (!free_fused && (f != 0) != t.fused) continue;
+            if (!free_thr && thr != t.cpr2Threads) continue;
+            rsg_solver::Tune c;
+            c.fused = f != 0;
+            c.cpr2Threads = thr;
+            cand.push_back(c);
+        }
+    bool fusedOk = true;
+    float best = 1e30f;
+    rsg_solver::Tune pick = cand.front();
+    std::string timings;
+    for (const auto& c : cand) {
+        if (c.fused && !fusedOk) continue;
+        h->tune = c;
+        int rc = precond_apply_dev(h, h->tmp, h->xout);        // warm-up (first launch of the shape)
+        if (rc == RSG_OK && c.fused && !fused_capturable(h, h->tmp, h->xout)) { fusedOk = false; continue; }
+        if (rc) return rc;
+        RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
+        for (int k = 0; k < 3; ++k)
+            if ((rc = precond_apply_dev(h, h->tmp, h->xout))) return rc;
+        RSG_CUDA(cudaEventRecord(h->ev1, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        ms /= 3;
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), "%s%s/%d %.3f ms", timings.empty() ? "" : ", ", c.fused ? "fused" : "launches", c.cpr2Threads, ms);
+        timings += buf;
+        if (ms < best) { best = ms; pick = c; }
+    }
+    const int rce = check_device_errors(h);
+    if (rce) return rce;
+    pick.desc = std::string("vcycle_fused=") + (pick.fused ? "1" : "2") + " cpr2_threads=" + std::to_string(pick.cpr2Threads) +
+                " source=tuned (CPR application: " + timings + (fusedOk ? "" : "; fused kernel not capturable here") + ")";
+    h->tune = pick;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = pick;
+    return RSG_OK;
+}
+
 int do_setup(rsg_solver* h, const double* acc) {
     if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
     h->escalated = false;
@@ -791,7 +928,7 @@ int do_setup(rsg_solver* h, const double* acc) {
     h->st.regularised_blocks = h->h_pin[2];
     h->st.amg_levels = amgPrec ? h->amgLevels : 0;
     h->haveSetup = true;
-    return RSG_OK;
+    return tune_shapes(h);
 }
 
 int launch_iterations(rsg_solver* h, int k) {
@@ -1016,6 +1153,103 @@ int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, i
     return RSG_ENOTCONV;
 }
 
+// FP64 defect correction around the handle's own solver (refineWithDevice, engine/src/bsr.cpp:1373-1396), per system
+// of the batch: x = 0, r = b; up to maxOuter times, while ||r|| / ||b|| > tol, solve A d = r with the handle's solver
+// to innerTol = clamp(10 tol, 1e-4, 1e-2) and at most innerIt iterations, x += d, r = b - A x (FP64 SpMV and norms on
+// the device). A system already within the tolerance gets a zero right-hand side, so its correction is exactly zero.
+// Iterations are the sum of the inner iterations; a system converges when its final FP64 residual is within tol.
+int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxOuter, int innerIt, int* iterations,
+                     double* relres) {
+    if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
+    if (!(tol > 0) || maxOuter < 0 || innerIt < 0) return fail(RSG_EINVAL, "tol must be > 0, maxOuter and innerIt >= 0");
+    const size_t N = size_t(h->plan.n) * NB;
+    const int ns = h->plan.nsys;
+    int rc;
+    if (!h->refB && ((rc = dalloc(h->pmem, &h->refB, N)) || (rc = dalloc(h->pmem, &h->refX, N)) || (rc = dalloc(h->pmem, &h->refR, N)) ||
+                     (rc = dalloc(h->pmem, &h->refRel, size_t(ns)))))
+        return rc;
+    RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
+    launch_gather_vec(h->dp, d_b, h->refB, h->stream);
+    RSG_CUDA(cudaMemsetAsync(h->refX, 0, N * sizeof(double), h->stream));
+    h->launches += 1;
+    const double innerTol = std::max(1e-4, std::min(1e-2, tol * 10));
+    std::vector<int> its(size_t(ns), 0);
+    std::vector<double> rel(size_t(ns), 0.0);
+    std::vector<KScal> k(static_cast<size_t>(ns));
+    int escalatedMax = 0;
+    for (int outer = 0;; ++outer) {
+        // r = b - A x and ||r|| / ||b|| per system (0 for a zero right-hand side, which is converged)
+        launch_true_residual(h->dp, h->val, h->refB, h->refX, h->refR, h->R, h->refRel, h->stream);
+        h->launches += 1;
+        RSG_CUDA(cudaGetLastError());
+        RSG_CUDA(cudaMemcpyAsync(rel.data(), h->refRel, sizeof(double) * rel.size(), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        bool any = false;
+        for (int sy = 0; sy < ns; ++sy) {
+            if (rel[size_t(sy)] <= tol) {
+                const size_t r0 = size_t(h->plan.sysRow0[size_t(sy)]) * NB, r1 = size_t(h->plan.sysRow0[size_t(sy) + 1]) * NB;
+                RSG_CUDA(cudaMemsetAsync(h->refR + r0, 0, (r1 - r0) * sizeof(double), h->stream));
+            } else {
+                any = true;
+            }
+        }
+        if (!any || outer >= maxOuter) break;
+        double* bSave = h->b;
+        h->b = h->refR;
+        rc = run_bicgstab(h, innerTol, innerIt);
+        if (!rc && h->opt.precision == RSG_MIXED_F32 && h->opt.precond != RSG_PREC_CPR_DEVICE && h->opt.precond != RSG_PREC_JACOBI &&
+            !h->escalated)
+            rc = escalate(h, innerTol, innerIt);
+        h->b = bSave;
+        if (rc) return rc;
+        escalatedMax = std::max(escalatedMax, h->st.escalated_systems);
+        RSG_CUDA(cudaMemcpyAsync(k.data(), h->ks, sizeof(KScal) * k.size(), cudaMemcpyDeviceToHost, h->stream));
+        launch_vec_add(h->plan.n, h->refX, h->V.x, h->stream);
+        h->launches += 1;
+        RSG_CUDA(cudaGetLastError());
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        for (int sy = 0; sy < ns; ++sy)
+            if (rel[size_t(sy)] > tol) its[size_t(sy)] += k[size_t(sy)].its;
+    }
+    // results as the plain solve reports them: per system its, relres and status in the device scalars
+    RSG_CUDA(cudaMemcpyAsync(k.data(), h->ks, sizeof(KScal) * k.size(), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    for (int sy = 0; sy < ns; ++sy) {
+        KScal& q = k[size_t(sy)];
+        q.its = its[size_t(sy)];
+        q.relres = rel[size_t(sy)];
+        q.status = rel[size_t(sy)] <= tol ? ST_CONV : ST_MAXIT;
+    }
+    RSG_CUDA(cudaMemcpyAsync(h->ks, k.data(), sizeof(KScal) * k.size(), cudaMemcpyHostToDevice, h->stream));
+    launch_scatter_vec(h->dp, h->refX, d_x, h->stream);
+    RSG_CUDA(cudaEventRecord(h->ev1, h->stream));
+    RSG_CUDA(cudaMemcpyAsync(h->d_trueres, h->refRel, sizeof(double) * size_t(ns), cudaMemcpyDeviceToDevice, h->stream));
+    h->launches += 1;
+    RSG_CUDA(cudaGetLastError());
+    if ((rc = check_device_errors(h))) return rc;
+    h->hks = k;
+    h->htrue = rel;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    int maxits = 0, conv = 1;
+    double mrel = 0;
+    for (int sy = 0; sy < ns; ++sy) {
+        maxits = std::max(maxits, its[size_t(sy)]);
+        mrel = std::max(mrel, rel[size_t(sy)]);
+        conv &= rel[size_t(sy)] <= tol;
+    }
+    h->st.iterations = maxits;
+    h->st.converged = conv;
+    h->st.rel_residual = mrel;
+    h->st.true_rel_residual = mrel;
+    h->st.solve_ms = ms;
+    h->st.escalated_systems = escalatedMax;
+    h->st.device_bytes = h->mem.bytes + h->pmem.bytes;
+    if (iterations) *iterations = maxits;
+    if (relres) *relres = mrel;
+    return conv ? RSG_OK : RSG_ENOTCONV;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1037,6 +1271,9 @@ void rsg_default_options(rsg_options* o) {
     o->device = 0;
     o->mem_budget = 0;
     o->sweep = 0;
+    o->autotune = 1;
+    o->vcycle_fused = 0;
+    o->cpr2_threads = 0;
 }
 
 int rsg_create(rsg_solver** out, const rsg_options* opts) {
@@ -1047,6 +1284,8 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     if (opts) o = *opts;
     if (o.precond < 0 || o.precond > 4 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 3)
         return fail(RSG_EINVAL, "invalid options");
+    if (o.vcycle_fused < 0 || o.vcycle_fused > 2 || (o.cpr2_threads != 0 && o.cpr2_threads != 256 && o.cpr2_threads != 512))
+        return fail(RSG_EINVAL, "invalid launch shape options (vcycle_fused 0..2, cpr2_threads 0 / 256 / 512)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
     if (o.device < 0 || o.device >= ndev) return fail(RSG_EINVAL, "device ordinal out of range");
@@ -1146,6 +1385,20 @@ int rsg_solve(rsg_solver* h, const double* b, double* x, double tol, int maxIt, 
     return rc;
 }
 
+int rsg_solve_refined(rsg_solver* h, const double* b, double* x, double tol, int maxOuter, int innerIt, int* iterations, double* relres) {
+    if (!h || !b || !x) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->havePlan) return fail(RSG_ESTATE, "solve before set_matrix");
+    const size_t N = size_t(h->plan.n) * NB;
+    RSG_CUDA(cudaMemcpyAsync(h->tmp, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const int rc = do_solve_refined(h, h->tmp, h->xout, tol, maxOuter, innerIt, iterations, relres);
+    if (rc < 0) return rc;
+    RSG_CUDA(cudaMemcpyAsync(x, h->xout, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    return rc;
+}
+
 int rsg_batch_results(rsg_solver* h, int* its, double* relres, double* true_relres) {
     if (!h) return fail(RSG_EINVAL, "null handle");
     for (size_t s = 0; s < h->hks.size(); ++s) {
@@ -1222,19 +1475,6 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
 }
 
 // level-space r -> level-space z
-static int precond_apply_dev(rsg_solver* h, const double* d_r, double* d_z) {
-    const PrecDev M = prec_dev(h);
-    if (M.devcpr) h->launches += launch_devcpr(h->dp, h->amg, h->val, 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream);
-    else if (M.cpr && M.cta && !M.split) { launch_cpr_cta(h->dp, M, *M.amg, 0, M.kind != 0, d_r, nullptr, nullptr, d_z, nullptr, h->stream); h->launches += 1; }
-    else if (M.cpr) h->launches += launch_cpr_grid(h->dp, M, *M.amg, 0, d_r, nullptr, nullptr, d_z, nullptr, h->S, h->d_err, h->stream);
-    else if (M.cta) { launch_ilu_cta_apply(h->dp, M, d_r, d_z, h->stream); h->launches += 1; }
-    else if (M.kind == 0) { launch_ilu_apply_f64(h->dp, h->lu, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
-    else if (M.kind == 1) { launch_ilu_apply_mixed(h->dp, h->luf, d_r, d_z, h->S, h->d_err, h->stream); h->launches += 2; }
-    else if (M.kind == 3) { launch_ilu_apply_f32(h->dp, h->luf, d_r, d_z, h->V.yt, h->S, h->d_err, h->stream); h->launches += 2; }
-    else { launch_block_jacobi_apply(h->dp, h->dinv, d_r, d_z, h->stream); h->launches += 1; }
-    RSG_CUDA(cudaGetLastError());
-    return RSG_OK;
-}
 
 int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z) {
     if (!h || !d_r || !d_z) return fail(RSG_EINVAL, "null argument");
@@ -1296,6 +1536,13 @@ int rsg_get_factors(rsg_solver* h, double* lu) {
     }
     for (size_t p = 0; p < size_t(h->plan.nnzb); ++p)   // back to the caller's block order
         std::memcpy(lu + size_t(h->plan.valSrc[p]) * NB2, lev.data() + p * NB2, sizeof(double) * NB2);
+    return RSG_OK;
+}
+
+int rsg_tuning(rsg_solver* h, char* buf, int len) {
+    if (!h || !buf || len < 1) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    std::snprintf(buf, size_t(len), "%s", h->tune.desc.c_str());
     return RSG_OK;
 }
 

@@ -124,6 +124,13 @@ struct AmgSysLv {
     int locOff = 0;                    // offset of the level's rows inside the system's V-cycle vectors
     int mc = 0;                        // Gauss-Seidel schedule: 0 forward levels (reference order), 1 colours
 };
+// One phase of the fused V-cycle kernel (the split CPR application in one cooperative launch): the pass it runs
+// over every system of the batch and that pass's row ranges and switches (rsg_sweep_cta.cu: vcycle_phases).
+enum : int { VP_IN = 0, VP_COLOUR = 1, VP_TAIL = 2, VP_GSGRID = 3, VP_RESID = 4, VP_RESTRICT = 5, VP_COARSE = 6, VP_PROLONG = 7,
+             VP_TSP = 8 };
+struct VPhase {
+    int kind, a, b, c, d, e, f, g;
+};
 constexpr int AMG_W0 = 8;              // V-cycle row slots on the finest level (7-point pressure matrix)
 constexpr int AMG_W1 = 16;             // on the Galerkin levels
 struct DevAmg {
@@ -193,7 +200,15 @@ struct DevAmg {
     std::vector<int> colTail;
     std::vector<int> gsBlocks;         // host: persistent grid of the sync-free Gauss-Seidel sweeps of each level
     bool posOrder = false;             // host: in every row the entries before the diagonal are exactly its earlier-wave neighbours
+    // fused V-cycle (split form): the phase table of one application, its grid-barrier counter, and the number of
+    // chunks the coarsest explicit-inverse products split into (0: no table; hierarchies with Gauss-Seidel coarsest levels)
+    VPhase* phases = nullptr;
+    int nPhases = 0;
+    unsigned* vbar = nullptr;
+    int coarseChunks = 1;
 };
+// phase table of the fused V-cycle for a built hierarchy (empty when the fused kernel does not apply)
+void vcycle_phases(const DevAmg& G, std::vector<VPhase>& out);
 // blocks of 4 warps for a sync-free sweep that keeps `inflight` of its levels (avgRows rows each) in flight
 int sweep_blocks_for(double avgRows, int inflight);
 // CPR set-up kernels (rsg_cpr.cu)
@@ -294,6 +309,8 @@ void launch_ilu_apply_mixed(const DevPlan& P, const float* luf, const double* r,
 void launch_ilu_grid_ks(const DevPlan& P, const PrecDev& M, const double* r, double* z, const KScal* ks, SweepState& S, int* err,
                         cudaStream_t st);
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st);
+// x += d over n block rows (3 values each)
+void launch_vec_add(int n, double* x, const double* d, cudaStream_t st);
 // raise (never lower) a kernel's dynamic shared-memory opt-in on the current device; thread-safe
 void raise_smem_limit(const void* fn, int bytes);
 // block-Jacobi: dinv = inverse diagonal blocks (FP64), z = dinv r
@@ -327,6 +344,8 @@ struct PrecDev {
     bool devcpr = false;              // the reference's GPU-shaped float CPR-AMG
     bool split = false;               // CPR with cta: V-cycle and second-stage input grid-wide (all systems at once),
                                       // the BILU0 sweeps one thread block per system
+    bool fused = false;               // split CPR: the grid-wide passes as the phases of one cooperative kernel
+    int cpr2Threads = 256;            // split CPR: threads per block of the BILU0 stage (256 or 512; same results)
     const DevAmg* amg = nullptr;
 };
 // all-FP32 factorisation (FP32 elimination, FP64 pivot inversion), one thread block per system

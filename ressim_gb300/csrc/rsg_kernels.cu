@@ -17,6 +17,7 @@
 #include "rsg_sync.cuh"
 
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -809,6 +810,15 @@ void raise_smem_limit(const void* fn, int bytes) {
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         cur = bytes;
     }
+}
+
+__global__ void k_vec_add(size_t m, double* x, const double* __restrict__ d) {
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < m; q += size_t(gridDim.x) * blockDim.x) x[q] += d[q];
+}
+void launch_vec_add(int n, double* x, const double* d, cudaStream_t st) {
+    const size_t m = size_t(n) * 3;
+    const int g = int(std::min<size_t>((m + 255) / 256, size_t(device_sm_count()) * 8));
+    k_vec_add<<<std::max(g, 1), 256, 0, st>>>(m, x, d);
 }
 
 void launch_spmv_f64(const DevPlan& P, const double* val, const double* x, double* y, cudaStream_t st) {

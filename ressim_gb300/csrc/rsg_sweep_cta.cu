@@ -788,6 +788,18 @@ __device__ __noinline__ void coarse_inverse(const AmgSysLv& A, const CprArgs<flo
     }
     __syncthreads();
 }
+// the same product for the rows [k0, min(k1, m)) only (no block barrier: rows are independent)
+__device__ __noinline__ void coarse_inverse_rows(const AmgSysLv& A, const CprArgs<float>& C, float* x, const float* b, int k0, int k1) {
+    const int m = A.n;
+    const float* inv = C.inv + A.luOff;
+    for (int k = k0 + int(threadIdx.x); k < min(k1, m); k += blockDim.x) {
+        const float* col = inv + k;
+        float acc = 0.f;
+#pragma unroll 32
+        for (int j = 0; j < m; ++j) acc = fmaf(__ldg(col + size_t(j) * m), b[j], acc);
+        x[k] = acc;
+    }
+}
 
 // FP32 forms, systems flagged at set-up: the coarsest level in FP64 (dense LU, as the FP64 form), from and back to
 // the FP32 V-cycle vectors
@@ -1334,7 +1346,7 @@ int grid_for(long long n, int threads) {
 // level-0 right-hand side b0 = w . input (bsr.cpp:1064-1067; TT: the arithmetic of the restriction, FP32 in the
 // all-FP32 form)
 template <int MODE, class TA, class TT, class TS>
-__global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ rowSys, const double* r, double* pv, const double* v,
+__device__ __forceinline__ void gcpr_in_body(int n, const int* __restrict__ rowSys, const double* r, double* pv, const double* v,
                                                  const double* __restrict__ w, TS* T, TA* b0, const KScal* ks) {
     for (int k = int(blockIdx.x * blockDim.x + threadIdx.x); k < n; k += int(gridDim.x * blockDim.x)) {
         double beta = 0, omega = 0, alpha = 0;
@@ -1357,6 +1369,11 @@ __global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ 
         else b0[k] = TA(da(da(dm(w0, in[0]), dm(w1, in[1])), dm(w2, in[2])));
     }
 }
+template <int MODE, class TA, class TT, class TS>
+__global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ rowSys, const double* r, double* pv, const double* v,
+                                                 const double* __restrict__ w, TS* T, TA* b0, const KScal* ks) {
+    gcpr_in_body<MODE, TA, TT, TS>(n, rowSys, r, pv, v, w, T, b0, ks);
+}
 
 // one Gauss-Seidel sweep of level l over every system (engine/src/amg.cpp:98-113). Positions [q0, q1) of the
 // level's schedule, claimed forward or backward. phase 0: the smoothing sweeps (systems whose level l is the
@@ -1364,7 +1381,7 @@ __global__ void __launch_bounds__(256) k_gcpr_in(int n, const int* __restrict__ 
 // x = 0 (the terms of the neighbours not yet updated vanish and are not read). Flags of skipped rows are set all
 // the same: after every forward sweep of a (level, phase) all its flags are 1, after every backward sweep 0.
 template <class TA, bool FWD, bool ZERO, bool POS>
-__global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int maxL, int phase, const int* __restrict__ rowLv,
+__device__ __forceinline__ void gs_grid_body(int q0, int q1, int maxL, int phase, const int* __restrict__ rowLv,
                                                           const AmgSysLv* __restrict__ lv, const int* __restrict__ gsRows,
                                                           const int* __restrict__ wave, const int* __restrict__ rp,
                                                           const int* __restrict__ ci, const TA* __restrict__ val,
@@ -1431,6 +1448,15 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int ma
         }
     }
 }
+template <class TA, bool FWD, bool ZERO, bool POS>
+__global__ void __launch_bounds__(kGridThreads) k_gs_grid(int q0, int q1, int maxL, int phase, const int* __restrict__ rowLv,
+                                                          const AmgSysLv* __restrict__ lv, const int* __restrict__ gsRows,
+                                                          const int* __restrict__ wave, const int* __restrict__ rp,
+                                                          const int* __restrict__ ci, const TA* __restrict__ val,
+                                                          const int* __restrict__ diag, const TA* b, TA* x, int* flag, unsigned* ctr,
+                                                          const KScal* ks, int* err) {
+    gs_grid_body<TA, FWD, ZERO, POS>(q0, q1, maxL, phase, rowLv, lv, gsRows, wave, rp, ci, val, diag, b, x, flag, ctr, ks, err);
+}
 
 // Multicolour Gauss-Seidel (FP32 forms) on the colour-major row descriptors {row, first entry, end, diagonal}:
 // the rows of a colour are independent. ZERO: pre-smoothing from x = 0 (the terms of later colours vanish and are
@@ -1467,7 +1493,7 @@ __device__ __forceinline__ void gs_colour_row(const int4 d, const int* __restric
 }
 // one large colour: a parallel pass over the descriptors [i0, i1)
 template <class TA, bool ZERO>
-__global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, const int4* __restrict__ cdesc, const int* __restrict__ gci,
+__device__ __forceinline__ void gs_colour_body(int i0, int i1, int maxL, const int4* __restrict__ cdesc, const int* __restrict__ gci,
                                                    const TA* __restrict__ val, const int* __restrict__ wave, const int* __restrict__ rowLv,
                                                    const TA* b, TA* x, const KScal* ks) {
     for (int i = i0 + int(blockIdx.x * blockDim.x + threadIdx.x); i < i1; i += int(gridDim.x * blockDim.x)) {
@@ -1475,6 +1501,12 @@ __global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, con
         if (ks && ks[__ldg(rowLv + d.x) / maxL].status != ST_RUNNING) continue;
         gs_colour_row<TA, ZERO>(d, gci, val, wave, b, x);
     }
+}
+template <class TA, bool ZERO>
+__global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, const int4* __restrict__ cdesc, const int* __restrict__ gci,
+                                                   const TA* __restrict__ val, const int* __restrict__ wave, const int* __restrict__ rowLv,
+                                                   const TA* b, TA* x, const KScal* ks) {
+    gs_colour_body<TA, ZERO>(i0, i1, maxL, cdesc, gci, val, wave, rowLv, b, x, ks);
 }
 // The small colours (from colour `tail` on) of a level in one sync-free pass. Their rows are the long rows of the
 // well cliques, so a warp takes one row: rows are claimed in colour order (forward ascending, backward
@@ -1484,7 +1516,7 @@ __global__ void __launch_bounds__(256) k_gs_colour(int i0, int i1, int maxL, con
 // their values are final or old as the multicolour order wants. Flags: 1 after the forward pass, 0 after the
 // backward one; bounded waits (ERR_TIMEOUT).
 template <class TA, bool FWD, bool ZERO>
-__global__ void __launch_bounds__(kGridThreads) k_gs_tail(int i0, int i1, int tail, int maxL, const int4* __restrict__ cdesc,
+__device__ __forceinline__ void gs_tail_body(int i0, int i1, int tail, int maxL, const int4* __restrict__ cdesc,
                                                           const int* __restrict__ gci, const TA* __restrict__ val,
                                                           const int* __restrict__ wave, const int* __restrict__ rowLv, const TA* b, TA* x,
                                                           int* flag, unsigned* ctr, const KScal* ks, int* err) {
@@ -1555,11 +1587,18 @@ __global__ void __launch_bounds__(kGridThreads) k_gs_tail(int i0, int i1, int ta
         if (lane == 0) st_release(flag + d.x, want);
     }
 }
+template <class TA, bool FWD, bool ZERO>
+__global__ void __launch_bounds__(kGridThreads) k_gs_tail(int i0, int i1, int tail, int maxL, const int4* __restrict__ cdesc,
+                                                          const int* __restrict__ gci, const TA* __restrict__ val,
+                                                          const int* __restrict__ wave, const int* __restrict__ rowLv, const TA* b, TA* x,
+                                                          int* flag, unsigned* ctr, const KScal* ks, int* err) {
+    gs_tail_body<TA, FWD, ZERO>(i0, i1, tail, maxL, cdesc, gci, val, wave, rowLv, b, x, flag, ctr, ks, err);
+}
 
 // r = b - A x on the rows [q0, q1) of one level of every system (engine/src/amg.cpp:321-322: the row sum from
 // zero in entry order, the diagonal at its place); rows of a system's coarsest level are skipped
 template <class TA>
-__global__ void __launch_bounds__(256) k_gcpr_resid(int q0, int q1, int maxL, const int* __restrict__ rowLv,
+__device__ __forceinline__ void gcpr_resid_body(int q0, int q1, int maxL, const int* __restrict__ rowLv,
                                                     const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
                                                     const int* __restrict__ ci, const TA* __restrict__ val, const TA* b, const TA* x, TA* r,
                                                     const KScal* ks) {
@@ -1592,11 +1631,18 @@ __global__ void __launch_bounds__(256) k_gcpr_resid(int q0, int q1, int maxL, co
         r[g] = asub(b[g], acc);
     }
 }
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_resid(int q0, int q1, int maxL, const int* __restrict__ rowLv,
+                                                    const AmgSysLv* __restrict__ lv, const int* __restrict__ rp,
+                                                    const int* __restrict__ ci, const TA* __restrict__ val, const TA* b, const TA* x, TA* r,
+                                                    const KScal* ks) {
+    gcpr_resid_body<TA>(q0, q1, maxL, rowLv, lv, rp, ci, val, b, x, r, ks);
+}
 
 // restriction b_{l+1} = R r for the coarse rows [c0, c1) of every system: members in ascending natural order
 // (engine/src/amg.cpp:324)
 template <class TA>
-__global__ void __launch_bounds__(256) k_gcpr_restrict(int c0, int c1, int maxL, const int* __restrict__ rowLv,
+__device__ __forceinline__ void gcpr_restrict_body(int c0, int c1, int maxL, const int* __restrict__ rowLv,
                                                        const AmgSysLv* __restrict__ lv, const int* __restrict__ memPtr,
                                                        const int* __restrict__ mem, TA* b, const TA* r, const KScal* ks) {
     for (int c = c0 + int(blockIdx.x * blockDim.x + threadIdx.x); c < c1; c += int(gridDim.x * blockDim.x)) {
@@ -1621,10 +1667,16 @@ __global__ void __launch_bounds__(256) k_gcpr_restrict(int c0, int c1, int maxL,
         b[c] = t;
     }
 }
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_restrict(int c0, int c1, int maxL, const int* __restrict__ rowLv,
+                                                       const AmgSysLv* __restrict__ lv, const int* __restrict__ memPtr,
+                                                       const int* __restrict__ mem, TA* b, const TA* r, const KScal* ks) {
+    gcpr_restrict_body<TA>(c0, c1, maxL, rowLv, lv, memPtr, mem, b, r, ks);
+}
 
 // x_l += P x_{l+1} (injection of the aggregate's value, engine/src/amg.cpp:326) on the rows [q0, q1) of level l
 template <class TA>
-__global__ void __launch_bounds__(256) k_gcpr_prolong(int q0, int q1, int maxL, const int* __restrict__ rowLv,
+__device__ __forceinline__ void gcpr_prolong_body(int q0, int q1, int maxL, const int* __restrict__ rowLv,
                                                       const AmgSysLv* __restrict__ lv, const int* __restrict__ agg, TA* x,
                                                       const KScal* ks) {
     for (int g = q0 + int(blockIdx.x * blockDim.x + threadIdx.x); g < q1; g += int(gridDim.x * blockDim.x)) {
@@ -1633,28 +1685,46 @@ __global__ void __launch_bounds__(256) k_gcpr_prolong(int q0, int q1, int maxL, 
         x[g] = aadd(x[g], x[__ldg(&lv[sl + 1].rowOff) + __ldg(agg + g)]);
     }
 }
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_prolong(int q0, int q1, int maxL, const int* __restrict__ rowLv,
+                                                      const AmgSysLv* __restrict__ lv, const int* __restrict__ agg, TA* x,
+                                                      const KScal* ks) {
+    gcpr_prolong_body<TA>(q0, q1, maxL, rowLv, lv, agg, x, ks);
+}
 
 // coarsest level of every system: dense LU (FP64) or explicit inverse (FP32 forms); without a dense LU, x = 0
 // before the symmetric GS sweeps of phase 1
 template <class TA>
-__global__ void __launch_bounds__(256) k_gcpr_coarse(CprArgs<TA> C, const KScal* ks) {
-    const int s = blockIdx.x;
-    if (ks && ks[s].status != ST_RUNNING) return;
-    int nlev = 0;
-    while (nlev < C.maxL && C.lv[s * C.maxL + nlev].n > 0) ++nlev;
-    if (nlev == 0) return;
-    const AmgSysLv A = C.lv[s * C.maxL + nlev - 1];
-    TA* x = C.x + A.rowOff;
-    if (A.dense) {
-        if constexpr (sizeof(TA) == 4) {
-            if (C.coarse64[s]) coarse_fp64(A, C, x, C.b + A.rowOff);
-            else coarse_inverse(A, C, x, C.b + A.rowOff);
-        } else {
-            coarse_dense<TA, 256>(A, C, x, C.b + A.rowOff, C.r + A.rowOff);
+__device__ __forceinline__ void gcpr_coarse_body(CprArgs<TA> C, const KScal* ks, int nsys, int chunks) {
+    // work items (system, chunk): with chunks > 1 the rows of an explicit FP32 inverse product are split over several
+    // blocks in chunks of blockDim rows (each row's sum is the same whichever block takes it); the LU solves and the
+    // FP64 fallback stay with the chunk-0 block of their system
+    for (int item = blockIdx.x; item < nsys * chunks; item += gridDim.x) {
+        const int s = item / chunks, c = item - s * chunks;
+        if (ks && ks[s].status != ST_RUNNING) continue;                  // uniform over the block
+        int nlev = 0;
+        while (nlev < C.maxL && C.lv[s * C.maxL + nlev].n > 0) ++nlev;
+        if (nlev == 0) continue;
+        const AmgSysLv A = C.lv[s * C.maxL + nlev - 1];
+        TA* x = C.x + A.rowOff;
+        if (A.dense) {
+            if constexpr (sizeof(TA) == 4) {
+                if (C.coarse64[s]) {
+                    if (c == 0) coarse_fp64(A, C, x, C.b + A.rowOff);
+                } else {
+                    coarse_inverse_rows(A, C, x, C.b + A.rowOff, c * int(blockDim.x), chunks > 1 ? (c + 1) * int(blockDim.x) : A.n);
+                }
+            } else if (c == 0) {
+                coarse_dense<TA, 256>(A, C, x, C.b + A.rowOff, C.r + A.rowOff);
+            }
+        } else if (c == 0) {
+            for (int k = threadIdx.x; k < A.n; k += blockDim.x) x[k] = TA(0);
         }
-    } else {
-        for (int k = threadIdx.x; k < A.n; k += blockDim.x) x[k] = TA(0);
     }
+}
+template <class TA>
+__global__ void __launch_bounds__(256) k_gcpr_coarse(CprArgs<TA> C, const KScal* ks) {
+    gcpr_coarse_body<TA>(C, ks, int(gridDim.x), 1);
 }
 
 // t = input - S[:,p] xp (pressure column of every block in row order, bsr.cpp:1071-1081), in place in T
@@ -1690,7 +1760,7 @@ __global__ void __launch_bounds__(256) k_gcpr_zp(int n, const int* __restrict__ 
 // split form, second-stage input: t = T - S[:,p] xp in the thread-block kernel's slot order and arithmetic
 // (bsr.cpp:1071-1081), one row per thread over every system; xp = the level-0 V-cycle solution of the row's system
 template <class TA, class TV>
-__global__ void __launch_bounds__(256) k_gcpr_tsp(int n, const int* __restrict__ rowSys, const int* __restrict__ sysRow0, int maxL,
+__device__ __forceinline__ void gcpr_tsp_body(int n, const int* __restrict__ rowSys, const int* __restrict__ sysRow0, int maxL,
                                                   const AmgSysLv* __restrict__ lv, const int4* __restrict__ Lslot,
                                                   const int4* __restrict__ Uslot, const int* __restrict__ LovCol,
                                                   const int* __restrict__ UovCol, const TA* __restrict__ sp, const TA* __restrict__ spLov,
@@ -1714,6 +1784,130 @@ __global__ void __launch_bounds__(256) k_gcpr_tsp(int n, const int* __restrict__
             if (slot_col(uc, j) >= 0) sub_p(acc, spr + 3 * (SLOTS + 1 + j), TV(xp[slot_col(uc, j)]));
         if (uc.w >= 0) ov_sub_p(acc, UovCol, spUov, uc.w, xp);
         T[size_t(k) * 3] = acc[0]; T[size_t(k) * 3 + 1] = acc[1]; T[size_t(k) * 3 + 2] = acc[2];
+    }
+}
+template <class TA, class TV>
+__global__ void __launch_bounds__(256) k_gcpr_tsp(int n, const int* __restrict__ rowSys, const int* __restrict__ sysRow0, int maxL,
+                                                  const AmgSysLv* __restrict__ lv, const int4* __restrict__ Lslot,
+                                                  const int4* __restrict__ Uslot, const int* __restrict__ LovCol,
+                                                  const int* __restrict__ UovCol, const TA* __restrict__ sp, const TA* __restrict__ spLov,
+                                                  const TA* __restrict__ spUov, const TA* x, TV* T, const KScal* ks) {
+    gcpr_tsp_body<TA, TV>(n, rowSys, sysRow0, maxL, lv, Lslot, Uslot, LovCol, UovCol, sp, spLov, spUov, x, T, ks);
+}
+
+// ------------------------------------------------------------------ fused V-cycle: the split form's grid passes in one launch
+// The passes above are short and latency-bound (a few dependent loads per row), so as separate launches each costs
+// its launch and ramp-up as much as its work. Here one cooperative launch runs them as phases of a persistent kernel:
+// every block executes phase after phase over the same row ranges with the same bodies (so every value is the one
+// the separate launches compute, bit for bit), separated by grid barriers. The barrier is a counter: each block
+// arrives once per barrier and waits until all blocks of the launch have arrived -- the cooperative launch
+// guarantees that they are all resident -- with a bounded wait (ERR_TIMEOUT, then the kernel runs on and the host
+// reports the error).
+template <class TA, class TT>
+struct VcArgs {
+    CprArgs<TA> C;
+    int n, nsys, maxL, totRows;
+    const int *rowSys, *sysRow0;
+    const double *r, *v;
+    double* pv;
+    TT* T;
+    const int *rowLv, *gsRows, *wave, *rp, *ci, *diag, *gci, *agg;
+    const AmgSysLv* lv;
+    const int4* cdesc;
+    const TA* val;
+    int* gsFlag;
+    unsigned* gsCtr;
+    const int4 *Lslot, *Uslot;
+    const int *LovCol, *UovCol;
+    int coarseChunks;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void grid_barrier(unsigned* bar, unsigned& target, int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        target += gridDim.x;
+        __threadfence();
+        atomicAdd(bar, 1u);
+        unsigned ns = 0;
+        for (unsigned it = 0; ld_acquire_u32(bar) < target; ++it) {
+            if (it >= 64) {
+                __nanosleep(ns);
+                ns = ns < 32 ? 32 : (ns < 256 ? 2 * ns : 256);
+                if (it >= 64 + kSpinLimit) { atomicOr(err, ERR_TIMEOUT); break; }
+                if ((it & 255u) == 255u && *(volatile int*)err != 0) break;
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+template <class TA, class TT, bool POS>
+__global__ void __launch_bounds__(256, 4) k_vcycle(const VPhase* __restrict__ ph, int nph, int mode, VcArgs<TA, TT> A, const KScal* ks,
+                                                unsigned* bar, int* err) {
+    unsigned target = 0;
+    for (int i = 0; i < nph; ++i) {
+        const VPhase f = ph[i];
+        switch (f.kind) {
+        case VP_IN:
+            if (mode == IN_PUPDATE) gcpr_in_body<IN_PUPDATE, TA, TT, TT>(A.n, A.rowSys, A.r, A.pv, A.v, A.C.w, A.T, A.C.b, ks);
+            else if (mode == IN_SUPDATE) gcpr_in_body<IN_SUPDATE, TA, TT, TT>(A.n, A.rowSys, A.r, A.pv, A.v, A.C.w, A.T, A.C.b, ks);
+            else gcpr_in_body<IN_PLAIN, TA, TT, TT>(A.n, A.rowSys, A.r, A.pv, A.v, A.C.w, A.T, A.C.b, ks);
+            break;
+        case VP_COLOUR:
+            if (f.c) gs_colour_body<TA, true>(f.a, f.b, A.maxL, A.cdesc, A.gci, A.val, A.wave, A.rowLv, A.C.b, A.C.x, ks);
+            else gs_colour_body<TA, false>(f.a, f.b, A.maxL, A.cdesc, A.gci, A.val, A.wave, A.rowLv, A.C.b, A.C.x, ks);
+            break;
+        case VP_TAIL: {
+            unsigned* ctr = A.gsCtr + 4 * f.d;
+            if (f.e && f.f)
+                gs_tail_body<TA, true, true>(f.a, f.b, f.c, A.maxL, A.cdesc, A.gci, A.val, A.wave, A.rowLv, A.C.b, A.C.x, A.gsFlag, ctr, ks, err);
+            else if (f.e)
+                gs_tail_body<TA, true, false>(f.a, f.b, f.c, A.maxL, A.cdesc, A.gci, A.val, A.wave, A.rowLv, A.C.b, A.C.x, A.gsFlag, ctr, ks, err);
+            else
+                gs_tail_body<TA, false, false>(f.a, f.b, f.c, A.maxL, A.cdesc, A.gci, A.val, A.wave, A.rowLv, A.C.b, A.C.x, A.gsFlag, ctr, ks,
+                                               err);
+            break;
+        }
+        case VP_GSGRID: {
+            int* flag = A.gsFlag + size_t(f.d) * size_t(A.totRows);
+            unsigned* ctr = A.gsCtr + 4 * f.c + 2 * f.d;
+            if (f.e && f.f)
+                gs_grid_body<TA, true, true, POS>(f.a, f.b, A.maxL, f.d, A.rowLv, A.lv, A.gsRows, A.wave, A.rp, A.ci, A.val, A.diag, A.C.b, A.C.x,
+                                                  flag, ctr, ks, err);
+            else if (f.e)
+                gs_grid_body<TA, true, false, POS>(f.a, f.b, A.maxL, f.d, A.rowLv, A.lv, A.gsRows, A.wave, A.rp, A.ci, A.val, A.diag, A.C.b,
+                                                   A.C.x, flag, ctr, ks, err);
+            else
+                gs_grid_body<TA, false, false, POS>(f.a, f.b, A.maxL, f.d, A.rowLv, A.lv, A.gsRows, A.wave, A.rp, A.ci, A.val, A.diag, A.C.b,
+                                                    A.C.x, flag, ctr, ks, err);
+            break;
+        }
+        case VP_RESID:
+            gcpr_resid_body<TA>(f.a, f.b, A.maxL, A.rowLv, A.lv, A.rp, A.ci, A.val, A.C.b, A.C.x, A.C.r, ks);
+            break;
+        case VP_RESTRICT:
+            gcpr_restrict_body<TA>(f.a, f.b, A.maxL, A.rowLv, A.lv, A.C.memPtr, A.C.mem, A.C.b, A.C.r, ks);
+            break;
+        case VP_COARSE:
+            gcpr_coarse_body<TA>(A.C, ks, A.nsys, A.coarseChunks);
+            break;
+        case VP_PROLONG:
+            gcpr_prolong_body<TA>(f.a, f.b, A.maxL, A.rowLv, A.lv, A.agg, A.C.x, ks);
+            break;
+        case VP_TSP:
+            gcpr_tsp_body<TA, TT>(A.n, A.rowSys, A.sysRow0, A.maxL, A.lv, A.Lslot, A.Uslot, A.LovCol, A.UovCol, A.C.sp, A.C.spLov, A.C.spUov,
+                                  A.C.x, A.T, ks);
+            break;
+        default:
+            break;
+        }
+        if (i + 1 < nph) grid_barrier(bar, target, err);
     }
 }
 
@@ -1742,6 +1936,58 @@ __global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const 
     }
 }
 
+// second stage of the split form: TF = TA (FP64 factors in the FP64 form, FP32 otherwise), TV = TT; 256 or 512 threads
+// per system (every row is swept by one thread in the same arithmetic either way)
+template <class TF, class TV, class TA, int NT>
+void launch_cpr2_nt(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, const TV* T, double* z, TV* yglob,
+                    const KScal* ks, cudaStream_t st) {
+    IluArgs<TF> F;
+    if constexpr (sizeof(TF) == 8) F = ilu_args(P, M.s64);
+    else F = ilu_args(P, M.s32);
+    raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<TF, TV, TA, NT>), int(M.smem));
+    k_cpr2_cta<TF, TV, TA, NT><<<P.nsys, NT, M.smem, st>>>(F, G.maxL, G.lv, C.x, T, z, yglob, M.smem, ks);
+}
+template <class TA, class TT>
+void launch_cpr2(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, TT* Tsplit, double* z, const KScal* ks,
+                 cudaStream_t st) {
+    const bool wide = M.cpr2Threads >= 512;
+    if constexpr (sizeof(TA) == 8) {
+        if (wide) launch_cpr2_nt<double, double, TA, 512>(P, M, G, C, Tsplit, z, z, ks, st);
+        else launch_cpr2_nt<double, double, TA, 256>(P, M, G, C, Tsplit, z, z, ks, st);
+    } else if constexpr (sizeof(TT) == 8) {
+        if (wide) launch_cpr2_nt<float, double, TA, 512>(P, M, G, C, Tsplit, z, z, ks, st);
+        else launch_cpr2_nt<float, double, TA, 256>(P, M, G, C, Tsplit, z, z, ks, st);
+    } else {
+        if (wide) launch_cpr2_nt<float, float, TA, 512>(P, M, G, C, Tsplit, z, M.y32, ks, st);
+        else launch_cpr2_nt<float, float, TA, 256>(P, M, G, C, Tsplit, z, M.y32, ks, st);
+    }
+}
+
+// the fused V-cycle as one cooperative launch: as many blocks as can be resident at once (queried once per kernel)
+template <class TA, class TT, bool POS>
+void launch_vcycle(const DevAmg& G, const VcArgs<TA, TT>& A, int mode, const KScal* ks, int* err, cudaStream_t st) {
+    static int perSm[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& nb = perSm[dev & 63];
+    if (nb == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_vcycle<TA, TT, POS>, 256, 0);
+        nb = b > 0 ? b : 1;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(nb * device_sm_count()));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_vcycle<TA, TT, POS>, (const VPhase*)G.phases, G.nPhases, mode, A, ks, G.vbar, err);
+}
+
 template <class TA, class TT>
 int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, const TA* val, int mode, const double* r,
              double* pv, const double* v, double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st) {
@@ -1750,6 +1996,18 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
     // the split form keeps t in the second stage's sweep type (TT: FP32 in the all-FP32 form), as the thread-block
     // kernel does
     TT* Tsplit = reinterpret_cast<TT*>(G.T);
+    if (M.split && M.fused && G.nPhases > 0) {
+        // the whole pass sequence (input .. t) as the phases of one cooperative launch, then the BILU0 stage
+        VcArgs<TA, TT> A{C, n, P.nsys, G.maxL, G.totRows, P.rowSys, P.sysRow0, r, v, pv, Tsplit, G.rowLv, G.gsRows, G.wave, G.rp, G.ci,
+                         G.diag, G.gci, G.agg, G.lv, G.cdesc, val, G.gsFlag, G.gsCtr, P.Lslot, P.Uslot, P.LovCol, P.UovCol,
+                         G.coarseChunks};
+        cudaMemsetAsync(G.vbar, 0, sizeof(unsigned), st);
+        if (G.posOrder) launch_vcycle<TA, TT, true>(G, A, mode, ks, err, st);
+        else launch_vcycle<TA, TT, false>(G, A, mode, ks, err, st);
+        launches += 1;
+        launch_cpr2<TA, TT>(P, M, G, C, Tsplit, z, ks, st);
+        return launches + 1;
+    }
     if (M.split) {
         if (mode == IN_PUPDATE) k_gcpr_in<IN_PUPDATE, TA, TT, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, Tsplit, C.b, ks);
         else if (mode == IN_SUPDATE) k_gcpr_in<IN_SUPDATE, TA, TT, TT><<<gn, 256, 0, st>>>(n, P.rowSys, r, pv, v, G.w, Tsplit, C.b, ks);
@@ -1844,23 +2102,7 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
     if (M.split) {
         k_gcpr_tsp<TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, P.sysRow0, G.maxL, G.lv, P.Lslot, P.Uslot, P.LovCol, P.UovCol, C.sp, C.spLov,
                                               C.spUov, C.x, Tsplit, ks);
-        // second stage: TF = TA (FP64 factors in the FP64 form, FP32 otherwise), TV = TT
-        if constexpr (sizeof(TA) == 8) {
-            const IluArgs<double> F = ilu_args(P, M.s64);
-            raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<double, double, TA>), int(M.smem));
-            k_cpr2_cta<double, double, TA><<<P.nsys, cta_threads<double, double>(), M.smem, st>>>(F, G.maxL, G.lv, C.x, Tsplit, z, z,
-                                                                                                  M.smem, ks);
-        } else if constexpr (sizeof(TT) == 8) {
-            const IluArgs<float> F = ilu_args(P, M.s32);
-            raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<float, double, TA>), int(M.smem));
-            k_cpr2_cta<float, double, TA><<<P.nsys, cta_threads<float, double>(), M.smem, st>>>(F, G.maxL, G.lv, C.x, Tsplit, z, z,
-                                                                                                M.smem, ks);
-        } else {
-            const IluArgs<float> F = ilu_args(P, M.s32);
-            raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<float, float, TA>), int(M.smem));
-            k_cpr2_cta<float, float, TA><<<P.nsys, cta_threads<float, float>(), M.smem, st>>>(F, G.maxL, G.lv, C.x, Tsplit, z, M.y32,
-                                                                                              M.smem, ks);
-        }
+        launch_cpr2<TA, TT>(P, M, G, C, Tsplit, z, ks, st);
         return launches + 2;
     }
     k_gcpr_t<TA, TT><<<gn, 256, 0, st>>>(n, P.rowSys, P.rowPtr, P.col, M.val, C.x, G.T, ks);
@@ -1870,6 +2112,43 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
 }
 
 }  // namespace
+
+void vcycle_phases(const DevAmg& G, std::vector<VPhase>& out) {
+    out.clear();
+    if (!G.coarseGsLevels.empty() || G.maxL < 1) return;        // coarsest levels smoothed 20 times: separate launches
+    const auto& LB = G.levelRowBeg;
+    out.push_back(VPhase{VP_IN, 0, 0, 0, 0, 0, 0, 0});
+    auto sweep = [&](int l, bool fwd, bool zero) {
+        const std::vector<int>& cb = G.colBeg[size_t(l)];
+        if (cb.size() > 1) {                                  // multicolour: large colours one phase each, the tail in one
+            const int nc = int(cb.size()) - 1, tail = G.colTail[size_t(l)];
+            auto big = [&](int c) { out.push_back(VPhase{VP_COLOUR, cb[size_t(c)], cb[size_t(c) + 1], zero ? 1 : 0, 0, 0, 0, 0}); };
+            auto small = [&]() {
+                if (tail < nc) out.push_back(VPhase{VP_TAIL, cb[size_t(tail)], cb[size_t(nc)], tail, l, fwd ? 1 : 0, zero ? 1 : 0, 0});
+            };
+            if (fwd) {
+                for (int c = 0; c < tail; ++c) big(c);
+                small();
+            } else {
+                small();
+                for (int c = tail - 1; c >= 0; --c) big(c);
+            }
+        } else {
+            out.push_back(VPhase{VP_GSGRID, LB[size_t(l)], LB[size_t(l) + 1], l, 0, fwd ? 1 : 0, zero ? 1 : 0, 0});
+        }
+    };
+    for (int l = 0; l + 1 < G.maxL; ++l) {
+        sweep(l, true, true);
+        out.push_back(VPhase{VP_RESID, LB[size_t(l)], LB[size_t(l) + 1], 0, 0, 0, 0, 0});
+        out.push_back(VPhase{VP_RESTRICT, LB[size_t(l) + 1], LB[size_t(l) + 2], 0, 0, 0, 0, 0});
+    }
+    out.push_back(VPhase{VP_COARSE, 0, 0, 0, 0, 0, 0, 0});
+    for (int l = G.maxL - 2; l >= 0; --l) {
+        out.push_back(VPhase{VP_PROLONG, LB[size_t(l)], LB[size_t(l) + 1], 0, 0, 0, 0, 0});
+        sweep(l, false, false);
+    }
+    out.push_back(VPhase{VP_TSP, 0, 0, 0, 0, 0, 0, 0});
+}
 
 int launch_cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, int mode, const double* r, double* pv, const double* v,
                     double* z, const KScal* ks, SweepState& S, int* err, cudaStream_t st) {

@@ -37,7 +37,7 @@ class DeviceSolver:
     def __init__(self, precond: str = "bilu0", krylov: str = "bicgstab", precision: str = "fp64", restart: int = 40,
                  check_every: int = 4, use_graphs: bool = True, device: int = 0, mem_budget: int = 0,
                  gmres_fallback: bool = False, sweep: str = "auto", fma: bool = True,
-                 sweep_inflight: int = 0):
+                 sweep_inflight: int = 0, autotune: bool = True, vcycle_fused: int = 0, cpr2_threads: int = 0):
         self.L = _lib.load()
         o = _lib.Options()
         self.L.rsg_default_options(C.byref(o))
@@ -53,6 +53,9 @@ class DeviceSolver:
         o.fma = 1 if fma else 0
         o.sweep = _lib.SWEEP[sweep]
         o.sweep_inflight = sweep_inflight
+        o.autotune = 1 if autotune else 0
+        o.vcycle_fused = vcycle_fused
+        o.cpr2_threads = cpr2_threads
         self.opts = o
         h = C.c_void_p()
         _lib.check(self.L.rsg_create(C.byref(h), C.byref(o)))
@@ -112,12 +115,30 @@ class DeviceSolver:
         st = self.stats()
         return x, LinResult(rc == 0, its.value, rr.value, st.true_rel_residual, rc)
 
+    def solve_refined(self, b, tol: float = 1e-8, max_outer: int = 6, inner_it: int = 120):
+        """FP64 defect correction around this solver (the engine's refineWithDevice, engine/src/bsr.cpp:1373-1396):
+        inner solves to clamp(10 tol, 1e-4, 1e-2), x += d, r = b - A x in FP64, at most ``max_outer`` passes."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if self.n and b.size != self.n:
+            raise ValueError(f"b has {b.size} entries, the system has {self.n}")
+        x = np.zeros(max(self.n, b.size))
+        its, rr = C.c_int(0), C.c_double(0)
+        rc = _lib.check(self.L.rsg_solve_refined(self.h, _lib.ptr(b), _lib.ptr(x), tol, max_outer, inner_it, C.byref(its), C.byref(rr)))
+        st = self.stats()
+        return x, LinResult(rc == 0, its.value, rr.value, st.true_rel_residual, rc)
+
     def solve_device(self, d_b: int, d_x: int, tol: float = 1e-6, maxit: int = 120):
         """Device pointers (e.g. torch ``data_ptr()``) of n float64 entries."""
         its, rr = C.c_int(0), C.c_double(0)
         rc = _lib.check(self.L.rsg_solve_device(self.h, C.c_void_p(d_b), C.c_void_p(d_x), tol, maxit, C.byref(its), C.byref(rr)))
         st = self.stats()
         return LinResult(rc == 0, its.value, rr.value, st.true_rel_residual, rc)
+
+    def tuning(self) -> str:
+        """Launch shapes in use after set-up and how they were chosen (rsg_tuning)."""
+        buf = C.create_string_buffer(1024)
+        _lib.check(self.L.rsg_tuning(self.h, buf, 1024))
+        return buf.value.decode()
 
     def batch_results(self):
         its = np.zeros(self.nsys, dtype=np.int32)

@@ -596,13 +596,15 @@ def test_gmres_cpr_matches_reference(name, sweep):
     assert true_res(A, x, z["b"]) <= 1e-5
 
 
-@pytest.mark.parametrize("name", GOLDEN_SYSTEMS + ["singular_pivots.npz"])
+@pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
 @pytest.mark.parametrize("case,prec,restart,maxit", [("gmres_bilu0_tight", "bilu0", 30, 1000), ("gmres_cpr_tight", "cpr", 30, 500),
                                                      ("gmres60_bilu0_tight", "bilu0", 60, 1000), ("gmres60_cpr_tight", "cpr", 60, 500)])
 def test_gmres_tight_matches_reference(name, case, prec, restart, maxit):
     """GMRES(30) (the one-large-system configuration) and GMRES(60) (the engine's fallback,
     engine/src/simulator.cpp:3390-3398), BILU0 and CPR, to 1e-12: the GPU solution within 1e-8 of the reference's
-    own solution of the same method, at the reference's iteration count within +-1."""
+    own solution of the same method, at the reference's iteration count within +-1. (The near-singular system is left
+    out: there the reference's own GMRES stops on its recursive residual at a true residual of order 0.1, so neither
+    solution is meaningful at 1e-12.)"""
     A, z = load_golden(name)
     if not bool(z["conv_" + case]):
         pytest.skip("the reference does not converge on this case")
@@ -752,3 +754,86 @@ def test_headline_ensemble_precision_form_error(headline_systems):
         assert e32 < max(10 * e64, 1e-5), (e32, e64)
         assert e32 < 5e-3
         off += N
+
+
+# ---------------------------------------------------------------- FP64 defect correction (refineWithDevice)
+@pytest.mark.parametrize("precond", ["bilu0", "cpr"])
+@pytest.mark.parametrize("name", GOLDEN_SYSTEMS)
+def test_refined_solve_matches_reference_refinement(name, precond):
+    """rsg_solve_refined: the reference's FP64 defect correction (engine/src/bsr.cpp:1373-1396: inner solves to
+    clamp(10 tol, 1e-4, 1e-2), at most 6 passes, FP64 residual) around the precision form, to 1e-8. The reference
+    refines its float device emulation the same way (golden x_refine); both end within 1e-8 in FP64, so both solutions
+    are within the system's conditioning of the tight FP64 solution."""
+    A, z = load_golden(name)
+    with dev(precond=precond, precision="mixed_f32", check_every=2) as d:
+        d.set_matrix(A)
+        d.setup()
+        x, res = d.solve_refined(z["b"], tol=1e-8, max_outer=6, inner_it=120)
+    assert res.converged and res.trueRelResidual <= 1e-8
+    assert true_res(A, x, z["b"]) <= 2e-8
+    xt = z["x_bicg_bilu0_tight"]
+    err_ref = rel(z["x_refine"], xt)                 # the reference's own refined solution against the tight one
+    assert rel(x, xt) < max(10 * err_ref, 1e-6), (rel(x, xt), err_ref)
+
+
+def test_refined_solve_batch_stops_converged_systems():
+    """In a batch, a system within the tolerance gets no further correction: its result is the one it has alone."""
+    mats, bs, singles = [], [], []
+    for name in ["waterflood_sys0.npz", "synth_small.npz", "waterflood_sys2.npz"]:
+        A, z = load_golden(name)
+        mats.append(A)
+        bs.append(z["b"])
+        with dev(precond="cpr", precision="mixed_f32") as d:
+            d.set_matrix(A)
+            d.setup()
+            singles.append(d.solve_refined(z["b"], tol=1e-9)[0])
+    with dev(precond="cpr", precision="mixed_f32") as d:
+        d.set_batch(mats)
+        d.setup()
+        xb, rb = d.solve_refined(np.concatenate(bs), tol=1e-9)
+        its, rr, tr = d.batch_results()
+    assert rb.converged and np.all(tr <= 1e-9)
+    off = 0
+    for A, xs in zip(mats, singles):
+        assert np.array_equal(xb[off:off + A.n * 3], xs)
+        off += A.n * 3
+
+
+# ---------------------------------------------------------------- launch shapes (autotuner candidates)
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_f32"])
+def test_launch_shapes_give_identical_results(precision):
+    """Every launch shape the autotuner chooses among computes the same values: the split CPR's grid passes as
+    separate launches or as the phases of one cooperative kernel, and its BILU0 stage with 256 or 512 threads per
+    system -- preconditioner output, solution and iterations bit for bit, on a batch with well cliques."""
+    from ressim_gb300 import synth
+    systems = synth.ensemble(n_real=6, nx=24, ny=24, nz=6, sigma=1.5)
+    b = np.concatenate([s.b for s in systems])
+    out = []
+    for fused, thr in ((2, 256), (1, 256), (1, 512), (2, 512)):
+        with dev(precond="cpr", precision=precision, sweep="split", autotune=False, vcycle_fused=fused, cpr2_threads=thr) as d:
+            d.set_batch([s.A for s in systems])
+            d.setup()
+            assert f"vcycle_fused={fused} cpr2_threads={thr}" in d.tuning()
+            z = d.precond_apply(b)
+            x, res = d.solve(b, tol=1e-6, maxit=300)
+            its, _, _ = d.batch_results()
+        out.append((z, x, its))
+        assert res.converged
+    for z, x, its in out[1:]:
+        assert np.array_equal(z, out[0][0]) and np.array_equal(x, out[0][1]) and np.array_equal(its, out[0][2])
+
+
+def test_autotuner_reports_its_choice():
+    """At the first set-up of a pattern the autotuner times the candidates and keeps the fastest; a second handle on
+    the same pattern reuses the choice (cached per pattern)."""
+    from ressim_gb300 import synth
+    systems = synth.ensemble(n_real=4, nx=20, ny=20, nz=5, sigma=1.5)
+    with dev(precond="cpr", precision="mixed_f32", sweep="split") as d:
+        d.set_batch([s.A for s in systems])
+        d.setup()
+        t1 = d.tuning()
+    assert "source=tuned" in t1 and "fused/256" in t1 and "launches/512" in t1
+    with dev(precond="cpr", precision="mixed_f32", sweep="split") as d:
+        d.set_batch([s.A for s in systems])
+        d.setup()
+        assert d.tuning() == t1
