@@ -76,8 +76,10 @@ typedef struct rsg_options {
     int autotune;           /* 1 (default): the launch shapes left at 0 below are chosen by timing the candidates on the
                                system at its first set-up (cached per pattern for the life of the process); 0: their
                                defaults. Every shape gives the same results bit for bit. */
-    int vcycle_fused;       /* split CPR: 1 = its grid-wide passes as the phases of one cooperative kernel (grid barriers
-                               between them), 2 = one launch per pass; 0 = tuned (default 1) */
+    int vcycle_form;        /* split CPR, how the V-cycle runs over the batch: 1 = every pass grid-wide, as the phases of
+                               one cooperative kernel (grid barriers between them); 2 = every pass grid-wide, one launch
+                               per pass; 3 = the finest level's passes grid-wide, the coarser levels one thread block per
+                               system in one launch; 0 = tuned (default 3) */
     int cpr2_threads;       /* split CPR: threads per system of the BILU0 stage, 256 or 512; 0 = tuned (default 256) */
 } rsg_options;
 
@@ -115,6 +117,33 @@ int rsg_release(rsg_solver* h);
  * reuses it (the engine's pattern reuse, engine/src/bsr.cpp:759-769 and AMG::refresh, amg.cpp:257-271).
  * Replaces: the BSR the engine hands to GpuBlockSolver::solve (engine/include/ressim/bsr.h:147). */
 int rsg_set_matrix(rsg_solver* h, int n, int nb, const int* rowPtr, const int* col, const double* val);
+
+/* The Newton Jacobian with its well rows, reduced on the device. A is the scalar CSR the engine assembles: na*nv cell
+ * rows followed by nw well (BHP) rows (nrows = na*nv + nw), host pattern, values on the host (rsg_set_jacobian, batch
+ * form with one set of arrays per system) or in device memory (rsg_set_jacobian_device; the caller keeps them valid
+ * until the solve). The well Schur complement S = A_cc - A_cw D_ww^-1 A_wc is computed on the device straight into the
+ * handle's block system (the same values as the engine's, bit for bit, in the engine's order of operations); its
+ * pattern is planned on the host and reused while the Jacobian pattern and the set of nonzero cell-to-well couplings
+ * stay the same. Returns RSG_EINVAL when a well row has no usable BHP derivative or couples wells (the engine then
+ * keeps the full system). Replaces: WellSchur::build / buildInPlace (engine/src/bsr.cpp:733-971) feeding
+ * GpuBlockSolver::solve. */
+int rsg_set_jacobian(rsg_solver* h, int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw);
+int rsg_set_jacobian_batch(rsg_solver* h, int nsys, int nv, const int* nrows, const int* na, const int* nw, const int* const* rowPtr,
+                           const int* const* col, const double* const* val);
+int rsg_set_jacobian_device(rsg_solver* h, int nrows, const int* rowPtr, const int* col, const double* d_val, int na, int nv, int nw);
+
+/* Solve after rsg_set_jacobian* and rsg_setup with the full right-hand side (per system: na*nv cell entries, then nw
+ * well entries; systems concatenated) and the full solution out (BHPs recovered on the device). Host vectors, or
+ * device vectors for the _device form. Replaces: WellSchur::reduceRhs + the block solve + WellSchur::recover
+ * (engine/src/bsr.cpp:973-990). */
+int rsg_solve_jacobian(rsg_solver* h, const double* b, double* x, double tol, int maxIt, int* iterations, double* relres);
+int rsg_solve_jacobian_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres);
+
+/* The current block system (after rsg_set_matrix / set_batch / set_jacobian) in the caller's row order: rowPtr[n+1],
+ * col[nnzb] (columns of the concatenated block-diagonal batch), val[nnzb*nb*nb]; any pointer may be NULL. Sizes from
+ * rsg_matrix_size. No reference counterpart (the reduced system of ressim::WellSchur::reduced(), bsr.h). */
+int rsg_get_matrix(rsg_solver* h, int* rowPtr, int* col, double* val);
+int rsg_matrix_size(rsg_solver* h, int* n, long long* nnzb);
 
 /* Upload a batch of independent systems (uneven sizes) that are solved together; system s has
  * n[s] block rows. Arrays are host pointers, one per system. */
@@ -197,7 +226,7 @@ int rsg_spmv_dot_noalloc(int n, int nb, const int* d_rowPtr, const int* d_col, c
 /* Statistics of the last setup / solve. */
 int rsg_get_stats(rsg_solver* h, rsg_stats* st);
 
-/* The launch shapes in use after rsg_setup and how they were chosen, as text ("vcycle_fused=1 cpr2_threads=512
+/* The launch shapes in use after rsg_setup and how they were chosen, as text ("vcycle_form=3 cpr2_threads=256
  * source=tuned ..." with the timed candidates), written NUL-terminated into buf (at most len bytes). No counterpart in
  * the reference, whose device kernels have fixed 64-thread groups (app/src/gpu_compute.cpp:57-80). */
 int rsg_tuning(rsg_solver* h, char* buf, int len);

@@ -25,6 +25,8 @@ EXPORTS = [
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
     "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
     "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes", "rsg_tuning",
+    "rsg_set_jacobian", "rsg_set_jacobian_batch", "rsg_set_jacobian_device", "rsg_solve_jacobian", "rsg_solve_jacobian_device",
+    "rsg_get_matrix", "rsg_matrix_size",
 ]
 
 
@@ -32,7 +34,7 @@ class Options(C.Structure):
     _fields_ = [("precond", C.c_int), ("krylov", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("gmres_fallback", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
                 ("mem_budget", C.c_size_t), ("sweep", C.c_int), ("fma", C.c_int), ("sweep_inflight", C.c_int),
-                ("autotune", C.c_int), ("vcycle_fused", C.c_int), ("cpr2_threads", C.c_int)]
+                ("autotune", C.c_int), ("vcycle_form", C.c_int), ("cpr2_threads", C.c_int)]
 
 
 class Result(C.Structure):
@@ -103,6 +105,13 @@ def load(build_if_missing: bool = True):
     L.rsg_server_load.argtypes = [vp, ip, ip, C.POINTER(C.c_size_t)]
     L.rsg_request_bytes.argtypes = [C.POINTER(Options), C.c_int, C.c_longlong]
     L.rsg_tuning.argtypes = [vp, C.c_char_p, C.c_int]
+    L.rsg_set_jacobian.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+    L.rsg_set_jacobian_batch.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp]
+    L.rsg_set_jacobian_device.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+    L.rsg_solve_jacobian.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
+    L.rsg_solve_jacobian_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, ip, dp]
+    L.rsg_get_matrix.argtypes = [vp, vp, vp, vp]
+    L.rsg_matrix_size.argtypes = [vp, ip, C.POINTER(C.c_longlong)]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype if name in ("rsg_last_error", "rsg_version", "rsg_stream") else (
             None if name == "rsg_default_options" else (C.c_longlong if name == "rsg_submit" else

@@ -140,11 +140,20 @@ struct rsg_solver {
     std::vector<double> htrue;
     // launch shapes (every choice gives the same results bit for bit) and how they were chosen
     struct Tune {
-        bool fused = true;
+        int vform = 3;
         int cpr2Threads = 256;
         std::string desc = "defaults";
     } tune;
     unsigned long long patHash = 0;   // FNV-1a of the plan's pattern (0: not computed)
+    // device well Schur complement (rsg_set_jacobian*): host plan, its device copy (pattern part and value maps), the
+    // Jacobian values (or the caller's device pointer), full and reduced vectors of the solve
+    WsPlan ws;
+    WsDev wsd;
+    DevMem wsPat, wsVal;
+    bool wsPlanned = false, wsValues = false, jac = false;
+    double* jval = nullptr;
+    const double* jv = nullptr;
+    double *wsB = nullptr, *wsX = nullptr, *wsBc = nullptr, *wsXc = nullptr;
     std::mutex mu;
 };
 
@@ -266,7 +275,7 @@ int check_device_errors(rsg_solver* h) {
 // kernel launches of one preconditioner application
 int precond_launches(const PrecDev& M) {
     if (M.devcpr) return devcpr_launches(*M.amg);
-    if (M.cpr && (!M.cta || M.split)) return cpr_grid_launches(*M.amg, M.split);
+    if (M.cpr && (!M.cta || M.split)) return cpr_grid_launches(*M.amg, M.split, M.vform);
     return M.cpr || M.cta || M.kind == 2 ? 1 : 2;
 }
 
@@ -287,7 +296,7 @@ PrecDev prec_dev(rsg_solver* h) {
         M.s64 = h->s64;
         M.s32 = h->s32;
         M.split = M.cpr && h->splitCpr;
-        M.fused = M.split && h->tune.fused;
+        M.vform = h->tune.vform;
         M.cpr2Threads = h->tune.cpr2Threads;
     }
     return M;
@@ -308,26 +317,20 @@ int set_values(rsg_solver* h, const std::vector<const double*>& vals, const std:
     return RSG_OK;
 }
 
-int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
-                 const double* const* val) {
-    if (nsys < 1 || !n || !rowPtr || !col || !val) return fail(RSG_EINVAL, "set_batch: null argument or nsys < 1");
-    if (nb != NB) return fail(RSG_EINVAL, "only nb = 3 (black-oil blocks) is supported, got nb = " + std::to_string(nb));
+// the plan of a batch pattern (kept when the pattern is the plan's); nnzbs gets the blocks of every system
+int set_batch_pattern(rsg_solver* h, int nsys, const int* n, const int* const* rowPtr, const int* const* col, std::vector<int>& nnzbs) {
     std::vector<int> sysRow0(size_t(nsys) + 1, 0);
     for (int s = 0; s < nsys; ++s) {
-        if (n[s] < 1 || !rowPtr[s] || !col[s] || !val[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " is empty");
+        if (n[s] < 1 || !rowPtr[s] || !col[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " is empty");
         sysRow0[size_t(s) + 1] = sysRow0[size_t(s)] + n[s];
     }
+    nnzbs.assign(static_cast<size_t>(nsys), 0);
+    for (int s = 0; s < nsys; ++s) nnzbs[size_t(s)] = rowPtr[s][n[s]];
     // the pattern of the current plan (a new Newton iteration or time step): values only, no pattern copy
-    if (h->havePlan && same_batch_pattern(h->plan, nsys, n, rowPtr, col)) {
-        std::vector<int> nnzbs(static_cast<size_t>(nsys));
-        for (int s = 0; s < nsys; ++s) nnzbs[size_t(s)] = rowPtr[s][n[s]];
-        std::vector<const double*> vals(val, val + nsys);
-        return set_values(h, vals, nnzbs);
-    }
+    if (h->havePlan && same_batch_pattern(h->plan, nsys, n, rowPtr, col)) return RSG_OK;
     const int ntot = sysRow0[size_t(nsys)];
     // concatenated pattern of the block-diagonal batch
     std::vector<int> rp(size_t(ntot) + 1, 0), ci;
-    std::vector<int> nnzbs(static_cast<size_t>(nsys));
     size_t total = 0;
     for (int s = 0; s < nsys; ++s) total += size_t(rowPtr[s][n[s]]);
     ci.reserve(total);
@@ -342,7 +345,6 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
                 ci.push_back(c + r0);
             }
         }
-        nnzbs[size_t(s)] = rowPtr[s][n[s]];
     }
     const bool same = h->havePlan && h->plan.nsys == nsys && h->plan.rowPtr0 == rp && h->plan.col0 == ci && h->plan.sysRow0 == sysRow0;
     if (!same) {
@@ -367,8 +369,107 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
         if (rc) { free_plan(h); return rc; }
         h->nsys = nsys;
     }
+    return RSG_OK;
+}
+
+int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
+                 const double* const* val) {
+    if (nsys < 1 || !n || !rowPtr || !col || !val) return fail(RSG_EINVAL, "set_batch: null argument or nsys < 1");
+    if (nb != NB) return fail(RSG_EINVAL, "only nb = 3 (black-oil blocks) is supported, got nb = " + std::to_string(nb));
+    for (int s = 0; s < nsys; ++s)
+        if (!val[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " has no values");
+    std::vector<int> nnzbs;
+    int rc = set_batch_pattern(h, nsys, n, rowPtr, col, nnzbs);
+    if (rc) return rc;
+    h->jac = false;
     std::vector<const double*> vals(val, val + nsys);
     return set_values(h, vals, nnzbs);
+}
+
+// Jacobians with well rows (full scalar CSR per system, values on the host (hval) or in one device array (dval)):
+// the well Schur complement on the device into the solver's block storage (rsg_wellschur.cu)
+int do_set_jacobian(rsg_solver* h, int nsys, int nv, const int* nrows, const int* na, const int* nw, const int* const* rowPtr,
+                    const int* const* col, const double* const* hval, const double* dval) {
+    if (nsys < 1 || !nrows || !na || !nw || !rowPtr || !col || (!hval && !dval)) return fail(RSG_EINVAL, "set_jacobian: null argument");
+    if (nv != NB) return fail(RSG_EINVAL, "only nv = 3 (black-oil) is supported, got nv = " + std::to_string(nv));
+    for (int s = 0; s < nsys; ++s)
+        if (!rowPtr[s] || !col[s] || (hval && !hval[s])) return fail(RSG_EINVAL, "set_jacobian: system " + std::to_string(s) + " is empty");
+    cudaStream_t st = h->stream;
+    int rc;
+    if (!h->wsPlanned || !ws_same_pattern(h->ws, nsys, nv, nrows, na, nw, rowPtr, col)) {
+        h->wsPat.release_all();
+        h->wsVal.release_all();
+        h->wsd = WsDev{};
+        h->wsPlanned = h->wsValues = false;
+        h->jval = h->wsB = h->wsX = h->wsBc = h->wsXc = nullptr;
+        std::string err;
+        if (!ws_plan_pattern(h->ws, nsys, nv, nrows, na, nw, rowPtr, col, err)) return fail(RSG_EINVAL, err);
+        const WsPlan& W = h->ws;
+        WsDev& D = h->wsd;
+        DevMem& M = h->wsPat;
+        D.ncpl = int(W.cplPos.size());
+        D.nwell = int(W.diagPos.size());
+        D.nred = W.red0.back();
+        if ((rc = upload(M, &D.cplPos, W.cplPos, st)) || (rc = upload(M, &D.diagPos, W.diagPos, st)) || (rc = upload(M, &D.wcBeg, W.wcBeg, st)) ||
+            (rc = upload(M, &D.wcPos, W.wcPos, st)) || (rc = upload(M, &D.wcRed, W.wcRed, st)) || (rc = upload(M, &D.wwBeg, W.wwBeg, st)) ||
+            (rc = upload(M, &D.wwPos, W.wwPos, st)) || (rc = upload(M, &D.wellFull, W.wellFull, st)) || (rc = upload(M, &D.redFull, W.redFull, st)) ||
+            (rc = dalloc(M, &D.mask, size_t(std::max(D.ncpl, 1)))) || (rc = dalloc(M, &D.wellOk, size_t(std::max(D.nwell, 1)))) ||
+            (rc = dalloc(M, &h->jval, size_t(W.jEnt0.back()))) || (rc = dalloc(M, &h->wsB, size_t(W.full0.back()))) ||
+            (rc = dalloc(M, &h->wsX, size_t(W.full0.back()))) || (rc = dalloc(M, &h->wsBc, size_t(D.nred))) ||
+            (rc = dalloc(M, &h->wsXc, size_t(D.nred))))
+            return rc;
+        h->wsPlanned = true;
+    }
+    const WsPlan& W = h->ws;
+    if (dval) {
+        h->jv = dval;
+    } else {
+        for (int s = 0; s < nsys; ++s) {
+            const size_t cnt = size_t(W.jEnt0[size_t(s) + 1] - W.jEnt0[size_t(s)]);
+            if (cnt) RSG_CUDA(cudaMemcpyAsync(h->jval + W.jEnt0[size_t(s)], hval[s], cnt * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        h->jv = h->jval;
+    }
+    // the value-dependent inputs of the plan: which couplings are nonzero, whether every well row is usable
+    launch_ws_check(h->wsd, h->jv, st);
+    h->launches += 1;
+    std::vector<unsigned char> mask(size_t(h->wsd.ncpl)), ok(size_t(h->wsd.nwell));
+    if (!mask.empty()) RSG_CUDA(cudaMemcpyAsync(mask.data(), h->wsd.mask, mask.size(), cudaMemcpyDeviceToHost, st));
+    if (!ok.empty()) RSG_CUDA(cudaMemcpyAsync(ok.data(), h->wsd.wellOk, ok.size(), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    for (size_t w = 0; w < ok.size(); ++w)
+        if (!ok[w]) {
+            h->wsValues = false;
+            return fail(RSG_EINVAL, "well row " + std::to_string(w) + " has no usable BHP derivative or couples wells: the engine keeps "
+                                    "the full system (engine/src/bsr.cpp:742-748)");
+        }
+    if (!h->wsValues || mask != W.mask || !h->havePlan) {
+        std::string err;
+        if (!ws_plan_values(h->ws, mask, err)) return fail(RSG_EINVAL, err);
+        std::vector<int> nS(na, na + nsys), nnzbs;
+        std::vector<const int*> rpS(static_cast<size_t>(nsys)), ciS(static_cast<size_t>(nsys));
+        for (int s = 0; s < nsys; ++s) { rpS[size_t(s)] = W.srp[size_t(s)].data(); ciS[size_t(s)] = W.sci[size_t(s)].data(); }
+        if ((rc = set_batch_pattern(h, nsys, nS.data(), rpS.data(), ciS.data(), nnzbs))) return rc;
+        h->wsVal.release_all();
+        WsDev& D = h->wsd;
+        DevMem& M = h->wsVal;
+        D.nval = (long long)W.sBase.size();
+        D.nfill = int(W.fillScalar.size());
+        if ((rc = upload(M, &D.sBase, W.sBase, st)) || (rc = upload(M, &D.fillScalar, W.fillScalar, st)) ||
+            (rc = upload(M, &D.fillBeg, W.fillBeg, st)) || (rc = upload(M, &D.tCw, W.tCw, st)) || (rc = upload(M, &D.tDiag, W.tDiag, st)) ||
+            (rc = upload(M, &D.tWc, W.tWc, st)) || (rc = upload(M, &D.rBeg, W.rBeg, st)) || (rc = upload(M, &D.rCw, W.rCw, st)) ||
+            (rc = upload(M, &D.rDiag, W.rDiag, st)) || (rc = upload(M, &D.rWellFull, W.rWellFull, st)))
+            return rc;
+        h->wsValues = true;
+    }
+    launch_ws_values(h->wsd, h->jv, h->val0, st);
+    launch_gather_blocks(h->dp, h->val0, h->val, st);
+    h->launches += 3;
+    RSG_CUDA(cudaGetLastError());
+    h->jac = true;
+    h->haveMatrix = true;
+    h->haveSetup = false;
+    return RSG_OK;
 }
 
 template <class T>
@@ -827,18 +928,21 @@ bool fused_capturable(rsg_solver* h, const double* d_r, double* d_z) {
 
 int tune_shapes(rsg_solver* h) {
     rsg_solver::Tune t;
-    const bool split = h->opt.precond == RSG_PREC_CPR && h->cta && h->splitCpr && h->haveAmg && h->amg.nPhases > 0;
-    t.fused = h->opt.vcycle_fused != 2;
+    const bool split = h->opt.precond == RSG_PREC_CPR && h->cta && h->splitCpr && h->haveAmg;
+    t.vform = h->opt.vcycle_form ? h->opt.vcycle_form : 3;
+    if (t.vform == 1 && h->amg.nPhases == 0) t.vform = 2;                  // no phase table for this hierarchy
     t.cpr2Threads = h->opt.cpr2_threads ? h->opt.cpr2_threads : 256;
-    const bool free_fused = h->opt.vcycle_fused == 0, free_thr = h->opt.cpr2_threads == 0;
+    const bool free_form = h->opt.vcycle_form == 0, free_thr = h->opt.cpr2_threads == 0;
+    auto describe = [](const rsg_solver::Tune& c) {
+        return std::string("vcycle_form=") + std::to_string(c.vform) + " cpr2_threads=" + std::to_string(c.cpr2Threads);
+    };
     if (!split) { t.desc = "no split CPR: fixed shapes"; h->tune = t; return RSG_OK; }
-    if (!h->opt.autotune || (!free_fused && !free_thr)) {
-        t.desc = std::string("vcycle_fused=") + (t.fused ? "1" : "2") + " cpr2_threads=" + std::to_string(t.cpr2Threads) +
-                 (h->opt.autotune ? " source=options" : " source=defaults");
+    if (!h->opt.autotune || (!free_form && !free_thr)) {
+        t.desc = describe(t) + (h->opt.autotune ? " source=options" : " source=defaults");
         h->tune = t;
         return RSG_OK;
     }
-    const int key2 = h->opt.precision * 1000 + h->opt.vcycle_fused * 10000 + h->opt.cpr2_threads + h->device * 100000;
+    const int key2 = h->opt.precision * 1000 + h->opt.vcycle_form * 10000 + h->opt.cpr2_threads + h->device * 100000;
     const auto key = std::make_pair(pattern_hash(h), key2);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -848,25 +952,27 @@ int tune_shapes(rsg_solver* h) {
     const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaMemsetAsync(h->tmp, 0, N * sizeof(double), h->stream));
     std::vector<rsg_solver::Tune> cand;
-    for (int f : {1, 0})
+    for (int f : {3, 2, 1})
         for (int thr : {256, 512}) {
-            if (!free_fused && (f != 0) != t.fused) continue;
+            if (!free_form && f != t.vform) continue;
             if (!free_thr && thr != t.cpr2Threads) continue;
+            if (f == 1 && h->amg.nPhases == 0) continue;
             rsg_solver::Tune c;
-            c.fused = f != 0;
+            c.vform = f;
             c.cpr2Threads = thr;
             cand.push_back(c);
         }
+    if (cand.empty()) { t.desc = describe(t) + " source=options"; h->tune = t; return RSG_OK; }
     bool fusedOk = true;
     float best = 1e30f;
     rsg_solver::Tune pick = cand.front();
     std::string timings;
     for (const auto& c : cand) {
-        if (c.fused && !fusedOk) continue;
+        if (c.vform == 1 && !fusedOk) continue;
         h->tune = c;
         int rc = precond_apply_dev(h, h->tmp, h->xout);        // warm-up (first launch of the shape)
-        if (rc == RSG_OK && c.fused && !fused_capturable(h, h->tmp, h->xout)) { fusedOk = false; continue; }
         if (rc) return rc;
+        if (c.vform == 1 && !fused_capturable(h, h->tmp, h->xout)) { fusedOk = false; continue; }
         RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
         for (int k = 0; k < 3; ++k)
             if ((rc = precond_apply_dev(h, h->tmp, h->xout))) return rc;
@@ -876,14 +982,13 @@ int tune_shapes(rsg_solver* h) {
         cudaEventElapsedTime(&ms, h->ev0, h->ev1);
         ms /= 3;
         char buf[96];
-        std::snprintf(buf, sizeof(buf), "%s%s/%d %.3f ms", timings.empty() ? "" : ", ", c.fused ? "fused" : "launches", c.cpr2Threads, ms);
+        std::snprintf(buf, sizeof(buf), "%sform%d/%d %.3f ms", timings.empty() ? "" : ", ", c.vform, c.cpr2Threads, ms);
         timings += buf;
         if (ms < best) { best = ms; pick = c; }
     }
     const int rce = check_device_errors(h);
     if (rce) return rce;
-    pick.desc = std::string("vcycle_fused=") + (pick.fused ? "1" : "2") + " cpr2_threads=" + std::to_string(pick.cpr2Threads) +
-                " source=tuned (CPR application: " + timings + (fusedOk ? "" : "; fused kernel not capturable here") + ")";
+    pick.desc = describe(pick) + " source=tuned (CPR application: " + timings + (fusedOk ? "" : "; fused kernel not capturable here") + ")";
     h->tune = pick;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache[key] = pick;
@@ -1250,9 +1355,92 @@ int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, 
     return conv ? RSG_OK : RSG_ENOTCONV;
 }
 
+// full right-hand sides (cells, then wells, per system) in, full solutions out: the reduction, the block solve, the
+// recovery of the BHPs (WellSchur::reduceRhs / recover, engine/src/bsr.cpp:973-990), all on the device
+int do_solve_jacobian(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h->jac || !h->wsValues) return fail(RSG_ESTATE, "solve_jacobian before set_jacobian");
+    if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
+    launch_ws_rhs(h->wsd, h->jv, d_b, h->wsBc, h->stream);
+    h->launches += 1;
+    const int rc = do_solve_device(h, h->wsBc, h->wsXc, tol, maxIt, iterations, relres);
+    if (rc < 0) return rc;
+    launch_ws_recover(h->wsd, h->jv, d_b, h->wsXc, d_x, h->stream);
+    h->launches += 1;
+    RSG_CUDA(cudaGetLastError());
+    return rc;
+}
+
 }  // namespace
 
 extern "C" {
+
+int rsg_set_jacobian(rsg_solver* h, int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_set_jacobian(h, 1, nv, &nrows, &na, &nw, &rowPtr, &col, &val, nullptr);
+}
+
+int rsg_set_jacobian_batch(rsg_solver* h, int nsys, int nv, const int* nrows, const int* na, const int* nw, const int* const* rowPtr,
+                           const int* const* col, const double* const* val) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    if (!val) return fail(RSG_EINVAL, "set_jacobian_batch: null values");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_set_jacobian(h, nsys, nv, nrows, na, nw, rowPtr, col, val, nullptr);
+}
+
+int rsg_set_jacobian_device(rsg_solver* h, int nrows, const int* rowPtr, const int* col, const double* d_val, int na, int nv, int nw) {
+    if (!h || !d_val) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_set_jacobian(h, 1, nv, &nrows, &na, &nw, &rowPtr, &col, nullptr, d_val);
+}
+
+int rsg_solve_jacobian(rsg_solver* h, const double* b, double* x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h || !b || !x) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->jac || !h->wsPlanned) return fail(RSG_ESTATE, "solve_jacobian before set_jacobian");
+    const size_t N = size_t(h->ws.full0.back());
+    RSG_CUDA(cudaMemcpyAsync(h->wsB, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const int rc = do_solve_jacobian(h, h->wsB, h->wsX, tol, maxIt, iterations, relres);
+    if (rc < 0) return rc;
+    RSG_CUDA(cudaMemcpyAsync(x, h->wsX, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    RSG_CUDA(cudaStreamSynchronize(h->stream));
+    return rc;
+}
+
+int rsg_solve_jacobian_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
+    if (!h || !d_b || !d_x) return fail(RSG_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    return do_solve_jacobian(h, d_b, d_x, tol, maxIt, iterations, relres);
+}
+
+int rsg_get_matrix(rsg_solver* h, int* rowPtr, int* col, double* val) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaSetDevice(h->device);
+    if (!h->haveMatrix) return fail(RSG_ESTATE, "get_matrix before set_matrix / set_jacobian");
+    const HostPlan& P = h->plan;
+    if (rowPtr) std::copy(P.rowPtr0.begin(), P.rowPtr0.end(), rowPtr);
+    if (col) std::copy(P.col0.begin(), P.col0.end(), col);
+    if (val) {
+        RSG_CUDA(cudaMemcpyAsync(val, h->val0, size_t(P.nnzb) * NB2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return RSG_OK;
+}
+
+int rsg_matrix_size(rsg_solver* h, int* n, long long* nnzb) {
+    if (!h) return fail(RSG_EINVAL, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->havePlan) return fail(RSG_ESTATE, "no matrix");
+    if (n) *n = h->plan.n;
+    if (nnzb) *nnzb = h->plan.nnzb;
+    return RSG_OK;
+}
 
 const char* rsg_version(void) { return "rsg 0.1 (sm_103a)"; }
 const char* rsg_last_error(void) { return g_err.c_str(); }
@@ -1272,7 +1460,7 @@ void rsg_default_options(rsg_options* o) {
     o->mem_budget = 0;
     o->sweep = 0;
     o->autotune = 1;
-    o->vcycle_fused = 0;
+    o->vcycle_form = 0;
     o->cpr2_threads = 0;
 }
 
@@ -1284,8 +1472,8 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     if (opts) o = *opts;
     if (o.precond < 0 || o.precond > 4 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 3)
         return fail(RSG_EINVAL, "invalid options");
-    if (o.vcycle_fused < 0 || o.vcycle_fused > 2 || (o.cpr2_threads != 0 && o.cpr2_threads != 256 && o.cpr2_threads != 512))
-        return fail(RSG_EINVAL, "invalid launch shape options (vcycle_fused 0..2, cpr2_threads 0 / 256 / 512)");
+    if (o.vcycle_form < 0 || o.vcycle_form > 3 || (o.cpr2_threads != 0 && o.cpr2_threads != 256 && o.cpr2_threads != 512))
+        return fail(RSG_EINVAL, "invalid launch shape options (vcycle_form 0..3, cpr2_threads 0 / 256 / 512)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
     if (o.device < 0 || o.device >= ndev) return fail(RSG_EINVAL, "device ordinal out of range");
@@ -1302,7 +1490,7 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
-    h->mem.st = h->pmem.st = h->stream;
+    h->mem.st = h->pmem.st = h->wsPat.st = h->wsVal.st = h->stream;
     if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(e, "cudaEventCreate");
     if ((e = cudaMallocHost(&h->h_pin, 4 * sizeof(int))) != cudaSuccess) return bail(e, "cudaMallocHost");

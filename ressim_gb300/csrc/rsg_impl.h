@@ -237,16 +237,62 @@ int launch_devcpr_setup(const DevPlan& P, const double* val, DevAmg& G, cudaStre
 int launch_devcpr(const DevPlan& P, const DevAmg& G, const double* val, int mode, const double* r, double* pv, const double* v, double* z,
                   const KScal* ks, cudaStream_t st);
 int devcpr_launches(const DevAmg& G);
-inline int cpr_grid_launches(const DevAmg& G, bool split = false) {
-    int n = (split ? 4 : 6) + 3 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
-    for (int l = 0; l + 1 < G.maxL; ++l) {          // pre- and post-smoothing: one sweep, or a launch per large colour + the tail
+inline int cpr_grid_launches(const DevAmg& G, bool split = false, int vform = 2) {
+    if (split && vform == 1 && G.nPhases > 0) return 2;            // the fused V-cycle and the BILU0 stage
+    auto sweeps = [&](int l) {                                     // one sweep: a launch per large colour + the tail, or one
         const int nc = l < int(G.colBeg.size()) ? int(G.colBeg[size_t(l)].size()) - 1 : 0;
-        n += 2 * (nc > 0 ? G.colTail[size_t(l)] + (G.colTail[size_t(l)] < nc ? 1 : 0) : 1);
-    }
+        return nc > 0 ? G.colTail[size_t(l)] + (G.colTail[size_t(l)] < nc ? 1 : 0) : 1;
+    };
+    if (split && vform == 3) return G.maxL > 1 ? 7 + 2 * sweeps(0) : 4;
+    int n = (split ? 4 : 6) + 3 * (G.maxL > 1 ? G.maxL - 1 : 0) + 40 * int(G.coarseGsLevels.size());
+    for (int l = 0; l + 1 < G.maxL; ++l) n += 2 * sweeps(l);      // pre- and post-smoothing
     return n;
 }
 
-// ---- well Schur complement (engine/src/bsr.cpp:733-840, 973-990)
+// ---- well Schur complement on the device (rsg_wellschur.cu): host plan of a batch of Jacobians with well rows.
+// Global indices: Jacobian entries concatenated over the systems (jEnt0), full vectors [cells, wells] per system
+// (full0), reduced vectors of the cells (red0), wells (well0), S blocks concatenated per system.
+struct WsPlan {
+    int nsys = 0, nv = 3;
+    std::vector<int> nrows, na, nw;
+    std::vector<int> jEnt0, full0, red0, well0;        // per-system offsets (nsys + 1 each)
+    std::vector<std::vector<int>> jrp, jci;            // the Jacobian patterns (same-pattern test)
+    std::vector<int> redFull;                          // reduced row -> full row
+    std::vector<int> cplPos, cplRow, cplWell;          // cell-to-well couplings: Jacobian entry, reduced row, well
+    std::vector<int> diagPos, wellFull, wcBeg, wcPos, wcRed, wwBeg, wwPos;   // per well: BHP derivative, full row,
+                                                       // cell entries (entry, reduced column), couplings to other wells
+    std::vector<unsigned char> mask;                   // nonzero set of the couplings the value maps were built for
+    std::vector<std::vector<int>> srp, sci;            // S pattern of every system
+    long long nnzbS = 0;
+    std::vector<int> sBase;                            // per S value: its Jacobian entry, or -1 (fill)
+    std::vector<long long> fillScalar;                 // S values with well terms, and their terms in the engine's order
+    std::vector<int> fillBeg, tCw, tDiag, tWc;
+    std::vector<int> rBeg, rCw, rDiag, rWellFull;      // right-hand side terms per reduced row
+};
+struct WsDev {
+    int ncpl = 0, nwell = 0, nred = 0, nfill = 0;
+    long long nval = 0;
+    int *cplPos = nullptr, *diagPos = nullptr, *wcBeg = nullptr, *wcPos = nullptr, *wwBeg = nullptr, *wwPos = nullptr,
+        *wcRed = nullptr, *wellFull = nullptr, *redFull = nullptr;
+    unsigned char *mask = nullptr, *wellOk = nullptr;
+    int* sBase = nullptr;
+    long long* fillScalar = nullptr;
+    int *fillBeg = nullptr, *tCw = nullptr, *tDiag = nullptr, *tWc = nullptr;
+    int *rBeg = nullptr, *rCw = nullptr, *rDiag = nullptr, *rWellFull = nullptr;
+};
+bool ws_same_pattern(const WsPlan& W, int nsys, int nv, const int* nrows, const int* na, const int* nw, const int* const* rowPtr,
+                     const int* const* col);
+bool ws_plan_pattern(WsPlan& W, int nsys, int nv, const int* nrows, const int* na, const int* nw, const int* const* rowPtr,
+                     const int* const* col, std::string& err);
+bool ws_plan_values(WsPlan& W, const std::vector<unsigned char>& mask, std::string& err);
+// per call: coupling nonzero flags and well checks; S values into sv (S blocks, original order); reduced right-hand
+// side; recovery of the full solution
+void launch_ws_check(const WsDev& D, const double* jv, cudaStream_t st);
+void launch_ws_values(const WsDev& D, const double* jv, double* sv, cudaStream_t st);
+void launch_ws_rhs(const WsDev& D, const double* jv, const double* bFull, double* bc, cudaStream_t st);
+void launch_ws_recover(const WsDev& D, const double* jv, const double* bFull, const double* xc, double* xFull, cudaStream_t st);
+
+// ---- well Schur complement on the host (engine/src/bsr.cpp:733-840, 973-990)
 int wellschur_reduce(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
                      const double* b, int* nnzb, int* sRowPtr, int* sCol, double* sVal, double* bc, std::string& err);
 int wellschur_recover(int nrows, const int* rowPtr, const int* col, const double* val, int na, int nv, int nw,
@@ -344,7 +390,8 @@ struct PrecDev {
     bool devcpr = false;              // the reference's GPU-shaped float CPR-AMG
     bool split = false;               // CPR with cta: V-cycle and second-stage input grid-wide (all systems at once),
                                       // the BILU0 sweeps one thread block per system
-    bool fused = false;               // split CPR: the grid-wide passes as the phases of one cooperative kernel
+    int vform = 2;                    // split CPR V-cycle: 1 fused cooperative kernel, 2 one launch per pass, 3 coarse
+                                      // levels one thread block per system
     int cpr2Threads = 256;            // split CPR: threads per block of the BILU0 stage (256 or 512; same results)
     const DevAmg* amg = nullptr;
 };

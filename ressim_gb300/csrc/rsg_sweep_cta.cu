@@ -846,12 +846,15 @@ __device__ void gs_any(const AmgSysLv& A, const CprArgs<TA>& C, const VVecs<TA>&
     else gs_sweep_w<TA, AMG_W1, NT>(A, C, V, forward, fromZero);
 }
 
-// AMG::cycle (engine/src/amg.cpp:303-329) for system s, level-0 right-hand side already in place
+// AMG::cycle (engine/src/amg.cpp:303-329) for system s from level lstart down and back (lstart 0: the whole V-cycle,
+// level-0 right-hand side already in place; lstart 1: the coarse part under a level 0 smoothed by the grid passes,
+// level-1 right-hand side in place, level-1 solution left for the grid prolongation)
 template <class TA, int NT>
-__device__ __forceinline__ void vcycle_body(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
+__device__ __forceinline__ void vcycle_body(int s, const CprArgs<TA>& C, const VVecs<TA>& V, int lstart) {
     int nlev = 0;
     while (nlev < C.maxL && C.lv[s * C.maxL + nlev].n > 0) ++nlev;
-    int l = 0;
+    if (lstart >= nlev) lstart = nlev > 0 ? nlev - 1 : 0;   // a system whose level 0 is its coarsest
+    int l = lstart;
     for (; l < nlev; ++l) {
         const AmgSysLv A = C.lv[s * C.maxL + l];
         if (A.coarse) {
@@ -898,7 +901,7 @@ __device__ __forceinline__ void vcycle_body(int s, const CprArgs<TA>& C, const V
         }
         __syncthreads();
     }
-    for (l = l - 1; l >= 0; --l) {                          // prolongation and post-smoothing (amg.cpp:326-327)
+    for (l = l - 1; l >= lstart; --l) {                     // prolongation and post-smoothing (amg.cpp:326-327)
         const AmgSysLv A = C.lv[s * C.maxL + l];
         const AmgSysLv Cl = C.lv[s * C.maxL + l + 1];
         TA* xl = V.x(A, C);
@@ -911,12 +914,12 @@ __device__ __forceinline__ void vcycle_body(int s, const CprArgs<TA>& C, const V
 }
 
 template <class TA, int NT>
-__device__ __noinline__ void vcycle_call(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
-    vcycle_body<TA, NT>(s, C, V);
+__device__ __noinline__ void vcycle_call(int s, const CprArgs<TA>& C, const VVecs<TA>& V, int lstart) {
+    vcycle_body<TA, NT>(s, C, V, lstart);
 }
 template <class TA, int NT>
-__device__ __forceinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>& V) {
-    vcycle_call<TA, NT>(s, C, V);
+__device__ __forceinline__ void vcycle(int s, const CprArgs<TA>& C, const VVecs<TA>& V, int lstart = 0) {
+    vcycle_call<TA, NT>(s, C, V, lstart);
 }
 
 // t -= S_kj[:,p] xp_j for the pressure column of one block (TT: the arithmetic of the second-stage input)
@@ -1727,6 +1730,17 @@ __global__ void __launch_bounds__(256) k_gcpr_coarse(CprArgs<TA> C, const KScal*
     gcpr_coarse_body<TA>(C, ks, int(gridDim.x), 1);
 }
 
+// the coarse part of the V-cycle (levels 1 .. coarsest: smoothing, residual, restriction, coarsest solve,
+// prolongation) of one system per thread block, with the thread-block V-cycle's arithmetic (so the values are those of
+// the grid passes it replaces); levels this small cost a block barrier per pass instead of a launch
+template <class TA, int NT>
+__global__ void __launch_bounds__(NT) k_vcycle_lo(CprArgs<TA> C, const KScal* ks) {
+    const int s = blockIdx.x;
+    if (ks && ks[s].status != ST_RUNNING) return;
+    const VVecs<TA> V{nullptr, nullptr, nullptr, true};
+    vcycle<TA, NT>(s, C, V, 1);
+}
+
 // t = input - S[:,p] xp (pressure column of every block in row order, bsr.cpp:1071-1081), in place in T
 template <class TA, class TT>
 __global__ void __launch_bounds__(256) k_gcpr_t(int n, const int* __restrict__ rowSys, const int* __restrict__ rowPtr,
@@ -1996,7 +2010,7 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
     // the split form keeps t in the second stage's sweep type (TT: FP32 in the all-FP32 form), as the thread-block
     // kernel does
     TT* Tsplit = reinterpret_cast<TT*>(G.T);
-    if (M.split && M.fused && G.nPhases > 0) {
+    if (M.split && M.vform == 1 && G.nPhases > 0) {
         // the whole pass sequence (input .. t) as the phases of one cooperative launch, then the BILU0 stage
         VcArgs<TA, TT> A{C, n, P.nsys, G.maxL, G.totRows, P.rowSys, P.sysRow0, r, v, pv, Tsplit, G.rowLv, G.gsRows, G.wave, G.rp, G.ci,
                          G.diag, G.gci, G.agg, G.lv, G.cdesc, val, G.gsFlag, G.gsCtr, P.Lslot, P.Uslot, P.LovCol, P.UovCol,
@@ -2079,21 +2093,29 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
         else go(std::false_type());
         ++launches;
     };
-    for (int l = 0; l + 1 < G.maxL; ++l) {                 // pre-smoothing and restriction, finest to coarsest
+    // form 3 (split only): the levels below the finest in one launch, a thread block per system
+    const bool lo = M.split && M.vform == 3;
+    const int lTop = lo ? std::min(1, G.maxL - 1) : G.maxL - 1;   // levels smoothed by grid passes: [0, lTop)
+    for (int l = 0; l < lTop; ++l) {                       // pre-smoothing and restriction, finest to coarsest
         sweep(l, 0, true, true);
         const int f0 = LB[size_t(l)], f1 = LB[size_t(l) + 1], c0 = LB[size_t(l) + 1], c1 = LB[size_t(l) + 2];
         k_gcpr_resid<TA><<<grid_for(f1 - f0, 256), 256, 0, st>>>(f0, f1, G.maxL, G.rowLv, G.lv, G.rp, G.ci, val, C.b, C.x, C.r, ks);
         k_gcpr_restrict<TA><<<grid_for(c1 - c0, 256), 256, 0, st>>>(c0, c1, G.maxL, G.rowLv, G.lv, G.memPtr, G.mem, C.b, C.r, ks);
         launches += 2;
     }
-    k_gcpr_coarse<TA><<<G.nsys, 256, 0, st>>>(C, ks);
-    ++launches;
-    for (int l : G.coarseGsLevels)                         // coarsest levels without dense LU (amg.cpp:313-315)
-        for (int it = 0; it < 20; ++it) {
-            sweep(l, 1, true, false);
-            sweep(l, 1, false, false);
-        }
-    for (int l = G.maxL - 2; l >= 0; --l) {                // prolongation and post-smoothing, coarsest to finest
+    if (lo) {
+        k_vcycle_lo<TA, 256><<<G.nsys, 256, 0, st>>>(C, ks);
+        ++launches;
+    } else {
+        k_gcpr_coarse<TA><<<G.nsys, 256, 0, st>>>(C, ks);
+        ++launches;
+        for (int l : G.coarseGsLevels)                     // coarsest levels without dense LU (amg.cpp:313-315)
+            for (int it = 0; it < 20; ++it) {
+                sweep(l, 1, true, false);
+                sweep(l, 1, false, false);
+            }
+    }
+    for (int l = lTop - 1; l >= 0; --l) {                  // prolongation and post-smoothing, coarsest to finest
         const int q0 = LB[size_t(l)], q1 = LB[size_t(l) + 1];
         k_gcpr_prolong<TA><<<grid_for(q1 - q0, 256), 256, 0, st>>>(q0, q1, G.maxL, G.rowLv, G.lv, G.agg, C.x, ks);
         ++launches;

@@ -34,7 +34,8 @@ def main(argv=None):
     ap.add_argument("--systems", type=int, default=64, help="ensemble64: realisations of the ensemble (the bench's 64)")
     ap.add_argument("--sweep", default=None, choices=["auto", "cta", "split", "grid"],
                     help="sweep / CPR form (default: the case's; cta = the one-kernel CPR application)")
-    ap.add_argument("--vcycle-fused", type=int, default=0, help="split CPR passes: 1 fused kernel, 2 separate launches, 0 tuned")
+    ap.add_argument("--vcycle-form", type=int, default=0,
+                    help="split CPR V-cycle: 1 fused kernel, 2 separate launches, 3 coarse levels per system, 0 tuned")
     ap.add_argument("--cpr2-threads", type=int, default=0, help="split CPR BILU0 stage: 256 or 512 threads per system, 0 tuned")
     args = ap.parse_args(argv)
     from ressim_gb300 import synth
@@ -47,7 +48,7 @@ def main(argv=None):
         s = synth.make_system(*c["shape"], sigma=1.5, seed=3, dt=5.0, wells="random", n_wells=4)
         mats, b = [s.A], s.b
     d = DeviceSolver(precond=c["precond"], precision=args.precision, sweep=args.sweep or c["sweep"], krylov="bicgstab",
-                     check_every=4, use_graphs=True, vcycle_fused=args.vcycle_fused, cpr2_threads=args.cpr2_threads)
+                     check_every=4, use_graphs=True, vcycle_form=args.vcycle_form, cpr2_threads=args.cpr2_threads)
     if len(mats) > 1:
         d.set_batch(mats)
     else:

@@ -37,7 +37,7 @@ class DeviceSolver:
     def __init__(self, precond: str = "bilu0", krylov: str = "bicgstab", precision: str = "fp64", restart: int = 40,
                  check_every: int = 4, use_graphs: bool = True, device: int = 0, mem_budget: int = 0,
                  gmres_fallback: bool = False, sweep: str = "auto", fma: bool = True,
-                 sweep_inflight: int = 0, autotune: bool = True, vcycle_fused: int = 0, cpr2_threads: int = 0):
+                 sweep_inflight: int = 0, autotune: bool = True, vcycle_form: int = 0, cpr2_threads: int = 0):
         self.L = _lib.load()
         o = _lib.Options()
         self.L.rsg_default_options(C.byref(o))
@@ -54,7 +54,7 @@ class DeviceSolver:
         o.sweep = _lib.SWEEP[sweep]
         o.sweep_inflight = sweep_inflight
         o.autotune = 1 if autotune else 0
-        o.vcycle_fused = vcycle_fused
+        o.vcycle_form = vcycle_form
         o.cpr2_threads = cpr2_threads
         self.opts = o
         h = C.c_void_p()
@@ -99,6 +99,50 @@ class DeviceSolver:
         self.n = int(sum(m.n * m.nb for m in mats))
         self.nsys = k
         self.sizes = [m.n * m.nb for m in mats]
+
+    def set_jacobian(self, J, na: int, nv: int, nw: int):
+        """The Newton Jacobian with its well rows (ScalarCSR, na*nv cell rows then nw well rows): the well Schur
+        complement on the device into this solver's block system (rsg_set_jacobian)."""
+        _lib.check(self.L.rsg_set_jacobian(self.h, J.n, _lib.ptr(J.rowPtr), _lib.ptr(J.col), _lib.ptr(J.val), na, nv, nw))
+        self.n = na * nv
+        self.nsys = 1
+        self.sizes = [na * nv]
+        self.full = J.n
+
+    def set_jacobian_batch(self, jacs):
+        """A batch of (ScalarCSR, na, nw) Jacobians with well rows (nv = 3), reduced on the device."""
+        k = len(jacs)
+        nrows = np.array([J.n for J, _, _ in jacs], dtype=np.int32)
+        na = np.array([a for _, a, _ in jacs], dtype=np.int32)
+        nw = np.array([w for _, _, w in jacs], dtype=np.int32)
+        rps = (C.c_void_p * k)(*[J.rowPtr.ctypes.data for J, _, _ in jacs])
+        cis = (C.c_void_p * k)(*[J.col.ctypes.data for J, _, _ in jacs])
+        vls = (C.c_void_p * k)(*[J.val.ctypes.data for J, _, _ in jacs])
+        self._keepj = (nrows, na, nw, rps, cis, vls)
+        _lib.check(self.L.rsg_set_jacobian_batch(self.h, k, 3, _lib.ptr(nrows), _lib.ptr(na), _lib.ptr(nw), rps, cis, vls))
+        self.n = int(na.sum()) * 3
+        self.nsys = k
+        self.sizes = [int(a) * 3 for a in na]
+        self.full = int(nrows.sum())
+
+    def solve_jacobian(self, b_full, tol: float = 1e-6, maxit: int = 120):
+        """Full right-hand side (cells then wells, per system) in, full solution (BHPs recovered) out."""
+        b = np.ascontiguousarray(b_full, dtype=np.float64)
+        x = np.zeros(self.full)
+        its, rr = C.c_int(0), C.c_double(0)
+        rc = _lib.check(self.L.rsg_solve_jacobian(self.h, _lib.ptr(b), _lib.ptr(x), tol, maxit, C.byref(its), C.byref(rr)))
+        st = self.stats()
+        return x, LinResult(rc == 0, its.value, rr.value, st.true_rel_residual, rc)
+
+    def matrix(self):
+        """The current block system (caller's order) as a BSR."""
+        n, nnzb = C.c_int(0), C.c_longlong(0)
+        _lib.check(self.L.rsg_matrix_size(self.h, C.byref(n), C.byref(nnzb)))
+        rp = np.zeros(n.value + 1, dtype=np.int32)
+        ci = np.zeros(nnzb.value, dtype=np.int32)
+        v = np.zeros(nnzb.value * 9)
+        _lib.check(self.L.rsg_get_matrix(self.h, _lib.ptr(rp), _lib.ptr(ci), _lib.ptr(v)))
+        return BSR(n.value, 3, rp, ci, v)
 
     def setup(self, acc=None):
         a = None if acc is None else np.ascontiguousarray(acc, dtype=np.float64)
