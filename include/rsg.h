@@ -283,6 +283,10 @@ long long rsg_submit(rsg_server* s, int n, int nb, const int* rowPtr, const int*
 int rsg_poll(rsg_server* s, long long id, int wait, double* x, rsg_result* res);
 /* The admission figure: estimated device bytes of one request of n block rows and nnzb blocks under opts. */
 size_t rsg_request_bytes(const rsg_options* opts, int n, long long nnzb);
+/* hold != 0: admit nothing until called again with hold = 0 (requests keep queuing); a caller that hands over a
+ * batch of systems at once (the realisations of an ensemble at a common time step) holds admission while it submits
+ * them, so that they are admitted together and run as one batched solve. */
+int rsg_server_hold(rsg_server* s, int hold);
 /* Requests queued / running and device bytes admitted right now. */
 int rsg_server_load(rsg_server* s, int* queued, int* running, size_t* bytes_in_use);
 

