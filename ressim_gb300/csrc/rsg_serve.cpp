@@ -336,7 +336,7 @@ long long rsg_submit(rsg_server* S, int n, int nb, const int* rowPtr, const int*
 
 int rsg_poll(rsg_server* S, long long id, int wait, double* x, rsg_result* res) {
     using rsg::set_last_error;
-    if (!S) { set_last_error("null server"); return RSG_EINVAL; }
+    if (!S) { rsg::set_last_error("null server"); return RSG_EINVAL; }
     std::shared_ptr<Request> R;
     {
         std::unique_lock<std::mutex> lk(S->mu);
@@ -362,7 +362,7 @@ size_t rsg_request_bytes(const rsg_options* opts, int n, long long nnzb) {
 }
 
 int rsg_server_hold(rsg_server* S, int hold) {
-    if (!S) { set_last_error("null server"); return RSG_EINVAL; }
+    if (!S) { rsg::set_last_error("null server"); return RSG_EINVAL; }
     {
         std::lock_guard<std::mutex> lk(S->mu);
         S->hold = hold != 0;

@@ -1940,11 +1940,14 @@ __global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const 
     const int l0 = __ldg(F.sysLvl0 + s), nl = __ldg(F.sysLvl0 + s + 1) - l0 - 1;
     __shared__ int lvc[kLvCache];
     const int* ls = level_starts(F.lvlStart + l0, nl, lvc);
+    // FP32 factors at 256 threads: three register buffers (rows loaded two levels ahead); at 512 threads (every row of a
+    // wide level has its own thread) the two-buffer sweep, whose registers fit the smaller per-thread budget
+    constexpr bool three = sizeof(TF) == 4 && NT <= 256;
     if (onchip || sizeof(TV) != sizeof(double)) {
-        if constexpr (sizeof(TF) == 4) ilu_body3<TF, TV, TV, true, TA>(F, row0, ls, nl, T, z, y, true, xpg);
+        if constexpr (three) ilu_body3<TF, TV, TV, true, TA>(F, row0, ls, nl, T, z, y, true, xpg);
         else ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, ls, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
     } else {
-        if constexpr (sizeof(TF) == 4) ilu_body3<TF, TV, TV, false, TA>(F, row0, ls, nl, T, z, y, false, (const TA*)nullptr);
+        if constexpr (three) ilu_body3<TF, TV, TV, false, TA>(F, row0, ls, nl, T, z, y, false, (const TA*)nullptr);
         else ilu_body<TF, TV, TV, IN_PLAIN, false, TA, NT>(F, row0, ls, nl, T, nullptr, nullptr, z, y, false, 0, 0, 0, nullptr);
         for (int k = row0 + tid; k < row0 + ns; k += nt) z[size_t(k) * 3] = da(z[size_t(k) * 3], double(xpg[k - row0]));
     }
