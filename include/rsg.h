@@ -115,7 +115,13 @@ int rsg_release(rsg_solver* h);
 /* Upload (or refresh) one system matrix from host memory. The pattern-dependent plan (level schedule,
  * elimination lists, AMG aggregates) is rebuilt only when the pattern changes; a values-only refresh
  * reuses it (the engine's pattern reuse, engine/src/bsr.cpp:759-769 and AMG::refresh, amg.cpp:257-271).
- * Replaces: the BSR the engine hands to GpuBlockSolver::solve (engine/include/ressim/bsr.h:147). */
+ * Replaces: the BSR the engine hands to GpuBlockSolver::solve (engine/include/ressim/bsr.h:147).
+ * nb = 3 (black-oil) runs the specialised path with every option. Any other 1 <= nb <= 16 (kMaxBlock,
+ * engine/include/ressim/bsr.h:21: the compositional simulator's nc + 1 unknowns, the thermal one's 4-5) runs the
+ * block-size-generic path: one system per handle, FP64 (precision RSG_FP64), preconditioner RSG_PREC_BILU0 or
+ * RSG_PREC_CPR, BiCGSTAB or GMRES(restart), with the reference's generic block arithmetic (BILU0 factors and sweeps bit
+ * for bit); other options are RSG_EINVAL for such blocks. The callers it serves: engine/src/compsim.cpp:1443-1449
+ * (BlockCPR + GMRES(60)) and engine/src/thermsim.cpp:1818-1828 (BlockCPR + GMRES(80)). */
 int rsg_set_matrix(rsg_solver* h, int n, int nb, const int* rowPtr, const int* col, const double* val);
 
 /* The Newton Jacobian with its well rows, reduced on the device. A is the scalar CSR the engine assembles: na*nv cell
@@ -146,7 +152,8 @@ int rsg_get_matrix(rsg_solver* h, int* rowPtr, int* col, double* val);
 int rsg_matrix_size(rsg_solver* h, int* n, long long* nnzb);
 
 /* Upload a batch of independent systems (uneven sizes) that are solved together; system s has
- * n[s] block rows. Arrays are host pointers, one per system. */
+ * n[s] block rows. Arrays are host pointers, one per system. Batches take nb = 3 (a single system of another block
+ * size, nsys = 1, goes to the block-size-generic path as in rsg_set_matrix). */
 int rsg_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
                   const double* const* val);
 
@@ -250,8 +257,11 @@ int rsg_wellschur_recover(int nrows, const int* rowPtr, const int* col, const do
  * A server runs `slots` workers, each with its own solver handle and CUDA stream. Requests are admitted in
  * arrival order as soon as a slot is free and their estimated device bytes fit the memory budget, so work that
  * arrives while others are on the GPU overlaps with them on the device. Matrices, factors and Krylov state stay
- * resident in HBM for the life of a request and are freed when it completes. Every request is solved exactly as
- * it would be alone (its own plan, deterministic kernels): the result does not depend on the mix. */
+ * resident in HBM for the life of a request; afterwards its slot keeps the plan resident (counted against the
+ * budget, released when an admission needs the room), so that the next request with the same pattern uploads values
+ * only, as the engine reuses a pattern's plan (engine/src/bsr.cpp:759-769). Every request is solved exactly as it
+ * would be alone (deterministic kernels, a plan that depends on the pattern only): the result does not depend on
+ * the mix. */
 typedef struct rsg_server rsg_server;
 
 typedef struct rsg_result {
@@ -287,7 +297,9 @@ size_t rsg_request_bytes(const rsg_options* opts, int n, long long nnzb);
  * batch of systems at once (the realisations of an ensemble at a common time step) holds admission while it submits
  * them, so that they are admitted together and run as one batched solve. */
 int rsg_server_hold(rsg_server* s, int hold);
-/* Requests queued / running and device bytes admitted right now. */
+/* Requests queued / running and device bytes counted against the budget right now: the admitted requests' estimates
+ * plus the plans idle slots keep resident for the next request with the same pattern (released first when an
+ * admission needs their room). */
 int rsg_server_load(rsg_server* s, int* queued, int* running, size_t* bytes_in_use);
 
 #ifdef __cplusplus

@@ -10,6 +10,10 @@
 //    By default it chooses the preconditioner as the engine does (CPR from 500 cells, else BILU0) and its GMRES
 //    fallback is GMRES(60), the engine's. solve() returns false on any device error or non-finite result (and, in
 //    the FP64 role, on a solve that missed the tolerance), so the engine falls back to its CPU path.
+//    The same hook serves the compositional and thermal simulators, whose blocks are nb = nc + 1 / 4-5 wide: those
+//    systems go to a third handle on the library's block-size-generic path, solved as those simulators solve them on
+//    the CPU (BlockCPR + GMRES, engine/src/compsim.cpp:1443-1449 with GMRES(60), engine/src/thermsim.cpp:1818-1828
+//    with GMRES(80): `genericRestart`), in FP64.
 //  * rsg::RsgBlockSolver -- the BlockSolver interface that tools/lsbench.cpp:65-81 expects from the (absent)
 //    header ressim/blocksolve.h: full scalar CSR with well rows -> well Schur complement -> device solve ->
 //    recovery of the BHPs.
@@ -36,8 +40,8 @@ public:
     enum class Role { Distributed, Refinement };
 
     explicit RsgGpuBlockSolver(int precision = RSG_FP64, int precond = kEngineChoice, int krylov = RSG_KRYLOV_BICGSTAB,
-                               Role role = Role::Distributed)
-        : precond_(precond), role_(role) {
+                               Role role = Role::Distributed, int genericRestart = 60)
+        : precond_(precond), role_(role), genericRestart_(genericRestart) {
         rsg_options o;
         rsg_default_options(&o);
         o.precision = precision;
@@ -54,6 +58,7 @@ public:
     ~RsgGpuBlockSolver() override {
         if (cpr_) rsg_destroy(cpr_);
         if (ilu_) rsg_destroy(ilu_);
+        if (gen_) rsg_destroy(gen_);
     }
     bool ok() const { return ok_; }
     const char* name() const override { return rsg_version(); }
@@ -61,8 +66,21 @@ public:
                int& iterations) override {
         std::lock_guard<std::mutex> lk(mu_);   // studies run several simulators at once: one solve per handle at a time
         iterations = 0;
-        if (!ok_ || A.nb != 3) return false;
+        if (!ok_) return false;
         rsg_solver* h = (precond_ == kEngineChoice && A.n < 500) ? ilu_ : cpr_;
+        if (A.nb != 3) {                        // compositional / thermal blocks: CPR + GMRES in FP64
+            if (!gen_) {
+                rsg_options o;
+                rsg_default_options(&o);
+                o.precision = RSG_FP64;
+                o.precond = precond_ == kEngineChoice ? RSG_PREC_CPR : precond_;
+                o.krylov = RSG_KRYLOV_GMRES;
+                o.restart = genericRestart_;
+                o.gmres_fallback = 0;
+                if (rsg_create(&gen_, &o) != RSG_OK) return false;
+            }
+            h = gen_;
+        }
         if (rsg_set_matrix(h, A.n, A.nb, A.rowPtr.data(), A.col.data(), A.val.data()) != RSG_OK) return false;
         if (rsg_setup(h, nullptr) != RSG_OK) return false;
         x.assign(size_t(A.size()), 0.0);
@@ -80,8 +98,10 @@ public:
 private:
     rsg_solver* cpr_ = nullptr;
     rsg_solver* ilu_ = nullptr;
+    rsg_solver* gen_ = nullptr;   // blocks other than 3 x 3
     int precond_;
     Role role_;
+    int genericRestart_;
     bool ok_ = false;
     double seconds_ = 0;
     std::mutex mu_;

@@ -1,6 +1,7 @@
 // C ABI of the rsg solver: handle lifecycle, uploads with pattern reuse, device set-up, Krylov drivers.
 #include "rsg.h"
 #include "rsg_impl.h"
+#include "rsg_generic.h"
 
 #include <cuda_runtime.h>
 
@@ -140,6 +141,7 @@ struct rsg_solver {
     std::vector<double> htrue;
     // launch shapes (every choice gives the same results bit for bit) and how they were chosen
     struct Tune {
+        int split = -1;              // CPR form on the thread-block path: -1 as planned (splitCpr), 0 one kernel, 1 split
         int vform = 3;
         int cpr2Threads = 256;
         std::string desc = "defaults";
@@ -154,6 +156,9 @@ struct rsg_solver {
     double* jval = nullptr;
     const double* jv = nullptr;
     double *wsB = nullptr, *wsX = nullptr, *wsBc = nullptr, *wsXc = nullptr;
+    // block sizes other than 3 (compositional / thermal callers): the block-size-generic path, one system per handle
+    GenEngine* gen = nullptr;
+    bool genActive = false;
     std::mutex mu;
 };
 
@@ -178,6 +183,8 @@ void free_plan(rsg_solver* h) {
     h->R = ReduceState{};
     h->ks = nullptr; h->d_trueres = nullptr;
     h->havePlan = h->haveMatrix = h->haveSetup = false;
+    if (h->gen) { gen_destroy(h->gen); h->gen = nullptr; }
+    h->genActive = false;
 }
 
 template <class T>
@@ -295,7 +302,7 @@ PrecDev prec_dev(rsg_solver* h) {
         M.cta = true;
         M.s64 = h->s64;
         M.s32 = h->s32;
-        M.split = M.cpr && h->splitCpr;
+        M.split = M.cpr && (h->tune.split >= 0 ? h->tune.split != 0 : h->splitCpr);
         M.vform = h->tune.vform;
         M.cpr2Threads = h->tune.cpr2Threads;
     }
@@ -375,7 +382,22 @@ int set_batch_pattern(rsg_solver* h, int nsys, const int* n, const int* const* r
 int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const* rowPtr, const int* const* col,
                  const double* const* val) {
     if (nsys < 1 || !n || !rowPtr || !col || !val) return fail(RSG_EINVAL, "set_batch: null argument or nsys < 1");
-    if (nb != NB) return fail(RSG_EINVAL, "only nb = 3 (black-oil blocks) is supported, got nb = " + std::to_string(nb));
+    if (nb != NB) {
+        // compositional (nb = nc + 1) and thermal blocks: the block-size-generic path (rsg_generic.cu)
+        if (nb < 1 || nb > GEN_MAX_NB) return fail(RSG_EINVAL, "block size nb = " + std::to_string(nb) + " outside [1, 16]");
+        if (nsys != 1) return fail(RSG_EINVAL, "block sizes other than 3 are solved one system per handle (nsys = 1)");
+        if (!h->genActive) {
+            free_plan(h);
+            h->gen = gen_create(h->stream);
+            h->genActive = true;
+        }
+        const int rc = gen_set_matrix(h->gen, h->opt, n[0], nb, rowPtr[0], col[0], val[0]);
+        if (rc) return rc;
+        h->haveMatrix = true;
+        h->haveSetup = false;
+        return RSG_OK;
+    }
+    if (h->genActive) free_plan(h);
     for (int s = 0; s < nsys; ++s)
         if (!val[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " has no values");
     std::vector<int> nnzbs;
@@ -928,21 +950,28 @@ bool fused_capturable(rsg_solver* h, const double* d_r, double* d_z) {
 
 int tune_shapes(rsg_solver* h) {
     rsg_solver::Tune t;
-    const bool split = h->opt.precond == RSG_PREC_CPR && h->cta && h->splitCpr && h->haveAmg;
+    const bool cprCta = h->opt.precond == RSG_PREC_CPR && h->cta && h->haveAmg;
+    // a single system under the automatic sweep choice: the one-kernel application (one launch, one SM) and the split
+    // form (the V-cycle's passes grid-wide) are both candidates; they give the same results bit for bit
+    const bool free_split = cprCta && h->opt.sweep == 0 && h->plan.nsys == 1;
+    const bool split = cprCta && (h->splitCpr || free_split);
+    t.split = h->splitCpr ? 1 : 0;
     t.vform = h->opt.vcycle_form ? h->opt.vcycle_form : 3;
     if (t.vform == 1 && h->amg.nPhases == 0) t.vform = 2;                  // no phase table for this hierarchy
     t.cpr2Threads = h->opt.cpr2_threads ? h->opt.cpr2_threads : 256;
     const bool free_form = h->opt.vcycle_form == 0, free_thr = h->opt.cpr2_threads == 0;
     auto describe = [](const rsg_solver::Tune& c) {
+        if (c.split == 0) return std::string("cpr_form=one-kernel");
         return std::string("vcycle_form=") + std::to_string(c.vform) + " cpr2_threads=" + std::to_string(c.cpr2Threads);
     };
     if (!split) { t.desc = "no split CPR: fixed shapes"; h->tune = t; return RSG_OK; }
-    if (!h->opt.autotune || (!free_form && !free_thr)) {
+    if (!h->opt.autotune || (!free_form && !free_thr && !free_split)) {
         t.desc = describe(t) + (h->opt.autotune ? " source=options" : " source=defaults");
         h->tune = t;
         return RSG_OK;
     }
-    const int key2 = h->opt.precision * 1000 + h->opt.vcycle_form * 10000 + h->opt.cpr2_threads + h->device * 100000;
+    const int key2 = h->opt.precision * 1000 + h->opt.vcycle_form * 10000 + h->opt.cpr2_threads + h->device * 100000 +
+                     (free_split ? 1000000 : 0);
     const auto key = std::make_pair(pattern_hash(h), key2);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -952,12 +981,18 @@ int tune_shapes(rsg_solver* h) {
     const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaMemsetAsync(h->tmp, 0, N * sizeof(double), h->stream));
     std::vector<rsg_solver::Tune> cand;
+    if (free_split) {
+        rsg_solver::Tune c;
+        c.split = 0;
+        cand.push_back(c);
+    }
     for (int f : {3, 2, 1})
         for (int thr : {256, 512}) {
             if (!free_form && f != t.vform) continue;
             if (!free_thr && thr != t.cpr2Threads) continue;
             if (f == 1 && h->amg.nPhases == 0) continue;
             rsg_solver::Tune c;
+            c.split = 1;
             c.vform = f;
             c.cpr2Threads = thr;
             cand.push_back(c);
@@ -982,7 +1017,8 @@ int tune_shapes(rsg_solver* h) {
         cudaEventElapsedTime(&ms, h->ev0, h->ev1);
         ms /= 3;
         char buf[96];
-        std::snprintf(buf, sizeof(buf), "%sform%d/%d %.3f ms", timings.empty() ? "" : ", ", c.vform, c.cpr2Threads, ms);
+        if (c.split == 0) std::snprintf(buf, sizeof(buf), "%sone-kernel %.3f ms", timings.empty() ? "" : ", ", ms);
+        else std::snprintf(buf, sizeof(buf), "%sform%d/%d %.3f ms", timings.empty() ? "" : ", ", c.vform, c.cpr2Threads, ms);
         timings += buf;
         if (ms < best) { best = ms; pick = c; }
     }
@@ -997,6 +1033,12 @@ int tune_shapes(rsg_solver* h) {
 
 int do_setup(rsg_solver* h, const double* acc) {
     if (!h->haveMatrix) return fail(RSG_ESTATE, "setup before set_matrix");
+    if (h->genActive) {
+        const int rc = gen_setup(h->gen, h->opt, acc);
+        h->haveSetup = rc == RSG_OK;
+        if (rc == RSG_OK) gen_stats(h->gen, &h->st);
+        return rc;
+    }
     h->escalated = false;
     h->st.escalated_systems = 0;
     const bool amgPrec = h->opt.precond == RSG_PREC_CPR || h->opt.precond == RSG_PREC_CPR_DEVICE;
@@ -1036,11 +1078,16 @@ int do_setup(rsg_solver* h, const double* acc) {
     return tune_shapes(h);
 }
 
+// what a captured graph depends on besides its iteration count: the preconditioner's kind and launch shapes
+int graph_kind(const PrecDev& M) {
+    return M.kind * 8 + (M.cpr ? 4 : 0) + (M.cta ? 2 : 0) + (M.split ? 1 : 0) + 16 * (M.vform + 4 * (M.cpr2Threads >= 512 ? 1 : 0));
+}
+
 int launch_iterations(rsg_solver* h, int k) {
     const PrecDev M = prec_dev(h);
     h->launches += (long long)k * (3 + 2 * precond_launches(M));
     if (h->opt.use_graphs) {
-        const int kind = M.kind;
+        const int kind = graph_kind(M);
         if (!h->gexec || h->gIters != k || h->gKind != kind) {
             if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
             cudaGraph_t g = nullptr;
@@ -1128,7 +1175,7 @@ int run_gmres(rsg_solver* h, double tol, int maxIt, bool onlyFailed) {
     int rc = ensure_gmres(h);
     if (rc) return rc;
     const PrecDev M = prec_dev(h);
-    const int kind = M.kind * 4 + (M.cpr ? 2 : 0) + (M.cta ? 1 : 0);
+    const int kind = graph_kind(M);
     if (kind != h->gmKind) { drop_gm_graphs(h); h->gmKind = kind; }
     GmState& G = h->gm;
     const int m = G.m;
@@ -1188,6 +1235,11 @@ int escalate(rsg_solver* h, double tol, int maxIt) {
 }
 
 int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
+    if (h->genActive) {
+        const int rc = gen_solve_device(h->gen, h->opt, d_b, d_x, tol, maxIt, iterations, relres);
+        gen_stats(h->gen, &h->st);
+        return rc;
+    }
     if (!h->haveSetup) return fail(RSG_ESTATE, "solve before setup");
     if (!(tol > 0) || maxIt < 0) return fail(RSG_EINVAL, "tol must be > 0 and maxIt >= 0");
     RSG_CUDA(cudaEventRecord(h->ev0, h->stream));
@@ -1563,6 +1615,11 @@ int rsg_solve(rsg_solver* h, const double* b, double* x, double tol, int maxIt, 
     if (!h || !b || !x) return fail(RSG_EINVAL, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
+    if (h->genActive) {
+        const int rc = gen_solve_host(h->gen, h->opt, b, x, tol, maxIt, iterations, relres);
+        gen_stats(h->gen, &h->st);
+        return rc;
+    }
     if (!h->havePlan) return fail(RSG_ESTATE, "solve before set_matrix");
     const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaMemcpyAsync(h->tmp, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -1577,6 +1634,7 @@ int rsg_solve_refined(rsg_solver* h, const double* b, double* x, double tol, int
     if (!h || !b || !x) return fail(RSG_EINVAL, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
+    if (h->genActive) return fail(RSG_EINVAL, "FP64 defect correction is for nb = 3 (block sizes other than 3 already solve in FP64)");
     if (!h->havePlan) return fail(RSG_ESTATE, "solve before set_matrix");
     const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaMemcpyAsync(h->tmp, b, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -1609,6 +1667,7 @@ int rsg_batch_status(rsg_solver* h, int* status) {
 int rsg_amg_level_sizes(rsg_solver* h, int maxlev, long long* rows, long long* nnz, long long* dense) {
     if (!h || maxlev < 0 || (maxlev > 0 && (!rows || !nnz))) return fail(RSG_EINVAL, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
+    if (h->genActive) return gen_amg_level_sizes(h->gen, maxlev, rows, nnz, dense);
     if (!h->haveAmg) {
         fail(RSG_ESTATE, "no CPR hierarchy (setup not run, or not a CPR preconditioner)");
         return -1;
@@ -1628,6 +1687,7 @@ int rsg_spmv_device(rsg_solver* h, const double* d_x, double* d_y) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
+    if (h->genActive) return gen_spmv_device(h->gen, d_x, d_y);
     launch_gather_vec(h->dp, d_x, h->b, h->stream);
     launch_spmv_f64(h->dp, h->val, h->b, h->xout, h->stream);
     launch_scatter_vec(h->dp, h->xout, d_y, h->stream);
@@ -1638,7 +1698,7 @@ int rsg_spmv_device(rsg_solver* h, const double* d_x, double* d_y) {
 
 // level-space SpMV on the handle's own vectors (per-kernel timing)
 int rsg_spmv_level_probe(rsg_solver* h, int reps) {
-    if (!h || !h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
+    if (!h || !h->haveMatrix || h->genActive) return fail(RSG_ESTATE, "spmv before set_matrix (nb = 3)");
     for (int r = 0; r < reps; ++r) launch_spmv_f64(h->dp, h->val, h->V.x, h->xout, h->stream);
     h->launches += reps;
     RSG_CUDA(cudaGetLastError());
@@ -1650,6 +1710,7 @@ int rsg_spmv(rsg_solver* h, const double* x, double* y) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveMatrix) return fail(RSG_ESTATE, "spmv before set_matrix");
+    if (h->genActive) return gen_spmv_host(h->gen, x, y);
     const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaMemcpyAsync(h->tmp, x, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     launch_gather_vec(h->dp, h->tmp, h->b, h->stream);
@@ -1669,6 +1730,7 @@ int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
+    if (h->genActive) return gen_precond_device(h->gen, d_r, d_z);
     launch_gather_vec(h->dp, d_r, h->b, h->stream);
     int rc = precond_apply_dev(h, h->b, h->xout);
     if (rc) return rc;
@@ -1680,7 +1742,7 @@ int rsg_precond_apply_device(rsg_solver* h, const double* d_r, double* d_z) {
 
 // level-space preconditioner application on the handle's own vectors (per-kernel timing)
 int rsg_precond_level_probe(rsg_solver* h, int reps) {
-    if (!h || !h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
+    if (!h || !h->haveSetup || h->genActive) return fail(RSG_ESTATE, "precond_apply before setup (nb = 3)");
     for (int r = 0; r < reps; ++r) {
         int rc = precond_apply_dev(h, h->b, h->xout);
         if (rc) return rc;
@@ -1693,6 +1755,7 @@ int rsg_precond_apply(rsg_solver* h, const double* r, double* z) {
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
     if (!h->haveSetup) return fail(RSG_ESTATE, "precond_apply before setup");
+    if (h->genActive) return gen_precond_host(h->gen, r, z);
     const size_t N = size_t(h->plan.n) * NB;
     RSG_CUDA(cudaMemcpyAsync(h->tmp, r, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     launch_gather_vec(h->dp, h->tmp, h->b, h->stream);
@@ -1711,6 +1774,7 @@ int rsg_get_factors(rsg_solver* h, double* lu) {
     if (!h || !lu) return fail(RSG_EINVAL, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
     cudaSetDevice(h->device);
+    if (h->genActive) return gen_get_factors(h->gen, lu);
     if (!h->haveSetup || (!h->lu && !h->luf)) return fail(RSG_ESTATE, "no BILU0 factors (setup not run, or not a BILU0 / CPR path)");
     std::vector<double> lev(size_t(h->plan.nnzb) * NB2);
     if (h->lu) {
@@ -1730,12 +1794,17 @@ int rsg_get_factors(rsg_solver* h, double* lu) {
 int rsg_tuning(rsg_solver* h, char* buf, int len) {
     if (!h || !buf || len < 1) return fail(RSG_EINVAL, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
-    std::snprintf(buf, size_t(len), "%s", h->tune.desc.c_str());
+    std::snprintf(buf, size_t(len), "%s", h->genActive ? "block-size-generic path: fixed shapes" : h->tune.desc.c_str());
     return RSG_OK;
 }
 
 int rsg_get_stats(rsg_solver* h, rsg_stats* st) {
     if (!h || !st) return fail(RSG_EINVAL, "null argument");
+    if (h->genActive) {
+        gen_stats(h->gen, st);
+        st->device_bytes += h->mem.bytes;
+        return RSG_OK;
+    }
     *st = h->st;
     st->device_bytes = h->mem.bytes + h->pmem.bytes;
     st->kernel_launches = h->launches;

@@ -5,9 +5,10 @@
 // fits in what the admitted requests leave of the budget. A small head (one SM's worth of rows) takes the small
 // requests queued behind it along, up to 64, and the slot solves them in one block-diagonal batch. Admitted requests run concurrently on their slots'
 // streams, so a request that arrives while others are on the GPU overlaps with them on the device; its matrix,
-// factors, hierarchy and Krylov state stay resident until it completes and are then freed (stream-ordered, no
-// device-wide synchronisation). A request is solved exactly as it would be alone: its own plan, deterministic
-// kernels, nothing shared with the other slots but the device.
+// factors, hierarchy and Krylov state stay resident until it completes, and the slot then keeps the plan for the
+// next request of the same pattern (counted against the budget; released, stream-ordered, when an admission needs
+// the room). A request is solved exactly as it would be alone: a plan that depends on its pattern only,
+// deterministic kernels, nothing shared with the other slots but the device.
 #include "rsg.h"
 #include "rsg_impl.h"
 
@@ -76,6 +77,15 @@ struct rsg_server {
     std::vector<rsg_solver*> handles, grid, bilu;   // per slot: the configured handle (batches of small requests), one
                                                     // with the grid-wide sweeps (larger requests), and two BILU0 handles
                                                     // (thread-block and grid-wide sweeps) for patterns CPR cannot take
+    // Resident plans: after a request (or batch) a handle keeps its plan -- pattern plan, hierarchy, factors, Krylov
+    // state -- so that the next request with the same pattern (the next Newton iteration of a simulator, or the
+    // same ensemble at the next step) only uploads values, as the engine reuses its Schur plan by pattern hash
+    // (engine/src/bsr.cpp:759-769). A resident plan counts against the budget; when an admission needs its room,
+    // the plans of idle slots are released first. cached[4 * slot + k]: bytes held by handle k of the slot
+    // (0 handles, 1 grid, 2 and 3 bilu), idle; busy[slot]: the slot is running work.
+    std::vector<size_t> cached;
+    std::vector<char> busy;
+    size_t cachedTotal = 0;
     Clock::time_point t0 = Clock::now();      // the server's clock origin (start_ms / end_ms of the results)
 };
 
@@ -125,7 +135,6 @@ void run_request(rsg_server* S, int slot, Request& R) {
     R.res.rel_residual = rr;
     R.res.true_rel_residual = rc >= 0 ? st.true_rel_residual : -1.0;
     R.res.device_bytes = st.device_bytes;
-    rsg_release(h);                                               // the request's state leaves the device
 }
 
 
@@ -182,7 +191,52 @@ void run_batch(rsg_server* S, int slot, std::vector<std::shared_ptr<Request>>& B
         R.res.slot = slot;
         R.res.batch = ns;
     }
-    rsg_release(h);
+}
+
+rsg_solver* slot_handle(rsg_server* S, int slot, int k) {
+    if (k == 0) return S->handles[size_t(slot)];
+    if (k == 1) return S->grid[size_t(slot)];
+    return S->bilu[size_t(2 * slot + (k - 2))];
+}
+
+// release idle resident plans (other slots first, then the caller's own) until `need` more bytes fit; with S->mu held
+void evict_idle(rsg_server* S, int self, size_t need) {
+    for (int pass = 0; pass < 2; ++pass)
+        for (int q = 0; q < S->slots; ++q) {
+            if ((pass == 0) == (q == self) || S->busy[size_t(q)]) continue;
+            for (int k = 0; k < 4; ++k) {
+                if (S->inUse + S->cachedTotal + need <= S->budget) return;
+                size_t& c = S->cached[size_t(4 * q + k)];
+                if (!c) continue;
+                rsg_release(slot_handle(S, q, k));
+                S->cachedTotal -= c;
+                c = 0;
+            }
+        }
+}
+
+// the work of a slot takes the resident plan of the handle it runs on over: that plan is now part of the running
+// footprint (a plan for another pattern is freed by the set-up of the new one before it allocates); the slot's other
+// handles keep theirs, still counted
+void take_cached(rsg_server* S, int slot, int k) {
+    size_t& c = S->cached[size_t(4 * slot + k)];
+    S->cachedTotal -= c;
+    c = 0;
+}
+
+// after a run: what each of the slot's handles holds stays resident (idle)
+void keep_cached(rsg_server* S, int slot) {
+    for (int k = 0; k < 4; ++k) {
+        rsg_solver* h = slot_handle(S, slot, k);
+        size_t& c = S->cached[size_t(4 * slot + k)];
+        S->cachedTotal -= c;
+        c = 0;
+        if (!h) continue;
+        rsg_stats st{};
+        rsg_get_stats(h, &st);
+        c = st.device_bytes;
+        S->cachedTotal += c;
+    }
 }
 
 void worker(rsg_server* S, int slot) {
@@ -195,9 +249,13 @@ void worker(rsg_server* S, int slot) {
                 if (S->stop) return true;
                 if (S->queue.empty() || S->hold) return false;
                 const size_t e = S->queue.front()->est;
-                return S->budget == 0 || S->inUse + e <= S->budget || S->running == 0;
+                if (S->budget == 0) return true;
+                if (S->running > 0 && S->inUse + e > S->budget) return false;
+                if (S->inUse + S->cachedTotal + e > S->budget) evict_idle(S, slot, e);
+                return true;                                      // alone on the device: admitted whatever its size
             });
             if (S->stop) return;
+            S->busy[size_t(slot)] = 1;
             B.push_back(S->queue.front());
             S->queue.pop_front();
             est = B[0]->est;
@@ -206,7 +264,7 @@ void worker(rsg_server* S, int slot) {
                 while (!S->queue.empty() && int(B.size()) < kMaxBatch) {
                     const auto& F = S->queue.front();
                     if (F->n > kBatchRows || F->tol != B[0]->tol || F->maxit != B[0]->maxit || rows + F->n > kMaxBatchRowsTotal) break;
-                    if (S->budget && S->inUse + est + F->est > S->budget) break;
+                    if (S->budget && S->inUse + S->cachedTotal + est + F->est > S->budget) break;
                     rows += F->n;
                     est += F->est;
                     B.push_back(F);
@@ -215,6 +273,7 @@ void worker(rsg_server* S, int slot) {
             }
             S->inUse += est;
             S->running += int(B.size());
+            take_cached(S, slot, B.size() == 1 && B[0]->n > kBatchRows && S->grid[size_t(slot)] ? 1 : 0);
         }
         S->cvWork.notify_all();                                   // the next head may fit as well
         const Clock::time_point t0 = Clock::now();
@@ -238,6 +297,8 @@ void worker(rsg_server* S, int slot) {
             std::lock_guard<std::mutex> lk(S->mu);
             S->inUse -= est;
             S->running -= int(B.size());
+            keep_cached(S, slot);
+            S->busy[size_t(slot)] = 0;
             for (auto& R : B) R->done = true;
         }
         S->cvDone.notify_all();
@@ -261,6 +322,8 @@ int rsg_server_create(rsg_server** out, const rsg_options* opts, int slots, size
     S->slots = slots;
     S->budget = mem_budget;
     S->handles.assign(size_t(slots), nullptr);
+    S->cached.assign(size_t(4 * slots), 0);
+    S->busy.assign(size_t(slots), 0);
     S->grid.assign(size_t(slots), nullptr);
     S->bilu.assign(size_t(2 * slots), nullptr);
     rsg_options og = S->opt;
@@ -376,7 +439,7 @@ int rsg_server_load(rsg_server* S, int* queued, int* running, size_t* bytes) {
     std::lock_guard<std::mutex> lk(S->mu);
     if (queued) *queued = int(S->queue.size());
     if (running) *running = S->running;
-    if (bytes) *bytes = S->inUse;
+    if (bytes) *bytes = S->inUse + S->cachedTotal;
     return RSG_OK;
 }
 

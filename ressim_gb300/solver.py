@@ -85,6 +85,7 @@ class DeviceSolver:
     def set_matrix(self, A: BSR):
         _lib.check(self.L.rsg_set_matrix(self.h, A.n, A.nb, _lib.ptr(A.rowPtr), _lib.ptr(A.col), _lib.ptr(A.val)))
         self.n = A.n * A.nb
+        self.nb = A.nb
         self.nsys = 1
         self.sizes = [A.n * A.nb]
 
@@ -210,7 +211,8 @@ class DeviceSolver:
         _lib.check(self.L.rsg_precond_apply_device(self.h, C.c_void_p(d_r), C.c_void_p(d_z)))
 
     def factors(self, nnzb: int):
-        lu = np.zeros(nnzb * 9)
+        """BILU0 factors in the caller's block order (nnzb blocks of nb x nb)."""
+        lu = np.zeros(nnzb * getattr(self, "nb", 3) ** 2)
         _lib.check(self.L.rsg_get_factors(self.h, _lib.ptr(lu)))
         return lu
 
@@ -286,7 +288,7 @@ class Server:
 
     def hold(self, on: bool = True):
         """Pause (or resume) admission: requests submitted while held are admitted together (rsg_server_hold)."""
-        _lib.check(self.L.rsg_server_hold(self.h, 1 if on else 0))
+        _lib.check(self.L.rsg_server_hold(self.s, 1 if on else 0))
 
     def load(self):
         q, rn, by = C.c_int(0), C.c_int(0), C.c_size_t(0)

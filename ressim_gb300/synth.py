@@ -100,12 +100,16 @@ def _corey(sw, sg):
 
 def make_system(nx, ny, nz, *, sigma=1.0, corr=(5, 5, 1), seed=0, dx=100.0, dy=100.0, dz=20.0, kmean=100.0,
                 actnum_fraction=0.0, channels=None, wells="corners+center", n_wells=None, dt=1.0, porosity=None,
-                with_full=False, xtrue_seed=None, front_radius=0.5) -> NewtonSystem:
+                with_full=False, xtrue_seed=None, front_radius=0.5, gravity_head=False, p_noise=5.0) -> NewtonSystem:
     """Build one Schur-reduced black-oil Newton system.
 
     channels: None or (first_layer, last_layer, width, multiplier) (layers zero-based inclusive).
     wells: "corners+center" (central water injector + 4 corner producers, all layers, as tools/gen_bigcase.py:44-52),
            "diagonal" (injector at (0,0), producer at (nx-1,ny-1), all layers), or "random" (n_wells seeded columns).
+    gravity_head: upwind and flux by the flow potential p - 0.45 psi/ft x depth (the hydrostatic gradient of the
+           initial pressure), so that vertical connections carry only the well-driven part of the pressure field, as in
+           a simulator's state at equilibrium; False: by the pressure difference alone.
+    p_noise: standard deviation (psi) of the per-cell pressure perturbation.
     """
     rng = np.random.default_rng(seed)
     shape = (nz, ny, nx)
@@ -154,7 +158,7 @@ def make_system(nx, ny, nz, *, sigma=1.0, corr=(5, 5, 1), seed=0, dx=100.0, dy=1
             front = np.maximum(front, 1.0 / (1.0 + np.exp((r - front_radius * L) / (0.1 * L))))
         else:
             p = p - 400.0 * np.exp(-r / L)
-    p = p + 5.0 * rng.standard_normal(na)
+    p = p + p_noise * rng.standard_normal(na)
     sw = SWC + (1 - SWC - SOR) * front * (0.8 + 0.2 * rng.random(na))
     sw = np.clip(sw + 0.02 * rng.random(na), SWC, 1 - SOR - 1e-3)
     sg = np.where(kk_ < max(1, nz // 4), 0.1 * rng.random(na) * (1.0 - front), 0.0)
@@ -199,6 +203,8 @@ def make_system(nx, ny, nz, *, sigma=1.0, corr=(5, 5, 1), seed=0, dx=100.0, dy=1
     cb = np.concatenate([c[1] for c in conns])
     cT = np.concatenate([c[2] for c in conns])
     dpc = p[cb] - p[ca]                                   # flow from a to b when dpc < 0
+    if gravity_head:
+        dpc = dpc - 0.45 * (depth[cb] - depth[ca])
     up = np.where(dpc < 0, ca, cb)
     lam_u = lam[up]                                        # (nc, 3)
     dsw_u = dlsw[up]
@@ -406,3 +412,82 @@ def serving_request(rng: np.random.Generator, cells_lo=1e3, cells_hi=1e6, max_ce
     ny = max(1, area // nx)
     return make_system(nx, ny, nz, sigma=float(rng.uniform(0.5, 3.0)), seed=int(rng.integers(0, 2**31 - 1)),
                        dt=float(rng.uniform(0.1, 30.0)), wells="random", n_wells=int(rng.integers(1, 9)))
+
+
+def make_block_system(nx, ny, nz, nb, *, sigma=1.0, seed=0, dt=5.0, well_columns=2) -> NewtonSystem:
+    """A Newton system with nb unknowns per cell (pressure first, then nb - 1 transported quantities: component
+    moles of a compositional model, or saturations and temperature of a thermal one), for the block-size-generic
+    path. Same structure as ``make_system``: 7-point TPFA connections with harmonic-mean transmissibilities of a
+    log-normal permeability, upstream-weighted mobilities of every equation with their derivatives in the transported
+    unknowns, accumulation blocks scaled by PV / dt (the true-IMPES ``acc``), and ``well_columns`` columns of cells
+    coupled to each other (the fill a well's Schur complement adds), so that some rows carry more than the stencil's
+    seven blocks. b = S x_true with a manufactured x_true."""
+    rng = np.random.default_rng(seed)
+    shape = (nz, ny, nx)
+    k = np.exp(math.log(100.0) + sigma * correlated_normal(shape, (5, 5, 1), rng)).reshape(-1)
+    n = nx * ny * nz
+    kk_, jj_, ii_ = np.unravel_index(np.arange(n), shape)
+    p = 3000.0 + 0.45 * 20.0 * (kk_ + 0.5) - 300.0 * np.exp(-np.hypot(ii_ - nx / 2.0, jj_ - ny / 2.0) / max(nx, ny))
+    mob = rng.uniform(0.2, 1.0, size=(n, nb))                # mobility of every equation's quantity
+    dmob = 0.05 * rng.standard_normal(size=(n, nb, nb - 1))  # its derivative in the transported unknowns
+    pv = 0.2 * 100.0 * 100.0 * 20.0 / 5.615
+    acc = np.zeros((n, nb, nb))
+    acc[:, :, 0] = 0.05 * rng.uniform(0.5, 1.5, size=(n, nb))     # compressibility terms
+    acc[:, :, 1:] = 0.1 * rng.standard_normal(size=(n, nb, nb - 1))
+    for e in range(1, nb):
+        acc[:, e, e] += 1.0
+    acc[:, 0, 1:] += 0.5 / (nb - 1)                            # the pressure equation sums the quantities
+    scale = dt / pv
+    conns = []
+    for (di, dj, dk, area, dist, kz) in ((1, 0, 0, 2000.0, 100.0, 1.0), (0, 1, 0, 2000.0, 100.0, 1.0), (0, 0, 1, 1e4, 20.0, 0.1)):
+        m = np.ones(shape, dtype=bool)
+        if di:
+            m[:, :, -1] = False
+        if dj:
+            m[:, -1, :] = False
+        if dk:
+            m[-1, :, :] = False
+        a = np.nonzero(m.reshape(-1))[0]
+        b_ = a + di + dj * nx + dk * nx * ny
+        kh = 2.0 / (1.0 / (kz * k[a]) + 1.0 / (kz * k[b_]))
+        conns.append((a, b_, 0.001127 * kh * area / dist))
+    ca = np.concatenate([c[0] for c in conns])
+    cb = np.concatenate([c[1] for c in conns])
+    T = np.concatenate([c[2] for c in conns])
+    dp = p[cb] - p[ca]
+    up = np.where(dp < 0, ca, cb)
+    ua = (up == ca)[:, None, None]
+    nc = ca.size
+    blk_ab = np.zeros((nc, nb, nb))
+    blk_ab[:, :, 0] = -(T[:, None] * mob[up])
+    dS = -(T * dp)[:, None, None] * dmob[up]
+    blk_ab[:, :, 1:] += np.where(ua, 0.0, dS)
+    blk_aa = np.zeros((nc, nb, nb))
+    blk_aa[:, :, 0] = T[:, None] * mob[up]
+    blk_aa[:, :, 1:] += np.where(ua, dS, 0.0)
+    diag = acc.copy()
+    np.add.at(diag, ca, scale * blk_aa)
+    np.add.at(diag, cb, scale * blk_aa)
+    rows, cols, vals = [np.arange(n), ca, cb], [np.arange(n), cb, ca], [diag, scale * blk_ab, scale * blk_ab]
+    for w in range(well_columns):
+        i0, j0 = int(rng.integers(0, nx)), int(rng.integers(0, ny))
+        cells = (np.arange(nz) * ny + j0) * nx + i0
+        m = cells.size
+        f = 0.05 * rng.standard_normal(size=(m, m, nb, nb)) * scale
+        rows.append(np.repeat(cells, m)); cols.append(np.tile(cells, m)); vals.append(f.reshape(m * m, nb, nb))
+    R = np.concatenate(rows).astype(np.int64)
+    Cc = np.concatenate(cols).astype(np.int64)
+    V = np.concatenate(vals, axis=0)
+    key = R * n + Cc
+    order = np.argsort(key, kind="stable")
+    uniq, start = np.unique(key[order], return_index=True)
+    Vs = np.add.reduceat(V[order], start, axis=0)
+    ur = (uniq // n).astype(np.int32)
+    rowPtr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rowPtr, ur + 1, 1)
+    A = BSR(n, nb, np.cumsum(rowPtr).astype(np.int32), (uniq % n).astype(np.int32), Vs.reshape(-1))
+    xt = rng.standard_normal(n * nb)
+    xt[0::nb] *= 20.0
+    b = bsr_matvec_host(A, xt)
+    return NewtonSystem(A, b, acc=acc.reshape(-1), na=n, nv=nb, nw=0, x_true=xt,
+                        meta=dict(nx=nx, ny=ny, nz=nz, nb=nb, sigma=sigma, seed=seed, dt=dt))

@@ -131,3 +131,51 @@ def test_lsbench_on_engine_dump(harness, tmp_path):
     for v, cpr, wp, its, res, conv, levels in rows:
         assert conv == "1" and float(res) <= 1e-6, r.stdout
         assert (int(levels) > 0) == (cpr == "1")
+
+
+# ---------------------------------------------------------------- the compositional and thermal callers
+@pytest.fixture(scope="module")
+def harness_nb():
+    if not os.path.exists(STAGED):
+        pytest.skip("reference engine sources not staged (make -f oracle/Makefile.ref stage REF=...)")
+    decks = os.path.join(REF, "src", "examples")
+    if not os.path.isdir(decks):
+        pytest.skip("reference example decks not staged")
+    jobs = str(max(2, os.cpu_count() or 2))
+    r = subprocess.run(["make", "-f", "oracle/Makefile.ref", "-j" + jobs, "oracle/_ref/ref_run_nb"], cwd=ROOT, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    return REF
+
+
+def run_nb(harness, kind, deck, mode, steps=3):
+    r = subprocess.run([os.path.join(harness, "ref_run_nb"), kind, os.path.join(harness, "src", "examples", deck), str(steps), mode],
+                       capture_output=True, text=True, env=dict(os.environ, OMP_NUM_THREADS="1"), timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    steps_out, run = [], {}
+    for line in r.stdout.splitlines():
+        f = line.split()
+        if line.startswith("ts "):
+            steps_out.append({f[i]: float(f[i + 1]) for i in range(1, len(f) - 1, 2)})
+        elif line.startswith("run "):
+            run = {f[i]: int(f[i + 1]) for i in range(1, len(f) - 1, 2)}
+    return steps_out, run
+
+
+@pytest.mark.parametrize("kind,deck", [("comp", "COMP.DATA"), ("thermal", "STEAMFLOOD.DATA")])
+def test_other_callers_run_with_gpu_solver(harness_nb, kind, deck):
+    """The reference's compositional (nb = 8) and thermal (nb = 5) simulators with the GPU solver in their solver hook
+    (the block-size-generic path: BlockCPR + GMRES(60) / GMRES(80) in FP64): every Newton system is solved on the
+    device, and the run reproduces the stock run -- the same time steps, Newton iterations and time-step cuts, and
+    summaries within 2e-5 relative. Each linear solve of either run meets the caller's tolerance (1e-5 / 1e-6 relative
+    residual) with a different Krylov trajectory, so every Newton update differs at that level and the cumulative
+    quantities, which integrate the updates over the run, agree to about ten times it (measured: 5e-6 on the thermal
+    run's water production, 1e-7 and below elsewhere)."""
+    s_cpu, run_cpu = run_nb(harness_nb, kind, deck, "cpu")
+    s_gpu, run_gpu = run_nb(harness_nb, kind, deck, "gpu")
+    assert run_gpu["hook_calls"] > 0 and run_gpu["hook_solved"] == run_gpu["hook_calls"]
+    assert run_cpu["steps"] == run_gpu["steps"] and run_cpu["newton"] == run_gpu["newton"] and run_cpu["cuts"] == run_gpu["cuts"]
+    assert len(s_cpu) == len(s_gpu) > 0
+    for a, b in zip(s_cpu, s_gpu):
+        assert a["time"] == b["time"]
+        for k in a:
+            assert abs(a[k] - b[k]) <= 2e-5 * max(abs(a[k]), 1.0), (k, a[k], b[k])

@@ -105,4 +105,26 @@ def test_poll_without_wait_and_load():
             if len(done) == len(ids):
                 break
         assert len(done) == len(ids)
-        assert s.load() == (0, 0, 0)
+        q, running, resident = s.load()
+        assert (q, running) == (0, 0)
+        assert resident >= 0                     # the idle slots' resident plans (released when an admission needs room)
+
+
+def test_held_requests_are_admitted_together():
+    """Requests submitted while admission is held (rsg_server_hold) wait in the queue and are then solved as one batch,
+    each with the result it has alone."""
+    from ressim_gb300.solver import Server
+    reqs = requests(5, seed=31, lo=1e3, hi=1.2e4)
+    with Server(slots=1, precond="cpr", precision="mixed_f32") as s:
+        alone = [s.poll(s.submit(r.A, r.b, tol=1e-6, maxit=500)) for r in reqs]
+    with Server(slots=1, precond="cpr", precision="mixed_f32") as s:
+        s.hold(True)
+        ids = [s.submit(r.A, r.b, tol=1e-6, maxit=500) for r in reqs]
+        q, running, _ = s.load()
+        assert running == 0 and q == len(reqs)                          # nothing admitted while held
+        s.hold(False)
+        mix = [s.poll(i) for i in ids]
+    assert max(rm["batch"] for _, rm in mix) == len(reqs)
+    for (xa, ra), (xm, rm) in zip(alone, mix):
+        assert ra["status"] == rm["status"] and ra["iterations"] == rm["iterations"]
+        assert np.array_equal(xa, xm, equal_nan=True)
