@@ -215,6 +215,16 @@ int alloc_plan(rsg_solver* h) {
         (rc = upload(M, reinterpret_cast<int**>(&D.Uslot), P.Uslot, st)) || (rc = upload(M, &D.UslotSrc, P.UslotSrc, st)) ||
         (rc = upload(M, &D.UovCol, P.UovCol, st)) || (rc = upload(M, &D.UovSrc, P.UovSrc, st)) || (rc = upload(M, &D.Dsrc, P.Dsrc, st)))
         return rc;
+    {   // (first row, rows) of every row's forward level: the component-major layout of the sweep records
+        std::vector<int> rl(size_t(P.n) * 2, 0);
+        for (int sy = 0; sy < P.nsys; ++sy)
+            for (int q = P.sysLvl0[size_t(sy)]; q + 1 < P.sysLvl0[size_t(sy) + 1]; ++q)
+                for (int k = P.lvlStart[size_t(q)]; k < P.lvlStart[size_t(q) + 1]; ++k) {
+                    rl[size_t(k) * 2] = P.lvlStart[size_t(q)];
+                    rl[size_t(k) * 2 + 1] = P.lvlStart[size_t(q) + 1] - P.lvlStart[size_t(q)];
+                }
+        if ((rc = upload(M, reinterpret_cast<int**>(&D.rowLevel), rl, st))) return rc;
+    }
     D.spmvFma = h->opt.fma != 0;
     D.nLov = int(P.LovCol.size());
     D.nUov = int(P.UovCol.size());

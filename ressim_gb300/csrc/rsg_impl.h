@@ -310,13 +310,16 @@ struct DevPlan {
     int4 *Lslot = nullptr, *Uslot = nullptr;
     int *LslotSrc = nullptr, *UslotSrc = nullptr, *LovCol = nullptr, *LovSrc = nullptr, *UovCol = nullptr, *UovSrc = nullptr;
     int* Dsrc = nullptr;
+    int2* rowLevel = nullptr;         // level-space row -> (first row of its forward level, rows of that level)
     int nLov = 0, nUov = 0, maxSysRows = 0;
     int sweepBlocks = 0;              // persistent grid of the sync-free sweeps (0: sized from n)
     bool spmvFma = true;              // SpMV with fused multiply-adds (else the reference's rounding, bitwise)
 };
 
 // Slot-layout factors for the CTA-per-system sweeps (FP64 or FP32 storage): L = n x LREC, UD = n x UREC,
-// Lov / Uov = overflow blocks (9 values each).
+// Lov / Uov = overflow blocks (9 values each). The records of a forward level (its rows are contiguous in level
+// space: [s, s + w)) fill [s * LREC, (s + w) * LREC) of L component-major: value j of row k at s * LREC + j * w + (k - s),
+// so the threads of consecutive rows read consecutive words (coalesced) when they load their records; UD likewise.
 template <class T>
 struct SplitFactors {
     T *L = nullptr, *UD = nullptr, *Lov = nullptr, *Uov = nullptr;

@@ -94,6 +94,13 @@ __device__ __forceinline__ void ldrec(int (&a)[N], const int* p) {
         a[4 * i] = t.x; a[4 * i + 1] = t.y; a[4 * i + 2] = t.z; a[4 * i + 3] = t.w;
     }
 }
+// N values of a row record stored component-major with stride w (the rows of its level): coalesced across the
+// threads of consecutive rows
+template <class T, int N>
+__device__ __forceinline__ void ldrec_cm(T (&a)[N], const T* p, int w) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) a[i] = __ldg(p + size_t(i) * size_t(w));
+}
 __device__ __forceinline__ int slot_col(const int4& c, int j) { return j == 0 ? c.x : (j == 1 ? c.y : c.z); }
 
 // ------------------------------------------------------------------ BILU0 sweeps on slot records
@@ -121,13 +128,14 @@ struct BwdRow {
     double xp;
 };
 
+// row k of the level [ls, ls + lw) (component-major records)
 template <class TF, class TI, int MODE>
-__device__ __forceinline__ void load_fwd(FwdRow<TF, TI, MODE>& R, int k, const IluArgs<TF>& F, const TI* r, const double* pv,
-                                         const double* v) {
+__device__ __forceinline__ void load_fwd(FwdRow<TF, TI, MODE>& R, int k, int ls, int lw, const IluArgs<TF>& F, const TI* r,
+                                         const double* pv, const double* v) {
     R.k = k;
     if (k < 0) return;
     R.c = __ldg(F.Lslot + k);
-    ldrec(R.a, F.L + size_t(k) * LREC);
+    ldrec_cm(R.a, F.L + size_t(ls) * LREC + size_t(k - ls), lw);
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
         const size_t q = size_t(k) * 3 + e;
@@ -137,11 +145,11 @@ __device__ __forceinline__ void load_fwd(FwdRow<TF, TI, MODE>& R, int k, const I
     }
 }
 template <class TF, class TX>
-__device__ __forceinline__ void load_bwd(BwdRow<TF>& R, int k, const IluArgs<TF>& F, const TX* xp, int row0) {
+__device__ __forceinline__ void load_bwd(BwdRow<TF>& R, int k, int ls, int lw, const IluArgs<TF>& F, const TX* xp, int row0) {
     R.k = k;
     if (k < 0) return;
     R.c = __ldg(F.Uslot + k);
-    ldrec(R.a, F.UD + size_t(k) * UREC);
+    ldrec_cm(R.a, F.UD + size_t(ls) * UREC + size_t(k - ls), lw);
     if (xp) R.xp = double(xp[k - row0]);
 }
 
@@ -265,18 +273,18 @@ __device__ __forceinline__ void fwd_level(const IluArgs<TF>& F, const int* lv, i
     if (L + 1 < nl) {
         const int e1 = lv[L + 2];
 #pragma unroll
-        for (int j = 0; j < NSET; ++j) load_fwd(nxt[j], row_of<NSET>(e, e1, j), F, r, pv, v);
+        for (int j = 0; j < NSET; ++j) load_fwd(nxt[j], row_of<NSET>(e, e1, j), e, e1 - e, F, r, pv, v);
     }
 #pragma unroll
     for (int j = 0; j < NSET; ++j) {
         const int k = row_of<NSET>(s, e, j);
         if (k >= 0) {
-            if (cur[j].k != k) load_fwd(cur[j], k, F, r, pv, v);
+            if (cur[j].k != k) load_fwd(cur[j], k, s, e - s, F, r, pv, v);
             fwd_step<TF, TV, TI, MODE>(cur[j], F, row0, y, pv, beta, omega, alpha);
         }
     }
     for (int k = s + int(threadIdx.x) + NSET * int(blockDim.x); k < e; k += blockDim.x) {
-        load_fwd(cur[0], k, F, r, pv, v);
+        load_fwd(cur[0], k, s, e - s, F, r, pv, v);
         fwd_step<TF, TV, TI, MODE>(cur[0], F, row0, y, pv, beta, omega, alpha);
     }
     __syncthreads();
@@ -290,18 +298,18 @@ __device__ __forceinline__ void bwd_level(const IluArgs<TF>& F, const int* lv, i
     if (L > 0) {
         const int s1 = lv[L - 1];
 #pragma unroll
-        for (int j = 0; j < NSET; ++j) load_bwd(nxt[j], row_of<NSET>(s1, s, j), F, xp, row0);
+        for (int j = 0; j < NSET; ++j) load_bwd(nxt[j], row_of<NSET>(s1, s, j), s1, s - s1, F, xp, row0);
     }
 #pragma unroll
     for (int j = 0; j < NSET; ++j) {
         const int k = row_of<NSET>(s, e, j);
         if (k >= 0) {
-            if (cur[j].k != k) load_bwd(cur[j], k, F, xp, row0);
+            if (cur[j].k != k) load_bwd(cur[j], k, s, e - s, F, xp, row0);
             bwd_step<TF, TV, XP>(cur[j], F, row0, y, z, writeZ);
         }
     }
     for (int k = s + int(threadIdx.x) + NSET * int(blockDim.x); k < e; k += blockDim.x) {
-        load_bwd(cur[0], k, F, xp, row0);
+        load_bwd(cur[0], k, s, e - s, F, xp, row0);
         bwd_step<TF, TV, XP>(cur[0], F, row0, y, z, writeZ);
     }
     __syncthreads();
@@ -332,7 +340,7 @@ __device__ void ilu_body(const IluArgs<TF>& F, int row0, const int* lv, int nl, 
         if (nl > 0) {
             const int s = lv[0], e = lv[1];
 #pragma unroll
-            for (int j = 0; j < NSET; ++j) load_fwd(A[j], row_of<NSET>(s, e, j), F, r, pv, v);
+            for (int j = 0; j < NSET; ++j) load_fwd(A[j], row_of<NSET>(s, e, j), s, e - s, F, r, pv, v);
         }
         for (int L = 0; L < nl; L += 2) {
             fwd_level<TF, TV, TI, MODE, NSET>(F, lv, L, nl, A, B, row0, r, pv, v, y, beta, omega, alpha);
@@ -347,7 +355,7 @@ __device__ void ilu_body(const IluArgs<TF>& F, int row0, const int* lv, int nl, 
         if (nl > 0) {
             const int s = lv[nl - 1], e = lv[nl];
 #pragma unroll
-            for (int j = 0; j < NSET; ++j) load_bwd(A[j], row_of<NSET>(s, e, j), F, xq, row0);
+            for (int j = 0; j < NSET; ++j) load_bwd(A[j], row_of<NSET>(s, e, j), s, e - s, F, xq, row0);
         }
         for (int L = nl - 1; L >= 0; L -= 2) {
             bwd_level<TF, TV, XP, NSET>(F, lv, L, A, B, row0, xq, y, z, writeZ);
@@ -369,7 +377,7 @@ __device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl,
         FwdRow<TF, TI, IN_PLAIN> R[3];
 #pragma unroll
         for (int b = 0; b < 2; ++b)
-            if (b < nl) load_fwd(R[b], row_of<1>(lv[b], lv[b + 1], 0), F, r, nullptr, nullptr);
+            if (b < nl) load_fwd(R[b], row_of<1>(lv[b], lv[b + 1], 0), lv[b], lv[b + 1] - lv[b], F, r, nullptr, nullptr);
         for (int L0 = 0; L0 < nl; L0 += 3) {
 #pragma unroll
             for (int b = 0; b < 3; ++b) {                    // level L0 + b works on R[b], loads level + 2 into R[(b + 2) % 3]
@@ -377,14 +385,14 @@ __device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl,
                 if (L >= nl) break;
                 const int s = lv[L], e = lv[L + 1];
                 if (threadIdx.x == 0 && L + kAhead < nl) prefetch_fwd_level<TF, TI, IN_PLAIN>(F, lv, L + kAhead, r, nullptr, nullptr);
-                if (L + 2 < nl) load_fwd(R[(b + 2) % 3], row_of<1>(lv[L + 2], lv[L + 3], 0), F, r, nullptr, nullptr);
+                if (L + 2 < nl) load_fwd(R[(b + 2) % 3], row_of<1>(lv[L + 2], lv[L + 3], 0), lv[L + 2], lv[L + 3] - lv[L + 2], F, r, nullptr, nullptr);
                 const int k = row_of<1>(s, e, 0);
                 if (k >= 0) {
-                    if (R[b].k != k) load_fwd(R[b], k, F, r, nullptr, nullptr);
+                    if (R[b].k != k) load_fwd(R[b], k, s, e - s, F, r, nullptr, nullptr);
                     fwd_step<TF, TV, TI, IN_PLAIN>(R[b], F, row0, y, nullptr, 0, 0, 0);
                 }
                 for (int k2 = s + int(threadIdx.x) + nt; k2 < e; k2 += nt) {
-                    load_fwd(R[b], k2, F, r, nullptr, nullptr);
+                    load_fwd(R[b], k2, s, e - s, F, r, nullptr, nullptr);
                     fwd_step<TF, TV, TI, IN_PLAIN>(R[b], F, row0, y, nullptr, 0, 0, 0);
                 }
                 __syncthreads();
@@ -398,7 +406,7 @@ __device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl,
         BwdRow<TF> R[3];
 #pragma unroll
         for (int b = 0; b < 2; ++b)
-            if (b < nl) load_bwd(R[b], row_of<1>(lv[nl - 1 - b], lv[nl - b], 0), F, xq, row0);
+            if (b < nl) load_bwd(R[b], row_of<1>(lv[nl - 1 - b], lv[nl - b], 0), lv[nl - 1 - b], lv[nl - b] - lv[nl - 1 - b], F, xq, row0);
         for (int g0 = 0; g0 < nl; g0 += 3) {
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
@@ -407,14 +415,14 @@ __device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl,
                 const int L = nl - 1 - g;
                 const int s = lv[L], e = lv[L + 1];
                 if (threadIdx.x == 0 && L - kAhead >= 0) prefetch_bwd_level(F, lv, L - kAhead);
-                if (L - 2 >= 0) load_bwd(R[(b + 2) % 3], row_of<1>(lv[L - 2], lv[L - 1], 0), F, xq, row0);
+                if (L - 2 >= 0) load_bwd(R[(b + 2) % 3], row_of<1>(lv[L - 2], lv[L - 1], 0), lv[L - 2], lv[L - 1] - lv[L - 2], F, xq, row0);
                 const int k = row_of<1>(s, e, 0);
                 if (k >= 0) {
-                    if (R[b].k != k) load_bwd(R[b], k, F, xq, row0);
+                    if (R[b].k != k) load_bwd(R[b], k, s, e - s, F, xq, row0);
                     bwd_step<TF, TV, XP>(R[b], F, row0, y, z, writeZ);
                 }
                 for (int k2 = s + int(threadIdx.x) + nt; k2 < e; k2 += nt) {
-                    load_bwd(R[b], k2, F, xq, row0);
+                    load_bwd(R[b], k2, s, e - s, F, xq, row0);
                     bwd_step<TF, TV, XP>(R[b], F, row0, y, z, writeZ);
                 }
                 __syncthreads();
@@ -1182,18 +1190,20 @@ __global__ void __launch_bounds__(kCtaThreads) k_factor_cta_f32(const int* __res
 template <class T>
 __global__ void k_pack(int n, int nLov, int nUov, const int* __restrict__ LslotSrc, const int* __restrict__ UslotSrc,
                        const int* __restrict__ Dsrc, const int* __restrict__ LovSrc, const int* __restrict__ UovSrc,
-                       const T* __restrict__ lu, T* L, T* UD, T* Lov, T* Uov) {
+                       const int2* __restrict__ rowLevel, const T* __restrict__ lu, T* L, T* UD, T* Lov, T* Uov) {
     const size_t nL = size_t(n) * LREC, nUD = size_t(n) * UREC, nO = (size_t(nLov) + size_t(nUov)) * 9;
     const size_t total = nL + nUD + nO;
     for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < total; q += size_t(gridDim.x) * blockDim.x) {
-        if (q < nL) {
+        if (q < nL) {                                  // value e of row k, component-major within k's level
             const size_t k = q / LREC, e = q % LREC, j = e / 9;
+            const int2 lw = __ldg(rowLevel + k);
             const int src = j < size_t(SLOTS) ? __ldg(LslotSrc + k * SLOTS + j) : -1;
-            L[q] = src >= 0 ? lu[size_t(src) * 9 + e % 9] : T(0);
+            L[size_t(lw.x) * LREC + e * size_t(lw.y) + (k - size_t(lw.x))] = src >= 0 ? lu[size_t(src) * 9 + e % 9] : T(0);
         } else if (q < nL + nUD) {
             const size_t q2 = q - nL, k = q2 / UREC, e = q2 % UREC, j = e / 9;
+            const int2 lw = __ldg(rowLevel + k);
             const int src = j < size_t(SLOTS) ? __ldg(UslotSrc + k * SLOTS + j) : __ldg(Dsrc + k);
-            UD[q2] = src >= 0 ? lu[size_t(src) * 9 + e % 9] : T(0);
+            UD[size_t(lw.x) * UREC + e * size_t(lw.y) + (k - size_t(lw.x))] = src >= 0 ? lu[size_t(src) * 9 + e % 9] : T(0);
         } else {
             const size_t q3 = q - nL - nUD, b = q3 / 9, e = q3 % 9;
             if (b < size_t(nLov)) {
@@ -1255,14 +1265,14 @@ bool cta_sweep_supported(const DevPlan& P, const HostPlan& H) {
 void launch_pack_f64(const DevPlan& P, const double* lu, SplitFactors<double>& F, cudaStream_t st) {
     const size_t total = size_t(P.n) * (LREC + UREC) + (size_t(P.nLov) + size_t(P.nUov)) * 9;
     const int grid = int(std::min<size_t>((total + 255) / 256, size_t(device_sm_count()) * 16));
-    k_pack<double><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, lu, F.L, F.UD, F.Lov,
-                                         F.Uov);
+    k_pack<double><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, P.rowLevel, lu, F.L,
+                                         F.UD, F.Lov, F.Uov);
 }
 void launch_pack_f32(const DevPlan& P, const float* luf, SplitFactors<float>& F, cudaStream_t st) {
     const size_t total = size_t(P.n) * (LREC + UREC) + (size_t(P.nLov) + size_t(P.nUov)) * 9;
     const int grid = int(std::min<size_t>((total + 255) / 256, size_t(device_sm_count()) * 16));
-    k_pack<float><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, luf, F.L, F.UD, F.Lov,
-                                        F.Uov);
+    k_pack<float><<<grid, 256, 0, st>>>(P.n, P.nLov, P.nUov, P.LslotSrc, P.UslotSrc, P.Dsrc, P.LovSrc, P.UovSrc, P.rowLevel, luf, F.L,
+                                        F.UD, F.Lov, F.Uov);
 }
 
 void launch_factor_cta_f32(const DevPlan& P, const double* val, float* luf, int* nreg, cudaStream_t st) {

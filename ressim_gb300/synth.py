@@ -382,10 +382,12 @@ def spe10_like(day: int = 1, seed: int = 0, nx=60, ny=220, nz=85) -> NewtonSyste
     phi = 0.05 + 0.02 ln k, central injector + 4 corner producers in all layers. ``day`` is the simulated time of the
     Jacobian: the run's own step there (run_step: 1 day on day 1, 30.4 days by day 100) and a water front that has
     grown with the injected volume (radius proportional to the square root of time, half the reservoir scale at
-    day 100)."""
+    day 100). Fluxes are upwinded by the flow potential (pressure less the hydrostatic head) of a smooth pressure
+    field (0.5 psi cell-to-cell perturbation), as in a simulator's state near equilibrium, so that the vertical
+    connections of the thin (2 ft) layers carry only the well-driven flow."""
     return make_system(nx, ny, nz, sigma=2.5, corr=(5, 5, 1), seed=seed, dx=20.0, dy=10.0, dz=2.0,
                        channels=(35, 84, 4, 100.0), wells="corners+center", dt=run_step(day),
-                       front_radius=0.5 * math.sqrt(day / 100.0))
+                       front_radius=0.5 * math.sqrt(day / 100.0), gravity_head=True, p_noise=0.5)
 
 
 def ensemble_member(r: int, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0, dt: float = 10.0):
