@@ -345,6 +345,20 @@ def spe10_report(local):
                     x64 = sol[("fp64", tol)]
                     e["rel_diff_vs_fp64"] = float(np.linalg.norm(x - x64) / np.linalg.norm(x64))
                 out["solves"].append(e)
+        # the precision form inside FP64 defect correction (rsg_solve_refined: the engine's refineWithDevice with the
+        # FP32-preconditioned GMRES(30) as its inner solve)
+        for tol in (1e-6, 1e-8):
+            with DeviceSolver(precond="cpr", krylov="gmres", restart=30, precision="mixed_f32", device=local) as d:
+                d.set_matrix(s.A)
+                d.setup(s.acc)
+                d.setup(s.acc)
+                x, res = d.solve_refined(s.b, tol=tol, max_outer=10, inner_it=600)
+                st = d.stats()
+            tr = float(np.linalg.norm(s.b - synth.bsr_matvec_host(s.A, x)) / np.linalg.norm(s.b))
+            x64 = sol[("fp64", tol)]
+            out["solves"].append({"day": day, "precision": "mixed_f32_refined", "tol": tol, "converged": bool(res.converged),
+                                  "iterations": res.iterations, "setup_ms": st.setup_ms, "solve_ms": st.solve_ms, "true_relres": tr,
+                                  "rel_diff_vs_fp64": float(np.linalg.norm(x - x64) / np.linalg.norm(x64))})
     return out
 
 

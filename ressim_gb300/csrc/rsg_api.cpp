@@ -1343,6 +1343,9 @@ int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, 
     std::vector<int> its(size_t(ns), 0);
     std::vector<double> rel(size_t(ns), 0.0);
     std::vector<KScal> k(static_cast<size_t>(ns));
+    // a system whose inner solve breaks down or ends non-finite stops refining with the x it has, as the reference
+    // ends its loop when the device solve fails (engine/src/bsr.cpp:1387)
+    std::vector<char> stopped(static_cast<size_t>(ns), 0);
     int escalatedMax = 0;
     for (int outer = 0;; ++outer) {
         // r = b - A x and ||r|| / ||b|| per system (0 for a zero right-hand side, which is converged)
@@ -1353,7 +1356,7 @@ int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, 
         RSG_CUDA(cudaStreamSynchronize(h->stream));
         bool any = false;
         for (int sy = 0; sy < ns; ++sy) {
-            if (rel[size_t(sy)] <= tol) {
+            if (rel[size_t(sy)] <= tol || stopped[size_t(sy)]) {
                 const size_t r0 = size_t(h->plan.sysRow0[size_t(sy)]) * NB, r1 = size_t(h->plan.sysRow0[size_t(sy) + 1]) * NB;
                 RSG_CUDA(cudaMemsetAsync(h->refR + r0, 0, (r1 - r0) * sizeof(double), h->stream));
             } else {
@@ -1363,7 +1366,7 @@ int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, 
         if (!any || outer >= maxOuter) break;
         double* bSave = h->b;
         h->b = h->refR;
-        rc = run_bicgstab(h, innerTol, innerIt);
+        rc = h->opt.krylov == RSG_KRYLOV_GMRES ? run_gmres(h, innerTol, innerIt, false) : run_bicgstab(h, innerTol, innerIt);
         if (!rc && h->opt.precision == RSG_MIXED_F32 && h->opt.precond != RSG_PREC_CPR_DEVICE && h->opt.precond != RSG_PREC_JACOBI &&
             !h->escalated)
             rc = escalate(h, innerTol, innerIt);
@@ -1371,12 +1374,19 @@ int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, 
         if (rc) return rc;
         escalatedMax = std::max(escalatedMax, h->st.escalated_systems);
         RSG_CUDA(cudaMemcpyAsync(k.data(), h->ks, sizeof(KScal) * k.size(), cudaMemcpyDeviceToHost, h->stream));
+        RSG_CUDA(cudaStreamSynchronize(h->stream));
+        for (int sy = 0; sy < ns; ++sy) {
+            if (rel[size_t(sy)] <= tol || stopped[size_t(sy)]) continue;
+            its[size_t(sy)] += k[size_t(sy)].its;
+            if (k[size_t(sy)].status == ST_BREAKDOWN || !std::isfinite(k[size_t(sy)].relres)) {
+                stopped[size_t(sy)] = 1;                          // its correction is not added
+                const size_t r0 = size_t(h->plan.sysRow0[size_t(sy)]) * NB, r1 = size_t(h->plan.sysRow0[size_t(sy) + 1]) * NB;
+                RSG_CUDA(cudaMemsetAsync(h->V.x + r0, 0, (r1 - r0) * sizeof(double), h->stream));
+            }
+        }
         launch_vec_add(h->plan.n, h->refX, h->V.x, h->stream);
         h->launches += 1;
         RSG_CUDA(cudaGetLastError());
-        RSG_CUDA(cudaStreamSynchronize(h->stream));
-        for (int sy = 0; sy < ns; ++sy)
-            if (rel[size_t(sy)] > tol) its[size_t(sy)] += k[size_t(sy)].its;
     }
     // results as the plain solve reports them: per system its, relres and status in the device scalars
     RSG_CUDA(cudaMemcpyAsync(k.data(), h->ks, sizeof(KScal) * k.size(), cudaMemcpyDeviceToHost, h->stream));

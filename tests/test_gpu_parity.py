@@ -774,6 +774,20 @@ def test_refined_solve_matches_reference_refinement(name, precond):
     assert rel(x, xt) < max(10 * err_ref, 1e-6), (rel(x, xt), err_ref)
 
 
+@pytest.mark.parametrize("name", ["waterflood_sys1.npz", "synth_small.npz"])
+def test_refined_solve_with_gmres_inner(name):
+    """The refinement's inner solve is the handle's own Krylov method: with GMRES(30) (the large-system configuration's
+    method) the FP64 defect correction around the precision form reaches 1e-8 as with BiCGSTAB, and its result is
+    finite at every pass (a system whose inner solve broke down keeps the x it had)."""
+    A, z = load_golden(name)
+    with dev(precond="cpr", krylov="gmres", restart=30, precision="mixed_f32") as d:
+        d.set_matrix(A)
+        d.setup()
+        x, res = d.solve_refined(z["b"], tol=1e-8, max_outer=6, inner_it=120)
+    assert np.all(np.isfinite(x))
+    assert res.converged and true_res(A, x, z["b"]) <= 2e-8
+
+
 def test_refined_solve_batch_stops_converged_systems():
     """In a batch, a system within the tolerance gets no further correction: its result is the one it has alone."""
     mats, bs, singles = [], [], []
