@@ -1225,7 +1225,7 @@ int run_gmres(rsg_solver* h, double tol, int maxIt, bool onlyFailed) {
 // triangular sweeps can diverge (the divergence guard stops them early). The systems that did not converge are
 // solved again from x = 0 with the same FP32 factors -- eliminated in FP64 on the thread-block path, as the grid
 // path already has them -- and the sweep vector in FP64 (the mixed form); the converged systems keep their result.
-int escalate(rsg_solver* h, double tol, int maxIt) {
+int escalate(rsg_solver* h, double tol, int maxIt, bool gmres = false) {
     std::vector<KScal> k0(size_t(h->plan.nsys));
     RSG_CUDA(cudaMemcpyAsync(k0.data(), h->ks, sizeof(KScal) * k0.size(), cudaMemcpyDeviceToHost, h->stream));
     RSG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1241,7 +1241,7 @@ int escalate(rsg_solver* h, double tol, int maxIt) {
     }
     h->escalated = true;
     h->st.escalated_systems = failed;
-    return run_bicgstab(h, tol, maxIt, true);
+    return gmres ? run_gmres(h, tol, maxIt, true) : run_bicgstab(h, tol, maxIt, true);
 }
 
 int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, int maxIt, int* iterations, double* relres) {
@@ -1259,6 +1259,11 @@ int do_solve_device(rsg_solver* h, const double* d_b, double* d_x, double tol, i
     int rc;
     if (h->opt.krylov == RSG_KRYLOV_GMRES) {
         if ((rc = run_gmres(h, tol, maxIt, false))) return rc;
+        // precision form: systems GMRES left unconverged (the all-FP32 sweeps can stall on hard systems) are solved
+        // again with FP64 sweep vectors, as after BiCGSTAB; converged systems keep their result
+        if (h->opt.precision == RSG_MIXED_F32 && h->opt.precond != RSG_PREC_CPR_DEVICE && h->opt.precond != RSG_PREC_JACOBI &&
+            !h->escalated && (rc = escalate(h, tol, maxIt, true)))
+            return rc;
     } else {
         if ((rc = run_bicgstab(h, tol, maxIt))) return rc;
         if (h->opt.precision == RSG_MIXED_F32 && h->opt.precond != RSG_PREC_CPR_DEVICE && h->opt.precond != RSG_PREC_JACOBI &&
@@ -1369,7 +1374,7 @@ int do_solve_refined(rsg_solver* h, const double* d_b, double* d_x, double tol, 
         rc = h->opt.krylov == RSG_KRYLOV_GMRES ? run_gmres(h, innerTol, innerIt, false) : run_bicgstab(h, innerTol, innerIt);
         if (!rc && h->opt.precision == RSG_MIXED_F32 && h->opt.precond != RSG_PREC_CPR_DEVICE && h->opt.precond != RSG_PREC_JACOBI &&
             !h->escalated)
-            rc = escalate(h, innerTol, innerIt);
+            rc = escalate(h, innerTol, innerIt, h->opt.krylov == RSG_KRYLOV_GMRES);
         h->b = bSave;
         if (rc) return rc;
         escalatedMax = std::max(escalatedMax, h->st.escalated_systems);

@@ -486,6 +486,26 @@ def test_precision_escalation():
     assert true_res(hard.A, xb[Ne:], hard.b) <= 1e-5
 
 
+def test_precision_escalation_after_gmres():
+    """The same escalation under GMRES: a system the all-FP32 sweeps leave unconverged in the precision form is solved
+    again with FP64 sweep vectors and reaches the tolerance; the converged system of the batch keeps its result."""
+    hard = _hard_request()
+    easy = load_golden("waterflood_sys1.npz")
+    with dev(precond="cpr", krylov="gmres", restart=30, precision="mixed_f32") as d:
+        d.set_matrix(easy[0])
+        d.setup()
+        xe, re_ = d.solve(easy[1]["b"], tol=1e-6, maxit=300)
+        assert d.stats().escalated_systems == 0
+    with dev(precond="cpr", krylov="gmres", restart=30, precision="mixed_f32") as d:
+        d.set_batch([easy[0], hard.A])
+        d.setup()
+        xb, rb = d.solve(np.concatenate([easy[1]["b"], hard.b]), tol=1e-6, maxit=300)
+        its, rr, tr = d.batch_results()
+    Ne = easy[0].n * 3
+    assert np.array_equal(xb[:Ne], xe) and its[0] == re_.iterations
+    assert true_res(hard.A, xb[Ne:], hard.b) <= 1e-5
+
+
 # ---------------------------------------------------------------- multicolour BILU0 (engine/src/bsr.cpp:599-730)
 @pytest.mark.parametrize("sweep", ["cta", "grid"])
 @pytest.mark.parametrize("name", ALL_GOLDEN)
