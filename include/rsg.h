@@ -302,6 +302,84 @@ int rsg_server_hold(rsg_server* s, int hold);
  * admission needs their room). */
 int rsg_server_load(rsg_server* s, int* queued, int* running, size_t* bytes_in_use);
 
+/* ---- Black-oil Jacobian assembly on the device: the reservoir part of the engine's Newton system, written straight
+ * into device memory in the engine's scalar Jacobian layout, so that a Newton step uploads the state (about 50 bytes
+ * per cell) instead of the matrix (about 500 bytes per cell) and hands the result to rsg_set_jacobian_device.
+ * Replaces Simulator::evalAll / evalCell (engine/src/simulator.cpp:2133-2276, 2429-2459), the cell loop of
+ * Simulator::assemble (:2500-2686) and its row scaling dt / PV (:3010-3032), bit for bit, for the standard black-oil
+ * model: water (PVTW), live oil (saturated nodes + undersaturated ratio tables), dry gas, rock compressibility,
+ * unscaled SWOF / SGOF tables, the ECLIPSE default three-phase oil kr, gravity, one PVT and one saturation region.
+ * Other model options are rejected with RSG_EINVAL. The wells remain the caller's (the engine's well loop,
+ * simulator.cpp:2692-2954): their terms are passed as addends. */
+typedef struct rsg_table {
+    int n;                    /* rows (0 = absent) */
+    const double* x;          /* abscissae, non-decreasing */
+    const double* y;
+    int clamp;                /* 1: constant beyond the ends (saturation tables); 0: linear extrapolation */
+} rsg_table;                  /* ressim::Table1D, engine/include/ressim/fluid.h:10-17 */
+
+typedef struct rsg_bo_grid {
+    int na;                   /* active cells */
+    int nv;                   /* unknowns per cell (3: p, Sw, x) */
+    int nconn;                /* connections */
+    const int* adj_start;     /* [na+1] cell c's connections are adj_start[c] .. adj_start[c+1]-1 */
+    const int* adj_nbr;       /* [adj_start[na]] the neighbour cell of each */
+    const int* adj_conn;      /* [adj_start[na]] the connection index of each */
+    const int* conn_a;        /* [nconn] first cell of each connection (dDepth is depth(b) - depth(a)) */
+    const double* conn_trans; /* [nconn] transmissibility */
+    const double* conn_ddepth;/* [nconn] */
+    const double* pore_vol;   /* [na] pore volume at the reference pressure */
+    double gravity;           /* pressure gradient per density and depth (ressim::Units::gravity) */
+    int i_sw, i_x;            /* unknown slots of Sw and of x (Sg / Rs / Rv) */
+    int eq[3];                /* equation offset of the water, oil and gas balances */
+} rsg_bo_grid;                /* ressim::Grid connections / adjacency, engine/include/ressim/grid.h:14-54 */
+
+typedef struct rsg_bo_fluid {
+    int water, oil, gas, live, vap;  /* phases; dissolved gas; vaporised oil (must be 0) */
+    double pvtw[5];           /* reference pressure, Bw, cw, water viscosity, viscosibility */
+    double rock[2];           /* reference pressure, rock compressibility */
+    double rho_sc[3];         /* surface densities: oil, water, gas */
+    double gas_factor;        /* gas volume unit conversion (ressim::FluidModel::gasFactor) */
+    rsg_table rs_of_p, pb_of_rs;     /* saturated Rs(p) and bubble point pb(Rs) */
+    rsg_table dead_b, dead_bmu;      /* dead oil 1/Bo, 1/(Bo mu) (unused with live oil) */
+    rsg_table gas_b, gas_bmu;        /* dry gas 1/Bg, 1/(Bg mu) vs p */
+    int nsat;                 /* live oil: saturated nodes */
+    const double* sat_rs;     /* [nsat] Rs of each node */
+    const double* sat_b;      /* [nsat] 1/Bo at saturation */
+    const double* sat_bmu;    /* [nsat] 1/(Bo mu) at saturation */
+    const rsg_table* under_b;   /* [nsat] ratio (1/Bo) / (1/Bo)_sat vs p - pb */
+    const rsg_table* under_bmu; /* [nsat] the same for 1/(Bo mu) */
+} rsg_bo_fluid;               /* the tables of ressim::FluidModel after setup, engine/include/ressim/fluid.h:60-73 */
+
+typedef struct rsg_bo_satfun {
+    rsg_table krw, krow, pcow;       /* SWOF columns vs Sw */
+    rsg_table krg, krog, pcog;       /* SGOF columns vs Sg */
+    double swco;              /* connate water (first SWOF row) */
+    int kro_model;            /* 0: ECLIPSE default (the only one supported) */
+    int water, gas;           /* two-phase systems present */
+    int three_point;          /* three-point end-point scaling (must be 0) */
+} rsg_bo_satfun;              /* ressim::SatFunctions tables, engine/include/ressim/fluid.h:76-124 */
+
+typedef struct rsg_bo_assembler rsg_bo_assembler;
+
+/* Plan an assembler for one grid on `device`: checks the model options and that J_rowPtr / J_col (nrows = na*nv + nw
+ * rows, host arrays) are the engine's scalar Jacobian pattern (Simulator::buildPattern, engine/src/simulator.cpp:
+ * 465-510: cell row a*nv+e holds the blocks of the cell and its neighbours in column order, then its well columns;
+ * then one row per well), and uploads the grid and tables. */
+int rsg_bo_create(rsg_bo_assembler** h, const rsg_bo_grid* grid, const rsg_bo_fluid* fluid, const rsg_bo_satfun* sat,
+                  int nrows, int nw, const int* J_rowPtr, const int* J_col, int device);
+/* Assemble J (d_J: the pattern's J_rowPtr[nrows] values) and R (d_R: nrows) at the state d_p, d_sw, d_x (na doubles
+ * each), d_state (na bytes: 0 no free gas, x = Rs; 1 oil and gas, x = Sg; 2 no oil, x = Rv) with the old
+ * accumulations d_acc_old (na*3: water, oil, gas) and step dt; all device pointers. The well terms are host lists:
+ * J[add_pos[k]] += add_val[k] and R[radd_pos[k]] += radd_val[k], applied after the reservoir terms and before the
+ * row scaling, in list order for entries at the same position -- the engine's well loop's additions; every well
+ * row starts from zero and is not scaled. Asynchronous on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream); consecutive calls on one assembler must be ordered (one stream). */
+int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const double* d_sw, const double* d_x, const unsigned char* d_state,
+                    const double* d_acc_old, double dt, int nadd, const long long* add_pos, const double* add_val, int nradd,
+                    const int* radd_pos, const double* radd_val, double* d_J, double* d_R, void* stream);
+int rsg_bo_destroy(rsg_bo_assembler* h);
+
 #ifdef __cplusplus
 }
 #endif

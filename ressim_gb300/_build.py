@@ -19,6 +19,8 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(HERE, "librsg.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# per-source flags: the assembly reproduces the engine's separately rounded products and sums (no fused multiply-add)
+EXTRA = {"rsg_assemble.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -58,7 +60,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", obj])
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *EXTRA.get(os.path.basename(src), []),
+                         *inc, "-c", src, "-o", obj])
     for src in cpp:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)

@@ -26,7 +26,7 @@ EXPORTS = [
     "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
     "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes", "rsg_tuning",
     "rsg_set_jacobian", "rsg_set_jacobian_batch", "rsg_set_jacobian_device", "rsg_solve_jacobian", "rsg_solve_jacobian_device",
-    "rsg_get_matrix", "rsg_matrix_size", "rsg_server_hold",
+    "rsg_get_matrix", "rsg_matrix_size", "rsg_server_hold", "rsg_bo_create", "rsg_bo_assemble", "rsg_bo_destroy",
 ]
 
 
@@ -47,6 +47,29 @@ class Stats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("rel_residual", C.c_double), ("true_rel_residual", C.c_double),
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("regularised_blocks", C.c_int), ("amg_levels", C.c_int),
                 ("device_bytes", C.c_size_t), ("kernel_launches", C.c_longlong), ("escalated_systems", C.c_int)]
+
+
+class Table(C.Structure):
+    _fields_ = [("n", C.c_int), ("x", C.c_void_p), ("y", C.c_void_p), ("clamp", C.c_int)]
+
+
+class BoGrid(C.Structure):
+    _fields_ = [("na", C.c_int), ("nv", C.c_int), ("nconn", C.c_int), ("adj_start", C.c_void_p), ("adj_nbr", C.c_void_p),
+                ("adj_conn", C.c_void_p), ("conn_a", C.c_void_p), ("conn_trans", C.c_void_p), ("conn_ddepth", C.c_void_p),
+                ("pore_vol", C.c_void_p), ("gravity", C.c_double), ("i_sw", C.c_int), ("i_x", C.c_int), ("eq", C.c_int * 3)]
+
+
+class BoFluid(C.Structure):
+    _fields_ = [("water", C.c_int), ("oil", C.c_int), ("gas", C.c_int), ("live", C.c_int), ("vap", C.c_int),
+                ("pvtw", C.c_double * 5), ("rock", C.c_double * 2), ("rho_sc", C.c_double * 3), ("gas_factor", C.c_double),
+                ("rs_of_p", Table), ("pb_of_rs", Table), ("dead_b", Table), ("dead_bmu", Table), ("gas_b", Table),
+                ("gas_bmu", Table), ("nsat", C.c_int), ("sat_rs", C.c_void_p), ("sat_b", C.c_void_p), ("sat_bmu", C.c_void_p),
+                ("under_b", C.c_void_p), ("under_bmu", C.c_void_p)]
+
+
+class BoSatfun(C.Structure):
+    _fields_ = [("krw", Table), ("krow", Table), ("pcow", Table), ("krg", Table), ("krog", Table), ("pcog", Table),
+                ("swco", C.c_double), ("kro_model", C.c_int), ("water", C.c_int), ("gas", C.c_int), ("three_point", C.c_int)]
 
 
 class RsgError(RuntimeError):
@@ -113,6 +136,10 @@ def load(build_if_missing: bool = True):
     L.rsg_get_matrix.argtypes = [vp, vp, vp, vp]
     L.rsg_server_hold.argtypes = [vp, C.c_int]
     L.rsg_matrix_size.argtypes = [vp, ip, C.POINTER(C.c_longlong)]
+    L.rsg_bo_create.argtypes = [C.POINTER(vp), C.POINTER(BoGrid), C.POINTER(BoFluid), C.POINTER(BoSatfun), C.c_int, C.c_int, vp, vp,
+                                C.c_int]
+    L.rsg_bo_assemble.argtypes = [vp, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp, vp, C.c_int, vp, vp, vp, vp, vp]
+    L.rsg_bo_destroy.argtypes = [vp]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype if name in ("rsg_last_error", "rsg_version", "rsg_stream") else (
             None if name == "rsg_default_options" else (C.c_longlong if name == "rsg_submit" else

@@ -155,8 +155,9 @@ def test_generic_solves_match_reference(name):
 @pytest.mark.parametrize("nb", [4, 6])
 def test_generic_large_system_level_launches(nb):
     """A system whose levels are too wide for the one-block sweeps (one launch per level; factorisation one launch
-    per level): same factors and sweeps bit for bit, GMRES-CPR and BiCGSTAB-BILU0 within 1e-8 of the oracle's
-    solutions at 1e-10."""
+    per level): same factors and sweeps bit for bit, GMRES-CPR at 1e-10 and BiCGSTAB-BILU0 at 1e-12 within 1e-8 of
+    the oracle's solutions. (BiCGSTAB-BILU0 takes ~400 iterations on the nb = 6 system: at 1e-10 the oracle's own
+    solutions with 1 and 8 threads differ by 2e-8, at 1e-12 by 3e-9.)"""
     from oracle import Oracle
     from ressim_gb300 import synth
     from ressim_gb300.solver import DeviceSolver
@@ -170,9 +171,9 @@ def test_generic_large_system_level_launches(nb):
         d.setup()
         assert np.array_equal(d.factors(A.nnzb), lu_o)
         assert np.array_equal(d.precond_apply(s.b), o.bilu0_apply(A, lu_o, s.b))
-        x, res = d.solve(s.b, tol=1e-10, maxit=1000)
-    xo, conv, _, _, _, _ = o.solve(A, s.b, prec=0, method=0, tol=1e-10, maxit=1000)
-    assert res.converged and conv and rel(x, xo) <= 1e-8
+        x, res = d.solve(s.b, tol=1e-12, maxit=1000)
+    xo, conv, _, _, _, _ = o.solve(A, s.b, prec=0, method=0, tol=1e-12, maxit=1000)
+    assert res.converged and conv and rel(x, xo) <= 1e-8, rel(x, xo)
     with DeviceSolver(precond="cpr", krylov="gmres", restart=60, precision="fp64") as d:
         d.set_matrix(A)
         d.setup(s.acc)

@@ -213,3 +213,56 @@ def test_same_pattern_check_of_set_batch():
     rp2 = B.rowPtr.copy()
     rp2[i + 1:] -= 1
     assert same(mats, [mats[0], Pattern(B.n, rp2, np.delete(B.col, B.rowPtr[i + 1] - 1)), mats[2]]) == 0
+
+
+def test_black_oil_assembler_checks_model_and_pattern_before_the_device():
+    """rsg_bo_create rejects model options outside the supported black-oil model and a Jacobian pattern that is not
+    the engine's with RSG_EINVAL, before it touches a device (so these checks run without a GPU); a valid model gets
+    as far as the device (RSG_ECUDA here, without a GPU)."""
+    from conftest import gpu_available
+    from ressim_gb300 import _lib
+    from ressim_gb300.assembly import BlackOilAssembler
+    z = dict(np.load(os.path.join(ROOT, "tests", "golden", "waterflood_asm.npz")))
+    bad = dict(z)
+    bad["phases"] = np.array([1, 1, 1, 1, 1], np.uint8)            # vaporised oil
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(bad)
+    assert e.value.code == _lib.RSG_EINVAL and "vaporised" in str(e.value)
+    bad = dict(z)
+    bad["kroModel"] = np.array([2], np.int32)                      # STONE2
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(bad)
+    assert e.value.code == _lib.RSG_EINVAL
+    bad = dict(z)
+    col = z["J_col"].copy()
+    col[[0, 1]] = col[[1, 0]]                                      # columns of a cell row out of the engine's order
+    bad["J_col"] = col
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(bad)
+    assert e.value.code == _lib.RSG_EINVAL and "pattern" in str(e.value)
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(z)
+    assert e.value.code == _lib.RSG_ECUDA
+
+
+def test_assembly_golden_is_consistent():
+    """The assembly golden vectors (the reference engine's): the full Jacobian is the reservoir terms plus the well
+    terms -- rows that take no well term equal the reservoir-only assembly bit for bit, and the grid, pattern and
+    tables describe the 20x20x4 three-phase live-oil waterflood."""
+    z = dict(np.load(os.path.join(ROOT, "tests", "golden", "waterflood_asm.npz")))
+    na, nv, nw = int(z["na"][0]), int(z["nv"][0]), int(z["nw"][0])
+    assert (na, nv, nw) == (1600, 3, 2) and list(z["phases"]) == [1, 1, 1, 1, 0]
+    rp = z["J_rowPtr"]
+    assert rp.size == na * nv + nw + 1 and z["s1_J_full"].size == rp[-1]
+    rows = np.searchsorted(rp, z["s1_add_pos"], side="right") - 1
+    touched = np.zeros(na, bool)
+    touched[rows[rows < na * nv] // nv] = True
+    touched[z["s1_radd_pos"][z["s1_radd_pos"] < na * nv] // nv] = True
+    free = np.repeat(~touched, nv)
+    pos = np.repeat(free, np.diff(rp[:na * nv + 1]))
+    assert np.array_equal(z["s1_J_full"][:rp[na * nv]][pos], z["s1_J_cell"][:rp[na * nv]][pos])
+    assert np.array_equal(z["s1_R_full"][:na * nv][free], z["s1_R_cell"][:na * nv][free])
+    states = [np.bincount(z[f"s{k}_hasGas"], minlength=3) for k in range(int(z["nstates"][0]))]
+    assert states[0][1] > 0 and states[0][2] > 0                   # the perturbed state has free-gas and no-oil cells
