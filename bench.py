@@ -315,6 +315,80 @@ def serving_ensemble(local, systems, rounds=3):
             "note": "host wall clock per round: submission (host copies), admission, batched set-up and solve, results"}
 
 
+def assembly_bytes(z):
+    """Bytes the assembly must move at least once per call: the state and old accumulations, the grid (adjacency,
+    connections, pore volumes, row starts of the pattern), the Jacobian and residual written, and the per-cell
+    property records (13 dual numbers) written by k_bo_props and read once by k_bo_cells."""
+    na, nconn = int(z["na"][0]), int(z["conn_trans"].size)
+    nadj, nnz, nrows = int(z["adjStart"][-1]), int(z["J_rowPtr"][-1]), na * 3 + int(z["nw"][0])
+    state = na * (3 * 8 + 1 + 3 * 8 + 8)
+    grid = (na + 1) * 4 + nadj * 12 + nconn * 20 + (nrows + 1) * 4 + na * 8
+    out = nnz * 8 + nrows * 8
+    rec = 2 * 52 * 8 * na
+    return {"state": state, "grid": grid, "jacobian_and_residual": out, "records": rec, "total": state + grid + out + rec}
+
+
+def assembly_leg(local, steps, warmup):
+    """Device Jacobian assembly (rsg_bo_assemble) of the ensemble's 64 grids taken as one (synthetic black-oil tables
+    and state, ressim_gb300.synth.assembly_ensemble): device time per assembly with the state resident, and end to
+    end with the state uploaded from pinned host memory and the residual read back (what a Newton step moves when the
+    Jacobian is built on the device) against the matrix upload it replaces."""
+    import torch
+    from ressim_gb300 import synth
+    from ressim_gb300.assembly import BlackOilAssembler
+    z, st = synth.assembly_ensemble(N_REAL, NX, NY, NZ, SIGMA, seed0=0)
+    dv = torch.device(f"cuda:{local}")
+    asm = BlackOilAssembler(z, device=local)
+    host = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in ("p", "sw", "x", "state", "acc_old")}
+    d = {k: v.to(dv) for k, v in host.items()}
+    J = torch.empty(asm.nnz, dtype=torch.float64, device=dv)
+    R = torch.empty(asm.nrows, dtype=torch.float64, device=dv)
+    R_host = torch.empty(asm.nrows, dtype=torch.float64).pin_memory()
+    s = torch.cuda.Stream(dv)
+    torch.cuda.synchronize()
+
+    def run():
+        asm.assemble_device(d["p"].data_ptr(), d["sw"].data_ptr(), d["x"].data_ptr(), d["state"].data_ptr(), d["acc_old"].data_ptr(),
+                            10.0, J.data_ptr(), R.data_ptr(), stream=s.cuda_stream)
+
+    for _ in range(max(3, warmup)):
+        run()
+    torch.cuda.synchronize()
+    reps = max(10, steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        run()             # J (339 MB) is written every call: more than L2 between consecutive calls
+    e1.record(s)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / reps / 1e3
+    # end to end: state in from pinned host memory, assembly, residual out (the engine's convergence check reads it)
+    te = []
+    for k in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(s):
+            for key in d:
+                d[key].copy_(host[key], non_blocking=True)
+            run()
+            R_host.copy_(R, non_blocking=True)
+        s.synchronize()
+        if k >= warmup:
+            te.append(time.perf_counter() - t0)
+    asm.close()
+    B = assembly_bytes(z)
+    hbm, peak_kind = peaks()
+    na = int(z["na"][0])
+    h2d = sum(int(v.numel() * v.element_size()) for v in host.values())
+    return {"workload": f"ensemble{N_REAL}_{NX}x{NY}x{NZ} grids as one ({na} cells, synthetic tables and state)",
+            "cells": na, "jacobian_values": int(asm.nnz), "ms": 1e3 * t, "value": na / t, "unit": "cells/s",
+            "launches_per_assembly": 2, "bytes": B, "roofline": {"bound": "hbm", "achieved": B["total"] / t / 1e9, "peak": hbm,
+                                                                 "unit": "GB/s", "frac": B["total"] / t / 1e9 / hbm,
+                                                                 "peak_kind": peak_kind + " burst copy"},
+            "e2e": {"ms": 1e3 * statistics.median(te), "h2d_bytes": h2d, "d2h_bytes": asm.nrows * 8,
+                    "matrix_upload_replaced_bytes": int(asm.nnz) * 8}}
+
+
 def spe10_report(local):
     """The one-large-system configurations (60x220x85, 1,122,000 block rows; Jacobians of day 1 and day 100):
     CPR + GMRES(30) in plain FP64 and in the FP32 precision form at 1e-6 and 1e-8, with iterations, device set-up and
@@ -421,6 +495,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--systems", type=int, default=64, help="ensemble size (64: the headline workload; smaller: profiling)")
     ap.add_argument("--spe10", action="store_true", help="print the one-large-system report (60x220x85) instead of the bench line")
+    ap.add_argument("--assembly", choices=["on", "off", "only"], default="on",
+                    help="the device Jacobian assembly leg (only: print it alone, for profiling)")
     ap.add_argument("--serving", choices=["on", "off", "only"], default="on",
                     help="the serving stream (Poisson arrivals through the continuous-batching server)")
     args = ap.parse_args()
@@ -443,6 +519,10 @@ def main():
     torch.cuda.set_device(local)
     from ressim_gb300.solver import DeviceSolver
 
+    if args.assembly == "only":
+        if rank == 0:
+            print(json.dumps({"metric": "device Jacobian assembly", "assembly": assembly_leg(local, args.steps, args.warmup)}))
+        return 0
     if args.spe10:
         if rank == 0:
             print(json.dumps(spe10_report(local)))
@@ -652,6 +732,7 @@ def main():
                   "p99_ms": 1e3 * float(np.percentile(lat, 99)), "all_converged": bool(plain_ok)}
 
     serving_ens = serving_ensemble(local, systems) if args.serving != "off" and world == 1 else None
+    assembly = assembly_leg(local, args.steps, args.warmup) if world == 1 and args.assembly != "off" else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -679,6 +760,7 @@ def main():
             "batched_mixed_over_batched_fp64": value / fp64_batched["value"],
             "e2e": e2e, "roofline": roofline, "roofline_spmv": roofline_spmv, "kernels": kernels, "gpu_launches": int(launches),
             "cpu_baseline": cpu, "clocks": clk.summary(), "serving": serving, "serving_ensemble": serving_ens,
+            "assembly": assembly,
         }
         print(json.dumps(line))
     if dist:

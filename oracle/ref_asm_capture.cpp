@@ -17,6 +17,9 @@
 // `private` defined as `public` (no reference source is changed; access does not affect the class layout).
 //
 //   ref_asm_capture OUTDIR DT CALL [CALL ...]
+//   ref_asm_capture --time NX NY NZ REPS     (CPU timing of the engine's own evalAll + assemble at the first Newton
+//                                             state of an NX x NY x NZ waterflood, the engine's default block assembly,
+//                                             OMP_NUM_THREADS threads; prints one JSON line)
 //
 // Output: OUTDIR/asm_CCC.bin and OUTDIR/asm_CCC_perturbed.bin, sequences of records
 // {char name[32], int32 kind (0 f64, 1 i32, 2 u8), int64 count, data}.
@@ -158,6 +161,35 @@ void writeState(Simulator& s, const std::string& path, double dt) {
     std::fclose(o.f);
 }
 
+struct Timer : GpuBlockSolver {
+    int reps = 5, count = 0;
+    double dt = 3.7;
+    const char* name() const override { return "asm-timer"; }
+    bool solve(const BSR&, const std::vector<double>&, std::vector<double>& x, double, int, int& its) override {
+        x.clear(); its = 0;
+        if (count++ != 0) return false;
+        Simulator& s = *g_sim;
+        const std::vector<Simulator::WellRT> wsave = s.wells_;
+        s.evalAll(false);
+        s.assemble(dt);   // warm-up
+        s.wells_ = wsave;
+        std::vector<double> t;
+        for (int r = 0; r < reps; ++r) {
+            const auto t0 = std::chrono::steady_clock::now();
+            s.evalAll(false);
+            s.assemble(dt);
+            t.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+            s.wells_ = wsave;
+        }
+        std::sort(t.begin(), t.end());
+        const char* th = std::getenv("OMP_NUM_THREADS");
+        std::printf("{\"cells\": %d, \"block_assembly\": %d, \"reps\": %d, \"median_ms\": %.4f, \"min_ms\": %.4f, \"threads\": \"%s\"}\n",
+                    s.grid_.numActive(), int(s.blkAsm_), reps, 1e3 * t[t.size() / 2], 1e3 * t[0], th ? th : "default");
+        std::fflush(stdout);
+        std::exit(0);
+    }
+};
+
 struct Hook : GpuBlockSolver {
     std::string dir;
     double dt = 1.0;
@@ -205,6 +237,19 @@ struct Hook : GpuBlockSolver {
 }  // namespace
 
 int main(int argc, char** argv) {
+    if (argc >= 6 && std::string(argv[1]) == "--time") {
+        Timer tm;
+        tm.reps = std::atoi(argv[5]);
+        const Case c = rsgref::waterfloodCase(1, 1.0, 0, std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]));
+        setDistributedSolver(&tm);
+        Simulator sim;
+        g_sim = &sim;
+        sim.setup(c);
+        sim.initialize();
+        while (sim.runReportStep()) {}
+        std::fprintf(stderr, "no Newton system reached the solver hook\n");
+        return 5;
+    }
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_asm_capture OUTDIR DT CALL [CALL ...]\n");
         return 1;

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "librsg.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # per-source flags: the assembly reproduces the engine's separately rounded products and sums (no fused multiply-add)
-EXTRA = {"rsg_assemble.cu": ["-fmad=false"]}
+EXTRA = {"rsg_assemble.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc() -> str:

@@ -72,19 +72,36 @@ __device__ __forceinline__ D3 chain2(D3 x, D3 y, double f, double fx, double fy)
     return D3{f, fx * x.d0 + fy * y.d0, fx * x.d1 + fy * y.d1, fx * x.d2 + fy * y.d2};
 }
 
-// Dual numbers over the two cells of a connection: slots 0-2 the cell's own unknowns, 3-5 the neighbour's.
-struct D6 {
-    double v, d[6];
-};
-__device__ __forceinline__ D6 liftA(D3 a) { return D6{a.v, {a.d0, a.d1, a.d2, 0.0, 0.0, 0.0}}; }
-__device__ __forceinline__ D6 liftB(D3 b) { return D6{b.v, {0.0, 0.0, 0.0, b.d0, b.d1, b.d2}}; }
-
 // ---------------------------------------------------------------------------------------------------------------
 // Tables (ressim::Table1D, engine/include/ressim/fluid.h:10-17): piecewise linear, extrapolated linearly beyond the
-// ends unless clamped, the segment found as upper_bound - 1 within [0, n - 2].
+// ends unless clamped, the segment found as upper_bound - 1 within [0, n - 2]. The slope of every segment,
+// (y[i+1] - y[i]) / (x[i+1] - x[i]) (0 for a zero-width segment), is computed once on the host -- the same IEEE
+// operations the engine performs at each evaluation, so the same value -- and the evaluation is y[i] + s (xv - x[i]).
 struct Tab {
-    int x, y, n, clamp;   // offsets of x and y in the table buffer, length, clamp flag
+    int x, y, s, k, n, clamp;   // offsets of x, y, the slopes and the order keys in the table buffer, length, clamp flag
 };
+
+// Order key of a double: a 64-bit integer that compares as the IEEE value does (-0 taken as +0; no NaN in the
+// tables), so that table searches run on the integer pipe and leave the FP64 pipe, the binding unit of the assembly,
+// to the arithmetic. The keys of the tables' abscissae are formed on the host.
+__device__ __forceinline__ long long okey(double v) {
+    long long b = __double_as_longlong(v);
+    b = b == (long long)0x8000000000000000ULL ? 0 : b;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+// upper_bound - 1 of xk among the n keys K, within [0, n - 2], with the engine's guards for the first and last segment
+__device__ __forceinline__ int seg_of(const long long* __restrict__ K, int n, long long xk) {
+    if (xk <= K[1]) return 0;
+    if (xk >= K[n - 2]) return n - 2;
+    int lo = 0, cnt = n;
+    while (cnt > 0) {
+        const int step = cnt >> 1;
+        if (!(xk < K[lo + step])) { lo += step + 1; cnt -= step + 1; }
+        else cnt = step;
+    }
+    return min(max(lo - 1, 0), n - 2);
+}
 
 __device__ double tab_eval(const double* __restrict__ T, Tab t, double xv, double& s) {
     const int n = t.n;
@@ -92,24 +109,14 @@ __device__ double tab_eval(const double* __restrict__ T, Tab t, double xv, doubl
     const double* x = T + t.x;
     const double* y = T + t.y;
     if (n == 1) { s = 0.0; return y[0]; }
+    const long long* K = reinterpret_cast<const long long*>(T + t.k);
+    const long long xk = okey(xv);
     if (t.clamp) {
-        if (xv <= x[0]) { s = 0.0; return y[0]; }
-        if (xv >= x[n - 1]) { s = 0.0; return y[n - 1]; }
+        if (xk <= K[0]) { s = 0.0; return y[0]; }
+        if (xk >= K[n - 1]) { s = 0.0; return y[n - 1]; }
     }
-    int i;
-    if (xv <= x[1]) i = 0;
-    else if (xv >= x[n - 2]) i = n - 2;
-    else {   // first index whose abscissa exceeds xv, less one
-        int lo = 0, cnt = n;
-        while (cnt > 0) {
-            const int step = cnt >> 1;
-            if (!(xv < x[lo + step])) { lo += step + 1; cnt -= step + 1; }
-            else cnt = step;
-        }
-        i = min(max(lo - 1, 0), n - 2);
-    }
-    const double dx = x[i + 1] - x[i];
-    s = dx != 0 ? (y[i + 1] - y[i]) / dx : 0.0;
+    const int i = seg_of(K, n, xk);
+    s = T[t.s + i];
     return y[i] + s * (xv - x[i]);
 }
 __device__ __forceinline__ D3 tab_ad(const double* __restrict__ T, Tab t, D3 xv) {
@@ -127,6 +134,9 @@ struct Model {
     double pw_ref, pw_bw, pw_cw, pw_visc, pw_cv;
     double rock_ref, rock_cr;
     double rho_oil, rho_water, rho_gas, gas_factor;
+    // constants of the engine's expressions, formed once with the same IEEE operations: 1 / Bw, 1 / (Bw mu_w),
+    // cw - cv, rho_gas * gasFactor
+    double inv_bw, inv_bwvisc, pw_cwv, rho_gfac;
     // tables
     Tab rsOfP, pbOfRs, deadB, deadBMu, gasB, gasBMu;
     Tab krw, krow, pcow, krg, krog, pcog;
@@ -134,53 +144,59 @@ struct Model {
     int sat_water, sat_gas;
     // live oil: nsat saturated nodes (Rs, 1/Bo, 1/(Bo mu)) at rs, bsat, bmusat; under tables at utab[2 k] (1/Bo
     // ratio) and utab[2 k + 1] (1/(Bo mu) ratio) of the descriptor array
-    int nsat, rs, bsat, bmusat;
+    int nsat, rs, rsk, bsat, bmusat;   // rsk: order keys of the nodes' Rs
 };
 
 // FluidModel::liveOil (engine/src/fluid.cpp:257-271): interpolation between the saturated nodes bracketing rs of
-// the undersaturated ratio at p - pb(rs)
-__device__ double live_oil(const double* __restrict__ T, const Tab* __restrict__ U, const Model& m, double p, double rs,
-                           int which) {
-    const int n = m.nsat;
-    const double* R = T + m.rs;
+// the undersaturated ratio at p - pb(rs). Split in two: the segment of rs (node k, pb(rs), weight w), then both
+// quantities (1/Bo and 1/(Bo mu)) at one p, so that evaluations at the same rs share the segment.
+struct LiveSeg {
     int k;
-    if (rs <= R[1]) k = 0;
-    else if (rs >= R[n - 2]) k = n - 2;
-    else {
-        int lo = 0, cnt = n;
-        while (cnt > 0) {
-            const int step = cnt >> 1;
-            if (!(rs < R[lo + step])) { lo += step + 1; cnt -= step + 1; }
-            else cnt = step;
-        }
-        k = min(max(lo - 1, 0), n - 2);
-    }
+    double pb, w;
+};
+
+__device__ LiveSeg live_seg(const double* __restrict__ T, const Model& m, double rs) {
+    const double* R = T + m.rs;
+    const int k = seg_of(reinterpret_cast<const long long*>(T + m.rsk), m.nsat, okey(rs));
     double s;
-    const double pb = tab_eval(T, m.pbOfRs, rs, s);
-    const double dp = p - pb;
-    const double* sat = T + (which == 0 ? m.bsat : m.bmusat);
-    const double v0 = sat[k] * tab_eval(T, U[2 * k + which], dp, s);
-    const double v1 = sat[k + 1] * tab_eval(T, U[2 * (k + 1) + which], dp, s);
-    const double w = (rs - R[k]) / (R[k + 1] - R[k]);
-    return v0 + w * (v1 - v0);
+    LiveSeg g;
+    g.k = k;
+    g.pb = tab_eval(T, m.pbOfRs, rs, s);
+    g.w = (rs - R[k]) / (R[k + 1] - R[k]);
+    return g;
 }
 
-// FluidModel::liveOilAD (engine/src/fluid.cpp:273-280): value and central differences in p and rs
-__device__ D3 live_oil_ad(const double* __restrict__ T, const Tab* __restrict__ U, const Model& m, D3 p, D3 rs, int which) {
-    const double f = live_oil(T, U, m, p.v, rs.v, which);
+__device__ __forceinline__ void live_pair(const double* __restrict__ T, const Tab* __restrict__ U, const Model& m, LiveSeg g,
+                                          double p, double& b, double& bmu) {
+    const double dp = p - g.pb;
+    const int k = g.k;
+    double s;
+    const double* sb = T + m.bsat;
+    const double* sm = T + m.bmusat;
+    const double b0 = sb[k] * tab_eval(T, U[2 * k], dp, s);
+    const double b1 = sb[k + 1] * tab_eval(T, U[2 * (k + 1)], dp, s);
+    b = b0 + g.w * (b1 - b0);
+    const double m0 = sm[k] * tab_eval(T, U[2 * k + 1], dp, s);
+    const double m1 = sm[k + 1] * tab_eval(T, U[2 * (k + 1) + 1], dp, s);
+    bmu = m0 + g.w * (m1 - m0);
+}
+
+// FluidModel::liveOilAD (engine/src/fluid.cpp:273-280) for 1/Bo and 1/(Bo mu) at once: the values and central
+// differences in p (at rs's segment) and in rs (at the segments of rs +- hr)
+__device__ void live_oil_ad2(const double* __restrict__ T, const Tab* __restrict__ U, const Model& m, D3 p, D3 rs, D3& bo, D3& bomu) {
+    const LiveSeg g0 = live_seg(T, m, rs.v);
     const double hp = 1e-4 * fmax(1.0, fabs(p.v));
     const double hr = 1e-5 * fmax(1e-2, fabs(rs.v));
-    const double fp = (live_oil(T, U, m, p.v + hp, rs.v, which) - live_oil(T, U, m, p.v - hp, rs.v, which)) / (2 * hp);
-    const double fr = (live_oil(T, U, m, p.v, rs.v + hr, which) - live_oil(T, U, m, p.v, rs.v - hr, which)) / (2 * hr);
-    return chain2(p, rs, f, fp, fr);
+    double fb, fm, pbp, pmp, pbm, pmm, rbp, rmp, rbm, rmm;
+    live_pair(T, U, m, g0, p.v, fb, fm);
+    live_pair(T, U, m, g0, p.v + hp, pbp, pmp);
+    live_pair(T, U, m, g0, p.v - hp, pbm, pmm);
+    live_pair(T, U, m, live_seg(T, m, rs.v + hr), p.v, rbp, rmp);
+    live_pair(T, U, m, live_seg(T, m, rs.v - hr), p.v, rbm, rmm);
+    bo = chain2(p, rs, fb, (pbp - pbm) / (2 * hp), (rbp - rbm) / (2 * hr));
+    bomu = chain2(p, rs, fm, (pmp - pmm) / (2 * hp), (rmp - rmm) / (2 * hr));
 }
 
-__device__ __forceinline__ D3 oil_b(const double* T, const Tab* U, const Model& m, D3 p, D3 rs) {
-    return m.live ? live_oil_ad(T, U, m, p, rs, 0) : tab_ad(T, m.deadB, p);
-}
-__device__ __forceinline__ D3 oil_bmu(const double* T, const Tab* U, const Model& m, D3 p, D3 rs) {
-    return m.live ? live_oil_ad(T, U, m, p, rs, 1) : tab_ad(T, m.deadBMu, p);
-}
 __device__ __forceinline__ D3 rs_sat(const double* T, const Model& m, D3 p) {   // FluidModel::rsSat (fluid.cpp:248-254)
     if (!m.live) return dconst(0.0);
     double d;
@@ -241,9 +257,9 @@ __global__ void __launch_bounds__(kThreads) k_bo_props(int na, Model m, const do
         Pp[PW] = m.oil ? sub(P, mulc(mulc(tab_ad(T, m.pcow, Sw), 1.0), 1.0)) : P;
         // FluidModel::bw / bwMu (fluid.cpp:191-198)
         const D3 X = mulc(subc(Pp[PW], m.pw_ref), m.pw_cw);
-        const D3 bw = mulc(add(addc(X, 1.0), mulc(mul(X, X), 0.5)), 1.0 / m.pw_bw);
-        const D3 Y = mulc(subc(Pp[PW], m.pw_ref), m.pw_cw - m.pw_cv);
-        const D3 bwmu = mulc(add(addc(Y, 1.0), mulc(mul(Y, Y), 0.5)), 1.0 / (m.pw_bw * m.pw_visc));
+        const D3 bw = mulc(add(addc(X, 1.0), mulc(mul(X, X), 0.5)), m.inv_bw);
+        const D3 Y = mulc(subc(Pp[PW], m.pw_ref), m.pw_cwv);
+        const D3 bwmu = mulc(add(addc(Y, 1.0), mulc(mul(Y, Y), 0.5)), m.inv_bwvisc);
         const D3 kr = !m.oil ? dconst(1.0) : tab_ad(T, m.krw, Sw);
         mob[PW] = mul(bwmu, kr);
         rho[PW] = mulc(bw, m.rho_water);
@@ -251,11 +267,13 @@ __global__ void __launch_bounds__(kThreads) k_bo_props(int na, Model m, const do
     }
     if (m.oil) {
         Pp[PO] = P;
-        bo = oil_b(T, U, m, P, rs);
+        D3 bomu;
+        if (m.live) live_oil_ad2(T, U, m, P, rs, bo, bomu);
+        else { bo = tab_ad(T, m.deadB, P); bomu = tab_ad(T, m.deadBMu, P); }
         D3 kr = dconst(1.0);
         if (m.water || m.gas) kr = kro3(T, m, Sw, Sg);
-        mob[PO] = mul(oil_bmu(T, U, m, P, rs), kr);
-        rho[PO] = mul(bo, addc(mulc(rs, m.rho_gas * m.gas_factor), m.rho_oil));
+        mob[PO] = mul(bomu, kr);
+        rho[PO] = mul(bo, addc(mulc(rs, m.rho_gfac), m.rho_oil));
         acc[PO] = mul(mul(pv, bo), So);
         mobRs = mul(mob[PO], rs);
     }
@@ -264,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_bo_props(int na, Model m, const do
         const D3 krg = tab_ad(T, m.krg, Sg);
         const D3 bg = tab_ad(T, m.gasB, Pp[PG]);
         mob[PG] = mul(tab_ad(T, m.gasBMu, Pp[PG]), krg);
-        rho[PG] = mulc(bg, m.rho_gas * m.gas_factor);
+        rho[PG] = mulc(bg, m.rho_gfac);
         acc[PG] = mul(pv, add(mul(bg, Sg), m.oil ? mul(mul(rs, bo), So) : dconst(0.0)));
     }
     const D3 f[kRec] = {Pp[0], Pp[1], Pp[2], mob[0], mob[1], mob[2], rho[0], rho[1], rho[2], mobRs, acc[0], acc[1], acc[2]};
@@ -299,10 +317,10 @@ __global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, Model m, 
     if (a >= na) return;
     const size_t N = size_t(na);
     const double invDt = 1.0 / dt;
-    // accumulators per phase balance (the equation row of phase p is m.eq[p]): the cell's own block and residual
-    double sj[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    double sr[3] = {0, 0, 0};
-    const bool ph[3] = {m.water != 0, m.oil != 0, m.gas != 0};
+    // Accumulators per phase balance (the equation row of phase p is m.eq[p]): the cell's own block and residual.
+    // The model has all three phases and dissolved gas (checked at creation), so the order of the terms is fixed: a
+    // balance's first term is assigned rather than added to zero (the same value).
+    double sj[3][3], sr[3];
     // does the cell take well terms (then its rows are finished by k_bo_addends)?
     bool finish = false;
     {
@@ -319,13 +337,12 @@ __global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, Model m, 
     // accumulation (acc - accOld) / dt
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
-        if (!ph[p]) continue;
         D3 acc = ld3(rec, N, 10 + p, a);
         acc.v = acc.v - __ldg(accOld + size_t(a) * 3 + p);
-        sr[p] += acc.v * invDt;
-        sj[p][0] += acc.d0 * invDt;
-        sj[p][1] += acc.d1 * invDt;
-        sj[p][2] += acc.d2 * invDt;
+        sr[p] = acc.v * invDt;
+        sj[p][0] = acc.d0 * invDt;
+        sj[p][1] = acc.d1 * invDt;
+        sj[p][2] = acc.d2 * invDt;
     }
     const int r0 = a * nv;
     int rowp[3];
@@ -341,57 +358,49 @@ __global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, Model m, 
         const double dD = __ldg(connA + cn) == a ? __ldg(dDepth + cn) : -__ldg(dDepth + cn);
         const double tr = __ldg(trans + cn);
         const double gd = m.gravity * dD;
-        double nbk[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // the neighbour's block of this connection
+        double nbk[3][3];   // the neighbour's block of this connection
+        // The dual numbers of a connection carry the cell's derivatives in slots 0-2 and the neighbour's in 3-5; the
+        // slots a lifted operand does not have are exact zeros, so their products and sums are left out (a term
+        // x + 0 or 0 * y changes no value), and so is the gravity term of a connection without depth difference.
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-            if (!ph[p]) continue;
-            // rho = (rho_a + rho_b) / 2, dphi = P_a - P_b + rho g dD
-            const D3 RB = ld3(rec, N, 6 + p, b);
+            // dphi = P_a - P_b + rho g dD with rho = (rho_a + rho_b) / 2
             const D3 PB = ld3(rec, N, p, b);
-            D6 rho = liftA(RA[p]);
-            {
-                const D6 rb = liftB(RB);
-                rho.v = rho.v + rb.v;
-#pragma unroll
-                for (int i = 0; i < 6; ++i) rho.d[i] = rho.d[i] + rb.d[i];
-                rho.v = rho.v * 0.5;
-#pragma unroll
-                for (int i = 0; i < 6; ++i) rho.d[i] = rho.d[i] * 0.5;
+            double dv = PA[p].v - PB.v;
+            double da[3] = {PA[p].d0, PA[p].d1, PA[p].d2};
+            double db[3] = {-PB.d0, -PB.d1, -PB.d2};
+            if (gd != 0.0) {
+                const D3 RB = ld3(rec, N, 6 + p, b);
+                dv = dv + ((RA[p].v + RB.v) * 0.5) * gd;
+                da[0] = da[0] + (RA[p].d0 * 0.5) * gd;
+                da[1] = da[1] + (RA[p].d1 * 0.5) * gd;
+                da[2] = da[2] + (RA[p].d2 * 0.5) * gd;
+                db[0] = db[0] + (RB.d0 * 0.5) * gd;
+                db[1] = db[1] + (RB.d1 * 0.5) * gd;
+                db[2] = db[2] + (RB.d2 * 0.5) * gd;
             }
-            D6 dphi = liftA(PA[p]);
-            {
-                const D6 pb = liftB(PB);
-                dphi.v = dphi.v - pb.v;
+            const bool upA = dv >= 0;
+            const int up = upA ? a : b;
+            // F = mob_upstream dphi T, added to balance `bal` (the phase's own; the gas balance for dissolved gas);
+            // `first`: the connection's first term of that balance in the neighbour's block
+            auto flux = [&](int field, int bal, bool first) {
+                const D3 mo = ld3(rec, N, field, up);
+                double fa[3], fb[3];
+                const double mu[3] = {mo.d0, mo.d1, mo.d2};
 #pragma unroll
-                for (int i = 0; i < 6; ++i) dphi.d[i] = dphi.d[i] - pb.d[i];
-                D6 g = rho;
-                g.v = g.v * gd;
-#pragma unroll
-                for (int i = 0; i < 6; ++i) g.d[i] = g.d[i] * gd;
-                dphi.v = dphi.v + g.v;
-#pragma unroll
-                for (int i = 0; i < 6; ++i) dphi.d[i] = dphi.d[i] + g.d[i];
-            }
-            const bool upA = dphi.v >= 0;
-            // F = mob_upstream dphi T, added to balance `ph` (the phase's own; the gas balance for dissolved gas)
-            auto flux = [&](D3 mA, D3 mB, double t, int bal) {
-                const D6 mo = upA ? liftA(mA) : liftB(mB);
-                D6 F;
-#pragma unroll
-                for (int i = 0; i < 6; ++i) F.d[i] = mo.d[i] * dphi.v + mo.v * dphi.d[i];
-                F.v = mo.v * dphi.v;
-                F.v = F.v * t;
-#pragma unroll
-                for (int i = 0; i < 6; ++i) F.d[i] = F.d[i] * t;
-                sr[bal] += F.v;
+                for (int i = 0; i < 3; ++i) {
+                    fa[i] = upA ? mu[i] * dv + mo.v * da[i] : mo.v * da[i];
+                    fb[i] = upA ? mo.v * db[i] : mu[i] * dv + mo.v * db[i];
+                }
+                sr[bal] += (mo.v * dv) * tr;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    sj[bal][k] += F.d[k];
-                    nbk[bal][k] += F.d[3 + k];
+                    sj[bal][k] += fa[k] * tr;
+                    nbk[bal][k] = first ? fb[k] * tr : nbk[bal][k] + fb[k] * tr;
                 }
             };
-            flux(ld3(rec, N, 3 + p, a), ld3(rec, N, 3 + p, b), tr, p);
-            if (p == PO && m.live) flux(ld3(rec, N, 9, a), ld3(rec, N, 9, b), tr, PG);
+            flux(3 + p, p, p != PG);            // water and oil: first terms; gas: after the dissolved gas
+            if (p == PO) flux(9, PG, true);     // dissolved gas carried by the oil flux
         }
         const int pos = __ldg(adjPos + q);
 #pragma unroll
@@ -490,8 +499,19 @@ struct rsg_bo_assembler {
 
 namespace {
 
+// order key of a double (the device's okey), stored in the table buffer
+double host_key(double v) {
+    long long b;
+    std::memcpy(&b, &v, 8);
+    if (b == (long long)0x8000000000000000ULL) b = 0;
+    b ^= (b >> 63) & 0x7fffffffffffffffLL;
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+}
+
 Tab put_table(std::vector<double>& buf, const rsg_table& t) {
-    Tab d{0, 0, 0, 0};
+    Tab d{0, 0, 0, 0, 0, 0};
     if (t.n <= 0) return d;
     d.n = t.n;
     d.clamp = t.clamp ? 1 : 0;
@@ -499,6 +519,14 @@ Tab put_table(std::vector<double>& buf, const rsg_table& t) {
     buf.insert(buf.end(), t.x, t.x + t.n);
     d.y = int(buf.size());
     buf.insert(buf.end(), t.y, t.y + t.n);
+    d.s = int(buf.size());
+    for (int i = 0; i + 1 < t.n; ++i) {   // Table1D::eval's slope (engine/src/fluid.cpp:22-23)
+        const double dx = t.x[i + 1] - t.x[i];
+        buf.push_back(dx != 0 ? (t.y[i + 1] - t.y[i]) / dx : 0.0);
+    }
+    buf.push_back(0.0);
+    d.k = int(buf.size());
+    for (int i = 0; i < t.n; ++i) buf.push_back(host_key(t.x[i]));
     return d;
 }
 
@@ -607,6 +635,10 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     m.pw_ref = f->pvtw[0]; m.pw_bw = f->pvtw[1]; m.pw_cw = f->pvtw[2]; m.pw_visc = f->pvtw[3]; m.pw_cv = f->pvtw[4];
     m.rock_ref = f->rock[0]; m.rock_cr = f->rock[1];
     m.rho_oil = f->rho_sc[0]; m.rho_water = f->rho_sc[1]; m.rho_gas = f->rho_sc[2]; m.gas_factor = f->gas_factor;
+    m.inv_bw = 1.0 / m.pw_bw;
+    m.inv_bwvisc = 1.0 / (m.pw_bw * m.pw_visc);
+    m.pw_cwv = m.pw_cw - m.pw_cv;
+    m.rho_gfac = m.rho_gas * m.gas_factor;
     std::vector<double> tb;
     m.rsOfP = put_table(tb, f->rs_of_p); m.pbOfRs = put_table(tb, f->pb_of_rs);
     m.deadB = put_table(tb, f->dead_b); m.deadBMu = put_table(tb, f->dead_bmu);
@@ -616,6 +648,8 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     m.swco = sf->swco; m.sat_water = sf->water; m.sat_gas = sf->gas;
     m.nsat = f->nsat;
     m.rs = int(tb.size()); tb.insert(tb.end(), f->sat_rs, f->sat_rs + f->nsat);
+    m.rsk = int(tb.size());
+    for (int k = 0; k < f->nsat; ++k) tb.push_back(host_key(f->sat_rs[k]));
     m.bsat = int(tb.size()); tb.insert(tb.end(), f->sat_b, f->sat_b + f->nsat);
     m.bmusat = int(tb.size()); tb.insert(tb.end(), f->sat_bmu, f->sat_bmu + f->nsat);
     std::vector<Tab> ut;

@@ -401,6 +401,174 @@ def ensemble(n_real: int = 64, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0, d
     return [ensemble_member(r, nx, ny, nz, sigma, seed0, dt) for r in range(n_real)]
 
 
+def black_oil_tables() -> dict:
+    """Synthetic black-oil fluid and saturation tables in the layout of the device assembler (ressim_gb300.assembly):
+    live oil from Standing's bubble-point correlation and Beggs-Robinson viscosities (API 35, gas gravity 0.8,
+    180 F), undersaturated ratio tables, dry gas with a constant z-factor, Corey SWOF / SGOF (Swc = Sor = 0.2,
+    exponents 2), field units. A stand-in of the engine's correlation-generated tables for timing the assembly."""
+    api, gg, temp = 35.0, 0.8, 180.0
+    go = 141.5 / (131.5 + api)
+    pb = np.linspace(14.7, 4500.0, 12)
+    rs_scf = gg * ((pb / 18.2 + 1.4) * 10 ** (0.0125 * api - 0.00091 * temp)) ** 1.2048
+    bo = 0.9759 + 0.000120 * (rs_scf * math.sqrt(gg / go) + 1.25 * temp) ** 1.2
+    mu_od = 10 ** (10 ** (3.0324 - 0.02023 * api) * temp ** -1.163) - 1.0
+    mu_o = 10.715 * (rs_scf + 100.0) ** -0.515 * mu_od ** (5.44 * (rs_scf + 150.0) ** -0.338)
+    rs = rs_scf / 1000.0                                  # Mscf/stb
+    dpu = np.array([0.0, 500.0, 1000.0, 2000.0, 5000.0])
+    ub_y = 1.0 + 1.0e-5 * dpu
+    ubmu_y = (1.0 + 1.0e-5 * dpu) / (1.0 + 4.0e-5 * dpu)
+    pg = np.linspace(0.0, 9000.0, 13)
+    bg = pg / (5.04 * 0.9 * (temp + 460.0))               # 1/Bg, Mscf/rb
+    mug = 0.0125 + 1.0e-6 * pg
+    sw = np.linspace(0.2, 1.0, 17)
+    swn = np.clip((sw - 0.2) / 0.6, 0.0, 1.0)
+    krw = 0.6 * swn ** 2
+    krow = np.clip((0.8 - sw) / 0.6, 0.0, 1.0) ** 2
+    sg = np.linspace(0.0, 0.8, 17)
+    krg = 0.8 * (sg / 0.8) ** 2
+    krog = ((0.8 - sg) / 0.8) ** 2
+    z = {}
+
+    def tab(name, x, y, clamp):
+        z[name + "_x"], z[name + "_y"], z[name + "_clamp"] = np.asarray(x, float), np.asarray(y, float), np.array([clamp], np.int32)
+
+    tab("rsOfP", pb, rs, 0)
+    tab("pbOfRs", rs, pb, 0)
+    tab("deadB", [], [], 0)
+    tab("deadBMu", [], [], 0)
+    tab("gasB", pg, bg, 0)
+    tab("gasBMu", pg, bg / mug, 0)
+    tab("krw", sw, krw, 1)
+    tab("krow", sw, krow, 1)
+    tab("pcow", sw, np.zeros_like(sw), 1)
+    tab("krg", sg, krg, 1)
+    tab("krog", sg, krog, 1)
+    tab("pcog", sg, np.zeros_like(sg), 1)
+    z["liveRs"], z["livePb"], z["bSat"], z["bmuSat"] = rs, pb, 1.0 / bo, 1.0 / (bo * mu_o)
+    n = pb.size
+    for name, y in (("uB", ub_y), ("uBMu", ubmu_y)):
+        z[name + "_x"] = np.tile(dpu, n)
+        z[name + "_y"] = np.tile(y, n)
+        z[name + "_off"] = (np.arange(n + 1) * dpu.size).astype(np.int32)
+        z[name + "_clamp"] = np.zeros(n, np.int32)
+    z["phases"] = np.array([1, 1, 1, 1, 0], np.uint8)
+    z["vars"] = np.array([1, 2, 0, 1, 2], np.int32)
+    z["pvtw"] = np.array([4014.7, 1.029, 3.13e-6, 0.31, 0.0])
+    z["rock"] = np.array([14.7, 3.0e-6])
+    z["rhoSC"] = np.array([53.0, 64.79, 0.0573])
+    z["gasFactor"] = np.array([1000.0 / 5.614583])
+    z["gravity"] = np.array([1.0 / 144.0])
+    z["swco"] = np.array([0.2])
+    z["kroModel"] = np.array([0], np.int32)
+    z["sat_flags"] = np.array([1, 1, 0], np.uint8)
+    z["fluid_flags"] = np.array([1, 0], np.uint8)
+    return z
+
+
+def assembly_grid(nx, ny, nz, *, sigma=1.5, seed=0, actnum_fraction=0.0, dx=100.0, dy=100.0, dz=20.0, kmean=100.0):
+    """The active cells, 7-point connections (transmissibility, depth difference) and pore volumes of make_system's
+    grid with the same seed (same permeability field and inactive-cell mask), plus a seeded black-oil state: pressure
+    with the hydrostatic gradient, water saturation, free gas (state 1, x = Sg) in the top quarter of the layers and
+    undersaturated oil (state 0, x = Rs) below."""
+    rng = np.random.default_rng(seed)
+    shape = (nz, ny, nx)
+    zf = correlated_normal(shape, (5, 5, 1), rng)
+    lnk = math.log(kmean) + sigma * zf
+    k = np.exp(lnk)
+    phi = np.clip(0.05 + 0.02 * lnk, 0.01, 0.45)
+    active = np.ones(shape, dtype=bool)
+    if actnum_fraction > 0:
+        f = correlated_normal(shape, (6, 6, 2), rng)
+        active = f > np.quantile(f, actnum_fraction)
+    act = active.reshape(-1)
+    idx = np.full(act.size, -1, dtype=np.int64)
+    na = int(act.sum())
+    idx[act] = np.arange(na)
+    kf = k.reshape(-1)[act]
+    kk_, jj_, ii_ = np.unravel_index(np.nonzero(act)[0], shape)
+    depth = 8325.0 + (kk_ + 0.5) * dz
+    ca, cb, ct, cd = [], [], [], []
+    for (di, dj, dk, area, dist) in ((1, 0, 0, dy * dz, dx), (0, 1, 0, dx * dz, dy), (0, 0, 1, dx * dy, dz)):
+        m = np.ones(shape, dtype=bool)
+        if di:
+            m[:, :, -1] = False
+        if dj:
+            m[:, -1, :] = False
+        if dk:
+            m[-1, :, :] = False
+        src = np.nonzero(m.reshape(-1))[0]
+        a, b_ = idx[src], idx[src + di + dj * nx + dk * nx * ny]
+        ok = (a >= 0) & (b_ >= 0)
+        a, b_ = a[ok], b_[ok]
+        kz = 0.1 if dk else 1.0
+        ca.append(a); cb.append(b_)
+        ct.append(0.001127 * 2.0 / (1.0 / (kz * kf[a]) + 1.0 / (kz * kf[b_])) * area / dist)
+        cd.append(depth[b_] - depth[a])
+    pv = phi.reshape(-1)[act] * dx * dy * dz / 5.614583
+    p = 4000.0 + 0.45 * (depth - 8325.0) + 200.0 * np.sin(0.1 * ii_) * np.cos(0.08 * jj_) + 5.0 * rng.standard_normal(na)
+    sw = np.clip(0.2 + 0.4 * rng.random(na), 0.2, 0.79)
+    state = np.where(kk_ < max(1, nz // 4), 1, 0).astype(np.uint8)
+    x = np.where(state == 1, 0.02 + 0.1 * rng.random(na), 0.5 + 0.3 * rng.random(na))
+    acc_old = np.stack([pv * 0.97 * sw, pv * 0.8 * (1 - sw), pv * (0.8 * (1 - sw) * 0.6 + 0.05)], axis=1).reshape(-1)
+    return dict(na=na, ca=np.concatenate(ca), cb=np.concatenate(cb), trans=np.concatenate(ct), dDepth=np.concatenate(cd),
+                pv=pv, p=p, sw=sw, x=x, state=state, acc_old=acc_old)
+
+
+def assembly_model(grids) -> dict:
+    """The device assembler's model (ressim_gb300.assembly) of one or more grids taken together as one disconnected
+    grid, without wells, and the concatenated state: the engine's scalar Jacobian pattern (cell row a*3+e holds the
+    blocks of the cell and its neighbours in column order) and adjacency (per cell, its connections in connection
+    order)."""
+    ca, cb, tr, dd, pv, st = [], [], [], [], [], {k: [] for k in ("p", "sw", "x", "state", "acc_old")}
+    off = 0
+    for g in grids:
+        ca.append(g["ca"] + off); cb.append(g["cb"] + off)
+        tr.append(g["trans"]); dd.append(g["dDepth"]); pv.append(g["pv"])
+        for k in st:
+            st[k].append(g[k])
+        off += g["na"]
+    na = off
+    ca, cb = np.concatenate(ca).astype(np.int64), np.concatenate(cb).astype(np.int64)
+    nconn = ca.size
+    # adjacency: every connection from both sides, ordered by cell then connection index
+    own = np.concatenate([ca, cb])
+    nbr = np.concatenate([cb, ca])
+    cid = np.concatenate([np.arange(nconn), np.arange(nconn)])
+    o = np.lexsort((cid, own))
+    adjStart = np.zeros(na + 1, np.int64)
+    np.add.at(adjStart, own + 1, 1)
+    adjStart = np.cumsum(adjStart)
+    # pattern: per cell its sorted blocks (self and neighbours), three rows with the same columns
+    bown = np.concatenate([own, np.arange(na)])
+    bnb = np.concatenate([nbr, np.arange(na)])
+    ob = np.lexsort((bnb, bown))
+    bnb = bnb[ob]
+    cnt = np.bincount(bown, minlength=na)
+    bstart = np.concatenate([[0], np.cumsum(cnt)])
+    cellcols = (3 * bnb[:, None] + np.arange(3)).reshape(-1)
+    rowlen = np.repeat(3 * cnt, 3)
+    rowPtr = np.concatenate([[0], np.cumsum(rowlen)])
+    a_of_row = np.repeat(np.arange(na), 3)
+    base = np.repeat(3 * bstart[a_of_row] - rowPtr[:-1], rowlen)
+    J_col = cellcols[np.arange(rowPtr[-1]) + base]
+    z = black_oil_tables()
+    z.update(na=np.array([na]), nv=np.array([3]), nw=np.array([0]), adjStart=adjStart.astype(np.int32),
+             adjNbr=nbr[o].astype(np.int32), adjConn=cid[o].astype(np.int32), conn_a=ca.astype(np.int32),
+             conn_b=cb.astype(np.int32), conn_trans=np.concatenate(tr), conn_dDepth=np.concatenate(dd),
+             poreVolRef=np.concatenate(pv), J_rowPtr=rowPtr.astype(np.int32), J_col=J_col.astype(np.int32))
+    state = {k: np.concatenate(v) for k, v in st.items()}
+    return z, state
+
+
+def assembly_ensemble(n_real: int = 64, nx=40, ny=40, nz=10, sigma=1.5, seed0: int = 0):
+    """The ensemble's grids (same permeability seeds and inactive-cell masks as ensemble()) as one assembly model."""
+    grids = []
+    for r in range(n_real):
+        frac = float(np.random.default_rng(10_000 + seed0 + r).uniform(0.1, 0.5))
+        grids.append(assembly_grid(nx, ny, nz, sigma=sigma, seed=seed0 + r, actnum_fraction=frac))
+    return assembly_model(grids)
+
+
 def serving_request(rng: np.random.Generator, cells_lo=1e3, cells_hi=1e6, max_cells=None) -> NewtonSystem:
     """One serving request: log-uniform cell count, random box with nz in [1, 50], sigma ln k in [0.5, 3],
     time step in [0.1, 30] days, 1-8 wells."""
