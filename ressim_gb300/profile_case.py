@@ -6,6 +6,7 @@ workload, for ncu captures of single kernels or of one step's launch list (the b
     python -m ressim_gb300.profile_case ensemble64 --applications 3
     python -m ressim_gb300.profile_case ensemble64 --steps 2
     python -m ressim_gb300.profile_case ensemble64 --steps 1 --sweep cta     # the one-kernel CPR application
+    python -m ressim_gb300.profile_case bilu0_grid180k --precision fp64 --steps 1 --krylov gmres   # GMRES kernels
 
 cpr_grid810k: 180x90x50 cells (810,000 block rows, sigma ln k = 1.5, 4 wells), CPR applied grid-wide (a system
 this size does not fit one SM). bilu0_grid180k: 100x60x30 cells (180,000 block rows), BILU0 with the grid-wide
@@ -37,6 +38,8 @@ def main(argv=None):
     ap.add_argument("--vcycle-form", type=int, default=0,
                     help="split CPR V-cycle: 1 fused kernel, 2 separate launches, 3 coarse levels per system, 0 tuned")
     ap.add_argument("--cpr2-threads", type=int, default=0, help="split CPR BILU0 stage: 256 or 512 threads per system, 0 tuned")
+    ap.add_argument("--krylov", default="bicgstab", choices=["bicgstab", "gmres"], help="Krylov method of --steps")
+    ap.add_argument("--restart", type=int, default=30, help="GMRES restart length")
     args = ap.parse_args(argv)
     from ressim_gb300 import synth
     from ressim_gb300.solver import DeviceSolver
@@ -47,8 +50,9 @@ def main(argv=None):
     else:
         s = synth.make_system(*c["shape"], sigma=1.5, seed=3, dt=5.0, wells="random", n_wells=4)
         mats, b = [s.A], s.b
-    d = DeviceSolver(precond=c["precond"], precision=args.precision, sweep=args.sweep or c["sweep"], krylov="bicgstab",
-                     check_every=4, use_graphs=True, vcycle_form=args.vcycle_form, cpr2_threads=args.cpr2_threads)
+    d = DeviceSolver(precond=c["precond"], precision=args.precision, sweep=args.sweep or c["sweep"], krylov=args.krylov,
+                     restart=args.restart, check_every=4, use_graphs=True, vcycle_form=args.vcycle_form,
+                     cpr2_threads=args.cpr2_threads)
     if len(mats) > 1:
         d.set_batch(mats)
     else:
