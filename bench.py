@@ -679,19 +679,36 @@ def main():
     roofline_spmv = {"bound": "hbm", "kernel": "bsr3_spmv_f64", "achieved": kernels["bsr3_spmv_f64"]["gbs"], "peak": hbm,
                      "unit": "GB/s", "frac": kernels["bsr3_spmv_f64"]["gbs"] / hbm}
 
-    # ---------------- e2e through the C ABI with host buffers (values + rhs in, solutions out, every step)
-    x_host = np.zeros(N)
+    # ---------------- e2e through the C ABI with host buffers (values + rhs in, solutions out, every step), the step's
+    # inputs and its solution in pinned host memory (the engine's staging buffers)
     from ressim_gb300 import _lib
+    from ressim_gb300.bsr import BSR
     import ctypes as C
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64).pin_memory()
+        out = t.numpy()
+        out[:] = a.reshape(-1)
+        return out, t
+
+    keep_pinned = []
+    mats_pinned = []
+    for A in mats:
+        v, t = pinned(A.val)
+        keep_pinned.append(t)
+        mats_pinned.append(BSR(A.n, A.nb, A.rowPtr, A.col, v))
+    b_pin, tb = pinned(b_host)
+    x_host, tx = pinned(np.zeros(N))
+    keep_pinned += [tb, tx]
     L = _lib.load()
     e2e_t = []
     for k in range(args.warmup + args.steps):
         barrier()
         t0 = time.perf_counter()
-        dev.set_batch(mats)
+        dev.set_batch(mats_pinned)
         dev.setup()
         itc, rrc = C.c_int(0), C.c_double(0)
-        rc = L.rsg_solve(dev.h, _lib.ptr(b_host), _lib.ptr(x_host), TOL, MAXIT, C.byref(itc), C.byref(rrc))
+        rc = L.rsg_solve(dev.h, _lib.ptr(b_pin), _lib.ptr(x_host), TOL, MAXIT, C.byref(itc), C.byref(rrc))
         _lib.check(rc)
         barrier()
         if k >= args.warmup:
@@ -700,7 +717,7 @@ def main():
     if dist:
         Te = max_over_ranks(Te, dist, f"cuda:{local}")
     e2e = {"value": world * N_REAL * len(e2e_t) / Te, "unit": "solves/s", "h2d_bytes_per_step": val_bytes + N * 8,
-           "d2h_bytes_per_step": N * 8, "p50_ms": 1e3 * statistics.median(e2e_t)}
+           "d2h_bytes_per_step": N * 8, "p50_ms": 1e3 * statistics.median(e2e_t), "host_buffers": "pinned"}
     dev.close()
 
     # ---------------- plain FP64 GPU path: one system after another (one handle each)

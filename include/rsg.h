@@ -80,7 +80,7 @@ typedef struct rsg_options {
                                one cooperative kernel (grid barriers between them); 2 = every pass grid-wide, one launch
                                per pass; 3 = the finest level's passes grid-wide, the coarser levels one thread block per
                                system in one launch; 0 = tuned (default 3) */
-    int cpr2_threads;       /* split CPR: threads per system of the BILU0 stage, 256 or 512; 0 = tuned (default 256) */
+    int cpr2_threads;       /* split CPR: threads per system of the BILU0 stage, 128, 256 or 512; 0 = tuned (default 256) */
 } rsg_options;
 
 typedef struct rsg_stats {

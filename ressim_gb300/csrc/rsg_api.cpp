@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <future>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -409,7 +410,39 @@ int do_set_batch(rsg_solver* h, int nsys, int nb, const int* n, const int* const
     }
     if (h->genActive) free_plan(h);
     for (int s = 0; s < nsys; ++s)
-        if (!val[s]) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " has no values");
+        if (!val[s] || !rowPtr[s] || !col[s] || n[s] < 1) return fail(RSG_EINVAL, "set_batch: system " + std::to_string(s) + " is empty");
+    // A new Newton iteration of the planned batch (same sizes): the values go up while another thread confirms the
+    // pattern; if the pattern turns out to differ, the batch is planned again and its values uploaded again.
+    if (h->havePlan && !h->jac && h->plan.nsys == nsys && int(h->plan.sysRow0.size()) == nsys + 1) {
+        const HostPlan& P = h->plan;
+        bool sizes = true;
+        std::vector<int> nnzbs(static_cast<size_t>(nsys));
+        for (int s = 0; s < nsys && sizes; ++s) {
+            const size_t r0 = size_t(P.sysRow0[size_t(s)]), r1 = size_t(P.sysRow0[size_t(s) + 1]);
+            nnzbs[size_t(s)] = rowPtr[s][n[s]];
+            sizes = int(r1 - r0) == n[s] && P.rowPtr0[r1] - P.rowPtr0[r0] == nnzbs[size_t(s)];
+        }
+        if (sizes) {
+            auto check = std::async(std::launch::async, [&] { return same_batch_pattern(P, nsys, n, rowPtr, col); });
+            size_t off = 0;
+            cudaError_t e = cudaSuccess;
+            for (int s = 0; s < nsys && e == cudaSuccess; ++s) {
+                const size_t cnt = size_t(nnzbs[size_t(s)]) * NB2;
+                if (cnt) e = cudaMemcpyAsync(h->val0 + off, val[s], cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+                off += cnt;
+            }
+            const bool same = check.get();
+            if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+            if (same) {
+                launch_gather_blocks(h->dp, h->val0, h->val, h->stream);   // into level space
+                h->launches += 1;
+                RSG_CUDA(cudaGetLastError());
+                h->haveMatrix = true;
+                h->haveSetup = false;
+                return RSG_OK;
+            }
+        }
+    }
     std::vector<int> nnzbs;
     int rc = set_batch_pattern(h, nsys, n, rowPtr, col, nnzbs);
     if (rc) return rc;
@@ -997,7 +1030,7 @@ int tune_shapes(rsg_solver* h) {
         cand.push_back(c);
     }
     for (int f : {3, 2, 1})
-        for (int thr : {256, 512}) {
+        for (int thr : {256, 512, 128}) {
             if (!free_form && f != t.vform) continue;
             if (!free_thr && thr != t.cpr2Threads) continue;
             if (f == 1 && h->amg.nPhases == 0) continue;
@@ -1090,7 +1123,9 @@ int do_setup(rsg_solver* h, const double* acc) {
 
 // what a captured graph depends on besides its iteration count: the preconditioner's kind and launch shapes
 int graph_kind(const PrecDev& M) {
-    return M.kind * 8 + (M.cpr ? 4 : 0) + (M.cta ? 2 : 0) + (M.split ? 1 : 0) + 16 * (M.vform + 4 * (M.cpr2Threads >= 512 ? 1 : 0));
+    // distinct fields: kind 0-3, the three form flags, V-cycle form 0-3, BILU0-stage thread count (256 / 512 / 128)
+    return (M.kind & 3) | (M.cpr ? 4 : 0) | (M.cta ? 8 : 0) | (M.split ? 16 : 0) | ((M.vform & 3) << 5) |
+           ((M.cpr2Threads >= 512 ? 1 : M.cpr2Threads <= 128 ? 2 : 0) << 7);
 }
 
 int launch_iterations(rsg_solver* h, int k) {
@@ -1549,8 +1584,9 @@ int rsg_create(rsg_solver** out, const rsg_options* opts) {
     if (opts) o = *opts;
     if (o.precond < 0 || o.precond > 4 || o.krylov < 0 || o.krylov > 1 || o.precision < 0 || o.precision > 2 || o.sweep < 0 || o.sweep > 3)
         return fail(RSG_EINVAL, "invalid options");
-    if (o.vcycle_form < 0 || o.vcycle_form > 3 || (o.cpr2_threads != 0 && o.cpr2_threads != 256 && o.cpr2_threads != 512))
-        return fail(RSG_EINVAL, "invalid launch shape options (vcycle_form 0..3, cpr2_threads 0 / 256 / 512)");
+    if (o.vcycle_form < 0 || o.vcycle_form > 3 ||
+        (o.cpr2_threads != 0 && o.cpr2_threads != 128 && o.cpr2_threads != 256 && o.cpr2_threads != 512))
+        return fail(RSG_EINVAL, "invalid launch shape options (vcycle_form 0..3, cpr2_threads 0 / 128 / 256 / 512)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(RSG_ECUDA, "no CUDA device available");
     if (o.device < 0 || o.device >= ndev) return fail(RSG_EINVAL, "device ordinal out of range");

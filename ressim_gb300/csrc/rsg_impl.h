@@ -395,7 +395,7 @@ struct PrecDev {
                                       // the BILU0 sweeps one thread block per system
     int vform = 2;                    // split CPR V-cycle: 1 fused cooperative kernel, 2 one launch per pass, 3 coarse
                                       // levels one thread block per system
-    int cpr2Threads = 256;            // split CPR: threads per block of the BILU0 stage (256 or 512; same results)
+    int cpr2Threads = 256;            // split CPR: threads per block of the BILU0 stage (128, 256 or 512; same results)
     const DevAmg* amg = nullptr;
 };
 // all-FP32 factorisation (FP32 elimination, FP64 pivot inversion), one thread block per system

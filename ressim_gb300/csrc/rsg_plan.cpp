@@ -3,6 +3,8 @@
 #include "rsg_impl.h"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -260,22 +262,50 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     return true;
 }
 
+namespace {
+// One system of a batch against the plan: its row starts relative to the system, its columns relative to the
+// system's first row. Branch-free chunks (the compiler vectorises them) with an exit between chunks.
+bool same_system(const HostPlan& P, int s, int ns, const int* rp, const int* c) {
+    constexpr int CH = 4096;
+    const int r0 = P.sysRow0[size_t(s)];
+    const int base = P.rowPtr0[size_t(r0)];
+    const int* prp = P.rowPtr0.data() + r0;
+    for (int i0 = 0; i0 <= ns; i0 += CH) {
+        const int i1 = std::min(ns + 1, i0 + CH);
+        int diff = 0;
+        for (int i = i0; i < i1; ++i) diff |= (prp[i] - base) ^ rp[i];
+        if (diff) return false;
+    }
+    const int* pc = P.col0.data() + base;
+    const int m = rp[ns];
+    for (int p0 = 0; p0 < m; p0 += CH) {
+        const int p1 = std::min(m, p0 + CH);
+        int diff = 0;
+        for (int p = p0; p < p1; ++p) diff |= (pc[p] - r0) ^ c[p];
+        if (diff) return false;
+    }
+    return true;
+}
+}  // namespace
+
 bool same_batch_pattern(const HostPlan& P, int nsys, const int* n, const int* const* rowPtr, const int* const* col) {
     if (P.nsys != nsys || int(P.sysRow0.size()) != nsys + 1) return false;
     for (int s = 0; s < nsys; ++s)
         if (P.sysRow0[size_t(s) + 1] - P.sysRow0[size_t(s)] != n[s]) return false;
-    for (int s = 0; s < nsys; ++s) {
-        const int r0 = P.sysRow0[size_t(s)];
-        const int base = P.rowPtr0[size_t(r0)];
-        const int* rp = rowPtr[s];
-        for (int i = 0; i <= n[s]; ++i)
-            if (P.rowPtr0[size_t(r0 + i)] - base != rp[i]) return false;
-        const int* pc = P.col0.data() + base;
-        const int* c = col[s];
-        for (int p = 0; p < rp[n[s]]; ++p)
-            if (pc[p] - r0 != c[p]) return false;
-    }
-    return true;
+    // large batches: the systems are compared on several threads (independent, read-only)
+    const int hw = int(std::max(1u, std::thread::hardware_concurrency()));
+    const int T = P.col0.size() > (size_t(1) << 20) ? std::min({8, hw, nsys}) : 1;
+    std::atomic<bool> ok{true};
+    std::atomic<int> next{0};
+    auto work = [&] {
+        for (int s = next++; s < nsys && ok.load(std::memory_order_relaxed); s = next++)
+            if (!same_system(P, s, n[s], rowPtr[s], col[s])) ok = false;
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; ++t) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    return ok;
 }
 
 // ====================================================================== well Schur complement

@@ -1963,8 +1963,8 @@ __global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const 
     }
 }
 
-// second stage of the split form: TF = TA (FP64 factors in the FP64 form, FP32 otherwise), TV = TT; 256 or 512 threads
-// per system (every row is swept by one thread in the same arithmetic either way)
+// second stage of the split form: TF = TA (FP64 factors in the FP64 form, FP32 otherwise), TV = TT; 128, 256 or 512
+// threads per system (every row is swept by one thread in the same arithmetic either way)
 template <class TF, class TV, class TA, int NT>
 void launch_cpr2_nt(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, const TV* T, double* z, TV* yglob,
                     const KScal* ks, cudaStream_t st) {
@@ -1977,15 +1977,18 @@ void launch_cpr2_nt(const DevPlan& P, const PrecDev& M, const DevAmg& G, const C
 template <class TA, class TT>
 void launch_cpr2(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, TT* Tsplit, double* z, const KScal* ks,
                  cudaStream_t st) {
-    const bool wide = M.cpr2Threads >= 512;
+    const int nt = M.cpr2Threads;
     if constexpr (sizeof(TA) == 8) {
-        if (wide) launch_cpr2_nt<double, double, TA, 512>(P, M, G, C, Tsplit, z, z, ks, st);
+        if (nt >= 512) launch_cpr2_nt<double, double, TA, 512>(P, M, G, C, Tsplit, z, z, ks, st);
+        else if (nt <= 128) launch_cpr2_nt<double, double, TA, 128>(P, M, G, C, Tsplit, z, z, ks, st);
         else launch_cpr2_nt<double, double, TA, 256>(P, M, G, C, Tsplit, z, z, ks, st);
     } else if constexpr (sizeof(TT) == 8) {
-        if (wide) launch_cpr2_nt<float, double, TA, 512>(P, M, G, C, Tsplit, z, z, ks, st);
+        if (nt >= 512) launch_cpr2_nt<float, double, TA, 512>(P, M, G, C, Tsplit, z, z, ks, st);
+        else if (nt <= 128) launch_cpr2_nt<float, double, TA, 128>(P, M, G, C, Tsplit, z, z, ks, st);
         else launch_cpr2_nt<float, double, TA, 256>(P, M, G, C, Tsplit, z, z, ks, st);
     } else {
-        if (wide) launch_cpr2_nt<float, float, TA, 512>(P, M, G, C, Tsplit, z, M.y32, ks, st);
+        if (nt >= 512) launch_cpr2_nt<float, float, TA, 512>(P, M, G, C, Tsplit, z, M.y32, ks, st);
+        else if (nt <= 128) launch_cpr2_nt<float, float, TA, 128>(P, M, G, C, Tsplit, z, M.y32, ks, st);
         else launch_cpr2_nt<float, float, TA, 256>(P, M, G, C, Tsplit, z, M.y32, ks, st);
     }
 }

@@ -836,13 +836,13 @@ def test_refined_solve_batch_stops_converged_systems():
 def test_launch_shapes_give_identical_results(precision):
     """Every launch shape the autotuner chooses among computes the same values: the split CPR's V-cycle as one launch
     per pass, as the phases of one cooperative kernel, or with its coarse levels one thread block per system, and its
-    BILU0 stage with 256 or 512 threads per system -- preconditioner output, solution and iterations bit for bit, on a
-    batch with well cliques."""
+    BILU0 stage with 128, 256 or 512 threads per system -- preconditioner output, solution and iterations bit for bit, on
+    a batch with well cliques."""
     from ressim_gb300 import synth
     systems = synth.ensemble(n_real=6, nx=24, ny=24, nz=6, sigma=1.5)
     b = np.concatenate([s.b for s in systems])
     out = []
-    for form, thr in ((2, 256), (1, 256), (3, 256), (3, 512), (2, 512)):
+    for form, thr in ((2, 256), (1, 256), (3, 256), (3, 512), (2, 512), (3, 128), (1, 128)):
         with dev(precond="cpr", precision=precision, sweep="split", autotune=False, vcycle_form=form, cpr2_threads=thr) as d:
             d.set_batch([s.A for s in systems])
             d.setup()
@@ -865,7 +865,7 @@ def test_autotuner_reports_its_choice():
         d.set_batch([s.A for s in systems])
         d.setup()
         t1 = d.tuning()
-    assert "source=tuned" in t1 and "form3/256" in t1 and "form2/512" in t1
+    assert "source=tuned" in t1 and "form3/256" in t1 and "form2/512" in t1 and "form3/128" in t1
     with dev(precond="cpr", precision="mixed_f32", sweep="split") as d:
         d.set_batch([s.A for s in systems])
         d.setup()
