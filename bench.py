@@ -317,15 +317,18 @@ def serving_ensemble(local, systems, rounds=3):
 
 def assembly_bytes(z):
     """Bytes the assembly must move at least once per call: the state and old accumulations, the grid (adjacency,
-    connections, pore volumes, row starts of the pattern), the Jacobian and residual written, and the per-cell
-    property records (13 dual numbers) written by k_bo_props and read once by k_bo_cells."""
+    connections, pore volumes, row starts of the pattern), the Jacobian and residual written, the per-cell property
+    records (13 dual numbers) written by k_bo_props and read once, and the per-connection flux terms (4 x 7 doubles)
+    written by k_bo_conn and read once from each of the connection's two cells."""
     na, nconn = int(z["na"][0]), int(z["conn_trans"].size)
     nadj, nnz, nrows = int(z["adjStart"][-1]), int(z["J_rowPtr"][-1]), na * 3 + int(z["nw"][0])
     state = na * (3 * 8 + 1 + 3 * 8 + 8)
     grid = (na + 1) * 4 + nadj * 12 + nconn * 20 + (nrows + 1) * 4 + na * 8
     out = nnz * 8 + nrows * 8
     rec = 2 * 52 * 8 * na
-    return {"state": state, "grid": grid, "jacobian_and_residual": out, "records": rec, "total": state + grid + out + rec}
+    flux = 3 * 28 * 8 * nconn
+    return {"state": state, "grid": grid, "jacobian_and_residual": out, "records": rec, "connection_fluxes": flux,
+            "total": state + grid + out + rec + flux}
 
 
 def assembly_leg(local, steps, warmup):
@@ -382,7 +385,7 @@ def assembly_leg(local, steps, warmup):
     h2d = sum(int(v.numel() * v.element_size()) for v in host.values())
     return {"workload": f"ensemble{N_REAL}_{NX}x{NY}x{NZ} grids as one ({na} cells, synthetic tables and state)",
             "cells": na, "jacobian_values": int(asm.nnz), "ms": 1e3 * t, "value": na / t, "unit": "cells/s",
-            "launches_per_assembly": 2, "bytes": B, "roofline": {"bound": "hbm", "achieved": B["total"] / t / 1e9, "peak": hbm,
+            "launches_per_assembly": 3, "bytes": B, "roofline": {"bound": "hbm", "achieved": B["total"] / t / 1e9, "peak": hbm,
                                                                  "unit": "GB/s", "frac": B["total"] / t / 1e9 / hbm,
                                                                  "peak_kind": peak_kind + " burst copy"},
             "e2e": {"ms": 1e3 * statistics.median(te), "h2d_bytes": h2d, "d2h_bytes": asm.nrows * 8,

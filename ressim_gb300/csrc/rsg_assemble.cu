@@ -301,10 +301,95 @@ __device__ __forceinline__ D3 ld3(const double* __restrict__ rec, size_t N, int 
               __ldg(rec + (4 * field + 3) * N + c)};
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Phase flux over a connection, in the perspective of its cell a (Simulator::assemble, engine/src/simulator.cpp:
+// 2567-2620): dphi = P_a - P_b + rho g dD with rho = (rho_a + rho_b) / 2, F = mob_upstream dphi T. The dual numbers
+// carry a's derivatives (fa) and b's (fb); the slots a lifted operand does not have are exact zeros, so their
+// products and sums are left out (x + 0 and 0 * y change no value), and so is the gravity term of a connection
+// without depth difference.
+struct Dphi {
+    double v, da[3], db[3];
+};
+
+__device__ __forceinline__ Dphi dphi_of(const double* __restrict__ rec, size_t N, int p, int b, const D3& PA, const D3& RA, double gd) {
+    const D3 PB = ld3(rec, N, p, b);
+    Dphi d{PA.v - PB.v, {PA.d0, PA.d1, PA.d2}, {-PB.d0, -PB.d1, -PB.d2}};
+    if (gd != 0.0) {
+        const D3 RB = ld3(rec, N, 6 + p, b);
+        d.v = d.v + ((RA.v + RB.v) * 0.5) * gd;
+        d.da[0] = d.da[0] + (RA.d0 * 0.5) * gd;
+        d.da[1] = d.da[1] + (RA.d1 * 0.5) * gd;
+        d.da[2] = d.da[2] + (RA.d2 * 0.5) * gd;
+        d.db[0] = d.db[0] + (RB.d0 * 0.5) * gd;
+        d.db[1] = d.db[1] + (RB.d1 * 0.5) * gd;
+        d.db[2] = d.db[2] + (RB.d2 * 0.5) * gd;
+    }
+    return d;
+}
+
+struct Flux {
+    double v, fa[3], fb[3];
+};
+
+// F = mob dphi T with the upstream cell's mobility `mo` (its own derivatives in the first or the second slots)
+__device__ __forceinline__ Flux flux_of(const D3& mo, bool upA, const Dphi& d, double tr) {
+    Flux F;
+    const double mu[3] = {mo.d0, mo.d1, mo.d2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        F.fa[i] = (upA ? mu[i] * d.v + mo.v * d.da[i] : mo.v * d.da[i]) * tr;
+        F.fb[i] = (upA ? mo.v * d.db[i] : mu[i] * d.v + mo.v * d.db[i]) * tr;
+    }
+    F.v = (mo.v * d.v) * tr;
+    return F;
+}
+
+constexpr int kFluxKinds = 4;                 // per connection: water, oil, dissolved gas (with the oil), gas
+constexpr int kFluxWords = kFluxKinds * 7;    // value, the first cell's 3 derivatives, the second's 3
+
+// The fluxes of every connection, once, in the perspective of its first cell a (conn_a). Seen from its second cell b
+// the engine's flux is the exact negative with the slots exchanged -- -(x) + -(y) = -(x + y) and (-x) y = -(x y) in
+// IEEE arithmetic, and b takes the same cell as upstream -- except where the potential difference is exactly zero
+// (then each side takes itself as upstream) or not a number: those phases are flagged and their two cells form them
+// themselves. Record layout: word j of term k of connection c at flux[(7 k + j) nconn + c].
+__global__ void __launch_bounds__(kThreads) k_bo_conn(int nconn, int na, Model m, const double* __restrict__ rec,
+                                                      const int* __restrict__ connA, const int* __restrict__ connB,
+                                                      const double* __restrict__ trans, const double* __restrict__ dDepth,
+                                                      double* __restrict__ flux, unsigned char* __restrict__ flag) {
+    const int c = blockIdx.x * kThreads + threadIdx.x;
+    if (c >= nconn) return;
+    const size_t N = size_t(na), NC = size_t(nconn);
+    const int a = __ldg(connA + c), b = __ldg(connB + c);
+    const double tr = __ldg(trans + c);
+    const double gd = m.gravity * __ldg(dDepth + c);
+    unsigned fl = 0;
+    auto put = [&](int k, const Flux& F) {
+        flux[(7 * k + 0) * NC + c] = F.v;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            flux[(7 * k + 1 + i) * NC + c] = F.fa[i];
+            flux[(7 * k + 4 + i) * NC + c] = F.fb[i];
+        }
+    };
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        const Dphi d = dphi_of(rec, N, p, b, ld3(rec, N, p, a), ld3(rec, N, 6 + p, a), gd);
+        if (!(d.v > 0 || d.v < 0)) { fl |= 1u << p; continue; }
+        const bool upA = d.v >= 0;
+        const int up = upA ? a : b;
+        put(p == PG ? 3 : p, flux_of(ld3(rec, N, 3 + p, up), upA, d, tr));
+        if (p == PO) put(2, flux_of(ld3(rec, N, 9, up), upA, d, tr));
+    }
+    flag[c] = static_cast<unsigned char>(fl);
+}
+
 // Accumulation and TPFA flux terms of cell a's rows (Simulator::assemble cell loop, engine/src/simulator.cpp:2511-2686,
-// without the features this model leaves out), then the row scaling dt / PV (:3010-3032). Rows that take well terms
-// (cells listed in acell) are written unscaled and finished by k_bo_addends.
-__global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, Model m, double dt, const double* __restrict__ rec,
+// without the features this model leaves out), then the row scaling dt / PV (:3010-3032). The flux terms come from
+// k_bo_conn (negated and exchanged for the connections whose second cell a is), except for flagged phases, which
+// the cell forms itself. Rows that take well terms (cells listed in acell) are written unscaled and finished by
+// k_bo_addends.
+__global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, int nconn, Model m, double dt, const double* __restrict__ rec,
+                                                       const double* __restrict__ flux, const unsigned char* __restrict__ flag,
                                                        const double* __restrict__ accOld, const double* __restrict__ pv0,
                                                        const int* __restrict__ adjStart, const int* __restrict__ adjNbr,
                                                        const int* __restrict__ adjConn, const int* __restrict__ adjPos,
@@ -315,7 +400,7 @@ __global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, Model m, 
                                                        double* __restrict__ R) {
     const int a = blockIdx.x * kThreads + threadIdx.x;
     if (a >= na) return;
-    const size_t N = size_t(na);
+    const size_t N = size_t(na), NC = size_t(nconn);
     const double invDt = 1.0 / dt;
     // Accumulators per phase balance (the equation row of phase p is m.eq[p]): the cell's own block and residual.
     // The model has all three phases and dissolved gas (checked at creation), so the order of the terms is fixed: a
@@ -349,58 +434,51 @@ __global__ void __launch_bounds__(kThreads) k_bo_cells(int na, int nv, Model m, 
 #pragma unroll
     for (int p = 0; p < 3; ++p) rowp[p] = __ldg(Jrow + r0 + m.eq[p]);
     const int nblk = __ldg(blkStart + a + 1) - __ldg(blkStart + a);
-    const D3 PA[3] = {ld3(rec, N, 0, a), ld3(rec, N, 1, a), ld3(rec, N, 2, a)};
-    const D3 RA[3] = {ld3(rec, N, 6, a), ld3(rec, N, 7, a), ld3(rec, N, 8, a)};
     const int e1 = __ldg(adjStart + a + 1);
     for (int q = __ldg(adjStart + a); q < e1; ++q) {
         const int cn = __ldg(adjConn + q);
-        const int b = __ldg(adjNbr + q);
-        const double dD = __ldg(connA + cn) == a ? __ldg(dDepth + cn) : -__ldg(dDepth + cn);
-        const double tr = __ldg(trans + cn);
-        const double gd = m.gravity * dD;
+        const bool first = __ldg(connA + cn) == a;            // the connection's first cell: its fluxes as stored
+        const unsigned fl = __ldg(flag + cn);
         double nbk[3][3];   // the neighbour's block of this connection
-        // The dual numbers of a connection carry the cell's derivatives in slots 0-2 and the neighbour's in 3-5; the
-        // slots a lifted operand does not have are exact zeros, so their products and sums are left out (a term
-        // x + 0 or 0 * y changes no value), and so is the gravity term of a connection without depth difference.
+        // add one flux term to balance `bal`; `lead`: the connection's first term of that balance in nbk
+        auto add = [&](int bal, bool lead, double v, const double* own, const double* nb) {
+            sr[bal] += v;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                sj[bal][k] += own[k];
+                nbk[bal][k] = lead ? nb[k] : nbk[bal][k] + nb[k];
+            }
+        };
+        auto stored = [&](int kind, int bal, bool lead) {
+            double w[7];
+#pragma unroll
+            for (int j = 0; j < 7; ++j) w[j] = __ldg(flux + (7 * kind + j) * NC + cn);
+            if (first) add(bal, lead, w[0], w + 1, w + 4);
+            else {
+                const double own[3] = {-w[4], -w[5], -w[6]}, nb[3] = {-w[1], -w[2], -w[3]};
+                add(bal, lead, -w[0], own, nb);
+            }
+        };
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-            // dphi = P_a - P_b + rho g dD with rho = (rho_a + rho_b) / 2
-            const D3 PB = ld3(rec, N, p, b);
-            double dv = PA[p].v - PB.v;
-            double da[3] = {PA[p].d0, PA[p].d1, PA[p].d2};
-            double db[3] = {-PB.d0, -PB.d1, -PB.d2};
-            if (gd != 0.0) {
-                const D3 RB = ld3(rec, N, 6 + p, b);
-                dv = dv + ((RA[p].v + RB.v) * 0.5) * gd;
-                da[0] = da[0] + (RA[p].d0 * 0.5) * gd;
-                da[1] = da[1] + (RA[p].d1 * 0.5) * gd;
-                da[2] = da[2] + (RA[p].d2 * 0.5) * gd;
-                db[0] = db[0] + (RB.d0 * 0.5) * gd;
-                db[1] = db[1] + (RB.d1 * 0.5) * gd;
-                db[2] = db[2] + (RB.d2 * 0.5) * gd;
+            if (!((fl >> p) & 1u)) {
+                stored(p == PG ? 3 : p, p, p != PG);
+                if (p == PO) stored(2, PG, true);
+                continue;
             }
-            const bool upA = dv >= 0;
+            // a zero (or undefined) potential difference: the cell forms the phase's terms itself
+            const int b = __ldg(adjNbr + q);
+            const double dD = first ? __ldg(dDepth + cn) : -__ldg(dDepth + cn);
+            const double tr = __ldg(trans + cn);
+            const Dphi d = dphi_of(rec, N, p, b, ld3(rec, N, p, a), ld3(rec, N, 6 + p, a), m.gravity * dD);
+            const bool upA = d.v >= 0;
             const int up = upA ? a : b;
-            // F = mob_upstream dphi T, added to balance `bal` (the phase's own; the gas balance for dissolved gas);
-            // `first`: the connection's first term of that balance in the neighbour's block
-            auto flux = [&](int field, int bal, bool first) {
-                const D3 mo = ld3(rec, N, field, up);
-                double fa[3], fb[3];
-                const double mu[3] = {mo.d0, mo.d1, mo.d2};
-#pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    fa[i] = upA ? mu[i] * dv + mo.v * da[i] : mo.v * da[i];
-                    fb[i] = upA ? mo.v * db[i] : mu[i] * dv + mo.v * db[i];
-                }
-                sr[bal] += (mo.v * dv) * tr;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    sj[bal][k] += fa[k] * tr;
-                    nbk[bal][k] = first ? fb[k] * tr : nbk[bal][k] + fb[k] * tr;
-                }
-            };
-            flux(3 + p, p, p != PG);            // water and oil: first terms; gas: after the dissolved gas
-            if (p == PO) flux(9, PG, true);     // dissolved gas carried by the oil flux
+            const Flux F = flux_of(ld3(rec, N, 3 + p, up), upA, d, tr);
+            add(p, p != PG, F.v, F.fa, F.fb);
+            if (p == PO) {
+                const Flux Fd = flux_of(ld3(rec, N, 9, up), upA, d, tr);
+                add(PG, true, Fd.v, Fd.fa, Fd.fb);
+            }
         }
         const int pos = __ldg(adjPos + q);
 #pragma unroll
@@ -488,6 +566,10 @@ struct rsg_bo_assembler {
     double *trans = nullptr, *dDepth = nullptr;
     int *blkStart = nullptr, *selfPos = nullptr, *Jrow = nullptr;
     double* rec = nullptr;
+    int* connB = nullptr;
+    int nconn = 0;
+    double* flux = nullptr;          // kFluxWords per connection (k_bo_conn)
+    unsigned char* flag = nullptr;   // per connection: phases whose potential difference is zero
     // well addend lists: packed on the host, one upload per assembly into a device buffer grown on demand
     std::vector<char> stage;
     char* dstage = nullptr;
@@ -580,6 +662,7 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     const int nadj = adjStart[na];
     std::vector<int> adjNbr(g->adj_nbr, g->adj_nbr + nadj), adjConn(g->adj_conn, g->adj_conn + nadj);
     std::vector<int> connA(g->conn_a, g->conn_a + nconn);
+    std::vector<int> connB(size_t(nconn), -1), seen(size_t(nconn), 0);   // second cell of each connection
     std::vector<int> blkStart(na + 1, 0), selfPos(na), adjPos(nadj);
     std::vector<int> nb;
     std::vector<int> JrowH(J_rowPtr, J_rowPtr + nrows + 1);
@@ -593,6 +676,9 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
             const int b = adjNbr[q], c = adjConn[q];
             if (b < 0 || b >= na || b == a) return fail(RSG_EINVAL, "rsg_bo_create: neighbour index out of range");
             if (c < 0 || c >= nconn) return fail(RSG_EINVAL, "rsg_bo_create: connection index out of range");
+            if (connA[size_t(c)] == a) connB[size_t(c)] = b;
+            else if (connA[size_t(c)] != b) return fail(RSG_EINVAL, "rsg_bo_create: adjacency names a connection that does not join its cells");
+            ++seen[size_t(c)];
             nb.push_back(b);
         }
         std::sort(nb.begin(), nb.end());
@@ -618,6 +704,9 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
         }
     }
 
+    for (long long c = 0; c < nconn; ++c)
+        if (seen[size_t(c)] != 2 || connB[size_t(c)] < 0)
+            return fail(RSG_EINVAL, "rsg_bo_create: every connection must appear once in the adjacency of each of its two cells");
     rsg_bo_assembler* h = new rsg_bo_assembler();
     h->device = device;
     h->na = na; h->nv = nv; h->nw = nw; h->nrows = nrows; h->nnz = JrowH[nrows];
@@ -670,12 +759,22 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     };
     up(&h->tab, tb); up(&h->utab, ut); up(&h->pv0, pv);
     up(&h->adjStart, adjStart); up(&h->adjNbr, adjNbr); up(&h->adjConn, adjConn); up(&h->adjPos, adjPos);
-    up(&h->connA, connA); up(&h->trans, trans); up(&h->dDepth, dd);
+    up(&h->connA, connA); up(&h->connB, connB); up(&h->trans, trans); up(&h->dDepth, dd);
+    h->nconn = int(nconn);
     up(&h->blkStart, blkStart); up(&h->selfPos, selfPos); up(&h->Jrow, JrowH);
     if (rc == RSG_OK) {
         e = cudaMallocAsync(reinterpret_cast<void**>(&h->rec), size_t(kRecWords) * size_t(na) * sizeof(double), st);
         if (e != cudaSuccess) rc = fail(RSG_ENOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
         else h->owned.push_back(h->rec);
+    }
+    if (rc == RSG_OK && nconn > 0) {
+        e = cudaMallocAsync(reinterpret_cast<void**>(&h->flux), size_t(kFluxWords) * size_t(nconn) * sizeof(double), st);
+        if (e == cudaSuccess) {
+            h->owned.push_back(h->flux);
+            e = cudaMallocAsync(reinterpret_cast<void**>(&h->flag), size_t(nconn), st);
+            if (e == cudaSuccess) h->owned.push_back(h->flag);
+        }
+        if (e != cudaSuccess) rc = fail(RSG_ENOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
     }
     if (rc == RSG_OK) {
         e = cudaStreamSynchronize(st);
@@ -775,9 +874,13 @@ extern "C" int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const dou
     const int* dIds = reinterpret_cast<const int*>(D + oId);
     const int grid = (na + kThreads - 1) / kThreads;
     k_bo_props<<<grid, kThreads, 0, st>>>(na, h->m, h->tab, h->utab, h->pv0, d_p, d_sw, d_x, d_state, h->rec);
-    k_bo_cells<<<grid, kThreads, 0, st>>>(na, nv, h->m, dt, h->rec, d_acc_old, h->pv0, h->adjStart, h->adjNbr, h->adjConn, h->adjPos,
+    if (h->nconn > 0)
+        k_bo_conn<<<(h->nconn + kThreads - 1) / kThreads, kThreads, 0, st>>>(h->nconn, na, h->m, h->rec, h->connA, h->connB, h->trans,
+                                                                         h->dDepth, h->flux, h->flag);
+    k_bo_cells<<<grid, kThreads, 0, st>>>(na, nv, h->nconn, h->m, dt, h->rec, h->flux, h->flag, d_acc_old, h->pv0, h->adjStart, h->adjNbr,
+                                          h->adjConn, h->adjPos,
                                           h->connA, h->trans, h->dDepth, h->blkStart, h->selfPos, h->Jrow, dIds, ncell, d_J, d_R);
-    h->launches += 2;
+    h->launches += h->nconn > 0 ? 3 : 2;
     if (nac > 0) {
         k_bo_addends<<<(nac + 127) / 128, 128, 0, st>>>(na, nv, nrows, dt, dIds, nac, reinterpret_cast<const int*>(D + oAB),
                                                         reinterpret_cast<const long long*>(D + oAP), reinterpret_cast<const double*>(D + oAV),
