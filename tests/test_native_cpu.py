@@ -240,6 +240,13 @@ def test_black_oil_assembler_checks_model_and_pattern_before_the_device():
     with pytest.raises(_lib.RsgError) as e:
         BlackOilAssembler(bad)
     assert e.value.code == _lib.RSG_EINVAL and "pattern" in str(e.value)
+    bad = dict(z)
+    conn = z["adjConn"].copy()
+    conn[0] = conn[-1]                                             # an adjacency entry naming another pair's connection
+    bad["adjConn"] = conn
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(bad)
+    assert e.value.code == _lib.RSG_EINVAL and "connection" in str(e.value)
     if gpu_available():
         pytest.skip("a GPU is present")
     with pytest.raises(_lib.RsgError) as e:
