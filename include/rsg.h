@@ -378,6 +378,11 @@ int rsg_bo_create(rsg_bo_assembler** h, const rsg_bo_grid* grid, const rsg_bo_fl
 int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const double* d_sw, const double* d_x, const unsigned char* d_state,
                     const double* d_acc_old, double dt, int nadd, const long long* add_pos, const double* add_val, int nradd,
                     const int* radd_pos, const double* radd_val, double* d_J, double* d_R, void* stream);
+/* The same with host vectors: the state in, J and R out (copied through buffers the assembler keeps on its device;
+ * synchronous). */
+int rsg_bo_assemble_host(rsg_bo_assembler* h, const double* p, const double* sw, const double* x, const unsigned char* state,
+                         const double* acc_old, double dt, int nadd, const long long* add_pos, const double* add_val, int nradd,
+                         const int* radd_pos, const double* radd_val, double* J, double* R);
 int rsg_bo_destroy(rsg_bo_assembler* h);
 
 #ifdef __cplusplus

@@ -26,7 +26,7 @@ EXPORTS = [
     "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
     "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes", "rsg_tuning",
     "rsg_set_jacobian", "rsg_set_jacobian_batch", "rsg_set_jacobian_device", "rsg_solve_jacobian", "rsg_solve_jacobian_device",
-    "rsg_get_matrix", "rsg_matrix_size", "rsg_server_hold", "rsg_bo_create", "rsg_bo_assemble", "rsg_bo_destroy",
+    "rsg_get_matrix", "rsg_matrix_size", "rsg_server_hold", "rsg_bo_create", "rsg_bo_assemble", "rsg_bo_assemble_host", "rsg_bo_destroy",
 ]
 
 
@@ -139,6 +139,7 @@ def load(build_if_missing: bool = True):
     L.rsg_bo_create.argtypes = [C.POINTER(vp), C.POINTER(BoGrid), C.POINTER(BoFluid), C.POINTER(BoSatfun), C.c_int, C.c_int, vp, vp,
                                 C.c_int]
     L.rsg_bo_assemble.argtypes = [vp, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp, vp, C.c_int, vp, vp, vp, vp, vp]
+    L.rsg_bo_assemble_host.argtypes = [vp, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp, vp, C.c_int, vp, vp, vp, vp]
     L.rsg_bo_destroy.argtypes = [vp]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype if name in ("rsg_last_error", "rsg_version", "rsg_stream") else (

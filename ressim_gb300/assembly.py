@@ -114,6 +114,22 @@ class BlackOilAssembler:
     def __exit__(self, *a):
         self.close()
 
+    def assemble(self, p, sw, x, state, acc_old, dt: float, add_pos=None, add_val=None, radd_pos=None, radd_val=None):
+        """Host vectors in (state: na float64 each, cell states na uint8, old accumulations na*3), J (the pattern's
+        nonzeros) and R (nrows) out as numpy arrays; well terms as in assemble_device."""
+        p, sw, x, acc = _f64(p), _f64(sw), _f64(x), _f64(acc_old)
+        st = np.ascontiguousarray(state, dtype=np.uint8)
+        ap = np.ascontiguousarray(add_pos if add_pos is not None else np.zeros(0), dtype=np.int64)
+        av = _f64(add_val if add_val is not None else np.zeros(0))
+        rp = _i32(radd_pos if radd_pos is not None else np.zeros(0))
+        rv = _f64(radd_val if radd_val is not None else np.zeros(0))
+        J = np.empty(self.nnz)
+        R = np.empty(self.nrows)
+        q = lambda a: C.c_void_p(a.ctypes.data) if a.size else None  # noqa: E731
+        _lib.check(self._L.rsg_bo_assemble_host(self._h, q(p), q(sw), q(x), q(st), q(acc), float(dt), int(ap.size), q(ap), q(av),
+                                                int(rp.size), q(rp), q(rv), q(J), q(R)))
+        return J, R
+
     def assemble_device(self, d_p: int, d_sw: int, d_x: int, d_state: int, d_acc_old: int, dt: float, d_J: int, d_R: int,
                         add_pos=None, add_val=None, radd_pos=None, radd_val=None, stream: int = 0):
         """Device pointers (e.g. torch ``data_ptr()``): state (na float64 each; na uint8), old accumulations (na*3),

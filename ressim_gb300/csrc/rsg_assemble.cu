@@ -576,6 +576,9 @@ struct rsg_bo_assembler {
     size_t capStage = 0;
     std::vector<int> JrowH;
     std::vector<void*> owned;
+    // buffers of the host-vector form (rsg_bo_assemble_host), allocated at its first call
+    double *hp = nullptr, *hsw = nullptr, *hx = nullptr, *hacc = nullptr, *hJ = nullptr, *hR = nullptr;
+    unsigned char* hst = nullptr;
     long long launches = 0;
 };
 
@@ -890,6 +893,42 @@ extern "C" int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const dou
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("rsg_bo_assemble launch: ") + cudaGetErrorString(e));
+    return RSG_OK;
+}
+
+extern "C" int rsg_bo_assemble_host(rsg_bo_assembler* h, const double* p, const double* sw, const double* x, const unsigned char* state,
+                                    const double* acc_old, double dt, int nadd, const long long* add_pos, const double* add_val,
+                                    int nradd, const int* radd_pos, const double* radd_val, double* J, double* R) {
+    if (!h) return fail(RSG_EINVAL, "rsg_bo_assemble_host: null handle");
+    if (!p || !sw || !x || !state || !acc_old || !J || !R) return fail(RSG_EINVAL, "rsg_bo_assemble_host: null host pointer");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    cudaStream_t st = h->own;
+    const size_t na = size_t(h->na);
+    if (!h->hp) {
+        void** bufs[] = {reinterpret_cast<void**>(&h->hp), reinterpret_cast<void**>(&h->hsw), reinterpret_cast<void**>(&h->hx),
+                         reinterpret_cast<void**>(&h->hacc), reinterpret_cast<void**>(&h->hJ), reinterpret_cast<void**>(&h->hR),
+                         reinterpret_cast<void**>(&h->hst)};
+        const size_t sizes[] = {na * 8, na * 8, na * 8, na * 24, size_t(h->nnz) * 8, size_t(h->nrows) * 8, na};
+        for (int k = 0; k < 7; ++k) {
+            e = cudaMallocAsync(bufs[k], std::max(sizes[k], size_t(8)), st);
+            if (e != cudaSuccess) return fail(RSG_ENOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+            h->owned.push_back(*bufs[k]);
+        }
+    }
+    const struct { void* d; const void* hsrc; size_t n; } in[] = {
+        {h->hp, p, na * 8}, {h->hsw, sw, na * 8}, {h->hx, x, na * 8}, {h->hacc, acc_old, na * 24}, {h->hst, state, na}};
+    for (const auto& c : in) {
+        e = cudaMemcpyAsync(c.d, c.hsrc, c.n, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    }
+    const int rc = rsg_bo_assemble(h, h->hp, h->hsw, h->hx, h->hst, h->hacc, dt, nadd, add_pos, add_val, nradd, radd_pos, radd_val,
+                                   h->hJ, h->hR, st);
+    if (rc != RSG_OK) return rc;
+    e = cudaMemcpyAsync(J, h->hJ, size_t(h->nnz) * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(R, h->hR, size_t(h->nrows) * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("rsg_bo_assemble_host: ") + cudaGetErrorString(e));
     return RSG_OK;
 }
 

@@ -150,3 +150,27 @@ def test_assembled_jacobian_solves_on_device():
         x_host, res = b.solve_jacobian(-z[f"s{k}_R_full"], tol=1e-8, maxit=200)
         assert res.converged
     assert np.array_equal(x_dev, x_host)
+
+
+def test_whole_run_assembly_matches_engine_every_newton_iteration():
+    """The reference simulator's whole 20x20x4 waterflood (6 report steps of 30 days), with oracle/ref_asm_run in the
+    engine's solver hook: at every Newton iteration the device assembles J and R from the simulator's state (with the
+    engine's well terms at that state) and both are compared with the engine's own assembly of that iteration, bit
+    for bit. The states evolve as in the stock run (the engine solves every system itself): free gas appears, the
+    wells' controls switch, time steps grow."""
+    import json
+    import subprocess
+    from conftest import ROOT
+    staged = os.path.join(ROOT, "oracle", "_ref", "src", "engine", "src", "simulator.cpp")
+    if not os.path.exists(staged):
+        pytest.skip("reference engine sources not staged (make -f oracle/Makefile.ref stage REF=...)")
+    jobs = str(max(2, os.cpu_count() or 2))
+    r = subprocess.run(["make", "-f", "oracle/Makefile.ref", "-j" + jobs, "oracle/_ref/ref_asm_run"], cwd=ROOT, capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_asm_run"), "6", "30"], capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, OMP_NUM_THREADS="1"))
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert r.returncode == 0 and not out["error"], out
+    assert out["compared"] == out["hook_calls"] and out["compared"] >= 30, out
+    assert out["mismatching_J"] == 0 and out["mismatching_R"] == 0, out
