@@ -431,6 +431,112 @@ __device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl,
     }
 }
 
+// ------------------------------------------------------------------ BILU0 sweeps with records staged by cp.async
+// A CTA barrier waits for the register loads its threads have in flight, so register lookahead cannot carry a row's
+// loads across the level barriers; asynchronous copies into shared memory (cp.async) are not waited for by the
+// barrier. Here every thread stages the record of its row of the next level (slot columns, factor record, input or
+// the CPR correction) into its own slot of a shared-memory stage while the current level computes, and waits for its
+// own copies (cp.async.wait_group) at the start of the next level: a level step no longer waits for its rows' data
+// to come in from L2. The stage holds one row per thread (kStageWords words each, component-major over the threads:
+// conflict-free); rows past blockDim in a level load directly when they are reached. FP32 records, vector on chip.
+constexpr int kStageWords = 4 + UREC + 1;     // slot columns, the larger record (U with the diagonal), input / correction
+
+__device__ __forceinline__ void cpa4(unsigned* dst, const void* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <class TX>
+__device__ void ilu_body_async(const IluArgs<float>& F, int row0, const int* lv, int nl, const float* r, double* z, float* y,
+                               const TX* xp, unsigned* stage) {
+    static_assert(sizeof(TX) == 4, "the CPR correction is staged as one 32-bit word");
+    const int t = int(threadIdx.x), nt = int(blockDim.x);
+    unsigned* st = stage + t;
+    auto word = [&](int f) { return st[size_t(f) * size_t(nt)]; };
+    // the copies of this thread's row of forward level L / backward level L (none if the level is narrower)
+    auto stage_fwd = [&](int L) {
+        const int s0 = lv[L], w = lv[L + 1] - s0, k = s0 + t;
+        if (t < w) {
+            const int* sl = reinterpret_cast<const int*>(F.Lslot + k);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cpa4(st + j * nt, sl + j);
+            const float* rec = F.L + size_t(s0) * LREC + size_t(t);
+#pragma unroll
+            for (int j = 0; j < LREC; ++j) cpa4(st + (4 + j) * nt, rec + size_t(j) * size_t(w));
+#pragma unroll
+            for (int e = 0; e < 3; ++e) cpa4(st + (4 + UREC + 0) * nt - (3 - e) * nt, r + size_t(k) * 3 + e);
+        }
+        cpa_commit();
+    };
+    auto stage_bwd = [&](int L) {
+        const int s0 = lv[L], w = lv[L + 1] - s0, k = s0 + t;
+        if (t < w) {
+            const int* sl = reinterpret_cast<const int*>(F.Uslot + k);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cpa4(st + j * nt, sl + j);
+            const float* rec = F.UD + size_t(s0) * UREC + size_t(t);
+#pragma unroll
+            for (int j = 0; j < UREC; ++j) cpa4(st + (4 + j) * nt, rec + size_t(j) * size_t(w));
+            cpa4(st + (4 + UREC) * nt, xp + (k - row0));
+        }
+        cpa_commit();
+    };
+    // the levels' records are also brought into L2 kAhead levels ahead (one thread), so the staged copies hit L2
+    if (t == 0)
+        for (int L = 0; L < kAhead && L < nl; ++L) prefetch_fwd_level<float, float, IN_PLAIN>(F, lv, L, r, nullptr, nullptr);
+    if (nl > 0) stage_fwd(0);
+    for (int L = 0; L < nl; ++L) {
+        const int s0 = lv[L], e = lv[L + 1], k = s0 + t;
+        if (t == 0) {
+            if (L + kAhead < nl) prefetch_fwd_level<float, float, IN_PLAIN>(F, lv, L + kAhead, r, nullptr, nullptr);
+            else if (nl - 1 - (L + kAhead - nl) >= 0) prefetch_bwd_level(F, lv, nl - 1 - (L + kAhead - nl));
+        }
+        cpa_wait_all();
+        FwdRow<float, float, IN_PLAIN> R;
+        R.k = -1;
+        if (k < e) {
+            R.k = k;
+            R.c = make_int4(int(word(0)), int(word(1)), int(word(2)), int(word(3)));
+#pragma unroll
+            for (int j = 0; j < LREC; ++j) R.a[j] = __uint_as_float(word(4 + j));
+#pragma unroll
+            for (int q = 0; q < 3; ++q) R.in[q] = __uint_as_float(word(4 + UREC - 3 + q));
+        }
+        if (L + 1 < nl) stage_fwd(L + 1);       // this thread's slot is free again: its values are in registers
+        else stage_bwd(nl - 1);                  // the first backward level comes in during the last forward one
+        if (k < e) fwd_step<float, float, float, IN_PLAIN>(R, F, row0, y, nullptr, 0, 0, 0);
+        for (int k2 = k + nt; k2 < e; k2 += nt) {
+            load_fwd(R, k2, s0, e - s0, F, r, nullptr, nullptr);
+            fwd_step<float, float, float, IN_PLAIN>(R, F, row0, y, nullptr, 0, 0, 0);
+        }
+        __syncthreads();
+    }
+    for (int g = 0; g < nl; ++g) {
+        const int L = nl - 1 - g;
+        const int s0 = lv[L], e = lv[L + 1], k = s0 + t;
+        if (t == 0 && L - kAhead >= 0) prefetch_bwd_level(F, lv, L - kAhead);
+        cpa_wait_all();
+        BwdRow<float> R;
+        R.k = -1;
+        if (k < e) {
+            R.k = k;
+            R.c = make_int4(int(word(0)), int(word(1)), int(word(2)), int(word(3)));
+#pragma unroll
+            for (int j = 0; j < UREC; ++j) R.a[j] = __uint_as_float(word(4 + j));
+            R.xp = double(__uint_as_float(word(4 + UREC)));
+        }
+        if (L > 0) stage_bwd(L - 1);
+        if (k < e) bwd_step<float, float, true>(R, F, row0, y, z, true);
+        for (int k2 = k + nt; k2 < e; k2 += nt) {
+            load_bwd(R, k2, s0, e - s0, F, xp, row0);
+            bwd_step<float, float, true>(R, F, row0, y, z, true);
+        }
+        __syncthreads();
+    }
+}
+
 template <class TF, class TV, int MODE, int NT = cta_threads<TF, TV>()>
 __global__ void __launch_bounds__(NT) k_ilu_cta(IluArgs<TF> F, const double* r, double* pv, const double* v, double* z,
                                                         TV* yglob, size_t smemBytes, const KScal* ks) {
@@ -1951,8 +2057,16 @@ __global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const 
     __shared__ int lvc[kLvCache];
     const int* ls = level_starts(F.lvlStart + l0, nl, lvc);
     // FP32 factors at 256 threads: three register buffers (rows loaded two levels ahead); at 512 threads (every row of a
-    // wide level has its own thread) the two-buffer sweep, whose registers fit the smaller per-thread budget
+    // wide level has its own thread) the two-buffer sweep, whose registers fit the smaller per-thread budget. With FP32
+    // factors, vector and correction and room beside the vector, the records staged by cp.async instead.
     constexpr bool three = sizeof(TF) == 4 && NT <= 256;
+    if constexpr (sizeof(TF) == 4 && sizeof(TV) == 4 && sizeof(TA) == 4) {
+        const size_t vec = (size_t(ns) * 3 * sizeof(TV) + 15) & ~size_t(15);
+        if (onchip && vec + size_t(kStageWords) * size_t(NT) * 4 <= smemBytes) {
+            ilu_body_async<TA>(F, row0, ls, nl, T, z, y, xpg, reinterpret_cast<unsigned*>(smraw + vec));
+            return;
+        }
+    }
     if (onchip || sizeof(TV) != sizeof(double)) {
         if constexpr (three) ilu_body3<TF, TV, TV, true, TA>(F, row0, ls, nl, T, z, y, true, xpg);
         else ilu_body<TF, TV, TV, IN_PLAIN, true, TA, NT>(F, row0, ls, nl, T, nullptr, nullptr, z, y, true, 0, 0, 0, xpg);
@@ -1971,8 +2085,15 @@ void launch_cpr2_nt(const DevPlan& P, const PrecDev& M, const DevAmg& G, const C
     IluArgs<TF> F;
     if constexpr (sizeof(TF) == 8) F = ilu_args(P, M.s64);
     else F = ilu_args(P, M.s32);
-    raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<TF, TV, TA, NT>), int(M.smem));
-    k_cpr2_cta<TF, TV, TA, NT><<<P.nsys, NT, M.smem, st>>>(F, G.maxL, G.lv, C.x, T, z, yglob, M.smem, ks);
+    // FP32 records, vector and correction: room for the cp.async stage beside the largest system's vector when it fits
+    size_t sm = M.smem;
+    if constexpr (sizeof(TF) == 4 && sizeof(TV) == 4 && sizeof(TA) == 4) {
+        const size_t vec = (size_t(P.maxSysRows) * 3 * sizeof(TV) + 15) & ~size_t(15);
+        const size_t want = vec + size_t(kStageWords) * size_t(NT) * 4;
+        if (want <= size_t(max_smem_optin()) - kCtaStaticSmem) sm = std::max(sm, want);
+    }
+    raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<TF, TV, TA, NT>), int(sm));
+    k_cpr2_cta<TF, TV, TA, NT><<<P.nsys, NT, sm, st>>>(F, G.maxL, G.lv, C.x, T, z, yglob, sm, ks);
 }
 template <class TA, class TT>
 void launch_cpr2(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<TA>& C, TT* Tsplit, double* z, const KScal* ks,
