@@ -174,3 +174,41 @@ def test_whole_run_assembly_matches_engine_every_newton_iteration():
     assert r.returncode == 0 and not out["error"], out
     assert out["compared"] == out["hook_calls"] and out["compared"] >= 30, out
     assert out["mismatching_J"] == 0 and out["mismatching_R"] == 0, out
+
+
+def test_well_terms_are_added_in_the_callers_order():
+    """Several terms at one position are added in list order (the engine's well loop adds a connection's terms one
+    after the other): on a well row, which starts from zero and is not scaled, J = (0 + v) + w exactly; positions out
+    of range are refused with RSG_EINVAL."""
+    torch = pytest.importorskip("torch")
+    from ressim_gb300 import _lib
+    from ressim_gb300.assembly import BlackOilAssembler
+    z = fixture()
+    k = 2
+    na, nv, nw = int(z["na"][0]), int(z["nv"][0]), int(z["nw"][0])
+    rp = z["J_rowPtr"]
+    wrow = na * nv                                   # the first well row
+    p0 = int(rp[wrow])
+    # 1 + 1e-16 rounds back to 1, 1e-16 + 1e-16 does not: the sum depends on the order of the terms
+    big, tiny = 1.0, 1.0e-16
+    assert ((0.0 + big) + tiny) + tiny != ((0.0 + tiny) + tiny) + big
+    with BlackOilAssembler(z) as asm:
+        J1, R1 = asm.assemble(z[f"s{k}_p"], z[f"s{k}_sw"], z[f"s{k}_x"], z[f"s{k}_hasGas"], z[f"s{k}_accOld"], float(z[f"s{k}_dt"][0]),
+                              add_pos=np.array([p0, p0, p0 + 1, p0]), add_val=np.array([big, tiny, -2.5, tiny]),
+                              radd_pos=np.array([wrow, wrow, wrow]), radd_val=np.array([tiny, tiny, big]))
+        assert J1[p0] == ((0.0 + big) + tiny) + tiny and J1[p0 + 1] == -2.5
+        assert R1[wrow] == ((0.0 + tiny) + tiny) + big
+        assert np.all(J1[p0 + 2:rp[wrow + 1]] == 0.0)
+        # the host form equals the device form
+        J, R = assemble(torch, asm, z, k)
+        J2, R2 = asm.assemble(z[f"s{k}_p"], z[f"s{k}_sw"], z[f"s{k}_x"], z[f"s{k}_hasGas"], z[f"s{k}_accOld"], float(z[f"s{k}_dt"][0]),
+                              add_pos=z[f"s{k}_add_pos"], add_val=z[f"s{k}_add_val"], radd_pos=z[f"s{k}_radd_pos"],
+                              radd_val=z[f"s{k}_radd_val"])
+        assert np.array_equal(J2, J) and np.array_equal(R2, R)
+        with pytest.raises(_lib.RsgError) as e:
+            asm.assemble(z[f"s{k}_p"], z[f"s{k}_sw"], z[f"s{k}_x"], z[f"s{k}_hasGas"], z[f"s{k}_accOld"], 1.0,
+                         add_pos=np.array([int(rp[-1])]), add_val=np.array([1.0]))
+        assert e.value.code == _lib.RSG_EINVAL
+        with pytest.raises(_lib.RsgError) as e:
+            asm.assemble(z[f"s{k}_p"], z[f"s{k}_sw"], z[f"s{k}_x"], z[f"s{k}_hasGas"], z[f"s{k}_accOld"], 0.0)
+        assert e.value.code == _lib.RSG_EINVAL
