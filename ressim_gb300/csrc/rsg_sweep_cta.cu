@@ -440,6 +440,7 @@ __device__ void ilu_body3(const IluArgs<TF>& F, int row0, const int* lv, int nl,
 // to come in from L2. The stage holds one row per thread (kStageWords words each, component-major over the threads:
 // conflict-free); rows past blockDim in a level load directly when they are reached. FP32 records, vector on chip.
 constexpr int kStageWords = 4 + UREC + 1;     // slot columns, the larger record (U with the diagonal), input / correction
+constexpr int kStageSlots = 256;               // threads with a stage slot; further threads (512-thread blocks) load directly
 
 __device__ __forceinline__ void cpa4(unsigned* dst, const void* src) {
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
@@ -453,33 +454,35 @@ __device__ void ilu_body_async(const IluArgs<float>& F, int row0, const int* lv,
                                const TX* xp, unsigned* stage) {
     static_assert(sizeof(TX) == 4, "the CPR correction is staged as one 32-bit word");
     const int t = int(threadIdx.x), nt = int(blockDim.x);
+    const int nsl = min(nt, kStageSlots);          // slots: the stage's stride
+    const bool slotted = t < nsl;                  // threads past the slots load their rows directly
     unsigned* st = stage + t;
-    auto word = [&](int f) { return st[size_t(f) * size_t(nt)]; };
+    auto word = [&](int f) { return st[size_t(f) * size_t(nsl)]; };
     // the copies of this thread's row of forward level L / backward level L (none if the level is narrower)
     auto stage_fwd = [&](int L) {
         const int s0 = lv[L], w = lv[L + 1] - s0, k = s0 + t;
-        if (t < w) {
+        if (slotted && t < w) {
             const int* sl = reinterpret_cast<const int*>(F.Lslot + k);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) cpa4(st + j * nt, sl + j);
+            for (int j = 0; j < 4; ++j) cpa4(st + j * nsl, sl + j);
             const float* rec = F.L + size_t(s0) * LREC + size_t(t);
 #pragma unroll
-            for (int j = 0; j < LREC; ++j) cpa4(st + (4 + j) * nt, rec + size_t(j) * size_t(w));
+            for (int j = 0; j < LREC; ++j) cpa4(st + (4 + j) * nsl, rec + size_t(j) * size_t(w));
 #pragma unroll
-            for (int e = 0; e < 3; ++e) cpa4(st + (4 + UREC + 0) * nt - (3 - e) * nt, r + size_t(k) * 3 + e);
+            for (int e = 0; e < 3; ++e) cpa4(st + (4 + UREC - 3 + e) * nsl, r + size_t(k) * 3 + e);
         }
         cpa_commit();
     };
     auto stage_bwd = [&](int L) {
         const int s0 = lv[L], w = lv[L + 1] - s0, k = s0 + t;
-        if (t < w) {
+        if (slotted && t < w) {
             const int* sl = reinterpret_cast<const int*>(F.Uslot + k);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) cpa4(st + j * nt, sl + j);
+            for (int j = 0; j < 4; ++j) cpa4(st + j * nsl, sl + j);
             const float* rec = F.UD + size_t(s0) * UREC + size_t(t);
 #pragma unroll
-            for (int j = 0; j < UREC; ++j) cpa4(st + (4 + j) * nt, rec + size_t(j) * size_t(w));
-            cpa4(st + (4 + UREC) * nt, xp + (k - row0));
+            for (int j = 0; j < UREC; ++j) cpa4(st + (4 + j) * nsl, rec + size_t(j) * size_t(w));
+            cpa4(st + (4 + UREC) * nsl, xp + (k - row0));
         }
         cpa_commit();
     };
@@ -496,13 +499,15 @@ __device__ void ilu_body_async(const IluArgs<float>& F, int row0, const int* lv,
         cpa_wait_all();
         FwdRow<float, float, IN_PLAIN> R;
         R.k = -1;
-        if (k < e) {
+        if (k < e && slotted) {
             R.k = k;
             R.c = make_int4(int(word(0)), int(word(1)), int(word(2)), int(word(3)));
 #pragma unroll
             for (int j = 0; j < LREC; ++j) R.a[j] = __uint_as_float(word(4 + j));
 #pragma unroll
             for (int q = 0; q < 3; ++q) R.in[q] = __uint_as_float(word(4 + UREC - 3 + q));
+        } else if (k < e) {
+            load_fwd(R, k, s0, e - s0, F, r, nullptr, nullptr);
         }
         if (L + 1 < nl) stage_fwd(L + 1);       // this thread's slot is free again: its values are in registers
         else stage_bwd(nl - 1);                  // the first backward level comes in during the last forward one
@@ -520,12 +525,14 @@ __device__ void ilu_body_async(const IluArgs<float>& F, int row0, const int* lv,
         cpa_wait_all();
         BwdRow<float> R;
         R.k = -1;
-        if (k < e) {
+        if (k < e && slotted) {
             R.k = k;
             R.c = make_int4(int(word(0)), int(word(1)), int(word(2)), int(word(3)));
 #pragma unroll
             for (int j = 0; j < UREC; ++j) R.a[j] = __uint_as_float(word(4 + j));
             R.xp = double(__uint_as_float(word(4 + UREC)));
+        } else if (k < e) {
+            load_bwd(R, k, s0, e - s0, F, xp, row0);
         }
         if (L > 0) stage_bwd(L - 1);
         if (k < e) bwd_step<float, float, true>(R, F, row0, y, z, true);
@@ -2062,7 +2069,7 @@ __global__ void __launch_bounds__(NT) k_cpr2_cta(IluArgs<TF> F, int maxL, const 
     constexpr bool three = sizeof(TF) == 4 && NT <= 256;
     if constexpr (sizeof(TF) == 4 && sizeof(TV) == 4 && sizeof(TA) == 4) {
         const size_t vec = (size_t(ns) * 3 * sizeof(TV) + 15) & ~size_t(15);
-        if (onchip && vec + size_t(kStageWords) * size_t(NT) * 4 <= smemBytes) {
+        if (onchip && vec + size_t(kStageWords) * size_t(NT < kStageSlots ? NT : kStageSlots) * 4 <= smemBytes) {
             ilu_body_async<TA>(F, row0, ls, nl, T, z, y, xpg, reinterpret_cast<unsigned*>(smraw + vec));
             return;
         }
@@ -2089,7 +2096,7 @@ void launch_cpr2_nt(const DevPlan& P, const PrecDev& M, const DevAmg& G, const C
     size_t sm = M.smem;
     if constexpr (sizeof(TF) == 4 && sizeof(TV) == 4 && sizeof(TA) == 4) {
         const size_t vec = (size_t(P.maxSysRows) * 3 * sizeof(TV) + 15) & ~size_t(15);
-        const size_t want = vec + size_t(kStageWords) * size_t(NT) * 4;
+        const size_t want = vec + size_t(kStageWords) * size_t(NT < kStageSlots ? NT : kStageSlots) * 4;
         if (want <= size_t(max_smem_optin()) - kCtaStaticSmem) sm = std::max(sm, want);
     }
     raise_smem_limit(reinterpret_cast<const void*>(k_cpr2_cta<TF, TV, TA, NT>), int(sm));
