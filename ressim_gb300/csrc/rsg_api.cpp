@@ -662,6 +662,9 @@ int build_dev_amg(rsg_solver* h, const std::vector<SysAmg>& H) {
     G.totSlots = slots;
     G.maxSysAmgRows = 0;
     for (int r : sysRows) G.maxSysAmgRows = std::max(G.maxSysAmgRows, r);
+    G.maxSysLoRows = 0;
+    for (int s = 0; s < nsys; ++s)
+        G.maxSysLoRows = std::max(G.maxSysLoRows, sysRows[size_t(s)] - (H[size_t(s)].lv.empty() ? 0 : H[size_t(s)].lv[0].n));
     // V-cycle row slots: first W off-diagonal entries of every row in row order, the rest from the CSR
     std::vector<int> slotSrc(size_t(std::max(slots, 1)), -1), slotCol(size_t(std::max(slots, 1)), -1), meta(size_t(rows) * 4, -1);
     for (int l = 0; l < maxL; ++l)

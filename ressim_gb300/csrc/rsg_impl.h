@@ -160,6 +160,7 @@ struct DevAmg {
     // the diagonal, off-diagonal entries, entry position where the entries beyond the slots continue, diagonal
     // position} (positions local to the level's entries)
     int totSlots = 0, maxSysAmgRows = 0;
+    int maxSysLoRows = 0;              // largest number of rows of one system's levels below the finest
     // Gauss-Seidel schedule per (system, level): rows in processing order (level space; identity for the forward
     // levels of the reference order, colour by colour for the multicolour smoother), boundaries in lvl
     int* gsRows = nullptr;

@@ -952,9 +952,10 @@ template <class TA>
 struct VVecs {
     TA *xs, *bs, *rs;                 // on-chip bases (null when global)
     bool bGlobal;
-    __device__ TA* x(const AmgSysLv& A, const CprArgs<TA>& C) const { return xs ? xs + A.locOff : C.x + A.rowOff; }
-    __device__ TA* b(const AmgSysLv& A, const CprArgs<TA>& C) const { return bs ? bs + A.locOff : C.b + A.rowOff; }
-    __device__ TA* r(const AmgSysLv& A, const CprArgs<TA>& C) const { return rs ? rs + A.locOff : C.r + A.rowOff; }
+    int loc0 = 0;                     // offset of the first level held on chip (the on-chip vectors start at that level)
+    __device__ TA* x(const AmgSysLv& A, const CprArgs<TA>& C) const { return xs ? xs + (A.locOff - loc0) : C.x + A.rowOff; }
+    __device__ TA* b(const AmgSysLv& A, const CprArgs<TA>& C) const { return bs ? bs + (A.locOff - loc0) : C.b + A.rowOff; }
+    __device__ TA* r(const AmgSysLv& A, const CprArgs<TA>& C) const { return rs ? rs + (A.locOff - loc0) : C.r + A.rowOff; }
 };
 
 template <class TA, int W, int NT>
@@ -1857,9 +1858,28 @@ __global__ void __launch_bounds__(256) k_gcpr_coarse(CprArgs<TA> C, const KScal*
 // prolongation) of one system per thread block, with the thread-block V-cycle's arithmetic (so the values are those of
 // the grid passes it replaces); levels this small cost a block barrier per pass instead of a launch
 template <class TA, int NT>
-__global__ void __launch_bounds__(NT) k_vcycle_lo(CprArgs<TA> C, const KScal* ks) {
+__global__ void __launch_bounds__(NT) k_vcycle_lo(CprArgs<TA> C, const KScal* ks, size_t smemBytes) {
+    extern __shared__ __align__(16) unsigned char smraw[];
     const int s = blockIdx.x;
     if (ks && ks[s].status != ST_RUNNING) return;
+    // x, b and r of the levels below the finest on chip when they fit (the Gauss-Seidel colours gather x from shared
+    // memory): level 1's right-hand side comes in from the grid restriction, its solution goes out to the grid
+    // prolongation; the coarser levels live on chip only
+    const AmgSysLv A1 = C.lv[s * C.maxL + 1];
+    int R1 = 0;
+    for (int l = 1; l < C.maxL; ++l) R1 += C.lv[s * C.maxL + l].n;
+    if (A1.n > 0 && size_t(3) * size_t(R1) * sizeof(TA) <= smemBytes) {
+        TA* sm = reinterpret_cast<TA*>(smraw);
+        VVecs<TA> V{sm, sm + R1, sm + 2 * R1, false};
+        V.loc0 = A1.locOff;
+        const TA* bg = C.b + A1.rowOff;
+        for (int k = threadIdx.x; k < A1.n; k += blockDim.x) V.bs[k] = bg[k];
+        __syncthreads();
+        vcycle<TA, NT>(s, C, V, 1);
+        TA* xg = C.x + A1.rowOff;
+        for (int k = threadIdx.x; k < A1.n; k += blockDim.x) xg[k] = V.xs[k];
+        return;
+    }
     const VVecs<TA> V{nullptr, nullptr, nullptr, true};
     vcycle<TA, NT>(s, C, V, 1);
 }
@@ -2248,7 +2268,11 @@ int cpr_grid(const DevPlan& P, const PrecDev& M, const DevAmg& G, const CprArgs<
         launches += 2;
     }
     if (lo) {
-        k_vcycle_lo<TA, 256><<<G.nsys, 256, 0, st>>>(C, ks);
+        // the on-chip vectors of the largest system's coarse levels, if they fit (no more: the rest is L1)
+        const size_t want = size_t(G.maxSysLoRows) * 3 * sizeof(TA);
+        const size_t sm = want <= size_t(max_smem_optin()) - kCtaStaticSmem ? want : 0;
+        raise_smem_limit(reinterpret_cast<const void*>(k_vcycle_lo<TA, 256>), int(sm));
+        k_vcycle_lo<TA, 256><<<G.nsys, 256, sm, st>>>(C, ks, sm);
         ++launches;
     } else {
         k_gcpr_coarse<TA><<<G.nsys, 256, 0, st>>>(C, ks);
