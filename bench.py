@@ -705,7 +705,8 @@ def main():
     keep_pinned += [tb, tx]
     L = _lib.load()
     e2e_t = []
-    for k in range(args.warmup + args.steps):
+    e2e_steps = max(args.steps, 20)        # host wall clock: more steps than the device timing, so one slow host step
+    for k in range(args.warmup + e2e_steps):   # (a scheduler or allocator pause) does not set the figure
         barrier()
         t0 = time.perf_counter()
         dev.set_batch(mats_pinned)
@@ -720,7 +721,7 @@ def main():
     if dist:
         Te = max_over_ranks(Te, dist, f"cuda:{local}")
     e2e = {"value": world * N_REAL * len(e2e_t) / Te, "unit": "solves/s", "h2d_bytes_per_step": val_bytes + N * 8,
-           "d2h_bytes_per_step": N * 8, "p50_ms": 1e3 * statistics.median(e2e_t), "host_buffers": "pinned"}
+           "d2h_bytes_per_step": N * 8, "p50_ms": 1e3 * statistics.median(e2e_t), "steps": len(e2e_t), "host_buffers": "pinned"}
     dev.close()
 
     # ---------------- plain FP64 GPU path: one system after another (one handle each)
