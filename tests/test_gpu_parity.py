@@ -430,9 +430,12 @@ def test_spe10_sized_cpr_gmres(oracle):
     from ressim_gb300 import synth
     s = synth.spe10_like(day=1)
     assert s.A.n == 1_122_000
-    oracle.set_threads(os.cpu_count() or 1)
-    _, _, its30, rr30, _, _ = oracle.solve(s.A, s.b, prec=1, method=1, restart=30, tol=1e-12, maxit=30, acc=s.acc)
-    _, conv_o, its_o, rr_o, _, _ = oracle.solve(s.A, s.b, prec=1, method=1, restart=30, tol=1e-6, maxit=600, acc=s.acc)
+    oracle.set_threads(os.cpu_count() or 1)     # a large system; the comparisons below allow for summation order
+    try:
+        _, _, its30, rr30, _, _ = oracle.solve(s.A, s.b, prec=1, method=1, restart=30, tol=1e-12, maxit=30, acc=s.acc)
+        _, conv_o, its_o, rr_o, _, _ = oracle.solve(s.A, s.b, prec=1, method=1, restart=30, tol=1e-6, maxit=600, acc=s.acc)
+    finally:
+        oracle.set_threads(1)                    # the session's oracle stays single-threaded (reproducible) for the rest
     assert its30 == 30 and conv_o
     for precision in ("fp64", "mixed_f32"):
         with dev(precond="cpr", krylov="gmres", restart=30, precision=precision) as d:
