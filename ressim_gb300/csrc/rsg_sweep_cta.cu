@@ -1865,9 +1865,10 @@ __global__ void __launch_bounds__(NT) k_vcycle_lo(CprArgs<TA> C, const KScal* ks
     // x, b and r of the levels below the finest on chip when they fit (the Gauss-Seidel colours gather x from shared
     // memory): level 1's right-hand side comes in from the grid restriction, its solution goes out to the grid
     // prolongation; the coarser levels live on chip only
-    const AmgSysLv A1 = C.lv[s * C.maxL + 1];
     int R1 = 0;
     for (int l = 1; l < C.maxL; ++l) R1 += C.lv[s * C.maxL + l].n;
+    // (a hierarchy of one level has no level 1: the descriptor array holds maxL entries per system)
+    const AmgSysLv A1 = C.maxL > 1 ? C.lv[s * C.maxL + 1] : AmgSysLv{};
     if (A1.n > 0 && size_t(3) * size_t(R1) * sizeof(TA) <= smemBytes) {
         TA* sm = reinterpret_cast<TA*>(smraw);
         VVecs<TA> V{sm, sm + R1, sm + 2 * R1, false};
