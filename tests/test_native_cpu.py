@@ -273,3 +273,23 @@ def test_assembly_golden_is_consistent():
     assert np.array_equal(z["s1_R_full"][:na * nv][free], z["s1_R_cell"][:na * nv][free])
     states = [np.bincount(z[f"s{k}_hasGas"], minlength=3) for k in range(int(z["nstates"][0]))]
     assert states[0][1] > 0 and states[0][2] > 0                   # the perturbed state has free-gas and no-oil cells
+
+
+def test_synthetic_assembly_model_is_the_engines_layout():
+    """ressim_gb300.synth.assembly_model (the bench's assembly workload: several masked grids taken as one) builds the
+    engine's scalar Jacobian pattern and adjacency: the assembler's checks accept it (and stop only at the device,
+    without a GPU), and every connection appears once on each side."""
+    from conftest import gpu_available
+    from ressim_gb300 import _lib, synth
+    from ressim_gb300.assembly import BlackOilAssembler
+    grids = [synth.assembly_grid(8, 6, 3, seed=s, actnum_fraction=0.3) for s in (1, 2)]
+    z, st = synth.assembly_model(grids)
+    na = int(z["na"][0])
+    assert na == sum(g["na"] for g in grids) and st["p"].size == na and st["acc_old"].size == 3 * na
+    conn = z["adjConn"]
+    assert np.array_equal(np.bincount(conn, minlength=z["conn_trans"].size), np.full(z["conn_trans"].size, 2))
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(z)
+    assert e.value.code == _lib.RSG_ECUDA, e.value
