@@ -229,6 +229,34 @@ class Oracle:
         """A set-up BlockCPR (engine/src/bsr.cpp:993-1084) kept for repeated applications: ``h.apply(r)``."""
         return _CprHandle(self, A, acc, lean)
 
+    def bo_assemble(self, model: dict, p, sw, x, state, acc_old, dt, add_pos=None, add_val=None, radd_pos=None, radd_val=None):
+        """The reference's black-oil assembly restated in C (rsg_oracle_asm.c): J (the model's pattern) and R at the
+        state, with the well terms as ordered addends, rows scaled by dt / PV. The model dict has the keys of
+        tests/golden/waterflood_asm.npz (described by ressim_gb300.assembly.model_structs)."""
+        from ressim_gb300.assembly import model_structs
+        g, f, s, rowPtr, col, keep = model_structs(model)
+        nrows = int(rowPtr.size - 1)
+        fn = self.L.orc_bo_assemble
+        fn.argtypes = [C.c_void_p] * 6 + [C.c_void_p] * 5 + [C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                                              C.c_void_p, C.c_void_p, C.c_void_p]
+        fn.argtypes[3] = C.c_int
+        fn.restype = C.c_int
+        st = [_arr(p, np.float64), _arr(sw, np.float64), _arr(x, np.float64), np.ascontiguousarray(state, dtype=np.uint8),
+              _arr(acc_old, np.float64)]
+        ap = np.ascontiguousarray(add_pos if add_pos is not None else np.zeros(0), dtype=np.int64)
+        av = _arr(add_val if add_val is not None else np.zeros(0), np.float64)
+        rp = np.ascontiguousarray(radd_pos if radd_pos is not None else np.zeros(0), dtype=np.int32)
+        rv = _arr(radd_val if radd_val is not None else np.zeros(0), np.float64)
+        J = np.empty(int(rowPtr[-1]))
+        R = np.empty(nrows)
+        q = lambda a: C.c_void_p(a.ctypes.data) if a.size else None  # noqa: E731
+        rc = fn(C.byref(g), C.byref(f), C.byref(s), nrows, q(rowPtr), q(col), *[q(a) for a in st], float(dt), int(ap.size), q(ap), q(av),
+                int(rp.size), q(rp), q(rv), q(J), q(R))
+        del keep
+        if rc != 0:
+            raise RuntimeError(f"orc_bo_assemble: {rc} (pattern is not the engine's)")
+        return J, R
+
     def wellschur(self, J, na, nv, nw, b):
         """J: scalar CSR (rowPtr, col, val); returns (S as BSR-like dict, bc) or None."""
         rp, ci, v = (_arr(J[0], np.int32), _arr(J[1], np.int32), _arr(J[2], np.float64))

@@ -33,68 +33,77 @@ def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+def model_structs(model: dict):
+    """The C-ABI descriptions of a model dict (rsg_bo_grid, rsg_bo_fluid, rsg_bo_satfun), the Jacobian pattern
+    (int32 rowPtr, col) and the arrays they point into (keep them alive while the structures are used)."""
+    keep = []
+
+    def arr(a, conv):
+        a = conv(a)
+        keep.append(a)
+        return C.c_void_p(a.ctypes.data) if a.size else None
+
+    def table(name):
+        x, y = _f64(model[name + "_x"]), _f64(model[name + "_y"])
+        keep.extend([x, y])
+        return _lib.Table(int(x.size), C.c_void_p(x.ctypes.data) if x.size else None,
+                          C.c_void_p(y.ctypes.data) if y.size else None, int(np.asarray(model[name + "_clamp"]).ravel()[0]))
+
+    def tables(name):
+        x, y, off, cl = _f64(model[name + "_x"]), _f64(model[name + "_y"]), _i32(model[name + "_off"]), _i32(model[name + "_clamp"])
+        keep.extend([x, y])
+        ts = (_lib.Table * (off.size - 1))()
+        for k in range(off.size - 1):
+            ts[k] = _lib.Table(int(off[k + 1] - off[k]), C.c_void_p(x.ctypes.data + 8 * int(off[k])),
+                               C.c_void_p(y.ctypes.data + 8 * int(off[k])), int(cl[k]))
+        keep.append(ts)
+        return C.cast(ts, C.c_void_p)
+
+    sc = lambda k: np.asarray(model[k]).ravel()  # noqa: E731
+    na, nv = int(sc("na")[0]), int(sc("nv")[0])
+    v = sc("vars")
+    g = _lib.BoGrid(na, nv, int(np.asarray(model["conn_trans"]).size), arr(model["adjStart"], _i32), arr(model["adjNbr"], _i32),
+                    arr(model["adjConn"], _i32), arr(model["conn_a"], _i32), arr(model["conn_trans"], _f64),
+                    arr(model["conn_dDepth"], _f64), arr(model["poreVolRef"], _f64), float(sc("gravity")[0]), int(v[0]), int(v[1]),
+                    (C.c_int * 3)(int(v[2]), int(v[3]), int(v[4])))
+    ph = sc("phases")
+    f = _lib.BoFluid()
+    f.water, f.oil, f.gas, f.live, f.vap = (int(t) for t in ph[:5])
+    f.pvtw = (C.c_double * 5)(*sc("pvtw"))
+    f.rock = (C.c_double * 2)(*sc("rock"))
+    f.rho_sc = (C.c_double * 3)(*sc("rhoSC"))
+    f.gas_factor = float(sc("gasFactor")[0])
+    f.rs_of_p, f.pb_of_rs = table("rsOfP"), table("pbOfRs")
+    f.dead_b, f.dead_bmu = table("deadB"), table("deadBMu")
+    f.gas_b, f.gas_bmu = table("gasB"), table("gasBMu")
+    f.nsat = int(np.asarray(model["liveRs"]).size)
+    f.sat_rs, f.sat_b, f.sat_bmu = arr(model["liveRs"], _f64), arr(model["bSat"], _f64), arr(model["bmuSat"], _f64)
+    f.under_b, f.under_bmu = tables("uB"), tables("uBMu")
+    s = _lib.BoSatfun()
+    s.krw, s.krow, s.pcow = table("krw"), table("krow"), table("pcow")
+    s.krg, s.krog, s.pcog = table("krg"), table("krog"), table("pcog")
+    s.swco = float(sc("swco")[0])
+    s.kro_model = int(sc("kroModel")[0])
+    sf = sc("sat_flags")
+    s.water, s.gas, s.three_point = int(sf[0]), int(sf[1]), int(sf[2])
+    rowPtr, col = _i32(model["J_rowPtr"]), _i32(model["J_col"])
+    keep.extend([rowPtr, col])
+    return g, f, s, rowPtr, col, keep
+
+
 class BlackOilAssembler:
     """One grid's assembler on ``device``: ``assemble_device`` writes J and R into caller-owned device buffers."""
 
     def __init__(self, model: dict, device: int = 0):
         self._L = _lib.load()
         self._h = C.c_void_p()
-        keep = []
-
-        def arr(a, conv):
-            a = conv(a)
-            keep.append(a)
-            return C.c_void_p(a.ctypes.data) if a.size else None
-
-        def table(name):
-            x, y = _f64(model[name + "_x"]), _f64(model[name + "_y"])
-            keep.extend([x, y])
-            return _lib.Table(int(x.size), C.c_void_p(x.ctypes.data) if x.size else None,
-                              C.c_void_p(y.ctypes.data) if y.size else None, int(np.asarray(model[name + "_clamp"]).ravel()[0]))
-
-        def tables(name):
-            x, y, off, cl = _f64(model[name + "_x"]), _f64(model[name + "_y"]), _i32(model[name + "_off"]), _i32(model[name + "_clamp"])
-            keep.extend([x, y])
-            ts = (_lib.Table * (off.size - 1))()
-            for k in range(off.size - 1):
-                ts[k] = _lib.Table(int(off[k + 1] - off[k]), C.c_void_p(x.ctypes.data + 8 * int(off[k])),
-                                   C.c_void_p(y.ctypes.data + 8 * int(off[k])), int(cl[k]))
-            keep.append(ts)
-            return C.cast(ts, C.c_void_p)
-
-        sc = lambda k: np.asarray(model[k]).ravel()  # noqa: E731
-        self.na, self.nv, self.nw = int(sc("na")[0]), int(sc("nv")[0]), int(sc("nw")[0])
+        g, f, s, rowPtr, col, keep = model_structs(model)
+        self.na, self.nv, self.nw = int(g.na), int(g.nv), int(np.asarray(model["nw"]).ravel()[0])
         self.nrows = self.na * self.nv + self.nw
-        self.rowPtr = _i32(model["J_rowPtr"])
+        self.rowPtr = rowPtr
         self.nnz = int(self.rowPtr[-1])
-        v = sc("vars")
-        g = _lib.BoGrid(self.na, self.nv, int(np.asarray(model["conn_trans"]).size), arr(model["adjStart"], _i32),
-                        arr(model["adjNbr"], _i32), arr(model["adjConn"], _i32), arr(model["conn_a"], _i32),
-                        arr(model["conn_trans"], _f64), arr(model["conn_dDepth"], _f64), arr(model["poreVolRef"], _f64),
-                        float(sc("gravity")[0]), int(v[0]), int(v[1]), (C.c_int * 3)(int(v[2]), int(v[3]), int(v[4])))
-        ph = sc("phases")
-        f = _lib.BoFluid()
-        f.water, f.oil, f.gas, f.live, f.vap = (int(t) for t in ph[:5])
-        f.pvtw = (C.c_double * 5)(*sc("pvtw"))
-        f.rock = (C.c_double * 2)(*sc("rock"))
-        f.rho_sc = (C.c_double * 3)(*sc("rhoSC"))
-        f.gas_factor = float(sc("gasFactor")[0])
-        f.rs_of_p, f.pb_of_rs = table("rsOfP"), table("pbOfRs")
-        f.dead_b, f.dead_bmu = table("deadB"), table("deadBMu")
-        f.gas_b, f.gas_bmu = table("gasB"), table("gasBMu")
-        f.nsat = int(np.asarray(model["liveRs"]).size)
-        f.sat_rs, f.sat_b, f.sat_bmu = arr(model["liveRs"], _f64), arr(model["bSat"], _f64), arr(model["bmuSat"], _f64)
-        f.under_b, f.under_bmu = tables("uB"), tables("uBMu")
-        s = _lib.BoSatfun()
-        s.krw, s.krow, s.pcow = table("krw"), table("krow"), table("pcow")
-        s.krg, s.krog, s.pcog = table("krg"), table("krog"), table("pcog")
-        s.swco = float(sc("swco")[0])
-        s.kro_model = int(sc("kroModel")[0])
-        sf = sc("sat_flags")
-        s.water, s.gas, s.three_point = int(sf[0]), int(sf[1]), int(sf[2])
-        col = _i32(model["J_col"])
         _lib.check(self._L.rsg_bo_create(C.byref(self._h), C.byref(g), C.byref(f), C.byref(s), self.nrows, self.nw,
-                                         C.c_void_p(self.rowPtr.ctypes.data), C.c_void_p(col.ctypes.data), device))
+                                         C.c_void_p(rowPtr.ctypes.data), C.c_void_p(col.ctypes.data), device))
         del keep
 
     def close(self):

@@ -212,3 +212,27 @@ def test_well_terms_are_added_in_the_callers_order():
         with pytest.raises(_lib.RsgError) as e:
             asm.assemble(z[f"s{k}_p"], z[f"s{k}_sw"], z[f"s{k}_x"], z[f"s{k}_hasGas"], z[f"s{k}_accOld"], 0.0)
         assert e.value.code == _lib.RSG_EINVAL
+
+
+def test_full_size_assembly_matches_oracle():
+    """The bench's assembly workload at full size -- the 64 ensemble grids taken as one, 742,384 cells, synthetic
+    live-oil / Corey tables and state -- against the C restatement of the reference's assembly (pinned to the
+    reference's J and R on CPU, tests/test_oracle.py), with 2,000 seeded addends on cell and well-free rows: bit for
+    bit."""
+    from oracle import Oracle
+    from ressim_gb300 import synth
+    from ressim_gb300.assembly import BlackOilAssembler
+    z, st = synth.assembly_ensemble(64)
+    rng = np.random.default_rng(3)
+    nnz, nrows = int(z["J_rowPtr"][-1]), int(z["na"][0]) * 3
+    add_pos = rng.integers(0, nnz, 2000)
+    add_val = rng.standard_normal(2000)
+    radd_pos = rng.integers(0, nrows, 500).astype(np.int32)
+    radd_val = rng.standard_normal(500)
+    args = (st["p"], st["sw"], st["x"], st["state"], st["acc_old"], 10.0)
+    kw = dict(add_pos=add_pos, add_val=add_val, radd_pos=radd_pos, radd_val=radd_val)
+    with BlackOilAssembler(z) as asm:
+        J, R = asm.assemble(*args, **kw)
+    Jo, Ro = Oracle().bo_assemble(z, *args, **kw)
+    assert np.array_equal(J, Jo), np.flatnonzero(J != Jo)[:10]
+    assert np.array_equal(R, Ro), np.flatnonzero(R != Ro)[:10]
