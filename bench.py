@@ -331,7 +331,39 @@ def assembly_bytes(z):
             "total": state + grid + out + rec + flux}
 
 
-def assembly_leg(local, steps, warmup):
+def assembly_cpu_baseline(z, st):
+    """The reference engine's own assembly on the host cores: its evalAll + assemble (block assembly, the engine's
+    default) at the first Newton state of a 100 x 100 x 74 waterflood (740,000 cells, about the ensemble's 742,384),
+    compiled from the staged reference sources (oracle/Makefile.ref, ~30 s with 16 cores) and timed over 5 repeats
+    by oracle/_ref/ref_asm_capture --time. Without the staged sources: the C restatement (oracle/rsg_oracle_asm.c,
+    one thread) on the same synthetic model as the device."""
+    cores = os.cpu_count() or 1
+    staged = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "src", "engine", "src", "simulator.cpp"))
+    if staged:
+        try:
+            r = subprocess.run(["make", "-f", "oracle/Makefile.ref", f"-j{cores}", "oracle/_ref/ref_asm_capture"], cwd=ROOT,
+                               capture_output=True, text=True, timeout=600)
+            if r.returncode == 0:
+                r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_asm_capture"), "--time", "100", "100", "74", "5"],
+                                   capture_output=True, text=True, timeout=600, env=dict(os.environ, OMP_NUM_THREADS=str(cores)))
+                if r.returncode == 0:
+                    out = json.loads(r.stdout.strip().splitlines()[-1])
+                    return {"value": out["cells"] / (out["median_ms"] / 1e3), "unit": "cells/s", "ms": out["median_ms"],
+                            "cells": out["cells"], "cores": cores, "kind": "reference",
+                            "sample": "the engine's evalAll + assemble at the first Newton state of a 100x100x74 waterflood, "
+                                      "median of 5"}
+        except Exception:
+            pass
+    from oracle import Oracle
+    t0 = time.perf_counter()
+    Oracle().bo_assemble(z, st["p"], st["sw"], st["x"], st["state"], st["acc_old"], 10.0)
+    dt = time.perf_counter() - t0
+    na = int(z["na"][0])
+    return {"value": na / dt, "unit": "cells/s", "ms": 1e3 * dt, "cells": na, "cores": 1, "kind": "port",
+            "sample": "the C restatement of the engine's assembly on the device's synthetic model, one pass"}
+
+
+def assembly_leg(local, steps, warmup, cpu=True):
     """Device Jacobian assembly (rsg_bo_assemble) of the ensemble's 64 grids taken as one (synthetic black-oil tables
     and state, ressim_gb300.synth.assembly_ensemble): device time per assembly with the state resident, and end to
     end with the state uploaded from pinned host memory and the residual read back (what a Newton step moves when the
@@ -379,6 +411,7 @@ def assembly_leg(local, steps, warmup):
         if k >= warmup:
             te.append(time.perf_counter() - t0)
     asm.close()
+    cpu_base = assembly_cpu_baseline(z, st) if cpu else None
     B = assembly_bytes(z)
     hbm, peak_kind = peaks()
     na = int(z["na"][0])
@@ -389,7 +422,8 @@ def assembly_leg(local, steps, warmup):
                                                                  "unit": "GB/s", "frac": B["total"] / t / 1e9 / hbm,
                                                                  "peak_kind": peak_kind + " burst copy"},
             "e2e": {"ms": 1e3 * statistics.median(te), "h2d_bytes": h2d, "d2h_bytes": asm.nrows * 8,
-                    "matrix_upload_replaced_bytes": int(asm.nnz) * 8}}
+                    "matrix_upload_replaced_bytes": int(asm.nnz) * 8},
+            "cpu_baseline": cpu_base}
 
 
 def spe10_report(local):
@@ -524,7 +558,8 @@ def main():
 
     if args.assembly == "only":
         if rank == 0:
-            print(json.dumps({"metric": "device Jacobian assembly", "assembly": assembly_leg(local, args.steps, args.warmup)}))
+            print(json.dumps({"metric": "device Jacobian assembly",
+                              "assembly": assembly_leg(local, args.steps, args.warmup, cpu=not args.no_cpu_baseline)}))
         return 0
     if args.spe10:
         if rank == 0:
@@ -753,7 +788,8 @@ def main():
                   "p99_ms": 1e3 * float(np.percentile(lat, 99)), "all_converged": bool(plain_ok)}
 
     serving_ens = serving_ensemble(local, systems) if args.serving != "off" and world == 1 else None
-    assembly = assembly_leg(local, args.steps, args.warmup) if world == 1 and args.assembly != "off" else None
+    assembly = assembly_leg(local, args.steps, args.warmup, cpu=rank == 0 and not args.no_cpu_baseline) \
+        if world == 1 and args.assembly != "off" else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
