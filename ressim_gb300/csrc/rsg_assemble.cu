@@ -15,10 +15,12 @@
 // reference's, in the reference's order (this file is compiled without contraction into fused multiply-adds), so the
 // Jacobian and residual are the engine's bit for bit.
 //
-// Two kernels per assembly, one thread per cell: k_bo_props evaluates every cell's properties with their derivatives
-// (13 dual numbers, stored component-major so that neighbouring threads read neighbouring words), k_bo_cells forms the
-// accumulation and the flux terms of a cell's three rows from its own and its neighbours' records and writes the rows
-// once; k_bo_addends finishes the few rows that take well terms.
+// Three kernels per assembly (four with well terms): k_bo_props evaluates every cell's properties with their
+// derivatives, one thread per cell (13 dual numbers, stored component-major so that neighbouring threads read
+// neighbouring words); k_bo_conn forms each connection's phase fluxes once, one thread per connection; k_bo_cells forms
+// the accumulation of a cell's three rows, adds its connections' fluxes (negated, with the two cells' derivative slots
+// exchanged, on a connection's second cell) and writes the rows once; k_bo_addends finishes the few rows that take
+// well terms.
 #include "rsg.h"
 
 #include <cuda_runtime.h>
