@@ -24,7 +24,7 @@ EXPORTS = [
     "rsg_setup", "rsg_solve", "rsg_solve_device", "rsg_solve_refined", "rsg_batch_results", "rsg_batch_status", "rsg_amg_level_sizes", "rsg_spmv", "rsg_spmv_device", "rsg_precond_apply",
     "rsg_precond_apply_device", "rsg_get_factors", "rsg_get_stats", "rsg_stream", "rsg_wellschur_reduce", "rsg_wellschur_recover",
     "rsg_spmv_level_probe", "rsg_precond_level_probe", "rsg_spmv_dot_noalloc", "rsg_release", "rsg_server_create",
-    "rsg_server_destroy", "rsg_submit", "rsg_poll", "rsg_server_load", "rsg_request_bytes", "rsg_tuning",
+    "rsg_server_destroy", "rsg_submit", "rsg_submit_view", "rsg_poll", "rsg_server_load", "rsg_request_bytes", "rsg_tuning",
     "rsg_set_jacobian", "rsg_set_jacobian_batch", "rsg_set_jacobian_device", "rsg_solve_jacobian", "rsg_solve_jacobian_device",
     "rsg_get_matrix", "rsg_matrix_size", "rsg_server_hold", "rsg_bo_create", "rsg_bo_assemble", "rsg_bo_assemble_host", "rsg_bo_destroy",
 ]
@@ -124,6 +124,7 @@ def load(build_if_missing: bool = True):
     L.rsg_server_create.argtypes = [C.POINTER(vp), C.POINTER(Options), C.c_int, C.c_size_t]
     L.rsg_server_destroy.argtypes = [vp]
     L.rsg_submit.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_double, C.c_int]
+    L.rsg_submit_view.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_double, C.c_int]
     L.rsg_poll.argtypes = [vp, C.c_longlong, C.c_int, vp, C.POINTER(Result)]
     L.rsg_server_load.argtypes = [vp, ip, ip, C.POINTER(C.c_size_t)]
     L.rsg_request_bytes.argtypes = [C.POINTER(Options), C.c_int, C.c_longlong]
@@ -143,7 +144,7 @@ def load(build_if_missing: bool = True):
     L.rsg_bo_destroy.argtypes = [vp]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype if name in ("rsg_last_error", "rsg_version", "rsg_stream") else (
-            None if name == "rsg_default_options" else (C.c_longlong if name == "rsg_submit" else
+            None if name == "rsg_default_options" else (C.c_longlong if name in ("rsg_submit", "rsg_submit_view") else
                                                          (C.c_size_t if name == "rsg_request_bytes" else C.c_int)))
     _LIB = L
     return L

@@ -32,8 +32,12 @@ using Clock = std::chrono::steady_clock;
 struct Request {
     long long id = 0;
     int n = 0, nb = 0;
-    std::vector<int> rp, ci;
+    std::vector<int> rp, ci;                  // the server's copy (rsg_submit); empty when the caller lends its arrays
     std::vector<double> val, b, x;
+    const int* prp = nullptr;                 // what the solve reads: the copy, or the caller's arrays (rsg_submit_view)
+    const int* pci = nullptr;
+    const double* pval = nullptr;
+    const double* pb = nullptr;
     double tol = 1e-6;
     int maxit = 100;
     size_t est = 0;
@@ -101,7 +105,7 @@ constexpr long long kMaxBatchRowsTotal = 1 << 21;
 void run_request(rsg_server* S, int slot, Request& R) {
     rsg_solver* h = R.n > kBatchRows && S->grid[size_t(slot)] ? S->grid[size_t(slot)] : S->handles[size_t(slot)];
     int prec = S->opt.precond;
-    int rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
+    int rc = rsg_set_matrix(h, R.n, R.nb, R.prp, R.pci, R.pval);
     if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
     if (rc == RSG_EINVAL && (prec == RSG_PREC_CPR || prec == RSG_PREC_CPR_DEVICE)) {   // CPR needs a structurally symmetric pattern: BILU0
         rsg_release(h);
@@ -116,7 +120,7 @@ void run_request(rsg_server* S, int slot, Request& R) {
         if (fb) {
             h = fb;
             prec = RSG_PREC_BILU0;
-            rc = rsg_set_matrix(h, R.n, R.nb, R.rp.data(), R.ci.data(), R.val.data());
+            rc = rsg_set_matrix(h, R.n, R.nb, R.prp, R.pci, R.pval);
             if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
         }
     }
@@ -125,8 +129,8 @@ void run_request(rsg_server* S, int slot, Request& R) {
     int its = 0;
     double rr = 0;
     if (rc == RSG_OK) {
-        R.x.assign(R.b.size(), 0.0);
-        rc = rsg_solve(h, R.b.data(), R.x.data(), R.tol, R.maxit, &its, &rr);
+        R.x.assign(size_t(R.n) * size_t(R.nb), 0.0);
+        rc = rsg_solve(h, R.pb, R.x.data(), R.tol, R.maxit, &its, &rr);
     }
     rsg_stats st{};
     rsg_get_stats(h, &st);
@@ -152,10 +156,10 @@ void run_batch(rsg_server* S, int slot, std::vector<std::shared_ptr<Request>>& B
     for (int k = 0; k < ns; ++k) {
         Request& R = *B[size_t(k)];
         n[size_t(k)] = R.n;
-        rp[size_t(k)] = R.rp.data();
-        ci[size_t(k)] = R.ci.data();
-        val[size_t(k)] = R.val.data();
-        b.insert(b.end(), R.b.begin(), R.b.end());
+        rp[size_t(k)] = R.prp;
+        ci[size_t(k)] = R.pci;
+        val[size_t(k)] = R.pval;
+        b.insert(b.end(), R.pb, R.pb + size_t(R.n) * size_t(R.nb));
     }
     int rc = rsg_set_batch(h, ns, rsg::NB, n.data(), rp.data(), ci.data(), val.data());
     if (rc == RSG_OK) rc = rsg_setup(h, nullptr);
@@ -179,7 +183,7 @@ void run_batch(rsg_server* S, int slot, std::vector<std::shared_ptr<Request>>& B
     size_t off = 0;
     for (int k = 0; k < ns; ++k) {
         Request& R = *B[size_t(k)];
-        const size_t N = R.b.size();
+        const size_t N = size_t(R.n) * size_t(R.nb);
         R.x.assign(x.begin() + long(off), x.begin() + long(off + N));
         off += N;
         R.res.status = sst[size_t(k)];
@@ -365,27 +369,45 @@ int rsg_server_destroy(rsg_server* S) {
     return RSG_OK;
 }
 
-long long rsg_submit(rsg_server* S, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b, double tol,
-                     int maxIt) {
+}  // extern "C"
+
+namespace {
+
+// Queues one request. copy: the server keeps its own copy of the arrays (the caller may reuse them at once);
+// otherwise it reads the caller's arrays in place until the request has finished.
+long long submit(rsg_server* S, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b, double tol,
+                 int maxIt, bool copy) {
     using rsg::set_last_error;
     if (!S || !rowPtr || !col || !val || !b) { set_last_error("null argument"); return RSG_EINVAL; }
     if (n <= 0 || nb != rsg::NB) { set_last_error("n must be > 0 and nb = 3"); return RSG_EINVAL; }
     const long long nnzb = rowPtr[n];
     if (nnzb <= 0) { set_last_error("empty matrix"); return RSG_EINVAL; }
+    const size_t est = footprint(n, nnzb, S->opt);
+    if (S->budget && est > S->budget) {
+        set_last_error("request needs about " + std::to_string(est >> 20) + " MiB, more than the whole budget");
+        return RSG_ENOMEM;
+    }
     auto R = std::make_shared<Request>();
     R->n = n;
     R->nb = nb;
-    R->rp.assign(rowPtr, rowPtr + n + 1);
-    R->ci.assign(col, col + nnzb);
-    R->val.assign(val, val + nnzb * nb * nb);
-    R->b.assign(b, b + size_t(n) * size_t(nb));
+    if (copy) {
+        R->rp.assign(rowPtr, rowPtr + n + 1);
+        R->ci.assign(col, col + nnzb);
+        R->val.assign(val, val + nnzb * nb * nb);
+        R->b.assign(b, b + size_t(n) * size_t(nb));
+        R->prp = R->rp.data();
+        R->pci = R->ci.data();
+        R->pval = R->val.data();
+        R->pb = R->b.data();
+    } else {
+        R->prp = rowPtr;
+        R->pci = col;
+        R->pval = val;
+        R->pb = b;
+    }
     R->tol = tol;
     R->maxit = maxIt;
-    R->est = footprint(n, nnzb, S->opt);
-    if (S->budget && R->est > S->budget) {
-        set_last_error("request needs about " + std::to_string(R->est >> 20) + " MiB, more than the whole budget");
-        return RSG_ENOMEM;
-    }
+    R->est = est;
     R->tSubmit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -395,6 +417,20 @@ long long rsg_submit(rsg_server* S, int n, int nb, const int* rowPtr, const int*
     }
     S->cvWork.notify_all();
     return R->id;
+}
+
+}  // namespace
+
+extern "C" {
+
+long long rsg_submit(rsg_server* S, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b, double tol,
+                     int maxIt) {
+    return submit(S, n, nb, rowPtr, col, val, b, tol, maxIt, true);
+}
+
+long long rsg_submit_view(rsg_server* S, int n, int nb, const int* rowPtr, const int* col, const double* val, const double* b,
+                          double tol, int maxIt) {
+    return submit(S, n, nb, rowPtr, col, val, b, tol, maxIt, false);
 }
 
 int rsg_poll(rsg_server* S, long long id, int wait, double* x, rsg_result* res) {

@@ -240,9 +240,11 @@ class DeviceSolver:
 
 class Server:
     """Serving form (``rsg_server_*``): continuous batching of independent systems over ``slots`` workers under a
-    device-memory budget. ``submit`` copies a system and returns its id; ``poll`` returns ``None`` while it is
-    queued or running, else ``(x, result)`` with the per-request latency split (queue / run / total ms). As the
-    engine does, a BiCGSTAB solve that does not converge is retried with GMRES (``gmres_fallback``, on by default)."""
+    device-memory budget. ``submit`` copies a system and returns its id (``copy=False``: the server reads the
+    arrays in place, and this object keeps them referenced until the result is polled; the caller must not change
+    them meanwhile); ``poll`` returns ``None`` while it is queued or running, else ``(x, result)`` with the
+    per-request latency split (queue / run / total ms). As the engine does, a BiCGSTAB solve that does not converge is
+    retried with GMRES (``gmres_fallback``, on by default)."""
 
     def __init__(self, slots: int = 4, mem_budget: int = 0, precond: str = "cpr", krylov: str = "bicgstab",
                  precision: str = "mixed_f32", restart: int = 40, check_every: int = 4, use_graphs: bool = True, device: int = 0,
@@ -262,17 +264,21 @@ class Server:
         self.s = C.c_void_p()
         _lib.check(self.L.rsg_server_create(C.byref(self.s), C.byref(o), slots, mem_budget))
         self.sizes = {}
+        self.lent = {}
 
     def request_bytes(self, A: BSR) -> int:
         """The admission figure of a system under this server's options."""
         return int(self.L.rsg_request_bytes(C.byref(self.opts), A.n, A.nnzb))
 
-    def submit(self, A: BSR, b, tol: float = 1e-6, maxit: int = 200) -> int:
+    def submit(self, A: BSR, b, tol: float = 1e-6, maxit: int = 200, copy: bool = True) -> int:
         b = np.ascontiguousarray(b, dtype=np.float64)
-        rid = int(self.L.rsg_submit(self.s, A.n, A.nb, _lib.ptr(A.rowPtr), _lib.ptr(A.col), _lib.ptr(A.val), _lib.ptr(b), tol, maxit))
+        fn = self.L.rsg_submit if copy else self.L.rsg_submit_view
+        rid = int(fn(self.s, A.n, A.nb, _lib.ptr(A.rowPtr), _lib.ptr(A.col), _lib.ptr(A.val), _lib.ptr(b), tol, maxit))
         if rid < 0:
             raise _lib.RsgError(rid, _lib.last_error())
         self.sizes[rid] = A.n * A.nb
+        if not copy:
+            self.lent[rid] = (A.rowPtr, A.col, A.val, b)
         return rid
 
     def poll(self, rid: int, wait: bool = True):
@@ -284,6 +290,7 @@ class Server:
         if rc == 0:
             return None
         del self.sizes[rid]
+        self.lent.pop(rid, None)
         return x, {k: getattr(r, k) for k, _ in _lib.Result._fields_}
 
     def hold(self, on: bool = True):
@@ -299,6 +306,7 @@ class Server:
         if getattr(self, "s", None):
             self.L.rsg_server_destroy(self.s)
             self.s = None
+            self.lent = {}                       # released only after the server no longer reads them
 
     def __enter__(self):
         return self

@@ -128,3 +128,29 @@ def test_held_requests_are_admitted_together():
     for (xa, ra), (xm, rm) in zip(alone, mix):
         assert ra["status"] == rm["status"] and ra["iterations"] == rm["iterations"]
         assert np.array_equal(xa, xm, equal_nan=True)
+
+
+def test_lent_arrays_give_the_copied_result():
+    """rsg_submit_view reads the caller's arrays in place instead of copying them: every result (alone and in a held
+    batch) is bit for bit the one rsg_submit gives, and the Python mirror keeps the lent arrays until they are
+    polled."""
+    from ressim_gb300.solver import Server
+    reqs = requests(4, seed=41, lo=1e3, hi=1.2e4)
+    with Server(slots=1, precond="cpr", precision="mixed_f32") as s:
+        s.hold(True)
+        ids = [s.submit(r.A, r.b, tol=1e-6, maxit=500) for r in reqs]
+        s.hold(False)
+        copied = [s.poll(i) for i in ids]
+        lent_alone = [s.poll(s.submit(r.A, r.b, tol=1e-6, maxit=500, copy=False)) for r in reqs]
+        s.hold(True)
+        ids = [s.submit(r.A, r.b, tol=1e-6, maxit=500, copy=False) for r in reqs]
+        assert len(s.lent) == len(reqs)
+        s.hold(False)
+        lent_batch = [s.poll(i) for i in ids]
+        assert not s.lent
+    assert max(rm["batch"] for _, rm in copied) == len(reqs)
+    assert max(rm["batch"] for _, rm in lent_batch) == len(reqs)
+    for (xc, rc), (xa, ra), (xb, rb) in zip(copied, lent_alone, lent_batch):
+        assert rc["status"] == ra["status"] == rb["status"]
+        assert rc["iterations"] == ra["iterations"] == rb["iterations"]
+        assert np.array_equal(xc, xa, equal_nan=True) and np.array_equal(xc, xb, equal_nan=True)
