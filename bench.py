@@ -293,7 +293,7 @@ def serving_arrivals_at(rate, n, seed=7):
     return [(float(t[i]), int(rng.integers(SERVE_POOL))) for i in range(n)]
 
 
-def serving_ensemble(local, systems, rounds=3):
+def serving_ensemble(local, systems, rounds=10, copied_rounds=3):
     """The ensemble's systems handed to the server at once (admission held while they are submitted), as a simulator
     running 64 realisations at a common step would: they are admitted together and solved as one batch. One slot, so
     that rounds after the first reuse its plan as the batched handle does. The simulator keeps its Jacobians, so it
@@ -311,11 +311,13 @@ def serving_ensemble(local, systems, rounds=3):
             return dt, max(r["batch"] for r in res), ok
         first = one_round(False)                  # the pattern's first sight: plan, hierarchy, tuning
         lent = [one_round(False) for _ in range(rounds)]
-        copied = [one_round(True) for _ in range(rounds)]
+        copied = [one_round(True) for _ in range(copied_rounds)]
     n = len(systems)
     return {"value": n * rounds / sum(t for t, _, _ in lent), "unit": "solves/s", "batch": int(lent[-1][1]), "rounds": rounds,
+            "p50_round_ms": 1e3 * statistics.median(t for t, _, _ in lent),
             "all_converged": bool(first[2] and all(ok for _, _, ok in lent + copied)),
-            "copying_submit": {"value": n * rounds / sum(t for t, _, _ in copied), "unit": "solves/s", "batch": int(copied[-1][1])},
+            "copying_submit": {"value": n * copied_rounds / sum(t for t, _, _ in copied), "unit": "solves/s",
+                               "batch": int(copied[-1][1]), "rounds": copied_rounds},
             "first_round_ms": 1e3 * first[0],
             "note": "host wall clock per round after the pattern's first round: submission (arrays lent in place; "
                     "copying_submit: copied), admission, batched value upload, set-up and solve, results"}
