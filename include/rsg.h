@@ -337,7 +337,7 @@ typedef struct rsg_bo_grid {
     const double* conn_ddepth;/* [nconn] */
     const double* pore_vol;   /* [na] pore volume at the reference pressure */
     double gravity;           /* pressure gradient per density and depth (ressim::Units::gravity) */
-    int i_sw, i_x;            /* unknown slots of Sw and of x (Sg / Rs / Rv) */
+    int i_sw, i_x;            /* unknown slots of Sw and of x (Sg / Rs / Rv): 1 and 2 in either order (p is slot 0) */
     int eq[3];                /* equation offset of the water, oil and gas balances */
 } rsg_bo_grid;                /* ressim::Grid connections / adjacency, engine/include/ressim/grid.h:14-54 */
 
@@ -381,7 +381,8 @@ int rsg_bo_create(rsg_bo_assembler** h, const rsg_bo_grid* grid, const rsg_bo_fl
  * J[add_pos[k]] += add_val[k] and R[radd_pos[k]] += radd_val[k], applied after the reservoir terms and before the
  * row scaling, in list order for entries at the same position -- the engine's well loop's additions; every well
  * row starts from zero and is not scaled. Asynchronous on `stream` (a cudaStream_t; NULL = the legacy default
- * stream); consecutive calls on one assembler must be ordered (one stream). */
+ * stream). The assembler's scratch is shared by its calls: each call waits for the previous call's work, whatever
+ * stream that ran on, and rsg_bo_destroy for the last one's. */
 int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const double* d_sw, const double* d_x, const unsigned char* d_state,
                     const double* d_acc_old, double dt, int nadd, const long long* add_pos, const double* add_val, int nradd,
                     const int* radd_pos, const double* radd_val, double* d_J, double* d_R, void* stream);

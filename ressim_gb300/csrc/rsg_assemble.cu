@@ -560,6 +560,8 @@ struct rsg_bo_assembler {
     long long nnz = 0;
     Model m{};
     cudaStream_t own = nullptr;
+    cudaEvent_t last = nullptr;      // recorded after each assembly's work, on the stream it ran on: the next call (and
+                                     // the release of the buffers) waits for it, so calls on different streams are ordered
     // device arrays
     double* tab = nullptr;
     Tab* utab = nullptr;
@@ -636,7 +638,7 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
         return fail(RSG_EINVAL, "rsg_bo_create: only the three-phase live-oil / dry-gas model is supported (water, oil, gas, live, no vaporised oil)");
     if (sf->kro_model != 0 || sf->three_point || !sf->water || !sf->gas)
         return fail(RSG_EINVAL, "rsg_bo_create: only unscaled SWOF / SGOF tables with the default three-phase oil kr are supported");
-    if (g->i_sw < 0 || g->i_sw > 2 || g->i_x < 0 || g->i_x > 2 || g->i_sw == g->i_x)
+    if (g->i_sw < 1 || g->i_sw > 2 || g->i_x < 1 || g->i_x > 2 || g->i_sw == g->i_x)
         return fail(RSG_EINVAL, "rsg_bo_create: unknown slots i_sw / i_x must be distinct values in 1..2");
     {
         int seen = 0;
@@ -660,6 +662,7 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     // a nv + e holds the blocks of the cell and its neighbours in column order, nv columns each, then the cell's well
     // columns; then one row per well
     const long long nconn = g->nconn;
+    if (nconn < 0) return fail(RSG_EINVAL, "rsg_bo_create: nconn must be >= 0");
     std::vector<int> adjStart(g->adj_start, g->adj_start + na + 1);
     if (adjStart[0] != 0) return fail(RSG_EINVAL, "rsg_bo_create: adj_start[0] must be 0");
     for (int a = 0; a < na; ++a)
@@ -667,7 +670,9 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     const int nadj = adjStart[na];
     std::vector<int> adjNbr(g->adj_nbr, g->adj_nbr + nadj), adjConn(g->adj_conn, g->adj_conn + nadj);
     std::vector<int> connA(g->conn_a, g->conn_a + nconn);
-    std::vector<int> connB(size_t(nconn), -1), seen(size_t(nconn), 0);   // second cell of each connection
+    // second cell of each connection, as named from its first cell's adjacency and from its own; how often each side
+    // names it
+    std::vector<int> connB(size_t(nconn), -1), connB2(size_t(nconn), -1), seenA(size_t(nconn), 0), seenB(size_t(nconn), 0);
     std::vector<int> blkStart(na + 1, 0), selfPos(na), adjPos(nadj);
     std::vector<int> nb;
     std::vector<int> JrowH(J_rowPtr, J_rowPtr + nrows + 1);
@@ -681,9 +686,15 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
             const int b = adjNbr[q], c = adjConn[q];
             if (b < 0 || b >= na || b == a) return fail(RSG_EINVAL, "rsg_bo_create: neighbour index out of range");
             if (c < 0 || c >= nconn) return fail(RSG_EINVAL, "rsg_bo_create: connection index out of range");
-            if (connA[size_t(c)] == a) connB[size_t(c)] = b;
-            else if (connA[size_t(c)] != b) return fail(RSG_EINVAL, "rsg_bo_create: adjacency names a connection that does not join its cells");
-            ++seen[size_t(c)];
+            if (connA[size_t(c)] == a) {
+                connB[size_t(c)] = b;
+                ++seenA[size_t(c)];
+            } else if (connA[size_t(c)] == b) {
+                connB2[size_t(c)] = a;
+                ++seenB[size_t(c)];
+            } else {
+                return fail(RSG_EINVAL, "rsg_bo_create: adjacency names a connection that does not join its cells");
+            }
             nb.push_back(b);
         }
         std::sort(nb.begin(), nb.end());
@@ -710,7 +721,7 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     }
 
     for (long long c = 0; c < nconn; ++c)
-        if (seen[size_t(c)] != 2 || connB[size_t(c)] < 0)
+        if (seenA[size_t(c)] != 1 || seenB[size_t(c)] != 1 || connB[size_t(c)] != connB2[size_t(c)])
             return fail(RSG_EINVAL, "rsg_bo_create: every connection must appear once in the adjacency of each of its two cells");
     rsg_bo_assembler* h = new rsg_bo_assembler();
     h->device = device;
@@ -720,6 +731,12 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     if (e != cudaSuccess) { delete h; return fail(RSG_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)); }
     e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return fail(RSG_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
+    e = cudaEventCreateWithFlags(&h->last, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        h->last = nullptr;
+        rsg_bo_destroy(h);
+        return fail(RSG_ECUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
+    }
 
     Model& m = h->m;
     m.water = f->water; m.oil = f->oil; m.gas = f->gas; m.live = f->live;
@@ -803,6 +820,8 @@ extern "C" int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const dou
     if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     cudaStream_t st = static_cast<cudaStream_t>(stream);   // NULL: the legacy default stream
     const int na = h->na, nv = h->nv, nrows = h->nrows;
+    e = cudaStreamWaitEvent(st, h->last, 0);               // the previous call's work, whatever stream it ran on
+    if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
     const std::vector<int>& Jr = h->JrowH;
 
     // well addends grouped by the cell (or well row) they belong to, the caller's order kept within each group
@@ -894,6 +913,7 @@ extern "C" int rsg_bo_assemble(rsg_bo_assembler* h, const double* d_p, const dou
         h->launches += 1;
     }
     e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(h->last, st);
     if (e != cudaSuccess) return fail(RSG_ECUDA, std::string("rsg_bo_assemble launch: ") + cudaGetErrorString(e));
     return RSG_OK;
 }
@@ -938,12 +958,14 @@ extern "C" int rsg_bo_destroy(rsg_bo_assembler* h) {
     if (!h) return RSG_OK;
     cudaSetDevice(h->device);
     cudaStream_t st = h->own;
+    if (st && h->last) cudaStreamWaitEvent(st, h->last, 0);   // the last assembly's work, on any stream, first
     for (void* p : h->owned) cudaFreeAsync(p, st);
     if (h->dstage) cudaFreeAsync(h->dstage, st);
     if (st) {
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
     }
+    if (h->last) cudaEventDestroy(h->last);
     delete h;
     return RSG_OK;
 }

@@ -57,6 +57,31 @@ def test_assembly_matches_engine_bitwise(k):
     assert np.array_equal(J2, J) and np.array_equal(R2, R)
 
 
+def test_calls_on_different_streams_are_ordered():
+    """Four assemblies issued back to back on two streams without a synchronisation between them (each call's scratch
+    is the assembler's, so each waits for the previous call): every J and R is the engine's, bit for bit."""
+    torch = pytest.importorskip("torch")
+    from ressim_gb300.assembly import BlackOilAssembler
+    z = fixture()
+    d = torch.device("cuda:0")
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    with BlackOilAssembler(z) as asm:
+        states = [dev_state(torch, z, k) for k in range(4)]
+        outs = [(torch.full((asm.nnz,), float("nan"), dtype=torch.float64, device=d),
+                 torch.full((asm.nrows,), float("nan"), dtype=torch.float64, device=d)) for _ in range(4)]
+        torch.cuda.synchronize()
+        for k in range(4):
+            p, sw, x, st, acc = states[k]
+            J, R = outs[k]
+            asm.assemble_device(p.data_ptr(), sw.data_ptr(), x.data_ptr(), st.data_ptr(), acc.data_ptr(), float(z[f"s{k}_dt"][0]),
+                                J.data_ptr(), R.data_ptr(), add_pos=z[f"s{k}_add_pos"], add_val=z[f"s{k}_add_val"],
+                                radd_pos=z[f"s{k}_radd_pos"], radd_val=z[f"s{k}_radd_val"], stream=streams[k % 2].cuda_stream)
+        torch.cuda.synchronize()
+        for k in range(4):
+            assert np.array_equal(outs[k][0].cpu().numpy(), z[f"s{k}_J_full"])
+            assert np.array_equal(outs[k][1].cpu().numpy(), z[f"s{k}_R_full"])
+
+
 def test_reservoir_terms_alone_match_engine():
     """Without well terms the cell rows are the engine's reservoir terms alone (its assembly with every well shut)."""
     torch = pytest.importorskip("torch")

@@ -247,6 +247,26 @@ def test_black_oil_assembler_checks_model_and_pattern_before_the_device():
     with pytest.raises(_lib.RsgError) as e:
         BlackOilAssembler(bad)
     assert e.value.code == _lib.RSG_EINVAL and "connection" in str(e.value)
+    # two connections exchanged between adjacency entries so that every connection is still named twice, once from
+    # each of two cells it touches: c1 = (a, b1) named for a's neighbour b2 as well, c2 = (a, b2) named by b1
+    st, nbr, cn, ca = z["adjStart"], z["adjNbr"], z["adjConn"].copy(), z["conn_a"]
+    a = next(a for a in range(len(st) - 1) if sum(ca[cn[q]] == a for q in range(st[a], st[a + 1])) >= 2)
+    q1, q2 = [q for q in range(st[a], st[a + 1]) if ca[cn[q]] == a][:2]
+    b1, c1, c2 = nbr[q1], cn[q1], cn[q2]
+    qb = next(q for q in range(st[b1], st[b1 + 1]) if nbr[q] == a)
+    cn[q2], cn[qb] = c1, c2
+    bad = dict(z)
+    bad["adjConn"] = cn
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(bad)
+    assert e.value.code == _lib.RSG_EINVAL and "connection" in str(e.value)
+    bad = dict(z)
+    v = z["vars"].copy()
+    v[[0, 1]] = [0, 2]                                             # Sw in the pressure slot
+    bad["vars"] = v
+    with pytest.raises(_lib.RsgError) as e:
+        BlackOilAssembler(bad)
+    assert e.value.code == _lib.RSG_EINVAL and "slots" in str(e.value)
     if gpu_available():
         pytest.skip("a GPU is present")
     with pytest.raises(_lib.RsgError) as e:
