@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <thread>
 
 namespace rsg {
 
@@ -27,25 +28,40 @@ std::vector<int> diag_of(const Csr& A) {
 }
 
 // reference aggregation of one level (engine/src/amg.cpp:150-201); returns the number of aggregates
-int aggregate(const Csr& A, const std::vector<int>& dg, std::vector<int>& agg) {
+int aggregate(const Csr& A, const std::vector<int>& dg, std::vector<int>& agg, int threads) {
     const int n = A.n;
     const double kTheta = 0.08, kRowTheta = 0.25;
+    // strong connections: flagged per entry (rows in parallel), then compacted in row order
+    std::vector<unsigned char> strong(A.ci.size(), 0);
     std::vector<int> sp(size_t(n) + 1, 0), sc;
-    sc.reserve(A.ci.size());
-    for (int i = 0; i < n; ++i) {
-        double rowMax = 0;
-        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p)
-            if (A.ci[size_t(p)] != i) rowMax = std::max(rowMax, std::fabs(A.v[size_t(p)]));
-        const double di = A.v[size_t(dg[size_t(i)])];
-        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) {
-            const int j = A.ci[size_t(p)];
-            if (j == i) continue;
-            const double dj = A.v[size_t(dg[size_t(j)])];
-            if (std::fabs(A.v[size_t(p)]) >= kTheta * std::sqrt(std::fabs(di * dj)) || std::fabs(A.v[size_t(p)]) >= kRowTheta * rowMax)
-                sc.push_back(j);
+    parallel_ranges(n, threads, [&](int lo, int hi) {
+        for (int i = lo; i < hi; ++i) {
+            double rowMax = 0;
+            for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p)
+                if (A.ci[size_t(p)] != i) rowMax = std::max(rowMax, std::fabs(A.v[size_t(p)]));
+            const double di = A.v[size_t(dg[size_t(i)])];
+            int c = 0;
+            for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) {
+                const int j = A.ci[size_t(p)];
+                if (j == i) continue;
+                const double dj = A.v[size_t(dg[size_t(j)])];
+                if (std::fabs(A.v[size_t(p)]) >= kTheta * std::sqrt(std::fabs(di * dj)) || std::fabs(A.v[size_t(p)]) >= kRowTheta * rowMax) {
+                    strong[size_t(p)] = 1;
+                    ++c;
+                }
+            }
+            sp[size_t(i) + 1] = c;
         }
-        sp[size_t(i) + 1] = int(sc.size());
-    }
+    });
+    for (int i = 0; i < n; ++i) sp[size_t(i) + 1] += sp[size_t(i)];
+    sc.resize(size_t(sp[size_t(n)]));
+    parallel_ranges(n, threads, [&](int lo, int hi) {
+        for (int i = lo; i < hi; ++i) {
+            int q = sp[size_t(i)];
+            for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p)
+                if (strong[size_t(p)]) sc[size_t(q++)] = A.ci[size_t(p)];
+        }
+    });
     agg.assign(size_t(n), -1);
     int na = 0;
     for (int i = 0; i < n; ++i) {                       // pass 1: roots with free strong neighbourhoods
@@ -109,10 +125,20 @@ struct RowAccumulator {
     template <class Emit>
     void emit(std::vector<int>& outSrc, Emit&& emitCol) {
         for (auto& c : cols) mark[size_t(c.first)] = -1;
-        std::sort(cols.begin(), cols.end());
         const size_t ns = cols.size();
-        rank.assign(ns, 0);
-        off.assign(ns + 1, 0);
+        if (ns <= 32) {                          // a row's few columns (distinct J): insertion sort
+            for (size_t a = 1; a < ns; ++a) {
+                const std::pair<int, int> c = cols[a];
+                size_t b = a;
+                for (; b > 0 && cols[b - 1].first > c.first; --b) cols[b] = cols[b - 1];
+                cols[b] = c;
+            }
+        } else {
+            std::sort(cols.begin(), cols.end());
+        }
+        if (rank.size() < ns) rank.resize(ns);
+        if (off.size() < ns + 1) off.resize(ns + 1);
+        std::fill(off.begin(), off.begin() + long(ns) + 1, 0);
         for (size_t r = 0; r < ns; ++r) rank[size_t(cols[r].second)] = int(r);
         for (int sl : srcSlot) off[size_t(rank[size_t(sl)]) + 1]++;
         for (size_t r = 0; r < ns; ++r) off[r + 1] += off[r];
@@ -126,21 +152,97 @@ struct RowAccumulator {
     }
 };
 
-void galerkin(const Csr& A, const std::vector<int>& agg, int na, Galerkin& G) {
-    const int n = A.n;
-    Csr& AP = G.AP;
-    AP.n = n;
-    AP.rp.assign(size_t(n) + 1, 0);
-    AP.ci.clear(); AP.v.clear();
-    AP.ci.reserve(A.ci.size()); AP.v.reserve(A.ci.size());
-    G.apPtr.assign(1, 0); G.apSrc.clear();
-    G.apPtr.reserve(A.ci.size() + 1); G.apSrc.reserve(A.ci.size());
-    RowAccumulator acc(na);
-    for (int i = 0; i < n; ++i) {
-        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) acc.take(agg[size_t(A.ci[size_t(p)])], A.v[size_t(p)], p);
-        acc.emit(G.apSrc, [&](int J, double v, int end) { AP.ci.push_back(J); AP.v.push_back(v); G.apPtr.push_back(end); });
-        AP.rp[size_t(i) + 1] = int(AP.ci.size());
+// Output rows [lo, hi) of one product, formed by one worker with its own accumulator: the rows' columns and sums,
+// their row ends, and per entry the end of its source list, all local to the piece (joined in row order after).
+struct ProductPiece {
+    std::vector<int> rowEnd{0}, ci, ptr{0}, src;   // rowEnd and ptr open with the piece's start (0)
+    std::vector<double> v;
+};
+
+// Runs row(w, k, piece) for k in [0, nrows) in `threads` contiguous pieces, piece w on worker w (one thread each;
+// 1: the caller's thread), and joins them: out.rp, out.ci, out.v, ptr (entry -> end of its source list, ptr[0] = 0)
+// and src. Each row is formed exactly as a serial pass would form it, so the result does not depend on the number
+// of pieces. sources(lo, hi): the number of sources rows [lo, hi) take (their entries are at most that plus one per
+// row), to size the pieces' buffers once.
+template <class Row, class Sources>
+void product_rows(int nrows, int threads, Csr& out, std::vector<int>& ptr, std::vector<int>& src, Row&& row, Sources&& sources) {
+    const int np = std::max(1, std::min(threads, nrows));
+    std::vector<ProductPiece> pc(static_cast<size_t>(np));
+    auto bounds = [&](int w) { return std::make_pair(int((long long)nrows * w / np), int((long long)nrows * (w + 1) / np)); };
+    auto work = [&](int w) {
+        const auto [lo, hi] = bounds(w);
+        ProductPiece& q = pc[size_t(w)];
+        const size_t ns = sources(lo, hi);
+        q.rowEnd.reserve(size_t(hi - lo) + 1);
+        q.src.reserve(ns);
+        q.ci.reserve(ns + size_t(hi - lo));
+        q.v.reserve(ns + size_t(hi - lo));
+        q.ptr.reserve(ns + size_t(hi - lo) + 1);
+        for (int k = lo; k < hi; ++k) {
+            row(w, k, q);
+            q.rowEnd.push_back(int(q.ci.size()));
+        }
+    };
+    out.n = nrows;
+    if (np == 1) {                                   // one piece: it is the result
+        work(0);
+        ProductPiece& q = pc[0];
+        out.rp = std::move(q.rowEnd);
+        out.ci = std::move(q.ci);
+        out.v = std::move(q.v);
+        ptr = std::move(q.ptr);
+        src = std::move(q.src);
+        return;
     }
+    std::vector<std::thread> pool;
+    for (int w = 0; w < np; ++w) {
+        try {
+            pool.emplace_back(work, w);
+        } catch (const std::system_error&) {     // no thread to be had: this piece on the caller's thread
+            work(w);
+        }
+    }
+    for (auto& t : pool) t.join();
+    std::vector<size_t> e0(size_t(np) + 1, 0), s0(size_t(np) + 1, 0);
+    for (int w = 0; w < np; ++w) {
+        e0[size_t(w) + 1] = e0[size_t(w)] + pc[size_t(w)].ci.size();
+        s0[size_t(w) + 1] = s0[size_t(w)] + pc[size_t(w)].src.size();
+    }
+    out.rp.resize(size_t(nrows) + 1);
+    out.ci.resize(e0[size_t(np)]);
+    out.v.resize(e0[size_t(np)]);
+    ptr.resize(e0[size_t(np)] + 1);
+    src.resize(s0[size_t(np)]);
+    out.rp[0] = 0;
+    ptr[0] = 0;
+    parallel_ranges(np, np, [&](int w0, int w1) {    // each piece copied to its place, offsets added
+        for (int w = w0; w < w1; ++w) {
+            const ProductPiece& q = pc[size_t(w)];
+            const int lo = bounds(w).first;
+            const int eb = int(e0[size_t(w)]), sb = int(s0[size_t(w)]);
+            for (size_t r = 1; r < q.rowEnd.size(); ++r) out.rp[size_t(lo) + r] = eb + q.rowEnd[r];
+            std::copy(q.ci.begin(), q.ci.end(), out.ci.begin() + eb);
+            std::copy(q.v.begin(), q.v.end(), out.v.begin() + eb);
+            for (size_t e = 1; e < q.ptr.size(); ++e) ptr[size_t(eb) + e] = sb + q.ptr[e];
+            std::copy(q.src.begin(), q.src.end(), src.begin() + sb);
+        }
+    }, 1);
+}
+
+// threads: workers for the two products (rows split into contiguous pieces; the result is the same for any count)
+void galerkin(const Csr& A, const std::vector<int>& agg, int na, Galerkin& G, int threads) {
+    const int n = A.n;
+    const int nth = std::max(1, std::min(n >= 65536 ? threads : 1, n));   // small levels: a thread costs more than it saves
+    std::vector<RowAccumulator> accs;
+    accs.reserve(size_t(nth));
+    for (int w = 0; w < nth; ++w) accs.emplace_back(na);
+    // AP = A P: row i sums its entries of each aggregate column in row order
+    product_rows(n, nth, G.AP, G.apPtr, G.apSrc, [&](int w, int i, ProductPiece& q) {
+        RowAccumulator& acc = accs[size_t(w)];
+        for (int p = A.rp[size_t(i)]; p < A.rp[size_t(i) + 1]; ++p) acc.take(agg[size_t(A.ci[size_t(p)])], A.v[size_t(p)], p);
+        acc.emit(q.src, [&](int J, double v, int end) { q.ci.push_back(J); q.v.push_back(v); q.ptr.push_back(end); });
+    }, [&](int lo, int hi) { return size_t(A.rp[size_t(hi)] - A.rp[size_t(lo)]); });
+    const Csr& AP = G.AP;
     // members of every aggregate in ascending row order (the rows of R = P^T)
     std::vector<int> mPtr(size_t(na) + 1, 0), mem(static_cast<size_t>(n));
     for (int i = 0; i < n; ++i) mPtr[size_t(agg[size_t(i)]) + 1]++;
@@ -149,30 +251,30 @@ void galerkin(const Csr& A, const std::vector<int>& agg, int na, Galerkin& G) {
         std::vector<int> fill(mPtr.begin(), mPtr.end() - 1);
         for (int i = 0; i < n; ++i) mem[size_t(fill[size_t(agg[size_t(i)])]++)] = i;
     }
-    Csr& Ac = G.Ac;
-    Ac.n = na;
-    Ac.rp.assign(size_t(na) + 1, 0);
-    Ac.ci.clear(); Ac.v.clear();
-    G.acPtr.assign(1, 0); G.acSrc.clear();
-    G.acSrc.reserve(AP.ci.size());
-    for (int I = 0; I < na; ++I) {
-        for (int q = mPtr[size_t(I)]; q < mPtr[size_t(I) + 1]; ++q) {
-            const int i = mem[size_t(q)];
+    // A_c = R AP: row I sums the AP rows of its members in ascending order; a row whose columns skip I gets an
+    // explicit zero diagonal (engine/src/amg.cpp:83-91)
+    product_rows(na, nth, G.Ac, G.acPtr, G.acSrc, [&](int w, int I, ProductPiece& q) {
+        RowAccumulator& acc = accs[size_t(w)];
+        for (int m = mPtr[size_t(I)]; m < mPtr[size_t(I) + 1]; ++m) {
+            const int i = mem[size_t(m)];
             for (int e = AP.rp[size_t(i)]; e < AP.rp[size_t(i) + 1]; ++e) acc.take(AP.ci[size_t(e)], AP.v[size_t(e)], e);
         }
         bool haveDiag = false;
-        acc.emit(G.acSrc, [&](int J, double v, int end) {
-            if (!haveDiag && J > I) {                        // inserted zero diagonal (engine/src/amg.cpp:83-91)
-                Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(G.acPtr.back()); haveDiag = true;
+        acc.emit(q.src, [&](int J, double v, int end) {
+            if (!haveDiag && J > I) {                      // an empty source list: ends where the previous entry's does
+                q.ci.push_back(I); q.v.push_back(0.0); q.ptr.push_back(q.ptr.back()); haveDiag = true;
             }
             if (J == I) haveDiag = true;
-            Ac.ci.push_back(J);
-            Ac.v.push_back(v);
-            G.acPtr.push_back(end);
+            q.ci.push_back(J);
+            q.v.push_back(v);
+            q.ptr.push_back(end);
         });
-        if (!haveDiag) { Ac.ci.push_back(I); Ac.v.push_back(0.0); G.acPtr.push_back(int(G.acSrc.size())); }
-        Ac.rp[size_t(I) + 1] = int(Ac.ci.size());
-    }
+        if (!haveDiag) { q.ci.push_back(I); q.v.push_back(0.0); q.ptr.push_back(int(q.src.size())); }
+    }, [&](int lo, int hi) {
+        size_t c = 0;
+        for (int m = mPtr[size_t(lo)]; m < mPtr[size_t(hi)]; ++m) c += size_t(AP.rp[size_t(mem[size_t(m)]) + 1] - AP.rp[size_t(mem[size_t(m)])]);
+        return c;
+    });
 }
 
 void fix_diag(Csr& A, const std::vector<int>& dg) {
@@ -209,7 +311,7 @@ void gs_levels(const Csr& A, const std::vector<int>& dg, std::vector<int>& perm,
 // Builds the hierarchy of one system. ap0: values of the fine pressure matrix in the system's LEVEL-SPACE block
 // order (positions [bp0, bp1) of the block pattern); the level-space pattern and its original numbering come from
 // the solver plan. Levels l >= 1 are expressed in their own level space.
-bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, SysAmg& out, std::string& err) {
+bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, SysAmg& out, std::string& err, int threads) {
     const int r0 = P.sysRow0[size_t(s)], r1 = P.sysRow0[size_t(s) + 1], n0 = r1 - r0;
     const int b0 = P.rowPtr[size_t(r0)];
     // natural-order fine matrix (original numbering of this system)
@@ -217,19 +319,24 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
     A.n = n0;
     A.rp.assign(size_t(n0) + 1, 0);
     const size_t nnz0 = size_t(P.rowPtr[size_t(r1)] - b0);
-    A.ci.reserve(nnz0);
-    A.v.reserve(nnz0);
-    std::vector<int> natPos;                     // natural position -> level-space position (relative to b0)
-    natPos.reserve(nnz0);
     for (int io = 0; io < n0; ++io) {
         const int k = P.iperm[size_t(r0 + io)];
-        for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p) {
-            A.ci.push_back(P.perm[size_t(P.col[size_t(p)])] - r0);
-            A.v.push_back(ap0[size_t(p - b0)]);
-            natPos.push_back(p - b0);
-        }
-        A.rp[size_t(io) + 1] = int(A.ci.size());
+        A.rp[size_t(io) + 1] = A.rp[size_t(io)] + (P.rowPtr[size_t(k) + 1] - P.rowPtr[size_t(k)]);
     }
+    A.ci.resize(nnz0);
+    A.v.resize(nnz0);
+    std::vector<int> natPos(nnz0);               // natural position -> level-space position (relative to b0)
+    parallel_ranges(n0, threads, [&](int lo, int hi) {
+        for (int io = lo; io < hi; ++io) {
+            const int k = P.iperm[size_t(r0 + io)];
+            int q = A.rp[size_t(io)];
+            for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p, ++q) {
+                A.ci[size_t(q)] = P.perm[size_t(P.col[size_t(p)])] - r0;
+                A.v[size_t(q)] = ap0[size_t(p - b0)];
+                natPos[size_t(q)] = p - b0;
+            }
+        }
+    });
     std::vector<int> dg = diag_of(A);
     for (int i = 0; i < n0; ++i)
         if (dg[size_t(i)] < 0) { err = "pressure matrix without a diagonal entry"; return false; }
@@ -239,14 +346,14 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
     {
         AmgLevel L0;
         L0.n = n0;
-        L0.rp.assign(size_t(n0) + 1, 0);
-        L0.ci.reserve(nnz0);
-        L0.diag.reserve(size_t(n0));
-        for (int k = r0; k < r1; ++k) {
-            for (int p = P.rowPtr[size_t(k)]; p < P.rowPtr[size_t(k) + 1]; ++p) L0.ci.push_back(P.col[size_t(p)] - r0);
-            L0.rp[size_t(k - r0) + 1] = int(L0.ci.size());
-            L0.diag.push_back(P.diag[size_t(k)] - b0);
-        }
+        L0.rp.resize(size_t(n0) + 1);
+        L0.ci.resize(nnz0);
+        L0.diag.resize(size_t(n0));
+        for (int k = r0; k <= r1; ++k) L0.rp[size_t(k - r0)] = P.rowPtr[size_t(k)] - b0;
+        for (int k = r0; k < r1; ++k) L0.diag[size_t(k - r0)] = P.diag[size_t(k)] - b0;
+        parallel_ranges(int(nnz0), threads, [&](int lo, int hi) {
+            for (int q = lo; q < hi; ++q) L0.ci[size_t(q)] = P.col[size_t(b0 + q)] - r0;
+        });
         for (int q = P.sysLvl0[size_t(s)]; q < P.sysLvl0[size_t(s) + 1]; ++q) L0.lvlStart.push_back(P.lvlStart[size_t(q)] - r0);
         L0.perm.resize(size_t(n0));
         L0.iperm.resize(size_t(n0));
@@ -262,10 +369,10 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
     while (true) {
         if (cur.n <= 400 || int(out.lv.size()) >= 14) break;          // engine/src/amg.cpp:153
         std::vector<int> agg;
-        const int na = aggregate(cur, curDiag, agg);
+        const int na = aggregate(cur, curDiag, agg, threads);
         if (na >= int(0.85 * cur.n) || na < 1) break;                   // coarsening stalled
         Galerkin G;
-        galerkin(cur, agg, na, G);
+        galerkin(cur, agg, na, G, threads);
         std::vector<int> cd = diag_of(G.Ac);
         fix_diag(G.Ac, cd);
         AmgLevel& F = out.lv.back();                                    // finer level (level space)
@@ -302,9 +409,11 @@ bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, S
         }
         // Galerkin gathers in level-space positions: AP entries (natural) <- finer level-space positions;
         // coarse level-space entries <- AP entries
-        C.apPtr = G.apPtr;
+        C.apPtr = std::move(G.apPtr);
         C.apSrc.resize(G.apSrc.size());
-        for (size_t q = 0; q < G.apSrc.size(); ++q) C.apSrc[q] = natToLev0[size_t(G.apSrc[q])];
+        parallel_ranges(int(G.apSrc.size()), threads, [&](int lo, int hi) {
+            for (int q = lo; q < hi; ++q) C.apSrc[size_t(q)] = natToLev0[size_t(G.apSrc[size_t(q)])];
+        });
         C.acPtr.assign(G.Ac.ci.size() + 1, 0);
         C.acSrc.clear();
         C.acSrc.reserve(G.acSrc.size());
@@ -362,5 +471,55 @@ extern "C" int rsg_debug_amg_plan(int n, const int* rowPtr, const int* col, cons
             for (int i = 0; i < L.n; ++i) agg[i] = C.perm[size_t(L.agg[size_t(L.iperm[size_t(i)])])];
         }
     }
+    return 0;
+}
+
+namespace {
+// FNV-1a over the bytes of a plan's arrays and sizes
+struct Digest {
+    unsigned long long h = 1469598103934665603ULL;
+    void bytes(const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ULL; }
+    }
+    void num(long long x) { bytes(&x, sizeof x); }
+    template <class T> void vec(const std::vector<T>& v) { num((long long)v.size()); bytes(v.data(), v.size() * sizeof(T)); }
+};
+}  // namespace
+
+// Diagnostics: digests of the whole solver plan (every array of the pattern plan) and of the whole AMG plan of one
+// system, built with `threads` host threads -- the plans must not depend on the thread count.
+extern "C" int rsg_debug_plan_digest(int n, const int* rowPtr, const int* col, const double* ap, int threads,
+                                     unsigned long long* planDigest, unsigned long long* amgDigest) {
+    using namespace rsg;
+    std::vector<int> rp0(rowPtr, rowPtr + n + 1), ci0(col, col + rowPtr[n]), s0 = {0, n};
+    HostPlan P;
+    std::string err;
+    if (!build_plan(P, 1, s0, rp0, ci0, err, threads)) { set_last_error(err); return -1; }
+    Digest d;
+    for (long long x : {(long long)P.n, (long long)P.nnzb, (long long)P.nsys, (long long)P.nlevF, (long long)P.nlevB,
+                        (long long)P.symmetric, (long long)P.maxSysRows})
+        d.num(x);
+    for (const std::vector<int>* v : {&P.rowPtr0, &P.col0, &P.perm, &P.iperm, &P.valSrc, &P.rowPtr, &P.col, &P.diag, &P.ford,
+                                      &P.bord, &P.elimPtr, &P.elimT, &P.elimQ, &P.rowSys, &P.sysRow0, &P.tileRow0, &P.tileSys,
+                                      &P.sysTile0, &P.lvlStart, &P.sysLvl0, &P.Lslot, &P.LslotSrc, &P.LovCol, &P.LovSrc, &P.Uslot,
+                                      &P.UslotSrc, &P.UovCol, &P.UovSrc, &P.Dsrc})
+        d.vec(*v);
+    *planDigest = d.h;
+    std::vector<double> ap0(size_t(P.nnzb));
+    for (int p = 0; p < P.nnzb; ++p) ap0[size_t(p)] = ap[P.valSrc[size_t(p)]];
+    SysAmg H;
+    if (!amg_plan_system(P, 0, ap0, H, err, threads)) { set_last_error(err); return -1; }
+    Digest a;
+    a.num(H.coarseDense ? 1 : 0);
+    a.num((long long)H.lv.size());
+    for (const AmgLevel& L : H.lv) {
+        a.num(L.n);
+        for (const std::vector<int>* v : {&L.rp, &L.ci, &L.diag, &L.lvlStart, &L.perm, &L.iperm, &L.agg, &L.memPtr, &L.mem, &L.apPtr,
+                                          &L.apSrc, &L.acPtr, &L.acSrc})
+            a.vec(*v);
+        a.vec(L.val);
+    }
+    *amgDigest = a.h;
     return 0;
 }

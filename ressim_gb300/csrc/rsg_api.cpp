@@ -373,14 +373,14 @@ int set_batch_pattern(rsg_solver* h, int nsys, const int* n, const int* const* r
             // caller's rows and blocks
             std::vector<int> rp2, ci2, rowOrig, blockOrig;
             multicolour_batch(nsys, sysRow0, rp, ci, rp2, ci2, rowOrig, blockOrig);
-            if (!build_plan(h->plan, nsys, sysRow0, rp2, ci2, err)) return fail(RSG_EINVAL, err);
+            if (!build_plan(h->plan, nsys, sysRow0, rp2, ci2, err, host_threads())) return fail(RSG_EINVAL, err);
             HostPlan& P = h->plan;
             for (auto& v : P.perm) v = rowOrig[size_t(v)];
             for (int k = 0; k < P.n; ++k) P.iperm[size_t(P.perm[size_t(k)])] = k;
             for (auto& v : P.valSrc) v = blockOrig[size_t(v)];
             P.rowPtr0 = rp;
             P.col0 = ci;
-        } else if (!build_plan(h->plan, nsys, sysRow0, rp, ci, err)) {
+        } else if (!build_plan(h->plan, nsys, sysRow0, rp, ci, err, host_threads())) {
             return fail(RSG_EINVAL, err);
         }
         int rc = alloc_plan(h);
@@ -908,14 +908,16 @@ int setup_cpr(rsg_solver* h, const double* acc) {
         std::vector<SysAmg> H(size_t(P.nsys));
         std::vector<std::string> errs(size_t(P.nsys));
         std::vector<char> ok(size_t(P.nsys), 1);
-        const int nth = std::max(1, std::min(P.nsys, int(std::thread::hardware_concurrency())));
+        const int hw = host_threads();
+        const int nth = std::max(1, std::min(P.nsys, hw));
+        const int inner = std::max(1, hw / nth);             // threads inside a system's plan (a lone large system)
         std::vector<std::thread> pool;
         for (int t = 0; t < nth; ++t)
             pool.emplace_back([&, t] {
                 for (int s = t; s < P.nsys; s += nth) {
                     const int b0 = P.rowPtr[size_t(P.sysRow0[size_t(s)])], b1 = P.rowPtr[size_t(P.sysRow0[size_t(s) + 1])];
                     std::vector<double> ap0(hap.begin() + b0, hap.begin() + b1);
-                    ok[size_t(s)] = amg_plan_system(P, s, ap0, H[size_t(s)], errs[size_t(s)]) ? 1 : 0;
+                    ok[size_t(s)] = amg_plan_system(P, s, ap0, H[size_t(s)], errs[size_t(s)], inner) ? 1 : 0;
                 }
             });
         for (auto& th : pool) th.join();

@@ -829,7 +829,7 @@ void precond(GenEngine& g, const double* r, double* z) {
 int build_amg(GenEngine& g, const std::vector<double>& ap0) {
     SysAmg H;
     std::string err;
-    if (!amg_plan_system(g.plan, 0, ap0, H, err)) return gfail(RSG_EINVAL, err);
+    if (!amg_plan_system(g.plan, 0, ap0, H, err, host_threads())) return gfail(RSG_EINVAL, err);
     g.lv.assign(H.lv.size(), GenLevel{});
     for (size_t l = 0; l < H.lv.size(); ++l) {
         const AmgLevel& A = H.lv[l];
@@ -1099,7 +1099,7 @@ int gen_set_matrix(GenEngine* gp, const rsg_options& o, int n, int nb, const int
         g.rp0.assign(rowPtr, rowPtr + n + 1);
         g.ci0.assign(col, col + nnzb);
         std::string err;
-        if (!build_plan(g.plan, 1, std::vector<int>{0, n}, g.rp0, g.ci0, err)) return gfail(RSG_EINVAL, err);
+        if (!build_plan(g.plan, 1, std::vector<int>{0, n}, g.rp0, g.ci0, err, host_threads())) return gfail(RSG_EINVAL, err);
         std::vector<int> dg(static_cast<size_t>(n));
         for (int i = 0; i < n; ++i)
             for (int p = rowPtr[i]; p < rowPtr[i + 1]; ++p)

@@ -3,10 +3,39 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <algorithm>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 namespace rsg {
+
+// Host threads the plan of a large pattern may use.
+inline int host_threads() { return std::max(1, int(std::thread::hardware_concurrency())); }
+
+// Host plan work on large patterns: fn(lo, hi) over [0, n) in up to `threads` contiguous ranges, one thread each
+// (one range on the caller's thread when threads <= 1 or n is below minPerThread per thread). Every use writes
+// disjoint outputs per index, so the result does not depend on the split.
+template <class Fn>
+void parallel_ranges(int n, int threads, Fn&& fn, int minPerThread = 32768) {
+    const int np = std::max(1, std::min(threads, n / std::max(1, minPerThread)));
+    if (np <= 1) {
+        fn(0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(size_t(np));
+    for (int w = 0; w < np; ++w) {
+        auto range = [&fn, n, np, w] { fn(int((long long)n * w / np), int((long long)n * (w + 1) / np)); };
+        try {
+            pool.emplace_back(range);
+        } catch (const std::system_error&) {   // no thread to be had: this range on the caller's thread
+            range();
+        }
+    }
+    for (auto& t : pool) t.join();
+}
 
 constexpr int NB = 3;                 // block size of the black-oil system (p, Sw, x_g)
 constexpr int NB2 = NB * NB;
@@ -82,8 +111,9 @@ struct SweepState;
 // True when a batch (per system: n[s] rows, rowPtr[s], col[s]) has exactly the pattern the plan was built from,
 // compared in place (no concatenated copy).
 bool same_batch_pattern(const HostPlan& P, int nsys, const int* n, const int* const* rowPtr, const int* const* col);
+// threads: host threads for the row-parallel parts of a large pattern (the plan is the same for any count)
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr,
-                const std::vector<int>& col, std::string& err);
+                const std::vector<int>& col, std::string& err, int threads = 1);
 // multicolour ordering of every system (MCBILU0, engine/src/bsr.cpp:599-653): permuted pattern and the original row /
 // block of every permuted row / block
 void multicolour_batch(int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rp, const std::vector<int>& ci,
@@ -106,7 +136,8 @@ struct SysAmg {
     std::vector<AmgLevel> lv;
     bool coarseDense = true;           // coarsest level <= 800 rows: dense solve (else 20 symmetric GS sweeps)
 };
-bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, SysAmg& out, std::string& err);
+// threads: host threads for the Galerkin products of the large levels (the result is the same for any count)
+bool amg_plan_system(const HostPlan& P, int s, const std::vector<double>& ap0, SysAmg& out, std::string& err, int threads = 1);
 
 // Device AMG of a batch: all arrays concatenated level-major (every system's level 0, then every system's level 1,
 // ...); indices inside a (system, level) are local. AmgSysLv[s * maxL + l] describes level l of system s.

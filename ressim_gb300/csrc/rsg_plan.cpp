@@ -89,7 +89,7 @@ void multicolour_batch(int nsys, const std::vector<int>& sysRow0, const std::vec
 }
 
 bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const std::vector<int>& rowPtr0,
-                const std::vector<int>& col0, std::string& err) {
+                const std::vector<int>& col0, std::string& err, int threads) {
     const int n = int(rowPtr0.size()) - 1;
     if (n < 1) { err = "empty matrix (n < 1)"; return false; }
     if (rowPtr0[0] != 0) { err = "rowPtr[0] must be 0"; return false; }
@@ -163,23 +163,33 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     P.diag.assign(size_t(n), -1);
     for (int k = 0; k < n; ++k) {
         const int i = P.perm[size_t(k)];
-        int q = P.rowPtr[size_t(k)];
-        for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p, ++q) {
-            P.col[size_t(q)] = P.iperm[size_t(P.col0[size_t(p)])];
-            P.valSrc[size_t(q)] = p;
-            if (p == diag0[size_t(i)]) P.diag[size_t(k)] = q;
-        }
-        P.rowPtr[size_t(k) + 1] = q;
+        P.rowPtr[size_t(k) + 1] = P.rowPtr[size_t(k)] + (rowPtr0[size_t(i) + 1] - rowPtr0[size_t(i)]);
     }
-    // structural symmetry (then the reversed forward levels are a topological order of the U dependencies)
-    P.symmetric = true;
-    for (int i = 0; i < n && P.symmetric; ++i)
-        for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p) {
-            const int j = P.col0[size_t(p)];
-            const int* c0 = P.col0.data() + rowPtr0[size_t(j)];
-            const int* c1 = P.col0.data() + rowPtr0[size_t(j) + 1];
-            if (!std::binary_search(c0, c1, i)) { P.symmetric = false; break; }
+    parallel_ranges(n, threads, [&](int lo, int hi) {
+        for (int k = lo; k < hi; ++k) {
+            const int i = P.perm[size_t(k)];
+            int q = P.rowPtr[size_t(k)];
+            for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p, ++q) {
+                P.col[size_t(q)] = P.iperm[size_t(P.col0[size_t(p)])];
+                P.valSrc[size_t(q)] = p;
+                if (p == diag0[size_t(i)]) P.diag[size_t(k)] = q;
+            }
         }
+    });
+    // structural symmetry (then the reversed forward levels are a topological order of the U dependencies)
+    {
+        std::atomic<bool> sym{true};
+        parallel_ranges(n, threads, [&](int lo, int hi) {
+            for (int i = lo; i < hi && sym.load(std::memory_order_relaxed); ++i)
+                for (int p = rowPtr0[size_t(i)]; p < rowPtr0[size_t(i) + 1]; ++p) {
+                    const int j = P.col0[size_t(p)];
+                    const int* c0 = P.col0.data() + rowPtr0[size_t(j)];
+                    const int* c1 = P.col0.data() + rowPtr0[size_t(j) + 1];
+                    if (!std::binary_search(c0, c1, i)) { sym.store(false, std::memory_order_relaxed); break; }
+                }
+        });
+        P.symmetric = sym.load();
+    }
     // claim orders of the grid-wide sync-free kernels: all systems' rows by forward level
     order_by_level(levNew, P.nlevF, P.ford);
     if (P.symmetric) {
@@ -201,24 +211,32 @@ bool build_plan(HostPlan& P, int nsys, const std::vector<int>& sysRow0, const st
     }
     // BILU0 elimination lists (engine/src/bsr.cpp:193-201): lower entries in row order, the U entries of the
     // eliminating row in row order, target = the block of row i in the same column
+    // (rows in parallel: the pairs of every entry counted, then written at their places)
     P.elimPtr.assign(size_t(nnzb) + 1, 0);
-    P.elimT.clear(); P.elimQ.clear();
-    std::vector<int> pos(size_t(n), -1);
-    for (int i = 0; i < n; ++i) {
-        const int r0 = P.rowPtr[size_t(i)], r1 = P.rowPtr[size_t(i) + 1];
-        for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = p;
-        for (int p = r0; p < r1; ++p) {
-            if (p < P.diag[size_t(i)]) {
+    auto elim_rows = [&](int lo, int hi, bool write) {
+        std::vector<int> pos(size_t(n), -1);
+        for (int i = lo; i < hi; ++i) {
+            const int r0 = P.rowPtr[size_t(i)], r1 = P.rowPtr[size_t(i) + 1];
+            for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = p;
+            for (int p = r0; p < P.diag[size_t(i)]; ++p) {
                 const int k = P.col[size_t(p)];
+                int c = write ? P.elimPtr[size_t(p)] : 0;
                 for (int q = P.diag[size_t(k)] + 1; q < P.rowPtr[size_t(k) + 1]; ++q) {
                     const int t = pos[size_t(P.col[size_t(q)])];
-                    if (t >= 0) { P.elimT.push_back(t); P.elimQ.push_back(q); }
+                    if (t < 0) continue;
+                    if (write) { P.elimT[size_t(c)] = t; P.elimQ[size_t(c)] = q; }
+                    ++c;
                 }
+                if (!write) P.elimPtr[size_t(p) + 1] = c;
             }
-            P.elimPtr[size_t(p) + 1] = int(P.elimT.size());
+            for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = -1;
         }
-        for (int p = r0; p < r1; ++p) pos[size_t(P.col[size_t(p)])] = -1;
-    }
+    };
+    parallel_ranges(n, threads, [&](int lo, int hi) { elim_rows(lo, hi, false); });
+    for (int p = 0; p < nnzb; ++p) P.elimPtr[size_t(p) + 1] += P.elimPtr[size_t(p)];
+    P.elimT.assign(size_t(P.elimPtr[size_t(nnzb)]), 0);
+    P.elimQ.assign(size_t(P.elimPtr[size_t(nnzb)]), 0);
+    parallel_ranges(n, threads, [&](int lo, int hi) { elim_rows(lo, hi, true); });
     // tiles of TILE_ROWS block rows, never crossing a system boundary
     P.tileRow0.clear(); P.tileSys.clear(); P.sysTile0.assign(size_t(nsys) + 1, 0);
     for (int s = 0; s < nsys; ++s) {

@@ -172,6 +172,24 @@ def test_host_amg_plan_matches_oracle(name, oracle):
         assert np.array_equal(v, vl)
 
 
+def test_host_plan_does_not_depend_on_thread_count():
+    """The host plan of a large pattern (level space, elimination lists, slots; the AMG hierarchy with its Galerkin
+    gather lists) is built with several host threads: every array is the same for 1, 2 and 5 threads (digests of the
+    whole plans). A 101k-row system, large enough for the threaded paths. Host code only."""
+    from ressim_gb300 import _build, synth
+    L = C.CDLL(_build.LIB)
+    L.rsg_debug_plan_digest.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    A = synth.make_system(48, 48, 44, sigma=1.5, seed=12, wells="corners+center").A
+    ap = np.ascontiguousarray(A.val.reshape(-1, 3, 3)[:, 0, 0])
+    digests = []
+    for threads in (1, 2, 5):
+        dp, da = C.c_ulonglong(0), C.c_ulonglong(0)
+        assert L.rsg_debug_plan_digest(A.n, A.rowPtr.ctypes.data, A.col.ctypes.data, ap.ctypes.data, threads, C.byref(dp),
+                                       C.byref(da)) == 0
+        digests.append((dp.value, da.value))
+    assert digests[0] == digests[1] == digests[2]
+
+
 def test_same_pattern_check_of_set_batch():
     """rsg_set_batch reuses its plan when the batch has the plan's pattern, compared in place: the same batch is
     the same; a moved column, a row of another length, another system count are not. Host code only."""
