@@ -630,7 +630,7 @@ extern "C" int rsg_bo_create(rsg_bo_assembler** out, const rsg_bo_grid* g, const
     if (!g || !f || !sf || !J_rowPtr || !J_col) return fail(RSG_EINVAL, "rsg_bo_create: null argument");
     const int na = g->na, nv = g->nv;
     if (na < 1 || nv != 3) return fail(RSG_EINVAL, "rsg_bo_create: na >= 1 and nv = 3 (water, oil, gas) are required");
-    if (nw < 0 || nrows != na * nv + nw) return fail(RSG_EINVAL, "rsg_bo_create: nrows must be na * nv + nw");
+    if (nw < 0 || (long long)nrows != (long long)na * nv + nw) return fail(RSG_EINVAL, "rsg_bo_create: nrows must be na * nv + nw");
     if (!g->adj_start || !g->adj_nbr || !g->adj_conn || !g->conn_a || !g->conn_trans || !g->conn_ddepth || !g->pore_vol)
         return fail(RSG_EINVAL, "rsg_bo_create: null grid array");
     // the model this path implements: three phases, live oil, dry gas, unscaled tables, ECLIPSE default oil kr
